@@ -1,0 +1,218 @@
+/*
+ * vkg.h -- C ABI of the GB300 path-tracing hot path (library: vierkant_gb300/libvkg.so).
+ *
+ * Drop-in scope: the closest-hit ray-triangle / ray-AABB queries over a BVH and the multi-bounce
+ * radiance estimator of vierkant's PBRPathTracer. Every entry point below names the reference
+ * interface it replaces (paths relative to the vierkant source tree).
+ *
+ * Conventions
+ *   - every call returns vkg_status (0 = VKG_OK); nothing throws across the ABI;
+ *     vkg_last_error(ctx) returns a human-readable message for the last failure on that context.
+ *   - device pointers (prefix d_) are caller-owned CUDA device memory; handles (vkg_bvh,
+ *     vkg_scene, vkg_tracer) are library-owned and released by their *_destroy call.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream); GPU work is
+ *     asynchronous on that stream unless the function says it synchronises.
+ *   - one vkg_ctx per host thread (contexts are not internally locked).
+ *   - plain C types only: no CUDA or C++ types appear in this header.
+ */
+#ifndef VKG_H
+#define VKG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status ---------------------------------------------------------------------------------- */
+typedef int vkg_status;
+enum
+{
+    VKG_OK = 0,
+    VKG_ERR_INVALID_ARGUMENT = 1,
+    VKG_ERR_CUDA = 2,
+    VKG_ERR_OUT_OF_MEMORY = 3,
+    VKG_ERR_NOT_SUPPORTED = 4,
+    VKG_ERR_TIMEOUT = 5,        /* a bounded device loop gave up (device work stopped cleanly) */
+    VKG_ERR_STACK_OVERFLOW = 6, /* a traversal exceeded its stack; results of that launch are invalid */
+    VKG_ERR_CAPACITY = 7        /* an input exceeds a documented maximum */
+};
+
+/* ---- value types ------------------------------------------------------------------------------ */
+/* intersection.hpp:18-23 */
+enum
+{
+    VKG_REJECT = 0,
+    VKG_INTERSECT = 1,
+    VKG_INSIDE = 2
+};
+
+/* ray record, 32 B: mirrors ray::Ray (shaders/slang/ray/ray_common.slang:23-29) */
+typedef struct vkg_ray
+{
+    float origin[3];
+    float tmin;
+    float direction[3];
+    float tmax;
+} vkg_ray;
+
+/* closest-hit record, 16 B: prim = triangle id (0xFFFFFFFF on miss), t, barycentrics u, v */
+typedef struct vkg_hit
+{
+    uint32_t prim;
+    float t, u, v;
+} vkg_hit;
+
+#define VKG_MISS 0xFFFFFFFFu
+
+/* intersection.hpp:28-51 (ray_intersection / ray_triangle_intersection) */
+typedef struct vkg_ray_intersection
+{
+    int type; /* VKG_REJECT / VKG_INTERSECT / VKG_INSIDE */
+    float distance;
+} vkg_ray_intersection;
+
+typedef struct vkg_ray_triangle_intersection
+{
+    int type;
+    float distance, u, v;
+} vkg_ray_triangle_intersection;
+
+/* ---- host scalar intersection API (pure, thread-safe, no allocation) ------------------------
+ * Bit-identical to vierkant::intersect() in src/intersection.cpp. The ray direction is used as
+ * given (vierkant::Ray's constructor normalises; callers that need that pass a unit vector).   */
+
+/* replaces intersect(const Triangle&, const Ray&), intersection.hpp:79 / intersection.cpp:114-129 */
+vkg_status vkg_intersect_ray_triangle(const float origin[3], const float direction[3], const float tri[9],
+                                      vkg_ray_triangle_intersection *out);
+/* replaces AABB::intersect(const Ray&) / intersect(const AABB&, const Ray&), intersection.hpp:90,349,
+   intersection.cpp:308-312 */
+vkg_status vkg_intersect_ray_aabb(const float origin[3], const float direction[3], const float bmin[3],
+                                  const float bmax[3], vkg_ray_intersection *out);
+/* replaces intersect(const OBB&, const Ray&), intersection.hpp:95 / intersection.cpp:152-184;
+   axes = 3 unit column vectors (9 floats), half_lengths = 3 floats */
+vkg_status vkg_intersect_ray_obb(const float origin[3], const float direction[3], const float center[3],
+                                 const float axes[9], const float half_lengths[3], vkg_ray_intersection *out);
+/* replaces intersect(const Sphere&, const Ray&), intersection.hpp:85 / intersection.cpp:133-148 */
+vkg_status vkg_intersect_ray_sphere(const float origin[3], const float direction[3], const float center[3],
+                                    float radius, vkg_ray_intersection *out);
+/* replaces intersect(const Plane&, const Ray&), intersection.hpp:74 / intersection.cpp:10-21;
+   plane = (a, b, c, d) as in Plane(float a, float b, float c, float d) (normalised internally) */
+vkg_status vkg_intersect_ray_plane(const float origin[3], const float direction[3], const float plane[4],
+                                   vkg_ray_intersection *out);
+/* replaces intersect(const Triangle&, const AABB&), intersection.hpp:101 / intersection.cpp:364-370
+   (triangle-box overlap, Akenine-Moeller separating axes); returns 0/1 in *out */
+vkg_status vkg_intersect_triangle_aabb(const float tri[9], const float bmin[3], const float bmax[3],
+                                       uint32_t *out);
+/* replaces intersect(const Triangle&, const Triangle&), intersection.hpp:105 / intersection.cpp:374-378
+   (triangle-triangle overlap, Guigue-Devillers orientation predicates); returns 0/1 in *out */
+vkg_status vkg_intersect_triangle_triangle(const float a[9], const float b[9], uint32_t *out);
+
+/* ---- context ---------------------------------------------------------------------------------- */
+typedef struct vkg_ctx vkg_ctx;
+
+/* library version string, e.g. "vkg 0.1 sm_103a" */
+const char *vkg_version(void);
+/* create a context bound to CUDA device `device` */
+vkg_status vkg_ctx_create(int device, vkg_ctx **out);
+vkg_status vkg_ctx_destroy(vkg_ctx *ctx);
+/* last error message of this context ("" if none); valid until the next call on ctx */
+const char *vkg_last_error(const vkg_ctx *ctx);
+
+/* ---- geometry generators (host, deterministic) ----------------------------------------------
+ * replaces Geometry::IcoSphere(radius, tessellation), Geometry.hpp:149 / Geometry.cpp:566-613:
+ * 12 + 3 * sum(20 * 4^i, i < tess) unshared vertices, 20 * 4^tess triangles */
+vkg_status vkg_geometry_icosphere_counts(uint32_t tess, uint32_t *num_vertices, uint32_t *num_tris);
+vkg_status vkg_geometry_icosphere(float radius, uint32_t tess, float *xyz, uint32_t *indices);
+
+/* Cornell box (5 quads over [-1,1]^3, open toward +z) + `num_spheres` cube-spheres of
+ * 12 * n^2 triangles each with PCG32-drawn radius / centre / GGX material. Counts first, then
+ * fill. per-triangle material id -> tri_material; materials: see vkg_material. */
+typedef struct vkg_material
+{
+    float base_color[3];
+    float roughness;
+    float metalness;
+    float emission[3];
+    uint32_t twosided; /* 1: back faces are not culled (RayBuilder.cpp:521-522) */
+    float pad[3];
+} vkg_material; /* 48 B */
+vkg_status vkg_scene_cornell_counts(uint32_t num_spheres, uint32_t n, uint32_t *num_vertices, uint32_t *num_tris,
+                                    uint32_t *num_materials);
+vkg_status vkg_scene_cornell(uint64_t seed, uint64_t stream, uint32_t num_spheres, uint32_t n, float *xyz,
+                             uint32_t *indices, uint32_t *tri_material, vkg_material *materials);
+
+/* ---- camera rays ---------------------------------------------------------------------------- */
+/* pinhole camera (raypipeline.slang:58-89 with projection.hpp:48-57, aperture 0) */
+typedef struct vkg_camera
+{
+    float eye[3];
+    float right[3], up[3], back[3]; /* camera-to-world rotation columns */
+    float tan_half_fovy;            /* tan(fovy / 2), evaluated by the caller */
+    float aspect;                   /* width / height */
+    uint32_t width, height;
+} vkg_camera;
+/* look-at helper (host): forward = normalize(target - eye), right = normalize(forward x up) */
+vkg_status vkg_camera_lookat(const float eye[3], const float target[3], const float up[3], float tan_half_fovy,
+                             uint32_t width, uint32_t height, vkg_camera *out);
+/* one jittered ray per pixel and sample: ray r = s*W*H + y*W + x uses PCG32(seed, stream) draws
+ * 2r and 2r+1 as the sub-pixel offset. d_rays holds spp*W*H records. */
+vkg_status vkg_camera_rays(vkg_ctx *ctx, const vkg_camera *cam, uint64_t seed, uint64_t stream, uint32_t spp,
+                           vkg_ray *d_rays, void *stream_);
+
+/* ---- BVH ------------------------------------------------------------------------------------- *
+ * replaces RayBuilder::create_mesh_structures (BLAS build, RayBuilder.cpp:98-300,
+ * vkCmdBuildAccelerationStructuresKHR :274) and compaction (:305-356): LBVH (30-bit Morton codes,
+ * radix sort, Karras hierarchy, refit) collapsed to an 8-wide BVH with 8-bit quantised child
+ * boxes, built entirely on the GPU. */
+typedef struct vkg_bvh vkg_bvh;
+
+typedef struct vkg_bvh_build_options
+{
+    uint32_t leaf_max; /* max triangles per leaf range, 1..16 (0 -> default 4) */
+} vkg_bvh_build_options;
+
+typedef struct vkg_bvh_info
+{
+    uint32_t num_tris, num_nodes, depth, leaf_max;
+    float scene_min[3], scene_max[3], margin;
+    size_t bytes;              /* device bytes held by the BVH */
+    const void *d_nodes;       /* num_nodes x 96 B nodes */
+    const void *d_tris;        /* num_tris x 48 B triangle records (sorted order) */
+    const uint32_t *d_morton;  /* num_tris Morton codes, input order */
+    const uint32_t *d_sorted;  /* num_tris triangle ids, sorted order */
+    float build_ms;            /* GPU time of the last build */
+} vkg_bvh_info;
+
+/* builds from device vertex (fp32 xyz) and index (uint32, 3 per triangle) buffers. Synchronises
+ * `stream` before returning (the node count is needed on the host). */
+vkg_status vkg_bvh_build(vkg_ctx *ctx, const float *d_xyz, uint32_t num_vertices, const uint32_t *d_indices,
+                         uint32_t num_tris, const vkg_bvh_build_options *opts, vkg_bvh **out, void *stream);
+vkg_status vkg_bvh_info_get(const vkg_bvh *bvh, vkg_bvh_info *out);
+vkg_status vkg_bvh_destroy(vkg_ctx *ctx, vkg_bvh *bvh);
+
+/* ---- bulk ray queries (replaces TraceRay / RayQuery, raypipeline.slang:182, visibility_test.slang:45-87)
+ * closest hit: accepts Moeller-Trumbore INTERSECT results with tmin < t < tmax, keeps the smallest t,
+ * ties -> smaller triangle id; hit ids are bit-identical to a brute-force loop over
+ * intersect(Triangle, Ray). any hit: d_occluded[i] = 1 if any such hit exists. */
+enum
+{
+    VKG_RAY_CULL_BACK_FACES = 1u, /* RAY_FLAG_CULL_BACK_FACING_TRIANGLES: reject det < 0 (clockwise seen from origin) */
+    VKG_RAY_COUNT_STATS = 2u      /* also count node visits / triangle tests (slower; see vkg_ray_stats_get) */
+};
+vkg_status vkg_closest_hit(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t num_rays,
+                           vkg_hit *d_hits, uint32_t flags, void *stream);
+vkg_status vkg_any_hit(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t num_rays,
+                       uint32_t *d_occluded, uint32_t flags, void *stream);
+/* host-buffer variant: copies rays host->device, traces, copies hits device->host, synchronises.
+ * h_rays / h_hits may be pinned or pageable host memory. */
+vkg_status vkg_closest_hit_host(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *h_rays, uint32_t num_rays,
+                                vkg_hit *h_hits, uint32_t flags, void *stream);
+/* node visits / triangle tests accumulated by launches with VKG_RAY_COUNT_STATS since the last reset */
+vkg_status vkg_ray_stats_get(vkg_ctx *ctx, uint64_t *node_visits, uint64_t *tri_tests, int reset);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VKG_H */

@@ -1,0 +1,218 @@
+"""CPU oracle loader. TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this package, and only as
+the checker / the timed CPU reference. The product (vierkant_gb300, libvkg.so) never imports it.
+
+- ``orc()``  -> liboracle.so: C restatement of the reference's algorithms (see oracle.h)
+- ``ref()``  -> _ref/libvkref.so: the reference's own src/intersection.cpp compiled unmodified
+               against the project-written shim (None if it was not built: it needs the reference
+               checkout, which only exists where the fixtures are generated)
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REF_ROOT = Path(os.environ.get("VKG_REFERENCE_ROOT", "/root/reference"))
+
+RAY_DTYPE = np.dtype([("o", "<f4", 3), ("tmin", "<f4"), ("d", "<f4", 3), ("tmax", "<f4")])
+HIT_DTYPE = np.dtype([("prim", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])
+
+
+class orc_bvh(C.Structure):
+    _fields_ = [("num_tris", C.c_uint32), ("num_nodes", C.c_uint32), ("depth", C.c_uint32), ("leaf_max", C.c_uint32),
+                ("scene_min", C.c_float * 3), ("scene_max", C.c_float * 3), ("margin", C.c_float),
+                ("morton", C.POINTER(C.c_uint32)), ("sorted_prim", C.POINTER(C.c_uint32)),
+                ("bvh2_left", C.POINTER(C.c_uint32)), ("bvh2_right", C.POINTER(C.c_uint32)),
+                ("nodes", C.c_void_p), ("tris", C.c_void_p)]
+
+
+class orc_camera(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("right", C.c_float * 3), ("up", C.c_float * 3), ("back", C.c_float * 3),
+                ("tan_half_fovy", C.c_float), ("aspect", C.c_float), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class orc_sphere_params(C.Structure):
+    _fields_ = [("radius", C.c_float), ("center", C.c_float * 3), ("roughness", C.c_float),
+                ("metalness", C.c_float), ("base", C.c_float * 3)]
+
+
+def build(ref: bool | None = None, quiet: bool = True) -> None:
+    """make liboracle.so (always) and _ref/libvkref.so (when the reference checkout is present)."""
+    out = subprocess.DEVNULL if quiet else None
+    subprocess.run(["make", "-s", "-C", str(HERE), "liboracle.so"], check=True, stdout=out)
+    if ref is None:
+        ref = (REF_ROOT / "src" / "intersection.cpp").exists()
+    if ref:
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF_ROOT={REF_ROOT}"], check=True, stdout=out)
+
+
+_orc = None
+_ref = None
+
+
+def orc() -> C.CDLL:
+    global _orc
+    if _orc is None:
+        p = HERE / "liboracle.so"
+        if not p.exists():
+            build(ref=False)
+        L = C.CDLL(str(p))
+        vp, u32, u64, i32, f32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int, C.c_float
+        sig = {
+            "orc_pcg32_fill": (None, [u64, u64, u64, u32, vp]),
+            "orc_xxhash32": (u32, [u32, u32]),
+            "orc_rnd": (f32, [C.POINTER(u32)]),
+            "orc_intersect_ray_triangle": (i32, [vp, vp, vp, vp]),
+            "orc_intersect_ray_triangle_cull": (i32, [vp, vp, vp, i32, vp]),
+            "orc_intersect_ray_aabb": (i32, [vp, vp, vp, vp, C.POINTER(f32)]),
+            "orc_closest_hit_bruteforce": (i32, [vp, vp, u32, vp, u32, vp, i32, i32]),
+            "orc_any_hit_bruteforce": (i32, [vp, vp, u32, vp, u32, vp, i32, i32]),
+            "orc_icosphere_counts": (u32, [u32, C.POINTER(u32)]),
+            "orc_icosphere": (None, [f32, u32, vp, vp]),
+            "orc_cornell_sphere_params": (None, [u64, u64, u32, vp]),
+            "orc_cornell_scene": (None, [u64, u64, u32, u32, vp, vp, vp]),
+            "orc_camera_lookat": (None, [vp, vp, vp, f32, u32, u32, C.POINTER(orc_camera)]),
+            "orc_camera_rays_pcg": (None, [C.POINTER(orc_camera), u64, u64, u32, vp]),
+            "orc_bvh_build": (i32, [vp, vp, u32, u32, C.POINTER(orc_bvh)]),
+            "orc_bvh_free": (None, [C.POINTER(orc_bvh)]),
+            "orc_bvh_closest_hit": (i32, [C.POINTER(orc_bvh), vp, u32, vp, i32, i32, vp]),
+            "orc_bvh_any_hit": (i32, [C.POINTER(orc_bvh), vp, u32, vp, i32, i32]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _orc = L
+    return _orc
+
+
+def ref() -> C.CDLL | None:
+    global _ref
+    if _ref is None:
+        p = HERE / "_ref" / "libvkref.so"
+        if not p.exists():
+            return None
+        L = C.CDLL(str(p))
+        vp, u32, i32, f32 = C.c_void_p, C.c_uint32, C.c_int, C.c_float
+        sig = {
+            "vkref_intersect_ray_triangle": (i32, [vp, vp, vp, vp]),
+            "vkref_intersect_ray_aabb": (i32, [vp, vp, vp, vp, C.POINTER(f32)]),
+            "vkref_intersect_ray_sphere": (i32, [vp, vp, vp, f32, C.POINTER(f32)]),
+            "vkref_intersect_ray_plane": (i32, [vp, vp, vp, C.POINTER(f32)]),
+            "vkref_triangle_aabb_overlap": (u32, [vp, vp, vp]),
+            "vkref_triangle_triangle_overlap": (u32, [vp, vp]),
+            "vkref_closest_hit_bruteforce": (i32, [vp, vp, u32, vp, u32, vp, i32, i32]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _ref = L
+    return _ref
+
+
+def ptr(a: np.ndarray) -> C.c_void_p:
+    return a.ctypes.data_as(C.c_void_p)
+
+
+# ---- convenience wrappers ----------------------------------------------------------------------
+def icosphere(radius=1.0, tess=5):
+    L = orc()
+    nt = C.c_uint32()
+    nv = L.orc_icosphere_counts(tess, C.byref(nt))
+    xyz = np.zeros((nv, 3), np.float32)
+    idx = np.zeros((nt.value, 3), np.uint32)
+    L.orc_icosphere(radius, tess, ptr(xyz), ptr(idx))
+    return xyz, idx
+
+
+def cornell_scene(seed=0x5EED, stream=2, num_spheres=64, n=16):
+    L = orc()
+    nv = 20 + num_spheres * 6 * (n + 1) ** 2
+    nt = 10 + num_spheres * 12 * n * n
+    xyz = np.zeros((nv, 3), np.float32)
+    idx = np.zeros((nt, 3), np.uint32)
+    tm = np.zeros(nt, np.uint32)
+    L.orc_cornell_scene(seed, stream, num_spheres, n, ptr(xyz), ptr(idx), ptr(tm))
+    params = (orc_sphere_params * max(1, num_spheres))()
+    L.orc_cornell_sphere_params(seed, stream, num_spheres, C.cast(params, C.c_void_p))
+    return {"xyz": xyz, "indices": idx, "tri_material": tm, "spheres": params}
+
+
+def camera(eye, target, up, tan_half_fovy, width, height) -> orc_camera:
+    cam = orc_camera()
+    e, t, u = (np.asarray(x, np.float32) for x in (eye, target, up))
+    orc().orc_camera_lookat(ptr(e), ptr(t), ptr(u), tan_half_fovy, width, height, C.byref(cam))
+    return cam
+
+
+def camera_rays(cam: orc_camera, seed: int, stream: int, spp: int = 1) -> np.ndarray:
+    rays = np.zeros(cam.width * cam.height * spp, RAY_DTYPE)
+    orc().orc_camera_rays_pcg(C.byref(cam), seed, stream, spp, ptr(rays))
+    return rays
+
+
+def closest_hit_bruteforce(xyz, idx, rays, nthreads=0, cull=False):
+    hits = np.zeros(len(rays), HIT_DTYPE)
+    orc().orc_closest_hit_bruteforce(ptr(xyz), ptr(idx), idx.shape[0], ptr(rays), len(rays), ptr(hits), nthreads,
+                                     int(cull))
+    return hits
+
+
+def any_hit_bruteforce(xyz, idx, rays, nthreads=0, cull=False):
+    occ = np.zeros(len(rays), np.uint32)
+    orc().orc_any_hit_bruteforce(ptr(xyz), ptr(idx), idx.shape[0], ptr(rays), len(rays), ptr(occ), nthreads,
+                                 int(cull))
+    return occ
+
+
+NODE_BYTES = 96
+TRI_BYTES = 48
+
+
+class CpuBVH:
+    """The oracle's LBVH -> 8-wide BVH (same algorithm as the GPU build), with CPU traversal."""
+
+    def __init__(self, xyz, idx, leaf_max=4):
+        self.xyz, self.idx = np.ascontiguousarray(xyz, np.float32), np.ascontiguousarray(idx, np.uint32)
+        self.b = orc_bvh()
+        rc = orc().orc_bvh_build(ptr(self.xyz), ptr(self.idx), self.idx.shape[0], leaf_max, C.byref(self.b))
+        if rc != 0:
+            raise RuntimeError(f"orc_bvh_build failed ({rc})")
+
+    def __del__(self):
+        try:
+            orc().orc_bvh_free(C.byref(self.b))
+        except Exception:
+            pass
+
+    @property
+    def morton(self):
+        return np.ctypeslib.as_array(self.b.morton, (self.b.num_tris,)).copy() if self.b.num_tris else np.zeros(0)
+
+    @property
+    def sorted_prim(self):
+        return np.ctypeslib.as_array(self.b.sorted_prim, (self.b.num_tris,)).copy() if self.b.num_tris else np.zeros(0)
+
+    def node_bytes(self) -> bytes:
+        return C.string_at(self.b.nodes, self.b.num_nodes * NODE_BYTES) if self.b.num_nodes else b""
+
+    def tri_bytes(self) -> bytes:
+        return C.string_at(self.b.tris, self.b.num_tris * TRI_BYTES) if self.b.num_tris else b""
+
+    def closest_hit(self, rays, nthreads=0, cull=False, stats=False):
+        hits = np.zeros(len(rays), HIT_DTYPE)
+        st = np.zeros(2, np.uint64)
+        orc().orc_bvh_closest_hit(C.byref(self.b), ptr(rays), len(rays), ptr(hits), nthreads, int(cull), ptr(st))
+        return (hits, (int(st[0]), int(st[1]))) if stats else hits
+
+    def any_hit(self, rays, nthreads=0, cull=False):
+        occ = np.zeros(len(rays), np.uint32)
+        orc().orc_bvh_any_hit(C.byref(self.b), ptr(rays), len(rays), ptr(occ), nthreads, int(cull))
+        return occ

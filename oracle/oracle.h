@@ -1,0 +1,113 @@
+/*
+ * CPU oracle for the path-tracing hot path. TEST INFRASTRUCTURE ONLY.
+ *
+ * This is a plain-C restatement of the reference's algorithms (vierkant: src/intersection.cpp,
+ * src/Geometry.cpp, shaders/slang/...) plus the project-defined parts the reference does not have
+ * (PCG32 streams, LBVH -> 8-wide BVH build, camera-ray batches). It exists only to check the CUDA
+ * product path: tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it; the
+ * product library (vierkant_gb300/libvkg.so) never does.
+ *
+ * Pinning: the ray-triangle / ray-box restatements are checked bit-for-bit against the
+ * reference's own src/intersection.cpp compiled unmodified into oracle/_ref/libvkref.so
+ * (see oracle/Makefile) and against the committed fixtures in tests/golden/.
+ *
+ * Compiled with -ffp-contract=off: every float operation rounds separately, like the
+ * reference's x86-64 build (no FMA without -march). Where the GPU kernels use a fused
+ * multiply-add on purpose (box slab tests), the oracle calls fmaf() explicitly.
+ */
+#ifndef VKG_ORACLE_H
+#define VKG_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- records (identical layouts to include/vkg.h) ---------------------------------------- */
+typedef struct { float o[3]; float tmin; float d[3]; float tmax; } orc_ray; /* 32 B */
+typedef struct { uint32_t prim; float t, u, v; } orc_hit;                   /* 16 B */
+
+#define ORC_MISS 0xFFFFFFFFu
+
+/* ---- RNG -------------------------------------------------------------------------------- */
+typedef struct { uint64_t state, inc; } orc_pcg32;
+void orc_pcg32_seed(orc_pcg32 *g, uint64_t initstate, uint64_t initseq);
+uint32_t orc_pcg32_next(orc_pcg32 *g);
+void orc_pcg32_advance(orc_pcg32 *g, uint64_t delta);
+float orc_u01(uint32_t x);
+void orc_pcg32_fill(uint64_t initstate, uint64_t initseq, uint64_t skip, uint32_t n, uint32_t *out);
+uint32_t orc_xxhash32(uint32_t lhs, uint32_t rhs);
+uint32_t orc_lcg(uint32_t *prev);
+float orc_rnd(uint32_t *prev);
+
+/* ---- intersection (intersection.cpp) --------------------------------------------------- */
+int orc_intersect_ray_triangle(const float o[3], const float d[3], const float tri[9], float out_tuv[3]);
+int orc_intersect_ray_triangle_cull(const float o[3], const float d[3], const float tri[9], int cull_back,
+                                    float out_tuv[3]);
+int orc_intersect_ray_aabb(const float o[3], const float d[3], const float bmin[3], const float bmax[3], float *t);
+int orc_closest_hit_bruteforce(const float *xyz, const uint32_t *idx, uint32_t ntri, const orc_ray *rays,
+                               uint32_t nray, orc_hit *hits, int nthreads, int cull_back);
+int orc_any_hit_bruteforce(const float *xyz, const uint32_t *idx, uint32_t ntri, const orc_ray *rays,
+                           uint32_t nray, uint32_t *occluded, int nthreads, int cull_back);
+
+/* ---- geometry (Geometry.cpp) and scenes ------------------------------------------------ */
+uint32_t orc_icosphere_counts(uint32_t tess, uint32_t *num_tris);
+void orc_icosphere(float radius, uint32_t tess, float *xyz, uint32_t *idx);
+void orc_cubesphere(float radius, const float center[3], uint32_t n, float *xyz, uint32_t *idx, uint32_t vbase);
+typedef struct {
+    float radius, center[3];
+    float roughness, metalness, base[3];
+} orc_sphere_params;
+void orc_cornell_sphere_params(uint64_t seed, uint64_t stream, uint32_t nspheres, orc_sphere_params *out);
+void orc_cornell_scene(uint64_t seed, uint64_t stream, uint32_t nspheres, uint32_t n, float *xyz, uint32_t *idx,
+                       uint32_t *tri_material);
+
+/* ---- camera rays ----------------------------------------------------------------------- */
+typedef struct {
+    float eye[3];
+    float right[3], up[3], back[3]; /* camera-to-world rotation columns */
+    float tan_half_fovy, aspect;
+    uint32_t width, height;
+} orc_camera;
+void orc_camera_lookat(const float eye[3], const float target[3], const float up[3], float tan_half_fovy,
+                       uint32_t width, uint32_t height, orc_camera *cam);
+void orc_camera_ray(const orc_camera *cam, uint32_t x, uint32_t y, float jx, float jy, orc_ray *ray);
+void orc_camera_rays_pcg(const orc_camera *cam, uint64_t seed, uint64_t stream, uint32_t spp, orc_ray *rays);
+
+/* ---- LBVH -> 8-wide BVH ---------------------------------------------------------------- */
+typedef struct {
+    float origin[3];
+    uint8_t exps[3];
+    uint8_t nchild;
+    uint8_t qlo[3][8];
+    uint8_t qhi[3][8];
+    uint32_t child[8];
+} orc_node8; /* 96 B */
+
+typedef struct {
+    float v[12]; /* v0.xyz, e1.xyz, e2.xyz, prim_id bits, pad, pad */
+} orc_tri;   /* 48 B */
+
+typedef struct {
+    uint32_t num_tris, num_nodes, depth, leaf_max;
+    float scene_min[3], scene_max[3], margin;
+    uint32_t *morton;      /* [num_tris] in triangle (input) order */
+    uint32_t *sorted_prim; /* [num_tris] */
+    uint32_t *bvh2_left, *bvh2_right; /* [num_tris-1], child encoding: bit31 leaf */
+    orc_node8 *nodes;      /* [num_nodes] */
+    orc_tri *tris;         /* [num_tris] in sorted order */
+} orc_bvh;
+
+int orc_bvh_build(const float *xyz, const uint32_t *idx, uint32_t ntri, uint32_t leaf_max, orc_bvh *out);
+void orc_bvh_free(orc_bvh *b);
+int orc_bvh_closest_hit(const orc_bvh *b, const orc_ray *rays, uint32_t nray, orc_hit *hits, int nthreads,
+                        int cull_back, uint64_t *stats /* [2]: node visits, tri tests; may be NULL */);
+int orc_bvh_any_hit(const orc_bvh *b, const orc_ray *rays, uint32_t nray, uint32_t *occluded, int nthreads,
+                    int cull_back);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,176 @@
+"""The CPU oracle is pinned before it is trusted: against the reference's own compiled code
+(oracle/_ref, when present), the committed golden fixtures made from it, and published
+known-answer vectors."""
+import ctypes as C
+import hashlib
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle import ptr
+
+
+def test_pcg32_published_known_answer():
+    # pcg32_srandom_r(42, 54): the first six outputs of O'Neill's reference demo
+    out = np.zeros(6, np.uint32)
+    oracle.orc().orc_pcg32_fill(42, 54, 0, 6, ptr(out))
+    assert [int(x) for x in out] == [0xa15c02b7, 0x7b47f409, 0xba1d3330, 0x83d2f293, 0xbfa4784b, 0xcbed606e]
+
+
+def test_pcg32_jump_ahead_matches_sequential():
+    seq = np.zeros(1000, np.uint32)
+    oracle.orc().orc_pcg32_fill(0x5EED, 7, 0, 1000, ptr(seq))
+    for skip in (1, 17, 500, 999):
+        one = np.zeros(1, np.uint32)
+        oracle.orc().orc_pcg32_fill(0x5EED, 7, skip, 1, ptr(one))
+        assert one[0] == seq[skip]
+
+
+def test_rng_tables_match_golden(golden):
+    g = golden("rng")
+    pcg = np.zeros(4096, np.uint32)
+    oracle.orc().orc_pcg32_fill(0x5EED, 1, 0, 4096, ptr(pcg))
+    assert np.array_equal(pcg, g["pcg32_5eed_1"])
+    xx = [oracle.orc().orc_xxhash32(int(a), int(b)) for a, b in zip(g["xx_lhs"], g["xx_rhs"])]
+    assert np.array_equal(np.array(xx, np.uint32), g["xxhash32"])
+
+
+def test_ray_triangle_matches_reference_fixture(golden):
+    g = golden("ray_triangle")
+    L = oracle.orc()
+    for i in range(len(g["type"])):
+        out = np.zeros(3, np.float32)
+        t = L.orc_intersect_ray_triangle(ptr(g["o"][i]), ptr(g["d"][i]), ptr(g["tri"][i]), ptr(out))
+        assert t == g["type"][i]
+        if t:
+            assert out.tobytes() == g["tuv"][i].tobytes(), i
+
+
+def test_ray_aabb_matches_reference_fixture(golden):
+    g = golden("ray_aabb")
+    L = oracle.orc()
+    for i in range(len(g["type"])):
+        tt = C.c_float()
+        t = L.orc_intersect_ray_aabb(ptr(g["o"][i]), ptr(g["d"][i]), ptr(g["lo"][i]), ptr(g["hi"][i]), C.byref(tt))
+        assert t == g["type"][i]
+        if t:
+            assert np.float32(tt.value).tobytes() == g["t"][i].tobytes()
+
+
+def test_oracle_against_live_reference_random():
+    R = oracle.ref()
+    if R is None:
+        pytest.skip("reference checkout not present here (fixtures cover this case)")
+    rng = np.random.default_rng(5)
+    L = oracle.orc()
+    for _ in range(20000):
+        o, d, tri = (rng.normal(size=k).astype(np.float32) for k in (3, 3, 9))
+        a, b = np.zeros(3, np.float32), np.zeros(3, np.float32)
+        ra = L.orc_intersect_ray_triangle(ptr(o), ptr(d), ptr(tri), ptr(a))
+        rb = R.vkref_intersect_ray_triangle(ptr(o), ptr(d), ptr(tri), ptr(b))
+        assert ra == rb and (not ra or a.tobytes() == b.tobytes())
+
+
+def test_icosphere_counts_and_fixture(golden):
+    xyz, idx = oracle.icosphere(1.0, 5)
+    assert xyz.shape == (20472, 3) and idx.shape == (20480, 3)
+    g = golden("config1_hits")
+    assert hashlib.sha256(xyz.tobytes()).hexdigest() == str(g["sha_xyz"])
+    assert hashlib.sha256(idx.tobytes()).hexdigest() == str(g["sha_idx"])
+    r = np.linalg.norm(xyz.astype(np.float64), axis=1)
+    assert np.all(np.abs(r - 1.0) < 1e-6)
+
+
+def test_config1_bruteforce_matches_reference_fixture(golden):
+    g = golden("config1_hits")
+    xyz, idx = oracle.icosphere(1.0, 5)
+    th = float(np.float32(math.tan(math.radians(60.0) / 2.0)))
+    assert np.float32(th) == g["tan_half_fovy"]
+    cam = oracle.camera((0, 0, 3), (0, 0, 0), (0, 1, 0), th, 1024, 1024)
+    rays = oracle.camera_rays(cam, 0x5EED, 1, 1)
+    assert hashlib.sha256(rays.tobytes()).hexdigest() == str(g["sha_rays"])
+    sub = np.ascontiguousarray(rays[g["ray_index"]][:2048])
+    hits = oracle.closest_hit_bruteforce(xyz, idx, sub)
+    assert np.array_equal(hits.view(np.uint32).reshape(-1, 4), g["hits"][:2048])
+
+
+def test_known_answers_from_reference_source():
+    xyz, idx = oracle.icosphere(1.0, 5)
+    r = np.zeros(1, oracle.RAY_DTYPE)
+    r["o"] = (0, 0, 3)
+    r["d"] = (0, 0, -1)
+    r["tmin"], r["tmax"] = 1e-4, 1e4
+    h = oracle.closest_hit_bruteforce(xyz, idx, r)
+    assert h["prim"][0] != 0xFFFFFFFF and 2.0 <= h["t"][0] < 2.01
+    # grazing ray: |det| < 1e-9 is rejected (intersection.cpp:119-120)
+    out = np.zeros(3, np.float32)
+    tri = np.array([0, 0, 0, 1, 0, 0, 0, 1, 0], np.float32)
+    assert oracle.orc().orc_intersect_ray_triangle(ptr(np.float32([0.2, 0.2, 0])), ptr(np.float32([1, 0, 0])),
+                                                   ptr(tri), ptr(out)) == 0
+    # origin inside the box returns t_max (intersection.cpp:179-183)
+    tt = C.c_float()
+    assert oracle.orc().orc_intersect_ray_aabb(ptr(np.float32([0, 0, 0])), ptr(np.float32([1, 0, 0])),
+                                               ptr(np.float32([-1, -1, -1])), ptr(np.float32([2, 1, 1])),
+                                               C.byref(tt)) == 1
+    assert tt.value == 2.0
+    # back-face culling: the outward face is front-facing for a ray from outside, a ray from the
+    # centre passes through when culling is on
+    r2 = np.zeros(1, oracle.RAY_DTYPE)
+    r2["o"] = (0, 0, 0)
+    r2["d"] = (0, 0, 1)
+    r2["tmin"], r2["tmax"] = 1e-4, 1e4
+    assert oracle.closest_hit_bruteforce(xyz, idx, r, cull=True)["prim"][0] != 0xFFFFFFFF
+    assert oracle.closest_hit_bruteforce(xyz, idx, r2, cull=True)["prim"][0] == 0xFFFFFFFF
+    assert oracle.closest_hit_bruteforce(xyz, idx, r2, cull=False)["prim"][0] != 0xFFFFFFFF
+
+
+def _random_mesh(rng, nt, spread=1.0):
+    xyz = (rng.normal(size=(3 * nt, 3)) * spread).astype(np.float32)
+    base = rng.normal(size=(nt, 1, 3)).astype(np.float32) * 2
+    xyz = (xyz.reshape(nt, 3, 3) * 0.2 + base).reshape(-1, 3).astype(np.float32)
+    idx = np.arange(3 * nt, dtype=np.uint32).reshape(nt, 3)
+    return xyz, idx
+
+
+def _random_rays(rng, n, spread=3.0):
+    rays = np.zeros(n, oracle.RAY_DTYPE)
+    o = (rng.normal(size=(n, 3)) * spread).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True).astype(np.float32)
+    rays["o"], rays["d"], rays["tmin"], rays["tmax"] = o, d, 1e-4, 1e4
+    return rays
+
+
+@pytest.mark.parametrize("leaf_max", [1, 4, 16])
+@pytest.mark.parametrize("nt", [1, 2, 3, 37, 1000])
+def test_oracle_bvh_equals_bruteforce(nt, leaf_max):
+    rng = np.random.default_rng(nt * 31 + leaf_max)
+    xyz, idx = _random_mesh(rng, nt)
+    rays = _random_rays(rng, 3000)
+    b = oracle.CpuBVH(xyz, idx, leaf_max)
+    for cull in (False, True):
+        assert b.closest_hit(rays, cull=cull).tobytes() == oracle.closest_hit_bruteforce(xyz, idx, rays,
+                                                                                         cull=cull).tobytes()
+        assert np.array_equal(b.any_hit(rays, cull=cull), oracle.any_hit_bruteforce(xyz, idx, rays, cull=cull))
+
+
+def test_oracle_bvh_ties_and_degenerates():
+    # duplicated triangles (exact t ties -> smaller id wins), degenerate and zero-area triangles
+    rng = np.random.default_rng(3)
+    xyz, idx = _random_mesh(rng, 200)
+    idx = np.concatenate([idx, idx[:50], idx[10:20][:, [0, 0, 1]]]).astype(np.uint32)
+    xyz = xyz.copy()
+    rays = _random_rays(rng, 5000)
+    rays["d"][::11, 1] = 0.0  # zero direction components
+    b = oracle.CpuBVH(xyz, idx, 4)
+    bf = oracle.closest_hit_bruteforce(xyz, idx, rays)
+    assert b.closest_hit(rays).tobytes() == bf.tobytes()
+    assert np.all(bf["prim"][bf["prim"] != 0xFFFFFFFF] < len(idx))
+
+
+def test_oracle_bvh_empty_mesh():
+    b = oracle.CpuBVH(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32))
+    rays = _random_rays(np.random.default_rng(0), 10)
+    assert np.all(b.closest_hit(rays)["prim"] == 0xFFFFFFFF)

@@ -1,0 +1,123 @@
+"""ctypes binding of libvkg.so (the C ABI declared in include/vkg.h).
+
+The library is loaded from the package directory; a missing library is a hard error (there is no
+CPU fallback for any GPU entry point). Build it with ``python -m vierkant_gb300.build``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libvkg.so"
+
+VKG_OK = 0
+STATUS_NAMES = {0: "VKG_OK", 1: "VKG_ERR_INVALID_ARGUMENT", 2: "VKG_ERR_CUDA", 3: "VKG_ERR_OUT_OF_MEMORY",
+                4: "VKG_ERR_NOT_SUPPORTED", 5: "VKG_ERR_TIMEOUT", 6: "VKG_ERR_STACK_OVERFLOW",
+                7: "VKG_ERR_CAPACITY"}
+VKG_MISS = 0xFFFFFFFF
+REJECT, INTERSECT, INSIDE = 0, 1, 2
+RAY_CULL_BACK_FACES = 1
+RAY_COUNT_STATS = 2
+
+
+class VkgError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class vkg_ray(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("tmin", C.c_float), ("direction", C.c_float * 3), ("tmax", C.c_float)]
+
+
+class vkg_hit(C.Structure):
+    _fields_ = [("prim", C.c_uint32), ("t", C.c_float), ("u", C.c_float), ("v", C.c_float)]
+
+
+class vkg_ray_intersection(C.Structure):
+    _fields_ = [("type", C.c_int), ("distance", C.c_float)]
+
+
+class vkg_ray_triangle_intersection(C.Structure):
+    _fields_ = [("type", C.c_int), ("distance", C.c_float), ("u", C.c_float), ("v", C.c_float)]
+
+
+class vkg_material(C.Structure):
+    _fields_ = [("base_color", C.c_float * 3), ("roughness", C.c_float), ("metalness", C.c_float),
+                ("emission", C.c_float * 3), ("twosided", C.c_uint32), ("pad", C.c_float * 3)]
+
+
+class vkg_camera(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("right", C.c_float * 3), ("up", C.c_float * 3), ("back", C.c_float * 3),
+                ("tan_half_fovy", C.c_float), ("aspect", C.c_float), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class vkg_bvh_build_options(C.Structure):
+    _fields_ = [("leaf_max", C.c_uint32)]
+
+
+class vkg_bvh_info(C.Structure):
+    _fields_ = [("num_tris", C.c_uint32), ("num_nodes", C.c_uint32), ("depth", C.c_uint32), ("leaf_max", C.c_uint32),
+                ("scene_min", C.c_float * 3), ("scene_max", C.c_float * 3), ("margin", C.c_float),
+                ("bytes", C.c_size_t), ("d_nodes", C.c_void_p), ("d_tris", C.c_void_p), ("d_morton", C.c_void_p),
+                ("d_sorted", C.c_void_p), ("build_ms", C.c_float)]
+
+
+P = C.c_void_p
+U32 = C.c_uint32
+U64 = C.c_uint64
+I32 = C.c_int
+F32 = C.c_float
+PF = C.POINTER(C.c_float)
+
+# name -> (restype, argtypes); keep in sync with include/vkg.h
+SIGNATURES = {
+    "vkg_version": (C.c_char_p, []),
+    "vkg_ctx_create": (I32, [I32, C.POINTER(P)]),
+    "vkg_ctx_destroy": (I32, [P]),
+    "vkg_last_error": (C.c_char_p, [P]),
+    "vkg_intersect_ray_triangle": (I32, [P, P, P, C.POINTER(vkg_ray_triangle_intersection)]),
+    "vkg_intersect_ray_aabb": (I32, [P, P, P, P, C.POINTER(vkg_ray_intersection)]),
+    "vkg_intersect_ray_obb": (I32, [P, P, P, P, P, C.POINTER(vkg_ray_intersection)]),
+    "vkg_intersect_ray_sphere": (I32, [P, P, P, F32, C.POINTER(vkg_ray_intersection)]),
+    "vkg_intersect_ray_plane": (I32, [P, P, P, C.POINTER(vkg_ray_intersection)]),
+    "vkg_intersect_triangle_aabb": (I32, [P, P, P, C.POINTER(U32)]),
+    "vkg_intersect_triangle_triangle": (I32, [P, P, C.POINTER(U32)]),
+    "vkg_geometry_icosphere_counts": (I32, [U32, C.POINTER(U32), C.POINTER(U32)]),
+    "vkg_geometry_icosphere": (I32, [F32, U32, P, P]),
+    "vkg_scene_cornell_counts": (I32, [U32, U32, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)]),
+    "vkg_scene_cornell": (I32, [U64, U64, U32, U32, P, P, P, P]),
+    "vkg_camera_lookat": (I32, [P, P, P, F32, U32, U32, C.POINTER(vkg_camera)]),
+    "vkg_camera_rays": (I32, [P, C.POINTER(vkg_camera), U64, U64, U32, P, P]),
+    "vkg_bvh_build": (I32, [P, P, U32, P, U32, C.POINTER(vkg_bvh_build_options), C.POINTER(P), P]),
+    "vkg_bvh_info_get": (I32, [P, C.POINTER(vkg_bvh_info)]),
+    "vkg_bvh_destroy": (I32, [P, P]),
+    "vkg_closest_hit": (I32, [P, P, P, U32, P, U32, P]),
+    "vkg_any_hit": (I32, [P, P, P, U32, P, U32, P]),
+    "vkg_closest_hit_host": (I32, [P, P, P, U32, P, U32, P]),
+    "vkg_ray_stats_get": (I32, [P, C.POINTER(U64), C.POINTER(U64), I32]),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libvkg.so (once). Raises if the library has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m vierkant_gb300.build` "
+                               "(the GPU path has no fallback)")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int, ctx=None, what: str = "") -> None:
+    if status != VKG_OK:
+        msg = lib().vkg_last_error(ctx).decode() if ctx else ""
+        raise VkgError(status, f"{what}: {msg}" if what else msg)

@@ -1,0 +1,778 @@
+// GPU LBVH build collapsed to an 8-wide quantised BVH.
+//
+// Replaces the reference's driver-built bottom-level acceleration structure
+// (RayBuilder::create_mesh_structures, src/RayBuilder.cpp:98-300, vkCmdBuildAccelerationStructuresKHR
+// at :274) and its compaction copy (:305-356). The reference's BVH is opaque; this one is fully
+// specified so that every stage can be compared bit-for-bit with the CPU statement of the same
+// algorithm:
+//   k_tri_boxes    triangle boxes + scene box (order-independent min/max atomics)
+//   k_morton       30-bit Morton code of each box centre over the scene box
+//   k_radix_*      stable LSD radix sort of (code, triangle id), 8 bits per pass
+//   k_karras       Karras 2012 radix tree (equal codes split by index)
+//   k_refit        bottom-up boxes, second arriving child finishes the parent
+//   k_collapse     breadth-first collapse to 8-wide nodes + 8-bit box quantisation (one CTA)
+//   k_tri_records  48-byte triangle records (v0, e1, e2, id) in sorted order
+// Data layout in HBM: nodes (96 B each) and triangle records (48 B each) are contiguous arrays read
+// with 16-byte vector loads by the traversal kernels.
+#include "internal.hpp"
+
+#include <cstring>
+#include <vector>
+
+namespace vkg
+{
+namespace
+{
+
+constexpr int SORT_THREADS = 256;
+constexpr int SORT_ITEMS = 16;
+constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS; // keys per block
+
+struct box6
+{
+    float lo[3], hi[3];
+};
+
+// ordered-uint encoding: monotone for every float, so min/max atomics on it are exact
+__device__ __forceinline__ uint32_t fenc(float f)
+{
+    uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float fdec(uint32_t u) { return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u); }
+
+// errors reported by the build kernels
+enum : uint32_t
+{
+    BUILD_ERR_INDEX = 1u,    // an index >= num_vertices
+    BUILD_ERR_CAPACITY = 2u, // node capacity exceeded
+};
+
+__global__ void k_tri_boxes(const float *__restrict__ xyz, uint32_t nv, const uint32_t *__restrict__ idx, uint32_t n,
+                            box6 *__restrict__ tbox, uint32_t *__restrict__ scene_enc, uint32_t *__restrict__ err)
+{
+    __shared__ uint32_t s_lo[3], s_hi[3];
+    if(threadIdx.x < 3)
+    {
+        s_lo[threadIdx.x] = fenc(__int_as_float(0x7f800000));  // +inf
+        s_hi[threadIdx.x] = fenc(__int_as_float(0xff800000));  // -inf
+    }
+    __syncthreads();
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i < n)
+    {
+        box6 b;
+        for(int a = 0; a < 3; ++a)
+        {
+            b.lo[a] = __int_as_float(0x7f800000);
+            b.hi[a] = __int_as_float(0xff800000);
+        }
+        for(int k = 0; k < 3; ++k)
+        {
+            uint32_t vi = __ldg(&idx[3 * (size_t)i + k]);
+            if(vi >= nv)
+            {
+                atomicOr(err, BUILD_ERR_INDEX);
+                vi = 0;
+            }
+            for(int a = 0; a < 3; ++a)
+            {
+                float p = __ldg(&xyz[3 * (size_t)vi + a]);
+                b.lo[a] = fminf(b.lo[a], p);
+                b.hi[a] = fmaxf(b.hi[a], p);
+            }
+        }
+        tbox[i] = b;
+        for(int a = 0; a < 3; ++a)
+        {
+            atomicMin(&s_lo[a], fenc(b.lo[a]));
+            atomicMax(&s_hi[a], fenc(b.hi[a]));
+        }
+    }
+    __syncthreads();
+    if(threadIdx.x < 3)
+    {
+        atomicMin(&scene_enc[threadIdx.x], s_lo[threadIdx.x]);
+        atomicMax(&scene_enc[3 + threadIdx.x], s_hi[threadIdx.x]);
+    }
+}
+
+__device__ __forceinline__ void scene_box(const uint32_t *scene_enc, float lo[3], float hi[3])
+{
+    for(int a = 0; a < 3; ++a)
+    {
+        lo[a] = fdec(scene_enc[a]);
+        hi[a] = fdec(scene_enc[3 + a]);
+    }
+}
+
+__global__ void k_morton(const box6 *__restrict__ tbox, uint32_t n, const uint32_t *__restrict__ scene_enc,
+                         uint32_t *__restrict__ keys, uint32_t *__restrict__ vals, uint32_t *__restrict__ morton_out)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n) return;
+    float lo[3], hi[3];
+    scene_box(scene_enc, lo, hi);
+    box6 b = tbox[i];
+    uint32_t q[3];
+    for(int a = 0; a < 3; ++a)
+    {
+        float e = fsub(hi[a], lo[a]);
+        float scale = e > 0.f ? fdiv(1024.0f, e) : 0.f;
+        float c = fmul(fadd(b.lo[a], b.hi[a]), 0.5f);
+        float f = fmul(fsub(c, lo[a]), scale);
+        uint32_t v = f > 0.f ? __float2uint_rz(f) : 0u;
+        q[a] = v > 1023u ? 1023u : v;
+    }
+    uint32_t code = (expand10(q[0]) << 2) | (expand10(q[1]) << 1) | expand10(q[2]);
+    keys[i] = code;
+    vals[i] = i;
+    morton_out[i] = code;
+}
+
+// ---- stable LSD radix sort ------------------------------------------------------------------
+__global__ void k_radix_hist(const uint32_t *__restrict__ keys, uint32_t n, int shift, uint32_t *__restrict__ counts,
+                             uint32_t nblocks)
+{
+    __shared__ uint32_t hist[256];
+    hist[threadIdx.x] = 0;
+    __syncthreads();
+    size_t base = (size_t)blockIdx.x * SORT_TILE;
+    for(int it = 0; it < SORT_ITEMS; ++it)
+    {
+        size_t i = base + (size_t)it * SORT_THREADS + threadIdx.x;
+        if(i < n) atomicAdd(&hist[(keys[i] >> shift) & 0xFFu], 1u);
+    }
+    __syncthreads();
+    counts[(size_t)threadIdx.x * nblocks + blockIdx.x] = hist[threadIdx.x];
+}
+
+// exclusive scan of `count` words in place (single CTA of 1024 threads)
+__global__ void k_scan_exclusive(uint32_t *__restrict__ data, uint32_t count, uint32_t *__restrict__ total)
+{
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t carry;
+    if(threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    for(uint32_t base = 0; base < count; base += 1024u)
+    {
+        uint32_t i = base + threadIdx.x;
+        uint32_t v = i < count ? data[i] : 0u;
+        uint32_t x = v;
+        for(int o = 1; o < 32; o <<= 1)
+        {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if(lane >= (uint32_t)o) x += y;
+        }
+        if(lane == 31) warp_sums[warp] = x;
+        __syncthreads();
+        if(warp == 0)
+        {
+            uint32_t w = warp_sums[lane];
+            for(int o = 1; o < 32; o <<= 1)
+            {
+                uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if(lane >= (uint32_t)o) w += y;
+            }
+            warp_sums[lane] = w; // inclusive over warps
+        }
+        __syncthreads();
+        uint32_t warp_prefix = warp ? warp_sums[warp - 1] : 0u;
+        uint32_t c = carry;
+        if(i < count) data[i] = c + warp_prefix + x - v;
+        __syncthreads();
+        if(threadIdx.x == 1023) carry = c + warp_sums[31];
+        __syncthreads();
+    }
+    if(threadIdx.x == 0 && total) *total = carry;
+}
+
+__global__ void k_radix_scatter(const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in, uint32_t n,
+                                int shift, const uint32_t *__restrict__ offsets, uint32_t nblocks,
+                                uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out)
+{
+    __shared__ uint32_t s_off[256];
+    __shared__ uint32_t s_warp[8][257];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    s_off[tid] = offsets[(size_t)tid * nblocks + blockIdx.x];
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    size_t base = (size_t)blockIdx.x * SORT_TILE;
+    for(int it = 0; it < SORT_ITEMS; ++it)
+    {
+        for(uint32_t j = tid; j < 8u * 257u; j += SORT_THREADS) (&s_warp[0][0])[j] = 0u;
+        __syncthreads();
+        size_t i = base + (size_t)it * SORT_THREADS + tid;
+        bool valid = i < n;
+        uint32_t key = valid ? keys_in[i] : 0u;
+        uint32_t val = valid ? vals_in[i] : 0u;
+        uint32_t digit = valid ? ((key >> shift) & 0xFFu) : 256u;
+        uint32_t peers = __match_any_sync(0xffffffffu, digit);
+        uint32_t rank = __popc(peers & lt_mask);
+        if(rank == 0) s_warp[warp][digit] = __popc(peers);
+        __syncthreads();
+        // exclusive prefix over the 8 warps for digit `tid`
+        uint32_t run = 0;
+        for(int w = 0; w < 8; ++w)
+        {
+            uint32_t c = s_warp[w][tid];
+            s_warp[w][tid] = run;
+            run += c;
+        }
+        __syncthreads();
+        if(valid)
+        {
+            uint32_t pos = s_off[digit] + s_warp[warp][digit] + rank;
+            keys_out[pos] = key;
+            vals_out[pos] = val;
+        }
+        __syncthreads();
+        s_off[tid] += run;
+        __syncthreads();
+    }
+}
+
+// ---- Karras radix tree ------------------------------------------------------------------------
+__device__ __forceinline__ int kdelta(const uint32_t *codes, int64_t n, int64_t i, int64_t j)
+{
+    if(j < 0 || j >= n) return -1;
+    uint32_t a = codes[i], b = codes[j];
+    if(a == b) return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+    return __clz(a ^ b);
+}
+
+__global__ void k_karras(const uint32_t *__restrict__ codes, uint32_t n, uint32_t *__restrict__ left,
+                         uint32_t *__restrict__ right, uint32_t *__restrict__ first, uint32_t *__restrict__ last,
+                         uint32_t *__restrict__ iparent, uint32_t *__restrict__ lparent)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= (int64_t)n - 1) return;
+    const int64_t nn = n;
+    int d = (kdelta(codes, nn, i, i + 1) - kdelta(codes, nn, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = kdelta(codes, nn, i, i - d);
+    int64_t lmax = 2;
+    while(kdelta(codes, nn, i, i + lmax * d) > dmin) lmax *= 2;
+    int64_t l = 0;
+    for(int64_t t = lmax / 2; t >= 1; t /= 2)
+        if(kdelta(codes, nn, i, i + (l + t) * d) > dmin) l += t;
+    int64_t j = i + l * d;
+    int dnode = kdelta(codes, nn, i, j);
+    int64_t s = 0, t = l;
+    do
+    {
+        t = (t + 1) / 2;
+        if(kdelta(codes, nn, i, i + (s + t) * d) > dnode) s += t;
+    } while(t > 1);
+    int64_t gamma = i + s * d + (d < 0 ? -1 : 0);
+    int64_t lo = i < j ? i : j, hi = i < j ? j : i;
+    uint32_t lc = (lo == gamma) ? (LEAF_BIT | (uint32_t)gamma) : (uint32_t)gamma;
+    uint32_t rc = (hi == gamma + 1) ? (LEAF_BIT | (uint32_t)(gamma + 1)) : (uint32_t)(gamma + 1);
+    left[i] = lc;
+    right[i] = rc;
+    first[i] = (uint32_t)lo;
+    last[i] = (uint32_t)hi;
+    if(lc & LEAF_BIT) lparent[lc & ~LEAF_BIT] = (uint32_t)i;
+    else iparent[lc] = (uint32_t)i;
+    if(rc & LEAF_BIT) lparent[rc & ~LEAF_BIT] = (uint32_t)i;
+    else iparent[rc] = (uint32_t)i;
+}
+
+__global__ void k_gather_leaf_boxes(const box6 *__restrict__ tbox, const uint32_t *__restrict__ sorted, uint32_t n,
+                                    box6 *__restrict__ lbox)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i < n) lbox[i] = tbox[sorted[i]];
+}
+
+__device__ __forceinline__ box6 load_box_cg(const box6 *p)
+{
+    const float *f = reinterpret_cast<const float *>(p);
+    box6 b;
+    for(int a = 0; a < 3; ++a)
+    {
+        b.lo[a] = __ldcg(f + a);
+        b.hi[a] = __ldcg(f + 3 + a);
+    }
+    return b;
+}
+
+__global__ void k_refit(const uint32_t *__restrict__ lparent, const uint32_t *__restrict__ iparent,
+                        const uint32_t *__restrict__ left, const uint32_t *__restrict__ right, const box6 *lbox,
+                        box6 *ibox, uint32_t *visits, uint32_t n)
+{
+    uint32_t leaf = blockIdx.x * blockDim.x + threadIdx.x;
+    if(leaf >= n || n < 2) return;
+    uint32_t p = lparent[leaf];
+    // bounded: a path to the root has at most n - 1 internal nodes
+    for(uint32_t guard = 0; guard < n; ++guard)
+    {
+        __threadfence();
+        if(atomicAdd(&visits[p], 1u) == 0u) return; // first arrival: the sibling finishes p
+        __threadfence();                            // acquire: the sibling's box is visible now
+        uint32_t l = left[p], r = right[p];
+        box6 a = (l & LEAF_BIT) ? load_box_cg(&lbox[l & ~LEAF_BIT]) : load_box_cg(&ibox[l]);
+        box6 b = (r & LEAF_BIT) ? load_box_cg(&lbox[r & ~LEAF_BIT]) : load_box_cg(&ibox[r]);
+        box6 u;
+        for(int k = 0; k < 3; ++k)
+        {
+            u.lo[k] = fminf(a.lo[k], b.lo[k]);
+            u.hi[k] = fmaxf(a.hi[k], b.hi[k]);
+        }
+        float *dst = reinterpret_cast<float *>(&ibox[p]);
+        for(int k = 0; k < 3; ++k)
+        {
+            __stcg(dst + k, u.lo[k]);
+            __stcg(dst + 3 + k, u.hi[k]);
+        }
+        if(p == 0) return;
+        p = iparent[p];
+    }
+}
+
+// ---- breadth-first collapse to 8-wide nodes (one CTA, deterministic numbering) ----------------
+struct collapse_args
+{
+    const uint32_t *left, *right, *first, *last;
+    const box6 *ibox, *lbox;
+    uint32_t n, leaf_max, capacity;
+    const uint32_t *scene_enc;
+    uint32_t *node_ref; // [capacity] BVH2 reference of each 8-wide node
+    node8 *nodes;       // [capacity]
+    uint32_t *out_info; // [0] num_nodes, [1] depth, [2] error flags
+    float *out_margin;
+};
+
+__device__ __forceinline__ uint32_t ref_count(const collapse_args &A, uint32_t r)
+{
+    return (r & LEAF_BIT) ? 1u : (A.last[r] - A.first[r] + 1u);
+}
+__device__ __forceinline__ uint32_t ref_first(const collapse_args &A, uint32_t r)
+{
+    return (r & LEAF_BIT) ? (r & ~LEAF_BIT) : A.first[r];
+}
+__device__ __forceinline__ box6 ref_box(const collapse_args &A, uint32_t r)
+{
+    return (r & LEAF_BIT) ? A.lbox[r & ~LEAF_BIT] : A.ibox[r];
+}
+__device__ __forceinline__ float box_area(const box6 &b)
+{
+    float dx = fsub(b.hi[0], b.lo[0]), dy = fsub(b.hi[1], b.lo[1]), dz = fsub(b.hi[2], b.lo[2]);
+    return fadd(fadd(fmul(dx, dy), fmul(dy, dz)), fmul(dz, dx));
+}
+
+constexpr int COLLAPSE_THREADS = 1024;
+
+__global__ void __launch_bounds__(COLLAPSE_THREADS) k_collapse(collapse_args A)
+{
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_level_end, s_next, s_err;
+    __shared__ float s_margin;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    if(tid == 0)
+    {
+        float lo[3], hi[3];
+        scene_box(A.scene_enc, lo, hi);
+        float ext = 0.f, amax = 0.f;
+        for(int a = 0; a < 3; ++a)
+        {
+            ext = fmaxf(ext, fsub(hi[a], lo[a]));
+            amax = fmaxf(amax, fmaxf(fabsf(lo[a]), fabsf(hi[a])));
+        }
+        s_margin = fmul(fmaxf(ext, amax), 3.0517578125e-05f); // 2^-15
+        *A.out_margin = s_margin;
+        A.node_ref[0] = (A.n == 1) ? (LEAF_BIT | 0u) : 0u;
+        s_next = 1;
+        s_err = 0;
+    }
+    __syncthreads();
+    const float m = s_margin;
+    uint32_t begin = 0, end = 1, depth = 0;
+    while(begin < end)
+    {
+        ++depth;
+        if(tid == 0) s_level_end = end;
+        __syncthreads();
+        for(uint32_t cbase = begin; cbase < end; cbase += COLLAPSE_THREADS)
+        {
+            uint32_t ni = cbase + tid;
+            bool active = ni < end;
+            uint32_t slots[8];
+            uint32_t ns = 0, nint = 0;
+            if(active)
+            {
+                uint32_t r = A.node_ref[ni];
+                if((r & LEAF_BIT) || ref_count(A, r) <= 1u) { slots[ns++] = r; }
+                else
+                {
+                    slots[ns++] = A.left[r];
+                    slots[ns++] = A.right[r];
+                    while(ns < 8)
+                    {
+                        int best = -1;
+                        float best_area = -1.f;
+                        for(uint32_t k = 0; k < ns; ++k)
+                        {
+                            uint32_t s = slots[k];
+                            if((s & LEAF_BIT) || ref_count(A, s) <= A.leaf_max) continue;
+                            float a = box_area(A.ibox[s]);
+                            if(a > best_area)
+                            {
+                                best_area = a;
+                                best = (int)k;
+                            }
+                        }
+                        if(best < 0) break;
+                        uint32_t s = slots[best];
+                        slots[best] = A.left[s];
+                        slots[ns++] = A.right[s];
+                    }
+                }
+                for(uint32_t k = 0; k < ns; ++k) nint += ref_count(A, slots[k]) > A.leaf_max ? 1u : 0u;
+            }
+            // block exclusive scan of nint
+            uint32_t x = nint;
+            for(int o = 1; o < 32; o <<= 1)
+            {
+                uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if(lane >= (uint32_t)o) x += y;
+            }
+            if(lane == 31) s_warp[warp] = x;
+            __syncthreads();
+            if(warp == 0)
+            {
+                uint32_t w = s_warp[lane];
+                for(int o = 1; o < 32; o <<= 1)
+                {
+                    uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                    if(lane >= (uint32_t)o) w += y;
+                }
+                s_warp[lane] = w;
+            }
+            __syncthreads();
+            uint32_t prefix = (warp ? s_warp[warp - 1] : 0u) + x - nint;
+            uint32_t chunk_total = s_warp[31];
+            uint32_t child_base = s_next + prefix;
+            if(active)
+            {
+                node8 nd;
+                nd.nchild = (uint8_t)ns;
+                box6 gb[8];
+                box6 nb;
+                for(int a = 0; a < 3; ++a)
+                {
+                    nb.lo[a] = __int_as_float(0x7f800000);
+                    nb.hi[a] = __int_as_float(0xff800000);
+                }
+                for(uint32_t k = 0; k < 8; ++k)
+                {
+                    if(k >= ns) break;
+                    box6 b = ref_box(A, slots[k]);
+                    for(int a = 0; a < 3; ++a)
+                    {
+                        gb[k].lo[a] = fsub(b.lo[a], m);
+                        gb[k].hi[a] = fadd(b.hi[a], m);
+                        nb.lo[a] = fminf(nb.lo[a], gb[k].lo[a]);
+                        nb.hi[a] = fmaxf(nb.hi[a], gb[k].hi[a]);
+                    }
+                }
+                for(int a = 0; a < 3; ++a)
+                {
+                    float range = fsub(nb.hi[a], nb.lo[a]);
+                    float xq = fdiv(range, 255.0f);
+                    uint32_t e = ((__float_as_uint(xq) >> 23) & 0xFFu) + 1u;
+                    if(e > 254u) e = 254u;
+                    nd.origin[a] = nb.lo[a];
+                    nd.exps[a] = (uint8_t)e;
+                    float inv_s = exp_scale(254u - e);
+                    for(uint32_t k = 0; k < 8; ++k)
+                    {
+                        uint8_t ql = 0, qh = 0;
+                        if(k < ns)
+                        {
+                            float fl = floorf(fmul(fsub(gb[k].lo[a], nb.lo[a]), inv_s));
+                            float fh = ceilf(fmul(fsub(gb[k].hi[a], nb.lo[a]), inv_s));
+                            ql = (uint8_t)(fl < 0.f ? 0.f : (fl > 255.f ? 255.f : fl));
+                            qh = (uint8_t)(fh < 0.f ? 0.f : (fh > 255.f ? 255.f : fh));
+                        }
+                        nd.qlo[a][k] = ql;
+                        nd.qhi[a][k] = qh;
+                    }
+                }
+                uint32_t c = child_base;
+                for(uint32_t k = 0; k < 8; ++k)
+                {
+                    uint32_t word = 0u;
+                    if(k < ns)
+                    {
+                        uint32_t s = slots[k];
+                        uint32_t cnt = ref_count(A, s);
+                        if(cnt <= A.leaf_max) { word = LEAF_BIT | ((cnt - 1u) << 27) | ref_first(A, s); }
+                        else
+                        {
+                            if(c < A.capacity) A.node_ref[c] = s;
+                            else atomicOr(&s_err, BUILD_ERR_CAPACITY);
+                            word = c++;
+                        }
+                    }
+                    nd.child[k] = word;
+                }
+                A.nodes[ni] = nd;
+            }
+            __syncthreads();
+            if(tid == 0) s_next += chunk_total;
+            __syncthreads();
+        }
+        __threadfence_block();
+        __syncthreads();
+        begin = end;
+        end = s_next;
+        if(s_err) break;
+        __syncthreads();
+    }
+    if(tid == 0)
+    {
+        A.out_info[0] = s_next;
+        A.out_info[1] = depth;
+        A.out_info[2] = s_err;
+    }
+}
+
+__global__ void k_tri_records(const float *__restrict__ xyz, uint32_t nv, const uint32_t *__restrict__ idx,
+                              const uint32_t *__restrict__ sorted, uint32_t n, tri_rec *__restrict__ out)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n) return;
+    uint32_t p = sorted[i];
+    float v[3][3];
+    for(int k = 0; k < 3; ++k)
+    {
+        uint32_t vi = idx[3 * (size_t)p + k];
+        if(vi >= nv) vi = 0;
+        for(int a = 0; a < 3; ++a) v[k][a] = xyz[3 * (size_t)vi + a];
+    }
+    tri_rec r;
+    for(int a = 0; a < 3; ++a)
+    {
+        r.v[a] = v[0][a];
+        r.v[3 + a] = fsub(v[1][a], v[0][a]);
+        r.v[6 + a] = fsub(v[2][a], v[0][a]);
+    }
+    r.prim = p;
+    r.pad[0] = r.pad[1] = 0u;
+    out[i] = r;
+}
+
+template<typename T>
+cudaError_t dalloc(T **p, size_t count, cudaStream_t s)
+{
+    return cudaMallocAsync(reinterpret_cast<void **>(p), count * sizeof(T) + 16, s);
+}
+
+}// namespace
+}// namespace vkg
+
+using namespace vkg;
+
+extern "C" vkg_status vkg_bvh_build(vkg_ctx *ctx, const float *d_xyz, uint32_t num_vertices,
+                                    const uint32_t *d_indices, uint32_t num_tris, const vkg_bvh_build_options *opts,
+                                    vkg_bvh **out, void *stream_)
+{
+    if(!ctx) return VKG_ERR_INVALID_ARGUMENT;
+    if(!out) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_bvh_build: out is NULL");
+    *out = nullptr;
+    if(num_tris > 0 && (!d_xyz || !d_indices || num_vertices == 0))
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_bvh_build: NULL geometry for %u triangles", num_tris);
+    if(num_tris >= MAX_TRIS)
+        return set_error(ctx, VKG_ERR_CAPACITY, "vkg_bvh_build: %u triangles exceed the maximum of %u", num_tris,
+                         MAX_TRIS - 1);
+    uint32_t leaf_max = (opts && opts->leaf_max) ? opts->leaf_max : 4u;
+    if(leaf_max > LEAF_MAX_LIMIT)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_bvh_build: leaf_max %u > %u", leaf_max, LEAF_MAX_LIMIT);
+    if(vkg_status s = bind_device(ctx); s != VKG_OK) return s;
+
+    cudaStream_t st = static_cast<cudaStream_t>(stream_);
+    auto *bvh = new vkg_bvh();
+    bvh->num_tris = num_tris;
+    bvh->leaf_max = leaf_max;
+    if(num_tris == 0)
+    {
+        *out = bvh;
+        return VKG_OK;
+    }
+    const uint32_t n = num_tris;
+    cudaEvent_t ev0, ev1;
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    cudaEventRecord(ev0, st);
+
+    // scratch
+    box6 *tbox = nullptr, *lbox = nullptr, *ibox = nullptr;
+    uint32_t *keys0 = nullptr, *keys1 = nullptr, *vals0 = nullptr, *vals1 = nullptr, *counts = nullptr;
+    uint32_t *left = nullptr, *right = nullptr, *first = nullptr, *last = nullptr, *iparent = nullptr,
+             *lparent = nullptr, *visits = nullptr, *node_ref = nullptr, *small = nullptr;
+    node8 *nodes_tmp = nullptr;
+    float *d_margin = nullptr;
+    const uint32_t nblocks = (n + SORT_TILE - 1) / SORT_TILE;
+    const uint32_t ni = n > 1 ? n - 1 : 1;
+    const uint32_t capacity = n + 8;
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) {
+        if(e == cudaSuccess) e = x;
+    };
+    chk(dalloc(&tbox, n, st));
+    chk(dalloc(&lbox, n, st));
+    chk(dalloc(&ibox, ni, st));
+    chk(dalloc(&keys0, n, st));
+    chk(dalloc(&keys1, n, st));
+    chk(dalloc(&vals0, n, st));
+    chk(dalloc(&vals1, n, st));
+    chk(dalloc(&counts, (size_t)256 * nblocks, st));
+    chk(dalloc(&left, ni, st));
+    chk(dalloc(&right, ni, st));
+    chk(dalloc(&first, ni, st));
+    chk(dalloc(&last, ni, st));
+    chk(dalloc(&iparent, ni, st));
+    chk(dalloc(&lparent, n, st));
+    chk(dalloc(&visits, ni, st));
+    chk(dalloc(&node_ref, capacity, st));
+    chk(dalloc(&nodes_tmp, capacity, st));
+    chk(dalloc(&small, 16, st));
+    chk(dalloc(&d_margin, 1, st));
+    chk(dalloc(&bvh->d_morton, n, st));
+    chk(dalloc(&bvh->d_sorted, n, st));
+    chk(dalloc(&bvh->d_tris, n, st));
+    if(e != cudaSuccess)
+    {
+        vkg_bvh_destroy(ctx, bvh);
+        return set_error(ctx, VKG_ERR_OUT_OF_MEMORY, "vkg_bvh_build: device allocation failed (%s)",
+                         cudaGetErrorString(e));
+    }
+    // small[0..5] scene box (ordered uints), [6] error flags, [8..10] collapse info
+    uint32_t init[16] = {0xFF800000u, 0xFF800000u, 0xFF800000u, 0x007FFFFFu, 0x007FFFFFu, 0x007FFFFFu, 0, 0,
+                         0,           0,           0,           0,           0,           0,           0, 0};
+    // +inf encodes as 0xFF800000, -inf as 0x007FFFFF
+    chk(cudaMemcpyAsync(small, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    chk(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * ni, st));
+
+    const int T = 256;
+    const uint32_t g = (n + T - 1) / T;
+    k_tri_boxes<<<g, T, 0, st>>>(d_xyz, num_vertices, d_indices, n, tbox, small, small + 6);
+    k_morton<<<g, T, 0, st>>>(tbox, n, small, keys0, vals0, bvh->d_morton);
+    uint32_t *kin = keys0, *kout = keys1, *vin = vals0, *vout = vals1;
+    for(int shift = 0; shift < 30; shift += 8)
+    {
+        k_radix_hist<<<nblocks, SORT_THREADS, 0, st>>>(kin, n, shift, counts, nblocks);
+        k_scan_exclusive<<<1, 1024, 0, st>>>(counts, 256u * nblocks, nullptr);
+        k_radix_scatter<<<nblocks, SORT_THREADS, 0, st>>>(kin, vin, n, shift, counts, nblocks, kout, vout);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    chk(cudaMemcpyAsync(bvh->d_sorted, vin, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st));
+    k_gather_leaf_boxes<<<g, T, 0, st>>>(tbox, vin, n, lbox);
+    if(n > 1)
+    {
+        k_karras<<<(ni + T - 1) / T, T, 0, st>>>(kin, n, left, right, first, last, iparent, lparent);
+        k_refit<<<g, T, 0, st>>>(lparent, iparent, left, right, lbox, ibox, visits, n);
+    }
+    collapse_args A{left, right, first, last, ibox, lbox, n, leaf_max, capacity, small, node_ref, nodes_tmp,
+                    small + 8, d_margin};
+    k_collapse<<<1, COLLAPSE_THREADS, 0, st>>>(A);
+    k_tri_records<<<g, T, 0, st>>>(d_xyz, num_vertices, d_indices, vin, n, bvh->d_tris);
+    chk(cudaGetLastError());
+
+    uint32_t info[16];
+    float margin = 0.f;
+    chk(cudaMemcpyAsync(info, small, sizeof(info), cudaMemcpyDeviceToHost, st));
+    chk(cudaMemcpyAsync(&margin, d_margin, sizeof(float), cudaMemcpyDeviceToHost, st));
+    chk(cudaStreamSynchronize(st));
+    if(e == cudaSuccess)
+    {
+        bvh->num_nodes = info[8];
+        bvh->depth = info[9];
+        bvh->margin = margin;
+        for(int a = 0; a < 3; ++a)
+        {
+            uint32_t lo = info[a], hi = info[3 + a];
+            uint32_t lb = (lo & 0x80000000u) ? (lo & 0x7FFFFFFFu) : ~lo;
+            uint32_t hb = (hi & 0x80000000u) ? (hi & 0x7FFFFFFFu) : ~hi;
+            std::memcpy(&bvh->scene_min[a], &lb, 4);
+            std::memcpy(&bvh->scene_max[a], &hb, 4);
+        }
+        chk(dalloc(&bvh->d_nodes, bvh->num_nodes, st));
+        if(e == cudaSuccess)
+            chk(cudaMemcpyAsync(bvh->d_nodes, nodes_tmp, sizeof(node8) * bvh->num_nodes, cudaMemcpyDeviceToDevice,
+                                st));
+    }
+    for(void *p: {(void *)tbox, (void *)lbox, (void *)ibox, (void *)keys0, (void *)keys1, (void *)vals0,
+                  (void *)vals1, (void *)counts, (void *)left, (void *)right, (void *)first, (void *)last,
+                  (void *)iparent, (void *)lparent, (void *)visits, (void *)node_ref, (void *)nodes_tmp,
+                  (void *)small, (void *)d_margin})
+        cudaFreeAsync(p, st);
+    cudaEventRecord(ev1, st);
+    chk(cudaEventSynchronize(ev1));
+    cudaEventElapsedTime(&bvh->build_ms, ev0, ev1);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    if(e != cudaSuccess)
+    {
+        vkg_bvh_destroy(ctx, bvh);
+        return cuda_check(ctx, e, "vkg_bvh_build");
+    }
+    if(info[6] & BUILD_ERR_INDEX)
+    {
+        vkg_bvh_destroy(ctx, bvh);
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_bvh_build: triangle index >= num_vertices (%u)",
+                         num_vertices);
+    }
+    if(info[10] & BUILD_ERR_CAPACITY)
+    {
+        vkg_bvh_destroy(ctx, bvh);
+        return set_error(ctx, VKG_ERR_CAPACITY, "vkg_bvh_build: node capacity exceeded");
+    }
+    const uint32_t max_depth = (TRAVERSAL_STACK - 1) / 7 + 1;
+    if(bvh->depth > max_depth)
+    {
+        uint32_t d = bvh->depth;
+        vkg_bvh_destroy(ctx, bvh);
+        return set_error(ctx, VKG_ERR_CAPACITY, "vkg_bvh_build: BVH depth %u exceeds the traversal limit %u", d,
+                         max_depth);
+    }
+    bvh->bytes = sizeof(node8) * bvh->num_nodes + sizeof(tri_rec) * n + 8 * (size_t)n;
+    *out = bvh;
+    return VKG_OK;
+}
+
+extern "C" vkg_status vkg_bvh_info_get(const vkg_bvh *bvh, vkg_bvh_info *out)
+{
+    if(!bvh || !out) return VKG_ERR_INVALID_ARGUMENT;
+    std::memset(out, 0, sizeof(*out));
+    out->num_tris = bvh->num_tris;
+    out->num_nodes = bvh->num_nodes;
+    out->depth = bvh->depth;
+    out->leaf_max = bvh->leaf_max;
+    for(int a = 0; a < 3; ++a)
+    {
+        out->scene_min[a] = bvh->scene_min[a];
+        out->scene_max[a] = bvh->scene_max[a];
+    }
+    out->margin = bvh->margin;
+    out->bytes = bvh->bytes;
+    out->d_nodes = bvh->d_nodes;
+    out->d_tris = bvh->d_tris;
+    out->d_morton = bvh->d_morton;
+    out->d_sorted = bvh->d_sorted;
+    out->build_ms = bvh->build_ms;
+    return VKG_OK;
+}
+
+extern "C" vkg_status vkg_bvh_destroy(vkg_ctx *ctx, vkg_bvh *bvh)
+{
+    if(!bvh) return VKG_OK;
+    if(ctx) bind_device(ctx);
+    cudaFree(bvh->d_nodes);
+    cudaFree(bvh->d_tris);
+    cudaFree(bvh->d_morton);
+    cudaFree(bvh->d_sorted);
+    delete bvh;
+    return VKG_OK;
+}

@@ -1,0 +1,56 @@
+// Internal host-side state shared by the libvkg translation units (not part of the C ABI).
+#pragma once
+
+#include "../../include/vkg.h"
+#include "vkg_common.cuh"
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+struct vkg_ctx
+{
+    int device = 0;
+    int num_sms = 0;
+    std::string last_error;
+    // device counters: [0] node visits, [1] triangle tests, [2] error flags (bit0 stack overflow)
+    unsigned long long *d_counters = nullptr;
+    // host-variant staging (grown on demand)
+    void *d_stage_rays = nullptr;
+    void *d_stage_hits = nullptr;
+    size_t stage_rays_bytes = 0, stage_hits_bytes = 0;
+};
+
+struct vkg_bvh
+{
+    uint32_t num_tris = 0, num_nodes = 0, depth = 0, leaf_max = 4;
+    float scene_min[3] = {0, 0, 0}, scene_max[3] = {0, 0, 0}, margin = 0.f;
+    vkg::node8 *d_nodes = nullptr;
+    vkg::tri_rec *d_tris = nullptr;
+    uint32_t *d_morton = nullptr; // input order
+    uint32_t *d_sorted = nullptr; // sorted order -> triangle id
+    size_t bytes = 0;
+    float build_ms = 0.f;
+};
+
+namespace vkg
+{
+// record an error message on ctx and return `status`
+vkg_status set_error(vkg_ctx *ctx, vkg_status status, const char *fmt, ...);
+// map a CUDA error to VKG_ERR_CUDA with location info; VKG_OK if err == cudaSuccess
+vkg_status cuda_check(vkg_ctx *ctx, cudaError_t err, const char *what);
+// ensure the context's device is current on this thread
+vkg_status bind_device(vkg_ctx *ctx);
+
+// traversal stack capacity (entries) of the traversal kernels; the build rejects deeper BVHs
+constexpr uint32_t TRAVERSAL_STACK = 128;
+}// namespace vkg
+
+#define VKG_TRY_CUDA(ctx, expr)                                                                                      \
+    do                                                                                                               \
+    {                                                                                                                \
+        vkg_status s_ = vkg::cuda_check((ctx), (expr), #expr);                                                       \
+        if(s_ != VKG_OK) return s_;                                                                                  \
+    } while(0)

@@ -1,0 +1,135 @@
+"""GPU ray queries through libvkg's C ABI: context, BVH build, closest-hit / any-hit, camera rays.
+
+Device buffers are torch tensors (torch provides device memory and the current CUDA stream; all
+work runs in libvkg's own kernels). Ray batches are float32 tensors of shape [N, 8]
+({origin.xyz, tmin, direction.xyz, tmax}, 32 B per ray); hits are int32 tensors [N, 4]
+({prim, t, u, v} with t/u/v as float bits, 16 B per hit; prim == -1 (0xFFFFFFFF) on a miss).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from ._lib import (RAY_COUNT_STATS, RAY_CULL_BACK_FACES, check, lib, vkg_bvh_build_options, vkg_bvh_info,
+                   vkg_camera)
+
+__all__ = ["Context", "BVH", "hits_view", "RAY_CULL_BACK_FACES", "RAY_COUNT_STATS"]
+
+
+def _stream_ptr(device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+class Context:
+    """One libvkg context per host thread and device (vkg_ctx_create / vkg_ctx_destroy)."""
+
+    def __init__(self, device: int = 0):
+        if not torch.cuda.is_available():
+            raise RuntimeError("vierkant_gb300.Context needs a CUDA device")
+        self.device = device
+        torch.cuda.init()
+        h = C.c_void_p()
+        check(lib().vkg_ctx_create(device, C.byref(h)), None, "vkg_ctx_create")
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().vkg_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- helpers -------------------------------------------------------------------------
+    def _check(self, status, what):
+        check(status, self.handle, what)
+
+    def stream(self) -> int:
+        return _stream_ptr(self.device)
+
+    def camera_rays(self, cam: vkg_camera, seed: int, stream_id: int, spp: int = 1, out: torch.Tensor | None = None):
+        n = cam.width * cam.height * spp
+        if out is None:
+            out = torch.empty((n, 8), dtype=torch.float32, device=f"cuda:{self.device}")
+        self._check(lib().vkg_camera_rays(self.handle, C.byref(cam), seed, stream_id, spp,
+                                          C.c_void_p(out.data_ptr()), C.c_void_p(self.stream())), "vkg_camera_rays")
+        return out
+
+    def stats(self, reset: bool = True):
+        v, t = C.c_uint64(), C.c_uint64()
+        self._check(lib().vkg_ray_stats_get(self.handle, C.byref(v), C.byref(t), int(reset)), "vkg_ray_stats_get")
+        return int(v.value), int(t.value)
+
+
+class BVH:
+    """8-wide quantised BVH built on the GPU from fp32 xyz vertices and uint32 triangle indices."""
+
+    def __init__(self, ctx: Context, xyz: torch.Tensor, indices: torch.Tensor, leaf_max: int = 4):
+        self.ctx = ctx
+        dev = f"cuda:{ctx.device}"
+        xyz = xyz.to(device=dev, dtype=torch.float32).contiguous()
+        idx = indices.to(device=dev).contiguous()
+        if idx.dtype != torch.int32:
+            idx = idx.to(torch.int64).to(torch.int32)
+        self._xyz, self._idx = xyz, idx  # keep alive for the build
+        opts = vkg_bvh_build_options(leaf_max)
+        h = C.c_void_p()
+        ctx._check(lib().vkg_bvh_build(ctx.handle, C.c_void_p(xyz.data_ptr()), xyz.numel() // 3,
+                                       C.c_void_p(idx.data_ptr()), idx.numel() // 3, C.byref(opts), C.byref(h),
+                                       C.c_void_p(ctx.stream())), "vkg_bvh_build")
+        self.handle = h
+
+    def info(self) -> vkg_bvh_info:
+        inf = vkg_bvh_info()
+        check(lib().vkg_bvh_info_get(self.handle, C.byref(inf)))
+        return inf
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().vkg_bvh_destroy(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def closest_hit(self, rays: torch.Tensor, out: torch.Tensor | None = None, flags: int = 0) -> torch.Tensor:
+        n = rays.shape[0]
+        if out is None:
+            out = torch.empty((n, 4), dtype=torch.int32, device=rays.device)
+        self.ctx._check(lib().vkg_closest_hit(self.ctx.handle, self.handle, C.c_void_p(rays.data_ptr()), n,
+                                              C.c_void_p(out.data_ptr()), flags, C.c_void_p(self.ctx.stream())),
+                        "vkg_closest_hit")
+        return out
+
+    def any_hit(self, rays: torch.Tensor, out: torch.Tensor | None = None, flags: int = 0) -> torch.Tensor:
+        n = rays.shape[0]
+        if out is None:
+            out = torch.empty((n,), dtype=torch.int32, device=rays.device)
+        self.ctx._check(lib().vkg_any_hit(self.ctx.handle, self.handle, C.c_void_p(rays.data_ptr()), n,
+                                          C.c_void_p(out.data_ptr()), flags, C.c_void_p(self.ctx.stream())),
+                        "vkg_any_hit")
+        return out
+
+    def closest_hit_host(self, rays_host: torch.Tensor, hits_host: torch.Tensor, flags: int = 0) -> torch.Tensor:
+        """Host buffers in, host buffers out (H2D copy, trace, D2H copy, synchronise)."""
+        n = rays_host.shape[0]
+        self.ctx._check(lib().vkg_closest_hit_host(self.ctx.handle, self.handle, C.c_void_p(rays_host.data_ptr()), n,
+                                                   C.c_void_p(hits_host.data_ptr()), flags,
+                                                   C.c_void_p(self.ctx.stream())), "vkg_closest_hit_host")
+        return hits_host
+
+
+def hits_view(hits):
+    """Split a [N,4] int32 hit tensor / array into (prim uint32, t, u, v float32) numpy arrays."""
+    import numpy as np
+    h = hits.cpu().numpy() if isinstance(hits, torch.Tensor) else np.asarray(hits)
+    h = np.ascontiguousarray(h).view(np.uint32).reshape(-1, 4)
+    return h[:, 0].copy(), h[:, 1].view(np.float32).copy(), h[:, 2].view(np.float32).copy(), \
+        h[:, 3].view(np.float32).copy()
