@@ -1,0 +1,349 @@
+"""Benchmark: closest-hit ray casting over the 196,618-triangle Cornell + 64-sphere scene.
+
+Workload (one step = one vkg_closest_hit launch over one resident batch):
+  scene   : 5-quad Cornell box + 64 cube-spheres of 3,072 triangles (PCG32 seed 0x5EED, stream 2),
+            fp32 xyz / uint32 indices, 8-wide BVH built on the GPU
+  batch   : 1280x720 pixels x 4 spp camera rays (fovy 45 deg, eye (0,0,3.4) -> origin, PCG32 jitter,
+            stream 2 + rank) plus one bounce ray per primary hit, leaving the hit point in a uniformly
+            random direction (seeded torch RNG): coherent and incoherent rays in one batch
+  metric  : Mrays/s closest-hit (hit ids bit-exact to brute force over the reference's ray-triangle
+            test; the GPU tests check this on the same scene)
+Inputs exceed L2 (rays + hits ~ 290 MB per step), so no explicit flush is needed between steps.
+
+--impl reference: the reference's CPU ray cast (brute-force closest hit over all triangles with
+vierkant's ray-triangle test, all host threads) on a bounded sample of the same batch.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WIDTH, HEIGHT, SPP = 1280, 720, 4
+SEED = 0x5EED
+NODE_BYTES, TRI_BYTES, RAY_BYTES, HIT_BYTES = 96, 48, 32, 16
+METRIC = "Mrays/s closest-hit"
+WORKLOAD = ("closest-hit, Cornell box + 64 cube-spheres (196,618 triangles), 1280x720x4 spp camera rays "
+            "+ one uniform bounce ray per primary hit")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic_per_ray():
+    """DRAM bytes per ray of the traversal kernel from the committed ncu capture summary, if any."""
+    p = ROOT / "profiles" / "traversal_dram_bytes.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["dram_bytes_per_ray"])
+        except (KeyError, ValueError):
+            return None
+    return None
+
+
+def make_batch(ctx, bvh, rank):
+    """camera rays + bounce rays from their hit points (built on the GPU, untimed)."""
+    import torch
+    from vierkant_gb300 import geometry
+    cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, WIDTH, HEIGHT)
+    prim = ctx.camera_rays(cam, SEED, 2 + rank, SPP)
+    hits = bvh.closest_hit(prim)
+    hit = hits[:, 0] != -1
+    t = hits[:, 1].view(torch.float32)
+    pos = prim[:, 0:3] + prim[:, 4:7] * t[:, None]
+    g = torch.Generator(device=prim.device)
+    g.manual_seed(SEED + rank)
+    d = torch.randn((prim.shape[0], 3), device=prim.device, generator=g)
+    d = d / d.norm(dim=1, keepdim=True)
+    n2 = int(hit.sum())
+    sec = torch.empty((n2, 8), device=prim.device, dtype=torch.float32)
+    sec[:, 0:3] = pos[hit]
+    sec[:, 3] = 1e-4
+    sec[:, 4:7] = d[hit]
+    sec[:, 7] = 1e4
+    batch = torch.cat([prim, sec]).contiguous()
+    del hits, pos, d, sec
+    return batch
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    from vierkant_gb300 import geometry
+    from vierkant_gb300._lib import RAY_COUNT_STATS
+    from vierkant_gb300.raytracing import BVH, Context
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    ctx = Context(local)
+    sc = geometry.cornell_scene(SEED, 2, 64, 16)
+    bvh = BVH(ctx, torch.from_numpy(sc["xyz"]).cuda(), torch.from_numpy(sc["indices"].astype(np.int32)).cuda())
+    info = bvh.info()
+    batch = make_batch(ctx, bvh, rank)
+    n = batch.shape[0]
+    hits = torch.empty((n, 4), dtype=torch.int32, device=batch.device)
+
+    # algorithmic work per ray, counted by the traversal itself (untimed; the GPU tests check these
+    # counters against the CPU traversal of the same BVH)
+    ctx.stats(reset=True)
+    bvh.closest_hit(batch, hits, flags=RAY_COUNT_STATS)
+    visits, tests = ctx.stats(reset=True)
+    bytes_per_launch = n * (RAY_BYTES + HIT_BYTES) + visits * NODE_BYTES + tests * TRI_BYTES
+
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        bvh.closest_hit(batch, hits)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        bvh.closest_hit(batch, hits)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    ms_total = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    ms_step = ms_total / args.steps
+    if ws > 1:
+        t = torch.tensor([ms_step], device=batch.device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    rays_all = n * ws
+    value = rays_all / (ms_step * 1e-3) / 1e6
+
+    # end to end through the host-buffer entry point: H2D rays, trace, D2H hits, synchronise
+    rays_host = batch.cpu().pin_memory()
+    hits_host = torch.empty((n, 4), dtype=torch.int32).pin_memory()
+    for _ in range(max(1, args.warmup // 2)):
+        bvh.closest_hit_host(rays_host, hits_host)
+    if ws > 1:
+        dist.barrier()
+    e2e_steps = max(3, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        bvh.closest_hit_host(rays_host, hits_host)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    if ws > 1:
+        t = torch.tensor([e2e_ms], device=batch.device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = rays_all / (e2e_ms * 1e-3) / 1e6
+    # the host-buffer results must equal the device results
+    dev_hits = hits.cpu()
+    e2e_ok = bool(torch.equal(dev_hits, hits_host))
+
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_per_launch / (ms_step * 1e-3) / 1e9
+    tpr = profiled_traffic_per_ray()
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": (round(tpr * n) if tpr is not None else None),
+                "peak_source": peak_kind,
+                "algorithmic_bytes_per_ray": round(bytes_per_launch / n, 1),
+                "node_visits_per_ray": round(visits / n, 3), "tri_tests_per_ray": round(tests / n, 3),
+                "note": "node (96 B) + triangle (48 B) reads per ray are served mostly from L2/L1; "
+                        "HBM sees the 48 B/ray ray+hit stream"}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu = cpu_baseline(sc, batch, budget_s=args.cpu_seconds)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 1), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "triangles": int(info.num_tris), "rays_per_step": n,
+                           "bvh_nodes": int(info.num_nodes), "bvh_depth": int(info.depth),
+                           "bvh_build_ms": round(float(info.build_ms), 3), "leaf_max": int(info.leaf_max),
+                           "l2": "inputs larger than L2 (%.0f MB rays+hits per step)" % (n * 48 / 1e6),
+                           "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+                "e2e": {"value": round(e2e_value, 1), "unit": "Mrays/s", "h2d_bytes_per_step": n * RAY_BYTES,
+                        "d2h_bytes_per_step": n * HIT_BYTES, "matches_device": e2e_ok},
+                "gpu_launches": args.steps, "roofline": roofline, "clocks": clk}
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    bvh.close()
+    ctx.close()
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def cpu_reference_lib():
+    """The reference's own ray-triangle code when it was compiled here (oracle/_ref), else the
+    oracle's C port of it (bit-identical; checked by the tests)."""
+    import oracle
+    R = oracle.ref()
+    if R is not None:
+        return "reference", (lambda *a: R.vkref_closest_hit_bruteforce(*a))
+    L = oracle.orc()
+    return "port", (lambda *a: L.orc_closest_hit_bruteforce(*a))
+
+
+def cpu_baseline(sc, batch_gpu, budget_s=12.0, sample_rays=None):
+    """Time the reference's brute-force CPU ray cast over all host threads on a bounded, evenly
+    strided sample of the batch (keeps the primary/bounce mix)."""
+    import numpy as np
+    import oracle
+    kind, fn = cpu_reference_lib()
+    rays = batch_gpu.cpu().numpy() if hasattr(batch_gpu, "cpu") else batch_gpu
+    n = rays.shape[0]
+    xyz = np.ascontiguousarray(sc["xyz"])
+    idx = np.ascontiguousarray(sc["indices"])
+    cores = os.cpu_count() or 1
+    # calibrate on a small sample, then size the timed sample to the budget
+    probe = np.ascontiguousarray(rays[:: max(1, n // 256)][:256])
+    hits = np.zeros((len(probe), 4), np.uint32)
+    t0 = time.perf_counter()
+    fn(oracle.ptr(xyz), oracle.ptr(idx), idx.shape[0], oracle.ptr(probe), len(probe), oracle.ptr(hits), 0, 0)
+    dt = max(time.perf_counter() - t0, 1e-6)
+    m = sample_rays or int(max(256, min(n, len(probe) * budget_s / dt)))
+    sample = np.ascontiguousarray(rays[:: max(1, n // m)][:m])
+    hits = np.zeros((len(sample), 4), np.uint32)
+    t0 = time.perf_counter()
+    used = fn(oracle.ptr(xyz), oracle.ptr(idx), idx.shape[0], oracle.ptr(sample), len(sample), oracle.ptr(hits), 0,
+              0)
+    dt = time.perf_counter() - t0
+    return {"value": round(len(sample) / dt / 1e6, 5), "unit": "Mrays/s", "cores": int(used or cores),
+            "kind": kind,
+            "sample": f"{len(sample)} rays (every {max(1, n // m)}th of the batch) x {idx.shape[0]} triangles, "
+                      f"brute force, {dt:.1f} s"}
+
+
+def run_reference(args):
+    """Reference arm: the reference's CPU ray cast on the host cores (rank 0 only)."""
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+    import torch
+    from vierkant_gb300 import geometry
+    sc = geometry.cornell_scene(SEED, 2, 64, 16)
+    if torch.cuda.is_available():
+        from vierkant_gb300.raytracing import BVH, Context
+        ctx = Context(local)
+        bvh = BVH(ctx, torch.from_numpy(sc["xyz"]).cuda(), torch.from_numpy(sc["indices"].astype(np.int32)).cuda())
+        batch = make_batch(ctx, bvh, 0).cpu().numpy()
+        bvh.close()
+        ctx.close()
+    else:
+        raise SystemExit("the benchmark batch is generated on the GPU")
+    per_step_budget = max(1.0, min(20.0, args.cpu_seconds / max(1, args.steps)))
+    for _ in range(args.warmup):
+        cpu_baseline(sc, batch, budget_s=0.2)
+    results = [cpu_baseline(sc, batch, budget_s=per_step_budget) for _ in range(args.steps)]
+    value = statistics.median(r["value"] for r in results)
+    cb = dict(results[-1])
+    cb["value"] = value
+    line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "triangles": int(sc["indices"].shape[0])},
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("note: timing rules want >= 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()
