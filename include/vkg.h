@@ -190,6 +190,27 @@ typedef struct vkg_bvh_info
 vkg_status vkg_bvh_build(vkg_ctx *ctx, const float *d_xyz, uint32_t num_vertices, const uint32_t *d_indices,
                          uint32_t num_tris, const vkg_bvh_build_options *opts, vkg_bvh **out, void *stream);
 vkg_status vkg_bvh_info_get(const vkg_bvh *bvh, vkg_bvh_info *out);
+
+/* Allocation-free BVH build. No counterpart in the reference: it exists for callers that cannot
+ * allocate device memory once they are running -- for example an engine that carves all of its
+ * device memory out of one arena at start-up, or code that records work where an allocation would
+ * synchronise the device. It produces the same nodes and triangle records as vkg_bvh_build, but
+ * keeps every temporary in one fixed device array inside libvkg (about 2.2 MB, held by each GPU
+ * that loads the library until the process exits) and calls no allocator.
+ *   - at most VKG_NOALLOC_MAX_TRIS triangles; larger inputs return VKG_ERR_CAPACITY
+ *   - the caller provides d_nodes (node_capacity >= num_tris nodes of 96 B, 16-byte aligned),
+ *     d_tris (num_tris records of 48 B, 16-byte aligned) and d_info (16 uint32 words, device):
+ *     [0] node count, [1] depth, [2] error flags (1: an index >= num_vertices, 2: node capacity),
+ *     [3] box margin (float bits), [4..6] scene min, [7..9] scene max (float bits)
+ *   - works on the current CUDA device; its first call on a device looks up the array's device
+ *     address (cudaGetSymbolAddress), so make that first call before any stream capture
+ *   - all calls share the one array: calls that overlap on the GPU (other streams, other threads)
+ *     race and must be serialised by the caller
+ *   - asynchronous on `stream`; no vkg_ctx (no error message: the status code says what failed) */
+#define VKG_NOALLOC_MAX_TRIS 16384u
+vkg_status vkg_bvh_build_noalloc(const float *d_xyz, uint32_t num_vertices, const uint32_t *d_indices,
+                                 uint32_t num_tris, uint32_t leaf_max, void *d_nodes, uint32_t node_capacity,
+                                 void *d_tris, uint32_t *d_info, void *stream);
 vkg_status vkg_bvh_destroy(vkg_ctx *ctx, vkg_bvh *bvh);
 
 /* ---- bulk ray queries (replaces TraceRay / RayQuery, raypipeline.slang:182, visibility_test.slang:45-87)

@@ -92,6 +92,7 @@ SIGNATURES = {
     "vkg_bvh_build": (I32, [P, P, U32, P, U32, C.POINTER(vkg_bvh_build_options), C.POINTER(P), P]),
     "vkg_bvh_info_get": (I32, [P, C.POINTER(vkg_bvh_info)]),
     "vkg_bvh_destroy": (I32, [P, P]),
+    "vkg_bvh_build_noalloc": (I32, [P, U32, P, U32, U32, P, U32, P, P, P]),
     "vkg_closest_hit": (I32, [P, P, P, U32, P, U32, P]),
     "vkg_any_hit": (I32, [P, P, P, U32, P, U32, P]),
     "vkg_closest_hit_host": (I32, [P, P, P, U32, P, U32, P]),

@@ -16,7 +16,9 @@
 // with 16-byte vector loads by the traversal kernels.
 #include "internal.hpp"
 
+#include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 namespace vkg
@@ -775,4 +777,142 @@ extern "C" vkg_status vkg_bvh_destroy(vkg_ctx *ctx, vkg_bvh *bvh)
     cudaFree(bvh->d_sorted);
     delete bvh;
     return VKG_OK;
+}
+
+// ---- allocation-free build ----------------------------------------------------------------------
+// For callers that cannot allocate device memory after start-up (for example an engine that
+// sub-allocates everything from one arena it received at initialisation, or code recording work
+// that must not synchronise): the build's temporaries live in one file-scope device array of fixed
+// size, so the call itself performs no allocation. The caller passes the inputs and the output
+// buffers (nodes, triangle records, info words).
+namespace vkg
+{
+namespace
+{
+
+constexpr uint32_t NOALLOC_MAX_TRIS = 16384;
+constexpr uint32_t NOALLOC_SORT_BLOCKS = (NOALLOC_MAX_TRIS + SORT_TILE - 1) / SORT_TILE;
+
+struct noalloc_scratch
+{
+    box6 tbox[NOALLOC_MAX_TRIS], lbox[NOALLOC_MAX_TRIS], ibox[NOALLOC_MAX_TRIS];
+    uint32_t keys0[NOALLOC_MAX_TRIS], keys1[NOALLOC_MAX_TRIS], vals0[NOALLOC_MAX_TRIS], vals1[NOALLOC_MAX_TRIS];
+    uint32_t counts[256 * NOALLOC_SORT_BLOCKS];
+    uint32_t left[NOALLOC_MAX_TRIS], right[NOALLOC_MAX_TRIS], first[NOALLOC_MAX_TRIS], last[NOALLOC_MAX_TRIS];
+    uint32_t iparent[NOALLOC_MAX_TRIS], lparent[NOALLOC_MAX_TRIS], visits[NOALLOC_MAX_TRIS];
+    uint32_t node_ref[NOALLOC_MAX_TRIS + 8];
+    uint32_t morton[NOALLOC_MAX_TRIS];
+    uint32_t small[16];
+    float margin[4];
+};
+
+// ~2.2 MB, held by every GPU that loads libvkg until the process exits. Host code must not use the
+// symbol's host-side name as a device address: the address comes from cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(noalloc_scratch)];
+
+std::mutex g_noalloc_mutex;
+void *g_noalloc_ptr[128] = {};
+
+// per device, on first use, with that device current
+vkg_status noalloc_scratch_for_current_device(noalloc_scratch **out)
+{
+    int dev = -1;
+    if(cudaGetDevice(&dev) != cudaSuccess) return VKG_ERR_CUDA;
+    if(dev < 0 || dev >= 128) return VKG_ERR_NOT_SUPPORTED;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if(!g_noalloc_ptr[dev])
+    {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if(e != cudaSuccess || p == nullptr) return VKG_ERR_CUDA;
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = static_cast<noalloc_scratch *>(g_noalloc_ptr[dev]);
+    return VKG_OK;
+}
+
+// the scratch keeps the previous call's contents: reset what the build expects to start at zero
+__global__ void k_noalloc_reset(noalloc_scratch *s, uint32_t n)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i < n) s->visits[i] = 0u;
+    if(i < 16)
+    {
+        const uint32_t init = i < 3 ? 0xFF800000u : (i < 6 ? 0x007FFFFFu : 0u); // +inf / -inf encodings, flags
+        s->small[i] = init;
+    }
+    if(i == 0) s->margin[0] = 0.f;
+}
+
+// info words: [0] nodes, [1] depth, [2] error flags (1 = index >= num_vertices, 2 = node capacity),
+// [3] margin (float bits), [4..6] scene min, [7..9] scene max (float bits)
+__global__ void k_noalloc_info(const noalloc_scratch *s, uint32_t n, uint32_t *info)
+{
+    if(threadIdx.x != 0 || blockIdx.x != 0) return;
+    for(int k = 0; k < 16; ++k) info[k] = 0u;
+    if(n == 0) return;
+    info[0] = s->small[8];
+    info[1] = s->small[9];
+    info[2] = s->small[10] | s->small[6];
+    info[3] = __float_as_uint(s->margin[0]);
+    for(int a = 0; a < 3; ++a)
+    {
+        info[4 + a] = __float_as_uint(fdec(s->small[a]));
+        info[7 + a] = __float_as_uint(fdec(s->small[3 + a]));
+    }
+}
+
+}// namespace
+}// namespace vkg
+
+extern "C" vkg_status vkg_bvh_build_noalloc(const float *d_xyz, uint32_t num_vertices, const uint32_t *d_indices,
+                                            uint32_t num_tris, uint32_t leaf_max, void *d_nodes,
+                                            uint32_t node_capacity, void *d_tris, uint32_t *d_info, void *stream_)
+{
+    if(num_tris > NOALLOC_MAX_TRIS) return VKG_ERR_CAPACITY;
+    if(!d_info) return VKG_ERR_INVALID_ARGUMENT;
+    if(leaf_max == 0) leaf_max = 4u;
+    if(leaf_max > LEAF_MAX_LIMIT) return VKG_ERR_INVALID_ARGUMENT;
+    if(num_tris > 0 && (!d_xyz || !d_indices || num_vertices == 0 || !d_nodes || !d_tris)) return VKG_ERR_INVALID_ARGUMENT;
+    if(num_tris > 0 && node_capacity < num_tris) return VKG_ERR_INVALID_ARGUMENT;
+    if((reinterpret_cast<uintptr_t>(d_nodes) & 15u) || (reinterpret_cast<uintptr_t>(d_tris) & 15u))
+        return VKG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream_);
+    noalloc_scratch *s = nullptr;
+    if(vkg_status r = noalloc_scratch_for_current_device(&s); r != VKG_OK) return r;
+    const uint32_t n = num_tris;
+    if(n == 0)
+    {
+        k_noalloc_info<<<1, 1, 0, st>>>(s, 0, d_info);
+        return cudaGetLastError() == cudaSuccess ? VKG_OK : VKG_ERR_CUDA;
+    }
+    const int T = 256;
+    const uint32_t g = (n + T - 1) / T;
+    const uint32_t nblocks = (n + SORT_TILE - 1) / SORT_TILE;
+    k_noalloc_reset<<<(n + 15 + T - 1) / T, T, 0, st>>>(s, n);
+    k_tri_boxes<<<g, T, 0, st>>>(d_xyz, num_vertices, d_indices, n, s->tbox, s->small, s->small + 6);
+    k_morton<<<g, T, 0, st>>>(s->tbox, n, s->small, s->keys0, s->vals0, s->morton);
+    uint32_t *kin = s->keys0, *kout = s->keys1, *vin = s->vals0, *vout = s->vals1;
+    for(int shift = 0; shift < 30; shift += 8)
+    {
+        k_radix_hist<<<nblocks, SORT_THREADS, 0, st>>>(kin, n, shift, s->counts, nblocks);
+        k_scan_exclusive<<<1, 1024, 0, st>>>(s->counts, 256u * nblocks, nullptr);
+        k_radix_scatter<<<nblocks, SORT_THREADS, 0, st>>>(kin, vin, n, shift, s->counts, nblocks, kout, vout);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    k_gather_leaf_boxes<<<g, T, 0, st>>>(s->tbox, vin, n, s->lbox);
+    if(n > 1)
+    {
+        k_karras<<<(n - 1 + T - 1) / T, T, 0, st>>>(kin, n, s->left, s->right, s->first, s->last, s->iparent,
+                                                      s->lparent);
+        k_refit<<<g, T, 0, st>>>(s->lparent, s->iparent, s->left, s->right, s->lbox, s->ibox, s->visits, n);
+    }
+    const uint32_t capacity = std::min<uint32_t>(node_capacity, NOALLOC_MAX_TRIS + 8);
+    collapse_args A{s->left, s->right, s->first, s->last, s->ibox, s->lbox, n, leaf_max, capacity, s->small,
+                    s->node_ref, static_cast<node8 *>(d_nodes), s->small + 8, s->margin};
+    k_collapse<<<1, COLLAPSE_THREADS, 0, st>>>(A);
+    k_tri_records<<<g, T, 0, st>>>(d_xyz, num_vertices, d_indices, vin, n, static_cast<tri_rec *>(d_tris));
+    k_noalloc_info<<<1, 1, 0, st>>>(s, n, d_info);
+    return cudaGetLastError() == cudaSuccess ? VKG_OK : VKG_ERR_CUDA;
 }
