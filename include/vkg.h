@@ -233,6 +233,102 @@ vkg_status vkg_closest_hit_host(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray 
 /* node visits / triangle tests accumulated by launches with VKG_RAY_COUNT_STATS since the last reset */
 vkg_status vkg_ray_stats_get(vkg_ctx *ctx, uint64_t *node_visits, uint64_t *tri_tests, int reset);
 
+
+/* ---- environment map ------------------------------------------------------------------------ *
+ * Equirectangular fp32 RGB, u = 0.5 + 0.5 * atan2(x, -z) / pi, v = acos(y) / pi
+ * (shaders/slang/unlit/panorama.slang:12-15), texel (i, j) at d_rgb[3 * (j * width + i)].
+ * Procedural sky: procedural_environment.slang:7-11 (environment_white) plus a sun lobe
+ * sun_peak * exp((dot(d, sun_dir) - 1) / sun_width) evaluated at each texel centre. */
+vkg_status vkg_env_procedural_sky(vkg_ctx *ctx, uint32_t width, uint32_t height, const float sun_dir[3],
+                                  float sun_peak, float sun_width, float *d_rgb, void *stream);
+
+/* ---- scene (replaces RayBuilder::build_scene_acceleration + the trace_data buffers,
+ *      src/RayBuilder.cpp:784, PBRPathTracer.cpp:529-653) ----------------------------------------
+ * One triangle mesh with per-triangle material ids, a material table and an environment map. The
+ * scene copies what it needs (the caller's buffers may be freed afterwards), builds the BVH, marks
+ * two-sided triangles and builds the environment's importance-sampling tables (FP64 prefix sums
+ * + alias table). Synchronises `stream`. */
+typedef struct vkg_scene vkg_scene;
+typedef struct vkg_scene_desc
+{
+    const float *d_xyz;
+    uint32_t num_vertices;
+    const uint32_t *d_indices;
+    uint32_t num_tris;
+    const uint32_t *d_tri_material; /* per triangle, index into d_materials */
+    const vkg_material *d_materials;
+    uint32_t num_materials;
+    const float *d_env_rgb; /* equirect map, env_width x env_height x 3 fp32 */
+    uint32_t env_width, env_height;
+    uint32_t leaf_max; /* BVH leaf size (0 -> 4) */
+} vkg_scene_desc;
+vkg_status vkg_scene_create(vkg_ctx *ctx, const vkg_scene_desc *desc, vkg_scene **out, void *stream);
+vkg_status vkg_scene_destroy(vkg_ctx *ctx, vkg_scene *scene);
+/* the scene's BVH (owned by the scene) for direct ray queries */
+vkg_status vkg_scene_bvh(const vkg_scene *scene, const vkg_bvh **out);
+/* device views of the environment sampling tables: per texel normalised weight (mean 1, fp32) and
+ * alias buckets {fp32 probability, uint32 alias} (8 B each) */
+vkg_status vkg_scene_env_tables(const vkg_scene *scene, const float **d_weights, const void **d_alias,
+                                uint32_t *width, uint32_t *height);
+
+/* ---- path tracer (replaces PBRPathTracer, include/vierkant/PBRPathTracer.hpp:37-386) ---------- */
+/* PBRPathTracer::settings_t (PBRPathTracer.hpp:42-110): the fields of the traced path */
+typedef struct vkg_settings
+{
+    uint32_t resolution[2];           /* {1280, 720} */
+    uint32_t max_num_batches;         /* 0 = no limit */
+    uint32_t num_samples;             /* samples per pixel per batch (one render call = one batch) */
+    uint32_t max_trace_depth;         /* path segments including the camera ray (6) */
+    float max_path_beta;              /* clamp of indirect throughput, 0 = off */
+    uint32_t suspend_trace_when_done; /* render is a no-op once max_num_batches batches are done */
+    uint32_t disable_material;        /* override base colours with 0.8 */
+    uint32_t mis_mode;                /* 0 = MIS, 1 = NEE only, 2 = BSDF only */
+    uint32_t draw_skybox;             /* camera rays that miss show the environment */
+    float environment;                /* environment radiance factor (Scene::environment_factor) */
+    uint32_t rr_start_depth;          /* Russian roulette from this surface interaction on
+                                         (q = 1 - max(beta)); 0 = the reference's rule
+                                         max(beta) <= 0.05 * depth (raypipeline.slang:668-677) */
+    uint32_t crop[4];                 /* x0, y0, width, height of the traced window (0 size: full) */
+    uint32_t samples_per_wave;        /* paths in flight = pixels x this (0 = automatic) */
+} vkg_settings;
+
+typedef struct vkg_tracer_create_info
+{
+    uint32_t seed; /* create_info_t::seed (PBRPathTracer.hpp:138) */
+    vkg_settings settings;
+} vkg_tracer_create_info;
+
+/* statistics_t / timings_t (PBRPathTracer.hpp:112-127) of the last render */
+typedef struct vkg_tracer_stats
+{
+    double raytrace_ms;
+    double total_ms;
+    uint64_t paths;
+    uint64_t extension_rays;
+    uint64_t shadow_rays;
+    uint32_t batch;
+    uint32_t pad;
+} vkg_tracer_stats;
+
+typedef struct vkg_tracer vkg_tracer;
+vkg_status vkg_settings_default(vkg_settings *out);
+/* PBRPathTracer::create (PBRPathTracer.hpp:144) */
+vkg_status vkg_tracer_create(vkg_ctx *ctx, const vkg_tracer_create_info *info, vkg_tracer **out);
+vkg_status vkg_tracer_set_settings(vkg_tracer *tracer, const vkg_settings *settings);
+vkg_status vkg_tracer_get_settings(const vkg_tracer *tracer, vkg_settings *out);
+/* PBRPathTracer::render_scene (PBRPathTracer.hpp:161): traces one batch of num_samples paths per
+ * pixel of the crop window and blends it into the running mean (new + b * old) / (b + 1)
+ * (raypipeline.slang:258-266). d_rgb_out (crop width x height x 3 fp32, may be NULL) receives the
+ * accumulated image. Asynchronous on `stream`. */
+vkg_status vkg_tracer_render(vkg_tracer *tracer, const vkg_scene *scene, const vkg_camera *camera, float *d_rgb_out,
+                             void *stream);
+/* PBRPathTracer::reset_accumulator / current_batch (PBRPathTracer.hpp:169-174) */
+vkg_status vkg_tracer_reset_accumulator(vkg_tracer *tracer);
+vkg_status vkg_tracer_current_batch(const vkg_tracer *tracer, uint32_t *out);
+/* PBRPathTracer::statistics (PBRPathTracer.hpp:179); waits for the last render */
+vkg_status vkg_tracer_statistics(vkg_tracer *tracer, vkg_tracer_stats *out);
+vkg_status vkg_tracer_destroy(vkg_tracer *tracer);
+
 #ifdef __cplusplus
 }
 #endif

@@ -216,3 +216,89 @@ class CpuBVH:
         occ = np.zeros(len(rays), np.uint32)
         orc().orc_bvh_any_hit(C.byref(self.b), ptr(rays), len(rays), ptr(occ), nthreads, int(cull))
         return occ
+
+
+# ---- path tracer (FP32 twin / FP64 oracle) ---------------------------------------------------------
+MATERIAL_DTYPE = np.dtype([("base_color", "<f4", 3), ("roughness", "<f4"), ("metalness", "<f4"),
+                           ("emission", "<f4", 3), ("twosided", "<u4"), ("pad", "<f4", 3)])
+
+
+class orc_pt_scene(C.Structure):
+    _fields_ = [("xyz", C.c_void_p), ("idx", C.c_void_p), ("tri_mat", C.c_void_p), ("mats", C.c_void_p),
+                ("ntri", C.c_uint32), ("nmat", C.c_uint32)]
+
+
+class orc_pt_env(C.Structure):
+    _fields_ = [("rgb", C.c_void_p), ("weight", C.c_void_p), ("alias_prob", C.c_void_p), ("alias", C.c_void_p),
+                ("cdf", C.c_void_p), ("w", C.c_uint32), ("h", C.c_uint32)]
+
+
+class orc_pt_settings(C.Structure):
+    _fields_ = [("seed", C.c_uint32), ("batch", C.c_uint32), ("spp", C.c_uint32), ("max_depth", C.c_uint32),
+                ("rr_depth", C.c_uint32), ("mis_mode", C.c_uint32), ("disable_material", C.c_uint32),
+                ("draw_skybox", C.c_uint32), ("max_path_beta", C.c_float), ("environment", C.c_float),
+                ("crop", C.c_uint32 * 4)]
+
+
+def cornell_materials(seed=0x5EED, stream=2, num_spheres=64):
+    """Material table of the Cornell benchmark scene (walls two-sided, spheres one-sided)."""
+    sc = cornell_scene(seed, stream, num_spheres, 1)
+    mats = np.zeros(3 + num_spheres, MATERIAL_DTYPE)
+    mats["base_color"][0] = (0.73, 0.73, 0.73)
+    mats["base_color"][1] = (0.65, 0.05, 0.05)
+    mats["base_color"][2] = (0.12, 0.45, 0.15)
+    mats["roughness"][:3] = 1.0
+    mats["twosided"][:3] = 1
+    for s in range(num_spheres):
+        p = sc["spheres"][s]
+        mats["base_color"][3 + s] = tuple(p.base)
+        mats["roughness"][3 + s] = p.roughness
+        mats["metalness"][3 + s] = p.metalness
+    return mats
+
+
+def env_procedural(w, h, sun_dir, peak=5e4, width=3.8e-5):
+    rgb = np.zeros((h, w, 3), np.float32)
+    sd = np.ascontiguousarray(sun_dir, np.float32)
+    orc().orc_pt_env_procedural.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, C.c_double, C.c_double, C.c_void_p]
+    orc().orc_pt_env_procedural(w, h, ptr(sd), peak, width, ptr(rgb))
+    return rgb
+
+
+def env_tables_fp64(rgb):
+    h, w = rgb.shape[:2]
+    weight = np.zeros(w * h, np.float32)
+    cdf = np.zeros(w * h + 1, np.float64)
+    L = orc()
+    L.orc_pt_env_tables.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]
+    L.orc_pt_env_tables(ptr(np.ascontiguousarray(rgb, np.float32)), w, h, ptr(weight), ptr(cdf))
+    return weight, cdf
+
+
+def pt_render(fp64, xyz, idx, tri_mat, mats, bvh: "CpuBVH", env_rgb, cam, spp, *, seed=0x5EED, batch=0, max_depth=6,
+              rr_depth=3, mis_mode=0, crop=(0, 0, 0, 0), environment=1.0, draw_skybox=1, max_path_beta=0.0,
+              alias_prob=None, alias=None, weight=None, cdf=None, nthreads=0):
+    """Mean radiance per crop pixel ([h, w, 3] float64), mean squared luminance per pixel, (ext, shadow) rays."""
+    L = orc()
+    L.orc_pt_render.argtypes = [C.c_int, C.POINTER(orc_pt_scene), C.POINTER(orc_bvh), C.POINTER(orc_pt_env),
+                                C.POINTER(orc_camera), C.POINTER(orc_pt_settings), C.c_void_p, C.c_void_p, C.c_void_p,
+                                C.c_int]
+    keep = [np.ascontiguousarray(a) for a in (xyz, idx, tri_mat, mats)]
+    scene = orc_pt_scene(ptr(keep[0]), ptr(keep[1]), ptr(keep[2]), ptr(keep[3]), keep[1].shape[0], len(mats))
+    rgb = np.ascontiguousarray(env_rgb, np.float32)
+    h, w = rgb.shape[:2]
+    if fp64 and (weight is None or cdf is None):
+        weight, cdf = env_tables_fp64(rgb)
+    env = orc_pt_env(ptr(rgb), ptr(np.ascontiguousarray(weight, np.float32)),
+                     ptr(alias_prob) if alias_prob is not None else None,
+                     ptr(alias) if alias is not None else None, ptr(cdf) if cdf is not None else None, w, h)
+    cw = crop[2] or cam.width
+    ch = crop[3] or cam.height
+    st = orc_pt_settings(seed, batch, spp, max_depth, rr_depth, mis_mode, 0, draw_skybox, max_path_beta, environment,
+                         (C.c_uint32 * 4)(*crop))
+    out = np.zeros((ch, cw, 3), np.float64)
+    sq = np.zeros((ch, cw), np.float64)
+    stats = np.zeros(2, np.uint64)
+    L.orc_pt_render(int(fp64), C.byref(scene), C.byref(bvh.b), C.byref(env), C.byref(cam), C.byref(st), ptr(out),
+                    ptr(sq), ptr(stats), nthreads)
+    return out, sq, (int(stats[0]), int(stats[1]))

@@ -412,8 +412,30 @@ static inline int tri_test(const float *r, const float o[3], const float d[3], i
     return 1;
 }
 
+/* cull: 0 none, 1 every back face, 2 back faces of triangles not flagged in twosided[prim] */
+static void trace_one_ex(const orc_bvh *b, const orc_ray *ray, int cull, const uint8_t *twosided, int any,
+                         orc_hit *hit, uint32_t *occ, uint64_t *nv, uint64_t *nt);
 static void trace_one(const orc_bvh *b, const orc_ray *ray, int cull, int any, orc_hit *hit, uint32_t *occ,
                       uint64_t *nv, uint64_t *nt)
+{
+    trace_one_ex(b, ray, cull ? 1 : 0, NULL, any, hit, occ, nv, nt);
+}
+
+void orc_bvh_trace1(const orc_bvh *b, const orc_ray *ray, int cull_mode, const uint8_t *twosided, int any,
+                    orc_hit *hit, uint32_t *occ)
+{
+    uint64_t nv = 0, nt = 0;
+    if(b->num_tris == 0)
+    {
+        if(hit) *hit = (orc_hit){ORC_MISS, 0.f, 0.f, 0.f};
+        if(occ) *occ = 0;
+        return;
+    }
+    trace_one_ex(b, ray, cull_mode, twosided, any, hit, occ, &nv, &nt);
+}
+
+static void trace_one_ex(const orc_bvh *b, const orc_ray *ray, int cull_mode, const uint8_t *twosided, int any,
+                         orc_hit *hit, uint32_t *occ, uint64_t *nv, uint64_t *nt)
 {
     float inv_d[3];
     int neg[3];
@@ -489,6 +511,7 @@ static void trace_one(const orc_bvh *b, const orc_ray *ray, int cull, int any, o
                 memcpy(&prim, &r[9], 4);
                 float t, u, v;
                 ++tests;
+                int cull = cull_mode == 1 || (cull_mode == 2 && !(twosided && twosided[prim]));
                 if(!tri_test(r, ray->o, ray->d, cull, &t, &u, &v)) continue;
                 if(!(t > ray->tmin && t < ray->tmax)) continue;
                 if(any)

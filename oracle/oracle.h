@@ -106,6 +106,54 @@ int orc_bvh_closest_hit(const orc_bvh *b, const orc_ray *rays, uint32_t nray, or
                         int cull_back, uint64_t *stats /* [2]: node visits, tri tests; may be NULL */);
 int orc_bvh_any_hit(const orc_bvh *b, const orc_ray *rays, uint32_t nray, uint32_t *occluded, int nthreads,
                     int cull_back);
+/* single ray; cull_mode 0 none, 1 all back faces, 2 back faces of triangles with twosided[prim] == 0 */
+void orc_bvh_trace1(const orc_bvh *b, const orc_ray *ray, int cull_mode, const uint8_t *twosided, int any,
+                    orc_hit *hit, uint32_t *occ);
+
+/* ---- path tracer (FP32 twin of the GPU kernels / FP64 radiance oracle) ------------------ */
+typedef struct {
+    float base[3];
+    float roughness, metalness;
+    float emission[3];
+    uint32_t twosided;
+    float pad[3];
+} orc_pt_material; /* same 48-byte layout as vkg_material */
+
+typedef struct {
+    const float *xyz;
+    const uint32_t *idx;
+    const uint32_t *tri_mat;
+    const orc_pt_material *mats;
+    uint32_t ntri, nmat;
+} orc_pt_scene;
+
+typedef struct {
+    const float *rgb;        /* w*h*3 */
+    const float *weight;     /* w*h normalised weights (mean 1) */
+    const float *alias_prob; /* w*h, FP32 twin only (NULL: CDF sampling) */
+    const uint32_t *alias;   /* w*h, FP32 twin only */
+    const double *cdf;       /* w*h+1, FP64 oracle only */
+    uint32_t w, h;
+} orc_pt_env;
+
+typedef struct {
+    uint32_t seed;
+    uint32_t batch;
+    uint32_t spp;
+    uint32_t max_depth, rr_depth, mis_mode, disable_material, draw_skybox;
+    float max_path_beta, environment;
+    uint32_t crop[4]; /* x0, y0, w, h (pixels of the full resolution camera) */
+} orc_pt_settings;
+
+/* mean radiance per crop pixel over spp paths (out: crop_w*crop_h*3 doubles); stats[0] extension
+   rays, stats[1] shadow rays (may be NULL); sq: per-pixel mean of the squared luminance (may be NULL) */
+int orc_pt_render(int fp64, const orc_pt_scene *scene, const orc_bvh *bvh, const orc_pt_env *env,
+                  const orc_camera *cam, const orc_pt_settings *set, double *out, double *sq, uint64_t *stats,
+                  int nthreads);
+/* FP64 env tables from an rgb map: weights (mean 1, as float) and the CDF (w*h+1 doubles) */
+void orc_pt_env_tables(const float *rgb, uint32_t w, uint32_t h, float *weight, double *cdf);
+/* procedural sky in double precision (environment_white + sun lobe), rounded to float */
+void orc_pt_env_procedural(uint32_t w, uint32_t h, const float sun_dir[3], double peak, double width, float *rgb);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,392 @@
+/*
+ * Path tracer on the CPU. TEST INFRASTRUCTURE ONLY (CPU oracle).
+ *
+ *  - FP32 twin (fp64 = 0): the GPU kernels' estimator path for path: the same PCG32 stream per path
+ *    (initseq = (batch << 40) ^ (sample * pixels + pixel), 2 jitter draws, 8 draws per segment), the
+ *    oracle's float BVH traversal (bit-identical hits to the GPU's), and the GPU's own environment
+ *    alias table as input. Differences come only from transcendental functions and fused
+ *    multiply-adds, so most paths agree to a few ulps.
+ *  - FP64 oracle (fp64 = 1): the same estimator in double precision with an independent
+ *    environment sampler (FP64 CDF + binary search), double-precision ray casting over the same
+ *    8-wide BVH (box tests in double, Moeller-Trumbore in double), and 32-bit uniforms.
+ * The estimator itself is oracle/pt_core.inc (see its header for the reference lines it follows).
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdatomic.h>
+#include <stdlib.h>
+#include <string.h>
+
+int orc__run_threads(void *(*fn)(void *), void *arg, int nthreads);
+
+#define LEAF_BIT 0x80000000u
+
+typedef struct {
+    const orc_pt_scene *scene;
+    const orc_bvh *bvh;
+    const orc_pt_env *env;
+    const orc_camera *cam;
+    const uint8_t *twosided; /* by triangle id */
+    uint32_t seed, batch, spp, max_depth, rr_depth, mis_mode, disable_material, draw_skybox;
+    float max_path_beta, environment;
+    uint32_t cx0, cy0, cw, ch;
+    double *out, *sq;
+    atomic_uint next;
+    atomic_ullong ext, shadow;
+    int fp64;
+} orc_pt_job;
+
+/* ---- FP32 twin hooks ------------------------------------------------------------------------ */
+static inline float f_draw_raw(orc_pcg32 *g) { return orc_u01(orc_pcg32_next(g)); }
+
+static void f_hit_raw(const orc_pt_job *J, float ox, float oy, float oz, float tmin, float dx, float dy, float dz,
+                      uint32_t *prim, float *u, float *v)
+{
+    orc_ray r = {{ox, oy, oz}, tmin, {dx, dy, dz}, 1e4f};
+    orc_hit h;
+    orc_bvh_trace1(J->bvh, &r, 2, J->twosided, 0, &h, NULL);
+    *prim = h.prim;
+    *u = h.u;
+    *v = h.v;
+}
+
+static int f_occluded_raw(const orc_pt_job *J, float ox, float oy, float oz, float dx, float dy, float dz)
+{
+    orc_ray r = {{ox, oy, oz}, 0.f, {dx, dy, dz}, 1e4f};
+    uint32_t occ = 0;
+    orc_bvh_trace1(J->bvh, &r, 0, NULL, 1, NULL, &occ);
+    return (int)occ;
+}
+
+/* alias-table sample, as env_sample() in the GPU kernels */
+static void f_env_sample_raw(const orc_pt_env *e, float u0, float u1, float u2, float u3, float *dx, float *dy,
+                             float *dz, float *pdf, uint32_t *texel)
+{
+    const uint32_t n = e->w * e->h;
+    uint32_t b = (uint32_t)(u0 * (float)n);
+    if(b > n - 1u) b = n - 1u;
+    uint32_t t = u1 < e->alias_prob[b] ? b : e->alias[b];
+    uint32_t i = t % e->w, j = t / e->w;
+    float u = ((float)i + u2) / (float)e->w, v = ((float)j + u3) / (float)e->h;
+    const float PI = 3.14159265358979323846f;
+    float phi = (u - 0.5f) * 2.f * PI, theta = v * PI;
+    float st = sinf(theta);
+    *dx = st * sinf(phi);
+    *dy = cosf(theta);
+    *dz = -st * cosf(phi);
+    *pdf = st > 0.f ? e->weight[t] / (2.f * PI * PI * st) : 0.f;
+    *texel = t;
+}
+
+/* ---- FP64 oracle hooks ---------------------------------------------------------------------- */
+static inline double d_draw_raw(orc_pcg32 *g) { return (double)orc_pcg32_next(g) * 0x1p-32; }
+
+static inline float exp_scale_f(uint8_t e)
+{
+    uint32_t bits = (uint32_t)e << 23;
+    float f;
+    memcpy(&f, &bits, 4);
+    return f;
+}
+
+/* closest hit (any = 0) or occlusion (any = 1) in double precision over the 8-wide BVH */
+static int d_trace(const orc_pt_job *J, const double o[3], double tmin, const double d[3], int cull_mode, int any,
+                   uint32_t *prim_out, double *u_out, double *v_out)
+{
+    const orc_bvh *b = J->bvh;
+    *prim_out = ORC_MISS;
+    if(b->num_tris == 0) return 0;
+    double inv[3];
+    for(int a = 0; a < 3; ++a) inv[a] = d[a] != 0.0 ? 1.0 / d[a] : copysign(1e300, d[a]);
+    double best_t = 1e4, bu = 0, bv = 0;
+    uint32_t best = ORC_MISS;
+    uint32_t stack[512];
+    int sp = 0;
+    stack[sp++] = 0;
+    while(sp > 0)
+    {
+        const orc_node8 *nd = &b->nodes[stack[--sp]];
+        for(int k = 0; k < nd->nchild; ++k)
+        {
+            double tn = tmin, tf = best_t;
+            for(int a = 0; a < 3; ++a)
+            {
+                double s = (double)exp_scale_f(nd->exps[a]);
+                double lo = (double)nd->origin[a] + (double)nd->qlo[a][k] * s;
+                double hi = (double)nd->origin[a] + (double)nd->qhi[a][k] * s;
+                double t0 = (lo - o[a]) * inv[a], t1 = (hi - o[a]) * inv[a];
+                if(t0 > t1)
+                {
+                    double tt = t0;
+                    t0 = t1;
+                    t1 = tt;
+                }
+                if(t0 > tn) tn = t0;
+                if(t1 < tf) tf = t1;
+            }
+            if(tn > tf) continue;
+            uint32_t c = nd->child[k];
+            if(!(c & LEAF_BIT))
+            {
+                if(sp < 512) stack[sp++] = c;
+                continue;
+            }
+            uint32_t start = c & 0x07FFFFFFu, cnt = ((c >> 27) & 0xFu) + 1u;
+            for(uint32_t i = start; i < start + cnt; ++i)
+            {
+                const float *r = b->tris[i].v;
+                uint32_t prim;
+                memcpy(&prim, &r[9], 4);
+                double v0[3] = {r[0], r[1], r[2]}, e1[3] = {r[3], r[4], r[5]}, e2[3] = {r[6], r[7], r[8]};
+                double p[3] = {d[1] * e2[2] - e2[1] * d[2], d[2] * e2[0] - e2[2] * d[0], d[0] * e2[1] - e2[0] * d[1]};
+                double det = e1[0] * p[0] + e1[1] * p[1] + e1[2] * p[2];
+                if(det > -1e-12 && det < 1e-12) continue;
+                int cull = cull_mode == 1 || (cull_mode == 2 && !(J->twosided && J->twosided[prim]));
+                if(cull && det < 0) continue;
+                double id = 1.0 / det;
+                double tv[3] = {o[0] - v0[0], o[1] - v0[1], o[2] - v0[2]};
+                double uu = id * (tv[0] * p[0] + tv[1] * p[1] + tv[2] * p[2]);
+                if(uu < 0.0 || uu > 1.0) continue;
+                double q[3] = {tv[1] * e1[2] - e1[1] * tv[2], tv[2] * e1[0] - e1[2] * tv[0],
+                               tv[0] * e1[1] - e1[0] * tv[1]};
+                double vv = (d[0] * q[0] + d[1] * q[1] + d[2] * q[2]) * id;
+                if(vv < 0.0 || uu + vv > 1.0) continue;
+                double t = (e2[0] * q[0] + e2[1] * q[1] + e2[2] * q[2]) * id;
+                if(!(t > tmin && t < 1e4)) continue;
+                if(any) return 1;
+                if(t < best_t)
+                {
+                    best_t = t;
+                    best = prim;
+                    bu = uu;
+                    bv = vv;
+                }
+            }
+        }
+    }
+    *prim_out = best;
+    *u_out = bu;
+    *v_out = bv;
+    return best != ORC_MISS;
+}
+
+/* CDF inversion sample (independent of the GPU's alias table) */
+static void d_env_sample_raw(const orc_pt_env *e, double u0, double u1, double u2, double u3, double *dx, double *dy,
+                             double *dz, double *pdf, uint32_t *texel)
+{
+    (void)u1;
+    const uint32_t n = e->w * e->h;
+    uint32_t lo = 0, hi = n; /* largest t with cdf[t] <= u0 */
+    while(hi - lo > 1)
+    {
+        uint32_t mid = (lo + hi) >> 1;
+        if(e->cdf[mid] <= u0) lo = mid;
+        else hi = mid;
+    }
+    uint32_t t = lo;
+    uint32_t i = t % e->w, j = t / e->w;
+    double u = ((double)i + u2) / (double)e->w, v = ((double)j + u3) / (double)e->h;
+    const double PI = 3.14159265358979323846;
+    double phi = (u - 0.5) * 2.0 * PI, theta = v * PI;
+    double st = sin(theta);
+    *dx = st * sin(phi);
+    *dy = cos(theta);
+    *dz = -st * cos(phi);
+    *pdf = st > 0.0 ? (double)e->weight[t] / (2.0 * PI * PI * st) : 0.0;
+    *texel = t;
+}
+
+static void d_hit_raw(const orc_pt_job *J, double ox, double oy, double oz, double tmin, double dx, double dy,
+                      double dz, uint32_t *prim, double *u, double *v)
+{
+    double o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz};
+    *u = *v = 0;
+    d_trace(J, o, tmin, d, 2, 0, prim, u, v);
+}
+
+static int d_occluded_raw(const orc_pt_job *J, double ox, double oy, double oz, double dx, double dy, double dz)
+{
+    double o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz}, u, v;
+    uint32_t prim;
+    return d_trace(J, o, 0.0, d, 0, 1, &prim, &u, &v);
+}
+
+/* ---- instantiate the estimator ------------------------------------------------------------- */
+#define REAL float
+#define SFX(n) f_##n
+#define RSQRT(x) sqrtf(x)
+#define RSIN(x) sinf(x)
+#define RCOS(x) cosf(x)
+#define RATAN2(y, x) atan2f(y, x)
+#define RACOS(x) acosf(x)
+#define RFMA(a, b, c) fmaf(a, b, c)
+#define RABS(x) fabsf(x)
+#define HIT_RAW f_hit_raw
+#define OCC_RAW f_occluded_raw
+#define ENV_RAW f_env_sample_raw
+#define DRAW_RAW f_draw_raw
+#include "pt_core.inc"
+#undef REAL
+#undef SFX
+#undef RSQRT
+#undef RSIN
+#undef RCOS
+#undef RATAN2
+#undef RACOS
+#undef RFMA
+#undef RABS
+#undef HIT_RAW
+#undef OCC_RAW
+#undef ENV_RAW
+#undef DRAW_RAW
+
+#define REAL double
+#define SFX(n) d_##n
+#define RSQRT(x) sqrt(x)
+#define RSIN(x) sin(x)
+#define RCOS(x) cos(x)
+#define RATAN2(y, x) atan2(y, x)
+#define RACOS(x) acos(x)
+#define RFMA(a, b, c) fma(a, b, c)
+#define RABS(x) fabs(x)
+#define HIT_RAW d_hit_raw
+#define OCC_RAW d_occluded_raw
+#define ENV_RAW d_env_sample_raw
+#define DRAW_RAW d_draw_raw
+#include "pt_core.inc"
+
+/* ---- render ---------------------------------------------------------------------------------- */
+static void *pt_worker(void *arg)
+{
+    orc_pt_job *J = (orc_pt_job *)arg;
+    const uint32_t npix = J->cw * J->ch;
+    uint64_t st[2] = {0, 0};
+    for(;;)
+    {
+        uint32_t pix = atomic_fetch_add(&J->next, 1u);
+        if(pix >= npix) break;
+        uint32_t x = J->cx0 + pix % J->cw, y = J->cy0 + pix / J->cw;
+        double acc[3] = {0, 0, 0}, sq = 0;
+        for(uint32_t s = 0; s < J->spp; ++s)
+        {
+            uint64_t seq = ((uint64_t)J->batch << 40) ^ ((uint64_t)s * npix + pix);
+            double L[3];
+            if(J->fp64)
+            {
+                d_v3 r = d_trace_path(J, x, y, seq, st);
+                L[0] = r.x;
+                L[1] = r.y;
+                L[2] = r.z;
+            }
+            else
+            {
+                f_v3 r = f_trace_path(J, x, y, seq, st);
+                L[0] = r.x;
+                L[1] = r.y;
+                L[2] = r.z;
+            }
+            /* the FP32 twin sums in float like the GPU's accumulation kernel */
+            for(int c = 0; c < 3; ++c) acc[c] = J->fp64 ? acc[c] + L[c] : (double)((float)acc[c] + (float)L[c]);
+            double lum = 0.2126 * L[0] + 0.7152 * L[1] + 0.0722 * L[2];
+            sq += lum * lum;
+        }
+        for(int c = 0; c < 3; ++c)
+            J->out[3 * (size_t)pix + c] = J->fp64 ? acc[c] / J->spp : (double)((float)acc[c] / (float)J->spp);
+        if(J->sq) J->sq[pix] = sq / J->spp;
+    }
+    atomic_fetch_add(&J->ext, st[0]);
+    atomic_fetch_add(&J->shadow, st[1]);
+    return NULL;
+}
+
+int orc_pt_render(int fp64, const orc_pt_scene *scene, const orc_bvh *bvh, const orc_pt_env *env,
+                  const orc_camera *cam, const orc_pt_settings *set, double *out, double *sq, uint64_t *stats,
+                  int nthreads)
+{
+    uint8_t *ts = (uint8_t *)calloc(scene->ntri ? scene->ntri : 1, 1);
+    for(uint32_t i = 0; i < scene->ntri; ++i)
+    {
+        uint32_t m = scene->tri_mat[i];
+        ts[i] = (m < scene->nmat && scene->mats[m].twosided) ? 1 : 0;
+    }
+    orc_pt_job J;
+    memset(&J, 0, sizeof(J));
+    J.scene = scene;
+    J.bvh = bvh;
+    J.env = env;
+    J.cam = cam;
+    J.twosided = ts;
+    J.seed = set->seed;
+    J.batch = set->batch;
+    J.spp = set->spp;
+    J.max_depth = set->max_depth;
+    J.rr_depth = set->rr_depth;
+    J.mis_mode = set->mis_mode;
+    J.disable_material = set->disable_material;
+    J.draw_skybox = set->draw_skybox;
+    J.max_path_beta = set->max_path_beta;
+    J.environment = set->environment;
+    J.cx0 = set->crop[0];
+    J.cy0 = set->crop[1];
+    J.cw = set->crop[2] ? set->crop[2] : cam->width;
+    J.ch = set->crop[3] ? set->crop[3] : cam->height;
+    J.out = out;
+    J.sq = sq;
+    J.fp64 = fp64;
+    atomic_init(&J.next, 0u);
+    atomic_init(&J.ext, 0ull);
+    atomic_init(&J.shadow, 0ull);
+    int n = orc__run_threads(pt_worker, &J, nthreads);
+    if(stats)
+    {
+        stats[0] = atomic_load(&J.ext);
+        stats[1] = atomic_load(&J.shadow);
+    }
+    free(ts);
+    return n;
+}
+
+void orc_pt_env_tables(const float *rgb, uint32_t w, uint32_t h, float *weight, double *cdf)
+{
+    const size_t n = (size_t)w * h;
+    double *wt = (double *)malloc(sizeof(double) * n);
+    double total = 0;
+    for(size_t t = 0; t < n; ++t)
+    {
+        uint32_t j = (uint32_t)(t / w);
+        double theta = ((double)j + 0.5) * 3.14159265358979323846 / (double)h;
+        double lum = 0.2126 * rgb[3 * t] + 0.7152 * rgb[3 * t + 1] + 0.0722 * rgb[3 * t + 2];
+        wt[t] = lum > 0 ? lum * sin(theta) : 0;
+        total += wt[t];
+    }
+    double run = 0;
+    for(size_t t = 0; t < n; ++t)
+    {
+        cdf[t] = run / total;
+        run += wt[t];
+        weight[t] = (float)(wt[t] * (double)n / total);
+    }
+    cdf[n] = 1.0;
+    free(wt);
+}
+
+void orc_pt_env_procedural(uint32_t w, uint32_t h, const float sun_dir[3], double peak, double width, float *rgb)
+{
+    const double PI = 3.14159265358979323846;
+    for(uint32_t j = 0; j < h; ++j)
+        for(uint32_t i = 0; i < w; ++i)
+        {
+            double u = ((double)i + 0.5) / w, v = ((double)j + 0.5) / h;
+            double phi = (u - 0.5) * 2.0 * PI, theta = v * PI;
+            double st = sin(theta);
+            double d[3] = {st * sin(phi), cos(theta), -st * cos(phi)};
+            /* environment_white (procedural_environment.slang:7-11) */
+            double sky = d[1] > 0 ? 0.6 + (1.3 - 0.6) * d[1] : 0.6 + (0.1 - 0.6) * (-d[1]);
+            double cg = d[0] * sun_dir[0] + d[1] * sun_dir[1] + d[2] * sun_dir[2];
+            double sun = peak * exp((cg - 1.0) / width);
+            size_t t = (size_t)j * w + i;
+            rgb[3 * t] = rgb[3 * t + 1] = rgb[3 * t + 2] = (float)(sky + sun);
+        }
+}

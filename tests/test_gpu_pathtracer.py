@@ -1,0 +1,199 @@
+"""GPU path tracer (vkg_tracer_render) against the CPU oracle.
+
+* environment: the GPU's procedural map equals the FP64 restatement, and the alias table's implied
+  distribution equals the normalised texel weights built with FP64 prefix sums;
+* path-for-path twin: the FP32 CPU twin (same PCG32 streams, bit-exact BVH hits, the GPU's alias
+  table) reproduces the GPU image pixel by pixel up to transcendental / FMA rounding;
+* radiance: the GPU image of the oracle crop has RMSE and relative bias against the committed FP64
+  oracle (4096 spp) consistent with Monte-Carlo noise;
+* the three MIS modes converge to the same image; accumulator / batch / settings semantics.
+"""
+import ctypes as C
+import glob
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from vierkant_gb300 import _lib, geometry
+from vierkant_gb300.pathtracer import PBRPathTracer, Scene, procedural_sky, sun_direction
+
+pytestmark = pytest.mark.gpu
+
+CROP = (576, 528, 128, 128)
+
+
+def _cudart():
+    for cand in ["libcudart.so.13", "libcudart.so"] + sorted(glob.glob("/usr/local/cuda/lib64/libcudart.so*")):
+        try:
+            lib = C.CDLL(cand)
+            lib.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+            return lib
+        except OSError:
+            continue
+    raise RuntimeError("libcudart not found")
+
+
+def d2h(ptr, nbytes, dtype):
+    out = np.empty(nbytes // np.dtype(dtype).itemsize, dtype)
+    assert _cudart().cudaMemcpy(out.ctypes.data_as(C.c_void_p), C.c_void_p(ptr), C.c_size_t(nbytes), 2) == 0
+    return out
+
+
+@pytest.fixture(scope="module")
+def world(ctx):
+    sc = geometry.cornell_scene(0x5EED, 2, 64, 16)
+    env = procedural_sky(ctx, 2048, 1024, sun_direction(), 5e4, 3.8e-5)
+    scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], sc["materials"], env)
+    cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, 1280, 720)
+    th = float(np.float32(math.tan(math.radians(45.0) / 2.0)))
+    ocam = oracle.camera((0, 0, 3.4), (0, 0, 0), (0, 1, 0), th, 1280, 720)
+    yield {"sc": sc, "env": env, "scene": scene, "cam": cam, "ocam": ocam}
+    scene.close()
+
+
+def settings(spp, crop=CROP, rr=3, mis=0, max_depth=6):
+    s = PBRPathTracer.default_settings()
+    s.num_samples = spp
+    s.max_trace_depth = max_depth
+    s.rr_start_depth = rr
+    s.mis_mode = mis
+    for k in range(4):
+        s.crop[k] = crop[k]
+    return s
+
+
+def test_environment_map_and_alias_table(world):
+    env = world["env"].cpu().numpy()
+    ref = oracle.env_procedural(2048, 1024, sun_direction())
+    rel = np.abs(env - ref) / np.maximum(ref, 1e-3)
+    assert rel.max() < 1e-3, rel.max()
+    wptr, aptr, W, H = world["scene"].env_tables()
+    n = W * H
+    w = d2h(wptr, 4 * n, np.float32).astype(np.float64)
+    tab = d2h(aptr, 8 * n, np.uint32).reshape(n, 2)
+    prob = tab[:, 0].view(np.float32).astype(np.float64)
+    alias = tab[:, 1]
+    assert np.all((prob >= 0) & (prob <= 1)) and np.all(alias < n)
+    implied = prob.copy()
+    np.add.at(implied, alias, 1.0 - prob)
+    # every texel's total probability equals its normalised weight
+    assert abs(w.sum() / n - 1.0) < 1e-5
+    assert np.max(np.abs(implied - w)) < 2e-4 * max(1.0, w.max()) ** 0.5
+    assert np.max(np.abs(implied - w) / np.maximum(w, 1.0)) < 1e-4
+    # the weights equal the FP64 restatement's (same map, sequential FP64 sums)
+    ow, _ = oracle.env_tables_fp64(env)
+    assert np.max(np.abs(ow - w) / np.maximum(ow, 1e-6)) < 1e-5
+    # the sun lobe carries most of the luminance
+    top = np.argsort(w)[::-1][:2000]
+    assert w[top].sum() / n > 0.5
+
+
+def test_twin_parity_path_for_path(ctx, world):
+    """GPU vs the FP32 CPU twin: same paths, same random numbers, bit-exact hits."""
+    crop = (600, 560, 48, 48)
+    spp = 8
+    pt = PBRPathTracer(ctx, seed=0x5EED, settings=settings(spp, crop))
+    img = pt.render_scene(world["scene"], world["cam"]).cpu().numpy().astype(np.float64)
+    st = pt.statistics()
+    pt.close()
+    wptr, aptr, W, H = world["scene"].env_tables()
+    n = W * H
+    w = d2h(wptr, 4 * n, np.float32)
+    tab = d2h(aptr, 8 * n, np.uint32).reshape(n, 2)
+    prob = np.ascontiguousarray(tab[:, 0].view(np.float32))
+    alias = np.ascontiguousarray(tab[:, 1])
+    sc = world["sc"]
+    bvh = oracle.CpuBVH(sc["xyz"], sc["indices"], 4)
+    twin, _, rays = oracle.pt_render(False, sc["xyz"], sc["indices"], sc["tri_material"], sc["materials"], bvh,
+                                     world["env"].cpu().numpy(), world["ocam"], spp, seed=0x5EED, batch=0,
+                                     rr_depth=3, crop=crop, alias_prob=prob, alias=alias, weight=w)
+    rel = np.abs(img - twin) / np.maximum(np.abs(twin), 1e-2)
+    close = np.mean(np.all(rel < 1e-3, axis=-1))
+    assert close > 0.97, close
+    assert abs(img.sum() / twin.sum() - 1.0) < 0.02
+    # the same paths: ray counts agree closely
+    assert abs(st.extension_rays / rays[0] - 1.0) < 0.01
+    assert abs(st.shadow_rays / rays[1] - 1.0) < 0.01
+
+
+def test_radiance_against_fp64_oracle(ctx, world, golden):
+    g = golden("pt_oracle_crop")
+    ref = g["mean"].astype(np.float64)
+    assert tuple(g["crop"]) == CROP
+    pt = PBRPathTracer(ctx, seed=0x5EED, settings=settings(64, CROP))
+    for _ in range(4):  # 4 batches x 64 spp, running mean
+        img = pt.render_scene(world["scene"], world["cam"])
+    assert pt.current_batch() == 4
+    img = img.cpu().numpy().astype(np.float64)
+    pt.close()
+    spp = 256
+    bias = (img.sum() - ref.sum()) / ref.sum()
+    lum = lambda a: 0.2126 * a[..., 0] + 0.7152 * a[..., 1] + 0.0722 * a[..., 2]
+    rmse = math.sqrt(np.mean((lum(img) - lum(ref)) ** 2))
+    expected = math.sqrt(np.mean(g["lum_var"]) / spp + np.mean(g["lum_var"]) / int(g["spp"]))
+    print(f"bias {bias:+.4f}  rmse {rmse:.4f}  expected noise {expected:.4f}")
+    assert abs(bias) < 0.02, bias
+    assert rmse < 2.5 * expected, (rmse, expected)
+
+
+def test_mis_modes_converge_on_low_dynamic_range_env(ctx, world):
+    env = procedural_sky(ctx, 512, 256, sun_direction(), 0.0, 3.8e-5)  # sky gradient only
+    sc = world["sc"]
+    scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], sc["materials"], env)
+    crop = (560, 500, 32, 32)
+    means = []
+    for mode in (0, 1, 2):
+        pt = PBRPathTracer(ctx, seed=7, settings=settings(2048, crop, mis=mode))
+        means.append(pt.render_scene(scene, world["cam"]).cpu().numpy().astype(np.float64).mean(axis=(0, 1)))
+        pt.close()
+    scene.close()
+    m = np.array(means)
+    assert np.all(np.abs(m / m[0] - 1.0) < 0.02), m
+
+
+def test_accumulator_batches_and_settings(ctx, world):
+    s = settings(2, (700, 400, 16, 16))
+    s.max_num_batches = 3
+    pt = PBRPathTracer(ctx, seed=3, settings=s)
+    a = pt.render_scene(world["scene"], world["cam"]).clone()
+    b = pt.render_scene(world["scene"], world["cam"]).clone()
+    assert pt.current_batch() == 2
+    c = pt.render_scene(world["scene"], world["cam"]).clone()
+    d = pt.render_scene(world["scene"], world["cam"]).clone()  # suspended: max_num_batches reached
+    assert pt.current_batch() == 3
+    assert torch.equal(c, d)
+    pt.reset_accumulator()
+    assert pt.current_batch() == 0
+    a2 = pt.render_scene(world["scene"], world["cam"]).clone()
+    assert torch.equal(a, a2)  # deterministic: the same seed and batch give the same image
+    assert not torch.equal(a, b)
+    st = pt.statistics()
+    assert st.paths == 16 * 16 * 2 and st.extension_rays >= st.paths and st.raytrace_ms > 0
+    pt.close()
+    bad = settings(2)
+    bad.mis_mode = 5
+    with pytest.raises(_lib.VkgError):
+        PBRPathTracer(ctx, seed=1, settings=bad)
+    bad = settings(2, (1200, 700, 128, 128))
+    with pytest.raises(_lib.VkgError):
+        PBRPathTracer(ctx, seed=1, settings=bad)
+
+
+def test_full_frame_and_wave_split_equal(ctx, world):
+    """splitting the samples into several waves changes nothing: paths are independent."""
+    s1 = settings(4, (500, 300, 64, 64))
+    s1.samples_per_wave = 4
+    s2 = settings(4, (500, 300, 64, 64))
+    s2.samples_per_wave = 1
+    p1 = PBRPathTracer(ctx, seed=11, settings=s1)
+    p2 = PBRPathTracer(ctx, seed=11, settings=s2)
+    i1 = p1.render_scene(world["scene"], world["cam"])
+    i2 = p2.render_scene(world["scene"], world["cam"])
+    torch.cuda.synchronize()
+    # the per-pixel sums add the same path radiances in the same order
+    assert torch.equal(i1, i2)
+    p1.close()
+    p2.close()

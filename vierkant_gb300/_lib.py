@@ -52,6 +52,31 @@ class vkg_camera(C.Structure):
                 ("tan_half_fovy", C.c_float), ("aspect", C.c_float), ("width", C.c_uint32), ("height", C.c_uint32)]
 
 
+class vkg_settings(C.Structure):
+    _fields_ = [("resolution", C.c_uint32 * 2), ("max_num_batches", C.c_uint32), ("num_samples", C.c_uint32),
+                ("max_trace_depth", C.c_uint32), ("max_path_beta", C.c_float), ("suspend_trace_when_done", C.c_uint32),
+                ("disable_material", C.c_uint32), ("mis_mode", C.c_uint32), ("draw_skybox", C.c_uint32),
+                ("environment", C.c_float), ("rr_start_depth", C.c_uint32), ("crop", C.c_uint32 * 4),
+                ("samples_per_wave", C.c_uint32)]
+
+
+class vkg_tracer_create_info(C.Structure):
+    _fields_ = [("seed", C.c_uint32), ("settings", vkg_settings)]
+
+
+class vkg_tracer_stats(C.Structure):
+    _fields_ = [("raytrace_ms", C.c_double), ("total_ms", C.c_double), ("paths", C.c_uint64),
+                ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("batch", C.c_uint32),
+                ("pad", C.c_uint32)]
+
+
+class vkg_scene_desc(C.Structure):
+    _fields_ = [("d_xyz", C.c_void_p), ("num_vertices", C.c_uint32), ("d_indices", C.c_void_p),
+                ("num_tris", C.c_uint32), ("d_tri_material", C.c_void_p), ("d_materials", C.c_void_p),
+                ("num_materials", C.c_uint32), ("d_env_rgb", C.c_void_p), ("env_width", C.c_uint32),
+                ("env_height", C.c_uint32), ("leaf_max", C.c_uint32)]
+
+
 class vkg_bvh_build_options(C.Structure):
     _fields_ = [("leaf_max", C.c_uint32)]
 
@@ -97,6 +122,20 @@ SIGNATURES = {
     "vkg_any_hit": (I32, [P, P, P, U32, P, U32, P]),
     "vkg_closest_hit_host": (I32, [P, P, P, U32, P, U32, P]),
     "vkg_ray_stats_get": (I32, [P, C.POINTER(U64), C.POINTER(U64), I32]),
+    "vkg_env_procedural_sky": (I32, [P, U32, U32, P, F32, F32, P, P]),
+    "vkg_scene_create": (I32, [P, C.POINTER(vkg_scene_desc), C.POINTER(P), P]),
+    "vkg_scene_destroy": (I32, [P, P]),
+    "vkg_scene_bvh": (I32, [P, C.POINTER(P)]),
+    "vkg_scene_env_tables": (I32, [P, C.POINTER(P), C.POINTER(P), C.POINTER(U32), C.POINTER(U32)]),
+    "vkg_settings_default": (I32, [C.POINTER(vkg_settings)]),
+    "vkg_tracer_create": (I32, [P, C.POINTER(vkg_tracer_create_info), C.POINTER(P)]),
+    "vkg_tracer_set_settings": (I32, [P, C.POINTER(vkg_settings)]),
+    "vkg_tracer_get_settings": (I32, [P, C.POINTER(vkg_settings)]),
+    "vkg_tracer_render": (I32, [P, P, C.POINTER(vkg_camera), P, P]),
+    "vkg_tracer_reset_accumulator": (I32, [P]),
+    "vkg_tracer_current_batch": (I32, [P, C.POINTER(U32)]),
+    "vkg_tracer_statistics": (I32, [P, C.POINTER(vkg_tracer_stats)]),
+    "vkg_tracer_destroy": (I32, [P]),
 }
 
 _lib = None

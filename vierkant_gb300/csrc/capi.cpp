@@ -612,7 +612,8 @@ vkg_status vkg_scene_cornell_counts(uint32_t num_spheres, uint32_t n, uint32_t *
 }
 
 // Cornell box: back (z=-1), floor (y=-1), ceiling (y=+1) white 0.73; left (x=-1) red; right (x=+1)
-// green; roughness 1, metalness 0; faces point into the box; open toward +z. Spheres: PCG32
+// green; roughness 1, metalness 0, two-sided; faces point into the box; open toward +z. Spheres are
+// closed one-sided meshes (back faces culled for path rays). Spheres: PCG32
 // (seed, stream) draws per sphere, in order: radius U[0.1,0.4]; centre U[-1+r, 1-r]^3;
 // roughness U[0.05, 1]; metalness Bernoulli(0.3); base colour U[0.1, 0.9]^3.
 vkg_status vkg_scene_cornell(uint64_t seed, uint64_t stream, uint32_t num_spheres, uint32_t n, float *xyz,
@@ -643,6 +644,7 @@ vkg_status vkg_scene_cornell(uint64_t seed, uint64_t stream, uint32_t num_sphere
             std::memcpy(mat.base_color, cols[m], sizeof(cols[m]));
             mat.roughness = 1.f;
             mat.metalness = 0.f;
+            mat.twosided = 1u; // walls block light from both sides (closed box)
             materials[m] = mat;
         }
     }

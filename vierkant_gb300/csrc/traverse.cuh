@@ -1,0 +1,198 @@
+// Traversal core shared by the ray-query kernels (traverse.cu) and the path tracer's queue
+// kernels (pathtrace.cu): one ray, 8-wide quantised BVH, closest hit or any hit.
+//
+// Per node: six 16-byte loads (96 B node), slab tests of all children as
+// fmaf(q, 2^e * inv_d, (origin - o) * inv_d), children ordered by entry distance with an 8-key
+// sorting network, leaf children intersected first (nearest first), internal children pushed
+// far-to-near with their entry distance so a pop is skipped once best_t has passed it. Triangle
+// test: the reference's Moeller-Trumbore (src/intersection.cpp:114-129) op for op.
+#pragma once
+
+#include "internal.hpp"
+
+namespace vkg
+{
+
+// culling modes: none, all back faces (RAY_FLAG_CULL_BACK_FACING_TRIANGLES), or back faces of
+// triangles whose record is not flagged two-sided (per-instance TRIANGLE_FACING_CULL_DISABLE,
+// src/RayBuilder.cpp:521-522)
+enum cull_mode : int
+{
+    CULL_NONE = 0,
+    CULL_BACK = 1,
+    CULL_BACK_UNLESS_TWOSIDED = 2
+};
+constexpr uint32_t TRI_FLAG_TWOSIDED = 1u;
+
+struct trace_result
+{
+    uint32_t prim;
+    float t, u, v;
+    bool occluded;
+};
+
+__device__ __forceinline__ uint32_t tenc(float f)
+{
+    uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float tdec(uint32_t u)
+{
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+__device__ __forceinline__ void cswap(unsigned long long &a, unsigned long long &b)
+{
+    unsigned long long lo = a < b ? a : b, hi = a < b ? b : a;
+    a = lo;
+    b = hi;
+}
+
+// Batcher odd-even merge network, 19 comparators
+__device__ __forceinline__ void sort8(unsigned long long k[8])
+{
+    cswap(k[0], k[1]); cswap(k[2], k[3]); cswap(k[4], k[5]); cswap(k[6], k[7]);
+    cswap(k[0], k[2]); cswap(k[1], k[3]); cswap(k[4], k[6]); cswap(k[5], k[7]);
+    cswap(k[1], k[2]); cswap(k[5], k[6]);
+    cswap(k[0], k[4]); cswap(k[1], k[5]); cswap(k[2], k[6]); cswap(k[3], k[7]);
+    cswap(k[2], k[4]); cswap(k[3], k[5]);
+    cswap(k[1], k[2]); cswap(k[3], k[4]); cswap(k[5], k[6]);
+}
+
+__device__ __forceinline__ uint32_t sel4(const uint4 &w, uint32_t j)
+{
+    uint32_t a = (j & 1u) ? w.y : w.x;
+    uint32_t b = (j & 1u) ? w.w : w.z;
+    return (j & 2u) ? b : a;
+}
+
+__device__ __forceinline__ float safe_rcp(float d)
+{
+    float dd = fabsf(d) < 1e-20f ? copysignf(1e-20f, d) : d;
+    return __frcp_rn(dd);
+}
+
+__device__ __forceinline__ float qbyte(uint32_t w, int k) { return (float)((w >> (8 * (k & 3))) & 0xFFu); }
+
+
+template<bool ANY, bool STATS>
+__device__ __forceinline__ trace_result trace_ray(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
+                                                  float ox, float oy, float oz, float tmin, float dx, float dy,
+                                                  float dz, float tmax, int cull,
+                                                  unsigned long long &visits, unsigned long long &tests,
+                                                  unsigned long long *__restrict__ counters)
+{
+    const float ix = safe_rcp(dx), iy = safe_rcp(dy), iz = safe_rcp(dz);
+    const bool negx = ix < 0.f, negy = iy < 0.f, negz = iz < 0.f;
+    float best_t = tmax, bu = 0.f, bv = 0.f;
+    uint32_t best = VKG_MISS;
+    bool done = false;
+    uint32_t st_node[TRAVERSAL_STACK];
+    float st_t[TRAVERSAL_STACK];
+    int sp = 1;
+    st_node[0] = 0;
+    st_t[0] = tmin;
+    while(sp > 0 && !done)
+    {
+        --sp;
+        const uint32_t ni = st_node[sp];
+        if(st_t[sp] > best_t) continue;
+        if(STATS) ++visits;
+        const uint4 *np = reinterpret_cast<const uint4 *>(nodes + ni);
+        const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2);
+        const uint4 w3 = __ldg(np + 3), w4 = __ldg(np + 4), w5 = __ldg(np + 5);
+        const uint32_t meta = w0.w;
+        const uint32_t nch = meta >> 24;
+        const float tox = __fmul_rn(__fsub_rn(__uint_as_float(w0.x), ox), ix);
+        const float toy = __fmul_rn(__fsub_rn(__uint_as_float(w0.y), oy), iy);
+        const float toz = __fmul_rn(__fsub_rn(__uint_as_float(w0.z), oz), iz);
+        const float sx = __fmul_rn(exp_scale(meta & 0xFFu), ix);
+        const float sy = __fmul_rn(exp_scale((meta >> 8) & 0xFFu), iy);
+        const float sz = __fmul_rn(exp_scale((meta >> 16) & 0xFFu), iz);
+        const uint32_t nx0 = negx ? w2.z : w1.x, nx1 = negx ? w2.w : w1.y;
+        const uint32_t fx0 = negx ? w1.x : w2.z, fx1 = negx ? w1.y : w2.w;
+        const uint32_t ny0 = negy ? w3.x : w1.z, ny1 = negy ? w3.y : w1.w;
+        const uint32_t fy0 = negy ? w1.z : w3.x, fy1 = negy ? w1.w : w3.y;
+        const uint32_t nz0 = negz ? w3.z : w2.x, nz1 = negz ? w3.w : w2.y;
+        const uint32_t fz0 = negz ? w2.x : w3.z, fz1 = negz ? w2.y : w3.w;
+        unsigned long long key[8];
+#pragma unroll
+        for(int k = 0; k < 8; ++k)
+        {
+            key[k] = ~0ull;
+            if((uint32_t)k < nch)
+            {
+                const uint32_t wnx = k < 4 ? nx0 : nx1, wfx = k < 4 ? fx0 : fx1;
+                const uint32_t wny = k < 4 ? ny0 : ny1, wfy = k < 4 ? fy0 : fy1;
+                const uint32_t wnz = k < 4 ? nz0 : nz1, wfz = k < 4 ? fz0 : fz1;
+                const float tnx = fmaf(qbyte(wnx, k), sx, tox), tfx = fmaf(qbyte(wfx, k), sx, tox);
+                const float tny = fmaf(qbyte(wny, k), sy, toy), tfy = fmaf(qbyte(wfy, k), sy, toy);
+                const float tnz = fmaf(qbyte(wnz, k), sz, toz), tfz = fmaf(qbyte(wfz, k), sz, toz);
+                const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+                const float tf = fminf(fminf(tfx, tfy), fminf(tfz, best_t));
+                if(tn <= tf) key[k] = ((unsigned long long)tenc(tn) << 32) | (unsigned long long)k;
+            }
+        }
+        sort8(key);
+#pragma unroll
+        for(int h = 0; h < 8; ++h)
+        {
+            if(key[h] == ~0ull || done) break;
+            const uint32_t k = (uint32_t)(key[h] & 7ull);
+            const uint32_t c = (k & 4u) ? sel4(w5, k & 3u) : sel4(w4, k & 3u);
+            if(!(c & LEAF_BIT)) continue;
+            if(tdec((uint32_t)(key[h] >> 32)) > best_t) continue;
+            const uint32_t start = c & 0x07FFFFFFu, cnt = ((c >> 27) & 0xFu) + 1u;
+            for(uint32_t ti = start; ti < start + cnt; ++ti)
+            {
+                const float4 *tp = reinterpret_cast<const float4 *>(tris + ti);
+                const float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
+                if(STATS) ++tests;
+                const int tcull = cull == CULL_BACK ||
+                                  (cull == CULL_BACK_UNLESS_TWOSIDED && !(__float_as_uint(cc.z) & TRI_FLAG_TWOSIDED));
+                float t, u, v;
+                if(!tri_test(a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, cc.x, ox, oy, oz, dx, dy, dz, tcull, t, u, v))
+                    continue;
+                if(!(t > tmin && t < tmax)) continue;
+                if(ANY)
+                {
+                    done = true;
+                    break;
+                }
+                const uint32_t prim = __float_as_uint(cc.y);
+                if(t < best_t || (t == best_t && prim < best))
+                {
+                    best_t = t;
+                    best = prim;
+                    bu = u;
+                    bv = v;
+                }
+            }
+        }
+        if(done) break;
+#pragma unroll
+        for(int h = 7; h >= 0; --h)
+        {
+            if(key[h] == ~0ull) continue;
+            const uint32_t k = (uint32_t)(key[h] & 7ull);
+            const uint32_t c = (k & 4u) ? sel4(w5, k & 3u) : sel4(w4, k & 3u);
+            if(c & LEAF_BIT) continue;
+            if(sp < (int)TRAVERSAL_STACK)
+            {
+                st_node[sp] = c;
+                st_t[sp] = tdec((uint32_t)(key[h] >> 32));
+                ++sp;
+            }
+            else if(counters) { atomicOr(&counters[2], 1ull); }
+        }
+    }
+    trace_result r;
+    r.occluded = done;
+    r.prim = best;
+    r.t = best == VKG_MISS ? 0.f : best_t;
+    r.u = best == VKG_MISS ? 0.f : bu;
+    r.v = best == VKG_MISS ? 0.f : bv;
+    return r;
+}
+
+}// namespace vkg

@@ -1,0 +1,143 @@
+"""Path tracer API mirroring vierkant's PBRPathTracer (include/vierkant/PBRPathTracer.hpp:37-386).
+
+    ctx = Context(0)
+    scene = Scene(ctx, xyz, indices, tri_material, materials, env_rgb)   # BVH + env sampling tables
+    pt = PBRPathTracer(ctx, seed=0x5EED, settings=PBRPathTracer.default_settings())
+    pt.settings.num_samples = 64
+    image = pt.render_scene(scene, camera)      # running mean over batches, [H, W, 3] fp32 on the GPU
+    pt.current_batch(); pt.reset_accumulator(); pt.statistics()
+
+All work runs in libvkg's kernels; torch only provides device memory and the stream.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from ._lib import (check, lib, vkg_camera, vkg_scene_desc, vkg_settings, vkg_tracer_create_info,
+                   vkg_tracer_stats)
+from .raytracing import Context
+
+# BASELINE sun: 30 deg elevation, 20 deg azimuth (measured from +z toward +x), 5e4 peak, width 3.8e-5
+SUN_ELEVATION_DEG = 30.0
+SUN_AZIMUTH_DEG = 20.0
+
+
+def sun_direction(elevation_deg=SUN_ELEVATION_DEG, azimuth_deg=SUN_AZIMUTH_DEG):
+    e, a = math.radians(elevation_deg), math.radians(azimuth_deg)
+    return np.array([math.sin(a) * math.cos(e), math.sin(e), math.cos(a) * math.cos(e)], np.float32)
+
+
+def procedural_sky(ctx: Context, width=2048, height=1024, sun_dir=None, sun_peak=5e4, sun_width=3.8e-5):
+    """environment_white gradient + sun lobe, as a [height, width, 3] fp32 CUDA tensor."""
+    if sun_dir is None:
+        sun_dir = sun_direction()
+    out = torch.empty((height, width, 3), dtype=torch.float32, device=f"cuda:{ctx.device}")
+    sd = np.ascontiguousarray(sun_dir, np.float32)
+    check(lib().vkg_env_procedural_sky(ctx.handle, width, height, sd.ctypes.data_as(C.c_void_p), C.c_float(sun_peak),
+                                       C.c_float(sun_width), C.c_void_p(out.data_ptr()), C.c_void_p(ctx.stream())),
+          ctx.handle, "vkg_env_procedural_sky")
+    return out
+
+
+class Scene:
+    def __init__(self, ctx: Context, xyz, indices, tri_material, materials, env_rgb, leaf_max=4):
+        dev = f"cuda:{ctx.device}"
+
+        def t(a, dt):
+            if isinstance(a, np.ndarray):
+                a = torch.from_numpy(np.ascontiguousarray(a))
+            return a.to(dev).contiguous().view(dt) if a.dtype.itemsize == dt.itemsize else a.to(dev, dt).contiguous()
+
+        self.ctx = ctx
+        xyz = t(xyz, torch.float32)
+        idx = torch.from_numpy(np.ascontiguousarray(indices, np.uint32).view(np.int32)).to(dev) \
+            if isinstance(indices, np.ndarray) else indices.to(dev).contiguous()
+        tm = torch.from_numpy(np.ascontiguousarray(tri_material, np.uint32).view(np.int32)).to(dev) \
+            if isinstance(tri_material, np.ndarray) else tri_material.to(dev).contiguous()
+        mats = torch.from_numpy(np.frombuffer(np.ascontiguousarray(materials).tobytes(), np.uint8).copy()).to(dev)
+        env = env_rgb.to(dev, torch.float32).contiguous()
+        d = vkg_scene_desc(xyz.data_ptr(), xyz.numel() // 3, idx.data_ptr(), idx.numel() // 3, tm.data_ptr(),
+                           mats.data_ptr(), len(materials), env.data_ptr(), env.shape[1], env.shape[0], leaf_max)
+        h = C.c_void_p()
+        check(lib().vkg_scene_create(ctx.handle, C.byref(d), C.byref(h), C.c_void_p(ctx.stream())), ctx.handle,
+              "vkg_scene_create")
+        self.handle = h
+        self.num_tris = idx.numel() // 3
+
+    def env_tables(self):
+        w, a = C.c_void_p(), C.c_void_p()
+        W, H = C.c_uint32(), C.c_uint32()
+        check(lib().vkg_scene_env_tables(self.handle, C.byref(w), C.byref(a), C.byref(W), C.byref(H)))
+        return w.value, a.value, W.value, H.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().vkg_scene_destroy(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PBRPathTracer:
+    """PBRPathTracer::create / settings / render_scene / reset_accumulator / current_batch / statistics."""
+
+    @staticmethod
+    def default_settings() -> vkg_settings:
+        s = vkg_settings()
+        check(lib().vkg_settings_default(C.byref(s)))
+        return s
+
+    def __init__(self, ctx: Context, seed: int = 0, settings: vkg_settings | None = None):
+        self.ctx = ctx
+        self.settings = settings if settings is not None else self.default_settings()
+        info = vkg_tracer_create_info(seed, self.settings)
+        h = C.c_void_p()
+        check(lib().vkg_tracer_create(ctx.handle, C.byref(info), C.byref(h)), ctx.handle, "vkg_tracer_create")
+        self.handle = h
+
+    def _crop(self):
+        s = self.settings
+        if s.crop[2] and s.crop[3]:
+            return s.crop[2], s.crop[3]
+        return s.resolution[0], s.resolution[1]
+
+    def render_scene(self, scene: Scene, camera: vkg_camera, out: torch.Tensor | None = None) -> torch.Tensor:
+        check(lib().vkg_tracer_set_settings(self.handle, C.byref(self.settings)), self.ctx.handle, "settings")
+        w, h = self._crop()
+        if out is None:
+            out = torch.empty((h, w, 3), dtype=torch.float32, device=f"cuda:{self.ctx.device}")
+        check(lib().vkg_tracer_render(self.handle, scene.handle, C.byref(camera), C.c_void_p(out.data_ptr()),
+                                      C.c_void_p(self.ctx.stream())), self.ctx.handle, "vkg_tracer_render")
+        return out
+
+    def reset_accumulator(self):
+        check(lib().vkg_tracer_reset_accumulator(self.handle))
+
+    def current_batch(self) -> int:
+        b = C.c_uint32()
+        check(lib().vkg_tracer_current_batch(self.handle, C.byref(b)))
+        return b.value
+
+    def statistics(self) -> vkg_tracer_stats:
+        st = vkg_tracer_stats()
+        check(lib().vkg_tracer_statistics(self.handle, C.byref(st)), self.ctx.handle, "vkg_tracer_statistics")
+        return st
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().vkg_tracer_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
