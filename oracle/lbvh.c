@@ -19,9 +19,9 @@
  *     child box first grown by the margin (conservative: a box never rejects a triangle whose
  *     Moeller-Trumbore hit lies inside it, for ray origins within ~16 scene extents)
  *
- * Traversal (closest hit): ordered by entry distance, leaves first, internal children pushed
- * far-to-near with their entry distance; slab tests evaluated as fmaf(q, s*inv_d, (o'-o)*inv_d)
- * exactly as the kernels do. Triangle test = intersection.cpp:114-129 on precomputed v0/e1/e2.
+ * Traversal (closest hit): ordered by 32-bit keys (ordered entry distance with its low 3 bits
+ * replaced by the slot), leaves first, internal children pushed far-to-near with the truncated
+ * entry distance; slab tests evaluated as fmaf(q, s*inv_d, (o'-o)*inv_d) exactly as the kernels do. Triangle test = intersection.cpp:114-129 on precomputed v0/e1/e2.
  */
 #include "oracle.h"
 
@@ -376,6 +376,19 @@ void orc_bvh_free(orc_bvh *b)
 }
 
 /* ---- traversal ----------------------------------------------------------------------------- */
+static inline uint32_t fenc_(float f)
+{
+    uint32_t b;
+    memcpy(&b, &f, 4);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+static inline float fdec_(uint32_t u)
+{
+    uint32_t b = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+}
 #define STACK_CAP 256
 
 typedef struct {
@@ -471,6 +484,7 @@ static void trace_one_ex(const orc_bvh *b, const orc_ray *ray, int cull_mode, co
         }
         float ht[8];
         int hk[8];
+        uint32_t hkey[8];
         int nh = 0;
         for(int k = 0; k < nd->nchild; ++k)
         {
@@ -486,17 +500,21 @@ static void trace_one_ex(const orc_bvh *b, const orc_ray *ray, int cull_mode, co
             float tf = fminf(fminf(tf3[0], tf3[1]), fminf(tf3[2], best_t));
             if(tn <= tf)
             {
-                /* insertion in ascending (t, slot) order */
+                /* 32-bit key as in the kernels: ordered entry distance, low 3 bits = slot */
+                uint32_t key = (fenc_(tn) & ~7u) | (uint32_t)k;
                 int p = nh++;
-                while(p > 0 && ht[p - 1] > tn)
+                while(p > 0 && hkey[p - 1] > key)
                 {
-                    ht[p] = ht[p - 1];
-                    hk[p] = hk[p - 1];
+                    hkey[p] = hkey[p - 1];
                     --p;
                 }
-                ht[p] = tn;
-                hk[p] = k;
+                hkey[p] = key;
             }
+        }
+        for(int h = 0; h < nh; ++h)
+        {
+            ht[h] = fdec_(hkey[h] & ~7u);
+            hk[h] = (int)(hkey[h] & 7u);
         }
         for(int h = 0; h < nh && !done; ++h)
         {

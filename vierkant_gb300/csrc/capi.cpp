@@ -62,7 +62,8 @@ vkg_status vkg_ctx_create(int device, vkg_ctx **out)
     if(cudaSetDevice(device) != cudaSuccess ||
        cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
        cudaMalloc(&ctx->d_counters, 4 * sizeof(unsigned long long)) != cudaSuccess ||
-       cudaMemset(ctx->d_counters, 0, 4 * sizeof(unsigned long long)) != cudaSuccess)
+       cudaMemset(ctx->d_counters, 0, 4 * sizeof(unsigned long long)) != cudaSuccess ||
+       cudaMalloc(&ctx->d_work, sizeof(uint32_t)) != cudaSuccess)
     {
         delete ctx;
         return VKG_ERR_CUDA;
@@ -76,6 +77,7 @@ vkg_status vkg_ctx_destroy(vkg_ctx *ctx)
     if(!ctx) return VKG_OK;
     bind_device(ctx);
     cudaFree(ctx->d_counters);
+    cudaFree(ctx->d_work);
     cudaFree(ctx->d_stage_rays);
     cudaFree(ctx->d_stage_hits);
     delete ctx;

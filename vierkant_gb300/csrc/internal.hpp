@@ -17,6 +17,8 @@ struct vkg_ctx
     std::string last_error;
     // device counters: [0] node visits, [1] triangle tests, [2] error flags (bit0 stack overflow)
     unsigned long long *d_counters = nullptr;
+    // ray index counter of the persistent traversal kernels
+    uint32_t *d_work = nullptr;
     // host-variant staging (grown on demand)
     void *d_stage_rays = nullptr;
     void *d_stage_hits = nullptr;

@@ -8,6 +8,9 @@
 // 96 B per node visit and 48 B per triangle test from L2/L1.
 #include "traverse.cuh"
 
+#include <cstdlib>
+#include <string>
+
 namespace vkg
 {
 namespace
@@ -51,6 +54,104 @@ __global__ void __launch_bounds__(TRACE_THREADS)
     }
 }
 
+// Persistent variant: a fixed grid of warps; every lane whose ray has finished takes the next ray
+// index from a global counter (one atomic per warp and refill), so warps stay full until the batch
+// is exhausted instead of idling behind their slowest ray.
+template<bool ANY, bool STATS>
+__global__ void __launch_bounds__(TRACE_THREADS)
+        k_trace_persistent(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
+                           const vkg_ray *__restrict__ rays, uint32_t n, vkg_hit *__restrict__ hits,
+                           uint32_t *__restrict__ occluded, int cull, unsigned long long *__restrict__ counters,
+                           uint32_t *__restrict__ next_ray)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt = (1u << lane) - 1u;
+    unsigned long long visits = 0, tests = 0;
+    ray_state s;
+    uint32_t cur = 0xFFFFFFFFu;
+    bool exhausted = false;
+    for(;;)
+    {
+        const bool need = cur == 0xFFFFFFFFu && !exhausted;
+        const unsigned m = __ballot_sync(0xffffffffu, need);
+        if(m)
+        {
+            const uint32_t leader = __ffs(m) - 1;
+            uint32_t base = 0;
+            if(lane == leader) base = atomicAdd(next_ray, (uint32_t)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if(need)
+            {
+                const uint32_t idx = base + __popc(m & lt);
+                if(idx < n)
+                {
+                    const float4 *rp = reinterpret_cast<const float4 *>(rays + idx);
+                    const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
+                    ray_init(s, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w);
+                    cur = idx;
+                }
+                else exhausted = true;
+            }
+        }
+        const bool active = cur != 0xFFFFFFFFu;
+        if(!__any_sync(0xffffffffu, active)) break;
+        if(active && !ray_step<ANY, STATS>(s, nodes, tris, cull, visits, tests, counters))
+        {
+            const trace_result r = ray_result(s);
+            if(ANY) occluded[cur] = r.occluded ? 1u : 0u;
+            else
+                reinterpret_cast<uint4 *>(hits)[cur] =
+                        make_uint4(r.prim, __float_as_uint(r.t), __float_as_uint(r.u), __float_as_uint(r.v));
+            cur = 0xFFFFFFFFu;
+        }
+    }
+    if(STATS)
+    {
+        for(int o = 16; o > 0; o >>= 1)
+        {
+            visits += __shfl_down_sync(0xffffffffu, visits, o);
+            tests += __shfl_down_sync(0xffffffffu, tests, o);
+        }
+        if(lane == 0 && counters)
+        {
+            atomicAdd(&counters[0], visits);
+            atomicAdd(&counters[1], tests);
+        }
+    }
+}
+
+template<bool ANY, bool STATS>
+void launch_persistent(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t n, vkg_hit *d_hits,
+                       uint32_t *d_occ, int cull, cudaStream_t st)
+{
+    static int blocks_per_sm = 0;
+    if(blocks_per_sm == 0)
+    {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace_persistent<ANY, STATS>, TRACE_THREADS,
+                                                      0);
+        if(blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    uint32_t grid = (uint32_t)ctx->num_sms * (uint32_t)blocks_per_sm;
+    const uint32_t need = (n + TRACE_THREADS - 1) / TRACE_THREADS;
+    if(grid > need) grid = need;
+    cudaMemsetAsync(ctx->d_work, 0, sizeof(uint32_t), st);
+    k_trace_persistent<ANY, STATS><<<grid, TRACE_THREADS, 0, st>>>(bvh->d_nodes, bvh->d_tris, d_rays, n, d_hits, d_occ,
+                                                                   cull, ctx->d_counters, ctx->d_work);
+}
+
+// kernel choice: the one-thread-per-ray kernel by default (faster on mixed primary/bounce batches);
+// VKG_TRACE_KERNEL=persistent selects the refilling persistent kernel
+bool use_persistent()
+{
+    static int v = -1;
+    if(v < 0)
+    {
+        const char *e = getenv("VKG_TRACE_KERNEL");
+        v = (e && std::string(e) == "persistent") ? 1 : 0;
+    }
+    return v == 1;
+}
+
 __global__ void k_fill_miss(vkg_hit *hits, uint32_t *occluded, uint32_t n)
 {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -70,6 +171,20 @@ vkg_status launch_trace(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays,
     }
     const int cull = (flags & VKG_RAY_CULL_BACK_FACES) ? 1 : 0;
     const bool stats = (flags & VKG_RAY_COUNT_STATS) != 0;
+    if(use_persistent())
+    {
+        if(d_occ)
+        {
+            if(stats) launch_persistent<true, true>(ctx, bvh, d_rays, n, nullptr, d_occ, cull, st);
+            else launch_persistent<true, false>(ctx, bvh, d_rays, n, nullptr, d_occ, cull, st);
+        }
+        else
+        {
+            if(stats) launch_persistent<false, true>(ctx, bvh, d_rays, n, d_hits, nullptr, cull, st);
+            else launch_persistent<false, false>(ctx, bvh, d_rays, n, d_hits, nullptr, cull, st);
+        }
+        return cuda_check(ctx, cudaGetLastError(), "k_trace_persistent");
+    }
     if(d_occ)
     {
         if(stats)

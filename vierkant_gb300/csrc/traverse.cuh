@@ -3,9 +3,10 @@
 //
 // Per node: six 16-byte loads (96 B node), slab tests of all children as
 // fmaf(q, 2^e * inv_d, (origin - o) * inv_d), children ordered by entry distance with an 8-key
-// sorting network, leaf children intersected first (nearest first), internal children pushed
-// far-to-near with their entry distance so a pop is skipped once best_t has passed it. Triangle
-// test: the reference's Moeller-Trumbore (src/intersection.cpp:114-129) op for op.
+// sorting network on 32-bit keys, leaf children intersected first (nearest first), internal
+// children pushed far-to-near with their entry distance so a pop is skipped once best_t has passed
+// it. Triangle test: the reference's Moeller-Trumbore (src/intersection.cpp:114-129) op for op.
+// ray_step() processes one node, so a persistent kernel can refill lanes whose ray has finished.
 #pragma once
 
 #include "internal.hpp"
@@ -41,15 +42,15 @@ __device__ __forceinline__ float tdec(uint32_t u)
     return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
 }
 
-__device__ __forceinline__ void cswap(unsigned long long &a, unsigned long long &b)
+__device__ __forceinline__ void cswap(uint32_t &a, uint32_t &b)
 {
-    unsigned long long lo = a < b ? a : b, hi = a < b ? b : a;
+    const uint32_t lo = min(a, b), hi = max(a, b);
     a = lo;
     b = hi;
 }
 
 // Batcher odd-even merge network, 19 comparators
-__device__ __forceinline__ void sort8(unsigned long long k[8])
+__device__ __forceinline__ void sort8(uint32_t k[8])
 {
     cswap(k[0], k[1]); cswap(k[2], k[3]); cswap(k[4], k[5]); cswap(k[6], k[7]);
     cswap(k[0], k[2]); cswap(k[1], k[3]); cswap(k[4], k[6]); cswap(k[5], k[7]);
@@ -75,51 +76,78 @@ __device__ __forceinline__ float safe_rcp(float d)
 __device__ __forceinline__ float qbyte(uint32_t w, int k) { return (float)((w >> (8 * (k & 3))) & 0xFFu); }
 
 
-template<bool ANY, bool STATS>
-__device__ __forceinline__ trace_result trace_ray(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
-                                                  float ox, float oy, float oz, float tmin, float dx, float dy,
-                                                  float dz, float tmax, int cull,
-                                                  unsigned long long &visits, unsigned long long &tests,
-                                                  unsigned long long *__restrict__ counters)
+// per-ray traversal state (the stack lives in local memory; only its used top is touched)
+struct ray_state
 {
-    const float ix = safe_rcp(dx), iy = safe_rcp(dy), iz = safe_rcp(dz);
-    const bool negx = ix < 0.f, negy = iy < 0.f, negz = iz < 0.f;
-    float best_t = tmax, bu = 0.f, bv = 0.f;
-    uint32_t best = VKG_MISS;
-    bool done = false;
+    float ox, oy, oz, tmin, dx, dy, dz, tmax, ix, iy, iz;
+    float best_t, bu, bv;
+    uint32_t best;
+    int sp;
+    bool done;
     uint32_t st_node[TRAVERSAL_STACK];
     float st_t[TRAVERSAL_STACK];
-    int sp = 1;
-    st_node[0] = 0;
-    st_t[0] = tmin;
-    while(sp > 0 && !done)
+};
+
+__device__ __forceinline__ void ray_init(ray_state &s, float ox, float oy, float oz, float tmin, float dx, float dy,
+                                         float dz, float tmax)
+{
+    s.ox = ox;
+    s.oy = oy;
+    s.oz = oz;
+    s.tmin = tmin;
+    s.dx = dx;
+    s.dy = dy;
+    s.dz = dz;
+    s.tmax = tmax;
+    s.ix = safe_rcp(dx);
+    s.iy = safe_rcp(dy);
+    s.iz = safe_rcp(dz);
+    s.best_t = tmax;
+    s.bu = s.bv = 0.f;
+    s.best = VKG_MISS;
+    s.done = false;
+    s.sp = 1;
+    s.st_node[0] = 0;
+    s.st_t[0] = tmin;
+}
+
+// one node of the traversal; returns false once the ray is finished
+template<bool ANY, bool STATS>
+__device__ __forceinline__ bool ray_step(ray_state &s, const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
+                                         int cull, unsigned long long &visits, unsigned long long &tests,
+                                         unsigned long long *__restrict__ counters)
+{
+    while(s.sp > 0 && !s.done)
     {
-        --sp;
-        const uint32_t ni = st_node[sp];
-        if(st_t[sp] > best_t) continue;
+        --s.sp;
+        const uint32_t ni = s.st_node[s.sp];
+        if(s.st_t[s.sp] > s.best_t) continue;
         if(STATS) ++visits;
         const uint4 *np = reinterpret_cast<const uint4 *>(nodes + ni);
         const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2);
         const uint4 w3 = __ldg(np + 3), w4 = __ldg(np + 4), w5 = __ldg(np + 5);
         const uint32_t meta = w0.w;
         const uint32_t nch = meta >> 24;
-        const float tox = __fmul_rn(__fsub_rn(__uint_as_float(w0.x), ox), ix);
-        const float toy = __fmul_rn(__fsub_rn(__uint_as_float(w0.y), oy), iy);
-        const float toz = __fmul_rn(__fsub_rn(__uint_as_float(w0.z), oz), iz);
-        const float sx = __fmul_rn(exp_scale(meta & 0xFFu), ix);
-        const float sy = __fmul_rn(exp_scale((meta >> 8) & 0xFFu), iy);
-        const float sz = __fmul_rn(exp_scale((meta >> 16) & 0xFFu), iz);
+        const bool negx = s.ix < 0.f, negy = s.iy < 0.f, negz = s.iz < 0.f;
+        const float tox = __fmul_rn(__fsub_rn(__uint_as_float(w0.x), s.ox), s.ix);
+        const float toy = __fmul_rn(__fsub_rn(__uint_as_float(w0.y), s.oy), s.iy);
+        const float toz = __fmul_rn(__fsub_rn(__uint_as_float(w0.z), s.oz), s.iz);
+        const float sx = __fmul_rn(exp_scale(meta & 0xFFu), s.ix);
+        const float sy = __fmul_rn(exp_scale((meta >> 8) & 0xFFu), s.iy);
+        const float sz = __fmul_rn(exp_scale((meta >> 16) & 0xFFu), s.iz);
         const uint32_t nx0 = negx ? w2.z : w1.x, nx1 = negx ? w2.w : w1.y;
         const uint32_t fx0 = negx ? w1.x : w2.z, fx1 = negx ? w1.y : w2.w;
         const uint32_t ny0 = negy ? w3.x : w1.z, ny1 = negy ? w3.y : w1.w;
         const uint32_t fy0 = negy ? w1.z : w3.x, fy1 = negy ? w1.w : w3.y;
         const uint32_t nz0 = negz ? w3.z : w2.x, nz1 = negz ? w3.w : w2.y;
         const uint32_t fz0 = negz ? w2.x : w3.z, fz1 = negz ? w2.y : w3.w;
-        unsigned long long key[8];
+        // 32-bit keys: ordered entry distance with its low 3 bits replaced by the slot. Truncation only
+        // lowers the stored distance, so pruning with it stays conservative.
+        uint32_t key[8];
 #pragma unroll
         for(int k = 0; k < 8; ++k)
         {
-            key[k] = ~0ull;
+            key[k] = 0xFFFFFFFFu;
             if((uint32_t)k < nch)
             {
                 const uint32_t wnx = k < 4 ? nx0 : nx1, wfx = k < 4 ? fx0 : fx1;
@@ -128,20 +156,20 @@ __device__ __forceinline__ trace_result trace_ray(const node8 *__restrict__ node
                 const float tnx = fmaf(qbyte(wnx, k), sx, tox), tfx = fmaf(qbyte(wfx, k), sx, tox);
                 const float tny = fmaf(qbyte(wny, k), sy, toy), tfy = fmaf(qbyte(wfy, k), sy, toy);
                 const float tnz = fmaf(qbyte(wnz, k), sz, toz), tfz = fmaf(qbyte(wfz, k), sz, toz);
-                const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-                const float tf = fminf(fminf(tfx, tfy), fminf(tfz, best_t));
-                if(tn <= tf) key[k] = ((unsigned long long)tenc(tn) << 32) | (unsigned long long)k;
+                const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, s.tmin));
+                const float tf = fminf(fminf(tfx, tfy), fminf(tfz, s.best_t));
+                if(tn <= tf) key[k] = (tenc(tn) & ~7u) | (uint32_t)k;
             }
         }
         sort8(key);
 #pragma unroll
         for(int h = 0; h < 8; ++h)
         {
-            if(key[h] == ~0ull || done) break;
-            const uint32_t k = (uint32_t)(key[h] & 7ull);
+            if(key[h] == 0xFFFFFFFFu || s.done) break;
+            const uint32_t k = key[h] & 7u;
             const uint32_t c = (k & 4u) ? sel4(w5, k & 3u) : sel4(w4, k & 3u);
             if(!(c & LEAF_BIT)) continue;
-            if(tdec((uint32_t)(key[h] >> 32)) > best_t) continue;
+            if(tdec(key[h] & ~7u) > s.best_t) continue;
             const uint32_t start = c & 0x07FFFFFFu, cnt = ((c >> 27) & 0xFu) + 1u;
             for(uint32_t ti = start; ti < start + cnt; ++ti)
             {
@@ -151,48 +179,68 @@ __device__ __forceinline__ trace_result trace_ray(const node8 *__restrict__ node
                 const int tcull = cull == CULL_BACK ||
                                   (cull == CULL_BACK_UNLESS_TWOSIDED && !(__float_as_uint(cc.z) & TRI_FLAG_TWOSIDED));
                 float t, u, v;
-                if(!tri_test(a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, cc.x, ox, oy, oz, dx, dy, dz, tcull, t, u, v))
+                if(!tri_test(a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, cc.x, s.ox, s.oy, s.oz, s.dx, s.dy, s.dz, tcull, t,
+                             u, v))
                     continue;
-                if(!(t > tmin && t < tmax)) continue;
+                if(!(t > s.tmin && t < s.tmax)) continue;
                 if(ANY)
                 {
-                    done = true;
+                    s.done = true;
                     break;
                 }
                 const uint32_t prim = __float_as_uint(cc.y);
-                if(t < best_t || (t == best_t && prim < best))
+                if(t < s.best_t || (t == s.best_t && prim < s.best))
                 {
-                    best_t = t;
-                    best = prim;
-                    bu = u;
-                    bv = v;
+                    s.best_t = t;
+                    s.best = prim;
+                    s.bu = u;
+                    s.bv = v;
                 }
             }
         }
-        if(done) break;
+        if(s.done) break;
 #pragma unroll
         for(int h = 7; h >= 0; --h)
         {
-            if(key[h] == ~0ull) continue;
-            const uint32_t k = (uint32_t)(key[h] & 7ull);
+            if(key[h] == 0xFFFFFFFFu) continue;
+            const uint32_t k = key[h] & 7u;
             const uint32_t c = (k & 4u) ? sel4(w5, k & 3u) : sel4(w4, k & 3u);
             if(c & LEAF_BIT) continue;
-            if(sp < (int)TRAVERSAL_STACK)
+            if(s.sp < (int)TRAVERSAL_STACK)
             {
-                st_node[sp] = c;
-                st_t[sp] = tdec((uint32_t)(key[h] >> 32));
-                ++sp;
+                s.st_node[s.sp] = c;
+                s.st_t[s.sp] = tdec(key[h] & ~7u);
+                ++s.sp;
             }
             else if(counters) { atomicOr(&counters[2], 1ull); }
         }
+        return true; // one node processed
     }
+    return false;
+}
+
+__device__ __forceinline__ trace_result ray_result(const ray_state &s)
+{
     trace_result r;
-    r.occluded = done;
-    r.prim = best;
-    r.t = best == VKG_MISS ? 0.f : best_t;
-    r.u = best == VKG_MISS ? 0.f : bu;
-    r.v = best == VKG_MISS ? 0.f : bv;
+    r.occluded = s.done;
+    r.prim = s.best;
+    r.t = s.best == VKG_MISS ? 0.f : s.best_t;
+    r.u = s.best == VKG_MISS ? 0.f : s.bu;
+    r.v = s.best == VKG_MISS ? 0.f : s.bv;
     return r;
+}
+
+template<bool ANY, bool STATS>
+__device__ __forceinline__ trace_result trace_ray(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
+                                                  float ox, float oy, float oz, float tmin, float dx, float dy,
+                                                  float dz, float tmax, int cull,
+                                                  unsigned long long &visits, unsigned long long &tests,
+                                                  unsigned long long *__restrict__ counters)
+{
+    ray_state s;
+    ray_init(s, ox, oy, oz, tmin, dx, dy, dz, tmax);
+    while(ray_step<ANY, STATS>(s, nodes, tris, cull, visits, tests, counters)) {}
+    return ray_result(s);
 }
 
 }// namespace vkg
