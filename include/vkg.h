@@ -329,6 +329,58 @@ vkg_status vkg_tracer_current_batch(const vkg_tracer *tracer, uint32_t *out);
 vkg_status vkg_tracer_statistics(vkg_tracer *tracer, vkg_tracer_stats *out);
 vkg_status vkg_tracer_destroy(vkg_tracer *tracer);
 
+
+/* ---- neural radiance cache (not in the reference) -------------------------------------------- *
+ * A small MLP (80 inputs -> 5 hidden layers of 64, ReLU -> RGB; BF16 weights and activations, FP32
+ * accumulation) over a multiresolution hash grid (position) and degree-4 spherical harmonics
+ * (outgoing direction, normal) plus roughness and albedo, trained online with a relative-L2 loss
+ * and Adam. Feature records are 13 floats: position xyz, outgoing direction xyz, normal xyz,
+ * roughness, albedo rgb. */
+typedef struct vkg_nrc vkg_nrc;
+typedef struct vkg_nrc_config
+{
+    uint32_t levels;          /* hash-grid levels (16) */
+    uint32_t log2_table_size; /* entries per level = 2^this (19) */
+    uint32_t base_resolution; /* coarsest grid resolution (16) */
+    uint32_t max_resolution;  /* finest grid resolution (2048) */
+    float learning_rate;      /* Adam (1e-2) */
+    float beta1, beta2, epsilon;
+    uint32_t seed;
+    float scene_min[3], scene_max[3]; /* positions are normalised to this box */
+    uint32_t batch_size;      /* training samples per optimiser step (65536) */
+    uint32_t train_paths;     /* training paths traced per frame (65536) */
+    uint32_t terminate_depth; /* rendering paths end in the cache at this surface interaction (2) */
+    uint32_t train_depth;     /* training targets are recorded at the first this-many interactions (4) */
+} vkg_nrc_config;
+typedef struct vkg_nrc_info_t
+{
+    uint32_t levels, table_size;
+    float growth;
+    uint32_t level_resolution[16];
+    uint32_t num_mlp_params;
+    uint64_t num_grid_params;
+    float *d_mlp_params;  /* FP32 master weights, layer l is [in][out] row-major */
+    float *d_grid_params; /* FP32 master hash-grid features [level][entry][2] */
+    float *d_mlp_grads;   /* gradients of the last vkg_nrc_backward (zeroed by vkg_nrc_adam_step) */
+    float *d_grid_grads;
+    uint32_t step;
+} vkg_nrc_info_t;
+vkg_status vkg_nrc_config_default(vkg_nrc_config *out);
+vkg_status vkg_nrc_create(vkg_ctx *ctx, const vkg_nrc_config *cfg, vkg_nrc **out);
+vkg_status vkg_nrc_destroy(vkg_nrc *nrc);
+vkg_status vkg_nrc_info(const vkg_nrc *nrc, vkg_nrc_info_t *out);
+/* prediction for n feature records -> n x 3 fp32 */
+vkg_status vkg_nrc_infer(vkg_nrc *nrc, const float *d_features, uint32_t n, float *d_rgb, void *stream);
+/* accumulate the gradients of the relative-L2 loss against n x 3 targets (no parameter update) */
+vkg_status vkg_nrc_backward(vkg_nrc *nrc, const float *d_features, const float *d_targets, uint32_t n, void *stream);
+/* one Adam update from the accumulated gradients (consumes them) */
+vkg_status vkg_nrc_adam_step(vkg_nrc *nrc, void *stream);
+/* backward + Adam; *h_loss (optional) receives the mean loss of the batch (synchronises) */
+vkg_status vkg_nrc_train_step(vkg_nrc *nrc, const float *d_features, const float *d_targets, uint32_t n,
+                              float *h_loss, void *stream);
+/* overwrite the FP32 master parameters (either may be NULL) */
+vkg_status vkg_nrc_load_params(vkg_nrc *nrc, const float *d_mlp, const float *d_grid, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

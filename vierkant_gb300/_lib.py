@@ -77,6 +77,21 @@ class vkg_scene_desc(C.Structure):
                 ("env_height", C.c_uint32), ("leaf_max", C.c_uint32)]
 
 
+class vkg_nrc_config(C.Structure):
+    _fields_ = [("levels", C.c_uint32), ("log2_table_size", C.c_uint32), ("base_resolution", C.c_uint32),
+                ("max_resolution", C.c_uint32), ("learning_rate", C.c_float), ("beta1", C.c_float),
+                ("beta2", C.c_float), ("epsilon", C.c_float), ("seed", C.c_uint32), ("scene_min", C.c_float * 3),
+                ("scene_max", C.c_float * 3), ("batch_size", C.c_uint32), ("train_paths", C.c_uint32),
+                ("terminate_depth", C.c_uint32), ("train_depth", C.c_uint32)]
+
+
+class vkg_nrc_info_t(C.Structure):
+    _fields_ = [("levels", C.c_uint32), ("table_size", C.c_uint32), ("growth", C.c_float),
+                ("level_resolution", C.c_uint32 * 16), ("num_mlp_params", C.c_uint32),
+                ("num_grid_params", C.c_uint64), ("d_mlp_params", C.c_void_p), ("d_grid_params", C.c_void_p),
+                ("d_mlp_grads", C.c_void_p), ("d_grid_grads", C.c_void_p), ("step", C.c_uint32)]
+
+
 class vkg_bvh_build_options(C.Structure):
     _fields_ = [("leaf_max", C.c_uint32)]
 
@@ -136,6 +151,15 @@ SIGNATURES = {
     "vkg_tracer_current_batch": (I32, [P, C.POINTER(U32)]),
     "vkg_tracer_statistics": (I32, [P, C.POINTER(vkg_tracer_stats)]),
     "vkg_tracer_destroy": (I32, [P]),
+    "vkg_nrc_config_default": (I32, [C.POINTER(vkg_nrc_config)]),
+    "vkg_nrc_create": (I32, [P, C.POINTER(vkg_nrc_config), C.POINTER(P)]),
+    "vkg_nrc_destroy": (I32, [P]),
+    "vkg_nrc_info": (I32, [P, C.POINTER(vkg_nrc_info_t)]),
+    "vkg_nrc_infer": (I32, [P, P, U32, P, P]),
+    "vkg_nrc_backward": (I32, [P, P, P, U32, P]),
+    "vkg_nrc_adam_step": (I32, [P, P]),
+    "vkg_nrc_train_step": (I32, [P, P, P, U32, C.POINTER(F32), P]),
+    "vkg_nrc_load_params": (I32, [P, P, P, P]),
 }
 
 _lib = None

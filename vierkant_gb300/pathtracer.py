@@ -67,6 +67,7 @@ class Scene:
               "vkg_scene_create")
         self.handle = h
         self.num_tris = idx.numel() // 3
+        ctx.adopt(self)
 
     def env_tables(self):
         w, a = C.c_void_p(), C.c_void_p()
@@ -75,9 +76,9 @@ class Scene:
         return w.value, a.value, W.value, H.value
 
     def close(self):
-        if getattr(self, "handle", None):
+        if getattr(self, "handle", None) and getattr(self.ctx, "handle", None):
             lib().vkg_scene_destroy(self.ctx.handle, self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
         try:
@@ -102,6 +103,7 @@ class PBRPathTracer:
         h = C.c_void_p()
         check(lib().vkg_tracer_create(ctx.handle, C.byref(info), C.byref(h)), ctx.handle, "vkg_tracer_create")
         self.handle = h
+        ctx.adopt(self)
 
     def _crop(self):
         s = self.settings
@@ -132,9 +134,9 @@ class PBRPathTracer:
         return st
 
     def close(self):
-        if getattr(self, "handle", None):
+        if getattr(self, "handle", None) and getattr(self.ctx, "handle", None):
             lib().vkg_tracer_destroy(self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
         try:

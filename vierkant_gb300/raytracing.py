@@ -8,6 +8,7 @@ work runs in libvkg's own kernels). Ray batches are float32 tensors of shape [N,
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 
 import torch
 
@@ -32,9 +33,20 @@ class Context:
         h = C.c_void_p()
         check(lib().vkg_ctx_create(device, C.byref(h)), None, "vkg_ctx_create")
         self.handle = h
+        self._children = weakref.WeakSet()
+
+    def adopt(self, obj):
+        """objects created on this context are released before it (the C API needs that order)"""
+        self._children.add(obj)
 
     def close(self):
         if getattr(self, "handle", None):
+            for child in list(self._children):
+                try:
+                    child.close()
+                except Exception:
+                    pass
+            torch.cuda.synchronize(self.device)
             lib().vkg_ctx_destroy(self.handle)
             self.handle = None
 
@@ -82,6 +94,7 @@ class BVH:
                                        C.c_void_p(idx.data_ptr()), idx.numel() // 3, C.byref(opts), C.byref(h),
                                        C.c_void_p(ctx.stream())), "vkg_bvh_build")
         self.handle = h
+        ctx.adopt(self)
 
     def info(self) -> vkg_bvh_info:
         inf = vkg_bvh_info()
@@ -89,9 +102,9 @@ class BVH:
         return inf
 
     def close(self):
-        if getattr(self, "handle", None):
+        if getattr(self, "handle", None) and getattr(self.ctx, "handle", None):
             lib().vkg_bvh_destroy(self.ctx.handle, self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
         try:
