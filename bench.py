@@ -231,6 +231,9 @@ def run_ours(args):
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_baseline(sc, batch, budget_s=args.cpu_seconds)
+    pt_block = None
+    if rank == 0 and not args.no_pt:
+        pt_block = path_tracer_block(ctx, frames=args.nrc_frames)
 
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 1), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
@@ -246,11 +249,102 @@ def run_ours(args):
                 "gpu_launches": args.steps, "roofline": roofline, "clocks": clk}
         if cpu is not None:
             line["cpu_baseline"] = cpu
+        if pt_block is not None:
+            line["path_tracer"] = pt_block
         print(json.dumps(line), flush=True)
     bvh.close()
     ctx.close()
     if ws > 1:
         dist.destroy_process_group()
+
+
+def _lum(a):
+    return 0.2126 * a[..., 0] + 0.7152 * a[..., 1] + 0.0722 * a[..., 2]
+
+
+def _crop_error(img, golden):
+    """(RMSE of the luminance, relative bias) of an image crop against the FP64 oracle fixture"""
+    import numpy as np
+    ref = golden["mean"].astype(np.float64)
+    x0, y0, w, h = (int(v) for v in golden["crop"])
+    c = img[y0:y0 + h, x0:x0 + w].astype(np.float64)
+    return math.sqrt(float(np.mean((_lum(c) - _lum(ref)) ** 2))), float((c.sum() - ref.sum()) / ref.sum())
+
+
+def path_tracer_block(ctx, frames=256):
+    """The radiance estimator on the same scene: the plain tracer at 1280x720 x 64 spp (samples/s,
+    Mrays/s, RMSE / bias against the FP64 oracle crop), and the equal-RMSE comparison at 1920x1080:
+    GPU time for the plain tracer's 64-spp image vs the radiance-cache tracer (1 spp per frame, trained
+    online) to reach the same crop RMSE. Times are CUDA-event totals of the renders (training included)."""
+    import numpy as np
+    from vierkant_gb300 import geometry
+    from vierkant_gb300.nrc import cache_for_scene
+    from vierkant_gb300.pathtracer import PBRPathTracer, Scene, procedural_sky, sun_direction
+
+    g720 = np.load(ROOT / "tests" / "golden" / "pt_oracle_crop.npz")
+    g1080 = np.load(ROOT / "tests" / "golden" / "pt_oracle_crop_1080.npz")
+    sc = geometry.cornell_scene(SEED, 2, 64, 16)
+    env = procedural_sky(ctx, 2048, 1024, sun_direction(), 5e4, 3.8e-5)
+    scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], sc["materials"], env)
+
+    def settings(spp, w, h):
+        s = PBRPathTracer.default_settings()
+        s.num_samples, s.max_trace_depth, s.rr_start_depth = spp, 6, 3
+        s.resolution[0], s.resolution[1] = w, h
+        return s
+
+    out = {}
+    cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, 1280, 720)
+    pt = PBRPathTracer(ctx, seed=SEED, settings=settings(64, 1280, 720))
+    pt.render_scene(scene, cam)
+    pt.reset_accumulator()
+    img = pt.render_scene(scene, cam).cpu().numpy()
+    st = pt.statistics()
+    rmse, bias = _crop_error(img, g720)
+    rays = st.extension_rays + st.shadow_rays
+    out["plain_720p_64spp"] = {"ms": round(st.total_ms, 2), "samples_per_s": round(st.paths / st.total_ms * 1e3),
+                               "mrays_per_s": round(rays / st.total_ms / 1e3, 1), "rays": int(rays),
+                               "rmse": round(rmse, 4), "bias": round(bias, 5),
+                               "oracle": "FP64 4096 spp, 128x128 crop at (576, 528)"}
+    pt.close()
+
+    cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, 1920, 1080)
+    pt = PBRPathTracer(ctx, seed=SEED, settings=settings(64, 1920, 1080))
+    pt.render_scene(scene, cam)
+    pt.reset_accumulator()
+    img = pt.render_scene(scene, cam).cpu().numpy()
+    st = pt.statistics()
+    target, pbias = _crop_error(img, g1080)
+    plain_ms = st.total_ms
+    pt.close()
+
+    pt = PBRPathTracer(ctx, seed=SEED + 1, settings=settings(1, 1920, 1080))
+    cache = cache_for_scene(ctx, scene)
+    pt.attach_cache(cache)
+    tot = render = train = 0.0
+    reached = None
+    rmse = bias = None
+    for f in range(frames):
+        img = pt.render_scene(scene, cam)
+        st = pt.statistics()
+        tot += st.total_ms
+        render += st.raytrace_ms
+        train += st.train_ms
+        rmse, bias = _crop_error(img.cpu().numpy(), g1080)
+        if reached is None and rmse <= target:
+            reached = {"frames": f + 1, "ms": round(tot, 2)}
+    pt.close()
+    cache.close()
+    scene.close()
+    out["equal_rmse_1080p"] = {
+        "rmse_target": round(target, 4), "plain_64spp_ms": round(plain_ms, 2), "plain_bias": round(pbias, 5),
+        "nrc_reached": reached, "nrc_vs_plain_time": round(reached["ms"] / plain_ms, 3) if reached else None,
+        "nrc_frames": frames, "nrc_ms_total": round(tot, 2), "nrc_ms_per_frame": round(tot / frames, 3),
+        "nrc_render_ms_per_frame": round(render / frames, 3), "nrc_train_ms_per_frame": round(train / frames, 3),
+        "nrc_rmse_final": round(rmse, 4), "nrc_bias_final": round(bias, 5),
+        "oracle": "FP64 4096 spp, 128x128 crop at (896, 824)",
+        "protocol": "1 spp per frame, 65,536 training paths per frame, terminate after 2 bounces"}
+    return out
 
 
 def cpu_reference_lib():
@@ -336,6 +430,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-pt", action="store_true", help="skip the path-tracer / radiance-cache block")
+    ap.add_argument("--nrc-frames", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("note: timing rules want >= 3 warm-up steps", file=sys.stderr)

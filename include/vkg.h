@@ -308,6 +308,9 @@ typedef struct vkg_tracer_stats
     uint64_t shadow_rays;
     uint32_t batch;
     uint32_t pad;
+    double train_ms;         /* radiance-cache training inside total_ms (0 without a cache) */
+    uint64_t cache_queries;  /* rendering paths that ended in the radiance cache */
+    uint64_t train_records;  /* training records (path vertices with targets) of the last render */
 } vkg_tracer_stats;
 
 typedef struct vkg_tracer vkg_tracer;
@@ -351,6 +354,7 @@ typedef struct vkg_nrc_config
     uint32_t train_paths;     /* training paths traced per frame (65536) */
     uint32_t terminate_depth; /* rendering paths end in the cache at this surface interaction (2) */
     uint32_t train_depth;     /* training targets are recorded at the first this-many interactions (4) */
+    uint32_t train_steps;     /* optimiser steps per frame; 0: ceil(train_paths * train_depth / batch_size) */
 } vkg_nrc_config;
 typedef struct vkg_nrc_info_t
 {
@@ -380,6 +384,14 @@ vkg_status vkg_nrc_train_step(vkg_nrc *nrc, const float *d_features, const float
                               float *h_loss, void *stream);
 /* overwrite the FP32 master parameters (either may be NULL) */
 vkg_status vkg_nrc_load_params(vkg_nrc *nrc, const float *d_mlp, const float *d_grid, void *stream);
+/* Attach a radiance cache to a path tracer (NULL detaches; the cache must outlive its use). With a
+ * cache attached, vkg_tracer_render ends every rendering path at its terminate_depth-th surface
+ * interaction in the cache: the path adds throughput x (emission + predicted outgoing radiance)
+ * and stops. After the frame it traces train_paths training paths through random pixels of the
+ * crop window with the plain estimator (up to max_trace_depth, Russian roulette as configured),
+ * records their first train_depth interactions together with the radiance that followed each,
+ * and runs train_steps optimiser steps on batches of batch_size records, all on `stream`. */
+vkg_status vkg_tracer_attach_cache(vkg_tracer *tracer, vkg_nrc *cache);
 
 #ifdef __cplusplus
 }

@@ -67,7 +67,8 @@ class vkg_tracer_create_info(C.Structure):
 class vkg_tracer_stats(C.Structure):
     _fields_ = [("raytrace_ms", C.c_double), ("total_ms", C.c_double), ("paths", C.c_uint64),
                 ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("batch", C.c_uint32),
-                ("pad", C.c_uint32)]
+                ("pad", C.c_uint32), ("train_ms", C.c_double), ("cache_queries", C.c_uint64),
+                ("train_records", C.c_uint64)]
 
 
 class vkg_scene_desc(C.Structure):
@@ -82,7 +83,7 @@ class vkg_nrc_config(C.Structure):
                 ("max_resolution", C.c_uint32), ("learning_rate", C.c_float), ("beta1", C.c_float),
                 ("beta2", C.c_float), ("epsilon", C.c_float), ("seed", C.c_uint32), ("scene_min", C.c_float * 3),
                 ("scene_max", C.c_float * 3), ("batch_size", C.c_uint32), ("train_paths", C.c_uint32),
-                ("terminate_depth", C.c_uint32), ("train_depth", C.c_uint32)]
+                ("terminate_depth", C.c_uint32), ("train_depth", C.c_uint32), ("train_steps", C.c_uint32)]
 
 
 class vkg_nrc_info_t(C.Structure):
@@ -151,6 +152,7 @@ SIGNATURES = {
     "vkg_tracer_current_batch": (I32, [P, C.POINTER(U32)]),
     "vkg_tracer_statistics": (I32, [P, C.POINTER(vkg_tracer_stats)]),
     "vkg_tracer_destroy": (I32, [P]),
+    "vkg_tracer_attach_cache": (I32, [P, P]),
     "vkg_nrc_config_default": (I32, [C.POINTER(vkg_nrc_config)]),
     "vkg_nrc_create": (I32, [P, C.POINTER(vkg_nrc_config), C.POINTER(P)]),
     "vkg_nrc_destroy": (I32, [P]),

@@ -16,11 +16,12 @@
 struct vkg_nrc
 {
     vkg_ctx *ctx = nullptr;
+    vkg_nrc_config cfg{};
     vkg::nrc::grid_config gc{};
     uint32_t table = 0;          // entries per level
     size_t ngrid = 0;            // grid parameters (levels * table * 2)
     float lr = 1e-2f, b1 = 0.9f, b2 = 0.99f, eps = 1e-15f;
-    uint32_t step = 0;
+    uint32_t *d_state = nullptr; // [0] Adam steps taken, [1] 1 if the current step has records
     float *grid = nullptr, *grid_g = nullptr, *grid_m = nullptr, *grid_v = nullptr;
     __half2 *grid_h = nullptr;
     float *w = nullptr, *w_g = nullptr, *w_m = nullptr, *w_v = nullptr;
@@ -508,30 +509,53 @@ __global__ void k_grid_backward(const float *__restrict__ feats, uint32_t n, con
     }
 }
 
-// Adam (Kingma & Ba 2015) with bias correction; gradients are consumed (zeroed). Each thread updates
-// one pair of parameters so the FP16 copy (feature pairs) is written from values it owns.
+// An optimiser step starts on the device: it counts (and runs) only if its batch has records, so a
+// frame whose training paths all escaped leaves the parameters and the moments untouched.
+__global__ void k_adam_begin(const uint32_t *__restrict__ d_n, uint32_t *__restrict__ state)
+{
+    const bool active = d_n == nullptr || *d_n > 0;
+    state[1] = active ? 1u : 0u;
+    if(active) state[0] += 1u;
+}
+
+// Adam (Kingma & Ba 2015) with bias correction 1 - beta^t, t the device step count; gradients are
+// consumed (zeroed). Each thread updates one pair of parameters so the FP16 copy (feature pairs) is
+// written from values it owns.
 __global__ void k_adam(float *__restrict__ p, float *__restrict__ g, float *__restrict__ m, float *__restrict__ v,
-                       size_t n, float lr, float b1, float b2, float eps, float c1, float c2,
+                       size_t n, float lr, float b1, float b2, float eps, const uint32_t *__restrict__ state,
                        __half2 *__restrict__ half_copy)
+{
+    if(state[1] == 0) return;
+    const float t = (float)state[0];
+    const float c1 = 1.f - powf(b1, t), c2 = 1.f - powf(b2, t);
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for(size_t i2 = (size_t)blockIdx.x * blockDim.x + threadIdx.x; 2 * i2 < n; i2 += stride)
+    {
+        const float2 gi = reinterpret_cast<const float2 *>(g)[i2];
+        float2 mi = reinterpret_cast<const float2 *>(m)[i2], vi = reinterpret_cast<const float2 *>(v)[i2];
+        float2 pi = reinterpret_cast<const float2 *>(p)[i2];
+        mi.x = b1 * mi.x + (1.f - b1) * gi.x;
+        mi.y = b1 * mi.y + (1.f - b1) * gi.y;
+        vi.x = b2 * vi.x + (1.f - b2) * gi.x * gi.x;
+        vi.y = b2 * vi.y + (1.f - b2) * gi.y * gi.y;
+        pi.x = pi.x - lr * (mi.x / c1) / (sqrtf(vi.x / c2) + eps);
+        pi.y = pi.y - lr * (mi.y / c1) / (sqrtf(vi.y / c2) + eps);
+        reinterpret_cast<float2 *>(m)[i2] = mi;
+        reinterpret_cast<float2 *>(v)[i2] = vi;
+        reinterpret_cast<float2 *>(p)[i2] = pi;
+        reinterpret_cast<float2 *>(g)[i2] = make_float2(0.f, 0.f);
+        if(half_copy) half_copy[i2] = __floats2half2_rn(pi.x, pi.y);
+    }
+}
+
+// FP16 copy of the FP32 master grid
+__global__ void k_to_half(const float *__restrict__ p, size_t n, __half2 *__restrict__ half_copy)
 {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for(size_t i2 = (size_t)blockIdx.x * blockDim.x + threadIdx.x; 2 * i2 < n; i2 += stride)
     {
-        float out[2];
-#pragma unroll
-        for(int q = 0; q < 2; ++q)
-        {
-            const size_t i = 2 * i2 + q;
-            const float gi = g[i];
-            const float mi = b1 * m[i] + (1.f - b1) * gi;
-            const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
-            m[i] = mi;
-            v[i] = vi;
-            out[q] = p[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
-            p[i] = out[q];
-            g[i] = 0.f;
-        }
-        if(half_copy) half_copy[i2] = __floats2half2_rn(out[0], out[1]);
+        const float2 v = reinterpret_cast<const float2 *>(p)[i2];
+        half_copy[i2] = __floats2half2_rn(v.x, v.y);
     }
 }
 
@@ -643,16 +667,32 @@ vkg_status nrc_backward(vkg_nrc *c, const float *feats, const float *targets, ui
     return cuda_check(c->ctx, cudaGetLastError(), "nrc backward");
 }
 
-vkg_status nrc_adam(vkg_nrc *c, cudaStream_t st)
+// d_n: optional device-side record count of the batch; an empty batch takes no step
+vkg_status nrc_adam(vkg_nrc *c, const uint32_t *d_n, cudaStream_t st)
 {
-    c->step += 1;
-    const float c1 = 1.f - powf(c->b1, (float)c->step), c2 = 1.f - powf(c->b2, (float)c->step);
     const uint32_t blocks = (uint32_t)c->ctx->num_sms * 8;
-    k_adam<<<blocks, 256, 0, st>>>(c->grid, c->grid_g, c->grid_m, c->grid_v, c->ngrid, c->lr, c->b1, c->b2, c->eps, c1, c2,
-                                   c->grid_h);
-    k_adam<<<64, 256, 0, st>>>(c->w, c->w_g, c->w_m, c->w_v, NPARAM, c->lr, c->b1, c->b2, c->eps, c1, c2, nullptr);
+    k_adam_begin<<<1, 1, 0, st>>>(d_n, c->d_state);
+    k_adam<<<blocks, 256, 0, st>>>(c->grid, c->grid_g, c->grid_m, c->grid_v, c->ngrid, c->lr, c->b1, c->b2, c->eps,
+                                   c->d_state, c->grid_h);
+    k_adam<<<64, 256, 0, st>>>(c->w, c->w_g, c->w_m, c->w_v, NPARAM, c->lr, c->b1, c->b2, c->eps, c->d_state, nullptr);
     k_pack<<<(NFRAG + 255) / 256, 256, 0, st>>>(c->w, c->frag, c->fragT);
     return cuda_check(c->ctx, cudaGetLastError(), "nrc adam");
+}
+
+const vkg_nrc_config &nrc_config(const vkg_nrc *c) { return c->cfg; }
+
+vkg_status nrc_predict(vkg_nrc *c, const float *feats, uint32_t n, const uint32_t *d_n, uint32_t *X, float *Y,
+                       cudaStream_t st)
+{
+    if(vkg_status s = nrc_encode(c, feats, n, d_n, X, st); s != VKG_OK) return s;
+    return nrc_forward(c, X, n, d_n, Y, st);
+}
+
+vkg_status nrc_train(vkg_nrc *c, const float *feats, const float *targets, uint32_t n, const uint32_t *d_n,
+                     cudaStream_t st)
+{
+    if(vkg_status s = nrc_backward(c, feats, targets, n, d_n, st); s != VKG_OK) return s;
+    return nrc_adam(c, d_n, st);
 }
 
 }// namespace nrc
@@ -682,6 +722,7 @@ vkg_status vkg_nrc_config_default(vkg_nrc_config *c)
     c->train_paths = 65536;
     c->terminate_depth = 2;
     c->train_depth = 4;
+    c->train_steps = 0;
     return VKG_OK;
 }
 
@@ -694,8 +735,11 @@ vkg_status vkg_nrc_create(vkg_ctx *ctx, const vkg_nrc_config *cfg, vkg_nrc **out
        cfg->base_resolution < 2 || cfg->max_resolution < cfg->base_resolution)
         return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_nrc_create: invalid hash-grid configuration");
     if(vkg_status s = bind_device(ctx); s != VKG_OK) return s;
+    if(cfg->batch_size == 0 || cfg->batch_size > (1u << 24) || cfg->train_paths > (1u << 24) || cfg->train_depth > 16)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_nrc_create: invalid training configuration");
     auto *c = new vkg_nrc();
     c->ctx = ctx;
+    c->cfg = *cfg;
     c->gc.levels = cfg->levels;
     c->gc.log2_t = cfg->log2_table_size;
     c->gc.base_res = cfg->base_resolution;
@@ -730,6 +774,7 @@ vkg_status vkg_nrc_create(vkg_ctx *ctx, const vkg_nrc_config *cfg, vkg_nrc **out
     al((void **)&c->frag, NFRAG * 8);
     al((void **)&c->fragT, NFRAG * 8);
     al((void **)&c->loss, 4 * 4);
+    al((void **)&c->d_state, 2 * sizeof(uint32_t));
     if(e == cudaSuccess)
     {
         for(void *p: {(void *)c->grid_g, (void *)c->grid_m, (void *)c->grid_v})
@@ -737,6 +782,7 @@ vkg_status vkg_nrc_create(vkg_ctx *ctx, const vkg_nrc_config *cfg, vkg_nrc **out
         for(void *p: {(void *)c->w_g, (void *)c->w_m, (void *)c->w_v})
             if(e == cudaSuccess) e = cudaMemset(p, 0, NPARAM * 4);
         if(e == cudaSuccess) e = cudaMemset(c->loss, 0, 16);
+        if(e == cudaSuccess) e = cudaMemset(c->d_state, 0, 2 * sizeof(uint32_t));
     }
     if(e != cudaSuccess)
     {
@@ -761,7 +807,8 @@ vkg_status vkg_nrc_destroy(vkg_nrc *c)
     if(c->ctx) bind_device(c->ctx);
     for(void *p: {(void *)c->grid, (void *)c->grid_g, (void *)c->grid_m, (void *)c->grid_v, (void *)c->grid_h,
                   (void *)c->w, (void *)c->w_g, (void *)c->w_m, (void *)c->w_v, (void *)c->frag, (void *)c->fragT,
-                  (void *)c->loss, (void *)c->X, (void *)c->H, (void *)c->G, (void *)c->Y, (void *)c->dXg})
+                  (void *)c->loss, (void *)c->d_state, (void *)c->X, (void *)c->H, (void *)c->G, (void *)c->Y,
+                  (void *)c->dXg})
         cudaFree(p);
     delete c;
     return VKG_OK;
@@ -781,7 +828,8 @@ vkg_status vkg_nrc_info(const vkg_nrc *c, vkg_nrc_info_t *out)
     out->d_grid_params = c->grid;
     out->d_mlp_grads = c->w_g;
     out->d_grid_grads = c->grid_g;
-    out->step = c->step;
+    if(vkg_status s = bind_device(c->ctx); s != VKG_OK) return s;
+    VKG_TRY_CUDA(c->ctx, cudaMemcpy(&out->step, c->d_state, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     return VKG_OK;
 }
 
@@ -809,7 +857,7 @@ vkg_status vkg_nrc_adam_step(vkg_nrc *c, void *stream)
 {
     if(!c) return VKG_ERR_INVALID_ARGUMENT;
     if(vkg_status s = bind_device(c->ctx); s != VKG_OK) return s;
-    return nrc_adam(c, static_cast<cudaStream_t>(stream));
+    return nrc_adam(c, nullptr, static_cast<cudaStream_t>(stream));
 }
 
 vkg_status vkg_nrc_train_step(vkg_nrc *c, const float *d_feats, const float *d_targets, uint32_t n, float *h_loss,
@@ -820,7 +868,7 @@ vkg_status vkg_nrc_train_step(vkg_nrc *c, const float *d_feats, const float *d_t
     if(vkg_status s = bind_device(c->ctx); s != VKG_OK) return s;
     if(h_loss) VKG_TRY_CUDA(c->ctx, cudaMemsetAsync(c->loss, 0, 4, st));
     if(vkg_status s = nrc_backward(c, d_feats, d_targets, n, nullptr, st); s != VKG_OK) return s;
-    if(vkg_status s = nrc_adam(c, st); s != VKG_OK) return s;
+    if(vkg_status s = nrc_adam(c, nullptr, st); s != VKG_OK) return s;
     if(h_loss)
     {
         VKG_TRY_CUDA(c->ctx, cudaMemcpyAsync(h_loss, c->loss, 4, cudaMemcpyDeviceToHost, st));
@@ -838,9 +886,8 @@ vkg_status vkg_nrc_load_params(vkg_nrc *c, const float *d_mlp, const float *d_gr
     if(d_grid)
     {
         VKG_TRY_CUDA(c->ctx, cudaMemcpyAsync(c->grid, d_grid, c->ngrid * 4, cudaMemcpyDeviceToDevice, st));
-        // refresh the FP16 copy: an Adam step with zero learning rate rewrites it without moving anything
-        k_adam<<<c->ctx->num_sms * 8, 256, 0, st>>>(c->grid, c->grid_g, c->grid_m, c->grid_v, c->ngrid, 0.f, 1.f, 1.f,
-                                                     1.f, 1.f, 1.f, c->grid_h);
+        // refresh the FP16 copy the encoder reads
+        k_to_half<<<c->ctx->num_sms * 8, 256, 0, st>>>(c->grid, c->ngrid, c->grid_h);
     }
     k_pack<<<(NFRAG + 255) / 256, 256, 0, st>>>(c->w, c->frag, c->fragT);
     return cuda_check(c->ctx, cudaGetLastError(), "vkg_nrc_load_params");

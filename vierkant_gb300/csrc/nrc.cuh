@@ -73,5 +73,17 @@ __host__ __device__ inline uint32_t level_res(const grid_config &g, uint32_t l)
     return (uint32_t)r;
 }
 
+// entry points for the path tracer. n is the capacity of the arrays; d_n (optional) points to the
+// device-side count (<= n) of valid records, so queue lengths never travel to the host.
+const vkg_nrc_config &nrc_config(const vkg_nrc *c);
+// encoded inputs of n records: n x 40 u32 (80 BF16 values per record)
+constexpr size_t ENCODED_BYTES = IN * 2;
+// predictions (n x 3 fp32) for n feature records (n x FEAT fp32); X is caller-owned scratch of n x ENCODED_BYTES
+vkg_status nrc_predict(vkg_nrc *c, const float *feats, uint32_t n, const uint32_t *d_n, uint32_t *X, float *Y,
+                       cudaStream_t st);
+// one optimiser step (backward + Adam) on n records; records past *d_n contribute nothing
+vkg_status nrc_train(vkg_nrc *c, const float *feats, const float *targets, uint32_t n, const uint32_t *d_n,
+                     cudaStream_t st);
+
 }// namespace nrc
 }// namespace vkg

@@ -20,6 +20,16 @@
 // RNG: PCG32 per path, initstate = create-info seed, initseq = (batch << 40) ^ (sample * pixels +
 // pixel); the camera jitter takes 2 draws, every segment exactly 8 (lobe, 2 BSDF, 4 environment,
 // roulette) whatever branch is taken.
+//
+// With a radiance cache attached (vkg_tracer_attach_cache) the same kernels run in two more modes:
+//   rendering  the shade kernel turns the terminate_depth-th interaction of every path into a cache
+//              query (features + throughput); one batched inference resolves all queries of the wave;
+//   training   train_paths paths through random pixels (initseq tagged with bit 62, first draw picks
+//              the pixel) run the plain estimator and record their first train_depth interactions
+//              (features, throughput on arrival, radiance gathered so far including the emission
+//              there); afterwards target_k = (L_path - L_k) / throughput_k, the radiance that left
+//              interaction k towards the previous vertex, feeds train_steps optimiser steps.
+#include "nrc.cuh"
 #include "pathtrace.cuh"
 #include "traverse.cuh"
 
@@ -56,11 +66,23 @@ struct vkg_tracer
     float4 *radiance = nullptr;
     float *sum = nullptr;
     float *accum = nullptr;
-    uint32_t *counters = nullptr;           // [0..1] queue lengths, [2] shadow queue length
-    unsigned long long *totals = nullptr;   // [0] extension rays, [1] shadow rays
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    uint32_t *counters = nullptr;           // [0..1] queue lengths, [2] shadow queue length, [3] cache queries,
+                                            // [4] training records, [5] training batch length
+    unsigned long long *totals = nullptr;   // [0] extension rays, [1] shadow rays, [2] cache queries
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_train = nullptr;
     uint64_t last_paths = 0;
     bool rendered = false;
+    bool trained = false;
+    // radiance cache
+    vkg_nrc *cache = nullptr;
+    size_t q_cap = 0, rec_cap = 0;
+    float *q_feat = nullptr;       // cache queries: q_cap x 13
+    float4 *q_beta = nullptr;      // throughput xyz, path id in w
+    uint32_t *q_x = nullptr;       // encoded queries
+    float *q_y = nullptr;          // predictions q_cap x 3
+    float4 *rec = nullptr;         // training records: rec_cap x 5 float4, path-major
+    uint32_t *vcount = nullptr;    // recorded interactions per training path
+    float *t_feat = nullptr, *t_target = nullptr; // compacted training set: rec_cap x 13, rec_cap x 3
 };
 
 namespace vkg
@@ -85,11 +107,34 @@ struct pt_params
     float max_path_beta;
     uint64_t seed, batch;
     uint32_t s0; // first sample index of the wave
+    uint32_t term_depth;  // with a cache: interaction at which rendering paths become cache queries
+    uint32_t rec_depth;   // interactions recorded per training path
+    uint32_t train_base;  // paths [train_base, train_base + train_paths) of the wave are training paths
+    uint32_t train_paths;
 };
+
+// the shade kernel's two modes
+enum : int
+{
+    MODE_PLAIN = 0,
+    MODE_CACHE = 1
+};
+
+struct cache_io
+{
+    float *q_feat;
+    float4 *q_beta;
+    uint32_t *q_count;
+    float4 *rec;
+    uint32_t *vcount;
+};
+
+constexpr int REC_F4 = 5; // float4 per training record
 
 __device__ __forceinline__ uint64_t path_seq(const pt_params &P, uint32_t pid)
 {
-    uint64_t g = (uint64_t)P.s0 * P.npix + pid; // = sample * npix + pixel
+    if(pid >= P.train_base) return ((P.batch << 40) ^ (uint64_t)(pid - P.train_base)) ^ (1ull << 62);
+    const uint64_t g = (uint64_t)P.s0 * P.npix + pid; // = sample * npix + pixel
     return (P.batch << 40) ^ g;
 }
 
@@ -108,14 +153,23 @@ __device__ __forceinline__ uint32_t warp_push(uint32_t *count, bool pred)
 __global__ void __launch_bounds__(PT_THREADS)
         k_pt_generate(pt_params P, uint32_t n, vkg_ray *__restrict__ q_ray, uint32_t *__restrict__ q_pid,
                       uint64_t *__restrict__ rng, float4 *__restrict__ beta_pdf, float4 *__restrict__ radiance,
-                      uint32_t *__restrict__ counters)
+                      uint32_t *__restrict__ counters, uint32_t *__restrict__ vcount)
 {
     const uint32_t stride = gridDim.x * blockDim.x;
     for(uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride)
     {
-        const uint32_t pix = p % P.npix;
-        const uint32_t x = P.cx0 + pix % P.cw, y = P.cy0 + pix / P.cw;
         pcg32 g = pcg32_seed(P.seed, path_seq(P, p));
+        uint32_t pix = p % P.npix;
+        if(p >= P.train_base)
+        {
+            // training path k: a random pixel of the k-th of train_paths equal runs of the window
+            // (stratified, so neighbouring lanes trace neighbouring pixels)
+            const uint64_t k = p - P.train_base, lo = k * P.npix / P.train_paths,
+                           hi = (k + 1) * P.npix / P.train_paths;
+            pix = (uint32_t)(lo + (hi > lo ? pcg32_next(g) % (uint32_t)(hi - lo) : 0u));
+            vcount[k] = 0;
+        }
+        const uint32_t x = P.cx0 + pix % P.cw, y = P.cy0 + pix / P.cw;
         const float jx = u01(pcg32_next(g)), jy = u01(pcg32_next(g));
         const vkg_camera &c = P.cam;
         const float sx = fdiv(fadd((float)x, jx), (float)c.width);
@@ -155,13 +209,15 @@ __global__ void __launch_bounds__(PT_THREADS)
     }
 }
 
+template<int MODE>
 __global__ void __launch_bounds__(PT_THREADS)
         k_pt_shade(pt_params P, uint32_t depth, const vkg_ray *__restrict__ in_ray,
                    const uint32_t *__restrict__ in_pid, const vkg_hit *__restrict__ hits,
                    const uint32_t *__restrict__ in_count, vkg_ray *__restrict__ out_ray,
                    uint32_t *__restrict__ out_pid, uint32_t *__restrict__ out_count, vkg_ray *__restrict__ s_ray,
                    uint32_t *__restrict__ s_pid, float4 *__restrict__ s_contrib, uint32_t *__restrict__ s_count,
-                   uint64_t *__restrict__ rng, float4 *__restrict__ beta_pdf, float4 *__restrict__ radiance)
+                   uint64_t *__restrict__ rng, float4 *__restrict__ beta_pdf, float4 *__restrict__ radiance,
+                   cache_io io)
 {
     const uint32_t n = *in_count;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -169,9 +225,10 @@ __global__ void __launch_bounds__(PT_THREADS)
     {
         const uint32_t i = base + threadIdx.x;
         const bool active = i < n;
-        bool push_ext = false, push_shadow = false;
+        bool push_ext = false, push_shadow = false, push_query = false;
         float3 P0 = f3(0.f, 0.f, 0.f), ndir = P0, sdir = P0, N = P0;
-        float3 contrib = P0;
+        float3 contrib = P0, qbeta = P0, albedo = P0, vq = P0;
+        float rough = 0.f;
         uint32_t pid = 0;
         if(active)
         {
@@ -225,8 +282,33 @@ __global__ void __launch_bounds__(PT_THREADS)
                 m.roughness = mt.roughness;
                 m.metalness = mt.metalness;
                 L = L + beta * f3(mt.emission[0], mt.emission[1], mt.emission[2]);
+                if constexpr(MODE == MODE_CACHE)
+                {
+                    if(pid < P.train_base && depth == P.term_depth)
+                    {
+                        push_query = true;
+                        qbeta = beta;
+                        vq = V;
+                        albedo = m.base;
+                        rough = m.roughness;
+                    }
+                }
+                if constexpr(MODE == MODE_CACHE)
+                {
+                    if(pid >= P.train_base && depth < P.rec_depth)
+                    {
+                        const uint32_t k = pid - P.train_base;
+                        float4 *r = io.rec + ((size_t)k * P.rec_depth + depth) * REC_F4;
+                        r[0] = make_float4(P0.x, P0.y, P0.z, V.x);
+                        r[1] = make_float4(V.y, V.z, N.x, N.y);
+                        r[2] = make_float4(N.z, m.roughness, m.base.x, m.base.y);
+                        r[3] = make_float4(m.base.z, beta.x, beta.y, beta.z);
+                        r[4] = make_float4(L.x, L.y, L.z, 0.f);
+                        io.vcount[k] = depth + 1;
+                    }
+                }
                 // next-event estimation against the environment (mis_weight_nee, direct_lighting.slang:239-244)
-                if(P.mis_mode != 2)
+                if(!push_query && P.mis_mode != 2)
                 {
                     float pdf_env;
                     uint32_t texel;
@@ -250,7 +332,7 @@ __global__ void __launch_bounds__(PT_THREADS)
                 }
                 // BSDF sample (sample_disney) and throughput
                 const bsdf_sample bs = sample_bsdf(m, N, V, u[0], u[1], u[2]);
-                bool alive = bs.pdf > 0.f;
+                bool alive = bs.pdf > 0.f && !push_query;
                 if(alive)
                 {
                     const float cost = fabsf(dot(N, bs.dir));
@@ -306,6 +388,22 @@ __global__ void __launch_bounds__(PT_THREADS)
             s_pid[ps] = pid;
             s_contrib[ps] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
         }
+        if constexpr(MODE == MODE_CACHE)
+        {
+            const uint32_t pq = warp_push(io.q_count, push_query);
+            if(push_query)
+            {
+                // feature record: position, outgoing direction, normal, roughness, albedo
+                float *f = io.q_feat + (size_t)nrc::FEAT * pq;
+                const float3 V = vq;
+                f[0] = P0.x; f[1] = P0.y; f[2] = P0.z;
+                f[3] = V.x; f[4] = V.y; f[5] = V.z;
+                f[6] = N.x; f[7] = N.y; f[8] = N.z;
+                f[9] = rough;
+                f[10] = albedo.x; f[11] = albedo.y; f[12] = albedo.z;
+                io.q_beta[pq] = make_float4(qbeta.x, qbeta.y, qbeta.z, __uint_as_float(pid));
+            }
+        }
     }
 }
 
@@ -348,6 +446,73 @@ __global__ void k_pt_tally(const uint32_t *__restrict__ ext_count, const uint32_
 {
     totals[0] += *ext_count;
     totals[1] += *s_count;
+}
+
+// rendering with a cache: path radiance += throughput x prediction (negative outputs clamped)
+__global__ void k_cache_resolve(const float4 *__restrict__ q_beta, const float *__restrict__ Y,
+                                const uint32_t *__restrict__ count, float4 *__restrict__ radiance,
+                                unsigned long long *__restrict__ totals)
+{
+    const uint32_t n = *count;
+    if(blockIdx.x == 0 && threadIdx.x == 0) totals[2] += n;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const float4 b = q_beta[i];
+        const uint32_t pid = __float_as_uint(b.w);
+        float4 L = radiance[pid];
+        L.x += b.x * fmaxf(Y[3 * (size_t)i], 0.f);
+        L.y += b.y * fmaxf(Y[3 * (size_t)i + 1], 0.f);
+        L.z += b.z * fmaxf(Y[3 * (size_t)i + 2], 0.f);
+        radiance[pid] = L;
+    }
+}
+
+// training wave done: one (features, target) pair per recorded interaction, compacted in path order
+__global__ void __launch_bounds__(PT_THREADS)
+        k_cache_targets(const float4 *__restrict__ rec, const uint32_t *__restrict__ vcount, uint32_t paths,
+                        uint32_t rec_depth, const float4 *__restrict__ radiance, float *__restrict__ t_feat,
+                        float *__restrict__ t_target, uint32_t *__restrict__ t_count)
+{
+    const uint32_t n = paths * rec_depth;
+    for(uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x)
+    {
+        const uint32_t i = base + threadIdx.x;
+        bool ok = false;
+        float f[nrc::FEAT], tg[3];
+        if(i < n)
+        {
+            const uint32_t p = i / rec_depth, k = i - p * rec_depth;
+            if(k < vcount[p])
+            {
+                const float4 *r = rec + (size_t)i * REC_F4;
+                const float4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3], r4 = r[4];
+                const float4 Lf = radiance[p];
+                const float beta[3] = {r3.y, r3.z, r3.w}, Lk[3] = {r4.x, r4.y, r4.z}, Lp[3] = {Lf.x, Lf.y, Lf.z};
+                ok = true;
+                for(int c = 0; c < 3; ++c)
+                {
+                    tg[c] = beta[c] > 0.f ? fmaxf(Lp[c] - Lk[c], 0.f) / beta[c] : 0.f;
+                    ok = ok && isfinite(tg[c]);
+                }
+                const float v[nrc::FEAT] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w, r3.x};
+                for(int c = 0; c < nrc::FEAT; ++c) f[c] = v[c];
+            }
+        }
+        const uint32_t o = warp_push(t_count, ok);
+        if(ok)
+        {
+            for(int c = 0; c < nrc::FEAT; ++c) t_feat[(size_t)o * nrc::FEAT + c] = f[c];
+            for(int c = 0; c < 3; ++c) t_target[(size_t)o * 3 + c] = tg[c];
+        }
+    }
+}
+
+// optimiser step k of the frame trains on the window [k * B, (k + 1) * B) of the compacted records
+__global__ void k_cache_window(const uint32_t *__restrict__ t_count, uint32_t k, uint32_t B,
+                               uint32_t *__restrict__ b_count)
+{
+    const uint64_t cnt = *t_count, lo = (uint64_t)k * B;
+    *b_count = cnt > lo ? (uint32_t)std::min<uint64_t>(cnt - lo, B) : 0u;
 }
 
 __global__ void k_pt_accumulate(uint32_t npix, uint32_t ns, const float4 *__restrict__ radiance, float *__restrict__ sum)
@@ -410,6 +575,51 @@ void tracer_free_buffers(vkg_tracer *t)
     t->beta_pdf = t->radiance = nullptr;
     t->sum = t->accum = nullptr;
     t->capacity = t->npix_cap = 0;
+}
+
+void tracer_free_cache_buffers(vkg_tracer *t)
+{
+    for(void *p: {(void *)t->q_feat, (void *)t->q_beta, (void *)t->q_x, (void *)t->q_y, (void *)t->rec,
+                  (void *)t->vcount, (void *)t->t_feat, (void *)t->t_target})
+        cudaFree(p);
+    t->q_feat = nullptr;
+    t->q_beta = nullptr;
+    t->q_x = nullptr;
+    t->q_y = nullptr;
+    t->rec = nullptr;
+    t->vcount = nullptr;
+    t->t_feat = t->t_target = nullptr;
+    t->q_cap = t->rec_cap = 0;
+}
+
+// query buffers for `queries` rendering paths, training buffers for the cache's configuration
+vkg_status tracer_ensure_cache(vkg_tracer *t, size_t queries)
+{
+    const vkg_nrc_config &cfg = nrc::nrc_config(t->cache);
+    const size_t recs = (size_t)cfg.train_paths * cfg.train_depth;
+    if(queries <= t->q_cap && recs <= t->rec_cap && (t->q_cap || !queries)) return VKG_OK;
+    queries = std::max(queries, t->q_cap);
+    tracer_free_cache_buffers(t);
+    cudaError_t e = cudaSuccess;
+    auto al = [&](void **p, size_t bytes) {
+        if(e == cudaSuccess && bytes) e = cudaMalloc(p, bytes);
+    };
+    al((void **)&t->q_feat, queries * nrc::FEAT * sizeof(float));
+    al((void **)&t->q_beta, queries * sizeof(float4));
+    al((void **)&t->q_x, queries * nrc::ENCODED_BYTES);
+    al((void **)&t->q_y, queries * 3 * sizeof(float));
+    al((void **)&t->rec, std::max<size_t>(recs, 1) * REC_F4 * sizeof(float4));
+    al((void **)&t->vcount, std::max<size_t>(cfg.train_paths, 1) * sizeof(uint32_t));
+    al((void **)&t->t_feat, std::max<size_t>(recs, 1) * nrc::FEAT * sizeof(float));
+    al((void **)&t->t_target, std::max<size_t>(recs, 1) * 3 * sizeof(float));
+    if(e != cudaSuccess)
+    {
+        tracer_free_cache_buffers(t);
+        return cuda_check(t->ctx, e, "radiance cache buffers");
+    }
+    t->q_cap = queries;
+    t->rec_cap = recs;
+    return VKG_OK;
 }
 
 // (re)allocates the wave buffers; a new pixel count also restarts the accumulation
@@ -602,9 +812,10 @@ vkg_status vkg_tracer_create(vkg_ctx *ctx, const vkg_tracer_create_info *info, v
     t->ctx = ctx;
     t->seed = info->seed;
     t->settings = info->settings;
-    if(cudaMalloc(&t->counters, 4 * sizeof(uint32_t)) != cudaSuccess ||
-       cudaMalloc(&t->totals, 2 * sizeof(unsigned long long)) != cudaSuccess ||
-       cudaEventCreate(&t->ev0) != cudaSuccess || cudaEventCreate(&t->ev1) != cudaSuccess)
+    if(cudaMalloc(&t->counters, 8 * sizeof(uint32_t)) != cudaSuccess ||
+       cudaMalloc(&t->totals, 3 * sizeof(unsigned long long)) != cudaSuccess ||
+       cudaEventCreate(&t->ev0) != cudaSuccess || cudaEventCreate(&t->ev1) != cudaSuccess ||
+       cudaEventCreate(&t->ev_train) != cudaSuccess)
     {
         vkg_tracer_destroy(t);
         return set_error(ctx, VKG_ERR_CUDA, "vkg_tracer_create: allocation failed");
@@ -663,10 +874,18 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
     spw = std::min(spw, S.num_samples);
     const size_t paths = (size_t)npix * spw;
     if(paths >= (1ull << 31)) return set_error(ctx, VKG_ERR_CAPACITY, "vkg_tracer_render: too many paths per wave");
+    const vkg_nrc_config *ccfg = t->cache ? &nrc::nrc_config(t->cache) : nullptr;
+    const bool cache_render = ccfg && ccfg->terminate_depth < S.max_trace_depth;
+    const uint32_t rec_depth = ccfg ? std::min(ccfg->train_depth, S.max_trace_depth) : 0u;
+    const uint32_t train_paths = ccfg && rec_depth ? ccfg->train_paths : 0u;
+    if(paths + train_paths >= (1ull << 31))
+        return set_error(ctx, VKG_ERR_CAPACITY, "vkg_tracer_render: too many paths per wave");
     const bool same_pixels = t->npix_cap == npix;
     const uint32_t old_batch = t->batch;
-    if(vkg_status s = tracer_ensure(t, paths, npix); s != VKG_OK) return s;
+    if(vkg_status s = tracer_ensure(t, paths + train_paths, npix); s != VKG_OK) return s;
     t->batch = same_pixels ? old_batch : 0u; // growing the wave keeps the accumulation of the same window
+    if(ccfg)
+        if(vkg_status s = tracer_ensure_cache(t, cache_render ? paths : 0u); s != VKG_OK) return s;
 
     pt_params P{};
     P.nodes = sc->bvh->d_nodes;
@@ -690,21 +909,34 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
     P.max_path_beta = S.max_path_beta;
     P.seed = t->seed;
     P.batch = t->batch;
+    P.term_depth = cache_render ? ccfg->terminate_depth : 0xFFFFFFFFu;
+    P.rec_depth = rec_depth;
+    P.train_paths = train_paths;
 
-    const uint32_t grid = (uint32_t)std::min<size_t>((paths + PT_THREADS - 1) / PT_THREADS, (size_t)ctx->num_sms * 16);
-    VKG_TRY_CUDA(ctx, cudaMemsetAsync(t->sum, 0, (size_t)npix * 3 * sizeof(float), st));
-    VKG_TRY_CUDA(ctx, cudaMemsetAsync(t->totals, 0, 2 * sizeof(unsigned long long), st));
-    VKG_TRY_CUDA(ctx, cudaEventRecord(t->ev0, st));
     const bool empty = sc->num_tris == 0;
+    uint32_t *cnt_q = t->counters + 3, *cnt_rec = t->counters + 4, *cnt_b = t->counters + 5;
+    cache_io io{t->q_feat, t->q_beta, cnt_q, t->rec, t->vcount};
+
+    VKG_TRY_CUDA(ctx, cudaMemsetAsync(t->sum, 0, (size_t)npix * 3 * sizeof(float), st));
+    VKG_TRY_CUDA(ctx, cudaMemsetAsync(t->totals, 0, 3 * sizeof(unsigned long long), st));
+    VKG_TRY_CUDA(ctx, cudaEventRecord(t->ev0, st));
     for(uint32_t s0 = 0; s0 < S.num_samples; s0 += spw)
     {
         const uint32_t ns = std::min(spw, S.num_samples - s0);
-        const uint32_t n = npix * ns;
+        const uint32_t n_render = npix * ns;
+        // the training paths ride along with the last wave of rendering paths
+        const bool last = s0 + ns >= S.num_samples;
+        const uint32_t n = n_render + (last ? train_paths : 0u);
+        const int mode = ccfg ? MODE_CACHE : MODE_PLAIN;
+        const uint32_t depths = (!cache_render || (last && train_paths)) ? S.max_trace_depth : ccfg->terminate_depth + 1;
         P.s0 = s0;
+        P.train_base = last && train_paths ? n_render : 0xFFFFFFFFu;
+        const uint32_t grid = (uint32_t)std::min<size_t>((n + PT_THREADS - 1) / PT_THREADS, (size_t)ctx->num_sms * 16);
+        if(cache_render) VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_q, 0, sizeof(uint32_t), st));
         k_pt_generate<<<grid, PT_THREADS, 0, st>>>(P, n, t->q_ray[0], t->q_pid[0], t->rng, t->beta_pdf, t->radiance,
-                                                   t->counters);
+                                                   t->counters, t->vcount);
         int a = 0;
-        for(uint32_t depth = 0; depth < S.max_trace_depth; ++depth)
+        for(uint32_t depth = 0; depth < depths; ++depth)
         {
             uint32_t *cnt_in = t->counters + a, *cnt_out = t->counters + (1 - a), *cnt_s = t->counters + 2;
             if(empty)
@@ -713,17 +945,53 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
                 k_pt_extend<<<grid, PT_THREADS, 0, st>>>(P.nodes, P.tris, t->q_ray[a], cnt_in, t->hits);
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_out, 0, sizeof(uint32_t), st));
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_s, 0, sizeof(uint32_t), st));
-            k_pt_shade<<<grid, PT_THREADS, 0, st>>>(P, depth, t->q_ray[a], t->q_pid[a], t->hits, cnt_in, t->q_ray[1 - a],
-                                                    t->q_pid[1 - a], cnt_out, t->s_ray, t->s_pid, t->s_contrib, cnt_s,
-                                                    t->rng, t->beta_pdf, t->radiance);
+#define VKG_SHADE(M)                                                                                                   \
+    k_pt_shade<M><<<grid, PT_THREADS, 0, st>>>(P, depth, t->q_ray[a], t->q_pid[a], t->hits, cnt_in, t->q_ray[1 - a],    \
+                                               t->q_pid[1 - a], cnt_out, t->s_ray, t->s_pid, t->s_contrib, cnt_s,         \
+                                               t->rng, t->beta_pdf, t->radiance, io)
+            if(mode == MODE_PLAIN) VKG_SHADE(MODE_PLAIN);
+            else VKG_SHADE(MODE_CACHE);
+#undef VKG_SHADE
             if(!empty)
                 k_pt_shadow<<<grid, PT_THREADS, 0, st>>>(P.nodes, P.tris, t->s_ray, t->s_pid, t->s_contrib, cnt_s,
                                                          t->radiance);
             k_pt_tally<<<1, 1, 0, st>>>(cnt_in, cnt_s, t->totals);
             a = 1 - a;
         }
+        if(cache_render)
+        {
+            if(vkg_status s = nrc::nrc_predict(t->cache, t->q_feat, n_render, cnt_q, t->q_x, t->q_y, st); s != VKG_OK)
+                return s;
+            const uint32_t rg = (uint32_t)std::min<size_t>((n_render + 255) / 256, (size_t)ctx->num_sms * 8);
+            k_cache_resolve<<<rg, 256, 0, st>>>(t->q_beta, t->q_y, cnt_q, t->radiance, t->totals);
+        }
         k_pt_accumulate<<<(npix + 255) / 256, 256, 0, st>>>(npix, ns, t->radiance, t->sum);
+        if(last && train_paths)
+        {
+            VKG_TRY_CUDA(ctx, cudaEventRecord(t->ev_train, st));
+            VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_rec, 0, sizeof(uint32_t), st));
+            const uint32_t nrec = train_paths * rec_depth;
+            const uint32_t tg = (uint32_t)std::min<size_t>((nrec + PT_THREADS - 1) / PT_THREADS, (size_t)ctx->num_sms * 16);
+            k_cache_targets<<<tg, PT_THREADS, 0, st>>>(t->rec, t->vcount, train_paths, rec_depth, t->radiance + n_render,
+                                                       t->t_feat, t->t_target, cnt_rec);
+            // train_steps windows of batch_size records (0: as many as the record capacity needs); a
+            // window past the frame's record count takes no optimiser step
+            const uint32_t B = std::min(ccfg->batch_size, nrec);
+            const uint32_t windows = (uint32_t)((nrec + (uint64_t)B - 1) / B);
+            const uint32_t steps = ccfg->train_steps ? std::min(ccfg->train_steps, windows) : windows;
+            for(uint32_t k = 0; k < steps; ++k)
+            {
+                k_cache_window<<<1, 1, 0, st>>>(cnt_rec, k, B, cnt_b);
+                const size_t lo = (size_t)k * B;
+                const uint32_t cap = (uint32_t)std::min<size_t>(B, nrec - lo);
+                if(vkg_status s = nrc::nrc_train(t->cache, t->t_feat + lo * nrc::FEAT, t->t_target + lo * 3, cap, cnt_b, st);
+                   s != VKG_OK)
+                    return s;
+            }
+        }
     }
+    if(!train_paths) VKG_TRY_CUDA(ctx, cudaEventRecord(t->ev_train, st));
+    t->trained = train_paths > 0;
     k_pt_finalize<<<(3 * npix + 255) / 256, 256, 0, st>>>(npix, S.num_samples, t->batch, t->sum, t->accum, d_rgb_out);
     VKG_TRY_CUDA(ctx, cudaEventRecord(t->ev1, st));
     VKG_TRY_CUDA(ctx, cudaGetLastError());
@@ -741,15 +1009,34 @@ vkg_status vkg_tracer_statistics(vkg_tracer *t, vkg_tracer_stats *out)
     if(!t->rendered) return VKG_OK;
     if(vkg_status s = bind_device(t->ctx); s != VKG_OK) return s;
     VKG_TRY_CUDA(t->ctx, cudaEventSynchronize(t->ev1));
-    float ms = 0.f;
+    float ms = 0.f, render_ms = 0.f;
     cudaEventElapsedTime(&ms, t->ev0, t->ev1);
-    unsigned long long tot[2] = {0, 0};
+    cudaEventElapsedTime(&render_ms, t->ev0, t->ev_train);
+    unsigned long long tot[3] = {0, 0, 0};
     VKG_TRY_CUDA(t->ctx, cudaMemcpy(tot, t->totals, sizeof(tot), cudaMemcpyDeviceToHost));
-    out->raytrace_ms = ms;
+    uint32_t recs = 0;
+    if(t->trained) VKG_TRY_CUDA(t->ctx, cudaMemcpy(&recs, t->counters + 4, sizeof(recs), cudaMemcpyDeviceToHost));
+    out->raytrace_ms = render_ms;
     out->total_ms = ms;
+    out->train_ms = ms - render_ms;
     out->paths = t->last_paths;
     out->extension_rays = tot[0];
     out->shadow_rays = tot[1];
+    out->cache_queries = tot[2];
+    out->train_records = recs;
+    return VKG_OK;
+}
+
+vkg_status vkg_tracer_attach_cache(vkg_tracer *t, vkg_nrc *cache)
+{
+    if(!t) return VKG_ERR_INVALID_ARGUMENT;
+    if(cache != t->cache)
+    {
+        if(vkg_status s = bind_device(t->ctx); s != VKG_OK) return s;
+        cudaDeviceSynchronize(); // buffers of the previous cache may still be in use
+        tracer_free_cache_buffers(t);
+    }
+    t->cache = cache;
     return VKG_OK;
 }
 
@@ -758,10 +1045,12 @@ vkg_status vkg_tracer_destroy(vkg_tracer *t)
     if(!t) return VKG_OK;
     if(t->ctx) bind_device(t->ctx);
     tracer_free_buffers(t);
+    tracer_free_cache_buffers(t);
     cudaFree(t->counters);
     cudaFree(t->totals);
     if(t->ev0) cudaEventDestroy(t->ev0);
     if(t->ev1) cudaEventDestroy(t->ev1);
+    if(t->ev_train) cudaEventDestroy(t->ev_train);
     delete t;
     return VKG_OK;
 }

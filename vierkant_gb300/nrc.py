@@ -73,3 +73,14 @@ class NeuralRadianceCache:
             self.close()
         except Exception:
             pass
+
+
+def cache_for_scene(ctx: Context, scene, config: vkg_nrc_config | None = None, margin: float = 1e-3):
+    """a NeuralRadianceCache whose hash grid spans `scene`'s bounds (slightly enlarged)"""
+    cfg = config if config is not None else NeuralRadianceCache.default_config()
+    lo, hi = scene.bounds()
+    for a in range(3):
+        pad = margin * max(hi[a] - lo[a], 1e-6)
+        cfg.scene_min[a] = lo[a] - pad
+        cfg.scene_max[a] = hi[a] + pad
+    return NeuralRadianceCache(ctx, cfg)

@@ -17,7 +17,7 @@ import math
 import numpy as np
 import torch
 
-from ._lib import (check, lib, vkg_camera, vkg_scene_desc, vkg_settings, vkg_tracer_create_info,
+from ._lib import (check, lib, vkg_bvh_info, vkg_camera, vkg_scene_desc, vkg_settings, vkg_tracer_create_info,
                    vkg_tracer_stats)
 from .raytracing import Context
 
@@ -69,6 +69,14 @@ class Scene:
         self.num_tris = idx.numel() // 3
         ctx.adopt(self)
 
+    def bounds(self):
+        """(min xyz, max xyz) of the scene's geometry, as the BVH build saw them"""
+        b = C.c_void_p()
+        check(lib().vkg_scene_bvh(self.handle, C.byref(b)))
+        inf = vkg_bvh_info()
+        check(lib().vkg_bvh_info_get(b, C.byref(inf)))
+        return tuple(inf.scene_min), tuple(inf.scene_max)
+
     def env_tables(self):
         w, a = C.c_void_p(), C.c_void_p()
         W, H = C.c_uint32(), C.c_uint32()
@@ -103,7 +111,14 @@ class PBRPathTracer:
         h = C.c_void_p()
         check(lib().vkg_tracer_create(ctx.handle, C.byref(info), C.byref(h)), ctx.handle, "vkg_tracer_create")
         self.handle = h
+        self.cache = None
         ctx.adopt(self)
+
+    def attach_cache(self, cache):
+        """render through a NeuralRadianceCache (None: plain estimator again); see vkg_tracer_attach_cache"""
+        check(lib().vkg_tracer_attach_cache(self.handle, cache.handle if cache is not None else None), self.ctx.handle,
+              "vkg_tracer_attach_cache")
+        self.cache = cache
 
     def _crop(self):
         s = self.settings
