@@ -355,6 +355,7 @@ typedef struct vkg_nrc_config
     uint32_t terminate_depth; /* rendering paths end in the cache at this surface interaction (2) */
     uint32_t train_depth;     /* training targets are recorded at the first this-many interactions (4) */
     uint32_t train_steps;     /* optimiser steps per frame; 0: ceil(train_paths * train_depth / batch_size) */
+    uint32_t infer_kernel;    /* 0: default, 1: mma.sync MLP, 2: tcgen05 MLP, 3: tcgen05 MLP with the encoding fused */
 } vkg_nrc_config;
 typedef struct vkg_nrc_info_t
 {
@@ -367,7 +368,9 @@ typedef struct vkg_nrc_info_t
     float *d_grid_params; /* FP32 master hash-grid features [level][entry][2] */
     float *d_mlp_grads;   /* gradients of the last vkg_nrc_backward (zeroed by vkg_nrc_adam_step) */
     float *d_grid_grads;
-    uint32_t step;
+    uint32_t step;            /* optimiser steps taken */
+    uint32_t kernel_error;    /* nonzero: a tensor-core kernel gave up waiting (its results are void) */
+    uint32_t infer_kernel;    /* the inference kernel in use (1..3, see vkg_nrc_config) */
 } vkg_nrc_info_t;
 vkg_status vkg_nrc_config_default(vkg_nrc_config *out);
 vkg_status vkg_nrc_create(vkg_ctx *ctx, const vkg_nrc_config *cfg, vkg_nrc **out);
@@ -392,6 +395,11 @@ vkg_status vkg_nrc_load_params(vkg_nrc *nrc, const float *d_mlp, const float *d_
  * records their first train_depth interactions together with the radiance that followed each,
  * and runs train_steps optimiser steps on batches of batch_size records, all on `stream`. */
 vkg_status vkg_tracer_attach_cache(vkg_tracer *tracer, vkg_nrc *cache);
+/* diagnostic: D (128 x n FP32, row-major) = A (128 x k BF16, row-major) * B^T (n x k BF16, row-major)
+ * with one tcgen05.mma chain through the library's shared-memory descriptors (16 <= n <= 64,
+ * k <= 256, both multiples of 16); *d_err (device) gets bit 0 if the completion wait ran out */
+vkg_status vkg_diag_tc_gemm(vkg_ctx *ctx, const uint16_t *d_a, const uint16_t *d_b, uint32_t k, uint32_t n, float *d_d,
+                            uint32_t *d_err, void *stream);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,73 @@
+"""tcgen05 (5th-generation tensor core) kernels of the radiance cache.
+
+* the descriptor / instruction-descriptor / TMEM plumbing: one tcgen05.mma chain equals a PyTorch
+  FP32 matmul of the same BF16 operands for every operand shape the MLP uses;
+* the fused encode + 6-layer inference kernel equals the mma.sync twin on the same parameters
+  (both BF16 x BF16 -> FP32; only the summation order differs), and no wait ran out.
+"""
+import ctypes as C
+
+import pytest
+import torch
+
+from nrc_reference import random_features
+from vierkant_gb300 import _lib
+from vierkant_gb300.nrc import NeuralRadianceCache
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("k,n", [(16, 16), (64, 64), (80, 64), (64, 16), (256, 32)])
+def test_tc_gemm_matches_fp32_matmul(ctx, k, n):
+    g = torch.Generator(device="cuda").manual_seed(k * 100 + n)
+    a = torch.randn((128, k), device="cuda", generator=g).to(torch.bfloat16)
+    b = torch.randn((n, k), device="cuda", generator=g).to(torch.bfloat16)
+    d = torch.full((128, n), float("nan"), device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _lib.check(_lib.lib().vkg_diag_tc_gemm(ctx.handle, C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()), k, n,
+                                           C.c_void_p(d.data_ptr()), C.c_void_p(err.data_ptr()),
+                                           C.c_void_p(ctx.stream())), ctx.handle, "vkg_diag_tc_gemm")
+    torch.cuda.synchronize()
+    assert err.item() == 0
+    ref = a.float() @ b.float().t()
+    assert torch.isfinite(d).all()
+    tol = 1e-5 * k * ref.abs().max().item()
+    assert (d - ref).abs().max().item() <= tol, (d - ref).abs().max().item()
+
+
+def _caches(ctx):
+    caches = []
+    for kind in (1, 2, 3):
+        cfg = NeuralRadianceCache.default_config()
+        cfg.log2_table_size = 16
+        cfg.infer_kernel = kind
+        caches.append(NeuralRadianceCache(ctx, cfg))
+    i = caches[0].info()
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    w = torch.randn(i.num_mlp_params, device="cuda", generator=gen) * 0.25
+    grid = torch.randn(i.num_grid_params, device="cuda", generator=gen) * 0.5
+    for c in caches:
+        c.load_params(w, grid)
+    return caches
+
+
+def test_tc_inference_matches_mma_twin(ctx):
+    mma, tcc, fused = _caches(ctx)
+    assert [c.info().infer_kernel for c in (mma, tcc, fused)] == [1, 2, 3]
+    for n in (1, 127, 128, 129, 70_001):
+        feats = random_features(n, 100 + n)
+        y1 = mma.infer(feats)
+        for c in (tcc, fused):
+            y2 = c.infer(feats)
+            torch.cuda.synchronize()
+            scale = y1.abs().mean().item()
+            assert scale > 1e-3
+            diff = (y1 - y2).abs()
+            assert diff.mean().item() < 2e-3 * scale, (n, diff.mean().item(), scale)
+            assert diff.max().item() < 5e-2 * max(scale, y1.abs().max().item() * 0.1), (n, diff.max().item())
+    # the two tcgen05 kernels see identical BF16 inputs and issue identical MMAs
+    y2, y3 = tcc.infer(feats), fused.infer(feats)
+    assert torch.equal(y2, y3)
+    assert tcc.info().kernel_error == 0 and fused.info().kernel_error == 0
+    for c in (mma, tcc, fused):
+        c.close()

@@ -83,14 +83,16 @@ class vkg_nrc_config(C.Structure):
                 ("max_resolution", C.c_uint32), ("learning_rate", C.c_float), ("beta1", C.c_float),
                 ("beta2", C.c_float), ("epsilon", C.c_float), ("seed", C.c_uint32), ("scene_min", C.c_float * 3),
                 ("scene_max", C.c_float * 3), ("batch_size", C.c_uint32), ("train_paths", C.c_uint32),
-                ("terminate_depth", C.c_uint32), ("train_depth", C.c_uint32), ("train_steps", C.c_uint32)]
+                ("terminate_depth", C.c_uint32), ("train_depth", C.c_uint32), ("train_steps", C.c_uint32),
+                ("infer_kernel", C.c_uint32)]
 
 
 class vkg_nrc_info_t(C.Structure):
     _fields_ = [("levels", C.c_uint32), ("table_size", C.c_uint32), ("growth", C.c_float),
                 ("level_resolution", C.c_uint32 * 16), ("num_mlp_params", C.c_uint32),
                 ("num_grid_params", C.c_uint64), ("d_mlp_params", C.c_void_p), ("d_grid_params", C.c_void_p),
-                ("d_mlp_grads", C.c_void_p), ("d_grid_grads", C.c_void_p), ("step", C.c_uint32)]
+                ("d_mlp_grads", C.c_void_p), ("d_grid_grads", C.c_void_p), ("step", C.c_uint32),
+                ("kernel_error", C.c_uint32), ("infer_kernel", C.c_uint32)]
 
 
 class vkg_bvh_build_options(C.Structure):
@@ -153,6 +155,7 @@ SIGNATURES = {
     "vkg_tracer_statistics": (I32, [P, C.POINTER(vkg_tracer_stats)]),
     "vkg_tracer_destroy": (I32, [P]),
     "vkg_tracer_attach_cache": (I32, [P, P]),
+    "vkg_diag_tc_gemm": (I32, [P, P, P, U32, U32, P, P, P]),
     "vkg_nrc_config_default": (I32, [C.POINTER(vkg_nrc_config)]),
     "vkg_nrc_create": (I32, [P, C.POINTER(vkg_nrc_config), C.POINTER(P)]),
     "vkg_nrc_destroy": (I32, [P]),

@@ -7,7 +7,7 @@
 // (weights, and transposed weights for the backward) are pre-packed per lane and staged in shared
 // memory. This mma.sync path is the correctness twin of the tcgen05 inference kernel
 // (nrc_tc.cu) and the training path.
-#include "nrc.cuh"
+#include "nrc_encode.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -26,6 +26,9 @@ struct vkg_nrc
     __half2 *grid_h = nullptr;
     float *w = nullptr, *w_g = nullptr, *w_m = nullptr, *w_v = nullptr;
     uint2 *frag = nullptr, *fragT = nullptr;
+    uint16_t *wtc = nullptr;     // BF16 weights in the tcgen05 operand layout
+    uint32_t *d_err = nullptr;   // tensor-core kernel error word
+    uint32_t tc_infer = 1;       // 1: mma.sync MLP, 2: tcgen05 MLP, 3: tcgen05 MLP with the encoding fused
     // training / inference scratch, sized for `cap` samples
     uint32_t cap = 0;
     uint32_t *X = nullptr, *H = nullptr, *G = nullptr;
@@ -41,11 +44,6 @@ namespace
 
 constexpr int MLP_THREADS = 128;
 
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
-{
-    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-    return *reinterpret_cast<uint32_t *>(&v);
-}
 __device__ __forceinline__ float bf_lo(uint32_t v) { return __uint_as_float(v << 16); }
 __device__ __forceinline__ float bf_hi(uint32_t v) { return __uint_as_float(v & 0xFFFF0000u); }
 
@@ -95,73 +93,6 @@ __device__ __forceinline__ void layer(const uint32_t (&a)[KT][4], const uint2 *_
     }
 }
 
-// ---- encodings ---------------------------------------------------------------------------------
-__device__ __forceinline__ void sh4(float x, float y, float z, float *o)
-{
-    // real spherical harmonics, bands 0..3
-    const float xx = x * x, yy = y * y, zz = z * z;
-    o[0] = 0.28209479177387814f;
-    o[1] = -0.48860251190291987f * y;
-    o[2] = 0.48860251190291987f * z;
-    o[3] = -0.48860251190291987f * x;
-    o[4] = 1.0925484305920792f * x * y;
-    o[5] = -1.0925484305920792f * y * z;
-    o[6] = 0.31539156525252005f * (3.f * zz - 1.f);
-    o[7] = -1.0925484305920792f * x * z;
-    o[8] = 0.5462742152960396f * (xx - yy);
-    o[9] = -0.5900435899266435f * y * (3.f * xx - yy);
-    o[10] = 2.890611442640554f * x * y * z;
-    o[11] = -0.4570457994644658f * y * (5.f * zz - 1.f);
-    o[12] = 0.3731763325901154f * z * (5.f * zz - 3.f);
-    o[13] = -0.4570457994644658f * x * (5.f * zz - 1.f);
-    o[14] = 1.445305721320277f * z * (xx - yy);
-    o[15] = -0.5900435899266435f * x * (xx - 3.f * yy);
-}
-
-struct corner_iter
-{
-    uint32_t res, table;
-    bool dense;
-    int cx, cy, cz;
-    float fx, fy, fz;
-};
-
-__device__ __forceinline__ corner_iter level_setup(const grid_config &gc, uint32_t l, float px, float py, float pz)
-{
-    corner_iter c;
-    c.res = level_res(gc, l);
-    c.table = 1u << gc.log2_t;
-    const uint64_t r1 = (uint64_t)c.res + 1;
-    c.dense = r1 * r1 * r1 <= (uint64_t)c.table;
-    const float x = px * (float)c.res, y = py * (float)c.res, z = pz * (float)c.res;
-    // the cell is clamped so p = 1 interpolates inside the last cell (every corner stays in range)
-    const float top = (float)(c.res - 1);
-    const float flx = fminf(floorf(x), top), fly = fminf(floorf(y), top), flz = fminf(floorf(z), top);
-    c.cx = (int)flx;
-    c.cy = (int)fly;
-    c.cz = (int)flz;
-    c.fx = x - flx;
-    c.fy = y - fly;
-    c.fz = z - flz;
-    return c;
-}
-
-__device__ __forceinline__ uint32_t corner_index(const corner_iter &c, int k, float &w)
-{
-    const uint32_t x = (uint32_t)(c.cx + (k & 1)), y = (uint32_t)(c.cy + ((k >> 1) & 1)),
-                   z = (uint32_t)(c.cz + ((k >> 2) & 1));
-    w = ((k & 1) ? c.fx : 1.f - c.fx) * ((k & 2) ? c.fy : 1.f - c.fy) * ((k & 4) ? c.fz : 1.f - c.fz);
-    if(c.dense) return x + y * (c.res + 1) + z * (c.res + 1) * (c.res + 1);
-    return (x * 1u ^ y * 2654435761u ^ z * 805459861u) & (c.table - 1u);
-}
-
-__device__ __forceinline__ void normalised_pos(const grid_config &gc, const float *f, float &px, float &py, float &pz)
-{
-    px = fminf(fmaxf((f[0] - gc.smin[0]) * gc.sinv[0], 0.f), 1.f);
-    py = fminf(fmaxf((f[1] - gc.smin[1]) * gc.sinv[1], 0.f), 1.f);
-    pz = fminf(fmaxf((f[2] - gc.smin[2]) * gc.sinv[2], 0.f), 1.f);
-}
-
 __device__ __forceinline__ uint32_t eff_count(uint32_t n, const uint32_t *d_n) { return d_n ? min(*d_n, n) : n; }
 
 __global__ void k_encode(const float *__restrict__ feats, uint32_t n, const uint32_t *__restrict__ d_n, grid_config gc,
@@ -169,38 +100,7 @@ __global__ void k_encode(const float *__restrict__ feats, uint32_t n, const uint
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= eff_count(n, d_n)) return;
-    const float *f = feats + (size_t)FEAT * i;
-    float px, py, pz;
-    normalised_pos(gc, f, px, py, pz);
-    uint32_t *out = X + (size_t)(IN / 2) * i;
-    const uint32_t T = 1u << gc.log2_t;
-    for(uint32_t l = 0; l < gc.levels; ++l)
-    {
-        corner_iter c = level_setup(gc, l, px, py, pz);
-        float f0 = 0.f, f1 = 0.f;
-#pragma unroll
-        for(int k = 0; k < 8; ++k)
-        {
-            float w;
-            const uint32_t idx = corner_index(c, k, w);
-            const float2 v = __half22float2(grid[(size_t)l * T + idx]);
-            f0 += w * v.x;
-            f1 += w * v.y;
-        }
-        out[l] = pack_bf16(f0, f1);
-    }
-    for(uint32_t l = gc.levels; l < 16; ++l) out[l] = 0u;
-    float s[16];
-    sh4(f[3], f[4], f[5], s);
-#pragma unroll
-    for(int k = 0; k < 8; ++k) out[16 + k] = pack_bf16(s[2 * k], s[2 * k + 1]);
-    sh4(f[6], f[7], f[8], s);
-#pragma unroll
-    for(int k = 0; k < 8; ++k) out[24 + k] = pack_bf16(s[2 * k], s[2 * k + 1]);
-    out[32] = pack_bf16(f[9], f[10]);
-    out[33] = pack_bf16(f[11], f[12]);
-#pragma unroll
-    for(int k = 34; k < 40; ++k) out[k] = 0u;
+    encode_record(gc, grid, feats + (size_t)FEAT * i, X + (size_t)(IN / 2) * i);
 }
 
 // ---- fused forward -------------------------------------------------------------------------------
@@ -676,6 +576,7 @@ vkg_status nrc_adam(vkg_nrc *c, const uint32_t *d_n, cudaStream_t st)
                                    c->d_state, c->grid_h);
     k_adam<<<64, 256, 0, st>>>(c->w, c->w_g, c->w_m, c->w_v, NPARAM, c->lr, c->b1, c->b2, c->eps, c->d_state, nullptr);
     k_pack<<<(NFRAG + 255) / 256, 256, 0, st>>>(c->w, c->frag, c->fragT);
+    if(vkg_status s = nrc_pack_tc(c->ctx, c->w, c->wtc, st); s != VKG_OK) return s;
     return cuda_check(c->ctx, cudaGetLastError(), "nrc adam");
 }
 
@@ -684,6 +585,12 @@ const vkg_nrc_config &nrc_config(const vkg_nrc *c) { return c->cfg; }
 vkg_status nrc_predict(vkg_nrc *c, const float *feats, uint32_t n, const uint32_t *d_n, uint32_t *X, float *Y,
                        cudaStream_t st)
 {
+    if(c->tc_infer == 3) return nrc_infer_tc(c->ctx, c->gc, c->grid_h, c->wtc, feats, nullptr, n, d_n, Y, c->d_err, st);
+    if(c->tc_infer == 2)
+    {
+        if(vkg_status s = nrc_encode(c, feats, n, d_n, X, st); s != VKG_OK) return s;
+        return nrc_infer_tc(c->ctx, c->gc, c->grid_h, c->wtc, feats, X, n, d_n, Y, c->d_err, st);
+    }
     if(vkg_status s = nrc_encode(c, feats, n, d_n, X, st); s != VKG_OK) return s;
     return nrc_forward(c, X, n, d_n, Y, st);
 }
@@ -737,9 +644,12 @@ vkg_status vkg_nrc_create(vkg_ctx *ctx, const vkg_nrc_config *cfg, vkg_nrc **out
     if(vkg_status s = bind_device(ctx); s != VKG_OK) return s;
     if(cfg->batch_size == 0 || cfg->batch_size > (1u << 24) || cfg->train_paths > (1u << 24) || cfg->train_depth > 16)
         return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_nrc_create: invalid training configuration");
+    if(cfg->infer_kernel > 3)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_nrc_create: infer_kernel must be 0..3");
     auto *c = new vkg_nrc();
     c->ctx = ctx;
     c->cfg = *cfg;
+    c->tc_infer = cfg->infer_kernel ? cfg->infer_kernel : 1u;
     c->gc.levels = cfg->levels;
     c->gc.log2_t = cfg->log2_table_size;
     c->gc.base_res = cfg->base_resolution;
@@ -775,6 +685,8 @@ vkg_status vkg_nrc_create(vkg_ctx *ctx, const vkg_nrc_config *cfg, vkg_nrc **out
     al((void **)&c->fragT, NFRAG * 8);
     al((void **)&c->loss, 4 * 4);
     al((void **)&c->d_state, 2 * sizeof(uint32_t));
+    al((void **)&c->wtc, NPARAM * 2);
+    al((void **)&c->d_err, sizeof(uint32_t));
     if(e == cudaSuccess)
     {
         for(void *p: {(void *)c->grid_g, (void *)c->grid_m, (void *)c->grid_v})
@@ -783,6 +695,7 @@ vkg_status vkg_nrc_create(vkg_ctx *ctx, const vkg_nrc_config *cfg, vkg_nrc **out
             if(e == cudaSuccess) e = cudaMemset(p, 0, NPARAM * 4);
         if(e == cudaSuccess) e = cudaMemset(c->loss, 0, 16);
         if(e == cudaSuccess) e = cudaMemset(c->d_state, 0, 2 * sizeof(uint32_t));
+        if(e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(uint32_t));
     }
     if(e != cudaSuccess)
     {
@@ -791,6 +704,11 @@ vkg_status vkg_nrc_create(vkg_ctx *ctx, const vkg_nrc_config *cfg, vkg_nrc **out
     }
     k_init<<<ctx->num_sms * 8, 256>>>(c->grid, c->grid_h, c->ngrid, c->w, cfg->seed);
     k_pack<<<(NFRAG + 255) / 256, 256>>>(c->w, c->frag, c->fragT);
+    if(vkg_status s = nrc_pack_tc(ctx, c->w, c->wtc, nullptr); s != VKG_OK)
+    {
+        vkg_nrc_destroy(c);
+        return s;
+    }
     e = cudaDeviceSynchronize();
     if(e != cudaSuccess)
     {
@@ -807,7 +725,7 @@ vkg_status vkg_nrc_destroy(vkg_nrc *c)
     if(c->ctx) bind_device(c->ctx);
     for(void *p: {(void *)c->grid, (void *)c->grid_g, (void *)c->grid_m, (void *)c->grid_v, (void *)c->grid_h,
                   (void *)c->w, (void *)c->w_g, (void *)c->w_m, (void *)c->w_v, (void *)c->frag, (void *)c->fragT,
-                  (void *)c->loss, (void *)c->d_state, (void *)c->X, (void *)c->H, (void *)c->G, (void *)c->Y,
+                  (void *)c->loss, (void *)c->d_state, (void *)c->wtc, (void *)c->d_err, (void *)c->X, (void *)c->H, (void *)c->G, (void *)c->Y,
                   (void *)c->dXg})
         cudaFree(p);
     delete c;
@@ -830,6 +748,8 @@ vkg_status vkg_nrc_info(const vkg_nrc *c, vkg_nrc_info_t *out)
     out->d_grid_grads = c->grid_g;
     if(vkg_status s = bind_device(c->ctx); s != VKG_OK) return s;
     VKG_TRY_CUDA(c->ctx, cudaMemcpy(&out->step, c->d_state, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    VKG_TRY_CUDA(c->ctx, cudaMemcpy(&out->kernel_error, c->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    out->infer_kernel = c->tc_infer;
     return VKG_OK;
 }
 
@@ -839,9 +759,12 @@ vkg_status vkg_nrc_infer(vkg_nrc *c, const float *d_feats, uint32_t n, float *d_
     if(n == 0) return VKG_OK;
     if(!d_feats || !d_rgb) return set_error(c->ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_nrc_infer: NULL buffer");
     if(vkg_status s = bind_device(c->ctx); s != VKG_OK) return s;
-    if(vkg_status s = nrc_ensure(c, n); s != VKG_OK) return s;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if(c->tc_infer == 3)
+        return nrc_infer_tc(c->ctx, c->gc, c->grid_h, c->wtc, d_feats, nullptr, n, nullptr, d_rgb, c->d_err, st);
+    if(vkg_status s = nrc_ensure(c, n); s != VKG_OK) return s;
     if(vkg_status s = nrc_encode(c, d_feats, n, nullptr, c->X, st); s != VKG_OK) return s;
+    if(c->tc_infer == 2) return nrc_infer_tc(c->ctx, c->gc, c->grid_h, c->wtc, d_feats, c->X, n, nullptr, d_rgb, c->d_err, st);
     return nrc_forward(c, c->X, n, nullptr, d_rgb, st);
 }
 
@@ -890,6 +813,7 @@ vkg_status vkg_nrc_load_params(vkg_nrc *c, const float *d_mlp, const float *d_gr
         k_to_half<<<c->ctx->num_sms * 8, 256, 0, st>>>(c->grid, c->ngrid, c->grid_h);
     }
     k_pack<<<(NFRAG + 255) / 256, 256, 0, st>>>(c->w, c->frag, c->fragT);
+    if(vkg_status s = nrc_pack_tc(c->ctx, c->w, c->wtc, st); s != VKG_OK) return s;
     return cuda_check(c->ctx, cudaGetLastError(), "vkg_nrc_load_params");
 }
 

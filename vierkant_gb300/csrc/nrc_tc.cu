@@ -1,0 +1,295 @@
+// Neural radiance cache inference on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// One CTA of 256 threads owns a tile of 128 queries at a time (persistent over tiles):
+//   1. two threads per query encode it (hash-grid levels 0..7 / levels 8..15 + SH + material,
+//      nrc_encode.cuh) straight into shared memory as the BF16 A operand of layer 0 (128 x 80,
+//      canonical K-major layout, tc.cuh);
+//   2. thread 0 issues the layer's tcgen05.mma steps (M = 128, N = 64 or 16, K = 16 each) against
+//      the weights, which stay in shared memory for the kernel's lifetime, and commits them to an
+//      mbarrier; the FP32 accumulator lives in TMEM (64 columns);
+//   3. after the mbarrier (bounded wait), the two threads of a query read its TMEM lane (32 columns
+//      each), apply ReLU, pack BF16 and write the next layer's A operand back to shared memory; the
+//      last layer's first three columns are the prediction.
+// The numerics equal the mma.sync twin (nrc.cu): BF16 inputs / weights / activations, FP32
+// accumulation; only the summation order inside an MMA differs.
+//
+// A wait that runs out (it never should) sets bit 0 of the error word, lets any MMA still in flight
+// finish (bounded), frees the TMEM and returns.
+#include "nrc_encode.cuh"
+#include "tc.cuh"
+
+#include <algorithm>
+
+namespace vkg
+{
+namespace nrc
+{
+
+constexpr uint32_t TC_THREADS = 128, TC_INFER_THREADS = 256, TC_TILE = 128, TC_TMEM_COLS = 64;
+constexpr uint32_t TC_W_BYTES = NPARAM * 2;      // all six layers, BF16 B operands (45,056 B)
+constexpr uint32_t TC_A_BYTES = TC_TILE * IN * 2; // one A operand (20,480 B)
+constexpr uint32_t TC_SMEM = TC_W_BYTES + TC_A_BYTES;
+constexpr uint32_t TC_TIMEOUT = 1u;
+
+namespace
+{
+
+__device__ __forceinline__ uint32_t eff_n(uint32_t n, const uint32_t *d_n) { return d_n ? min(*d_n, n) : n; }
+
+// FP32 master weights ([in][out] row-major per layer) -> BF16 B operands: layer l as N x K, K-major
+__global__ void k_pack_tc(const float *__restrict__ W, uint16_t *__restrict__ wtc)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if(e >= NPARAM) return;
+    int l = 0;
+    while(l + 1 < NLAYER && e >= layer_off(l + 1)) ++l;
+    const int K = layer_in(l), N = layer_out(l), local = e - layer_off(l);
+    const int k = local / N, n = local - k * N;
+    const __nv_bfloat16 b = __float2bfloat16_rn(W[e]);
+    wtc[(layer_off(l) * 2 + tc::canon_offset(n, k, K)) / 2] = *reinterpret_cast<const uint16_t *>(&b);
+}
+
+// FUSED: encode the feature records here; else read the encoded inputs X (n x 40 u32) written by k_encode
+template<bool FUSED>
+__global__ void __launch_bounds__(TC_INFER_THREADS)
+        k_infer_tc(const float *__restrict__ feats, const uint32_t *__restrict__ X, uint32_t n_cap,
+                   const uint32_t *__restrict__ d_n, grid_config gc, const __half2 *__restrict__ grid,
+                   const uint16_t *__restrict__ wtc, float *__restrict__ Y, uint32_t *__restrict__ err)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tslot;
+    uint8_t *sw = smem, *sa = smem + TC_W_BYTES;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    // thread t works on row r = t mod 128 of the tile; its half h = t / 128 picks the hash-grid levels
+    // it encodes (0..7 or 8..15 + the SH / material inputs) and the TMEM columns it drains (warp w reads
+    // TMEM lanes 32 (w mod 4) .. + 31)
+    const uint32_t r = tid & (TC_TILE - 1), h = tid >> 7;
+
+    for(uint32_t i = tid; i < TC_W_BYTES / 16; i += TC_INFER_THREADS)
+        reinterpret_cast<uint4 *>(sw)[i] = reinterpret_cast<const uint4 *>(wtc)[i];
+    if(warp == 0) tc::tmem_alloc(&tslot, TC_TMEM_COLS);
+    if(tid == 0) tc::mbar_init(&mbar, 1);
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tslot, lane_base = ((warp & 3u) * 32u) << 16;
+    const uint32_t sw_addr = tc::smem_addr(sw), sa_addr = tc::smem_addr(sa);
+    const uint32_t n = eff_n(n_cap, d_n), tiles = (n + TC_TILE - 1) / TC_TILE;
+    uint32_t phase = 0;
+    bool failed = false;
+
+    for(uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x)
+    {
+        const uint32_t q = tile * TC_TILE + r;
+        if constexpr(!FUSED)
+        {
+            // half h copies 16-byte groups h, h + 2, ... of row r
+            const uint4 *src = reinterpret_cast<const uint4 *>(X + (size_t)(IN / 2) * q);
+#pragma unroll
+            for(int j = h; j < IN / 8; j += 2)
+                *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 8 * j, IN)) =
+                        q < n ? src[j] : make_uint4(0u, 0u, 0u, 0u);
+        }
+        else if(h == 0)
+        {
+            uint32_t x[8];
+            if(q < n)
+            {
+                const float *f = feats + (size_t)FEAT * q;
+                float px, py, pz;
+                normalised_pos(gc, f, px, py, pz);
+                encode_levels<0, 8>(gc, grid, px, py, pz, x);
+            }
+            else
+                for(int j = 0; j < 8; ++j) x[j] = 0u;
+#pragma unroll
+            for(int j = 0; j < 2; ++j)
+                *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 8 * j, IN)) =
+                        make_uint4(x[4 * j], x[4 * j + 1], x[4 * j + 2], x[4 * j + 3]);
+        }
+        else
+        {
+            uint32_t x[32];
+            if(q < n)
+            {
+                const float *f = feats + (size_t)FEAT * q;
+                float px, py, pz;
+                normalised_pos(gc, f, px, py, pz);
+                encode_levels<8, 16>(gc, grid, px, py, pz, x);
+                encode_rest(f, x + 8);
+            }
+            else
+                for(int j = 0; j < 32; ++j) x[j] = 0u;
+#pragma unroll
+            for(int j = 0; j < 8; ++j)
+                *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 16 + 8 * j, IN)) =
+                        make_uint4(x[4 * j], x[4 * j + 1], x[4 * j + 2], x[4 * j + 3]);
+        }
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+#pragma unroll 1
+        for(int l = 0; l < NLAYER; ++l)
+        {
+            const uint32_t K = layer_in(l), N = layer_out(l);
+            if(tid == 0)
+            {
+                tc::fence_after_sync();
+                const uint32_t idesc = tc::idesc_bf16(TC_TILE, N);
+                const uint32_t wb = sw_addr + (uint32_t)layer_off(l) * 2u;
+                for(uint32_t s = 0; s < K / 16; ++s)
+                    tc::mma_bf16(tmem, tc::smem_desc(sa_addr + 256u * s, 128u, K * 16u),
+                                 tc::smem_desc(wb + 256u * s, 128u, K * 16u), idesc, s > 0);
+                tc::mma_commit(&mbar);
+            }
+            const bool ok = tc::mbar_wait(&mbar, phase);
+            if(__syncthreads_or(!ok))
+            {
+                failed = true;
+                break;
+            }
+            phase ^= 1u;
+            tc::fence_after_sync();
+            if(l + 1 < NLAYER)
+            {
+                // this thread's 32 of the 64 columns of row r
+                uint32_t hv[16];
+#pragma unroll
+                for(int c = 0; c < 2; ++c)
+                {
+                    float v[16];
+                    tc::tmem_ld16(tmem + lane_base + 32u * h + 16u * c, v);
+                    tc::tmem_ld_wait();
+#pragma unroll
+                    for(int j = 0; j < 8; ++j) hv[8 * c + j] = pack_bf16(fmaxf(v[2 * j], 0.f), fmaxf(v[2 * j + 1], 0.f));
+                }
+#pragma unroll
+                for(int j = 0; j < 4; ++j)
+                    *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 32 * h + 8 * j, HID)) =
+                            make_uint4(hv[4 * j], hv[4 * j + 1], hv[4 * j + 2], hv[4 * j + 3]);
+                tc::fence_async_smem();
+            }
+            else if(h == 0)
+            {
+                float v[16];
+                tc::tmem_ld16(tmem + lane_base, v);
+                tc::tmem_ld_wait();
+                if(q < n)
+                {
+                    Y[3 * (size_t)q] = v[0];
+                    Y[3 * (size_t)q + 1] = v[1];
+                    Y[3 * (size_t)q + 2] = v[2];
+                }
+            }
+            tc::fence_before_sync();
+            __syncthreads();
+        }
+    }
+    if(failed)
+    {
+        if(tid == 0) atomicOr(err, TC_TIMEOUT);
+        tc::mbar_wait(&mbar, phase); // the MMAs in flight, if any
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if(warp == 0) tc::tmem_dealloc(tmem, TC_TMEM_COLS);
+}
+
+// diagnostic: D (128 x N, FP32) = A (128 x K BF16, row-major) * B^T (N x K BF16, row-major) through the
+// same descriptors, one CTA
+__global__ void __launch_bounds__(TC_THREADS)
+        k_tc_gemm(const uint16_t *__restrict__ A, const uint16_t *__restrict__ B, uint32_t K, uint32_t N,
+                  float *__restrict__ D, uint32_t *__restrict__ err)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tslot;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    uint8_t *sa = smem, *sb = smem + TC_TILE * K * 2;
+    for(uint32_t k = 0; k < K; ++k)
+        *reinterpret_cast<uint16_t *>(sa + tc::canon_offset(tid, k, K)) = A[(size_t)tid * K + k];
+    for(uint32_t e = tid; e < N * K; e += TC_THREADS)
+        *reinterpret_cast<uint16_t *>(sb + tc::canon_offset(e / K, e % K, K)) = B[e];
+    if(warp == 0) tc::tmem_alloc(&tslot, TC_TMEM_COLS);
+    if(tid == 0) tc::mbar_init(&mbar, 1);
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tslot;
+    if(tid == 0)
+    {
+        const uint32_t idesc = tc::idesc_bf16(TC_TILE, N);
+        for(uint32_t s = 0; s < K / 16; ++s)
+            tc::mma_bf16(tmem, tc::smem_desc(tc::smem_addr(sa) + 256u * s, 128u, K * 16u),
+                         tc::smem_desc(tc::smem_addr(sb) + 256u * s, 128u, K * 16u), idesc, s > 0);
+        tc::mma_commit(&mbar);
+    }
+    const bool ok = tc::mbar_wait(&mbar, 0);
+    if(__syncthreads_or(!ok))
+    {
+        if(tid == 0) atomicOr(err, TC_TIMEOUT);
+        tc::mbar_wait(&mbar, 0);
+    }
+    else
+    {
+        tc::fence_after_sync();
+        for(uint32_t c = 0; c < N / 16; ++c)
+        {
+            float v[16];
+            tc::tmem_ld16(tmem + ((warp * 32u) << 16) + 16u * c, v);
+            tc::tmem_ld_wait();
+            for(int j = 0; j < 16; ++j) D[(size_t)tid * N + 16 * c + j] = v[j];
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if(warp == 0) tc::tmem_dealloc(tmem, TC_TMEM_COLS);
+}
+
+}// namespace
+
+vkg_status nrc_pack_tc(vkg_ctx *ctx, const float *W, uint16_t *wtc, cudaStream_t st)
+{
+    k_pack_tc<<<(NPARAM + 255) / 256, 256, 0, st>>>(W, wtc);
+    return cuda_check(ctx, cudaGetLastError(), "k_pack_tc");
+}
+
+vkg_status nrc_infer_tc(vkg_ctx *ctx, const grid_config &gc, const __half2 *grid, const uint16_t *wtc,
+                        const float *feats, const uint32_t *X, uint32_t n, const uint32_t *d_n, float *Y, uint32_t *err,
+                        cudaStream_t st)
+{
+    if(n == 0) return VKG_OK;
+    auto kern = X ? k_infer_tc<false> : k_infer_tc<true>;
+    VKG_TRY_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
+    int per_sm = 0;
+    VKG_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TC_INFER_THREADS, TC_SMEM));
+    // TMEM: every resident CTA holds 64 of the SM's 512 columns
+    per_sm = std::max(1, std::min(per_sm, (int)(512 / TC_TMEM_COLS)));
+    const uint32_t tiles = (n + TC_TILE - 1) / TC_TILE;
+    const uint32_t grid_n = std::min<uint32_t>(tiles, (uint32_t)(ctx->num_sms * per_sm));
+    kern<<<grid_n, TC_INFER_THREADS, TC_SMEM, st>>>(feats, X, n, d_n, gc, grid, wtc, Y, err);
+    return cuda_check(ctx, cudaGetLastError(), "k_infer_tc");
+}
+
+}// namespace nrc
+}// namespace vkg
+
+using namespace vkg;
+
+extern "C" vkg_status vkg_diag_tc_gemm(vkg_ctx *ctx, const uint16_t *d_a, const uint16_t *d_b, uint32_t k,
+                                       uint32_t n, float *d_d, uint32_t *d_err, void *stream)
+{
+    if(!ctx) return VKG_ERR_INVALID_ARGUMENT;
+    if(!d_a || !d_b || !d_d || !d_err || k == 0 || k % 16 || k > 256 || n < 16 || n > nrc::TC_TMEM_COLS || n % 16)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_diag_tc_gemm: need 16 <= n <= 64, k <= 256, multiples of 16");
+    if(vkg_status s = bind_device(ctx); s != VKG_OK) return s;
+    const uint32_t smem = nrc::TC_TILE * k * 2 + n * k * 2;
+    VKG_TRY_CUDA(ctx, cudaFuncSetAttribute(nrc::k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    nrc::k_tc_gemm<<<1, nrc::TC_THREADS, smem, static_cast<cudaStream_t>(stream)>>>(d_a, d_b, k, n, d_d, d_err);
+    return cuda_check(ctx, cudaGetLastError(), "k_tc_gemm");
+}
