@@ -333,6 +333,52 @@ vkg_status vkg_tracer_statistics(vkg_tracer *tracer, vkg_tracer_stats *out);
 vkg_status vkg_tracer_destroy(vkg_tracer *tracer);
 
 
+/* ---- batched uneven rendering (not in the reference) ------------------------------------------ *
+ * Many (scene, camera, settings) jobs of uneven size rendered together: the paths of all jobs share
+ * one set of wavefront queues (every path carries its job index), waves are packed from whole
+ * samples of the jobs, and a render is one CUDA-graph launch. Each job's image equals what
+ * vkg_tracer_render would produce for it alone with the same seed and settings (same PCG32 streams,
+ * same per-pixel summation order). No radiance cache in batch mode. */
+typedef struct vkg_batch vkg_batch;
+typedef struct vkg_batch_job
+{
+    const vkg_scene *scene;
+    vkg_camera camera;        /* camera->width / height must equal settings.resolution */
+    vkg_settings settings;    /* resolution, crop, num_samples, max_trace_depth, rr_start_depth, ... */
+    uint32_t seed;            /* PBRPathTracer create-info seed of this job */
+    uint32_t pad;
+    float *d_rgb_out;         /* crop width x height x 3 fp32 running mean (device; may be NULL) */
+} vkg_batch_job;
+typedef struct vkg_batch_tuning
+{
+    uint32_t extend_kernel;   /* 1: grid-stride queue kernels, 2: persistent work-stealing tracers */
+    uint32_t ctas_per_sm;     /* grid of the grid-stride queue kernels = SMs x this */
+    uint32_t wave_paths;      /* paths in flight per wave */
+    uint32_t use_graph;       /* 1: capture a render as a CUDA graph and replay it */
+} vkg_batch_tuning;
+typedef struct vkg_batch_stats
+{
+    double render_ms;         /* GPU time of the last render */
+    uint64_t paths;
+    uint64_t extension_rays;
+    uint64_t shadow_rays;
+    uint32_t waves;           /* waves per render */
+    uint32_t batch;           /* renders accumulated */
+} vkg_batch_stats;
+vkg_status vkg_batch_tuning_default(vkg_batch_tuning *out);
+/* jobs are copied; the scenes and output buffers must outlive the batch */
+vkg_status vkg_batch_create(vkg_ctx *ctx, const vkg_batch_job *jobs, uint32_t njobs, const vkg_batch_tuning *tuning,
+                            vkg_batch **out);
+/* times every candidate tuning on a one-sample-per-job render and keeps the fastest (*chosen, optional,
+ * receives it); the accumulation is reset. Synchronises. */
+vkg_status vkg_batch_autotune(vkg_batch *batch, void *stream, vkg_batch_tuning *chosen);
+vkg_status vkg_batch_set_tuning(vkg_batch *batch, const vkg_batch_tuning *tuning);
+/* one batch of num_samples paths per pixel for every job, blended into each job's running mean */
+vkg_status vkg_batch_render(vkg_batch *batch, void *stream);
+vkg_status vkg_batch_reset_accumulator(vkg_batch *batch);
+vkg_status vkg_batch_statistics(vkg_batch *batch, vkg_batch_stats *out);
+vkg_status vkg_batch_destroy(vkg_batch *batch);
+
 /* ---- neural radiance cache (not in the reference) -------------------------------------------- *
  * A small MLP (80 inputs -> 5 hidden layers of 64, ReLU -> RGB; BF16 weights and activations, FP32
  * accumulation) over a multiresolution hash grid (position) and degree-4 spherical harmonics

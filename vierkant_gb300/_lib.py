@@ -64,6 +64,21 @@ class vkg_tracer_create_info(C.Structure):
     _fields_ = [("seed", C.c_uint32), ("settings", vkg_settings)]
 
 
+class vkg_batch_job(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", vkg_camera), ("settings", vkg_settings), ("seed", C.c_uint32),
+                ("pad", C.c_uint32), ("d_rgb_out", C.c_void_p)]
+
+
+class vkg_batch_tuning(C.Structure):
+    _fields_ = [("extend_kernel", C.c_uint32), ("ctas_per_sm", C.c_uint32), ("wave_paths", C.c_uint32),
+                ("use_graph", C.c_uint32)]
+
+
+class vkg_batch_stats(C.Structure):
+    _fields_ = [("render_ms", C.c_double), ("paths", C.c_uint64), ("extension_rays", C.c_uint64),
+                ("shadow_rays", C.c_uint64), ("waves", C.c_uint32), ("batch", C.c_uint32)]
+
+
 class vkg_tracer_stats(C.Structure):
     _fields_ = [("raytrace_ms", C.c_double), ("total_ms", C.c_double), ("paths", C.c_uint64),
                 ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("batch", C.c_uint32),
@@ -155,6 +170,14 @@ SIGNATURES = {
     "vkg_tracer_statistics": (I32, [P, C.POINTER(vkg_tracer_stats)]),
     "vkg_tracer_destroy": (I32, [P]),
     "vkg_tracer_attach_cache": (I32, [P, P]),
+    "vkg_batch_tuning_default": (I32, [C.POINTER(vkg_batch_tuning)]),
+    "vkg_batch_create": (I32, [P, C.POINTER(vkg_batch_job), U32, C.POINTER(vkg_batch_tuning), C.POINTER(P)]),
+    "vkg_batch_autotune": (I32, [P, P, C.POINTER(vkg_batch_tuning)]),
+    "vkg_batch_set_tuning": (I32, [P, C.POINTER(vkg_batch_tuning)]),
+    "vkg_batch_render": (I32, [P, P]),
+    "vkg_batch_reset_accumulator": (I32, [P]),
+    "vkg_batch_statistics": (I32, [P, C.POINTER(vkg_batch_stats)]),
+    "vkg_batch_destroy": (I32, [P]),
     "vkg_diag_tc_gemm": (I32, [P, P, P, U32, U32, P, P, P]),
     "vkg_nrc_config_default": (I32, [C.POINTER(vkg_nrc_config)]),
     "vkg_nrc_create": (I32, [P, C.POINTER(vkg_nrc_config), C.POINTER(P)]),

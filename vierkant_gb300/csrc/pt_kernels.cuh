@@ -1,0 +1,649 @@
+// Wavefront path-tracer kernels shared by the single-scene tracer (pathtrace.cu) and the batch
+// renderer (batch.cu). The queue kernels are templated on a scene resolver: `single_scene` (one
+// scene per launch, its parameters in the kernel arguments) or `job_table` (every path carries the
+// index of its job in a device table). Everything lives in an anonymous namespace: each translation
+// unit instantiates its own kernels.
+#pragma once
+
+#include "nrc.cuh"
+#include "pathtrace.cuh"
+#include "traverse.cuh"
+
+// a scene: geometry, materials, its BVH and its environment tables
+struct vkg_scene
+{
+    vkg_bvh *bvh = nullptr;
+    float *xyz = nullptr;
+    uint32_t *idx = nullptr;
+    uint32_t *tri_mat = nullptr;
+    vkg_material *mats = nullptr;
+    uint32_t num_tris = 0, num_vertices = 0, num_materials = 0;
+    vkg::env_tables env;
+};
+
+namespace vkg
+{
+namespace
+{
+
+constexpr int PT_THREADS = 128;
+
+struct pt_params
+{
+    const node8 *nodes;
+    const tri_rec *tris;
+    const float *xyz;
+    const uint32_t *idx;
+    const uint32_t *tri_mat;
+    const vkg_material *mats;
+    env_view env;
+    vkg_camera cam;
+    uint32_t cx0, cy0, cw, ch, npix;
+    uint32_t max_depth, rr_depth, mis_mode, disable_material, draw_skybox;
+    float max_path_beta;
+    uint64_t seed, batch;
+    uint32_t s0; // first sample index of the wave
+    uint32_t term_depth;  // with a cache: interaction at which rendering paths become cache queries
+    uint32_t rec_depth;   // interactions recorded per training path
+    uint32_t train_base;  // paths [train_base, train_base + train_paths) of the wave are training paths
+    uint32_t train_paths;
+};
+
+// the shade kernel's two modes
+enum : int
+{
+    MODE_PLAIN = 0,
+    MODE_CACHE = 1
+};
+
+struct cache_io
+{
+    float *q_feat;
+    float4 *q_beta;
+    uint32_t *q_count;
+    float4 *rec;
+    uint32_t *vcount;
+};
+
+constexpr int REC_F4 = 5; // float4 per training record
+
+__device__ __forceinline__ uint64_t path_seq(const pt_params &P, uint32_t pid)
+{
+    if(pid >= P.train_base) return ((P.batch << 40) ^ (uint64_t)(pid - P.train_base)) ^ (1ull << 62);
+    const uint64_t g = (uint64_t)P.s0 * P.npix + pid; // = sample * npix + pixel
+    return (P.batch << 40) ^ g;
+}
+
+__device__ __forceinline__ uint32_t warp_push(uint32_t *count, bool pred)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const unsigned m = __ballot_sync(0xffffffffu, pred);
+    if(m == 0) return 0;
+    const uint32_t leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if(lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
+// scene parameters and PCG32 increment of a queued path: one scene per launch (the tracer) ...
+struct single_scene
+{
+    pt_params P;
+    static constexpr bool per_path = false;
+    __device__ __forceinline__ const pt_params &params(uint32_t) const { return P; }
+    __device__ __forceinline__ uint64_t inc(uint32_t pid) const { return (path_seq(P, pid) << 1u) | 1u; }
+};
+
+// ... or one job per path (the batch renderer): a job table plus per-path job index and increment
+struct job_table
+{
+    const pt_params *jobs;
+    const uint32_t *pjob;
+    const uint64_t *pinc;
+    static constexpr bool per_path = true;
+    __device__ __forceinline__ const pt_params &params(uint32_t pid) const { return jobs[pjob[pid]]; }
+    __device__ __forceinline__ uint64_t inc(uint32_t pid) const { return pinc[pid]; }
+};
+
+// camera ray through pixel (x, y) jittered by (jx, jy): PBRPathTracer's pinhole (raypipeline.slang:58-89)
+__device__ __forceinline__ void camera_ray(const vkg_camera &c, uint32_t x, uint32_t y, float jx, float jy,
+                                           float4 *o)
+{
+    const float sx = fdiv(fadd((float)x, jx), (float)c.width);
+    const float sy = fdiv(fadd((float)y, jy), (float)c.height);
+    const float nx = fsub(fmul(2.0f, sx), 1.0f), ny = fsub(fmul(2.0f, sy), 1.0f);
+    const float cx = fmul(nx, fmul(c.tan_half_fovy, c.aspect));
+    const float cy = -fmul(ny, c.tan_half_fovy);
+    float d[3];
+    for(int a = 0; a < 3; ++a) d[a] = fadd(fadd(fmul(c.right[a], cx), fmul(c.up[a], cy)), fmul(c.back[a], -1.0f));
+    const float inv = frcp(fsqrt(dot3(d[0], d[1], d[2], d[0], d[1], d[2])));
+    o[0] = make_float4(c.eye[0], c.eye[1], c.eye[2], PT_EPS);
+    o[1] = make_float4(fmul(d[0], inv), fmul(d[1], inv), fmul(d[2], inv), PT_TMAX);
+}
+
+__global__ void __launch_bounds__(PT_THREADS)
+        k_pt_generate(pt_params P, uint32_t n, vkg_ray *__restrict__ q_ray, uint32_t *__restrict__ q_pid,
+                      uint64_t *__restrict__ rng, float4 *__restrict__ beta_pdf, float4 *__restrict__ radiance,
+                      uint32_t *__restrict__ counters, uint32_t *__restrict__ vcount)
+{
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for(uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride)
+    {
+        pcg32 g = pcg32_seed(P.seed, path_seq(P, p));
+        uint32_t pix = p % P.npix;
+        if(p >= P.train_base)
+        {
+            // training path k: a random pixel of the k-th of train_paths equal runs of the window
+            // (stratified, so neighbouring lanes trace neighbouring pixels)
+            const uint64_t k = p - P.train_base, lo = k * P.npix / P.train_paths,
+                           hi = (k + 1) * P.npix / P.train_paths;
+            pix = (uint32_t)(lo + (hi > lo ? pcg32_next(g) % (uint32_t)(hi - lo) : 0u));
+            vcount[k] = 0;
+        }
+        const uint32_t x = P.cx0 + pix % P.cw, y = P.cy0 + pix / P.cw;
+        const float jx = u01(pcg32_next(g)), jy = u01(pcg32_next(g));
+        camera_ray(P.cam, x, y, jx, jy, reinterpret_cast<float4 *>(q_ray + p));
+        q_pid[p] = p;
+        rng[p] = g.state;
+        beta_pdf[p] = make_float4(1.f, 1.f, 1.f, 0.f);
+        radiance[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    if(blockIdx.x == 0 && threadIdx.x == 0) counters[0] = n;
+}
+
+template<class J>
+__global__ void __launch_bounds__(PT_THREADS)
+        k_pt_extend(J S, const vkg_ray *__restrict__ q_ray, const uint32_t *__restrict__ q_pid,
+                    const uint32_t *__restrict__ count, vkg_hit *__restrict__ hits)
+{
+    const uint32_t n = *count;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        const pt_params &P = S.params(J::per_path ? q_pid[i] : 0u);
+        const node8 *nodes = P.nodes;
+        const tri_rec *tris = P.tris;
+        const float4 *rp = reinterpret_cast<const float4 *>(q_ray + i);
+        const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
+        unsigned long long v = 0, t = 0;
+        trace_result r = trace_ray<false, false>(nodes, tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w,
+                                                 CULL_BACK_UNLESS_TWOSIDED, v, t, nullptr);
+        reinterpret_cast<uint4 *>(hits)[i] =
+                make_uint4(r.prim, __float_as_uint(r.t), __float_as_uint(r.u), __float_as_uint(r.v));
+    }
+}
+
+template<int MODE, class J>
+__global__ void __launch_bounds__(PT_THREADS)
+        k_pt_shade(J S, uint32_t depth, const vkg_ray *__restrict__ in_ray,
+                   const uint32_t *__restrict__ in_pid, const vkg_hit *__restrict__ hits,
+                   const uint32_t *__restrict__ in_count, vkg_ray *__restrict__ out_ray,
+                   uint32_t *__restrict__ out_pid, uint32_t *__restrict__ out_count, vkg_ray *__restrict__ s_ray,
+                   uint32_t *__restrict__ s_pid, float4 *__restrict__ s_contrib, uint32_t *__restrict__ s_count,
+                   uint64_t *__restrict__ rng, float4 *__restrict__ beta_pdf, float4 *__restrict__ radiance,
+                   cache_io io)
+{
+    const uint32_t n = *in_count;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for(uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride)
+    {
+        const uint32_t i = base + threadIdx.x;
+        const bool active = i < n;
+        bool push_ext = false, push_shadow = false, push_query = false;
+        float3 P0 = f3(0.f, 0.f, 0.f), ndir = P0, sdir = P0, N = P0;
+        float3 contrib = P0, qbeta = P0, albedo = P0, vq = P0;
+        float rough = 0.f;
+        uint32_t pid = 0;
+        if(active)
+        {
+            pid = in_pid[i];
+            const pt_params &P = S.params(pid);
+            const float4 *rp = reinterpret_cast<const float4 *>(in_ray + i);
+            const float4 r1 = rp[1];
+            const float3 dir = f3(r1.x, r1.y, r1.z);
+            const uint4 h = reinterpret_cast<const uint4 *>(hits)[i];
+            pcg32 g{rng[pid], S.inc(pid)};
+            float u[8];
+            for(int k = 0; k < 8; ++k) u[k] = u01(pcg32_next(g));
+            const float4 bp = beta_pdf[pid];
+            float3 beta = f3(bp.x, bp.y, bp.z);
+            float prev_pdf = bp.w;
+            const float4 lr = radiance[pid];
+            float3 L = f3(lr.x, lr.y, lr.z);
+            if(h.x == VKG_MISS)
+            {
+                // miss_environment (raypipeline.slang:764-781) with the hit-side MIS weight
+                const uint32_t t = env_texel(dir, P.env.w, P.env.h);
+                float3 le = env_radiance(P.env, t);
+                if(depth == 0 && !P.draw_skybox) le = f3(0.f, 0.f, 0.f);
+                float w = 1.f;
+                if(prev_pdf > 0.f)
+                {
+                    if(P.mis_mode == 1) w = 0.f;
+                    else if(P.mis_mode == 0) w = power_heuristic(prev_pdf, env_pdf(P.env, dir, t));
+                }
+                L = L + beta * le * w;
+            }
+            else
+            {
+                const uint32_t prim = h.x;
+                const float bu = __uint_as_float(h.z), bv = __uint_as_float(h.w);
+                const uint32_t i0 = __ldg(&P.idx[3 * (size_t)prim]), i1 = __ldg(&P.idx[3 * (size_t)prim + 1]),
+                               i2 = __ldg(&P.idx[3 * (size_t)prim + 2]);
+                const float3 v0 = f3(__ldg(&P.xyz[3 * (size_t)i0]), __ldg(&P.xyz[3 * (size_t)i0 + 1]),
+                                     __ldg(&P.xyz[3 * (size_t)i0 + 2]));
+                const float3 v1 = f3(__ldg(&P.xyz[3 * (size_t)i1]), __ldg(&P.xyz[3 * (size_t)i1 + 1]),
+                                     __ldg(&P.xyz[3 * (size_t)i1 + 2]));
+                const float3 v2 = f3(__ldg(&P.xyz[3 * (size_t)i2]), __ldg(&P.xyz[3 * (size_t)i2 + 1]),
+                                     __ldg(&P.xyz[3 * (size_t)i2 + 2]));
+                const float3 e1 = v1 - v0, e2 = v2 - v0;
+                P0 = v0 + e1 * bu + e2 * bv;
+                const float3 ng = normalize(cross(e1, e2));
+                N = dot(ng, dir) < 0.f ? ng : -ng; // shading normal faces the incoming ray
+                const float3 V = -dir;
+                const vkg_material mt = P.mats[__ldg(&P.tri_mat[prim])];
+                material_view m;
+                m.base = P.disable_material ? f3(0.8f, 0.8f, 0.8f) : f3(mt.base_color[0], mt.base_color[1], mt.base_color[2]);
+                m.roughness = mt.roughness;
+                m.metalness = mt.metalness;
+                L = L + beta * f3(mt.emission[0], mt.emission[1], mt.emission[2]);
+                if constexpr(MODE == MODE_CACHE)
+                {
+                    if(pid < P.train_base && depth == P.term_depth)
+                    {
+                        push_query = true;
+                        qbeta = beta;
+                        vq = V;
+                        albedo = m.base;
+                        rough = m.roughness;
+                    }
+                }
+                if constexpr(MODE == MODE_CACHE)
+                {
+                    if(pid >= P.train_base && depth < P.rec_depth)
+                    {
+                        const uint32_t k = pid - P.train_base;
+                        float4 *r = io.rec + ((size_t)k * P.rec_depth + depth) * REC_F4;
+                        r[0] = make_float4(P0.x, P0.y, P0.z, V.x);
+                        r[1] = make_float4(V.y, V.z, N.x, N.y);
+                        r[2] = make_float4(N.z, m.roughness, m.base.x, m.base.y);
+                        r[3] = make_float4(m.base.z, beta.x, beta.y, beta.z);
+                        r[4] = make_float4(L.x, L.y, L.z, 0.f);
+                        io.vcount[k] = depth + 1;
+                    }
+                }
+                // next-event estimation against the environment (mis_weight_nee, direct_lighting.slang:239-244)
+                if(!push_query && P.mis_mode != 2)
+                {
+                    float pdf_env;
+                    uint32_t texel;
+                    const float3 ld = env_sample(P.env, u[3], u[4], u[5], u[6], pdf_env, texel);
+                    const float cosl = dot(N, ld);
+                    if(pdf_env > 0.f && cosl > 0.f)
+                    {
+                        float pdf_b;
+                        const float3 f = eval_bsdf(m, ld, N, V, pdf_b);
+                        if(pdf_b > 0.f)
+                        {
+                            const float w = P.mis_mode == 1 ? 1.f : power_heuristic(pdf_env, pdf_b);
+                            contrib = beta * f * env_radiance(P.env, texel) * (w * cosl / pdf_env);
+                            if(max3(contrib) > 0.f)
+                            {
+                                push_shadow = true;
+                                sdir = ld;
+                            }
+                        }
+                    }
+                }
+                // BSDF sample (sample_disney) and throughput
+                const bsdf_sample bs = sample_bsdf(m, N, V, u[0], u[1], u[2]);
+                bool alive = bs.pdf > 0.f && !push_query;
+                if(alive)
+                {
+                    const float cost = fabsf(dot(N, bs.dir));
+                    float3 tp = bs.f * (cost / fmaxf(bs.pdf, PT_PDF_EPS));
+                    if(depth >= 1 && P.max_path_beta > 0.f)
+                        tp = f3(fminf(tp.x, P.max_path_beta), fminf(tp.y, P.max_path_beta), fminf(tp.z, P.max_path_beta));
+                    beta = beta * tp;
+                    float pdf_mix = 0.f;
+                    eval_bsdf(m, bs.dir, N, V, pdf_mix);
+                    prev_pdf = pdf_mix;
+                    // Russian roulette
+                    if(P.rr_depth == 0)
+                    {
+                        if(max3(beta) <= 0.05f * (float)depth)
+                        {
+                            const float q = 1.f - max3(beta);
+                            if(u[7] < q) alive = false;
+                            else beta = beta * (1.f / (1.f - q));
+                        }
+                    }
+                    else if(depth + 1 >= P.rr_depth)
+                    {
+                        const float q = fmaxf(0.f, 1.f - max3(beta));
+                        if(u[7] < q) alive = false;
+                        else beta = beta * (1.f / (1.f - q));
+                    }
+                    if(alive && depth + 1 < P.max_depth)
+                    {
+                        push_ext = true;
+                        ndir = bs.dir;
+                    }
+                }
+            }
+            rng[pid] = g.state;
+            beta_pdf[pid] = make_float4(beta.x, beta.y, beta.z, prev_pdf);
+            radiance[pid] = make_float4(L.x, L.y, L.z, 0.f);
+        }
+        const uint32_t pe = warp_push(out_count, push_ext);
+        if(push_ext)
+        {
+            float4 *o = reinterpret_cast<float4 *>(out_ray + pe);
+            o[0] = make_float4(P0.x, P0.y, P0.z, PT_EPS);
+            o[1] = make_float4(ndir.x, ndir.y, ndir.z, PT_TMAX);
+            out_pid[pe] = pid;
+        }
+        const uint32_t ps = warp_push(s_count, push_shadow);
+        if(push_shadow)
+        {
+            const float3 so = P0 + N * PT_EPS;
+            float4 *o = reinterpret_cast<float4 *>(s_ray + ps);
+            o[0] = make_float4(so.x, so.y, so.z, 0.f);
+            o[1] = make_float4(sdir.x, sdir.y, sdir.z, PT_TMAX);
+            s_pid[ps] = pid;
+            s_contrib[ps] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
+        }
+        if constexpr(MODE == MODE_CACHE)
+        {
+            const uint32_t pq = warp_push(io.q_count, push_query);
+            if(push_query)
+            {
+                // feature record: position, outgoing direction, normal, roughness, albedo
+                float *f = io.q_feat + (size_t)nrc::FEAT * pq;
+                const float3 V = vq;
+                f[0] = P0.x; f[1] = P0.y; f[2] = P0.z;
+                f[3] = V.x; f[4] = V.y; f[5] = V.z;
+                f[6] = N.x; f[7] = N.y; f[8] = N.z;
+                f[9] = rough;
+                f[10] = albedo.x; f[11] = albedo.y; f[12] = albedo.z;
+                io.q_beta[pq] = make_float4(qbeta.x, qbeta.y, qbeta.z, __uint_as_float(pid));
+            }
+        }
+    }
+}
+
+template<class J>
+__global__ void __launch_bounds__(PT_THREADS)
+        k_pt_shadow(J S, const vkg_ray *__restrict__ s_ray, const uint32_t *__restrict__ s_pid,
+                    const float4 *__restrict__ s_contrib, const uint32_t *__restrict__ count,
+                    float4 *__restrict__ radiance)
+{
+    const uint32_t n = *count;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        const pt_params &P = S.params(J::per_path ? s_pid[i] : 0u);
+        const node8 *nodes = P.nodes;
+        const tri_rec *tris = P.tris;
+        const float4 *rp = reinterpret_cast<const float4 *>(s_ray + i);
+        const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
+        unsigned long long v = 0, t = 0;
+        trace_result r = trace_ray<true, false>(nodes, tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, CULL_NONE,
+                                                v, t, nullptr);
+        if(!r.occluded)
+        {
+            const uint32_t pid = s_pid[i];
+            const float4 c = s_contrib[i];
+            float4 L = radiance[pid];
+            L.x += c.x;
+            L.y += c.y;
+            L.z += c.z;
+            radiance[pid] = L;
+        }
+    }
+}
+
+// persistent queue tracer: each warp refills its finished lanes from the queue with one atomic
+// (work stealing), so rays of cheap and expensive scenes balance across the machine. SHADOW: any-hit
+// visibility of NEE rays, adding the contribution of unoccluded ones; else closest hit of extension
+// rays. `work` must be zero at launch.
+template<bool SHADOW, class J>
+__global__ void __launch_bounds__(PT_THREADS)
+        k_pt_trace_persistent(J S, const vkg_ray *__restrict__ q_ray, const uint32_t *__restrict__ q_pid,
+                              const uint32_t *__restrict__ count, vkg_hit *__restrict__ hits,
+                              const float4 *__restrict__ s_contrib, float4 *__restrict__ radiance,
+                              uint32_t *__restrict__ work)
+{
+    const uint32_t n = *count;
+    const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
+    unsigned long long v = 0, t = 0;
+    ray_state s;
+    const node8 *nodes = nullptr;
+    const tri_rec *tris = nullptr;
+    uint32_t cur = 0xFFFFFFFFu;
+    bool exhausted = false;
+    for(;;)
+    {
+        const bool need = cur == 0xFFFFFFFFu && !exhausted;
+        const unsigned m = __ballot_sync(0xffffffffu, need);
+        if(m)
+        {
+            const uint32_t leader = __ffs(m) - 1;
+            uint32_t base = 0;
+            if(lane == leader) base = atomicAdd(work, (uint32_t)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if(need)
+            {
+                const uint32_t idx = base + __popc(m & lt);
+                if(idx < n)
+                {
+                    const pt_params &P = S.params(J::per_path ? q_pid[idx] : 0u);
+                    nodes = P.nodes;
+                    tris = P.tris;
+                    const float4 *rp = reinterpret_cast<const float4 *>(q_ray + idx);
+                    const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
+                    ray_init(s, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w);
+                    cur = idx;
+                }
+                else
+                    exhausted = true;
+            }
+        }
+        const bool active = cur != 0xFFFFFFFFu;
+        if(!__any_sync(0xffffffffu, active)) break;
+        if(active &&
+           !ray_step<SHADOW, false>(s, nodes, tris, SHADOW ? CULL_NONE : CULL_BACK_UNLESS_TWOSIDED, v, t, nullptr))
+        {
+            const trace_result r = ray_result(s);
+            if constexpr(SHADOW)
+            {
+                if(!r.occluded)
+                {
+                    const uint32_t pid = q_pid[cur];
+                    const float4 c = s_contrib[cur];
+                    float4 L = radiance[pid];
+                    L.x += c.x;
+                    L.y += c.y;
+                    L.z += c.z;
+                    radiance[pid] = L;
+                }
+            }
+            else
+                reinterpret_cast<uint4 *>(hits)[cur] =
+                        make_uint4(r.prim, __float_as_uint(r.t), __float_as_uint(r.u), __float_as_uint(r.v));
+            cur = 0xFFFFFFFFu;
+        }
+    }
+}
+
+__global__ void k_fill_miss_queue(const uint32_t *__restrict__ count, vkg_hit *__restrict__ hits)
+{
+    const uint32_t n = *count;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        reinterpret_cast<uint4 *>(hits)[i] = make_uint4(VKG_MISS, 0u, 0u, 0u);
+}
+
+__global__ void k_pt_tally(const uint32_t *__restrict__ ext_count, const uint32_t *__restrict__ s_count,
+                           unsigned long long *__restrict__ totals)
+{
+    totals[0] += *ext_count;
+    totals[1] += *s_count;
+}
+
+// rendering with a cache: path radiance += throughput x prediction (negative outputs clamped)
+__global__ void k_cache_resolve(const float4 *__restrict__ q_beta, const float *__restrict__ Y,
+                                const uint32_t *__restrict__ count, float4 *__restrict__ radiance,
+                                unsigned long long *__restrict__ totals)
+{
+    const uint32_t n = *count;
+    if(blockIdx.x == 0 && threadIdx.x == 0) totals[2] += n;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const float4 b = q_beta[i];
+        const uint32_t pid = __float_as_uint(b.w);
+        float4 L = radiance[pid];
+        L.x += b.x * fmaxf(Y[3 * (size_t)i], 0.f);
+        L.y += b.y * fmaxf(Y[3 * (size_t)i + 1], 0.f);
+        L.z += b.z * fmaxf(Y[3 * (size_t)i + 2], 0.f);
+        radiance[pid] = L;
+    }
+}
+
+// training wave done: one (features, target) pair per recorded interaction, compacted in path order
+__global__ void __launch_bounds__(PT_THREADS)
+        k_cache_targets(const float4 *__restrict__ rec, const uint32_t *__restrict__ vcount, uint32_t paths,
+                        uint32_t rec_depth, const float4 *__restrict__ radiance, float *__restrict__ t_feat,
+                        float *__restrict__ t_target, uint32_t *__restrict__ t_count)
+{
+    const uint32_t n = paths * rec_depth;
+    for(uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x)
+    {
+        const uint32_t i = base + threadIdx.x;
+        bool ok = false;
+        float f[nrc::FEAT], tg[3];
+        if(i < n)
+        {
+            const uint32_t p = i / rec_depth, k = i - p * rec_depth;
+            if(k < vcount[p])
+            {
+                const float4 *r = rec + (size_t)i * REC_F4;
+                const float4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3], r4 = r[4];
+                const float4 Lf = radiance[p];
+                const float beta[3] = {r3.y, r3.z, r3.w}, Lk[3] = {r4.x, r4.y, r4.z}, Lp[3] = {Lf.x, Lf.y, Lf.z};
+                ok = true;
+                for(int c = 0; c < 3; ++c)
+                {
+                    tg[c] = beta[c] > 0.f ? fmaxf(Lp[c] - Lk[c], 0.f) / beta[c] : 0.f;
+                    ok = ok && isfinite(tg[c]);
+                }
+                const float v[nrc::FEAT] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w, r3.x};
+                for(int c = 0; c < nrc::FEAT; ++c) f[c] = v[c];
+            }
+        }
+        const uint32_t o = warp_push(t_count, ok);
+        if(ok)
+        {
+            for(int c = 0; c < nrc::FEAT; ++c) t_feat[(size_t)o * nrc::FEAT + c] = f[c];
+            for(int c = 0; c < 3; ++c) t_target[(size_t)o * 3 + c] = tg[c];
+        }
+    }
+}
+
+// optimiser step k of the frame trains on the window [k * B, (k + 1) * B) of the compacted records
+__global__ void k_cache_window(const uint32_t *__restrict__ t_count, uint32_t k, uint32_t B,
+                               uint32_t *__restrict__ b_count)
+{
+    const uint64_t cnt = *t_count, lo = (uint64_t)k * B;
+    *b_count = cnt > lo ? (uint32_t)std::min<uint64_t>(cnt - lo, B) : 0u;
+}
+
+__global__ void k_pt_accumulate(uint32_t npix, uint32_t ns, const float4 *__restrict__ radiance, float *__restrict__ sum)
+{
+    uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if(pix >= npix) return;
+    float sx = sum[3 * (size_t)pix], sy = sum[3 * (size_t)pix + 1], sz = sum[3 * (size_t)pix + 2];
+    for(uint32_t k = 0; k < ns; ++k)
+    {
+        const float4 L = radiance[(size_t)k * npix + pix];
+        sx += L.x;
+        sy += L.y;
+        sz += L.z;
+    }
+    sum[3 * (size_t)pix] = sx;
+    sum[3 * (size_t)pix + 1] = sy;
+    sum[3 * (size_t)pix + 2] = sz;
+}
+
+__global__ void k_pt_finalize(uint32_t npix, uint32_t spp, uint32_t batch, const float *__restrict__ sum,
+                              float *__restrict__ accum, float *__restrict__ out)
+{
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if(k >= 3 * npix) return;
+    const float mean = sum[k] / (float)spp;
+    const float a = batch == 0 ? mean : (mean + (float)batch * accum[k]) / (float)(batch + 1);
+    accum[k] = a;
+    if(out) out[k] = a;
+}
+
+__global__ void k_tri_flags(tri_rec *__restrict__ tris, uint32_t n, const uint32_t *__restrict__ tri_mat,
+                            const vkg_material *__restrict__ mats, uint32_t num_mats)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n) return;
+    const uint32_t m = tri_mat[tris[i].prim];
+    tris[i].pad[0] = (m < num_mats && mats[m].twosided) ? TRI_FLAG_TWOSIDED : 0u;
+}
+
+__global__ void k_check_materials(const uint32_t *__restrict__ tri_mat, uint32_t n, uint32_t num_mats,
+                                  uint32_t *__restrict__ bad)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i < n && tri_mat[i] >= num_mats) atomicOr(bad, 1u);
+}
+
+}// namespace
+
+// settings checks shared by the tracer and the batch renderer (pathtrace.cu)
+vkg_status check_tracer_settings(vkg_ctx *ctx, const vkg_settings *s);
+
+// the crop window of a settings block: (x0, y0, width, height); the whole image if no crop is set
+inline void crop_window(const vkg_settings &S, uint32_t &x0, uint32_t &y0, uint32_t &w, uint32_t &h)
+{
+    const bool crop = S.crop[2] && S.crop[3];
+    x0 = crop ? S.crop[0] : 0;
+    y0 = crop ? S.crop[1] : 0;
+    w = crop ? S.crop[2] : S.resolution[0];
+    h = crop ? S.crop[3] : S.resolution[1];
+}
+
+// the per-launch parameters of one scene, camera and settings block (no radiance cache)
+inline pt_params make_params(const vkg_scene *sc, const vkg_camera &cam, const vkg_settings &S, uint32_t seed,
+                             uint32_t batch)
+{
+    pt_params P{};
+    P.nodes = sc->bvh->d_nodes;
+    P.tris = sc->bvh->d_tris;
+    P.xyz = sc->xyz;
+    P.idx = sc->idx;
+    P.tri_mat = sc->tri_mat;
+    P.mats = sc->mats;
+    P.env = env_view{sc->env.rgb, sc->env.pdf_w, sc->env.alias, sc->env.w, sc->env.h, S.environment};
+    P.cam = cam;
+    crop_window(S, P.cx0, P.cy0, P.cw, P.ch);
+    P.npix = P.cw * P.ch;
+    P.max_depth = S.max_trace_depth;
+    P.rr_depth = S.rr_start_depth;
+    P.mis_mode = S.mis_mode;
+    P.disable_material = S.disable_material;
+    P.draw_skybox = S.draw_skybox;
+    P.max_path_beta = S.max_path_beta;
+    P.seed = seed;
+    P.batch = batch;
+    P.term_depth = 0xFFFFFFFFu;
+    P.rec_depth = 0;
+    P.train_base = 0xFFFFFFFFu;
+    P.train_paths = 0;
+    return P;
+}
+}// namespace vkg

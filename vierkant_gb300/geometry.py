@@ -55,3 +55,43 @@ def camera_lookat(eye, target, up, fovy_deg: float, width: int, height: int) -> 
     tan_half = float(np.float32(math.tan(math.radians(fovy_deg) / 2.0)))
     check(L.vkg_camera_lookat(_p(e), _p(t), _p(u), C.c_float(tan_half), width, height, C.byref(cam)))
     return cam
+
+
+class _Pcg32:
+    """PCG32 (XSH-RR, O'Neill 2014) for host-side workload parameters; the same generator as the kernels'."""
+    MULT = 6364136223846793005
+    MASK = (1 << 64) - 1
+
+    def __init__(self, initstate: int, initseq: int):
+        self.state = 0
+        self.inc = ((initseq << 1) | 1) & self.MASK
+        self.next()
+        self.state = (self.state + initstate) & self.MASK
+        self.next()
+
+    def next(self) -> int:
+        old = self.state
+        self.state = (old * self.MULT + self.inc) & self.MASK
+        xorshifted = (((old >> 18) ^ old) >> 27) & 0xFFFFFFFF
+        rot = old >> 59
+        return ((xorshifted >> rot) | (xorshifted << ((-rot) & 31))) & 0xFFFFFFFF
+
+    def uniform(self) -> float:
+        return (self.next() >> 8) * (1.0 / (1 << 24))
+
+
+BATCH_RESOLUTIONS = (256, 512, 768, 1024)
+BATCH_SPP = (4, 16, 64)
+
+
+def batch_scene_params(index: int, seed: int = 0x5EED, min_tris: int = 5_000, max_tris: int = 2_000_000):
+    """Parameters of scene `index` of the batched uneven workload (PCG32 seed 0x5EED, stream 3 + index):
+    triangle count log-uniform in [min_tris, max_tris] (a Cornell box plus that many 3,072-triangle
+    cube-spheres as fit, at least one), square resolution from {256, 512, 768, 1024}, spp from {4, 16, 64}.
+    Returns dict(stream, spheres, triangles, resolution, spp)."""
+    g = _Pcg32(seed, 3 + index)
+    u_tris, u_res, u_spp = g.uniform(), g.uniform(), g.uniform()
+    target = math.exp(math.log(min_tris) + u_tris * (math.log(max_tris) - math.log(min_tris)))
+    spheres = max(1, int(round((target - 10) / 3072)))
+    return {"stream": 3 + index, "spheres": spheres, "triangles": 10 + 3072 * spheres,
+            "resolution": BATCH_RESOLUTIONS[min(3, int(u_res * 4))], "spp": BATCH_SPP[min(2, int(u_spp * 3))]}
