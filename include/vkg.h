@@ -234,6 +234,49 @@ vkg_status vkg_closest_hit_host(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray 
 vkg_status vkg_ray_stats_get(vkg_ctx *ctx, uint64_t *node_visits, uint64_t *tri_tests, int reset);
 
 
+/* ---- two-level BVH (instances over bottom-level BVHs) ------------------------------------------- *
+ * RayBuilder::create_toplevel (RayBuilder.cpp:386-760) builds the driver TLAS over mesh entries that
+ * carry a vk_transform_matrix (:518). Here the top level is the same 8-wide quantised BVH over the
+ * instances' world boxes; a ray reaching an instance leaf is moved to object space (separately
+ * rounded float operations) and traced through that instance's BLAS. Transforms with a negative
+ * determinant mirror the geometry and therefore flip the back-face rule. */
+typedef struct vkg_instance
+{
+    float transform[12]; /* object -> world, row-major 3x4 (VkTransformMatrixKHR layout) */
+    uint32_t blas;       /* index into the BLAS array given to vkg_tlas_build */
+    uint32_t material;   /* material index for the path tracer */
+    uint32_t pad[2];
+} vkg_instance;          /* 64 B */
+/* closest hit of a two-level query; a miss has prim = instance = 0xFFFFFFFF. Closest-hit ties
+ * (equal t) go to the smaller instance, then the smaller triangle. */
+typedef struct vkg_inst_hit
+{
+    uint32_t prim;       /* triangle id within the instance's mesh */
+    uint32_t instance;   /* input index of the instance */
+    float t, u, v;
+    uint32_t pad[3];
+} vkg_inst_hit;          /* 32 B */
+typedef struct vkg_tlas vkg_tlas;
+typedef struct vkg_tlas_info
+{
+    uint32_t num_instances, num_blas, num_nodes, depth;
+    float scene_min[3], scene_max[3];
+    const void *d_nodes;           /* 96 B nodes */
+    const void *d_instances;       /* 128 B records {w2o[12], o2w[12], blas, instance, material, pad[5]}, leaf order */
+    const void *d_instances_by_id; /* the same records in input order */
+    float build_ms;
+} vkg_tlas_info;
+/* d_instances: device array; the BLASes must outlive the TLAS. Synchronises like vkg_bvh_build. */
+vkg_status vkg_tlas_build(vkg_ctx *ctx, const vkg_bvh *const *blas, uint32_t num_blas, const vkg_instance *d_instances,
+                          uint32_t num_instances, const vkg_bvh_build_options *opts, vkg_tlas **out, void *stream);
+vkg_status vkg_tlas_info_get(const vkg_tlas *tlas, vkg_tlas_info *out);
+vkg_status vkg_tlas_destroy(vkg_ctx *ctx, vkg_tlas *tlas);
+/* flags: VKG_RAY_CULL_BACK_FACES (object-space facing) */
+vkg_status vkg_tlas_closest_hit(vkg_ctx *ctx, const vkg_tlas *tlas, const vkg_ray *d_rays, uint32_t n,
+                                vkg_inst_hit *d_hits, uint32_t flags, void *stream);
+vkg_status vkg_tlas_any_hit(vkg_ctx *ctx, const vkg_tlas *tlas, const vkg_ray *d_rays, uint32_t n, uint32_t *d_occluded,
+                            uint32_t flags, void *stream);
+
 /* ---- environment map ------------------------------------------------------------------------ *
  * Equirectangular fp32 RGB, u = 0.5 + 0.5 * atan2(x, -z) / pi, v = acos(y) / pi
  * (shaders/slang/unlit/panorama.slang:12-15), texel (i, j) at d_rgb[3 * (j * width + i)].

@@ -218,6 +218,29 @@ class CpuBVH:
         return occ
 
 
+INST_HIT_DTYPE = np.dtype([("prim", "<u4"), ("inst", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4"),
+                           ("pad", "<u4", 3)])
+
+
+def tlas_closest_hit(blas: list, w2o, inst_blas, rays, cull=False, nthreads=0):
+    """two-level closest hit (oracle/tlas.c): instances in input order, w2o [N, 12] world -> object"""
+    w2o = np.ascontiguousarray(w2o, np.float32)
+    ib = np.ascontiguousarray(inst_blas, np.uint32)
+    arr = (C.POINTER(orc_bvh) * len(blas))(*[C.pointer(b.b) for b in blas])
+    hits = np.zeros(len(rays), INST_HIT_DTYPE)
+    orc().orc_tlas_closest_hit(arr, ptr(w2o), ptr(ib), len(ib), ptr(rays), len(rays), int(cull), ptr(hits), nthreads)
+    return hits
+
+
+def tlas_any_hit(blas: list, w2o, inst_blas, rays, cull=False, nthreads=0):
+    w2o = np.ascontiguousarray(w2o, np.float32)
+    ib = np.ascontiguousarray(inst_blas, np.uint32)
+    arr = (C.POINTER(orc_bvh) * len(blas))(*[C.pointer(b.b) for b in blas])
+    occ = np.zeros(len(rays), np.uint32)
+    orc().orc_tlas_any_hit(arr, ptr(w2o), ptr(ib), len(ib), ptr(rays), len(rays), int(cull), ptr(occ), nthreads)
+    return occ
+
+
 # ---- path tracer (FP32 twin / FP64 oracle) ---------------------------------------------------------
 MATERIAL_DTYPE = np.dtype([("base_color", "<f4", 3), ("roughness", "<f4"), ("metalness", "<f4"),
                            ("emission", "<f4", 3), ("twosided", "<u4"), ("pad", "<f4", 3)])

@@ -109,6 +109,11 @@ int orc_bvh_any_hit(const orc_bvh *b, const orc_ray *rays, uint32_t nray, uint32
 /* single ray; cull_mode 0 none, 1 all back faces, 2 back faces of triangles with twosided[prim] == 0 */
 void orc_bvh_trace1(const orc_bvh *b, const orc_ray *ray, int cull_mode, const uint8_t *twosided, int any,
                     orc_hit *hit, uint32_t *occ);
+/* two-level queries: instances in input order, w2o [ninst][12], hits are 32-byte {prim, inst, t, u, v, pad} */
+int orc_tlas_closest_hit(const orc_bvh *const *blas, const float *w2o, const uint32_t *inst_blas, uint32_t ninst,
+                         const orc_ray *rays, uint32_t nray, int cull, void *hits, int nthreads);
+int orc_tlas_any_hit(const orc_bvh *const *blas, const float *w2o, const uint32_t *inst_blas, uint32_t ninst,
+                     const orc_ray *rays, uint32_t nray, int cull, uint32_t *occluded, int nthreads);
 
 /* ---- path tracer (FP32 twin of the GPU kernels / FP64 radiance oracle) ------------------ */
 typedef struct {

@@ -64,6 +64,13 @@ class vkg_tracer_create_info(C.Structure):
     _fields_ = [("seed", C.c_uint32), ("settings", vkg_settings)]
 
 
+class vkg_tlas_info(C.Structure):
+    _fields_ = [("num_instances", C.c_uint32), ("num_blas", C.c_uint32), ("num_nodes", C.c_uint32),
+                ("depth", C.c_uint32), ("scene_min", C.c_float * 3), ("scene_max", C.c_float * 3),
+                ("d_nodes", C.c_void_p), ("d_instances", C.c_void_p), ("d_instances_by_id", C.c_void_p),
+                ("build_ms", C.c_float)]
+
+
 class vkg_batch_job(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("camera", vkg_camera), ("settings", vkg_settings), ("seed", C.c_uint32),
                 ("pad", C.c_uint32), ("d_rgb_out", C.c_void_p)]
@@ -170,6 +177,11 @@ SIGNATURES = {
     "vkg_tracer_statistics": (I32, [P, C.POINTER(vkg_tracer_stats)]),
     "vkg_tracer_destroy": (I32, [P]),
     "vkg_tracer_attach_cache": (I32, [P, P]),
+    "vkg_tlas_build": (I32, [P, P, U32, P, U32, P, C.POINTER(P), P]),
+    "vkg_tlas_info_get": (I32, [P, C.POINTER(vkg_tlas_info)]),
+    "vkg_tlas_destroy": (I32, [P, P]),
+    "vkg_tlas_closest_hit": (I32, [P, P, P, U32, P, U32, P]),
+    "vkg_tlas_any_hit": (I32, [P, P, P, U32, P, U32, P]),
     "vkg_batch_tuning_default": (I32, [C.POINTER(vkg_batch_tuning)]),
     "vkg_batch_create": (I32, [P, C.POINTER(vkg_batch_job), U32, C.POINTER(vkg_batch_tuning), C.POINTER(P)]),
     "vkg_batch_autotune": (I32, [P, P, C.POINTER(vkg_batch_tuning)]),

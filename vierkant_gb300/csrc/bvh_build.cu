@@ -46,8 +46,9 @@ __device__ __forceinline__ float fdec(uint32_t u) { return __uint_as_float((u & 
 // errors reported by the build kernels
 enum : uint32_t
 {
-    BUILD_ERR_INDEX = 1u,    // an index >= num_vertices
+    BUILD_ERR_INDEX = 1u,    // an index >= num_vertices (triangles) / a BLAS index >= num_blas (instances)
     BUILD_ERR_CAPACITY = 2u, // node capacity exceeded
+    BUILD_ERR_SINGULAR = 4u, // an instance transform that cannot be inverted
 };
 
 __global__ void k_tri_boxes(const float *__restrict__ xyz, uint32_t nv, const uint32_t *__restrict__ idx, uint32_t n,
@@ -570,38 +571,136 @@ cudaError_t dalloc(T **p, size_t count, cudaStream_t s)
     return cudaMallocAsync(reinterpret_cast<void **>(p), count * sizeof(T) + 16, s);
 }
 
-}// namespace
-}// namespace vkg
-
-using namespace vkg;
-
-extern "C" vkg_status vkg_bvh_build(vkg_ctx *ctx, const float *d_xyz, uint32_t num_vertices,
-                                    const uint32_t *d_indices, uint32_t num_tris, const vkg_bvh_build_options *opts,
-                                    vkg_bvh **out, void *stream_)
+// ---- instances (two-level BVH) -------------------------------------------------------------------
+struct blas_box
 {
-    if(!ctx) return VKG_ERR_INVALID_ARGUMENT;
-    if(!out) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_bvh_build: out is NULL");
-    *out = nullptr;
-    if(num_tris > 0 && (!d_xyz || !d_indices || num_vertices == 0))
-        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_bvh_build: NULL geometry for %u triangles", num_tris);
-    if(num_tris >= MAX_TRIS)
-        return set_error(ctx, VKG_ERR_CAPACITY, "vkg_bvh_build: %u triangles exceed the maximum of %u", num_tris,
-                         MAX_TRIS - 1);
-    uint32_t leaf_max = (opts && opts->leaf_max) ? opts->leaf_max : 4u;
-    if(leaf_max > LEAF_MAX_LIMIT)
-        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_bvh_build: leaf_max %u > %u", leaf_max, LEAF_MAX_LIMIT);
-    if(vkg_status s = bind_device(ctx); s != VKG_OK) return s;
+    float lo[3], hi[3];
+    uint32_t num_tris, pad;
+};
 
-    cudaStream_t st = static_cast<cudaStream_t>(stream_);
-    auto *bvh = new vkg_bvh();
-    bvh->num_tris = num_tris;
-    bvh->leaf_max = leaf_max;
-    if(num_tris == 0)
+// world -> object transform of an object -> world 3x4 transform: inverse of the 3x3 part by the
+// adjugate in double precision, translation -A^-1 t, rounded to float once. false if singular.
+__device__ __forceinline__ bool invert_3x4(const float *m, float *inv)
+{
+    const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], h = m[9], i = m[10];
+    const double A = __dsub_rn(__dmul_rn(e, i), __dmul_rn(f, h));
+    const double B = __dsub_rn(__dmul_rn(f, g), __dmul_rn(d, i));
+    const double C = __dsub_rn(__dmul_rn(d, h), __dmul_rn(e, g));
+    const double det = __dadd_rn(__dadd_rn(__dmul_rn(a, A), __dmul_rn(b, B)), __dmul_rn(c, C));
+    if(!(fabs(det) > 1e-30) || !isfinite(det)) return false;
+    const double r = 1.0 / det;
+    const double M[9] = {A, __dsub_rn(__dmul_rn(c, h), __dmul_rn(b, i)), __dsub_rn(__dmul_rn(b, f), __dmul_rn(c, e)),
+                         B, __dsub_rn(__dmul_rn(a, i), __dmul_rn(c, g)), __dsub_rn(__dmul_rn(c, d), __dmul_rn(a, f)),
+                         C, __dsub_rn(__dmul_rn(b, g), __dmul_rn(a, h)), __dsub_rn(__dmul_rn(a, e), __dmul_rn(b, d))};
+    const double t[3] = {m[3], m[7], m[11]};
+    for(int row = 0; row < 3; ++row)
     {
-        *out = bvh;
-        return VKG_OK;
+        double acc = 0.0;
+        for(int k = 0; k < 3; ++k)
+        {
+            const double v = __dmul_rn(M[3 * row + k], r);
+            inv[4 * row + k] = __double2float_rn(v);
+            acc = __dadd_rn(acc, __dmul_rn(v, t[k]));
+        }
+        inv[4 * row + 3] = __double2float_rn(-acc);
     }
-    const uint32_t n = num_tris;
+    return true;
+}
+
+__global__ void k_instance_boxes(const vkg_instance *__restrict__ inst, uint32_t n, const blas_box *__restrict__ bb,
+                                 uint32_t nblas, box6 *__restrict__ tbox, uint32_t *__restrict__ scene_enc,
+                                 uint32_t *__restrict__ err)
+{
+    __shared__ uint32_t s_lo[3], s_hi[3];
+    if(threadIdx.x < 3)
+    {
+        s_lo[threadIdx.x] = fenc(__int_as_float(0x7f800000));
+        s_hi[threadIdx.x] = fenc(__int_as_float(0xff800000));
+    }
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i < n)
+    {
+        const vkg_instance I = inst[i];
+        box6 b;
+        uint32_t bl = I.blas;
+        if(bl >= nblas)
+        {
+            atomicOr(err, BUILD_ERR_INDEX);
+            bl = 0;
+        }
+        const blas_box B = bb[bl];
+        float inv[12];
+        if(!invert_3x4(I.transform, inv)) atomicOr(err, BUILD_ERR_SINGULAR);
+        if(B.num_tris == 0)
+        {
+            // an empty mesh: a point box at the instance origin (the traversal skips it)
+            for(int a = 0; a < 3; ++a) b.lo[a] = b.hi[a] = I.transform[4 * a + 3];
+        }
+        else
+        {
+            double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+            for(int c = 0; c < 8; ++c)
+            {
+                const double p[3] = {(c & 1) ? B.hi[0] : B.lo[0], (c & 2) ? B.hi[1] : B.lo[1], (c & 4) ? B.hi[2] : B.lo[2]};
+                for(int a = 0; a < 3; ++a)
+                {
+                    const double w = (double)I.transform[4 * a] * p[0] + (double)I.transform[4 * a + 1] * p[1] +
+                                     (double)I.transform[4 * a + 2] * p[2] + (double)I.transform[4 * a + 3];
+                    lo[a] = fmin(lo[a], w);
+                    hi[a] = fmax(hi[a], w);
+                }
+            }
+            // rounded outward; the collapse grows every box by its margin on top
+            for(int a = 0; a < 3; ++a)
+            {
+                b.lo[a] = __double2float_rd(lo[a]);
+                b.hi[a] = __double2float_ru(hi[a]);
+            }
+        }
+        tbox[i] = b;
+        for(int a = 0; a < 3; ++a)
+        {
+            atomicMin(&s_lo[a], fenc(b.lo[a]));
+            atomicMax(&s_hi[a], fenc(b.hi[a]));
+        }
+    }
+    __syncthreads();
+    if(threadIdx.x < 3)
+    {
+        atomicMin(&scene_enc[threadIdx.x], s_lo[threadIdx.x]);
+        atomicMax(&scene_enc[3 + threadIdx.x], s_hi[threadIdx.x]);
+    }
+}
+
+// instance records in leaf (sorted) order and in input order
+__global__ void k_instance_records(const vkg_instance *__restrict__ inst, const uint32_t *__restrict__ sorted,
+                                   uint32_t n, uint32_t nblas, inst_rec *__restrict__ out, inst_rec *__restrict__ by_id)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n) return;
+    const uint32_t id = sorted[i];
+    const vkg_instance I = inst[id];
+    inst_rec r{};
+    if(!invert_3x4(I.transform, r.w2o))
+        for(int k = 0; k < 12; ++k) r.w2o[k] = 0.f;
+    for(int k = 0; k < 12; ++k) r.o2w[k] = I.transform[k];
+    r.blas = I.blas < nblas ? I.blas : 0u;
+    r.instance = id;
+    r.material = I.material;
+    out[i] = r;
+    by_id[id] = r;
+}
+
+// The primitive-independent part of a build: make_boxes(tbox, scene_enc, err) fills the n primitive
+// boxes, the scene box (ordered uints) and error bits; Morton codes, the radix sort, the Karras tree,
+// the refit and the 8-wide collapse follow; make_records(sorted) writes the leaf records in sorted
+// order. On success bvh holds the nodes, Morton codes, sorted order, scene box, margin and depth, and
+// err_bits the error bits that make_boxes raised. The caller frees bvh on failure.
+template<class MakeBoxes, class MakeRecords>
+vkg_status build_core(vkg_ctx *ctx, vkg_bvh *bvh, uint32_t n, uint32_t leaf_max, cudaStream_t st,
+                      MakeBoxes make_boxes, MakeRecords make_records, uint32_t &err_bits)
+{
     cudaEvent_t ev0, ev1;
     cudaEventCreate(&ev0);
     cudaEventCreate(&ev1);
@@ -642,13 +741,8 @@ extern "C" vkg_status vkg_bvh_build(vkg_ctx *ctx, const float *d_xyz, uint32_t n
     chk(dalloc(&d_margin, 1, st));
     chk(dalloc(&bvh->d_morton, n, st));
     chk(dalloc(&bvh->d_sorted, n, st));
-    chk(dalloc(&bvh->d_tris, n, st));
     if(e != cudaSuccess)
-    {
-        vkg_bvh_destroy(ctx, bvh);
-        return set_error(ctx, VKG_ERR_OUT_OF_MEMORY, "vkg_bvh_build: device allocation failed (%s)",
-                         cudaGetErrorString(e));
-    }
+        return set_error(ctx, VKG_ERR_OUT_OF_MEMORY, "BVH build: device allocation failed (%s)", cudaGetErrorString(e));
     // small[0..5] scene box (ordered uints), [6] error flags, [8..10] collapse info
     uint32_t init[16] = {0xFF800000u, 0xFF800000u, 0xFF800000u, 0x007FFFFFu, 0x007FFFFFu, 0x007FFFFFu, 0, 0,
                          0,           0,           0,           0,           0,           0,           0, 0};
@@ -658,7 +752,7 @@ extern "C" vkg_status vkg_bvh_build(vkg_ctx *ctx, const float *d_xyz, uint32_t n
 
     const int T = 256;
     const uint32_t g = (n + T - 1) / T;
-    k_tri_boxes<<<g, T, 0, st>>>(d_xyz, num_vertices, d_indices, n, tbox, small, small + 6);
+    make_boxes(tbox, small, small + 6);
     k_morton<<<g, T, 0, st>>>(tbox, n, small, keys0, vals0, bvh->d_morton);
     uint32_t *kin = keys0, *kout = keys1, *vin = vals0, *vout = vals1;
     for(int shift = 0; shift < 30; shift += 8)
@@ -679,7 +773,7 @@ extern "C" vkg_status vkg_bvh_build(vkg_ctx *ctx, const float *d_xyz, uint32_t n
     collapse_args A{left, right, first, last, ibox, lbox, n, leaf_max, capacity, small, node_ref, nodes_tmp,
                     small + 8, d_margin};
     k_collapse<<<1, COLLAPSE_THREADS, 0, st>>>(A);
-    k_tri_records<<<g, T, 0, st>>>(d_xyz, num_vertices, d_indices, vin, n, bvh->d_tris);
+    make_records(static_cast<const uint32_t *>(vin));
     chk(cudaGetLastError());
 
     uint32_t info[16];
@@ -715,29 +809,71 @@ extern "C" vkg_status vkg_bvh_build(vkg_ctx *ctx, const float *d_xyz, uint32_t n
     cudaEventElapsedTime(&bvh->build_ms, ev0, ev1);
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
-    if(e != cudaSuccess)
-    {
-        vkg_bvh_destroy(ctx, bvh);
-        return cuda_check(ctx, e, "vkg_bvh_build");
-    }
-    if(info[6] & BUILD_ERR_INDEX)
-    {
-        vkg_bvh_destroy(ctx, bvh);
-        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_bvh_build: triangle index >= num_vertices (%u)",
-                         num_vertices);
-    }
-    if(info[10] & BUILD_ERR_CAPACITY)
-    {
-        vkg_bvh_destroy(ctx, bvh);
-        return set_error(ctx, VKG_ERR_CAPACITY, "vkg_bvh_build: node capacity exceeded");
-    }
+    if(e != cudaSuccess) return cuda_check(ctx, e, "BVH build");
+    err_bits = info[6];
+    if(info[10] & BUILD_ERR_CAPACITY) return set_error(ctx, VKG_ERR_CAPACITY, "BVH build: node capacity exceeded");
     const uint32_t max_depth = (TRAVERSAL_STACK - 1) / 7 + 1;
     if(bvh->depth > max_depth)
-    {
-        uint32_t d = bvh->depth;
-        vkg_bvh_destroy(ctx, bvh);
-        return set_error(ctx, VKG_ERR_CAPACITY, "vkg_bvh_build: BVH depth %u exceeds the traversal limit %u", d,
+        return set_error(ctx, VKG_ERR_CAPACITY, "BVH build: depth %u exceeds the traversal limit %u", bvh->depth,
                          max_depth);
+    return VKG_OK;
+}
+
+}// namespace
+}// namespace vkg
+
+using namespace vkg;
+
+extern "C" vkg_status vkg_bvh_build(vkg_ctx *ctx, const float *d_xyz, uint32_t num_vertices,
+                                    const uint32_t *d_indices, uint32_t num_tris, const vkg_bvh_build_options *opts,
+                                    vkg_bvh **out, void *stream_)
+{
+    if(!ctx) return VKG_ERR_INVALID_ARGUMENT;
+    if(!out) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_bvh_build: out is NULL");
+    *out = nullptr;
+    if(num_tris > 0 && (!d_xyz || !d_indices || num_vertices == 0))
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_bvh_build: NULL geometry for %u triangles", num_tris);
+    if(num_tris >= MAX_TRIS)
+        return set_error(ctx, VKG_ERR_CAPACITY, "vkg_bvh_build: %u triangles exceed the maximum of %u", num_tris,
+                         MAX_TRIS - 1);
+    uint32_t leaf_max = (opts && opts->leaf_max) ? opts->leaf_max : 4u;
+    if(leaf_max > LEAF_MAX_LIMIT)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_bvh_build: leaf_max %u > %u", leaf_max, LEAF_MAX_LIMIT);
+    if(vkg_status s = bind_device(ctx); s != VKG_OK) return s;
+
+    cudaStream_t st = static_cast<cudaStream_t>(stream_);
+    auto *bvh = new vkg_bvh();
+    bvh->num_tris = num_tris;
+    bvh->leaf_max = leaf_max;
+    if(num_tris == 0)
+    {
+        *out = bvh;
+        return VKG_OK;
+    }
+    const uint32_t n = num_tris;
+    if(cudaMallocAsync(reinterpret_cast<void **>(&bvh->d_tris), n * sizeof(tri_rec) + 16, st) != cudaSuccess)
+    {
+        vkg_bvh_destroy(ctx, bvh);
+        return set_error(ctx, VKG_ERR_OUT_OF_MEMORY, "vkg_bvh_build: device allocation failed");
+    }
+    const int T = 256;
+    const uint32_t g = (n + T - 1) / T;
+    uint32_t err_bits = 0;
+    vkg_status s = build_core(
+            ctx, bvh, n, leaf_max, st,
+            [&](box6 *tbox, uint32_t *scene_enc, uint32_t *err) {
+                k_tri_boxes<<<g, T, 0, st>>>(d_xyz, num_vertices, d_indices, n, tbox, scene_enc, err);
+            },
+            [&](const uint32_t *sorted) {
+                k_tri_records<<<g, T, 0, st>>>(d_xyz, num_vertices, d_indices, sorted, n, bvh->d_tris);
+            },
+            err_bits);
+    if(s == VKG_OK && (err_bits & BUILD_ERR_INDEX))
+        s = set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_bvh_build: triangle index >= num_vertices (%u)", num_vertices);
+    if(s != VKG_OK)
+    {
+        vkg_bvh_destroy(ctx, bvh);
+        return s;
     }
     bvh->bytes = sizeof(node8) * bvh->num_nodes + sizeof(tri_rec) * n + 8 * (size_t)n;
     *out = bvh;
@@ -776,6 +912,139 @@ extern "C" vkg_status vkg_bvh_destroy(vkg_ctx *ctx, vkg_bvh *bvh)
     cudaFree(bvh->d_morton);
     cudaFree(bvh->d_sorted);
     delete bvh;
+    return VKG_OK;
+}
+
+// ---- two-level BVH -----------------------------------------------------------------------------
+// The top level is the same 8-wide quantised BVH, built by the same core over the instances' world
+// boxes (the 8 transformed corners of the mesh's bounds, rounded outward); its leaves index
+// 128-byte instance records (world <-> object transforms, BLAS, input index, material). Mirrors
+// RayBuilder::create_toplevel (RayBuilder.cpp:386-760), which builds the driver TLAS over entries
+// carrying a vk_transform_matrix (:518).
+extern "C" vkg_status vkg_tlas_build(vkg_ctx *ctx, const vkg_bvh *const *blas, uint32_t num_blas,
+                                     const vkg_instance *d_instances, uint32_t num_instances,
+                                     const vkg_bvh_build_options *opts, vkg_tlas **out, void *stream_)
+{
+    if(!ctx) return VKG_ERR_INVALID_ARGUMENT;
+    if(!out) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_tlas_build: out is NULL");
+    *out = nullptr;
+    if(num_instances > 0 && (!d_instances || !blas || num_blas == 0))
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_tlas_build: NULL instances or BLAS array");
+    for(uint32_t b = 0; b < num_blas; ++b)
+        if(!blas[b]) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_tlas_build: BLAS %u is NULL", b);
+    if(num_instances >= MAX_TRIS)
+        return set_error(ctx, VKG_ERR_CAPACITY, "vkg_tlas_build: %u instances exceed the maximum", num_instances);
+    const uint32_t leaf_max = (opts && opts->leaf_max) ? opts->leaf_max : 4u;
+    if(leaf_max > LEAF_MAX_LIMIT)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_tlas_build: leaf_max %u > %u", leaf_max, LEAF_MAX_LIMIT);
+    if(vkg_status s = bind_device(ctx); s != VKG_OK) return s;
+    cudaStream_t st = static_cast<cudaStream_t>(stream_);
+    auto *t = new vkg_tlas();
+    t->num_instances = num_instances;
+    t->num_blas = num_blas;
+    t->top.leaf_max = leaf_max;
+    std::vector<blas_ref> refs(num_blas);
+    std::vector<blas_box> boxes(num_blas);
+    for(uint32_t b = 0; b < num_blas; ++b)
+    {
+        refs[b] = blas_ref{blas[b]->d_nodes, blas[b]->d_tris, blas[b]->num_tris, 0u};
+        for(int a = 0; a < 3; ++a)
+        {
+            boxes[b].lo[a] = blas[b]->scene_min[a];
+            boxes[b].hi[a] = blas[b]->scene_max[a];
+        }
+        boxes[b].num_tris = blas[b]->num_tris;
+    }
+    blas_box *d_bb = nullptr;
+    cudaError_t e = cudaSuccess;
+    if(num_blas)
+    {
+        e = cudaMalloc(&t->d_blas, num_blas * sizeof(blas_ref));
+        if(e == cudaSuccess) e = cudaMalloc(&d_bb, num_blas * sizeof(blas_box));
+        if(e == cudaSuccess)
+            e = cudaMemcpyAsync(t->d_blas, refs.data(), num_blas * sizeof(blas_ref), cudaMemcpyHostToDevice, st);
+        if(e == cudaSuccess) e = cudaMemcpyAsync(d_bb, boxes.data(), num_blas * sizeof(blas_box), cudaMemcpyHostToDevice, st);
+    }
+    if(e == cudaSuccess && num_instances)
+    {
+        e = cudaMalloc(&t->d_inst, num_instances * sizeof(inst_rec));
+        if(e == cudaSuccess) e = cudaMalloc(&t->d_inst_by_id, num_instances * sizeof(inst_rec));
+    }
+    if(e != cudaSuccess)
+    {
+        cudaFree(d_bb);
+        vkg_tlas_destroy(ctx, t);
+        return cuda_check(ctx, e, "vkg_tlas_build");
+    }
+    if(num_instances == 0)
+    {
+        cudaStreamSynchronize(st);
+        cudaFree(d_bb);
+        *out = t;
+        return VKG_OK;
+    }
+    const uint32_t n = num_instances;
+    const int T = 256;
+    const uint32_t g = (n + T - 1) / T;
+    uint32_t err_bits = 0;
+    vkg_status s = build_core(
+            ctx, &t->top, n, leaf_max, st,
+            [&](box6 *tbox, uint32_t *scene_enc, uint32_t *err) {
+                k_instance_boxes<<<g, T, 0, st>>>(d_instances, n, d_bb, num_blas, tbox, scene_enc, err);
+            },
+            [&](const uint32_t *sorted) {
+                k_instance_records<<<g, T, 0, st>>>(d_instances, sorted, n, num_blas, t->d_inst, t->d_inst_by_id);
+            },
+            err_bits);
+    cudaFree(d_bb);
+    t->top.num_tris = n;
+    if(s == VKG_OK && (err_bits & BUILD_ERR_INDEX))
+        s = set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_tlas_build: an instance's BLAS index >= %u", num_blas);
+    if(s == VKG_OK && (err_bits & BUILD_ERR_SINGULAR))
+        s = set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_tlas_build: an instance transform is singular");
+    if(s == VKG_OK && t->top.depth > TLAS_MAX_DEPTH)
+        s = set_error(ctx, VKG_ERR_CAPACITY, "vkg_tlas_build: top-level depth %u exceeds %u", t->top.depth, TLAS_MAX_DEPTH);
+    if(s != VKG_OK)
+    {
+        vkg_tlas_destroy(ctx, t);
+        return s;
+    }
+    t->top.bytes = sizeof(node8) * t->top.num_nodes + 2 * sizeof(inst_rec) * (size_t)n;
+    *out = t;
+    return VKG_OK;
+}
+
+extern "C" vkg_status vkg_tlas_info_get(const vkg_tlas *t, vkg_tlas_info *out)
+{
+    if(!t || !out) return VKG_ERR_INVALID_ARGUMENT;
+    std::memset(out, 0, sizeof(*out));
+    out->num_instances = t->num_instances;
+    out->num_blas = t->num_blas;
+    out->num_nodes = t->top.num_nodes;
+    out->depth = t->top.depth;
+    for(int a = 0; a < 3; ++a)
+    {
+        out->scene_min[a] = t->top.scene_min[a];
+        out->scene_max[a] = t->top.scene_max[a];
+    }
+    out->d_nodes = t->top.d_nodes;
+    out->d_instances = t->d_inst;
+    out->d_instances_by_id = t->d_inst_by_id;
+    out->build_ms = t->top.build_ms;
+    return VKG_OK;
+}
+
+extern "C" vkg_status vkg_tlas_destroy(vkg_ctx *ctx, vkg_tlas *t)
+{
+    if(!t) return VKG_OK;
+    if(ctx) bind_device(ctx);
+    cudaFree(t->top.d_nodes);
+    cudaFree(t->top.d_morton);
+    cudaFree(t->top.d_sorted);
+    cudaFree(t->d_inst);
+    cudaFree(t->d_inst_by_id);
+    cudaFree(t->d_blas);
+    delete t;
     return VKG_OK;
 }
 

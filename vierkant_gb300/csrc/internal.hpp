@@ -39,6 +39,41 @@ struct vkg_bvh
 
 namespace vkg
 {
+// instance record of a two-level BVH (128 B): world->object and object->world 3x4 row-major
+// transforms, the BLAS the instance refers to, its input index and material
+struct alignas(16) inst_rec
+{
+    float w2o[12];
+    float o2w[12];
+    uint32_t blas, instance, material, pad0;
+    uint32_t pad1[4];
+};
+static_assert(sizeof(inst_rec) == 128, "inst_rec layout");
+
+// top-level traversal stack; the build rejects top levels deeper than it supports
+constexpr uint32_t TLAS_STACK = 64;
+constexpr uint32_t TLAS_MAX_DEPTH = (TLAS_STACK - 1) / 7 + 1;
+
+// a bottom-level BVH as the top level sees it
+struct alignas(16) blas_ref
+{
+    const node8 *nodes;
+    const tri_rec *tris;
+    uint32_t num_tris, pad;
+};
+}// namespace vkg
+
+struct vkg_tlas
+{
+    vkg_bvh top;                       // 8-wide BVH over the instances' world boxes (no triangle records)
+    vkg::inst_rec *d_inst = nullptr;   // instance records in sorted (leaf) order
+    vkg::inst_rec *d_inst_by_id = nullptr; // the same records in input order
+    vkg::blas_ref *d_blas = nullptr;
+    uint32_t num_instances = 0, num_blas = 0;
+};
+
+namespace vkg
+{
 // record an error message on ctx and return `status`
 vkg_status set_error(vkg_ctx *ctx, vkg_status status, const char *fmt, ...);
 // map a CUDA error to VKG_ERR_CUDA with location info; VKG_OK if err == cudaSuccess

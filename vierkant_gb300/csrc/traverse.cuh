@@ -111,6 +111,53 @@ __device__ __forceinline__ void ray_init(ray_state &s, float ox, float oy, float
     s.st_t[0] = tmin;
 }
 
+// entry-distance keys of the children of node ni for a ray (origin o, reciprocal direction i,
+// interval [tmin, tmax]): key = ordered entry distance with its low 3 bits replaced by the slot,
+// 0xFFFFFFFF for a child the ray misses. Truncation only lowers the stored distance, so pruning with
+// it stays conservative. w4 / w5 receive the node's child words.
+__device__ __forceinline__ void node_keys(const node8 *__restrict__ nodes, uint32_t ni, float ox, float oy, float oz,
+                                          float ix, float iy, float iz, float tmin, float tmax, uint32_t (&key)[8],
+                                          uint4 &w4, uint4 &w5)
+{
+    const uint4 *np = reinterpret_cast<const uint4 *>(nodes + ni);
+    const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2);
+    const uint4 w3 = __ldg(np + 3);
+    w4 = __ldg(np + 4);
+    w5 = __ldg(np + 5);
+    const uint32_t meta = w0.w;
+    const uint32_t nch = meta >> 24;
+    const bool negx = ix < 0.f, negy = iy < 0.f, negz = iz < 0.f;
+    const float tox = __fmul_rn(__fsub_rn(__uint_as_float(w0.x), ox), ix);
+    const float toy = __fmul_rn(__fsub_rn(__uint_as_float(w0.y), oy), iy);
+    const float toz = __fmul_rn(__fsub_rn(__uint_as_float(w0.z), oz), iz);
+    const float sx = __fmul_rn(exp_scale(meta & 0xFFu), ix);
+    const float sy = __fmul_rn(exp_scale((meta >> 8) & 0xFFu), iy);
+    const float sz = __fmul_rn(exp_scale((meta >> 16) & 0xFFu), iz);
+    const uint32_t nx0 = negx ? w2.z : w1.x, nx1 = negx ? w2.w : w1.y;
+    const uint32_t fx0 = negx ? w1.x : w2.z, fx1 = negx ? w1.y : w2.w;
+    const uint32_t ny0 = negy ? w3.x : w1.z, ny1 = negy ? w3.y : w1.w;
+    const uint32_t fy0 = negy ? w1.z : w3.x, fy1 = negy ? w1.w : w3.y;
+    const uint32_t nz0 = negz ? w3.z : w2.x, nz1 = negz ? w3.w : w2.y;
+    const uint32_t fz0 = negz ? w2.x : w3.z, fz1 = negz ? w2.y : w3.w;
+#pragma unroll
+    for(int k = 0; k < 8; ++k)
+    {
+        key[k] = 0xFFFFFFFFu;
+        if((uint32_t)k < nch)
+        {
+            const uint32_t wnx = k < 4 ? nx0 : nx1, wfx = k < 4 ? fx0 : fx1;
+            const uint32_t wny = k < 4 ? ny0 : ny1, wfy = k < 4 ? fy0 : fy1;
+            const uint32_t wnz = k < 4 ? nz0 : nz1, wfz = k < 4 ? fz0 : fz1;
+            const float tnx = fmaf(qbyte(wnx, k), sx, tox), tfx = fmaf(qbyte(wfx, k), sx, tox);
+            const float tny = fmaf(qbyte(wny, k), sy, toy), tfy = fmaf(qbyte(wfy, k), sy, toy);
+            const float tnz = fmaf(qbyte(wnz, k), sz, toz), tfz = fmaf(qbyte(wfz, k), sz, toz);
+            const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+            const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+            if(tn <= tf) key[k] = (tenc(tn) & ~7u) | (uint32_t)k;
+        }
+    }
+}
+
 // one node of the traversal; returns false once the ray is finished
 template<bool ANY, bool STATS>
 __device__ __forceinline__ bool ray_step(ray_state &s, const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
@@ -123,44 +170,9 @@ __device__ __forceinline__ bool ray_step(ray_state &s, const node8 *__restrict__
         const uint32_t ni = s.st_node[s.sp];
         if(s.st_t[s.sp] > s.best_t) continue;
         if(STATS) ++visits;
-        const uint4 *np = reinterpret_cast<const uint4 *>(nodes + ni);
-        const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2);
-        const uint4 w3 = __ldg(np + 3), w4 = __ldg(np + 4), w5 = __ldg(np + 5);
-        const uint32_t meta = w0.w;
-        const uint32_t nch = meta >> 24;
-        const bool negx = s.ix < 0.f, negy = s.iy < 0.f, negz = s.iz < 0.f;
-        const float tox = __fmul_rn(__fsub_rn(__uint_as_float(w0.x), s.ox), s.ix);
-        const float toy = __fmul_rn(__fsub_rn(__uint_as_float(w0.y), s.oy), s.iy);
-        const float toz = __fmul_rn(__fsub_rn(__uint_as_float(w0.z), s.oz), s.iz);
-        const float sx = __fmul_rn(exp_scale(meta & 0xFFu), s.ix);
-        const float sy = __fmul_rn(exp_scale((meta >> 8) & 0xFFu), s.iy);
-        const float sz = __fmul_rn(exp_scale((meta >> 16) & 0xFFu), s.iz);
-        const uint32_t nx0 = negx ? w2.z : w1.x, nx1 = negx ? w2.w : w1.y;
-        const uint32_t fx0 = negx ? w1.x : w2.z, fx1 = negx ? w1.y : w2.w;
-        const uint32_t ny0 = negy ? w3.x : w1.z, ny1 = negy ? w3.y : w1.w;
-        const uint32_t fy0 = negy ? w1.z : w3.x, fy1 = negy ? w1.w : w3.y;
-        const uint32_t nz0 = negz ? w3.z : w2.x, nz1 = negz ? w3.w : w2.y;
-        const uint32_t fz0 = negz ? w2.x : w3.z, fz1 = negz ? w2.y : w3.w;
-        // 32-bit keys: ordered entry distance with its low 3 bits replaced by the slot. Truncation only
-        // lowers the stored distance, so pruning with it stays conservative.
         uint32_t key[8];
-#pragma unroll
-        for(int k = 0; k < 8; ++k)
-        {
-            key[k] = 0xFFFFFFFFu;
-            if((uint32_t)k < nch)
-            {
-                const uint32_t wnx = k < 4 ? nx0 : nx1, wfx = k < 4 ? fx0 : fx1;
-                const uint32_t wny = k < 4 ? ny0 : ny1, wfy = k < 4 ? fy0 : fy1;
-                const uint32_t wnz = k < 4 ? nz0 : nz1, wfz = k < 4 ? fz0 : fz1;
-                const float tnx = fmaf(qbyte(wnx, k), sx, tox), tfx = fmaf(qbyte(wfx, k), sx, tox);
-                const float tny = fmaf(qbyte(wny, k), sy, toy), tfy = fmaf(qbyte(wfy, k), sy, toy);
-                const float tnz = fmaf(qbyte(wnz, k), sz, toz), tfz = fmaf(qbyte(wfz, k), sz, toz);
-                const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, s.tmin));
-                const float tf = fminf(fminf(tfx, tfy), fminf(tfz, s.best_t));
-                if(tn <= tf) key[k] = (tenc(tn) & ~7u) | (uint32_t)k;
-            }
-        }
+        uint4 w4, w5;
+        node_keys(nodes, ni, s.ox, s.oy, s.oz, s.ix, s.iy, s.iz, s.tmin, s.best_t, key, w4, w5);
         sort8(key);
 #pragma unroll
         for(int h = 0; h < 8; ++h)

@@ -10,12 +10,13 @@ from __future__ import annotations
 import ctypes as C
 import weakref
 
+import numpy as np
 import torch
 
-from ._lib import (RAY_COUNT_STATS, RAY_CULL_BACK_FACES, check, lib, vkg_bvh_build_options, vkg_bvh_info,
+from ._lib import (RAY_COUNT_STATS, RAY_CULL_BACK_FACES, check, lib, vkg_bvh_build_options, vkg_bvh_info, vkg_tlas_info,
                    vkg_camera)
 
-__all__ = ["Context", "BVH", "hits_view", "RAY_CULL_BACK_FACES", "RAY_COUNT_STATS"]
+__all__ = ["Context", "BVH", "TLAS", "INSTANCE_DTYPE", "hits_view", "RAY_CULL_BACK_FACES", "RAY_COUNT_STATS"]
 
 
 def _stream_ptr(device) -> int:
@@ -137,6 +138,90 @@ class BVH:
                                                    C.c_void_p(hits_host.data_ptr()), flags,
                                                    C.c_void_p(self.ctx.stream())), "vkg_closest_hit_host")
         return hits_host
+
+
+INSTANCE_DTYPE = np.dtype([("transform", "<f4", 12), ("blas", "<u4"), ("material", "<u4"), ("pad", "<u4", 2)])
+
+
+class TLAS:
+    """Two-level BVH: instances (INSTANCE_DTYPE: object -> world 3x4 transform, BLAS index, material)
+    over bottom-level BVHs, which must outlive it."""
+
+    def __init__(self, ctx: Context, blas: list, instances, leaf_max: int = 4):
+        self.ctx = ctx
+        self.blas = list(blas)
+        dev = f"cuda:{ctx.device}"
+        inst = np.ascontiguousarray(instances, INSTANCE_DTYPE)
+        self.num_instances = len(inst)
+        self._inst = torch.from_numpy(inst.view(np.uint8).copy()).to(dev)
+        arr = (C.c_void_p * max(1, len(self.blas)))(*[b.handle.value for b in self.blas])
+        opts = vkg_bvh_build_options(leaf_max)
+        h = C.c_void_p()
+        ctx._check(lib().vkg_tlas_build(ctx.handle, arr, len(self.blas), C.c_void_p(self._inst.data_ptr()),
+                                        len(inst), C.byref(opts), C.byref(h), C.c_void_p(ctx.stream())),
+                   "vkg_tlas_build")
+        self.handle = h
+        ctx.adopt(self)
+
+    def info(self) -> vkg_tlas_info:
+        inf = vkg_tlas_info()
+        check(lib().vkg_tlas_info_get(self.handle, C.byref(inf)))
+        return inf
+
+    def instance_records(self, by_id: bool = True) -> np.ndarray:
+        """the device's 128-byte instance records as float32 [N, 32] (w2o = [:, 0:12], o2w = [:, 12:24])"""
+        inf = self.info()
+        n = inf.num_instances
+        if n == 0:
+            return np.zeros((0, 32), np.float32)
+        t = torch.empty(n * 32, dtype=torch.float32, device=f"cuda:{self.ctx.device}")
+        src = inf.d_instances_by_id if by_id else inf.d_instances
+        torch.cuda.synchronize()
+        rt = _cudart()
+        rt.cudaMemcpy(C.c_void_p(t.data_ptr()), C.c_void_p(src), C.c_size_t(n * 128), 3)
+        return t.cpu().numpy().reshape(n, 32)
+
+    def close(self):
+        if getattr(self, "handle", None) and getattr(self.ctx, "handle", None):
+            lib().vkg_tlas_destroy(self.ctx.handle, self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def closest_hit(self, rays: torch.Tensor, out: torch.Tensor | None = None, flags: int = 0) -> torch.Tensor:
+        """int32 [N, 8] = {prim, instance, t, u, v, pad x 3} (t, u, v as float bits)"""
+        n = rays.shape[0]
+        if out is None:
+            out = torch.empty((n, 8), dtype=torch.int32, device=rays.device)
+        self.ctx._check(lib().vkg_tlas_closest_hit(self.ctx.handle, self.handle, C.c_void_p(rays.data_ptr()), n,
+                                                   C.c_void_p(out.data_ptr()), flags, C.c_void_p(self.ctx.stream())),
+                        "vkg_tlas_closest_hit")
+        return out
+
+    def any_hit(self, rays: torch.Tensor, out: torch.Tensor | None = None, flags: int = 0) -> torch.Tensor:
+        n = rays.shape[0]
+        if out is None:
+            out = torch.empty(n, dtype=torch.int32, device=rays.device)
+        self.ctx._check(lib().vkg_tlas_any_hit(self.ctx.handle, self.handle, C.c_void_p(rays.data_ptr()), n,
+                                               C.c_void_p(out.data_ptr()), flags, C.c_void_p(self.ctx.stream())),
+                        "vkg_tlas_any_hit")
+        return out
+
+
+def _cudart():
+    import glob
+    for cand in ["libcudart.so.13", "libcudart.so"] + sorted(glob.glob("/usr/local/cuda/lib64/libcudart.so*")):
+        try:
+            rt = C.CDLL(cand)
+            rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+            return rt
+        except OSError:
+            continue
+    raise RuntimeError("libcudart not found")
 
 
 def hits_view(hits):
