@@ -276,6 +276,19 @@ vkg_status vkg_tlas_closest_hit(vkg_ctx *ctx, const vkg_tlas *tlas, const vkg_ra
                                 vkg_inst_hit *d_hits, uint32_t flags, void *stream);
 vkg_status vkg_tlas_any_hit(vkg_ctx *ctx, const vkg_tlas *tlas, const vkg_ray *d_rays, uint32_t n, uint32_t *d_occluded,
                             uint32_t flags, void *stream);
+/* stress workload generators (two-level scenes) */
+/* cube-sphere of n x n quads per face: 6 (n+1)^2 vertices, 12 n^2 outward triangles */
+vkg_status vkg_geometry_cubesphere(uint32_t n, float radius, float *xyz, uint32_t *indices);
+/* terrain: n x n vertex grid over [-extent/2, extent/2]^2 (x, z), y = height * fBm, with `octaves`
+ * octaves (lacunarity 2, gain 0.5) of 3-D simplex noise (the basis of shaders/slang/utils/simplex.slang)
+ * at (x f, z f, seed offset); 2 (n-1)^2 triangles counter-clockwise seen from +y */
+vkg_status vkg_geometry_terrain(uint32_t n, float extent, float height, float frequency, uint32_t octaves,
+                                uint32_t seed, float *xyz, uint32_t *indices);
+/* n random instances from PCG32(seed, stream): translation U[lo, hi], uniform rotation, scale
+ * U[smin, smax], mesh U{0..num_meshes-1}, material mat_base + U{0..num_mats-1} */
+vkg_status vkg_instances_random(uint64_t seed, uint64_t stream, uint32_t n, uint32_t num_meshes, uint32_t mat_base,
+                                uint32_t num_mats, const float lo[3], const float hi[3], float smin, float smax,
+                                vkg_instance *out);
 
 /* ---- environment map ------------------------------------------------------------------------ *
  * Equirectangular fp32 RGB, u = 0.5 + 0.5 * atan2(x, -z) / pi, v = acos(y) / pi
@@ -306,6 +319,34 @@ typedef struct vkg_scene_desc
     uint32_t leaf_max; /* BVH leaf size (0 -> 4) */
 } vkg_scene_desc;
 vkg_status vkg_scene_create(vkg_ctx *ctx, const vkg_scene_desc *desc, vkg_scene **out, void *stream);
+/* instanced scenes (RayBuilder's BLAS-per-mesh + TLAS-over-entries layout, RayBuilder.cpp:98-300,
+ * :386-760): meshes are copied and get one BVH each, the instances (device array; material indexes
+ * d_materials) a two-level BVH. Mesh triangles are one-sided unless the mesh is flagged two-sided. */
+typedef struct vkg_mesh_desc
+{
+    const float *d_xyz;
+    uint32_t num_vertices;
+    const uint32_t *d_indices;
+    uint32_t num_tris;
+    uint32_t twosided;
+    uint32_t pad;
+} vkg_mesh_desc;
+typedef struct vkg_instanced_scene_desc
+{
+    const vkg_mesh_desc *meshes; /* host array */
+    uint32_t num_meshes;
+    const vkg_instance *d_instances;
+    uint32_t num_instances;
+    const vkg_material *d_materials;
+    uint32_t num_materials;
+    const float *d_env_rgb;
+    uint32_t env_width, env_height;
+    uint32_t leaf_max; /* BVH leaf size of the meshes (0 -> 4) */
+} vkg_instanced_scene_desc;
+vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_desc *desc, vkg_scene **out,
+                                      void *stream);
+/* the two-level BVH of an instanced scene (NULL for a single-level scene) */
+vkg_status vkg_scene_tlas(const vkg_scene *scene, const vkg_tlas **out);
 vkg_status vkg_scene_destroy(vkg_ctx *ctx, vkg_scene *scene);
 /* the scene's BVH (owned by the scene) for direct ray queries */
 vkg_status vkg_scene_bvh(const vkg_scene *scene, const vkg_bvh **out);

@@ -71,6 +71,18 @@ class vkg_tlas_info(C.Structure):
                 ("build_ms", C.c_float)]
 
 
+class vkg_mesh_desc(C.Structure):
+    _fields_ = [("d_xyz", C.c_void_p), ("num_vertices", C.c_uint32), ("d_indices", C.c_void_p),
+                ("num_tris", C.c_uint32), ("twosided", C.c_uint32), ("pad", C.c_uint32)]
+
+
+class vkg_instanced_scene_desc(C.Structure):
+    _fields_ = [("meshes", C.POINTER(vkg_mesh_desc)), ("num_meshes", C.c_uint32), ("d_instances", C.c_void_p),
+                ("num_instances", C.c_uint32), ("d_materials", C.c_void_p), ("num_materials", C.c_uint32),
+                ("d_env_rgb", C.c_void_p), ("env_width", C.c_uint32), ("env_height", C.c_uint32),
+                ("leaf_max", C.c_uint32)]
+
+
 class vkg_batch_job(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("camera", vkg_camera), ("settings", vkg_settings), ("seed", C.c_uint32),
                 ("pad", C.c_uint32), ("d_rgb_out", C.c_void_p)]
@@ -177,6 +189,11 @@ SIGNATURES = {
     "vkg_tracer_statistics": (I32, [P, C.POINTER(vkg_tracer_stats)]),
     "vkg_tracer_destroy": (I32, [P]),
     "vkg_tracer_attach_cache": (I32, [P, P]),
+    "vkg_scene_create_instanced": (I32, [P, C.POINTER(vkg_instanced_scene_desc), C.POINTER(P), P]),
+    "vkg_scene_tlas": (I32, [P, C.POINTER(P)]),
+    "vkg_geometry_cubesphere": (I32, [U32, C.c_float, P, P]),
+    "vkg_geometry_terrain": (I32, [U32, C.c_float, C.c_float, C.c_float, U32, U32, P, P]),
+    "vkg_instances_random": (I32, [C.c_uint64, C.c_uint64, U32, U32, U32, U32, P, P, C.c_float, C.c_float, P]),
     "vkg_tlas_build": (I32, [P, P, U32, P, U32, P, C.POINTER(P), P]),
     "vkg_tlas_info_get": (I32, [P, C.POINTER(vkg_tlas_info)]),
     "vkg_tlas_destroy": (I32, [P, P]),

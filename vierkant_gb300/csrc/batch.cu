@@ -162,6 +162,7 @@ struct vkg_batch
     vkg_ray *q_ray[2] = {nullptr, nullptr};
     uint32_t *q_pid[2] = {nullptr, nullptr};
     vkg_hit *hits = nullptr;
+    uint32_t *hit_inst = nullptr;
     vkg_ray *s_ray = nullptr;
     uint32_t *s_pid = nullptr;
     float4 *s_contrib = nullptr;
@@ -181,12 +182,14 @@ namespace
 void free_waves(vkg_batch *b)
 {
     for(void *p: {(void *)b->q_ray[0], (void *)b->q_ray[1], (void *)b->q_pid[0], (void *)b->q_pid[1], (void *)b->hits,
+                  (void *)b->hit_inst,
                   (void *)b->s_ray, (void *)b->s_pid, (void *)b->s_contrib, (void *)b->rng, (void *)b->pinc,
                   (void *)b->pjob, (void *)b->beta_pdf, (void *)b->radiance, (void *)b->d_chunks})
         cudaFree(p);
     b->q_ray[0] = b->q_ray[1] = nullptr;
     b->q_pid[0] = b->q_pid[1] = nullptr;
     b->hits = nullptr;
+    b->hit_inst = nullptr;
     b->s_ray = nullptr;
     b->s_pid = nullptr;
     b->s_contrib = nullptr;
@@ -261,6 +264,7 @@ vkg_status ensure_waves(vkg_batch *b, const std::vector<vkg_batch::wave> &waves,
             al((void **)&b->q_pid[q], need * sizeof(uint32_t));
         }
         al((void **)&b->hits, need * sizeof(vkg_hit));
+        al((void **)&b->hit_inst, need * sizeof(uint32_t));
         al((void **)&b->s_ray, need * sizeof(vkg_ray));
         al((void **)&b->s_pid, need * sizeof(uint32_t));
         al((void **)&b->s_contrib, need * sizeof(float4));
@@ -308,20 +312,21 @@ vkg_status enqueue(vkg_batch *b, const std::vector<vkg_batch::wave> &waves, cuda
             {
                 VKG_TRY_CUDA(ctx, cudaMemsetAsync(b->counters + 3, 0, sizeof(uint32_t), st));
                 k_pt_trace_persistent<false><<<grid, PT_THREADS, 0, st>>>(J, b->q_ray[a], b->q_pid[a], cnt_in, b->hits,
-                                                                         nullptr, nullptr, b->counters + 3);
+                                                                         b->hit_inst, nullptr, nullptr, b->counters + 3);
             }
             else
-                k_pt_extend<<<grid, PT_THREADS, 0, st>>>(J, b->q_ray[a], b->q_pid[a], cnt_in, b->hits);
+                k_pt_extend<<<grid, PT_THREADS, 0, st>>>(J, b->q_ray[a], b->q_pid[a], cnt_in, b->hits, b->hit_inst);
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_out, 0, sizeof(uint32_t), st));
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_s, 0, sizeof(uint32_t), st));
-            k_pt_shade<MODE_PLAIN><<<grid, PT_THREADS, 0, st>>>(J, depth, b->q_ray[a], b->q_pid[a], b->hits, cnt_in,
+            k_pt_shade<MODE_PLAIN><<<grid, PT_THREADS, 0, st>>>(J, depth, b->q_ray[a], b->q_pid[a], b->hits, b->hit_inst,
+                                                                cnt_in,
                                                                 b->q_ray[1 - a], b->q_pid[1 - a], cnt_out, b->s_ray,
                                                                 b->s_pid, b->s_contrib, cnt_s, b->rng, b->beta_pdf,
                                                                 b->radiance, io);
             if(T.extend_kernel == 2)
             {
                 VKG_TRY_CUDA(ctx, cudaMemsetAsync(b->counters + 3, 0, sizeof(uint32_t), st));
-                k_pt_trace_persistent<true><<<grid, PT_THREADS, 0, st>>>(J, b->s_ray, b->s_pid, cnt_s, nullptr,
+                k_pt_trace_persistent<true><<<grid, PT_THREADS, 0, st>>>(J, b->s_ray, b->s_pid, cnt_s, nullptr, nullptr,
                                                                         b->s_contrib, b->radiance, b->counters + 3);
             }
             else

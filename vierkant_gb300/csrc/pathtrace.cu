@@ -46,6 +46,7 @@ struct vkg_tracer
     vkg_ray *q_ray[2] = {nullptr, nullptr};
     uint32_t *q_pid[2] = {nullptr, nullptr};
     vkg_hit *hits = nullptr;
+    uint32_t *hit_inst = nullptr; // instance of each hit (instanced scenes)
     vkg_ray *s_ray = nullptr;
     uint32_t *s_pid = nullptr;
     float4 *s_contrib = nullptr;
@@ -78,15 +79,30 @@ namespace vkg
 namespace
 {
 
+__global__ void k_set_tri_flags(tri_rec *__restrict__ tris, uint32_t n, uint32_t flags)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i < n) tris[i].pad[0] |= flags;
+}
+
+__global__ void k_check_instance_materials(const vkg_instance *__restrict__ inst, uint32_t n, uint32_t num_mats,
+                                           uint32_t *__restrict__ bad)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i < n && inst[i].material >= num_mats) atomicOr(bad, 1u);
+}
+
 void tracer_free_buffers(vkg_tracer *t)
 {
     for(void *p: {(void *)t->q_ray[0], (void *)t->q_ray[1], (void *)t->q_pid[0], (void *)t->q_pid[1], (void *)t->hits,
+                  (void *)t->hit_inst,
                   (void *)t->s_ray, (void *)t->s_pid, (void *)t->s_contrib, (void *)t->rng, (void *)t->beta_pdf,
                   (void *)t->radiance, (void *)t->sum, (void *)t->accum})
         cudaFree(p);
     t->q_ray[0] = t->q_ray[1] = nullptr;
     t->q_pid[0] = t->q_pid[1] = nullptr;
     t->hits = nullptr;
+    t->hit_inst = nullptr;
     t->s_ray = nullptr;
     t->s_pid = nullptr;
     t->s_contrib = nullptr;
@@ -157,6 +173,7 @@ vkg_status tracer_ensure(vkg_tracer *t, size_t paths, size_t npix)
         al((void **)&t->q_pid[q], paths * sizeof(uint32_t));
     }
     al((void **)&t->hits, paths * sizeof(vkg_hit));
+    al((void **)&t->hit_inst, paths * sizeof(uint32_t));
     al((void **)&t->s_ray, paths * sizeof(vkg_ray));
     al((void **)&t->s_pid, paths * sizeof(uint32_t));
     al((void **)&t->s_contrib, paths * sizeof(float4));
@@ -274,12 +291,113 @@ vkg_status vkg_scene_destroy(vkg_ctx *ctx, vkg_scene *sc)
     if(!sc) return VKG_OK;
     if(ctx) bind_device(ctx);
     vkg_bvh_destroy(ctx, sc->bvh);
+    vkg_tlas_destroy(ctx, sc->tlas);
+    for(vkg_bvh *b: sc->blas) vkg_bvh_destroy(ctx, b);
+    for(float *p: sc->mesh_xyz) cudaFree(p);
+    for(uint32_t *p: sc->mesh_idx) cudaFree(p);
+    cudaFree(sc->d_meshes);
     cudaFree(sc->xyz);
     cudaFree(sc->idx);
     cudaFree(sc->tri_mat);
     cudaFree(sc->mats);
     env_free(sc->env);
     delete sc;
+    return VKG_OK;
+}
+
+vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_desc *d, vkg_scene **out, void *stream)
+{
+    if(!ctx) return VKG_ERR_INVALID_ARGUMENT;
+    if(!d || !out) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_create_instanced: NULL argument");
+    *out = nullptr;
+    if(!d->d_materials || d->num_materials == 0)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_create_instanced: materials are required");
+    if(!d->d_env_rgb || d->env_width == 0 || d->env_height == 0)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_create_instanced: an environment map is required");
+    if((d->num_meshes && !d->meshes) || (d->num_instances && (!d->d_instances || d->num_meshes == 0)))
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_create_instanced: NULL meshes or instances");
+    if(vkg_status s = bind_device(ctx); s != VKG_OK) return s;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    auto *sc = new vkg_scene();
+    sc->num_materials = d->num_materials;
+    sc->num_instances = d->num_instances;
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) {
+        if(e == cudaSuccess) e = x;
+    };
+    auto fail = [&](vkg_status s) {
+        vkg_scene_destroy(ctx, sc);
+        return s;
+    };
+    chk(cudaMalloc(&sc->mats, d->num_materials * sizeof(vkg_material)));
+    chk(cudaMemcpyAsync(sc->mats, d->d_materials, d->num_materials * sizeof(vkg_material), cudaMemcpyDeviceToDevice, st));
+    std::vector<mesh_ref> refs(d->num_meshes);
+    uint64_t tris = 0;
+    for(uint32_t m = 0; m < d->num_meshes && e == cudaSuccess; ++m)
+    {
+        const vkg_mesh_desc &M = d->meshes[m];
+        if(M.num_tris && (!M.d_xyz || !M.d_indices || M.num_vertices == 0))
+            return fail(set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_create_instanced: mesh %u has no geometry", m));
+        float *xyz = nullptr;
+        uint32_t *idx = nullptr;
+        chk(cudaMalloc(&xyz, std::max<size_t>(M.num_vertices, 1) * 3 * sizeof(float)));
+        chk(cudaMalloc(&idx, std::max<size_t>(M.num_tris, 1) * 3 * sizeof(uint32_t)));
+        sc->mesh_xyz.push_back(xyz);
+        sc->mesh_idx.push_back(idx);
+        if(M.num_tris)
+        {
+            chk(cudaMemcpyAsync(xyz, M.d_xyz, (size_t)M.num_vertices * 3 * sizeof(float), cudaMemcpyDeviceToDevice, st));
+            chk(cudaMemcpyAsync(idx, M.d_indices, (size_t)M.num_tris * 3 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+        }
+        if(e != cudaSuccess) break;
+        vkg_bvh_build_options opt{d->leaf_max};
+        vkg_bvh *b = nullptr;
+        if(vkg_status s = vkg_bvh_build(ctx, xyz, M.num_vertices, idx, M.num_tris, &opt, &b, stream); s != VKG_OK)
+            return fail(s);
+        sc->blas.push_back(b);
+        if(M.twosided && M.num_tris)
+            k_set_tri_flags<<<(M.num_tris + 255) / 256, 256, 0, st>>>(b->d_tris, M.num_tris, TRI_FLAG_TWOSIDED);
+        refs[m] = mesh_ref{xyz, idx};
+        tris += M.num_tris;
+    }
+    if(e == cudaSuccess && d->num_meshes)
+    {
+        chk(cudaMalloc(&sc->d_meshes, d->num_meshes * sizeof(mesh_ref)));
+        chk(cudaMemcpyAsync(sc->d_meshes, refs.data(), d->num_meshes * sizeof(mesh_ref), cudaMemcpyHostToDevice, st));
+    }
+    if(e != cudaSuccess) return fail(cuda_check(ctx, e, "vkg_scene_create_instanced"));
+    if(d->num_instances)
+    {
+        uint32_t *bad = nullptr, hbad = 0;
+        chk(cudaMallocAsync(&bad, sizeof(uint32_t), st));
+        chk(cudaMemsetAsync(bad, 0, sizeof(uint32_t), st));
+        k_check_instance_materials<<<(d->num_instances + 255) / 256, 256, 0, st>>>(d->d_instances, d->num_instances,
+                                                                                   d->num_materials, bad);
+        chk(cudaMemcpyAsync(&hbad, bad, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        chk(cudaFreeAsync(bad, st));
+        chk(cudaStreamSynchronize(st));
+        if(e != cudaSuccess) return fail(cuda_check(ctx, e, "vkg_scene_create_instanced"));
+        if(hbad) return fail(set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_create_instanced: an instance material >= num_materials"));
+    }
+    std::vector<const vkg_bvh *> bl(sc->blas.begin(), sc->blas.end());
+    vkg_bvh_build_options topt{4};
+    if(vkg_status s = vkg_tlas_build(ctx, bl.data(), (uint32_t)bl.size(), d->d_instances, d->num_instances, &topt,
+                                     &sc->tlas, stream);
+       s != VKG_OK)
+        return fail(s);
+    // an empty scene (no instances or no triangles) traces misses only
+    sc->num_tris = d->num_instances ? (uint32_t)std::min<uint64_t>(tris, 0xFFFFFFFFu) : 0u;
+    if(vkg_status s = env_build(ctx, d->d_env_rgb, d->env_width, d->env_height, sc->env, st); s != VKG_OK) return fail(s);
+    chk(cudaStreamSynchronize(st));
+    if(e != cudaSuccess) return fail(cuda_check(ctx, e, "vkg_scene_create_instanced"));
+    *out = sc;
+    return VKG_OK;
+}
+
+vkg_status vkg_scene_tlas(const vkg_scene *sc, const vkg_tlas **out)
+{
+    if(!sc || !out) return VKG_ERR_INVALID_ARGUMENT;
+    *out = sc->tlas;
     return VKG_OK;
 }
 
@@ -442,11 +560,12 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
             if(empty)
                 k_fill_miss_queue<<<grid, PT_THREADS, 0, st>>>(cnt_in, t->hits);
             else
-                k_pt_extend<<<grid, PT_THREADS, 0, st>>>(SS, t->q_ray[a], t->q_pid[a], cnt_in, t->hits);
+                k_pt_extend<<<grid, PT_THREADS, 0, st>>>(SS, t->q_ray[a], t->q_pid[a], cnt_in, t->hits, t->hit_inst);
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_out, 0, sizeof(uint32_t), st));
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_s, 0, sizeof(uint32_t), st));
 #define VKG_SHADE(M)                                                                                                   \
-    k_pt_shade<M><<<grid, PT_THREADS, 0, st>>>(SS, depth, t->q_ray[a], t->q_pid[a], t->hits, cnt_in, t->q_ray[1 - a],    \
+    k_pt_shade<M><<<grid, PT_THREADS, 0, st>>>(SS, depth, t->q_ray[a], t->q_pid[a], t->hits, t->hit_inst, cnt_in,        \
+                                               t->q_ray[1 - a],                                                          \
                                                t->q_pid[1 - a], cnt_out, t->s_ray, t->s_pid, t->s_contrib, cnt_s,         \
                                                t->rng, t->beta_pdf, t->radiance, io)
             if(mode == MODE_PLAIN) VKG_SHADE(MODE_PLAIN);

@@ -7,18 +7,38 @@
 
 #include "nrc.cuh"
 #include "pathtrace.cuh"
+#include "tlas.cuh"
 #include "traverse.cuh"
+
+#include <vector>
+
+namespace vkg
+{
+// vertex and index arrays of one mesh of an instanced scene (device)
+struct mesh_ref
+{
+    const float *xyz;
+    const uint32_t *idx;
+};
+}// namespace vkg
 
 // a scene: geometry, materials, its BVH and its environment tables
 struct vkg_scene
 {
-    vkg_bvh *bvh = nullptr;
+    vkg_bvh *bvh = nullptr;         // single-level scenes
     float *xyz = nullptr;
     uint32_t *idx = nullptr;
     uint32_t *tri_mat = nullptr;
     vkg_material *mats = nullptr;
     uint32_t num_tris = 0, num_vertices = 0, num_materials = 0;
     vkg::env_tables env;
+    // instanced scenes: meshes (owned copies + their BLASes) and the two-level BVH over the instances
+    vkg_tlas *tlas = nullptr;
+    std::vector<vkg_bvh *> blas;
+    std::vector<float *> mesh_xyz;
+    std::vector<uint32_t *> mesh_idx;
+    vkg::mesh_ref *d_meshes = nullptr;
+    uint32_t num_instances = 0;
 };
 
 namespace vkg
@@ -32,6 +52,13 @@ struct pt_params
 {
     const node8 *nodes;
     const tri_rec *tris;
+    // instanced scenes: two-level BVH (nodes, leaf-order and input-order instance records, BLASes)
+    // and the meshes' vertex / index arrays; two_level selects them
+    const node8 *tl_nodes;
+    const inst_rec *tl_inst, *tl_by_id;
+    const blas_ref *tl_blas;
+    const mesh_ref *meshes;
+    uint32_t two_level;
     const float *xyz;
     const uint32_t *idx;
     const uint32_t *tri_mat;
@@ -155,29 +182,80 @@ __global__ void __launch_bounds__(PT_THREADS)
 template<class J>
 __global__ void __launch_bounds__(PT_THREADS)
         k_pt_extend(J S, const vkg_ray *__restrict__ q_ray, const uint32_t *__restrict__ q_pid,
-                    const uint32_t *__restrict__ count, vkg_hit *__restrict__ hits)
+                    const uint32_t *__restrict__ count, vkg_hit *__restrict__ hits, uint32_t *__restrict__ hit_inst)
 {
     const uint32_t n = *count;
     const uint32_t stride = gridDim.x * blockDim.x;
     for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
     {
         const pt_params &P = S.params(J::per_path ? q_pid[i] : 0u);
-        const node8 *nodes = P.nodes;
-        const tri_rec *tris = P.tris;
         const float4 *rp = reinterpret_cast<const float4 *>(q_ray + i);
         const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
+        if(P.two_level)
+        {
+            const tlas_result r = trace_tlas<false>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y,
+                                                    r1.z, r1.w, CULL_BACK_UNLESS_TWOSIDED);
+            reinterpret_cast<uint4 *>(hits)[i] =
+                    make_uint4(r.prim, __float_as_uint(r.t), __float_as_uint(r.u), __float_as_uint(r.v));
+            hit_inst[i] = r.inst;
+            continue;
+        }
         unsigned long long v = 0, t = 0;
-        trace_result r = trace_ray<false, false>(nodes, tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w,
+        trace_result r = trace_ray<false, false>(P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w,
                                                  CULL_BACK_UNLESS_TWOSIDED, v, t, nullptr);
         reinterpret_cast<uint4 *>(hits)[i] =
                 make_uint4(r.prim, __float_as_uint(r.t), __float_as_uint(r.u), __float_as_uint(r.v));
     }
 }
 
+// surface point, unit geometric normal (world space) and material of a hit: the triangle's vertices,
+// the barycentric point; for an instanced scene both moved to world space (point by the
+// object -> world transform, normal by the transpose of world -> object)
+__device__ __forceinline__ void hit_surface(const pt_params &P, uint32_t prim, uint32_t inst, float bu, float bv,
+                                            float3 &p, float3 &ng, uint32_t &mat)
+{
+    const float *xyz = P.xyz;
+    const uint32_t *idx = P.idx;
+    const inst_rec *R = nullptr;
+    if(P.two_level)
+    {
+        R = P.tl_by_id + inst;
+        const mesh_ref M = P.meshes[__ldg(&R->blas)];
+        xyz = M.xyz;
+        idx = M.idx;
+    }
+    const uint32_t i0 = __ldg(&idx[3 * (size_t)prim]), i1 = __ldg(&idx[3 * (size_t)prim + 1]),
+                   i2 = __ldg(&idx[3 * (size_t)prim + 2]);
+    const float3 v0 = f3(__ldg(&xyz[3 * (size_t)i0]), __ldg(&xyz[3 * (size_t)i0 + 1]), __ldg(&xyz[3 * (size_t)i0 + 2]));
+    const float3 v1 = f3(__ldg(&xyz[3 * (size_t)i1]), __ldg(&xyz[3 * (size_t)i1 + 1]), __ldg(&xyz[3 * (size_t)i1 + 2]));
+    const float3 v2 = f3(__ldg(&xyz[3 * (size_t)i2]), __ldg(&xyz[3 * (size_t)i2 + 1]), __ldg(&xyz[3 * (size_t)i2 + 2]));
+    const float3 e1 = v1 - v0, e2 = v2 - v0;
+    p = v0 + e1 * bu + e2 * bv;
+    float3 n = cross(e1, e2);
+    if(R)
+    {
+        float o[12], w[12];
+        for(int k = 0; k < 12; ++k)
+        {
+            o[k] = __ldg(&R->o2w[k]);
+            w[k] = __ldg(&R->w2o[k]);
+        }
+        p = f3(o[0] * p.x + o[1] * p.y + o[2] * p.z + o[3], o[4] * p.x + o[5] * p.y + o[6] * p.z + o[7],
+               o[8] * p.x + o[9] * p.y + o[10] * p.z + o[11]);
+        n = f3(w[0] * n.x + w[4] * n.y + w[8] * n.z, w[1] * n.x + w[5] * n.y + w[9] * n.z,
+               w[2] * n.x + w[6] * n.y + w[10] * n.z);
+        mat = __ldg(&R->material);
+    }
+    else
+        mat = __ldg(&P.tri_mat[prim]);
+    ng = normalize(n);
+}
+
 template<int MODE, class J>
 __global__ void __launch_bounds__(PT_THREADS)
         k_pt_shade(J S, uint32_t depth, const vkg_ray *__restrict__ in_ray,
                    const uint32_t *__restrict__ in_pid, const vkg_hit *__restrict__ hits,
+                   const uint32_t *__restrict__ hit_inst,
                    const uint32_t *__restrict__ in_count, vkg_ray *__restrict__ out_ray,
                    uint32_t *__restrict__ out_pid, uint32_t *__restrict__ out_count, vkg_ray *__restrict__ s_ray,
                    uint32_t *__restrict__ s_pid, float4 *__restrict__ s_contrib, uint32_t *__restrict__ s_count,
@@ -227,22 +305,13 @@ __global__ void __launch_bounds__(PT_THREADS)
             }
             else
             {
-                const uint32_t prim = h.x;
-                const float bu = __uint_as_float(h.z), bv = __uint_as_float(h.w);
-                const uint32_t i0 = __ldg(&P.idx[3 * (size_t)prim]), i1 = __ldg(&P.idx[3 * (size_t)prim + 1]),
-                               i2 = __ldg(&P.idx[3 * (size_t)prim + 2]);
-                const float3 v0 = f3(__ldg(&P.xyz[3 * (size_t)i0]), __ldg(&P.xyz[3 * (size_t)i0 + 1]),
-                                     __ldg(&P.xyz[3 * (size_t)i0 + 2]));
-                const float3 v1 = f3(__ldg(&P.xyz[3 * (size_t)i1]), __ldg(&P.xyz[3 * (size_t)i1 + 1]),
-                                     __ldg(&P.xyz[3 * (size_t)i1 + 2]));
-                const float3 v2 = f3(__ldg(&P.xyz[3 * (size_t)i2]), __ldg(&P.xyz[3 * (size_t)i2 + 1]),
-                                     __ldg(&P.xyz[3 * (size_t)i2 + 2]));
-                const float3 e1 = v1 - v0, e2 = v2 - v0;
-                P0 = v0 + e1 * bu + e2 * bv;
-                const float3 ng = normalize(cross(e1, e2));
+                float3 ng;
+                uint32_t mat;
+                hit_surface(P, h.x, P.two_level ? hit_inst[i] : 0u, __uint_as_float(h.z), __uint_as_float(h.w), P0,
+                            ng, mat);
                 N = dot(ng, dir) < 0.f ? ng : -ng; // shading normal faces the incoming ray
                 const float3 V = -dir;
-                const vkg_material mt = P.mats[__ldg(&P.tri_mat[prim])];
+                const vkg_material mt = P.mats[mat];
                 material_view m;
                 m.base = P.disable_material ? f3(0.8f, 0.8f, 0.8f) : f3(mt.base_color[0], mt.base_color[1], mt.base_color[2]);
                 m.roughness = mt.roughness;
@@ -384,14 +453,21 @@ __global__ void __launch_bounds__(PT_THREADS)
     for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
     {
         const pt_params &P = S.params(J::per_path ? s_pid[i] : 0u);
-        const node8 *nodes = P.nodes;
-        const tri_rec *tris = P.tris;
         const float4 *rp = reinterpret_cast<const float4 *>(s_ray + i);
         const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
-        unsigned long long v = 0, t = 0;
-        trace_result r = trace_ray<true, false>(nodes, tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, CULL_NONE,
-                                                v, t, nullptr);
-        if(!r.occluded)
+        bool occluded;
+        if(P.two_level)
+            occluded = trace_tlas<true>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w,
+                                        CULL_NONE)
+                               .occluded;
+        else
+        {
+            unsigned long long v = 0, t = 0;
+            occluded = trace_ray<true, false>(P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, CULL_NONE,
+                                              v, t, nullptr)
+                               .occluded;
+        }
+        if(!occluded)
         {
             const uint32_t pid = s_pid[i];
             const float4 c = s_contrib[i];
@@ -412,8 +488,8 @@ template<bool SHADOW, class J>
 __global__ void __launch_bounds__(PT_THREADS)
         k_pt_trace_persistent(J S, const vkg_ray *__restrict__ q_ray, const uint32_t *__restrict__ q_pid,
                               const uint32_t *__restrict__ count, vkg_hit *__restrict__ hits,
-                              const float4 *__restrict__ s_contrib, float4 *__restrict__ radiance,
-                              uint32_t *__restrict__ work)
+                              uint32_t *__restrict__ hit_inst, const float4 *__restrict__ s_contrib,
+                              float4 *__restrict__ radiance, uint32_t *__restrict__ work)
 {
     const uint32_t n = *count;
     const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
@@ -439,12 +515,41 @@ __global__ void __launch_bounds__(PT_THREADS)
                 if(idx < n)
                 {
                     const pt_params &P = S.params(J::per_path ? q_pid[idx] : 0u);
-                    nodes = P.nodes;
-                    tris = P.tris;
                     const float4 *rp = reinterpret_cast<const float4 *>(q_ray + idx);
                     const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
-                    ray_init(s, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w);
-                    cur = idx;
+                    if(P.two_level)
+                    {
+                        // instanced scene: the whole two-level query at once, the lane asks again
+                        const tlas_result r = trace_tlas<SHADOW>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z,
+                                                                 r0.w, r1.x, r1.y, r1.z, r1.w,
+                                                                 SHADOW ? CULL_NONE : CULL_BACK_UNLESS_TWOSIDED);
+                        if constexpr(SHADOW)
+                        {
+                            if(!r.occluded)
+                            {
+                                const uint32_t pid = q_pid[idx];
+                                const float4 c = s_contrib[idx];
+                                float4 L = radiance[pid];
+                                L.x += c.x;
+                                L.y += c.y;
+                                L.z += c.z;
+                                radiance[pid] = L;
+                            }
+                        }
+                        else
+                        {
+                            reinterpret_cast<uint4 *>(hits)[idx] =
+                                    make_uint4(r.prim, __float_as_uint(r.t), __float_as_uint(r.u), __float_as_uint(r.v));
+                            hit_inst[idx] = r.inst;
+                        }
+                    }
+                    else
+                    {
+                        nodes = P.nodes;
+                        tris = P.tris;
+                        ray_init(s, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w);
+                        cur = idx;
+                    }
                 }
                 else
                     exhausted = true;
@@ -622,8 +727,17 @@ inline pt_params make_params(const vkg_scene *sc, const vkg_camera &cam, const v
                              uint32_t batch)
 {
     pt_params P{};
-    P.nodes = sc->bvh->d_nodes;
-    P.tris = sc->bvh->d_tris;
+    P.nodes = sc->bvh ? sc->bvh->d_nodes : nullptr;
+    P.tris = sc->bvh ? sc->bvh->d_tris : nullptr;
+    if(sc->tlas)
+    {
+        P.two_level = 1;
+        P.tl_nodes = sc->tlas->top.d_nodes;
+        P.tl_inst = sc->tlas->d_inst;
+        P.tl_by_id = sc->tlas->d_inst_by_id;
+        P.tl_blas = sc->tlas->d_blas;
+        P.meshes = sc->d_meshes;
+    }
     P.xyz = sc->xyz;
     P.idx = sc->idx;
     P.tri_mat = sc->tri_mat;

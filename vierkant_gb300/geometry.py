@@ -95,3 +95,68 @@ def batch_scene_params(index: int, seed: int = 0x5EED, min_tris: int = 5_000, ma
     spheres = max(1, int(round((target - 10) / 3072)))
     return {"stream": 3 + index, "spheres": spheres, "triangles": 10 + 3072 * spheres,
             "resolution": BATCH_RESOLUTIONS[min(3, int(u_res * 4))], "spp": BATCH_SPP[min(2, int(u_spp * 3))]}
+
+
+def cubesphere(n: int, radius: float = 1.0):
+    """cube-sphere of n x n quads per face: (xyz [6(n+1)^2, 3] f32, indices [12 n^2, 3] u32)"""
+    xyz = np.zeros((6 * (n + 1) ** 2, 3), np.float32)
+    idx = np.zeros((12 * n * n, 3), np.uint32)
+    check(lib().vkg_geometry_cubesphere(n, C.c_float(radius), _p(xyz), _p(idx)))
+    return xyz, idx
+
+
+def terrain(n: int = 2048, extent: float = 512.0, height: float = 40.0, frequency: float = 1.0 / 128.0,
+            octaves: int = 8, seed: int = 0x5EED):
+    """fBm-over-simplex heightfield: (xyz [n^2, 3] f32, indices [2 (n-1)^2, 3] u32)"""
+    xyz = np.zeros((n * n, 3), np.float32)
+    idx = np.zeros((2 * (n - 1) ** 2, 3), np.uint32)
+    check(lib().vkg_geometry_terrain(n, C.c_float(extent), C.c_float(height), C.c_float(frequency), octaves, seed,
+                                     _p(xyz), _p(idx)))
+    return xyz, idx
+
+
+def random_instances(n: int, num_meshes: int, lo, hi, *, seed: int = 0x5EED, stream: int = 5, mat_base: int = 0,
+                     num_mats: int = 1, smin: float = 0.5, smax: float = 2.0):
+    """n instances (vierkant_gb300.raytracing.INSTANCE_DTYPE) with uniform translation in [lo, hi],
+    uniform rotation, scale U[smin, smax], uniform mesh and material (PCG32(seed, stream))"""
+    from .raytracing import INSTANCE_DTYPE
+    out = np.zeros(n, INSTANCE_DTYPE)
+    lo = np.asarray(lo, np.float32)
+    hi = np.asarray(hi, np.float32)
+    check(lib().vkg_instances_random(seed, stream, n, num_meshes, mat_base, num_mats, _p(lo), _p(hi), C.c_float(smin),
+                                     C.c_float(smax), _p(out)))
+    return out
+
+
+def stress_scene(*, terrain_n: int = 2048, num_instances: int = 100_000, num_meshes: int = 20,
+                 num_materials: int = 256, seed: int = 0x5EED):
+    """The stress workload: a terrain_n^2-vertex fBm terrain (8 octaves, 512 x 512 units, +-40 height)
+    and num_instances instances of num_meshes cube-spheres (n = 21 .. 65 quads per face, i.e. 5,292 to
+    50,700 triangles) with uniform translation over the terrain's box, uniform rotation, scale U[0.5, 2]
+    and one of num_materials random metal-rough materials (PCG32(seed, stream 5)).
+    Returns dict(meshes=[(xyz, idx, twosided)], instances, materials)."""
+    tx, ti = terrain(terrain_n, seed=seed)
+    meshes = [(tx, ti, 1)]
+    for k in range(num_meshes):
+        n = 21 + int(round(44 * k / max(1, num_meshes - 1)))
+        x, i = cubesphere(n, 1.0)
+        meshes.append((x, i, 0))
+    lo = tx.min(axis=0)
+    hi = tx.max(axis=0)
+    inst = random_instances(num_instances, num_meshes, lo, hi, seed=seed, stream=5, mat_base=1,
+                            num_mats=num_materials)
+    inst["blas"] += 1  # mesh 0 is the terrain
+    from .raytracing import INSTANCE_DTYPE
+    ground = np.zeros(1, INSTANCE_DTYPE)
+    ground[0]["transform"] = np.array([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], np.float32)
+    ground[0]["blas"] = 0
+    ground[0]["material"] = 0
+    mats = np.zeros(1 + num_materials, MATERIAL_DTYPE)
+    mats[0]["base_color"] = (0.35, 0.45, 0.30)
+    mats[0]["roughness"] = 0.9
+    g = _Pcg32(seed, 6)
+    for m in range(1, 1 + num_materials):
+        mats[m]["base_color"] = [0.1 + 0.8 * g.uniform() for _ in range(3)]
+        mats[m]["roughness"] = 0.05 + 0.95 * g.uniform()
+        mats[m]["metalness"] = 1.0 if g.uniform() < 0.3 else 0.0
+    return {"meshes": meshes, "instances": np.concatenate([ground, inst]), "materials": mats}

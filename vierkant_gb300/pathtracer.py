@@ -95,6 +95,57 @@ class Scene:
             pass
 
 
+class InstancedScene:
+    """A two-level scene: meshes [(xyz, indices, twosided)] each with its own BVH, instances
+    (raytracing.INSTANCE_DTYPE: object -> world transform, mesh, material) under a top-level BVH,
+    materials (MATERIAL_DTYPE) and the environment map. Renders with PBRPathTracer like Scene."""
+
+    def __init__(self, ctx: Context, meshes, instances, materials, env_rgb, leaf_max=4):
+        from ._lib import vkg_instanced_scene_desc, vkg_mesh_desc
+        from .raytracing import INSTANCE_DTYPE
+        dev = f"cuda:{ctx.device}"
+        self.ctx = ctx
+        self._keep = []
+        descs = (vkg_mesh_desc * max(1, len(meshes)))()
+        for k, (xyz, idx, twosided) in enumerate(meshes):
+            x = torch.from_numpy(np.ascontiguousarray(xyz, np.float32)).to(dev)
+            i = torch.from_numpy(np.ascontiguousarray(idx, np.uint32).view(np.int32)).to(dev)
+            self._keep += [x, i]
+            descs[k] = vkg_mesh_desc(x.data_ptr(), x.shape[0], i.data_ptr(), i.shape[0], int(twosided), 0)
+        inst = torch.from_numpy(np.ascontiguousarray(instances, INSTANCE_DTYPE).view(np.uint8).copy()).to(dev)
+        mats = torch.from_numpy(np.frombuffer(np.ascontiguousarray(materials).tobytes(), np.uint8).copy()).to(dev)
+        env = env_rgb.to(dev, torch.float32).contiguous()
+        self._keep += [inst, mats, env]
+        d = vkg_instanced_scene_desc(descs, len(meshes), inst.data_ptr(), len(instances), mats.data_ptr(),
+                                     len(materials), env.data_ptr(), env.shape[1], env.shape[0], leaf_max)
+        h = C.c_void_p()
+        check(lib().vkg_scene_create_instanced(ctx.handle, C.byref(d), C.byref(h), C.c_void_p(ctx.stream())),
+              ctx.handle, "vkg_scene_create_instanced")
+        self.handle = h
+        self._keep = []  # the scene copied everything it needs
+        self.num_instances = len(instances)
+        ctx.adopt(self)
+
+    def bounds(self):
+        from ._lib import vkg_tlas_info
+        t = C.c_void_p()
+        check(lib().vkg_scene_tlas(self.handle, C.byref(t)))
+        inf = vkg_tlas_info()
+        check(lib().vkg_tlas_info_get(t, C.byref(inf)))
+        return tuple(inf.scene_min), tuple(inf.scene_max)
+
+    def close(self):
+        if getattr(self, "handle", None) and getattr(self.ctx, "handle", None):
+            lib().vkg_scene_destroy(self.ctx.handle, self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class PBRPathTracer:
     """PBRPathTracer::create / settings / render_scene / reset_accumulator / current_batch / statistics."""
 
