@@ -231,10 +231,11 @@ def run_ours(args):
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_baseline(sc, batch, budget_s=args.cpu_seconds)
-    pt_block = batch_block = None
+    pt_block = batch_block = stress = None
     if rank == 0 and not args.no_pt:
         pt_block = path_tracer_block(ctx, frames=args.nrc_frames)
         batch_block = batched_block(ctx)
+        stress = stress_block(ctx)
 
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 1), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
@@ -254,6 +255,8 @@ def run_ours(args):
             line["path_tracer"] = pt_block
         if batch_block is not None:
             line["batched"] = batch_block
+        if stress is not None:
+            line["stress"] = stress
         print(json.dumps(line), flush=True)
     bvh.close()
     ctx.close()
@@ -404,6 +407,47 @@ def batched_block(ctx):
                        "ctas_per_sm": int(tun.ctas_per_sm), "wave_paths": int(tun.wave_paths),
                        "autotune_s": round(tune_s, 2), "graph": True},
             "one_scene_at_a_time_ms": round(seq_ms, 2), "speedup_vs_one_at_a_time": round(seq_ms / best, 3)}
+
+
+def stress_block(ctx):
+    """The stress workload: an 8,380,418-triangle fBm terrain (2048^2 vertices) plus 100,000 instances of
+    20 cube-spheres (5,292 to 50,700 triangles) under a two-level BVH, rendered at 3840x2160 x 16 spp,
+    8 segments, Russian roulette from the 3rd interaction, environment as the Cornell workload."""
+    import torch
+    from vierkant_gb300 import geometry
+    from vierkant_gb300.pathtracer import InstancedScene, PBRPathTracer, procedural_sky, sun_direction
+
+    t0 = time.perf_counter()
+    st = geometry.stress_scene()
+    gen_s = time.perf_counter() - t0
+    env = procedural_sky(ctx, 2048, 1024, sun_direction(), 5e4, 3.8e-5)
+    t0 = time.perf_counter()
+    scene = InstancedScene(ctx, st["meshes"], st["instances"], st["materials"], env)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    W, H = 3840, 2160
+    cam = geometry.camera_lookat((0, 120, 300), (0, 0, 0), (0, 1, 0), 40.0, W, H)
+    s = PBRPathTracer.default_settings()
+    s.resolution[0], s.resolution[1] = W, H
+    s.num_samples, s.max_trace_depth, s.rr_start_depth = 16, 8, 3
+    pt = PBRPathTracer(ctx, seed=SEED, settings=s)
+    pt.render_scene(scene, cam)
+    best = None
+    for _ in range(2):
+        pt.render_scene(scene, cam)
+        stt = pt.statistics()
+        if best is None or stt.total_ms < best.total_ms:
+            best = stt
+    pt.close()
+    tris = sum(len(m[1]) for m in st["meshes"])
+    inst_tris = sum(len(st["meshes"][int(b)][1]) for b in st["instances"]["blas"])
+    scene.close()
+    rays = best.extension_rays + best.shadow_rays
+    return {"terrain_triangles": len(st["meshes"][0][1]), "instances": len(st["instances"]) - 1,
+            "mesh_triangles": tris, "instanced_triangles": int(inst_tris), "resolution": [W, H], "spp": 16,
+            "segments": 8, "render_ms": round(best.total_ms, 1), "samples_per_s": round(best.paths / best.total_ms * 1e3),
+            "mrays_per_s": round(rays / best.total_ms / 1e3, 1), "rays": int(rays),
+            "generate_s": round(gen_s, 2), "scene_build_s": round(build_s, 2)}
 
 
 def cpu_reference_lib():

@@ -582,6 +582,77 @@ __global__ void __launch_bounds__(PT_THREADS)
     }
 }
 
+// the same persistent refilling for instanced scenes: one two-level node per step (tl_step), so a
+// lane whose ray finished takes the next ray of the queue at once instead of idling until the slowest
+// lane of its warp is done. One scene per launch. `work` must be zero at launch.
+template<bool SHADOW>
+__global__ void __launch_bounds__(PT_THREADS)
+        k_pt_tl_persistent(single_scene S, const vkg_ray *__restrict__ q_ray, const uint32_t *__restrict__ q_pid,
+                           const uint32_t *__restrict__ count, vkg_hit *__restrict__ hits,
+                           uint32_t *__restrict__ hit_inst, const float4 *__restrict__ s_contrib,
+                           float4 *__restrict__ radiance, uint32_t *__restrict__ work)
+{
+    const pt_params &P = S.P;
+    const uint32_t n = *count;
+    const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
+    const int cull = SHADOW ? CULL_NONE : CULL_BACK_UNLESS_TWOSIDED;
+    tl_state s;
+    uint32_t cur = 0xFFFFFFFFu;
+    bool exhausted = false;
+    for(;;)
+    {
+        const bool need = cur == 0xFFFFFFFFu && !exhausted;
+        const unsigned m = __ballot_sync(0xffffffffu, need);
+        if(m)
+        {
+            const uint32_t leader = __ffs(m) - 1;
+            uint32_t base = 0;
+            if(lane == leader) base = atomicAdd(work, (uint32_t)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if(need)
+            {
+                const uint32_t idx = base + __popc(m & lt);
+                if(idx < n)
+                {
+                    const float4 *rp = reinterpret_cast<const float4 *>(q_ray + idx);
+                    const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
+                    tl_init(s, P.tl_nodes, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w);
+                    cur = idx;
+                }
+                else
+                    exhausted = true;
+            }
+        }
+        const bool active = cur != 0xFFFFFFFFu;
+        if(!__any_sync(0xffffffffu, active)) break;
+        if(active && !tl_step<SHADOW>(s, P.tl_nodes, P.tl_inst, P.tl_blas, cull))
+        {
+            if constexpr(SHADOW)
+            {
+                if(!s.done)
+                {
+                    const uint32_t pid = q_pid[cur];
+                    const float4 c = s_contrib[cur];
+                    float4 L = radiance[pid];
+                    L.x += c.x;
+                    L.y += c.y;
+                    L.z += c.z;
+                    radiance[pid] = L;
+                }
+            }
+            else
+            {
+                const bool hit = s.best_prim != VKG_MISS;
+                reinterpret_cast<uint4 *>(hits)[cur] =
+                        make_uint4(s.best_prim, __float_as_uint(hit ? s.best_t : 0.f), __float_as_uint(hit ? s.bu : 0.f),
+                                   __float_as_uint(hit ? s.bv : 0.f));
+                hit_inst[cur] = s.best_inst;
+            }
+            cur = 0xFFFFFFFFu;
+        }
+    }
+}
+
 __global__ void k_fill_miss_queue(const uint32_t *__restrict__ count, vkg_hit *__restrict__ hits)
 {
     const uint32_t n = *count;
