@@ -142,6 +142,7 @@ struct vkg_batch
     std::vector<pt_params> params;
     std::vector<batch_job_dev> jdev;
     uint32_t njobs = 0, total_pix = 0, max_depth = 0;
+    bool any_instanced = false;
     uint64_t total_paths = 0;
     vkg_batch_tuning tuning{};
     pt_params *d_params = nullptr;
@@ -291,7 +292,8 @@ vkg_status ensure_waves(vkg_batch *b, const std::vector<vkg_batch::wave> &waves,
 vkg_status enqueue(vkg_batch *b, const std::vector<vkg_batch::wave> &waves, cudaStream_t st)
 {
     vkg_ctx *ctx = b->ctx;
-    const vkg_batch_tuning &T = b->tuning;
+    vkg_batch_tuning T = b->tuning;
+    if(b->any_instanced) T.extend_kernel = 1; // the persistent tracers handle single-level scenes only
     const job_table J{b->d_params, b->pjob, b->pinc};
     VKG_TRY_CUDA(ctx, cudaMemsetAsync(b->sum, 0, (size_t)b->total_pix * 3 * sizeof(float), st));
     cache_io io{};
@@ -445,6 +447,7 @@ vkg_status vkg_batch_create(vkg_ctx *ctx, const vkg_batch_job *jobs, uint32_t nj
     {
         const vkg_batch_job &jb = jobs[j];
         b->params.push_back(make_params(jb.scene, jb.camera, jb.settings, jb.seed, 0));
+        b->any_instanced = b->any_instanced || jb.scene->tlas != nullptr;
         const uint32_t npix = b->params.back().npix;
         b->jdev.push_back(batch_job_dev{npix, jb.settings.num_samples, off, jb.d_rgb_out});
         off += npix;

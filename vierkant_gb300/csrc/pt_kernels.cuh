@@ -483,7 +483,8 @@ __global__ void __launch_bounds__(PT_THREADS)
 // persistent queue tracer: each warp refills its finished lanes from the queue with one atomic
 // (work stealing), so rays of cheap and expensive scenes balance across the machine. SHADOW: any-hit
 // visibility of NEE rays, adding the contribution of unoccluded ones; else closest hit of extension
-// rays. `work` must be zero at launch.
+// rays. Single-level scenes only (instanced scenes use k_pt_tl_persistent or the grid-stride
+// kernels). `work` must be zero at launch.
 template<bool SHADOW, class J>
 __global__ void __launch_bounds__(PT_THREADS)
         k_pt_trace_persistent(J S, const vkg_ray *__restrict__ q_ray, const uint32_t *__restrict__ q_pid,
@@ -517,39 +518,10 @@ __global__ void __launch_bounds__(PT_THREADS)
                     const pt_params &P = S.params(J::per_path ? q_pid[idx] : 0u);
                     const float4 *rp = reinterpret_cast<const float4 *>(q_ray + idx);
                     const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
-                    if(P.two_level)
-                    {
-                        // instanced scene: the whole two-level query at once, the lane asks again
-                        const tlas_result r = trace_tlas<SHADOW>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z,
-                                                                 r0.w, r1.x, r1.y, r1.z, r1.w,
-                                                                 SHADOW ? CULL_NONE : CULL_BACK_UNLESS_TWOSIDED);
-                        if constexpr(SHADOW)
-                        {
-                            if(!r.occluded)
-                            {
-                                const uint32_t pid = q_pid[idx];
-                                const float4 c = s_contrib[idx];
-                                float4 L = radiance[pid];
-                                L.x += c.x;
-                                L.y += c.y;
-                                L.z += c.z;
-                                radiance[pid] = L;
-                            }
-                        }
-                        else
-                        {
-                            reinterpret_cast<uint4 *>(hits)[idx] =
-                                    make_uint4(r.prim, __float_as_uint(r.t), __float_as_uint(r.u), __float_as_uint(r.v));
-                            hit_inst[idx] = r.inst;
-                        }
-                    }
-                    else
-                    {
-                        nodes = P.nodes;
-                        tris = P.tris;
-                        ray_init(s, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w);
-                        cur = idx;
-                    }
+                    nodes = P.nodes;
+                    tris = P.tris;
+                    ray_init(s, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w);
+                    cur = idx;
                 }
                 else
                     exhausted = true;
