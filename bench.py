@@ -450,6 +450,76 @@ def stress_block(ctx):
             "generate_s": round(gen_s, 2), "scene_build_s": round(build_s, 2)}
 
 
+def profile_case(name: str):
+    """Small workloads for profiler captures (ncu): one case per call, no JSON line.
+    pt-frame   plain path tracer, Cornell scene, 1280x720 x 4 spp
+    nrc        radiance-cache kernels: 4 training steps of 65,536 records, inference of 262,144 queries
+               with the mma.sync, tcgen05 and fused tcgen05 kernels
+    batch      batched renderer, 4 scenes of the batched workload at 1 spp
+    stress     instanced scene: 512^2 terrain + 10,000 instances, 960x540 x 2 spp, 8 segments"""
+    import numpy as np
+    import torch
+    from vierkant_gb300 import geometry
+    from vierkant_gb300.raytracing import Context
+    from vierkant_gb300.pathtracer import InstancedScene, PBRPathTracer, Scene, procedural_sky, sun_direction
+    ctx = Context(0)
+    env = procedural_sky(ctx, 2048, 1024, sun_direction(), 5e4, 3.8e-5)
+    if name == "pt-frame":
+        sc = geometry.cornell_scene(SEED, 2, 64, 16)
+        scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], sc["materials"], env)
+        cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, 1280, 720)
+        s = PBRPathTracer.default_settings()
+        s.num_samples, s.max_trace_depth, s.rr_start_depth = 4, 6, 3
+        pt = PBRPathTracer(ctx, seed=SEED, settings=s)
+        pt.render_scene(scene, cam)
+    elif name == "nrc":
+        from vierkant_gb300.nrc import NeuralRadianceCache
+        g = torch.Generator(device="cuda").manual_seed(1)
+
+        def feats(n):
+            p = torch.rand((n, 3), device="cuda", generator=g) * 2 - 1
+            d = torch.nn.functional.normalize(torch.randn((n, 3), device="cuda", generator=g), dim=1)
+            nn_ = torch.nn.functional.normalize(torch.randn((n, 3), device="cuda", generator=g), dim=1)
+            return torch.cat([p, d, nn_, torch.rand((n, 4), device="cuda", generator=g)], dim=1).contiguous()
+        caches = []
+        for kind in (1, 2, 3):
+            cfg = NeuralRadianceCache.default_config()
+            cfg.infer_kernel = kind
+            caches.append(NeuralRadianceCache(ctx, cfg))
+        x, t = feats(65536), torch.rand((65536, 3), device="cuda", generator=g)
+        for _ in range(4):
+            caches[0].train_step(x, t)
+        q = feats(262144)
+        for c in caches:
+            c.infer(q)
+    elif name == "batch":
+        from vierkant_gb300.batch import BatchJob, BatchRenderer
+        jobs = []
+        for i in range(4):
+            p = geometry.batch_scene_params(i)
+            sc = geometry.cornell_scene(SEED, p["stream"], p["spheres"], 16)
+            scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], sc["materials"], env)
+            r = p["resolution"]
+            cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, r, r)
+            s = PBRPathTracer.default_settings()
+            s.resolution[0] = s.resolution[1] = r
+            s.num_samples, s.max_trace_depth, s.rr_start_depth = 1, 6, 3
+            jobs.append(BatchJob(scene, cam, s, SEED + i))
+        BatchRenderer(ctx, jobs).render()
+    elif name == "stress":
+        st = geometry.stress_scene(terrain_n=512, num_instances=10_000)
+        scene = InstancedScene(ctx, st["meshes"], st["instances"], st["materials"], env)
+        cam = geometry.camera_lookat((0, 120, 300), (0, 0, 0), (0, 1, 0), 40.0, 960, 540)
+        s = PBRPathTracer.default_settings()
+        s.resolution[0], s.resolution[1] = 960, 540
+        s.num_samples, s.max_trace_depth, s.rr_start_depth = 2, 8, 3
+        PBRPathTracer(ctx, seed=SEED, settings=s).render_scene(scene, cam)
+    else:
+        raise SystemExit(f"unknown profile case {name}")
+    torch.cuda.synchronize()
+    print(f"profile case {name} done")
+
+
 def cpu_reference_lib():
     """The reference's own ray-triangle code when it was compiled here (oracle/_ref), else the
     oracle's C port of it (bit-identical; checked by the tests)."""
@@ -535,7 +605,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-pt", action="store_true", help="skip the path-tracer / radiance-cache block")
     ap.add_argument("--nrc-frames", type=int, default=256)
+    ap.add_argument("--profile-case", choices=["pt-frame", "nrc", "batch", "stress"], default=None,
+                    help="run one small workload for a profiler capture and exit (no JSON line)")
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return
     if args.warmup < 3 and args.impl == "ours":
         print("note: timing rules want >= 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
