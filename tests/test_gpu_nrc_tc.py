@@ -71,3 +71,60 @@ def test_tc_inference_matches_mma_twin(ctx):
     assert tcc.info().kernel_error == 0 and fused.info().kernel_error == 0
     for c in (mma, tcc, fused):
         c.close()
+
+
+def _grads(ctx, train_kernel, feats, targets, w, g):
+    cfg = NeuralRadianceCache.default_config()
+    cfg.log2_table_size = 16
+    cfg.train_kernel = train_kernel
+    c = NeuralRadianceCache(ctx, cfg)
+    c.load_params(w, g)
+    c.backward(feats, targets)
+    torch.cuda.synchronize()
+    i = c.info()
+    from test_gpu_nrc import tensor_from
+    out = (tensor_from(i.d_mlp_grads, i.num_mlp_params), tensor_from(i.d_grid_grads, i.num_grid_params), i)
+    c.close()
+    return out
+
+
+@pytest.mark.parametrize("n", [1, 127, 4096, 70_001])
+def test_tc_weight_gradients_match_fp32_kernel(ctx, n):
+    """same BF16 activations and gradients, FP32 accumulation on both: equal up to summation order"""
+    gen = torch.Generator(device="cuda").manual_seed(n)
+    cfg = NeuralRadianceCache.default_config()
+    cfg.log2_table_size = 16
+    probe = NeuralRadianceCache(ctx, cfg)
+    i = probe.info()
+    w = torch.randn(i.num_mlp_params, device="cuda", generator=gen) * 0.2
+    g = torch.randn(i.num_grid_params, device="cuda", generator=gen) * 0.5
+    probe.close()
+    feats = random_features(n, 40 + n)
+    targets = torch.rand((n, 3), device="cuda", generator=gen)
+    w1, g1, i1 = _grads(ctx, 1, feats, targets, w, g)
+    w2, g2, i2 = _grads(ctx, 2, feats, targets, w, g)
+    assert i1.train_kernel == 1 and i2.train_kernel == 2 and i2.kernel_error == 0
+    # the hash-grid gradients do not depend on the weight-gradient kernel (float atomics: order only)
+    assert (g1 - g2).abs().max().item() <= 1e-5 * g1.abs().max().item() + 1e-9
+    scale = w1.abs().max().item()
+    assert scale > 0
+    assert (w1 - w2).abs().max().item() <= 1e-4 * scale + 1e-7, (w1 - w2).abs().max().item()
+
+
+def test_tc_training_fits_like_fp32(ctx):
+    from test_gpu_nrc import _field
+    test = random_features(8192, 999)
+    tt = _field(test)
+    errs = []
+    for kind in (1, 2):
+        cfg = NeuralRadianceCache.default_config()
+        cfg.train_kernel = kind
+        c = NeuralRadianceCache(ctx, cfg)
+        for step in range(200):
+            feats = random_features(65536, 1000 + step)
+            c.train_step(feats, _field(feats))
+        errs.append(((c.infer(test) - tt).abs().mean() / tt.abs().mean()).item())
+        assert c.info().kernel_error == 0
+        c.close()
+    print("held-out relative error fp32 / tcgen05 weight gradients:", errs)
+    assert errs[1] < 0.18 and abs(errs[1] - errs[0]) < 0.06

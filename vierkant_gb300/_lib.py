@@ -118,7 +118,7 @@ class vkg_nrc_config(C.Structure):
                 ("beta2", C.c_float), ("epsilon", C.c_float), ("seed", C.c_uint32), ("scene_min", C.c_float * 3),
                 ("scene_max", C.c_float * 3), ("batch_size", C.c_uint32), ("train_paths", C.c_uint32),
                 ("terminate_depth", C.c_uint32), ("train_depth", C.c_uint32), ("train_steps", C.c_uint32),
-                ("infer_kernel", C.c_uint32)]
+                ("infer_kernel", C.c_uint32), ("train_kernel", C.c_uint32)]
 
 
 class vkg_nrc_info_t(C.Structure):
@@ -126,7 +126,7 @@ class vkg_nrc_info_t(C.Structure):
                 ("level_resolution", C.c_uint32 * 16), ("num_mlp_params", C.c_uint32),
                 ("num_grid_params", C.c_uint64), ("d_mlp_params", C.c_void_p), ("d_grid_params", C.c_void_p),
                 ("d_mlp_grads", C.c_void_p), ("d_grid_grads", C.c_void_p), ("step", C.c_uint32),
-                ("kernel_error", C.c_uint32), ("infer_kernel", C.c_uint32)]
+                ("kernel_error", C.c_uint32), ("infer_kernel", C.c_uint32), ("train_kernel", C.c_uint32)]
 
 
 class vkg_bvh_build_options(C.Structure):

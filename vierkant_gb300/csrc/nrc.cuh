@@ -88,6 +88,9 @@ vkg_status nrc_pack_tc(vkg_ctx *ctx, const float *W, uint16_t *wtc, cudaStream_t
 vkg_status nrc_infer_tc(vkg_ctx *ctx, const grid_config &gc, const __half2 *grid, const uint16_t *wtc,
                         const float *feats, const uint32_t *X, uint32_t n, const uint32_t *d_n, float *Y, uint32_t *err,
                         cudaStream_t st);
+// weight gradients of n records on tcgen05 (accumulated into dW); err receives 1 if a wait ran out
+vkg_status nrc_wgrad_tc(vkg_ctx *ctx, const uint32_t *X, const uint32_t *H, const uint32_t *G, uint32_t n,
+                        const uint32_t *d_n, float *dW, uint32_t *err, cudaStream_t st);
 // one optimiser step (backward + Adam) on n records; records past *d_n contribute nothing
 vkg_status nrc_train(vkg_nrc *c, const float *feats, const float *targets, uint32_t n, const uint32_t *d_n,
                      cudaStream_t st);

@@ -251,7 +251,181 @@ __global__ void __launch_bounds__(TC_THREADS)
     if(warp == 0) tc::tmem_dealloc(tmem, TC_TMEM_COLS);
 }
 
+// ---- weight gradients on tcgen05 --------------------------------------------------------------
+// dW_l[k][o] = sum over records s of H_l[s][k] * G_l[s][o] (H_0 = the encoded inputs X, G_l the
+// gradient of layer l's pre-activation, both BF16 as the backward stored them). As one UMMA chain per
+// layer and chunk of 128 records: D (128 x N_l, FP32 in TMEM) += A (128 x 128) * B (N_l x 128)^T with
+// A = H_l^T zero-padded to 128 rows and B = G_l^T, both K-major over the records. The six
+// accumulators (336 TMEM columns) stay resident while the CTA walks its chunks; two shared-memory
+// buffer pairs let the staging of one layer overlap the MMAs of the previous one.
+constexpr uint32_t WG_TC_THREADS = 256, WG_TC_CHUNK = 128, WG_TC_TMEM = 512;
+constexpr uint32_t WG_A_BYTES = 128 * WG_TC_CHUNK * 2, WG_B_BYTES = 64 * WG_TC_CHUNK * 2;
+// two buffer pairs (96 KB) padded so that a single CTA fits per SM (its TMEM allocation takes all 512
+// columns)
+constexpr uint32_t WG_TC_SMEM = 120u * 1024u;
+
+__device__ __forceinline__ uint32_t tmem_col(int l) { return l < NLAYER - 1 ? 64u * (uint32_t)l : 320u; }
+
+// 16 BF16 values (8 u32) of record s into rows [r0, r0 + 16) of a K-major operand (K = 128 records)
+__device__ __forceinline__ void scatter16(uint8_t *buf, uint32_t r0, uint32_t s, const uint4 (&v)[2])
+{
+    const uint32_t w[8] = {v[0].x, v[0].y, v[0].z, v[0].w, v[1].x, v[1].y, v[1].z, v[1].w};
+#pragma unroll
+    for(int j = 0; j < 8; ++j)
+    {
+        *reinterpret_cast<uint16_t *>(buf + tc::canon_offset(r0 + 2 * j, s, WG_TC_CHUNK)) = (uint16_t)(w[j] & 0xFFFFu);
+        *reinterpret_cast<uint16_t *>(buf + tc::canon_offset(r0 + 2 * j + 1, s, WG_TC_CHUNK)) = (uint16_t)(w[j] >> 16);
+    }
+}
+
+__global__ void __launch_bounds__(WG_TC_THREADS)
+        k_wgrad_tc(const uint32_t *__restrict__ X, const uint32_t *__restrict__ H, const uint32_t *__restrict__ G,
+                   uint32_t n_cap, const uint32_t *__restrict__ d_n, float *__restrict__ dW, uint32_t *__restrict__ err)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t mbar[2];
+    __shared__ uint32_t tslot;
+    uint8_t *sA[2] = {smem, smem + WG_A_BYTES}, *sB[2] = {smem + 2 * WG_A_BYTES, smem + 2 * WG_A_BYTES + WG_B_BYTES};
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, s = tid & (WG_TC_CHUNK - 1), h = tid >> 7;
+    // A rows past a layer's inputs stay zero: clear both A buffers once
+    for(uint32_t i = tid; i < 2 * WG_A_BYTES / 16; i += WG_TC_THREADS)
+        reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0u, 0u, 0u, 0u);
+    if(warp == 0) tc::tmem_alloc(&tslot, WG_TC_TMEM);
+    if(tid == 0)
+    {
+        tc::mbar_init(&mbar[0], 1);
+        tc::mbar_init(&mbar[1], 1);
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tslot;
+    const uint32_t n = d_n ? min(*d_n, n_cap) : n_cap;
+    const uint32_t chunks = (n + WG_TC_CHUNK - 1) / WG_TC_CHUNK;
+    uint32_t phase[2] = {0u, 0u};
+    bool used[2] = {false, false}, failed = false, any = false;
+    for(uint32_t c = blockIdx.x; c < chunks && !failed; c += gridDim.x)
+    {
+        const uint32_t r = c * WG_TC_CHUNK + s;
+        const bool valid = r < n;
+#pragma unroll 1
+        for(int l = 0; l < NLAYER; ++l)
+        {
+            const uint32_t b = (uint32_t)l & 1u, K = layer_in(l), N = layer_out(l);
+            if(used[b])
+            {
+                // the MMAs that read this buffer pair last must be done before it is overwritten
+                const bool ok = tc::mbar_wait(&mbar[b], phase[b]);
+                if(__syncthreads_or(!ok))
+                {
+                    failed = true;
+                    break;
+                }
+                phase[b] ^= 1u;
+                used[b] = false;
+            }
+            // A: this record's layer inputs in blocks of 16 rows, the two halves of the CTA alternating
+            const uint32_t *arow = l == 0 ? X + (size_t)r * 40 : H + (size_t)r * 160 + 32 * (l - 1);
+            for(uint32_t k0 = 16 * h; k0 < K; k0 += 32)
+            {
+                uint4 v[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
+                if(valid)
+                {
+                    v[0] = *reinterpret_cast<const uint4 *>(arow + k0 / 2);
+                    v[1] = *reinterpret_cast<const uint4 *>(arow + k0 / 2 + 4);
+                }
+                scatter16(sA[b], k0, s, v);
+            }
+            if(b == 0 && l > 0 && h == 1)
+                // rows 64..79 of buffer 0 still hold layer 0's last inputs
+                for(uint32_t k = 64; k < 80; ++k)
+                    *reinterpret_cast<uint16_t *>(sA[b] + tc::canon_offset(k, s, WG_TC_CHUNK)) = 0;
+            // B: this record's output gradients in blocks of 16 rows
+            const uint32_t *grow = G + (size_t)r * 168 + (l == NLAYER - 1 ? 160 : 32 * l);
+            for(uint32_t o0 = 16 * h; o0 < N; o0 += 32)
+            {
+                uint4 v[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
+                if(valid)
+                {
+                    v[0] = *reinterpret_cast<const uint4 *>(grow + o0 / 2);
+                    v[1] = *reinterpret_cast<const uint4 *>(grow + o0 / 2 + 4);
+                }
+                scatter16(sB[b], o0, s, v);
+            }
+            tc::fence_async_smem();
+            tc::fence_before_sync();
+            __syncthreads();
+            if(tid == 0)
+            {
+                tc::fence_after_sync();
+                const uint32_t idesc = tc::idesc_bf16(128, N);
+                const uint32_t a0 = tc::smem_addr(sA[b]), b0 = tc::smem_addr(sB[b]);
+                for(uint32_t k = 0; k < WG_TC_CHUNK / 16; ++k)
+                    tc::mma_bf16(tmem + tmem_col(l), tc::smem_desc(a0 + 256u * k, 128u, WG_TC_CHUNK * 16u),
+                                 tc::smem_desc(b0 + 256u * k, 128u, WG_TC_CHUNK * 16u), idesc, any || k > 0);
+                tc::mma_commit(&mbar[b]);
+            }
+            used[b] = true;
+        }
+        any = true;
+    }
+    // the last MMAs of both buffers
+    for(int b = 0; b < 2 && !failed; ++b)
+        if(used[b])
+        {
+            const bool ok = tc::mbar_wait(&mbar[b], phase[b]);
+            if(__syncthreads_or(!ok)) failed = true;
+            else
+            {
+                phase[b] ^= 1u;
+                used[b] = false;
+            }
+        }
+    if(failed)
+    {
+        if(tid == 0) atomicOr(err, TC_TIMEOUT);
+        for(int b = 0; b < 2; ++b)
+            if(used[b]) tc::mbar_wait(&mbar[b], phase[b]);
+    }
+    else if(any)
+    {
+        tc::fence_after_sync();
+        // lane k = 32 (warp mod 4) + lane of TMEM holds row k of every layer's accumulator
+        const uint32_t k = 32u * (warp & 3u) + (tid & 31u), lane_base = (32u * (warp & 3u)) << 16;
+#pragma unroll 1
+        for(int l = 0; l < NLAYER; ++l)
+        {
+            const uint32_t K = layer_in(l), N = layer_out(l);
+            for(uint32_t c0 = 16u * h; c0 < N; c0 += 32u)
+            {
+                float v[16];
+                tc::tmem_ld16(tmem + lane_base + tmem_col(l) + c0, v);
+                tc::tmem_ld_wait();
+                if(k < K)
+                    for(int j = 0; j < 16; ++j)
+                        if(c0 + j < N) atomicAdd(&dW[layer_off(l) + k * N + c0 + j], v[j]);
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if(warp == 0) tc::tmem_dealloc(tmem, WG_TC_TMEM);
+}
+
 }// namespace
+
+vkg_status nrc_wgrad_tc(vkg_ctx *ctx, const uint32_t *X, const uint32_t *H, const uint32_t *G, uint32_t n,
+                        const uint32_t *d_n, float *dW, uint32_t *err, cudaStream_t st)
+{
+    if(n == 0) return VKG_OK;
+    VKG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WG_TC_SMEM));
+    const uint32_t chunks = (n + WG_TC_CHUNK - 1) / WG_TC_CHUNK;
+    const uint32_t grid = std::min<uint32_t>(chunks, (uint32_t)ctx->num_sms);
+    k_wgrad_tc<<<grid, WG_TC_THREADS, WG_TC_SMEM, st>>>(X, H, G, n, d_n, dW, err);
+    return cuda_check(ctx, cudaGetLastError(), "k_wgrad_tc");
+}
 
 vkg_status nrc_pack_tc(vkg_ctx *ctx, const float *W, uint16_t *wtc, cudaStream_t st)
 {
