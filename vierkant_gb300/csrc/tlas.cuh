@@ -48,8 +48,7 @@ struct tl_state
     const tri_rec *tris;
     int sp;
     bool in_blas, done;
-    uint32_t st_node[TL_STACK];
-    float st_t[TL_STACK];
+    uint2 st[TL_STACK]; // {entry, entry distance (float bits)}
 };
 
 __device__ __forceinline__ void tl_init(tl_state &s, const node8 *tnodes, float ox, float oy, float oz, float tmin,
@@ -75,8 +74,7 @@ __device__ __forceinline__ void tl_init(tl_state &s, const node8 *tnodes, float 
     s.in_blas = false;
     s.done = false;
     s.sp = 1;
-    s.st_node[0] = 0;
-    s.st_t[0] = tmin;
+    s.st[0] = make_uint2(0u, __float_as_uint(tmin));
 }
 
 // one node of the two-level traversal; false once the ray is finished
@@ -87,7 +85,8 @@ __device__ __forceinline__ bool tl_step(tl_state &s, const node8 *__restrict__ t
     while(s.sp > 0 && !s.done)
     {
         --s.sp;
-        const uint32_t e = s.st_node[s.sp];
+        const uint2 ent = s.st[s.sp];
+        const uint32_t e = ent.x;
         if(e == TL_RETURN)
         {
             for(int a = 0; a < 3; ++a)
@@ -100,7 +99,7 @@ __device__ __forceinline__ bool tl_step(tl_state &s, const node8 *__restrict__ t
             s.in_blas = false;
             continue;
         }
-        if(s.st_t[s.sp] > s.best_t) continue;
+        if(__uint_as_float(ent.y) > s.best_t) continue;
         if(!s.in_blas && (e & INST_BIT))
         {
             // enter an instance: object-space ray, RETURN marker, BLAS root
@@ -115,10 +114,8 @@ __device__ __forceinline__ bool tl_step(tl_state &s, const node8 *__restrict__ t
             s.tris = B.tris;
             s.cur_inst = meta.y;
             s.in_blas = true;
-            s.st_node[s.sp] = TL_RETURN;
-            s.st_t[s.sp] = s.tmin;
-            s.st_node[s.sp + 1] = 0;
-            s.st_t[s.sp + 1] = s.tmin;
+            s.st[s.sp] = make_uint2(TL_RETURN, __float_as_uint(s.tmin));
+            s.st[s.sp + 1] = make_uint2(0u, __float_as_uint(s.tmin));
             s.sp += 2;
             continue;
         }
@@ -183,16 +180,14 @@ __device__ __forceinline__ bool tl_step(tl_state &s, const node8 *__restrict__ t
                 for(uint32_t q = cnt; q-- > 0;)
                     if(s.sp < (int)TL_STACK)
                     {
-                        s.st_node[s.sp] = INST_BIT | (start + q);
-                        s.st_t[s.sp] = te;
+                        s.st[s.sp] = make_uint2(INST_BIT | (start + q), __float_as_uint(te));
                         ++s.sp;
                     }
                 continue;
             }
             if(s.sp < (int)TL_STACK)
             {
-                s.st_node[s.sp] = c;
-                s.st_t[s.sp] = te;
+                s.st[s.sp] = make_uint2(c, __float_as_uint(te));
                 ++s.sp;
             }
         }

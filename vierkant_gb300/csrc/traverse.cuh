@@ -84,8 +84,7 @@ struct ray_state
     uint32_t best;
     int sp;
     bool done;
-    uint32_t st_node[TRAVERSAL_STACK];
-    float st_t[TRAVERSAL_STACK];
+    uint2 st[TRAVERSAL_STACK]; // {node, entry distance (float bits)}: one 64-bit access per push / pop
 };
 
 __device__ __forceinline__ void ray_init(ray_state &s, float ox, float oy, float oz, float tmin, float dx, float dy,
@@ -107,8 +106,7 @@ __device__ __forceinline__ void ray_init(ray_state &s, float ox, float oy, float
     s.best = VKG_MISS;
     s.done = false;
     s.sp = 1;
-    s.st_node[0] = 0;
-    s.st_t[0] = tmin;
+    s.st[0] = make_uint2(0u, __float_as_uint(tmin));
 }
 
 // entry-distance keys of the children of node ni for a ray (origin o, reciprocal direction i,
@@ -167,8 +165,9 @@ __device__ __forceinline__ bool ray_step(ray_state &s, const node8 *__restrict__
     while(s.sp > 0 && !s.done)
     {
         --s.sp;
-        const uint32_t ni = s.st_node[s.sp];
-        if(s.st_t[s.sp] > s.best_t) continue;
+        const uint2 ent = s.st[s.sp];
+        const uint32_t ni = ent.x;
+        if(__uint_as_float(ent.y) > s.best_t) continue;
         if(STATS) ++visits;
         uint32_t key[8];
         uint4 w4, w5;
@@ -220,8 +219,7 @@ __device__ __forceinline__ bool ray_step(ray_state &s, const node8 *__restrict__
             if(c & LEAF_BIT) continue;
             if(s.sp < (int)TRAVERSAL_STACK)
             {
-                s.st_node[s.sp] = c;
-                s.st_t[s.sp] = tdec(key[h] & ~7u);
+                s.st[s.sp] = make_uint2(c, __float_as_uint(tdec(key[h] & ~7u)));
                 ++s.sp;
             }
             else if(counters) { atomicOr(&counters[2], 1ull); }
