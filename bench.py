@@ -405,6 +405,7 @@ def batched_block(ctx):
             "samples_per_s": round(st.paths / best * 1e3), "waves": int(st.waves),
             "tuning": {"extend_kernel": "persistent" if tun.extend_kernel == 2 else "grid-stride",
                        "ctas_per_sm": int(tun.ctas_per_sm), "wave_paths": int(tun.wave_paths),
+                       "block_size": int(tun.block_size), "stack_depth": int(tun.stack_depth),
                        "autotune_s": round(tune_s, 2), "graph": True},
             "one_scene_at_a_time_ms": round(seq_ms, 2), "speedup_vs_one_at_a_time": round(seq_ms / best, 3)}
 

@@ -439,6 +439,8 @@ typedef struct vkg_batch_tuning
     uint32_t ctas_per_sm;     /* grid of the grid-stride queue kernels = SMs x this */
     uint32_t wave_paths;      /* paths in flight per wave */
     uint32_t use_graph;       /* 1: capture a render as a CUDA graph and replay it */
+    uint32_t block_size;      /* threads per block of the queue kernels: 64 or 128 */
+    uint32_t stack_depth;     /* traversal stack entries: 64 (used when every BVH is at most 10 deep) or 128 */
 } vkg_batch_tuning;
 typedef struct vkg_batch_stats
 {

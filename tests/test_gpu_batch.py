@@ -49,11 +49,12 @@ def single(ctx, job, renders):
     return img
 
 
-@pytest.mark.parametrize("extend,cps,wave,graph", [(1, 16, 8 << 20, 1), (2, 8, 20_000, 1), (1, 4, 5_000, 0),
-                                                   (2, 16, 1024, 0)])
-def test_batch_equals_single_scene_tracer(ctx, jobs, extend, cps, wave, graph):
+@pytest.mark.parametrize("extend,cps,wave,graph,bs,stack", [(1, 16, 8 << 20, 1, 128, 128), (2, 8, 20_000, 1, 64, 64),
+                                                             (1, 4, 5_000, 0, 64, 128), (2, 16, 1024, 0, 128, 64)])
+def test_batch_equals_single_scene_tracer(ctx, jobs, extend, cps, wave, graph, bs, stack):
     t = BatchRenderer.default_tuning()
     t.extend_kernel, t.ctas_per_sm, t.wave_paths, t.use_graph = extend, cps, wave, graph
+    t.block_size, t.stack_depth = bs, stack
     br = BatchRenderer(ctx, jobs, t)
     for r in (1, 2):
         imgs = [i.clone() for i in br.render()]
@@ -72,7 +73,8 @@ def test_batch_equals_single_scene_tracer(ctx, jobs, extend, cps, wave, graph):
 def test_autotune_keeps_images(ctx, jobs):
     br = BatchRenderer(ctx, jobs)
     t = br.autotune()
-    assert t.extend_kernel in (1, 2) and t.ctas_per_sm in (4, 8, 16) and t.wave_paths in (4 << 20, 8 << 20, 16 << 20)
+    assert t.extend_kernel in (1, 2) and t.ctas_per_sm in (8, 16) and t.wave_paths in (8 << 20, 16 << 20)
+    assert t.block_size in (64, 128) and t.stack_depth in (64, 128)
     assert br.statistics().batch == 0
     imgs = [i.clone() for i in br.render()]
     for k, job in enumerate(jobs):

@@ -90,7 +90,7 @@ class vkg_batch_job(C.Structure):
 
 class vkg_batch_tuning(C.Structure):
     _fields_ = [("extend_kernel", C.c_uint32), ("ctas_per_sm", C.c_uint32), ("wave_paths", C.c_uint32),
-                ("use_graph", C.c_uint32)]
+                ("use_graph", C.c_uint32), ("block_size", C.c_uint32), ("stack_depth", C.c_uint32)]
 
 
 class vkg_batch_stats(C.Structure):

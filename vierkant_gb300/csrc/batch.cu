@@ -16,8 +16,9 @@
 //
 // The render is recorded once into a CUDA graph (the batch index lives in device memory, so the
 // same graph serves every render) and replayed. The autotuner times the candidate tunings
-// (grid-stride vs persistent work-stealing queue tracers, grid size, wave size) on a one-sample
-// render and keeps the fastest; tunings change timing only, never the images.
+// (grid-stride vs persistent work-stealing queue tracers, grid size, wave size, block size, traversal
+// stack depth) on a one-sample render and keeps the fastest; tunings change timing only, never the
+// images.
 #include "pt_kernels.cuh"
 
 #include <algorithm>
@@ -143,6 +144,7 @@ struct vkg_batch
     std::vector<batch_job_dev> jdev;
     uint32_t njobs = 0, total_pix = 0, max_depth = 0;
     bool any_instanced = false;
+    uint32_t max_bvh_depth = 0;
     uint64_t total_paths = 0;
     vkg_batch_tuning tuning{};
     pt_params *d_params = nullptr;
@@ -294,18 +296,20 @@ vkg_status enqueue(vkg_batch *b, const std::vector<vkg_batch::wave> &waves, cuda
     vkg_ctx *ctx = b->ctx;
     vkg_batch_tuning T = b->tuning;
     if(b->any_instanced) T.extend_kernel = 1; // the persistent tracers handle single-level scenes only
+    // a 64-entry stack serves BVHs of depth <= 10 (7 (depth - 1) + 1 entries at most)
+    if(b->max_bvh_depth > 10) T.stack_depth = 128;
     const job_table J{b->d_params, b->pjob, b->pinc};
     VKG_TRY_CUDA(ctx, cudaMemsetAsync(b->sum, 0, (size_t)b->total_pix * 3 * sizeof(float), st));
     cache_io io{};
+    const uint32_t bs = T.block_size;
     for(const auto &w: waves)
     {
         const batch_chunk *ch = b->d_chunks + w.chunk_off;
         const uint32_t n = w.paths;
-        const uint32_t grid = (uint32_t)std::min<size_t>((n + PT_THREADS - 1) / PT_THREADS,
+        const uint32_t grid = (uint32_t)std::min<size_t>((n + bs - 1) / bs,
                                                          (size_t)ctx->num_sms * std::max(1u, T.ctas_per_sm));
-        k_batch_generate<<<grid, PT_THREADS, 0, st>>>(b->d_params, ch, w.nchunks, n, b->d_batch, b->q_ray[0],
-                                                      b->q_pid[0], b->rng, b->pinc, b->pjob, b->beta_pdf, b->radiance,
-                                                      b->counters);
+        k_batch_generate<<<grid, bs, 0, st>>>(b->d_params, ch, w.nchunks, n, b->d_batch, b->q_ray[0], b->q_pid[0], b->rng,
+                                             b->pinc, b->pjob, b->beta_pdf, b->radiance, b->counters);
         int a = 0;
         for(uint32_t depth = 0; depth < w.depths; ++depth)
         {
@@ -313,26 +317,36 @@ vkg_status enqueue(vkg_batch *b, const std::vector<vkg_batch::wave> &waves, cuda
             if(T.extend_kernel == 2)
             {
                 VKG_TRY_CUDA(ctx, cudaMemsetAsync(b->counters + 3, 0, sizeof(uint32_t), st));
-                k_pt_trace_persistent<false><<<grid, PT_THREADS, 0, st>>>(J, b->q_ray[a], b->q_pid[a], cnt_in, b->hits,
-                                                                         b->hit_inst, nullptr, nullptr, b->counters + 3);
+                if(T.stack_depth == 64)
+                    k_pt_trace_persistent<false, job_table, 64><<<grid, bs, 0, st>>>(
+                            J, b->q_ray[a], b->q_pid[a], cnt_in, b->hits, b->hit_inst, nullptr, nullptr, b->counters + 3);
+                else
+                    k_pt_trace_persistent<false, job_table><<<grid, bs, 0, st>>>(
+                            J, b->q_ray[a], b->q_pid[a], cnt_in, b->hits, b->hit_inst, nullptr, nullptr, b->counters + 3);
             }
+            else if(T.stack_depth == 64)
+                k_pt_extend<job_table, 64><<<grid, bs, 0, st>>>(J, b->q_ray[a], b->q_pid[a], cnt_in, b->hits, b->hit_inst);
             else
-                k_pt_extend<<<grid, PT_THREADS, 0, st>>>(J, b->q_ray[a], b->q_pid[a], cnt_in, b->hits, b->hit_inst);
+                k_pt_extend<<<grid, bs, 0, st>>>(J, b->q_ray[a], b->q_pid[a], cnt_in, b->hits, b->hit_inst);
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_out, 0, sizeof(uint32_t), st));
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_s, 0, sizeof(uint32_t), st));
-            k_pt_shade<MODE_PLAIN><<<grid, PT_THREADS, 0, st>>>(J, depth, b->q_ray[a], b->q_pid[a], b->hits, b->hit_inst,
-                                                                cnt_in,
-                                                                b->q_ray[1 - a], b->q_pid[1 - a], cnt_out, b->s_ray,
-                                                                b->s_pid, b->s_contrib, cnt_s, b->rng, b->beta_pdf,
-                                                                b->radiance, io);
+            k_pt_shade<MODE_PLAIN><<<grid, bs, 0, st>>>(J, depth, b->q_ray[a], b->q_pid[a], b->hits, b->hit_inst, cnt_in,
+                                                       b->q_ray[1 - a], b->q_pid[1 - a], cnt_out, b->s_ray, b->s_pid,
+                                                       b->s_contrib, cnt_s, b->rng, b->beta_pdf, b->radiance, io);
             if(T.extend_kernel == 2)
             {
                 VKG_TRY_CUDA(ctx, cudaMemsetAsync(b->counters + 3, 0, sizeof(uint32_t), st));
-                k_pt_trace_persistent<true><<<grid, PT_THREADS, 0, st>>>(J, b->s_ray, b->s_pid, cnt_s, nullptr, nullptr,
-                                                                        b->s_contrib, b->radiance, b->counters + 3);
+                if(T.stack_depth == 64)
+                    k_pt_trace_persistent<true, job_table, 64><<<grid, bs, 0, st>>>(
+                            J, b->s_ray, b->s_pid, cnt_s, nullptr, nullptr, b->s_contrib, b->radiance, b->counters + 3);
+                else
+                    k_pt_trace_persistent<true, job_table><<<grid, bs, 0, st>>>(
+                            J, b->s_ray, b->s_pid, cnt_s, nullptr, nullptr, b->s_contrib, b->radiance, b->counters + 3);
             }
+            else if(T.stack_depth == 64)
+                k_pt_shadow<job_table, 64><<<grid, bs, 0, st>>>(J, b->s_ray, b->s_pid, b->s_contrib, cnt_s, b->radiance);
             else
-                k_pt_shadow<<<grid, PT_THREADS, 0, st>>>(J, b->s_ray, b->s_pid, b->s_contrib, cnt_s, b->radiance);
+                k_pt_shadow<<<grid, bs, 0, st>>>(J, b->s_ray, b->s_pid, b->s_contrib, cnt_s, b->radiance);
             k_pt_tally<<<1, 1, 0, st>>>(cnt_in, cnt_s, b->totals);
             a = 1 - a;
         }
@@ -398,6 +412,8 @@ vkg_status vkg_batch_tuning_default(vkg_batch_tuning *out)
     out->ctas_per_sm = 16;
     out->wave_paths = 8u << 20;
     out->use_graph = 1;
+    out->block_size = 128;
+    out->stack_depth = 128;
     return VKG_OK;
 }
 
@@ -409,6 +425,10 @@ static vkg_status check_tuning(vkg_ctx *ctx, const vkg_batch_tuning *t)
         return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "batch tuning: ctas_per_sm must be 1..64");
     if(t->wave_paths < 1024 || t->wave_paths > (1u << 30))
         return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "batch tuning: wave_paths must be 1024..2^30");
+    if(t->block_size != 64 && t->block_size != 128)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "batch tuning: block_size must be 64 or 128");
+    if(t->stack_depth != 64 && t->stack_depth != 128)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "batch tuning: stack_depth must be 64 or 128");
     return VKG_OK;
 }
 
@@ -448,6 +468,7 @@ vkg_status vkg_batch_create(vkg_ctx *ctx, const vkg_batch_job *jobs, uint32_t nj
         const vkg_batch_job &jb = jobs[j];
         b->params.push_back(make_params(jb.scene, jb.camera, jb.settings, jb.seed, 0));
         b->any_instanced = b->any_instanced || jb.scene->tlas != nullptr;
+        if(jb.scene->bvh) b->max_bvh_depth = std::max(b->max_bvh_depth, jb.scene->bvh->depth);
         const uint32_t npix = b->params.back().npix;
         b->jdev.push_back(batch_job_dev{npix, jb.settings.num_samples, off, jb.d_rgb_out});
         off += npix;
@@ -513,29 +534,33 @@ vkg_status vkg_batch_autotune(vkg_batch *b, void *stream, vkg_batch_tuning *chos
     float best_ms = 3.4e38f;
     std::vector<vkg_batch::wave> waves;
     std::vector<batch_chunk> chunks;
+    const bool small_stack = b->max_bvh_depth <= 10;
     for(uint32_t ek: {1u, 2u})
-        for(uint32_t cps: {4u, 8u, 16u})
-            for(uint32_t wp: {4u << 20, 8u << 20, 16u << 20})
-            {
-                b->tuning = vkg_batch_tuning{ek, cps, wp, 0};
-                plan(b, 1, waves, chunks);
-                drop_graph(b);
-                if(vkg_status s = ensure_waves(b, waves, chunks); s != VKG_OK) return s;
-                float ms = 0.f;
-                for(int rep = 0; rep < 2; ++rep) // the first run warms caches and the instruction cache
-                {
-                    VKG_TRY_CUDA(ctx, cudaEventRecord(b->ev0, st));
-                    if(vkg_status s = enqueue(b, waves, st); s != VKG_OK) return s;
-                    VKG_TRY_CUDA(ctx, cudaEventRecord(b->ev1, st));
-                    VKG_TRY_CUDA(ctx, cudaEventSynchronize(b->ev1));
-                    VKG_TRY_CUDA(ctx, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
-                }
-                if(ms < best_ms)
-                {
-                    best_ms = ms;
-                    best = b->tuning;
-                }
-            }
+        for(uint32_t cps: {8u, 16u})
+            for(uint32_t wp: {8u << 20, 16u << 20})
+                for(uint32_t bs: {64u, 128u})
+                    for(uint32_t sd: {64u, 128u})
+                    {
+                        if(sd == 64 && !small_stack) continue;
+                        b->tuning = vkg_batch_tuning{ek, cps, wp, 0, bs, sd};
+                        plan(b, 1, waves, chunks);
+                        drop_graph(b);
+                        if(vkg_status s = ensure_waves(b, waves, chunks); s != VKG_OK) return s;
+                        float ms = 0.f;
+                        for(int rep = 0; rep < 2; ++rep) // the first run warms the caches
+                        {
+                            VKG_TRY_CUDA(ctx, cudaEventRecord(b->ev0, st));
+                            if(vkg_status s = enqueue(b, waves, st); s != VKG_OK) return s;
+                            VKG_TRY_CUDA(ctx, cudaEventRecord(b->ev1, st));
+                            VKG_TRY_CUDA(ctx, cudaEventSynchronize(b->ev1));
+                            VKG_TRY_CUDA(ctx, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+                        }
+                        if(ms < best_ms)
+                        {
+                            best_ms = ms;
+                            best = b->tuning;
+                        }
+                    }
     best.use_graph = keep.use_graph;
     b->tuning = best;
     if(chosen) *chosen = best;

@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(PT_THREADS)
     if(blockIdx.x == 0 && threadIdx.x == 0) counters[0] = n;
 }
 
-template<class J>
+template<class J, int STACK = (int)TRAVERSAL_STACK>
 __global__ void __launch_bounds__(PT_THREADS)
         k_pt_extend(J S, const vkg_ray *__restrict__ q_ray, const uint32_t *__restrict__ q_pid,
                     const uint32_t *__restrict__ count, vkg_hit *__restrict__ hits, uint32_t *__restrict__ hit_inst)
@@ -201,8 +201,8 @@ __global__ void __launch_bounds__(PT_THREADS)
             continue;
         }
         unsigned long long v = 0, t = 0;
-        trace_result r = trace_ray<false, false>(P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w,
-                                                 CULL_BACK_UNLESS_TWOSIDED, v, t, nullptr);
+        trace_result r = trace_ray<false, false, STACK>(P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z,
+                                                        r1.w, CULL_BACK_UNLESS_TWOSIDED, v, t, nullptr);
         reinterpret_cast<uint4 *>(hits)[i] =
                 make_uint4(r.prim, __float_as_uint(r.t), __float_as_uint(r.u), __float_as_uint(r.v));
     }
@@ -442,7 +442,7 @@ __global__ void __launch_bounds__(PT_THREADS)
     }
 }
 
-template<class J>
+template<class J, int STACK = (int)TRAVERSAL_STACK>
 __global__ void __launch_bounds__(PT_THREADS)
         k_pt_shadow(J S, const vkg_ray *__restrict__ s_ray, const uint32_t *__restrict__ s_pid,
                     const float4 *__restrict__ s_contrib, const uint32_t *__restrict__ count,
@@ -463,8 +463,8 @@ __global__ void __launch_bounds__(PT_THREADS)
         else
         {
             unsigned long long v = 0, t = 0;
-            occluded = trace_ray<true, false>(P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, CULL_NONE,
-                                              v, t, nullptr)
+            occluded = trace_ray<true, false, STACK>(P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w,
+                                                     CULL_NONE, v, t, nullptr)
                                .occluded;
         }
         if(!occluded)
@@ -485,7 +485,7 @@ __global__ void __launch_bounds__(PT_THREADS)
 // visibility of NEE rays, adding the contribution of unoccluded ones; else closest hit of extension
 // rays. Single-level scenes only (instanced scenes use k_pt_tl_persistent or the grid-stride
 // kernels). `work` must be zero at launch.
-template<bool SHADOW, class J>
+template<bool SHADOW, class J, int STACK = (int)TRAVERSAL_STACK>
 __global__ void __launch_bounds__(PT_THREADS)
         k_pt_trace_persistent(J S, const vkg_ray *__restrict__ q_ray, const uint32_t *__restrict__ q_pid,
                               const uint32_t *__restrict__ count, vkg_hit *__restrict__ hits,
@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(PT_THREADS)
     const uint32_t n = *count;
     const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
     unsigned long long v = 0, t = 0;
-    ray_state s;
+    ray_state_t<STACK> s;
     const node8 *nodes = nullptr;
     const tri_rec *tris = nullptr;
     uint32_t cur = 0xFFFFFFFFu;

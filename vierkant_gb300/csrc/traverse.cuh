@@ -77,17 +77,20 @@ __device__ __forceinline__ float qbyte(uint32_t w, int k) { return (float)((w >>
 
 
 // per-ray traversal state (the stack lives in local memory; only its used top is touched)
-struct ray_state
+template<int STACK = (int)TRAVERSAL_STACK>
+struct ray_state_t
 {
     float ox, oy, oz, tmin, dx, dy, dz, tmax, ix, iy, iz;
     float best_t, bu, bv;
     uint32_t best;
     int sp;
     bool done;
-    uint2 st[TRAVERSAL_STACK]; // {node, entry distance (float bits)}: one 64-bit access per push / pop
+    uint2 st[STACK]; // {node, entry distance (float bits)}: one 64-bit access per push / pop
 };
+using ray_state = ray_state_t<>;
 
-__device__ __forceinline__ void ray_init(ray_state &s, float ox, float oy, float oz, float tmin, float dx, float dy,
+template<int STACK>
+__device__ __forceinline__ void ray_init(ray_state_t<STACK> &s, float ox, float oy, float oz, float tmin, float dx, float dy,
                                          float dz, float tmax)
 {
     s.ox = ox;
@@ -157,8 +160,8 @@ __device__ __forceinline__ void node_keys(const node8 *__restrict__ nodes, uint3
 }
 
 // one node of the traversal; returns false once the ray is finished
-template<bool ANY, bool STATS>
-__device__ __forceinline__ bool ray_step(ray_state &s, const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
+template<bool ANY, bool STATS, int STACK>
+__device__ __forceinline__ bool ray_step(ray_state_t<STACK> &s, const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
                                          int cull, unsigned long long &visits, unsigned long long &tests,
                                          unsigned long long *__restrict__ counters)
 {
@@ -217,7 +220,7 @@ __device__ __forceinline__ bool ray_step(ray_state &s, const node8 *__restrict__
             const uint32_t k = key[h] & 7u;
             const uint32_t c = (k & 4u) ? sel4(w5, k & 3u) : sel4(w4, k & 3u);
             if(c & LEAF_BIT) continue;
-            if(s.sp < (int)TRAVERSAL_STACK)
+            if(s.sp < STACK)
             {
                 s.st[s.sp] = make_uint2(c, __float_as_uint(tdec(key[h] & ~7u)));
                 ++s.sp;
@@ -229,7 +232,8 @@ __device__ __forceinline__ bool ray_step(ray_state &s, const node8 *__restrict__
     return false;
 }
 
-__device__ __forceinline__ trace_result ray_result(const ray_state &s)
+template<int STACK>
+__device__ __forceinline__ trace_result ray_result(const ray_state_t<STACK> &s)
 {
     trace_result r;
     r.occluded = s.done;
@@ -240,14 +244,14 @@ __device__ __forceinline__ trace_result ray_result(const ray_state &s)
     return r;
 }
 
-template<bool ANY, bool STATS>
+template<bool ANY, bool STATS, int STACK = (int)TRAVERSAL_STACK>
 __device__ __forceinline__ trace_result trace_ray(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
                                                   float ox, float oy, float oz, float tmin, float dx, float dy,
                                                   float dz, float tmax, int cull,
                                                   unsigned long long &visits, unsigned long long &tests,
                                                   unsigned long long *__restrict__ counters)
 {
-    ray_state s;
+    ray_state_t<STACK> s;
     ray_init(s, ox, oy, oz, tmin, dx, dy, dz, tmax);
     while(ray_step<ANY, STATS>(s, nodes, tris, cull, visits, tests, counters)) {}
     return ray_result(s);
