@@ -547,6 +547,8 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
     // instanced scenes: grid-stride two-level tracers (faster on the stress scene: 274 vs 252 Mrays/s);
     // VKG_TL_KERNEL=persistent selects the refilling persistent ones
     const bool tl_persistent = sc->tlas && tl_persistent_selected();
+    // a 64-entry traversal stack serves BVHs up to 10 levels deep (7 (depth - 1) + 1 entries)
+    const bool small_stack = sc->bvh && sc->bvh->depth <= 10;
     uint32_t tl_grid = 0;
     if(tl_persistent)
     {
@@ -587,6 +589,9 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
                 k_pt_tl_persistent<false><<<tl_grid, PT_THREADS, 0, st>>>(SS, t->q_ray[a], t->q_pid[a], cnt_in, t->hits,
                                                                          t->hit_inst, nullptr, nullptr, cnt_work);
             }
+            else if(small_stack)
+                k_pt_extend<single_scene, 64><<<grid, PT_THREADS, 0, st>>>(SS, t->q_ray[a], t->q_pid[a], cnt_in, t->hits,
+                                                                            t->hit_inst);
             else
                 k_pt_extend<<<grid, PT_THREADS, 0, st>>>(SS, t->q_ray[a], t->q_pid[a], cnt_in, t->hits, t->hit_inst);
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_out, 0, sizeof(uint32_t), st));
@@ -605,6 +610,9 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
                 k_pt_tl_persistent<true><<<tl_grid, PT_THREADS, 0, st>>>(SS, t->s_ray, t->s_pid, cnt_s, nullptr, nullptr,
                                                                         t->s_contrib, t->radiance, cnt_work);
             }
+            else if(!empty && small_stack)
+                k_pt_shadow<single_scene, 64><<<grid, PT_THREADS, 0, st>>>(SS, t->s_ray, t->s_pid, t->s_contrib, cnt_s,
+                                                                            t->radiance);
             else if(!empty)
                 k_pt_shadow<<<grid, PT_THREADS, 0, st>>>(SS, t->s_ray, t->s_pid, t->s_contrib, cnt_s,
                                                          t->radiance);

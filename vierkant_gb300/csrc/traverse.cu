@@ -18,7 +18,8 @@ namespace
 
 constexpr int TRACE_THREADS = 128;
 
-template<bool ANY, bool STATS>
+// STACK: traversal stack entries; 64 serve BVHs up to 10 levels deep (7 (depth - 1) + 1 entries)
+template<bool ANY, bool STATS, int STACK>
 __global__ void __launch_bounds__(TRACE_THREADS)
         k_trace(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris, const vkg_ray *__restrict__ rays,
                 uint32_t n, vkg_hit *__restrict__ hits, uint32_t *__restrict__ occluded, int cull,
@@ -30,8 +31,8 @@ __global__ void __launch_bounds__(TRACE_THREADS)
     {
         const float4 *rp = reinterpret_cast<const float4 *>(rays + i);
         const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
-        trace_result r = trace_ray<ANY, STATS>(nodes, tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, cull,
-                                               visits, tests, counters);
+        trace_result r = trace_ray<ANY, STATS, STACK>(nodes, tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w,
+                                                      cull, visits, tests, counters);
         if(ANY) { occluded[i] = r.occluded ? 1u : 0u; }
         else
         {
@@ -152,6 +153,18 @@ bool use_persistent()
     return v == 1;
 }
 
+template<bool ANY, bool STATS>
+void launch_simple(bool small_stack, uint32_t grid, cudaStream_t st, const vkg_bvh *bvh, const vkg_ray *rays,
+                   uint32_t n, vkg_hit *hits, uint32_t *occ, int cull, unsigned long long *counters)
+{
+    if(small_stack)
+        k_trace<ANY, STATS, 64><<<grid, TRACE_THREADS, 0, st>>>(bvh->d_nodes, bvh->d_tris, rays, n, hits, occ, cull,
+                                                                counters);
+    else
+        k_trace<ANY, STATS, (int)TRAVERSAL_STACK><<<grid, TRACE_THREADS, 0, st>>>(bvh->d_nodes, bvh->d_tris, rays, n,
+                                                                                   hits, occ, cull, counters);
+}
+
 __global__ void k_fill_miss(vkg_hit *hits, uint32_t *occluded, uint32_t n)
 {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -185,23 +198,16 @@ vkg_status launch_trace(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays,
         }
         return cuda_check(ctx, cudaGetLastError(), "k_trace_persistent");
     }
+    const bool small = bvh->depth <= 10;
     if(d_occ)
     {
-        if(stats)
-            k_trace<true, true><<<grid, TRACE_THREADS, 0, st>>>(bvh->d_nodes, bvh->d_tris, d_rays, n, nullptr, d_occ,
-                                                                cull, ctx->d_counters);
-        else
-            k_trace<true, false><<<grid, TRACE_THREADS, 0, st>>>(bvh->d_nodes, bvh->d_tris, d_rays, n, nullptr, d_occ,
-                                                                 cull, ctx->d_counters);
+        if(stats) launch_simple<true, true>(small, grid, st, bvh, d_rays, n, nullptr, d_occ, cull, ctx->d_counters);
+        else launch_simple<true, false>(small, grid, st, bvh, d_rays, n, nullptr, d_occ, cull, ctx->d_counters);
     }
     else
     {
-        if(stats)
-            k_trace<false, true><<<grid, TRACE_THREADS, 0, st>>>(bvh->d_nodes, bvh->d_tris, d_rays, n, d_hits,
-                                                                 nullptr, cull, ctx->d_counters);
-        else
-            k_trace<false, false><<<grid, TRACE_THREADS, 0, st>>>(bvh->d_nodes, bvh->d_tris, d_rays, n, d_hits,
-                                                                  nullptr, cull, ctx->d_counters);
+        if(stats) launch_simple<false, true>(small, grid, st, bvh, d_rays, n, d_hits, nullptr, cull, ctx->d_counters);
+        else launch_simple<false, false>(small, grid, st, bvh, d_rays, n, d_hits, nullptr, cull, ctx->d_counters);
     }
     return cuda_check(ctx, cudaGetLastError(), "k_trace");
 }
