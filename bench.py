@@ -435,20 +435,53 @@ def stress_block(ctx):
     pt.render_scene(scene, cam)
     best = None
     for _ in range(2):
-        pt.render_scene(scene, cam)
+        pt.reset_accumulator()
+        img = pt.render_scene(scene, cam)
         stt = pt.statistics()
         if best is None or stt.total_ms < best.total_ms:
             best = stt
     pt.close()
     tris = sum(len(m[1]) for m in st["meshes"])
     inst_tris = sum(len(st["meshes"][int(b)][1]) for b in st["instances"]["blas"])
-    scene.close()
     rays = best.extension_rays + best.shadow_rays
-    return {"terrain_triangles": len(st["meshes"][0][1]), "instances": len(st["instances"]) - 1,
-            "mesh_triangles": tris, "instanced_triangles": int(inst_tris), "resolution": [W, H], "spp": 16,
-            "segments": 8, "render_ms": round(best.total_ms, 1), "samples_per_s": round(best.paths / best.total_ms * 1e3),
-            "mrays_per_s": round(rays / best.total_ms / 1e3, 1), "rays": int(rays),
-            "generate_s": round(gen_s, 2), "scene_build_s": round(build_s, 2)}
+    out = {"terrain_triangles": len(st["meshes"][0][1]), "instances": len(st["instances"]) - 1,
+           "mesh_triangles": tris, "instanced_triangles": int(inst_tris), "resolution": [W, H], "spp": 16,
+           "segments": 8, "render_ms": round(best.total_ms, 1), "samples_per_s": round(best.paths / best.total_ms * 1e3),
+           "mrays_per_s": round(rays / best.total_ms / 1e3, 1), "rays": int(rays),
+           "generate_s": round(gen_s, 2), "scene_build_s": round(build_s, 2)}
+    fixture = ROOT / "tests" / "golden" / "pt_oracle_stress_crop.npz"
+    if fixture.exists():
+        # the plain tracer's 16-spp image and the radiance-cache tracer (1 spp per frame) against the FP64
+        # oracle crop: GPU time for the cache tracer to reach the plain tracer's RMSE
+        import numpy as np
+        g = np.load(fixture)
+        target, pbias = _crop_error(img.cpu().numpy(), g)
+        from vierkant_gb300.nrc import cache_for_scene
+        s1 = PBRPathTracer.default_settings()
+        s1.resolution[0], s1.resolution[1] = W, H
+        s1.num_samples, s1.max_trace_depth, s1.rr_start_depth = 1, 8, 3
+        ptc = PBRPathTracer(ctx, seed=SEED + 1, settings=s1)
+        cache = cache_for_scene(ctx, scene)
+        ptc.attach_cache(cache)
+        tot, reached, rmse, bias = 0.0, None, None, None
+        frames = 48
+        for f in range(frames):
+            im = ptc.render_scene(scene, cam)
+            tot += ptc.statistics().total_ms
+            rmse, bias = _crop_error(im.cpu().numpy(), g)
+            if reached is None and rmse <= target:
+                reached = {"frames": f + 1, "ms": round(tot, 1)}
+                break
+        ptc.close()
+        cache.close()
+        out["equal_rmse"] = {"oracle": "FP64 %d spp, 128x128 crop at (1856, 1016)" % int(g["spp"]),
+                             "plain_16spp_rmse": round(target, 4), "plain_bias": round(pbias, 5),
+                             "plain_16spp_ms": round(best.total_ms, 1), "nrc_reached": reached,
+                             "nrc_vs_plain_time": round(reached["ms"] / best.total_ms, 3) if reached else None,
+                             "nrc_frames_run": f + 1, "nrc_ms_total": round(tot, 1),
+                             "nrc_rmse_last": round(rmse, 4), "nrc_bias_last": round(bias, 5)}
+    scene.close()
+    return out
 
 
 def profile_case(name: str):

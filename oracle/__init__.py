@@ -325,3 +325,54 @@ def pt_render(fp64, xyz, idx, tri_mat, mats, bvh: "CpuBVH", env_rgb, cam, spp, *
     L.orc_pt_render(int(fp64), C.byref(scene), C.byref(bvh.b), C.byref(env), C.byref(cam), C.byref(st), ptr(out),
                     ptr(sq), ptr(stats), nthreads)
     return out, sq, (int(stats[0]), int(stats[1]))
+
+
+class orc_pt_instances(C.Structure):
+    _fields_ = [("mesh_bvh", C.c_void_p), ("mesh_xyz", C.c_void_p), ("mesh_idx", C.c_void_p),
+                ("mesh_nvert", C.c_void_p), ("mesh_twosided", C.c_void_p), ("num_meshes", C.c_uint32),
+                ("o2w", C.c_void_p), ("inst_mesh", C.c_void_p), ("inst_mat", C.c_void_p),
+                ("num_instances", C.c_uint32)]
+
+
+def pt_render_instanced(meshes, o2w, inst_mesh, inst_mat, mats, env_rgb, cam, spp, *, seed=0x5EED, batch=0,
+                        max_depth=6, rr_depth=3, mis_mode=0, crop=(0, 0, 0, 0), environment=1.0, draw_skybox=1,
+                        nthreads=0, mesh_bvhs=None):
+    """FP64 oracle of an instanced scene: meshes [(xyz, idx, twosided)], o2w [N, 12] object -> world,
+    mesh and material index per instance. Returns (mean radiance [h, w, 3], mean squared luminance,
+    (ext, shadow) rays)."""
+    L = orc()
+    L.orc_pt_render_instanced.argtypes = [C.POINTER(orc_pt_scene), C.POINTER(orc_pt_instances),
+                                          C.POINTER(orc_pt_env), C.POINTER(orc_camera),
+                                          C.POINTER(orc_pt_settings), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+    keep = []
+    bvhs = mesh_bvhs if mesh_bvhs is not None else [CpuBVH(x, i, 4) for x, i, _ in meshes]
+    xyzs = [np.ascontiguousarray(x, np.float32) for x, _, _ in meshes]
+    idxs = [np.ascontiguousarray(i, np.uint32) for _, i, _ in meshes]
+    keep += xyzs + idxs
+    bvh_arr = (C.POINTER(orc_bvh) * len(meshes))(*[C.pointer(b.b) for b in bvhs])
+    xyz_arr = (C.c_void_p * len(meshes))(*[x.ctypes.data for x in xyzs])
+    idx_arr = (C.c_void_p * len(meshes))(*[i.ctypes.data for i in idxs])
+    nvert = np.array([len(x) for x in xyzs], np.uint32)
+    twos = np.array([int(t) for _, _, t in meshes], np.uint8)
+    o2w = np.ascontiguousarray(o2w, np.float32)
+    im = np.ascontiguousarray(inst_mesh, np.uint32)
+    imat = np.ascontiguousarray(inst_mat, np.uint32)
+    mats = np.ascontiguousarray(mats)
+    keep += [nvert, twos, o2w, im, imat, mats]
+    inst = orc_pt_instances(C.cast(bvh_arr, C.c_void_p), C.cast(xyz_arr, C.c_void_p), C.cast(idx_arr, C.c_void_p),
+                            ptr(nvert), ptr(twos), len(meshes), ptr(o2w), ptr(im), ptr(imat), len(im))
+    scene = orc_pt_scene(None, None, None, ptr(mats), 0, len(mats))
+    rgb = np.ascontiguousarray(env_rgb, np.float32)
+    h, w = rgb.shape[:2]
+    weight, cdf = env_tables_fp64(rgb)
+    env = orc_pt_env(ptr(rgb), ptr(np.ascontiguousarray(weight, np.float32)), None, None, ptr(cdf), w, h)
+    cw = crop[2] or cam.width
+    ch = crop[3] or cam.height
+    st = orc_pt_settings(seed, batch, spp, max_depth, rr_depth, mis_mode, 0, draw_skybox, 0.0, environment,
+                         (C.c_uint32 * 4)(*crop))
+    out = np.zeros((ch, cw, 3), np.float64)
+    sq = np.zeros((ch, cw), np.float64)
+    stats = np.zeros(2, np.uint64)
+    L.orc_pt_render_instanced(C.byref(scene), C.byref(inst), C.byref(env), C.byref(cam), C.byref(st), ptr(out),
+                              ptr(sq), ptr(stats), nthreads)
+    return out, sq, (int(stats[0]), int(stats[1]))

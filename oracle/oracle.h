@@ -150,11 +150,29 @@ typedef struct {
     uint32_t crop[4]; /* x0, y0, w, h (pixels of the full resolution camera) */
 } orc_pt_settings;
 
+/* an instanced scene for the FP64 oracle: meshes (each with the oracle's BVH) and instances with an
+   object -> world 3x4 transform, a mesh and a material index into the scene's materials */
+typedef struct {
+    const orc_bvh *const *mesh_bvh;
+    const float *const *mesh_xyz;
+    const uint32_t *const *mesh_idx;
+    const uint32_t *mesh_nvert;
+    const uint8_t *mesh_twosided;
+    uint32_t num_meshes;
+    const float *o2w;        /* [num_instances][12] */
+    const uint32_t *inst_mesh, *inst_mat;
+    uint32_t num_instances;
+} orc_pt_instances;
+
 /* mean radiance per crop pixel over spp paths (out: crop_w*crop_h*3 doubles); stats[0] extension
    rays, stats[1] shadow rays (may be NULL); sq: per-pixel mean of the squared luminance (may be NULL) */
 int orc_pt_render(int fp64, const orc_pt_scene *scene, const orc_bvh *bvh, const orc_pt_env *env,
                   const orc_camera *cam, const orc_pt_settings *set, double *out, double *sq, uint64_t *stats,
                   int nthreads);
+/* the same for an instanced scene (FP64 oracle only; scene supplies the materials) */
+int orc_pt_render_instanced(const orc_pt_scene *scene, const orc_pt_instances *inst, const orc_pt_env *env,
+                            const orc_camera *cam, const orc_pt_settings *set, double *out, double *sq,
+                            uint64_t *stats, int nthreads);
 /* FP64 env tables from an rgb map: weights (mean 1, as float) and the CDF (w*h+1 doubles) */
 void orc_pt_env_tables(const float *rgb, uint32_t w, uint32_t h, float *weight, double *cdf);
 /* procedural sky in double precision (environment_white + sun lobe), rounded to float */

@@ -33,6 +33,8 @@ typedef struct {
     float max_path_beta, environment;
     uint32_t cx0, cy0, cw, ch;
     double *out, *sq;
+    const orc_pt_instances *inst; /* NULL: single-level scene */
+    const void *ibvh;             /* instance BVH of an instanced scene */
     atomic_uint next;
     atomic_ullong ext, shadow;
     int fp64;
@@ -42,8 +44,9 @@ typedef struct {
 static inline float f_draw_raw(orc_pcg32 *g) { return orc_u01(orc_pcg32_next(g)); }
 
 static void f_hit_raw(const orc_pt_job *J, float ox, float oy, float oz, float tmin, float dx, float dy, float dz,
-                      uint32_t *prim, float *u, float *v)
+                      uint32_t *prim, uint32_t *inst, float *u, float *v)
 {
+    *inst = 0;
     orc_ray r = {{ox, oy, oz}, tmin, {dx, dy, dz}, 1e4f};
     orc_hit h;
     orc_bvh_trace1(J->bvh, &r, 2, J->twosided, 0, &h, NULL);
@@ -91,16 +94,17 @@ static inline float exp_scale_f(uint8_t e)
     return f;
 }
 
-/* closest hit (any = 0) or occlusion (any = 1) in double precision over the 8-wide BVH */
-static int d_trace(const orc_pt_job *J, const double o[3], double tmin, const double d[3], int cull_mode, int any,
-                   uint32_t *prim_out, double *u_out, double *v_out)
+/* closest hit (any = 0) or occlusion (any = 1) in double precision over one 8-wide BVH, t in
+   (tmin, tmax); two-sidedness per triangle (twosided[prim]) or for the whole mesh (all_twosided) */
+static int d_trace_bvh(const orc_bvh *b, const uint8_t *twosided, int all_twosided, const double o[3], double tmin,
+                       const double d[3], double tmax, int cull_mode, int any, uint32_t *prim_out, double *t_out,
+                       double *u_out, double *v_out)
 {
-    const orc_bvh *b = J->bvh;
     *prim_out = ORC_MISS;
     if(b->num_tris == 0) return 0;
     double inv[3];
     for(int a = 0; a < 3; ++a) inv[a] = d[a] != 0.0 ? 1.0 / d[a] : copysign(1e300, d[a]);
-    double best_t = 1e4, bu = 0, bv = 0;
+    double best_t = tmax, bu = 0, bv = 0;
     uint32_t best = ORC_MISS;
     uint32_t stack[512];
     int sp = 0;
@@ -143,7 +147,7 @@ static int d_trace(const orc_pt_job *J, const double o[3], double tmin, const do
                 double p[3] = {d[1] * e2[2] - e2[1] * d[2], d[2] * e2[0] - e2[2] * d[0], d[0] * e2[1] - e2[0] * d[1]};
                 double det = e1[0] * p[0] + e1[1] * p[1] + e1[2] * p[2];
                 if(det > -1e-12 && det < 1e-12) continue;
-                int cull = cull_mode == 1 || (cull_mode == 2 && !(J->twosided && J->twosided[prim]));
+                int cull = cull_mode == 1 || (cull_mode == 2 && !all_twosided && !(twosided && twosided[prim]));
                 if(cull && det < 0) continue;
                 double id = 1.0 / det;
                 double tv[3] = {o[0] - v0[0], o[1] - v0[1], o[2] - v0[2]};
@@ -154,7 +158,7 @@ static int d_trace(const orc_pt_job *J, const double o[3], double tmin, const do
                 double vv = (d[0] * q[0] + d[1] * q[1] + d[2] * q[2]) * id;
                 if(vv < 0.0 || uu + vv > 1.0) continue;
                 double t = (e2[0] * q[0] + e2[1] * q[1] + e2[2] * q[2]) * id;
-                if(!(t > tmin && t < 1e4)) continue;
+                if(!(t > tmin && t < tmax)) continue;
                 if(any) return 1;
                 if(t < best_t)
                 {
@@ -167,9 +171,253 @@ static int d_trace(const orc_pt_job *J, const double o[3], double tmin, const do
         }
     }
     *prim_out = best;
+    *t_out = best_t;
     *u_out = bu;
     *v_out = bv;
     return best != ORC_MISS;
+}
+
+static int d_trace(const orc_pt_job *J, const double o[3], double tmin, const double d[3], int cull_mode, int any,
+                   uint32_t *prim_out, double *u_out, double *v_out)
+{
+    double t;
+    return d_trace_bvh(J->bvh, J->twosided, 0, o, tmin, d, 1e4, cull_mode, any, prim_out, &t, u_out, v_out);
+}
+
+/* ---- instanced scenes (FP64) ----------------------------------------------------------------
+   A binary BVH over the instances' exact world boxes (the 8 transformed corners of the mesh bounds,
+   in double), split at the median centroid of the longest axis; an instance leaf moves the ray to
+   object space with the inverse transform (computed in double) and traces the mesh BVH. */
+typedef struct
+{
+    double lo[3], hi[3];
+    uint32_t left, count; /* count > 0: leaf over order[left .. left + count) */
+} ib_node;
+
+typedef struct
+{
+    ib_node *nodes;
+    uint32_t *order;
+    double *w2o;  /* [n][12] */
+    double *o2w;  /* [n][12] */
+    double (*box)[6];
+} inst_bvh;
+
+static void inv3x4(const double *m, double *r)
+{
+    const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], h = m[9], i = m[10];
+    const double A = e * i - f * h, B = f * g - d * i, C = d * h - e * g;
+    const double det = a * A + b * B + c * C, q = 1.0 / det;
+    const double M[9] = {A, c * h - b * i, b * f - c * e, B, a * i - c * g, c * d - a * f, C, b * g - a * h, a * e - b * d};
+    for(int row = 0; row < 3; ++row)
+    {
+        double acc = 0;
+        for(int k = 0; k < 3; ++k)
+        {
+            r[4 * row + k] = M[3 * row + k] * q;
+            acc += r[4 * row + k] * m[4 * k + 3];
+        }
+        r[4 * row + 3] = -acc;
+    }
+}
+
+typedef struct
+{
+    double c;
+    uint32_t i;
+} ib_key;
+
+static int ib_key_cmp(const void *a, const void *b)
+{
+    const ib_key *x = (const ib_key *)a, *y = (const ib_key *)b;
+    if(x->c < y->c) return -1;
+    if(x->c > y->c) return 1;
+    return x->i < y->i ? -1 : (x->i > y->i);
+}
+
+static inst_bvh *build_inst_bvh(const orc_pt_instances *I)
+{
+    const uint32_t n = I->num_instances;
+    inst_bvh *B = (inst_bvh *)calloc(1, sizeof(inst_bvh));
+    B->nodes = (ib_node *)calloc(2 * (size_t)n + 1, sizeof(ib_node));
+    B->order = (uint32_t *)malloc(sizeof(uint32_t) * (n ? n : 1));
+    B->w2o = (double *)malloc(sizeof(double) * 12 * (n ? n : 1));
+    B->o2w = (double *)malloc(sizeof(double) * 12 * (n ? n : 1));
+    B->box = (double(*)[6])malloc(sizeof(double[6]) * (n ? n : 1));
+    double (*mb)[6] = (double(*)[6])malloc(sizeof(double[6]) * (I->num_meshes ? I->num_meshes : 1));
+    for(uint32_t m = 0; m < I->num_meshes; ++m)
+    {
+        for(int a = 0; a < 3; ++a)
+        {
+            mb[m][a] = 1e300;
+            mb[m][3 + a] = -1e300;
+        }
+        for(uint32_t v = 0; v < I->mesh_nvert[m]; ++v)
+            for(int a = 0; a < 3; ++a)
+            {
+                const double x = I->mesh_xyz[m][3 * (size_t)v + a];
+                if(x < mb[m][a]) mb[m][a] = x;
+                if(x > mb[m][3 + a]) mb[m][3 + a] = x;
+            }
+    }
+    for(uint32_t k = 0; k < n; ++k)
+    {
+        double *o = B->o2w + 12 * (size_t)k;
+        for(int j = 0; j < 12; ++j) o[j] = I->o2w[12 * (size_t)k + j];
+        inv3x4(o, B->w2o + 12 * (size_t)k);
+        const double *bb = mb[I->inst_mesh[k]];
+        for(int a = 0; a < 3; ++a)
+        {
+            B->box[k][a] = 1e300;
+            B->box[k][3 + a] = -1e300;
+        }
+        for(int c = 0; c < 8; ++c)
+        {
+            const double p[3] = {(c & 1) ? bb[3] : bb[0], (c & 2) ? bb[4] : bb[1], (c & 4) ? bb[5] : bb[2]};
+            for(int a = 0; a < 3; ++a)
+            {
+                const double w = o[4 * a] * p[0] + o[4 * a + 1] * p[1] + o[4 * a + 2] * p[2] + o[4 * a + 3];
+                if(w < B->box[k][a]) B->box[k][a] = w;
+                if(w > B->box[k][3 + a]) B->box[k][3 + a] = w;
+            }
+        }
+        B->order[k] = k;
+    }
+    free(mb);
+    /* iterative median split */
+    uint32_t used = 1;
+    typedef struct { uint32_t node, lo, hi; } task;
+    task *stack = (task *)malloc(sizeof(task) * (2 * (size_t)n + 2));
+    int sp = 0;
+    stack[sp++] = (task){0, 0, n};
+    while(sp > 0)
+    {
+        task t = stack[--sp];
+        ib_node *nd = &B->nodes[t.node];
+        for(int a = 0; a < 3; ++a)
+        {
+            nd->lo[a] = 1e300;
+            nd->hi[a] = -1e300;
+        }
+        for(uint32_t i = t.lo; i < t.hi; ++i)
+            for(int a = 0; a < 3; ++a)
+            {
+                if(B->box[B->order[i]][a] < nd->lo[a]) nd->lo[a] = B->box[B->order[i]][a];
+                if(B->box[B->order[i]][3 + a] > nd->hi[a]) nd->hi[a] = B->box[B->order[i]][3 + a];
+            }
+        if(t.hi - t.lo <= 2)
+        {
+            nd->left = t.lo;
+            nd->count = t.hi - t.lo;
+            continue;
+        }
+        int axis = 0;
+        for(int a = 1; a < 3; ++a)
+            if(nd->hi[a] - nd->lo[a] > nd->hi[axis] - nd->lo[axis]) axis = a;
+        /* order the range by centroid along the axis; the median splits it */
+        const uint32_t cnt = t.hi - t.lo, mid = (t.lo + t.hi) / 2;
+        ib_key *keys = (ib_key *)malloc(sizeof(ib_key) * cnt);
+        for(uint32_t i = 0; i < cnt; ++i)
+        {
+            const uint32_t k = B->order[t.lo + i];
+            keys[i].c = B->box[k][axis] + B->box[k][3 + axis];
+            keys[i].i = k;
+        }
+        qsort(keys, cnt, sizeof(ib_key), ib_key_cmp);
+        for(uint32_t i = 0; i < cnt; ++i) B->order[t.lo + i] = keys[i].i;
+        free(keys);
+        nd->left = used;
+        nd->count = 0;
+        const uint32_t l = used, r = used + 1;
+        used += 2;
+        stack[sp++] = (task){l, t.lo, mid};
+        stack[sp++] = (task){r, mid, t.hi};
+    }
+    free(stack);
+    return B;
+}
+
+static void free_inst_bvh(inst_bvh *B)
+{
+    if(!B) return;
+    free(B->nodes);
+    free(B->order);
+    free(B->w2o);
+    free(B->o2w);
+    free(B->box);
+    free(B);
+}
+
+static int slab(const double lo[3], const double hi[3], const double o[3], const double inv[3], double tmin, double tmax)
+{
+    for(int a = 0; a < 3; ++a)
+    {
+        double t0 = (lo[a] - o[a]) * inv[a], t1 = (hi[a] - o[a]) * inv[a];
+        if(t0 > t1)
+        {
+            double tt = t0;
+            t0 = t1;
+            t1 = tt;
+        }
+        if(t0 > tmin) tmin = t0;
+        if(t1 < tmax) tmax = t1;
+    }
+    return tmin <= tmax;
+}
+
+static int d_trace_inst(const orc_pt_job *J, const double o[3], double tmin, const double d[3], int cull_mode,
+                        int any, uint32_t *prim_out, uint32_t *inst_out, double *u_out, double *v_out)
+{
+    const orc_pt_instances *I = J->inst;
+    const inst_bvh *B = (const inst_bvh *)J->ibvh;
+    *prim_out = *inst_out = ORC_MISS;
+    if(I->num_instances == 0) return 0;
+    double inv[3];
+    for(int a = 0; a < 3; ++a) inv[a] = d[a] != 0.0 ? 1.0 / d[a] : copysign(1e300, d[a]);
+    double best_t = 1e4, bu = 0, bv = 0;
+    uint32_t stack[256];
+    int sp = 0;
+    stack[sp++] = 0;
+    while(sp > 0)
+    {
+        const ib_node *nd = &B->nodes[stack[--sp]];
+        if(!slab(nd->lo, nd->hi, o, inv, tmin, best_t)) continue;
+        if(nd->count == 0)
+        {
+            if(sp + 2 <= 256)
+            {
+                stack[sp++] = nd->left;
+                stack[sp++] = nd->left + 1;
+            }
+            continue;
+        }
+        for(uint32_t i = nd->left; i < nd->left + nd->count; ++i)
+        {
+            const uint32_t k = B->order[i];
+            const double *w = B->w2o + 12 * (size_t)k;
+            double oo[3], dd[3];
+            for(int r = 0; r < 3; ++r)
+            {
+                oo[r] = w[4 * r] * o[0] + w[4 * r + 1] * o[1] + w[4 * r + 2] * o[2] + w[4 * r + 3];
+                dd[r] = w[4 * r] * d[0] + w[4 * r + 1] * d[1] + w[4 * r + 2] * d[2];
+            }
+            const uint32_t m = I->inst_mesh[k];
+            uint32_t prim;
+            double t, u, v;
+            if(!d_trace_bvh(I->mesh_bvh[m], NULL, I->mesh_twosided[m], oo, tmin, dd, best_t, cull_mode, any, &prim, &t,
+                            &u, &v))
+                continue;
+            if(any) return 1;
+            best_t = t;
+            *prim_out = prim;
+            *inst_out = k;
+            bu = u;
+            bv = v;
+        }
+    }
+    *u_out = bu;
+    *v_out = bv;
+    return *prim_out != ORC_MISS;
 }
 
 /* CDF inversion sample (independent of the GPU's alias table) */
@@ -199,17 +447,20 @@ static void d_env_sample_raw(const orc_pt_env *e, double u0, double u1, double u
 }
 
 static void d_hit_raw(const orc_pt_job *J, double ox, double oy, double oz, double tmin, double dx, double dy,
-                      double dz, uint32_t *prim, double *u, double *v)
+                      double dz, uint32_t *prim, uint32_t *inst, double *u, double *v)
 {
     double o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz};
     *u = *v = 0;
-    d_trace(J, o, tmin, d, 2, 0, prim, u, v);
+    *inst = 0;
+    if(J->inst) d_trace_inst(J, o, tmin, d, 2, 0, prim, inst, u, v);
+    else d_trace(J, o, tmin, d, 2, 0, prim, u, v);
 }
 
 static int d_occluded_raw(const orc_pt_job *J, double ox, double oy, double oz, double dx, double dy, double dz)
 {
     double o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz}, u, v;
-    uint32_t prim;
+    uint32_t prim, inst;
+    if(J->inst) return d_trace_inst(J, o, 0.0, d, 0, 1, &prim, &inst, &u, &v);
     return d_trace(J, o, 0.0, d, 0, 1, &prim, &u, &v);
 }
 
@@ -345,6 +596,48 @@ int orc_pt_render(int fp64, const orc_pt_scene *scene, const orc_bvh *bvh, const
         stats[1] = atomic_load(&J.shadow);
     }
     free(ts);
+    return n;
+}
+
+int orc_pt_render_instanced(const orc_pt_scene *scene, const orc_pt_instances *inst, const orc_pt_env *env,
+                            const orc_camera *cam, const orc_pt_settings *set, double *out, double *sq,
+                            uint64_t *stats, int nthreads)
+{
+    inst_bvh *B = build_inst_bvh(inst);
+    orc_pt_job J;
+    memset(&J, 0, sizeof(J));
+    J.scene = scene;
+    J.inst = inst;
+    J.ibvh = B;
+    J.env = env;
+    J.cam = cam;
+    J.seed = set->seed;
+    J.batch = set->batch;
+    J.spp = set->spp;
+    J.max_depth = set->max_depth;
+    J.rr_depth = set->rr_depth;
+    J.mis_mode = set->mis_mode;
+    J.disable_material = set->disable_material;
+    J.draw_skybox = set->draw_skybox;
+    J.max_path_beta = set->max_path_beta;
+    J.environment = set->environment;
+    J.cx0 = set->crop[0];
+    J.cy0 = set->crop[1];
+    J.cw = set->crop[2] ? set->crop[2] : cam->width;
+    J.ch = set->crop[3] ? set->crop[3] : cam->height;
+    J.out = out;
+    J.sq = sq;
+    J.fp64 = 1;
+    atomic_init(&J.next, 0u);
+    atomic_init(&J.ext, 0ull);
+    atomic_init(&J.shadow, 0ull);
+    int n = orc__run_threads(pt_worker, &J, nthreads);
+    if(stats)
+    {
+        stats[0] = atomic_load(&J.ext);
+        stats[1] = atomic_load(&J.shadow);
+    }
+    free_inst_bvh(B);
     return n;
 }
 

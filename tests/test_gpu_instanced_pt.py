@@ -13,29 +13,10 @@ import torch
 
 from vierkant_gb300 import geometry
 from vierkant_gb300.pathtracer import InstancedScene, PBRPathTracer, Scene, procedural_sky, sun_direction
-from vierkant_gb300.raytracing import INSTANCE_DTYPE
 
 pytestmark = pytest.mark.gpu
 
-IDENTITY = np.array([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], np.float32)
-
-
-def split_cornell(sc, tess=16):
-    """one mesh per wall quad (2 triangles) and per sphere (12 tess^2 triangles), in triangle order"""
-    xyz, idx, tm, mats = sc["xyz"], sc["indices"], sc["tri_material"], sc["materials"]
-    groups = [(2 * q, 2 * q + 2) for q in range(5)]
-    per = 12 * tess * tess
-    groups += [(10 + k * per, 10 + (k + 1) * per) for k in range((len(idx) - 10) // per)]
-    meshes, inst = [], np.zeros(len(groups), INSTANCE_DTYPE)
-    for k, (a, b) in enumerate(groups):
-        used, local = np.unique(idx[a:b].reshape(-1), return_inverse=True)
-        m = int(tm[a])
-        assert np.all(tm[a:b] == m)
-        meshes.append((xyz[used], local.reshape(-1, 3).astype(np.uint32), int(mats[m]["twosided"])))
-        inst[k]["transform"] = IDENTITY
-        inst[k]["blas"] = k
-        inst[k]["material"] = m
-    return meshes, inst
+from scene_helpers import split_cornell
 
 
 def settings(spp, crop):
@@ -86,3 +67,39 @@ def test_small_stress_scene_renders(ctx):
     assert img[:10].mean() > 0 and img[-10:].mean() > 0
     pt.close()
     scene.close()
+
+
+def test_instanced_radiance_against_fp64_oracle(ctx):
+    """a small stress scene (terrain + 2,000 transformed instances): the GPU image of a crop against
+    the FP64 oracle's instanced path at the same sample count, bias and RMSE within Monte-Carlo noise"""
+    import math
+    import oracle
+    st = geometry.stress_scene(terrain_n=129, num_instances=2000, num_meshes=4, num_materials=16)
+    sun = sun_direction()
+    env_gpu = procedural_sky(ctx, 512, 256, sun, 5e4, 3.8e-5)
+    scene = InstancedScene(ctx, st["meshes"], st["instances"], st["materials"], env_gpu)
+    W, H, crop, spp = 384, 216, (150, 90, 32, 32), 512
+    cam = geometry.camera_lookat((0, 120, 300), (0, 0, 0), (0, 1, 0), 40.0, W, H)
+    s = PBRPathTracer.default_settings()
+    s.resolution[0], s.resolution[1] = W, H
+    s.num_samples, s.max_trace_depth, s.rr_start_depth = spp, 8, 3
+    for k in range(4):
+        s.crop[k] = crop[k]
+    pt = PBRPathTracer(ctx, seed=17, settings=s)
+    img = pt.render_scene(scene, cam).cpu().numpy().astype(np.float64)
+    pt.close()
+    scene.close()
+    th = float(np.float32(math.tan(math.radians(40.0) / 2.0)))
+    ocam = oracle.camera((0, 120, 300), (0, 0, 0), (0, 1, 0), th, W, H)
+    inst = st["instances"]
+    ref, sq, _ = oracle.pt_render_instanced(st["meshes"], inst["transform"], inst["blas"], inst["material"],
+                                            st["materials"], env_gpu.cpu().numpy(), ocam, spp, seed=99, max_depth=8,
+                                            rr_depth=3, crop=crop)
+    lum = lambda a: 0.2126 * a[..., 0] + 0.7152 * a[..., 1] + 0.0722 * a[..., 2]
+    var = np.maximum(sq - lum(ref) ** 2, 0.0)
+    rmse = math.sqrt(np.mean((lum(img) - lum(ref)) ** 2))
+    expected = math.sqrt(2 * np.mean(var) / spp)
+    bias = (img.sum() - ref.sum()) / ref.sum()
+    print(f"instanced scene vs FP64 oracle: bias {bias:+.4f} rmse {rmse:.4f} expected noise {expected:.4f}")
+    assert rmse < 2.0 * expected, (rmse, expected)
+    assert abs(bias) < 0.03, bias

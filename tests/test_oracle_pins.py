@@ -174,3 +174,24 @@ def test_oracle_bvh_empty_mesh():
     b = oracle.CpuBVH(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32))
     rays = _random_rays(np.random.default_rng(0), 10)
     assert np.all(b.closest_hit(rays)["prim"] == 0xFFFFFFFF)
+
+
+def test_instanced_fp64_oracle_equals_flat_oracle():
+    """the FP64 oracle's instanced path (instance BVH, object-space traversal, transformed shading),
+    given the Cornell scene split into identity-instanced meshes, reproduces the flat FP64 oracle"""
+    import math
+    from scene_helpers import split_cornell
+    sc = oracle.cornell_scene(0x5EED, 2, 64, 16)
+    mats = oracle.cornell_materials(0x5EED, 2, 64)
+    meshes, inst = split_cornell(dict(sc, materials=mats))
+    th = float(np.float32(math.tan(math.radians(45.0) / 2.0)))
+    cam = oracle.camera((0, 0, 3.4), (0, 0, 0), (0, 1, 0), th, 1280, 720)
+    sun = np.array([0.2961981, 0.5, 0.8137977], np.float32)
+    env = oracle.env_procedural(256, 128, sun)
+    bvh = oracle.CpuBVH(sc["xyz"], sc["indices"], 4)
+    crop = (600, 500, 24, 24)
+    a, _, ra = oracle.pt_render(True, sc["xyz"], sc["indices"], sc["tri_material"], mats, bvh, env, cam, 8, crop=crop)
+    b, _, rb = oracle.pt_render_instanced(meshes, inst["transform"], inst["blas"], inst["material"], mats, env, cam, 8,
+                                          crop=crop)
+    assert ra == rb
+    assert np.array_equal(a, b)
