@@ -44,8 +44,12 @@ def test_identity_instances_render_like_the_flat_scene(ctx):
         assert sa.extension_rays == sb.extension_rays and sa.shadow_rays == sb.shadow_rays
         a.close()
         b.close()
-    lo, hi = inst_scene.bounds()
-    assert np.allclose(lo, sc["xyz"].min(axis=0), atol=1e-3) and np.allclose(hi, sc["xyz"].max(axis=0), atol=1e-3)
+    # the instance boxes are unions of quantised (outward-rounded) BLAS child boxes: they contain the
+    # geometry and exceed it by little
+    lo, hi = np.array(inst_scene.bounds()[0]), np.array(inst_scene.bounds()[1])
+    glo, ghi = sc["xyz"].min(axis=0), sc["xyz"].max(axis=0)
+    assert np.all(lo <= glo) and np.all(hi >= ghi)
+    assert np.all(glo - lo < 0.05 * (ghi - glo)) and np.all(hi - ghi < 0.05 * (ghi - glo))
     flat.close()
     inst_scene.close()
 

@@ -576,7 +576,41 @@ struct blas_box
 {
     float lo[3], hi[3];
     uint32_t num_tris, pad;
+    const node8 *nodes; // the BLAS's nodes: its upper levels give a tighter instance box than its bounds
 };
+
+// child box k of a node, dequantised (the quantised boxes contain their geometry)
+__device__ __forceinline__ void node_child_box(const node8 *nd, int k, double lo[3], double hi[3])
+{
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(nd);
+    const float ox = __uint_as_float(w[0]), oy = __uint_as_float(w[1]), oz = __uint_as_float(w[2]);
+    const uint32_t meta = w[3];
+    const double sx = exp_scale(meta & 0xFFu), sy = exp_scale((meta >> 8) & 0xFFu), sz = exp_scale((meta >> 16) & 0xFFu);
+    auto q = [&](int word, int kk) { return (double)((w[word + (kk >> 2)] >> (8 * (kk & 3))) & 0xFFu); };
+    // layout (traverse.cuh, node_keys): lo x / y / z in words 4-5 / 6-7 / 8-9, hi x / y / z in 10-11 / 12-13 / 14-15
+    lo[0] = ox + q(4, k) * sx;
+    lo[1] = oy + q(6, k) * sy;
+    lo[2] = oz + q(8, k) * sz;
+    hi[0] = ox + q(10, k) * sx;
+    hi[1] = oy + q(12, k) * sy;
+    hi[2] = oz + q(14, k) * sz;
+}
+
+__device__ __forceinline__ void grow_transformed(const float *T, const double lo[3], const double hi[3], double wlo[3],
+                                                 double whi[3])
+{
+    for(int c = 0; c < 8; ++c)
+    {
+        const double p[3] = {(c & 1) ? hi[0] : lo[0], (c & 2) ? hi[1] : lo[1], (c & 4) ? hi[2] : lo[2]};
+        for(int a = 0; a < 3; ++a)
+        {
+            const double w = (double)T[4 * a] * p[0] + (double)T[4 * a + 1] * p[1] + (double)T[4 * a + 2] * p[2] +
+                             (double)T[4 * a + 3];
+            wlo[a] = fmin(wlo[a], w);
+            whi[a] = fmax(whi[a], w);
+        }
+    }
+}
 
 // world -> object transform of an object -> world 3x4 transform: inverse of the 3x3 part by the
 // adjugate in double precision, translation -A^-1 t, rounded to float once. false if singular.
@@ -639,16 +673,28 @@ __global__ void k_instance_boxes(const vkg_instance *__restrict__ inst, uint32_t
         }
         else
         {
+            // the union of the transformed boxes two levels below the BLAS root (a rotated mesh's own
+            // bounds would be loose: a sphere's rotated bounding cube holds up to 5x its volume)
             double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-            for(int c = 0; c < 8; ++c)
+            const node8 *root = B.nodes;
+            const uint32_t *rw = reinterpret_cast<const uint32_t *>(root);
+            const int nch = (int)(rw[3] >> 24);
+            for(int k = 0; k < nch; ++k)
             {
-                const double p[3] = {(c & 1) ? B.hi[0] : B.lo[0], (c & 2) ? B.hi[1] : B.lo[1], (c & 4) ? B.hi[2] : B.lo[2]};
-                for(int a = 0; a < 3; ++a)
+                const uint32_t c = rw[16 + k];
+                double clo[3], chi[3];
+                if(c & LEAF_BIT)
                 {
-                    const double w = (double)I.transform[4 * a] * p[0] + (double)I.transform[4 * a + 1] * p[1] +
-                                     (double)I.transform[4 * a + 2] * p[2] + (double)I.transform[4 * a + 3];
-                    lo[a] = fmin(lo[a], w);
-                    hi[a] = fmax(hi[a], w);
+                    node_child_box(root, k, clo, chi);
+                    grow_transformed(I.transform, clo, chi, lo, hi);
+                    continue;
+                }
+                const node8 *ch = B.nodes + c;
+                const int gch = (int)(reinterpret_cast<const uint32_t *>(ch)[3] >> 24);
+                for(int g = 0; g < gch; ++g)
+                {
+                    node_child_box(ch, g, clo, chi);
+                    grow_transformed(I.transform, clo, chi, lo, hi);
                 }
             }
             // rounded outward; the collapse grows every box by its margin on top
@@ -954,6 +1000,7 @@ extern "C" vkg_status vkg_tlas_build(vkg_ctx *ctx, const vkg_bvh *const *blas, u
             boxes[b].hi[a] = blas[b]->scene_max[a];
         }
         boxes[b].num_tris = blas[b]->num_tris;
+        boxes[b].nodes = blas[b]->d_nodes;
     }
     blas_box *d_bb = nullptr;
     cudaError_t e = cudaSuccess;
