@@ -129,15 +129,29 @@ vkg_status vkg_geometry_icosphere(float radius, uint32_t tess, float *xyz, uint3
 /* Cornell box (5 quads over [-1,1]^3, open toward +z) + `num_spheres` cube-spheres of
  * 12 * n^2 triangles each with PCG32-drawn radius / centre / GGX material. Counts first, then
  * fill. per-triangle material id -> tri_material; materials: see vkg_material. */
+/* Disney material record (the reference's material_struct_t, RayBuilder.hpp:40-80, without textures,
+   media and iridescence). A triangle whose material has transmission > 0 or diffuse_transmission > 0
+   is never culled: rays leave such objects through their back faces. */
 typedef struct vkg_material
 {
     float base_color[3];
-    float roughness;
+    float roughness;            /* perceptual roughness; the BSDF's alpha is max(0.001, roughness^2) */
     float metalness;
     float emission[3];
-    uint32_t twosided; /* 1: back faces are not culled (RayBuilder.cpp:521-522) */
+    uint32_t twosided;          /* 1: back faces are not culled (RayBuilder.cpp:521-522) */
+    float transmission;         /* weight of the dielectric (refracting) lobe, [0, 1] */
+    float ior;                  /* index of refraction of the interior; > 0 when transmission > 0 */
+    float clearcoat;            /* clearcoat factor, >= 0 */
+    float clearcoat_roughness;  /* alpha of the clearcoat's GTR2 term */
+    float sheen_color[3];
+    float sheen_roughness;
+    float diffuse_transmission; /* share of the diffuse lobe sent through the surface, [0, 1] */
+    float diffuse_transmission_color[3];
     float pad[3];
-} vkg_material; /* 48 B */
+} vkg_material; /* 96 B */
+/* fills *m with the reference's defaults: base colour 1, roughness 1, ior 1.5, diffuse-transmission colour 1,
+   everything else 0 */
+vkg_status vkg_material_defaults(vkg_material *m);
 vkg_status vkg_scene_cornell_counts(uint32_t num_spheres, uint32_t n, uint32_t *num_vertices, uint32_t *num_tris,
                                     uint32_t *num_materials);
 vkg_status vkg_scene_cornell(uint64_t seed, uint64_t stream, uint32_t num_spheres, uint32_t n, float *xyz,

@@ -243,7 +243,10 @@ def tlas_any_hit(blas: list, w2o, inst_blas, rays, cull=False, nthreads=0):
 
 # ---- path tracer (FP32 twin / FP64 oracle) ---------------------------------------------------------
 MATERIAL_DTYPE = np.dtype([("base_color", "<f4", 3), ("roughness", "<f4"), ("metalness", "<f4"),
-                           ("emission", "<f4", 3), ("twosided", "<u4"), ("pad", "<f4", 3)])
+                           ("emission", "<f4", 3), ("twosided", "<u4"), ("transmission", "<f4"), ("ior", "<f4"),
+                           ("clearcoat", "<f4"), ("clearcoat_roughness", "<f4"), ("sheen_color", "<f4", 3),
+                           ("sheen_roughness", "<f4"), ("diffuse_transmission", "<f4"),
+                           ("diffuse_transmission_color", "<f4", 3), ("pad", "<f4", 3)])
 
 
 class orc_pt_scene(C.Structure):
@@ -376,3 +379,29 @@ def pt_render_instanced(meshes, o2w, inst_mesh, inst_mat, mats, env_rgb, cam, sp
     L.orc_pt_render_instanced(C.byref(scene), C.byref(inst), C.byref(env), C.byref(cam), C.byref(st), ptr(out),
                               ptr(sq), ptr(stats), nthreads)
     return out, sq, (int(stats[0]), int(stats[1]))
+
+
+def bsdf_sample(material, n, v, eta, u):
+    """one FP64 sample_disney: (direction, pdf, f, transmission)"""
+    L = orc()
+    L.orc_bsdf_sample.argtypes = [C.c_void_p] * 3 + [C.c_double] + [C.c_void_p] * 5
+    m = np.ascontiguousarray(material)
+    d = np.zeros(3)
+    f = np.zeros(3)
+    pdf = C.c_double()
+    tr = C.c_int()
+    L.orc_bsdf_sample(ptr(m), ptr(np.asarray(n, np.float64)), ptr(np.asarray(v, np.float64)), eta,
+                      ptr(np.asarray(u, np.float64)), ptr(d), C.byref(pdf), ptr(f), C.byref(tr))
+    return d, pdf.value, f, bool(tr.value)
+
+
+def bsdf_eval(material, l, n, v, eta):
+    """one FP64 eval_disney: (f, mixture pdf)"""
+    L = orc()
+    L.orc_bsdf_eval.argtypes = [C.c_void_p] * 4 + [C.c_double, C.c_void_p]
+    L.orc_bsdf_eval.restype = C.c_double
+    m = np.ascontiguousarray(material)
+    f = np.zeros(3)
+    pdf = L.orc_bsdf_eval(ptr(m), ptr(np.asarray(l, np.float64)), ptr(np.asarray(n, np.float64)),
+                          ptr(np.asarray(v, np.float64)), eta, ptr(f))
+    return f, pdf

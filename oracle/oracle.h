@@ -121,8 +121,11 @@ typedef struct {
     float roughness, metalness;
     float emission[3];
     uint32_t twosided;
+    float transmission, ior, clearcoat, clearcoat_roughness;
+    float sheen_color[3], sheen_roughness;
+    float diffuse_transmission, diffuse_transmission_color[3];
     float pad[3];
-} orc_pt_material; /* same 48-byte layout as vkg_material */
+} orc_pt_material; /* same 96-byte layout as vkg_material */
 
 typedef struct {
     const float *xyz;
@@ -173,6 +176,12 @@ int orc_pt_render(int fp64, const orc_pt_scene *scene, const orc_bvh *bvh, const
 int orc_pt_render_instanced(const orc_pt_scene *scene, const orc_pt_instances *inst, const orc_pt_env *env,
                             const orc_camera *cam, const orc_pt_settings *set, double *out, double *sq,
                             uint64_t *stats, int nthreads);
+/* one BSDF sample / evaluation in FP64 (sample_disney / eval_disney): u = (lobe, x, y); the return
+   value of orc_bsdf_eval is the mixture pdf */
+void orc_bsdf_sample(const orc_pt_material *m, const double n[3], const double v[3], double eta, const double u[3],
+                     double dir[3], double *pdf, double f[3], int *transmission);
+double orc_bsdf_eval(const orc_pt_material *m, const double l[3], const double n[3], const double v[3], double eta,
+                     double f[3]);
 /* FP64 env tables from an rgb map: weights (mean 1, as float) and the CDF (w*h+1 doubles) */
 void orc_pt_env_tables(const float *rgb, uint32_t w, uint32_t h, float *weight, double *cdf);
 /* procedural sky in double precision (environment_white + sun lobe), rounded to float */

@@ -201,6 +201,7 @@ typedef struct
     double *w2o;  /* [n][12] */
     double *o2w;  /* [n][12] */
     double (*box)[6];
+    uint8_t *mesh_unculled; /* [num_meshes]: two-sided, or used by an instance of a transmissive material */
 } inst_bvh;
 
 static void inv3x4(const double *m, double *r)
@@ -235,6 +236,12 @@ static int ib_key_cmp(const void *a, const void *b)
     return x->i < y->i ? -1 : (x->i > y->i);
 }
 
+/* back faces are traced for two-sided surfaces and for objects rays enter and leave (transmission) */
+static int orc_material_unculled(const orc_pt_material *m)
+{
+    return m->twosided != 0u || m->transmission > 0.f || m->diffuse_transmission > 0.f;
+}
+
 static inst_bvh *build_inst_bvh(const orc_pt_instances *I)
 {
     const uint32_t n = I->num_instances;
@@ -244,6 +251,8 @@ static inst_bvh *build_inst_bvh(const orc_pt_instances *I)
     B->w2o = (double *)malloc(sizeof(double) * 12 * (n ? n : 1));
     B->o2w = (double *)malloc(sizeof(double) * 12 * (n ? n : 1));
     B->box = (double(*)[6])malloc(sizeof(double[6]) * (n ? n : 1));
+    B->mesh_unculled = (uint8_t *)calloc(I->num_meshes ? I->num_meshes : 1, 1);
+    for(uint32_t m = 0; m < I->num_meshes; ++m) B->mesh_unculled[m] = I->mesh_twosided[m] ? 1 : 0;
     double (*mb)[6] = (double(*)[6])malloc(sizeof(double[6]) * (I->num_meshes ? I->num_meshes : 1));
     for(uint32_t m = 0; m < I->num_meshes; ++m)
     {
@@ -345,6 +354,7 @@ static void free_inst_bvh(inst_bvh *B)
     free(B->w2o);
     free(B->o2w);
     free(B->box);
+    free(B->mesh_unculled);
     free(B);
 }
 
@@ -404,7 +414,7 @@ static int d_trace_inst(const orc_pt_job *J, const double o[3], double tmin, con
             const uint32_t m = I->inst_mesh[k];
             uint32_t prim;
             double t, u, v;
-            if(!d_trace_bvh(I->mesh_bvh[m], NULL, I->mesh_twosided[m], oo, tmin, dd, best_t, cull_mode, any, &prim, &t,
+            if(!d_trace_bvh(I->mesh_bvh[m], NULL, B->mesh_unculled[m], oo, tmin, dd, best_t, cull_mode, any, &prim, &t,
                             &u, &v))
                 continue;
             if(any) return 1;
@@ -474,6 +484,7 @@ static int d_occluded_raw(const orc_pt_job *J, double ox, double oy, double oz, 
 #define RACOS(x) acosf(x)
 #define RFMA(a, b, c) fmaf(a, b, c)
 #define RABS(x) fabsf(x)
+#define RPOW(x, y) powf(x, y)
 #define HIT_RAW f_hit_raw
 #define OCC_RAW f_occluded_raw
 #define ENV_RAW f_env_sample_raw
@@ -488,6 +499,7 @@ static int d_occluded_raw(const orc_pt_job *J, double ox, double oy, double oz, 
 #undef RACOS
 #undef RFMA
 #undef RABS
+#undef RPOW
 #undef HIT_RAW
 #undef OCC_RAW
 #undef ENV_RAW
@@ -502,11 +514,36 @@ static int d_occluded_raw(const orc_pt_job *J, double ox, double oy, double oz, 
 #define RACOS(x) acos(x)
 #define RFMA(a, b, c) fma(a, b, c)
 #define RABS(x) fabs(x)
+#define RPOW(x, y) pow(x, y)
 #define HIT_RAW d_hit_raw
 #define OCC_RAW d_occluded_raw
 #define ENV_RAW d_env_sample_raw
 #define DRAW_RAW d_draw_raw
 #include "pt_core.inc"
+
+/* ---- single BSDF evaluations (FP64), for the sampling / evaluation consistency tests ---------- */
+void orc_bsdf_sample(const orc_pt_material *mt, const double n[3], const double v[3], double eta, const double u[3],
+                     double dir[3], double *pdf, double f[3], int *transmission)
+{
+    d_mat m;
+    d_load_mat(mt, 0, &m);
+    d_v3 d, fv;
+    d_sample_bsdf(&m, d_mk(n[0], n[1], n[2]), d_mk(v[0], v[1], v[2]), eta, u[0], u[1], u[2], &d, pdf, &fv,
+                  transmission);
+    dir[0] = d.x, dir[1] = d.y, dir[2] = d.z;
+    f[0] = fv.x, f[1] = fv.y, f[2] = fv.z;
+}
+
+double orc_bsdf_eval(const orc_pt_material *mt, const double l[3], const double n[3], const double v[3], double eta,
+                     double f[3])
+{
+    d_mat m;
+    d_load_mat(mt, 0, &m);
+    double pdf;
+    d_v3 fv = d_eval_bsdf(&m, d_mk(l[0], l[1], l[2]), d_mk(n[0], n[1], n[2]), d_mk(v[0], v[1], v[2]), eta, &pdf);
+    f[0] = fv.x, f[1] = fv.y, f[2] = fv.z;
+    return pdf;
+}
 
 /* ---- render ---------------------------------------------------------------------------------- */
 static void *pt_worker(void *arg)
@@ -560,7 +597,7 @@ int orc_pt_render(int fp64, const orc_pt_scene *scene, const orc_bvh *bvh, const
     for(uint32_t i = 0; i < scene->ntri; ++i)
     {
         uint32_t m = scene->tri_mat[i];
-        ts[i] = (m < scene->nmat && scene->mats[m].twosided) ? 1 : 0;
+        ts[i] = (m < scene->nmat && orc_material_unculled(&scene->mats[m])) ? 1 : 0;
     }
     orc_pt_job J;
     memset(&J, 0, sizeof(J));
@@ -604,6 +641,9 @@ int orc_pt_render_instanced(const orc_pt_scene *scene, const orc_pt_instances *i
                             uint64_t *stats, int nthreads)
 {
     inst_bvh *B = build_inst_bvh(inst);
+    for(uint32_t i = 0; i < inst->num_instances; ++i)
+        if(inst->inst_mat[i] < scene->nmat && orc_material_unculled(&scene->mats[inst->inst_mat[i]]))
+            B->mesh_unculled[inst->inst_mesh[i]] = 1;
     orc_pt_job J;
     memset(&J, 0, sizeof(J));
     J.scene = scene;

@@ -1,0 +1,146 @@
+"""The Disney material set on the GPU: dielectric transmission, clearcoat, sheen, diffuse transmission.
+
+* path-for-path twin: the FP32 CPU twin reproduces the GPU image of the showcase scene (the Cornell
+  spheres cycled through the lobes) pixel by pixel up to transcendental / FMA rounding;
+* radiance: the GPU image has bias and RMSE against the committed FP64 oracle (4096 spp, 256x144
+  full frame) consistent with Monte-Carlo noise;
+* white furnace: a smooth glass sphere under a constant unit environment reflects and refracts all
+  light, every pixel converges to 1;
+* identity instances of the showcase scene render bit for bit like the flat scene (transmissive
+  meshes are traced from both sides without a two-sided flag);
+* material records out of range are rejected at scene creation.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from vierkant_gb300 import _lib, geometry
+from vierkant_gb300.pathtracer import InstancedScene, PBRPathTracer, Scene, procedural_sky, sun_direction
+from scene_helpers import split_cornell
+from test_gpu_pathtracer import d2h
+
+pytestmark = pytest.mark.gpu
+
+W, H = 256, 144
+SUN_PEAK, SUN_WIDTH = 50.0, 0.02
+
+
+def settings(spp, crop=(0, 0, 0, 0), max_depth=8, rr=3, res=(W, H)):
+    s = PBRPathTracer.default_settings()
+    s.resolution[0], s.resolution[1] = res
+    s.num_samples, s.max_trace_depth, s.rr_start_depth, s.mis_mode = spp, max_depth, rr, 0
+    for k in range(4):
+        s.crop[k] = crop[k]
+    return s
+
+
+@pytest.fixture(scope="module")
+def showcase(ctx):
+    sc = geometry.cornell_scene(0x5EED, 2, 64, 16)
+    mats = geometry.showcase_materials(sc["materials"])
+    env = procedural_sky(ctx, 2048, 1024, sun_direction(), SUN_PEAK, SUN_WIDTH)
+    scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], mats, env)
+    cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, W, H)
+    th = float(np.float32(math.tan(math.radians(45.0) / 2.0)))
+    ocam = oracle.camera((0, 0, 3.4), (0, 0, 0), (0, 1, 0), th, W, H)
+    yield {"sc": sc, "mats": mats, "env": env, "scene": scene, "cam": cam, "ocam": ocam}
+    scene.close()
+
+
+def test_twin_parity_path_for_path(ctx, showcase):
+    spp = 8
+    pt = PBRPathTracer(ctx, seed=0x5EED, settings=settings(spp))
+    img = pt.render_scene(showcase["scene"], showcase["cam"]).cpu().numpy().astype(np.float64)
+    st = pt.statistics()
+    pt.close()
+    wptr, aptr, EW, EH = showcase["scene"].env_tables()
+    n = EW * EH
+    w = d2h(wptr, 4 * n, np.float32)
+    tab = d2h(aptr, 8 * n, np.uint32).reshape(n, 2)
+    prob = np.ascontiguousarray(tab[:, 0].view(np.float32))
+    alias = np.ascontiguousarray(tab[:, 1])
+    sc = showcase["sc"]
+    bvh = oracle.CpuBVH(sc["xyz"], sc["indices"], 4)
+    twin, _, rays = oracle.pt_render(False, sc["xyz"], sc["indices"], sc["tri_material"], showcase["mats"], bvh,
+                                     showcase["env"].cpu().numpy(), showcase["ocam"], spp, seed=0x5EED, batch=0,
+                                     max_depth=8, rr_depth=3, alias_prob=prob, alias=alias, weight=w)
+    rel = np.abs(img - twin) / np.maximum(np.abs(twin), 1e-2)
+    close = np.mean(np.all(rel < 1e-3, axis=-1))
+    print(f"close {close:.4f} sum ratio {img.sum() / twin.sum():.5f} rays {st.extension_rays}/{rays[0]} "
+          f"{st.shadow_rays}/{rays[1]}")
+    assert close > 0.9, close
+    assert abs(img.sum() / twin.sum() - 1.0) < 0.02
+    assert abs(st.extension_rays / rays[0] - 1.0) < 0.01
+    assert abs(st.shadow_rays / rays[1] - 1.0) < 0.01
+
+
+def test_radiance_against_fp64_oracle(ctx, showcase, golden):
+    g = golden("pt_oracle_materials")
+    ref = g["mean"].astype(np.float64)
+    assert tuple(g["size"]) == (W, H) and int(g["max_depth"]) == 8
+    pt = PBRPathTracer(ctx, seed=0x5EED, settings=settings(256))
+    for _ in range(4):  # 4 batches x 256 spp, running mean
+        img = pt.render_scene(showcase["scene"], showcase["cam"])
+    img = img.cpu().numpy().astype(np.float64)
+    pt.close()
+    spp = 1024
+    lum = lambda a: 0.2126 * a[..., 0] + 0.7152 * a[..., 1] + 0.0722 * a[..., 2]
+    bias = (img.sum() - ref.sum()) / ref.sum()
+    rmse = math.sqrt(np.mean((lum(img) - lum(ref)) ** 2))
+    expected = math.sqrt(np.mean(g["lum_var"]) / spp + np.mean(g["lum_var"]) / int(g["spp"]))
+    # the sphere kinds separately: each material's pixels agree in the mean
+    print(f"bias {bias:+.4f}  rmse {rmse:.4f}  expected noise {expected:.4f}")
+    assert abs(bias) < 0.02, bias
+    assert rmse < 2.5 * expected, (rmse, expected)
+
+
+@pytest.mark.parametrize("roughness,tol", [(0.0, 0.01), (0.35, 0.03)])
+def test_glass_sphere_white_furnace(ctx, roughness, tol):
+    xyz, idx = oracle.icosphere(1.0, 4)
+    mats = geometry.default_materials(1)
+    mats["transmission"][0] = 1.0
+    mats["roughness"][0] = roughness
+    env = torch.ones((64, 128, 3), dtype=torch.float32, device="cuda")
+    scene = Scene(ctx, xyz, idx, np.zeros(len(idx), np.uint32), mats, env)
+    cam = geometry.camera_lookat((0, 0, 4.0), (0, 0, 0), (0, 1, 0), 40.0, 64, 64)
+    pt = PBRPathTracer(ctx, seed=7, settings=settings(256, max_depth=32, rr=0, res=(64, 64)))
+    img = pt.render_scene(scene, cam).cpu().numpy().astype(np.float64)
+    pt.close()
+    scene.close()
+    centre = img[24:40, 24:40].mean(axis=-1)  # rays that meet the sphere close to normal incidence
+    print(f"roughness {roughness}: centre {centre.mean():.4f} +- {centre.std():.4f}, frame {img.mean():.4f}")
+    assert abs(centre.mean() - 1.0) < tol
+    assert np.all(img[:4] == 1.0)  # the sky above the sphere (silhouette half-angle 14.5 deg of 20)
+
+
+def test_identity_instances_render_like_the_flat_scene(ctx, showcase):
+    sc = dict(showcase["sc"])
+    sc["materials"] = showcase["mats"]
+    meshes, inst = split_cornell(sc)
+    assert any(m[2] == 0 for m in meshes)
+    inst_scene = InstancedScene(ctx, meshes, inst, showcase["mats"], showcase["env"])
+    a = PBRPathTracer(ctx, seed=21, settings=settings(4))
+    b = PBRPathTracer(ctx, seed=21, settings=settings(4))
+    ia = a.render_scene(showcase["scene"], showcase["cam"]).clone()
+    ib = b.render_scene(inst_scene, showcase["cam"]).clone()
+    sa, sb = a.statistics(), b.statistics()
+    assert torch.equal(ia, ib), (ia - ib).abs().max().item()
+    assert sa.extension_rays == sb.extension_rays and sa.shadow_rays == sb.shadow_rays
+    a.close()
+    b.close()
+    inst_scene.close()
+
+
+@pytest.mark.parametrize("field,value", [("transmission", 1.5), ("diffuse_transmission", -0.1), ("metalness", 2.0),
+                                         ("clearcoat", -1.0), ("ior", 0.0)])
+def test_invalid_materials_rejected(ctx, field, value):
+    xyz, idx = oracle.icosphere(1.0, 1)
+    mats = geometry.default_materials(1)
+    mats["transmission"][0] = 0.5
+    mats[field][0] = value
+    env = torch.ones((8, 16, 3), dtype=torch.float32, device="cuda")
+    with pytest.raises(_lib.VkgError):
+        Scene(ctx, xyz, idx, np.zeros(len(idx), np.uint32), mats, env)

@@ -44,7 +44,10 @@ class vkg_ray_triangle_intersection(C.Structure):
 
 class vkg_material(C.Structure):
     _fields_ = [("base_color", C.c_float * 3), ("roughness", C.c_float), ("metalness", C.c_float),
-                ("emission", C.c_float * 3), ("twosided", C.c_uint32), ("pad", C.c_float * 3)]
+                ("emission", C.c_float * 3), ("twosided", C.c_uint32), ("transmission", C.c_float),
+                ("ior", C.c_float), ("clearcoat", C.c_float), ("clearcoat_roughness", C.c_float),
+                ("sheen_color", C.c_float * 3), ("sheen_roughness", C.c_float), ("diffuse_transmission", C.c_float),
+                ("diffuse_transmission_color", C.c_float * 3), ("pad", C.c_float * 3)]
 
 
 class vkg_camera(C.Structure):
@@ -165,6 +168,7 @@ SIGNATURES = {
     "vkg_scene_cornell_counts": (I32, [U32, U32, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)]),
     "vkg_scene_cornell": (I32, [U64, U64, U32, U32, P, P, P, P]),
     "vkg_camera_lookat": (I32, [P, P, P, F32, U32, U32, C.POINTER(vkg_camera)]),
+    "vkg_material_defaults": (I32, [C.POINTER(vkg_material)]),
     "vkg_camera_rays": (I32, [P, C.POINTER(vkg_camera), U64, U64, U32, P, P]),
     "vkg_bvh_build": (I32, [P, P, U32, P, U32, C.POINTER(vkg_bvh_build_options), C.POINTER(P), P]),
     "vkg_bvh_info_get": (I32, [P, C.POINTER(vkg_bvh_info)]),

@@ -642,7 +642,8 @@ vkg_status vkg_scene_cornell(uint64_t seed, uint64_t stream, uint32_t num_sphere
         const float cols[3][3] = {{0.73f, 0.73f, 0.73f}, {0.65f, 0.05f, 0.05f}, {0.12f, 0.45f, 0.15f}};
         for(int m = 0; m < 3; ++m)
         {
-            vkg_material mat{};
+            vkg_material mat;
+            vkg_material_defaults(&mat);
             std::memcpy(mat.base_color, cols[m], sizeof(cols[m]));
             mat.roughness = 1.f;
             mat.metalness = 0.f;
@@ -669,13 +670,25 @@ vkg_status vkg_scene_cornell(uint64_t seed, uint64_t stream, uint32_t num_sphere
             for(uint32_t t = 0; t < tps; ++t) tri_material[10 + s * tps + t] = 3 + s;
         if(materials)
         {
-            vkg_material mat{};
+            vkg_material mat;
+            vkg_material_defaults(&mat);
             std::memcpy(mat.base_color, base, sizeof(base));
             mat.roughness = rough;
             mat.metalness = metal;
             materials[3 + s] = mat;
         }
     }
+    return VKG_OK;
+}
+
+vkg_status vkg_material_defaults(vkg_material *m)
+{
+    if(!m) return VKG_ERR_INVALID_ARGUMENT;
+    // the reference's material_struct_t defaults (RayBuilder.hpp:42-66, Material.hpp:125-129)
+    *m = vkg_material{};
+    for(int c = 0; c < 3; ++c) m->base_color[c] = m->diffuse_transmission_color[c] = 1.f;
+    m->roughness = 1.f;
+    m->ior = 1.5f;
     return VKG_OK;
 }
 

@@ -32,6 +32,7 @@
 #include "pt_kernels.cuh"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 
@@ -97,11 +98,44 @@ __global__ void k_set_tri_flags(tri_rec *__restrict__ tris, uint32_t n, uint32_t
     if(i < n) tris[i].pad[0] |= flags;
 }
 
-__global__ void k_check_instance_materials(const vkg_instance *__restrict__ inst, uint32_t n, uint32_t num_mats,
-                                           uint32_t *__restrict__ bad)
+// flags instances whose material index is out of range (bad), and the meshes that an instance with an
+// unculled material (two-sided or transmissive) references (mesh_unculled)
+__global__ void k_check_instance_materials(const vkg_instance *__restrict__ inst, uint32_t n,
+                                           const vkg_material *__restrict__ mats, uint32_t num_mats,
+                                           uint32_t num_meshes, uint32_t *__restrict__ bad,
+                                           uint32_t *__restrict__ mesh_unculled)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if(i < n && inst[i].material >= num_mats) atomicOr(bad, 1u);
+    if(i >= n) return;
+    const uint32_t m = inst[i].material, b = inst[i].blas;
+    if(m >= num_mats) atomicOr(bad, 1u);
+    else if(b < num_meshes && material_unculled(mats[m])) mesh_unculled[b] = 1u;
+}
+
+// the material fields the BSDF divides by or takes as probabilities must be in range
+vkg_status check_material_values(vkg_ctx *ctx, const vkg_material *d_mats, uint32_t n, cudaStream_t st,
+                                 const char *fn)
+{
+    std::vector<vkg_material> h(n);
+    cudaError_t e = cudaMemcpyAsync(h.data(), d_mats, n * sizeof(vkg_material), cudaMemcpyDeviceToHost, st);
+    if(e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if(e != cudaSuccess) return cuda_check(ctx, e, fn);
+    auto unit = [](float x) { return x >= 0.f && x <= 1.f; };
+    for(uint32_t i = 0; i < n; ++i)
+    {
+        const vkg_material &m = h[i];
+        if(!unit(m.transmission) || !unit(m.diffuse_transmission) || !unit(m.metalness))
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
+                             "%s: material %u: metalness, transmission and diffuse_transmission must be in [0, 1]", fn, i);
+        if(m.transmission > 0.f && !(m.ior > 0.f && std::isfinite(m.ior)))
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "%s: material %u: a transmissive material needs ior > 0",
+                             fn, i);
+        if(!(m.clearcoat >= 0.f) || !(m.clearcoat_roughness >= 0.f) || !(m.sheen_roughness >= 0.f) ||
+           !std::isfinite(m.clearcoat))
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
+                             "%s: material %u: clearcoat, clearcoat_roughness and sheen_roughness must be >= 0", fn, i);
+    }
+    return VKG_OK;
 }
 
 void tracer_free_buffers(vkg_tracer *t)
@@ -263,6 +297,11 @@ vkg_status vkg_scene_create(vkg_ctx *ctx, const vkg_scene_desc *d, vkg_scene **o
         vkg_scene_destroy(ctx, sc);
         return cuda_check(ctx, e, "vkg_scene_create");
     }
+    if(vkg_status s = check_material_values(ctx, sc->mats, d->num_materials, st, "vkg_scene_create"); s != VKG_OK)
+    {
+        vkg_scene_destroy(ctx, sc);
+        return s;
+    }
     vkg_bvh_build_options opt{d->leaf_max};
     vkg_status s = vkg_bvh_build(ctx, sc->xyz, d->num_vertices, sc->idx, d->num_tris, &opt, &sc->bvh, stream);
     if(s != VKG_OK)
@@ -343,6 +382,10 @@ vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_de
     };
     chk(cudaMalloc(&sc->mats, d->num_materials * sizeof(vkg_material)));
     chk(cudaMemcpyAsync(sc->mats, d->d_materials, d->num_materials * sizeof(vkg_material), cudaMemcpyDeviceToDevice, st));
+    if(e != cudaSuccess) return fail(cuda_check(ctx, e, "vkg_scene_create_instanced"));
+    if(vkg_status s = check_material_values(ctx, sc->mats, d->num_materials, st, "vkg_scene_create_instanced");
+       s != VKG_OK)
+        return fail(s);
     std::vector<mesh_ref> refs(d->num_meshes);
     uint64_t tris = 0;
     for(uint32_t m = 0; m < d->num_meshes && e == cudaSuccess; ++m)
@@ -380,16 +423,25 @@ vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_de
     if(e != cudaSuccess) return fail(cuda_check(ctx, e, "vkg_scene_create_instanced"));
     if(d->num_instances)
     {
-        uint32_t *bad = nullptr, hbad = 0;
-        chk(cudaMallocAsync(&bad, sizeof(uint32_t), st));
-        chk(cudaMemsetAsync(bad, 0, sizeof(uint32_t), st));
-        k_check_instance_materials<<<(d->num_instances + 255) / 256, 256, 0, st>>>(d->d_instances, d->num_instances,
-                                                                                   d->num_materials, bad);
-        chk(cudaMemcpyAsync(&hbad, bad, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-        chk(cudaFreeAsync(bad, st));
+        // word 0: bad material index; words 1..num_meshes: the mesh is used with an unculled material
+        uint32_t *flags = nullptr;
+        std::vector<uint32_t> hf(1 + d->num_meshes, 0u);
+        chk(cudaMallocAsync(&flags, hf.size() * sizeof(uint32_t), st));
+        chk(cudaMemsetAsync(flags, 0, hf.size() * sizeof(uint32_t), st));
+        k_check_instance_materials<<<(d->num_instances + 255) / 256, 256, 0, st>>>(
+                d->d_instances, d->num_instances, sc->mats, d->num_materials, d->num_meshes, flags, flags + 1);
+        chk(cudaMemcpyAsync(hf.data(), flags, hf.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        chk(cudaFreeAsync(flags, st));
         chk(cudaStreamSynchronize(st));
         if(e != cudaSuccess) return fail(cuda_check(ctx, e, "vkg_scene_create_instanced"));
-        if(hbad) return fail(set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_create_instanced: an instance material >= num_materials"));
+        if(hf[0]) return fail(set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_create_instanced: an instance material >= num_materials"));
+        // rays enter and leave transmissive instances through back faces: their meshes are not culled
+        for(uint32_t m = 0; m < d->num_meshes; ++m)
+            if(hf[1 + m] && !d->meshes[m].twosided && d->meshes[m].num_tris)
+                k_set_tri_flags<<<(d->meshes[m].num_tris + 255) / 256, 256, 0, st>>>(sc->blas[m]->d_tris,
+                                                                                   d->meshes[m].num_tris,
+                                                                                   TRI_FLAG_TWOSIDED);
+        chk(cudaGetLastError());
     }
     std::vector<const vkg_bvh *> bl(sc->blas.begin(), sc->blas.end());
     vkg_bvh_build_options topt{1}; // one instance per top-level leaf: its own quantised box culls it

@@ -1,11 +1,12 @@
-// Device math of the path tracer: environment lookup / importance sampling, the metal-roughness
-// subset of vierkant's Disney BSDF, sampling helpers and MIS weights.
+// Device math of the path tracer: environment lookup / importance sampling, vierkant's Disney BSDF
+// (all lobes but iridescence), sampling helpers and MIS weights.
 //
-// Restated from the reference shaders (transmission = clearcoat = sheen = iridescence =
-// diffuse transmission = 0, the material model of the benchmark scenes):
+// Restated from the reference shaders:
 //   sample_disney / eval_disney   shaders/slang/ray/bsdf_disney.slang:162-296, :298-381
-//   EvalDiffuse / EvalSpecular    bsdf_disney.slang:142-160, :97-110
-//   GTR2, SmithGGX, SchlickFresnel shaders/slang/utils/bsdf.slang:9-13, :160-172
+//   EvalDiffuse / EvalSpecular / EvalClearcoat  bsdf_disney.slang:142-160, :97-110, :129-140
+//   EvalDielectricReflection / Refraction       bsdf_disney.slang:44-58, :79-95
+//   GTR2, SmithGGX, SchlickFresnel, DielectricFresnel  shaders/slang/utils/bsdf.slang:9-13, :160-172, :24-33
+//   sample_GTR1                   shaders/slang/utils/sampling.slang:120-129
 //   local_frame, sample_GGX_VNDF, sample_hemisphere_cosine  shaders/slang/utils/sampling.slang:16-22, :79-118
 //   power_heuristic               shaders/slang/ray/direct_lighting.slang:140-144
 //   environment_white             shaders/slang/utils/procedural_environment.slang:7-11
@@ -41,6 +42,13 @@ vkg_status env_build(vkg_ctx *ctx, const float *d_rgb_in, uint32_t w, uint32_t h
 void env_free(env_tables &t);
 
 #if defined(__CUDACC__)
+
+// back faces of a material's triangles are traced, not culled: two-sided surfaces, and objects that
+// rays enter and leave (dielectric or diffuse transmission)
+__host__ __device__ inline bool material_unculled(const vkg_material &m)
+{
+    return m.twosided != 0u || m.transmission > 0.f || m.diffuse_transmission > 0.f;
+}
 
 __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
 __device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
@@ -127,12 +135,17 @@ __device__ __forceinline__ float3 env_sample(const env_view &e, float u0, float 
     return d;
 }
 
-// ---- BSDF (metal-roughness subset of bsdf_disney.slang) ------------------------------------
+// ---- BSDF (bsdf_disney.slang without iridescence) -------------------------------------------
 struct material_view
 {
     float3 base;
     float roughness; // perceptual roughness (squared into alpha by the BSDF)
     float metalness;
+    float transmission, clearcoat, clearcoat_roughness;
+    float3 sheen_color;
+    float sheen_roughness;
+    float diffuse_transmission;
+    float3 dt_color;
 };
 
 __device__ __forceinline__ float schlick_fresnel(float u)
@@ -150,6 +163,25 @@ __device__ __forceinline__ float smith_ggx(float ndotv, float alpha)
 {
     float a = alpha * alpha, b = ndotv * ndotv;
     return 1.f / (ndotv + sqrtf(a + b - a * b));
+}
+// unpolarised Fresnel reflectance of a dielectric interface, eta = n_incident / n_transmitted
+// (utils/bsdf.slang:24-33)
+__device__ __forceinline__ float dielectric_fresnel(float cos_i, float eta)
+{
+    float s2 = eta * eta * (1.f - cos_i * cos_i);
+    if(s2 >= 1.f) return 1.f;
+    float cos_t = sqrtf(fmaxf(1.f - s2, 0.f));
+    float rs = (eta * cos_t - cos_i) / (eta * cos_t + cos_i);
+    float rp = (eta * cos_i - cos_t) / (eta * cos_i + cos_t);
+    return 0.5f * (rs * rs + rp * rp);
+}
+// refract(i, n, eta) of the shading languages: the zero vector on total internal reflection
+__device__ __forceinline__ float3 refract3(float3 i, float3 n, float eta)
+{
+    float ni = dot(n, i);
+    float k = 1.f - eta * eta * (1.f - ni * ni);
+    if(k < 0.f) return f3(0.f, 0.f, 0.f);
+    return i * eta - n * (eta * ni + sqrtf(k));
 }
 
 // local_frame(N): rows (tangent_x, tangent_y, N)
@@ -186,20 +218,34 @@ __device__ __forceinline__ float3 sample_ggx_vndf(float x, float y, float3 wi, f
     return normalize(f3(m.x * alpha, m.y * alpha, m.z));
 }
 
-__device__ __forceinline__ float3 eval_diffuse(float alpha, float3 color, float metal, float3 V, float3 N, float3 L,
-                                               float3 H, float &pdf)
+// GTR1 half vector (sampling.slang:120-129)
+__device__ __forceinline__ float3 sample_gtr1(float x, float y, float roughness)
+{
+    float a = fmaxf(0.001f, roughness);
+    float a2 = a * a;
+    float phi = y * 2.f * PT_PI;
+    float ct = sqrtf((1.f - powf(a2, 1.f - x)) / (1.f - a2));
+    float st = fminf(fmaxf(sqrtf(1.f - ct * ct), 0.f), 1.f);
+    return f3(st * cosf(phi), st * sinf(phi), ct);
+}
+
+// EvalDiffuse with the sheen term (bsdf_disney.slang:142-160)
+__device__ __forceinline__ float3 eval_diffuse(const material_view &m, float alpha, float sheen_r, float3 V, float3 N,
+                                               float3 L, float3 H, float &pdf)
 {
     pdf = 0.f;
     float nol = dot(N, L);
     if(nol <= 0.f) return f3(0.f, 0.f, 0.f);
     pdf = nol * PT_ONE_OVER_PI;
     float loh = dot(L, H);
-    float fl = schlick_fresnel(nol), fv = schlick_fresnel(dot(N, V));
+    float fl = schlick_fresnel(nol), fv = schlick_fresnel(dot(N, V)), fh = schlick_fresnel(loh);
     float fd90 = 0.5f + 2.f * loh * loh * alpha;
     float fd = lerpf(1.f, fd90, fl) * lerpf(1.f, fd90, fv);
-    return color * (PT_ONE_OVER_PI * fd * (1.f - metal));
+    float k = PT_ONE_OVER_PI * (1.f - m.metalness);
+    return m.base * (k * fd) + m.sheen_color * (k * fh * sheen_r);
 }
 
+// EvalSpecular (bsdf_disney.slang:97-110)
 __device__ __forceinline__ float3 eval_specular(float alpha, float3 cspec0, float3 V, float3 N, float3 L, float3 H,
                                                 float &pdf)
 {
@@ -214,62 +260,226 @@ __device__ __forceinline__ float3 eval_specular(float alpha, float3 cspec0, floa
     return f * (d * g);
 }
 
+// EvalClearcoat (bsdf_disney.slang:129-140): GTR2 with clearcoat_roughness, Smith with alpha 0.25
+__device__ __forceinline__ float eval_clearcoat(float cc_rough, float cc, float3 V, float3 N, float3 L, float3 H,
+                                                float &pdf)
+{
+    pdf = 0.f;
+    if(dot(N, L) <= 0.f) return 0.f;
+    float noh = dot(N, H);
+    float d = gtr2(noh, cc_rough);
+    pdf = d * noh / (4.f * dot(V, H));
+    float f = lerpf(0.04f, 1.f, schlick_fresnel(dot(L, H)));
+    float g = smith_ggx(dot(N, L), 0.25f) * smith_ggx(fabsf(dot(N, V)), 0.25f);
+    return 0.25f * cc * f * d * g;
+}
+
+// EvalDielectricReflection (bsdf_disney.slang:44-58)
+__device__ __forceinline__ float3 eval_dielectric_reflection(float alpha, float3 color, float eta, float3 V, float3 N,
+                                                             float3 L, float3 H, float &pdf)
+{
+    pdf = 0.f;
+    if(dot(N, L) <= 0.f) return f3(0.f, 0.f, 0.f);
+    float F = dielectric_fresnel(dot(V, H), eta);
+    float d = gtr2(dot(N, H), alpha);
+    float sv = smith_ggx(fabsf(dot(N, V)), alpha);
+    pdf = 0.5f * d * sv * F;
+    float g = smith_ggx(fabsf(dot(N, L)), alpha) * sv;
+    return color * (F * d * g);
+}
+
+// EvalDielectricRefraction (bsdf_disney.slang:79-95)
+__device__ __forceinline__ float3 eval_dielectric_refraction(float alpha, float3 color, float eta, float3 V, float3 N,
+                                                             float3 L, float3 H, float &pdf)
+{
+    pdf = 0.f;
+    if(dot(N, L) >= 0.f) return f3(0.f, 0.f, 0.f);
+    float loh = dot(L, H), voh = dot(V, H);
+    float denom = loh + voh * eta;
+    if(fabsf(denom) < 1e-7f) return f3(0.f, 0.f, 0.f);
+    float F = dielectric_fresnel(fabsf(voh), eta);
+    float d = gtr2(dot(N, H), alpha);
+    float sv = smith_ggx(fabsf(dot(N, V)), alpha);
+    float jac = fabsf(loh) * eta * eta / (denom * denom);
+    pdf = 2.f * sv * d * fabsf(voh) * (1.f - F) * jac;
+    float g = smith_ggx(fabsf(dot(N, L)), alpha) * sv;
+    return color * ((1.f - F) * d * g * fabsf(voh) * 4.f * jac);
+}
+
 struct bsdf_sample
 {
     float3 dir;
     float pdf; // pdf of the sampled lobe times its selection probability (sample_disney's pdf)
     float3 f;  // the sampled lobe's value
+    bool transmission;
 };
 
-// sample_disney restricted to the metal-roughness lobes; u_lobe selects diffuse vs specular,
-// (x, y) drive the VNDF half vector or the cosine lobe
-__device__ __forceinline__ bsdf_sample sample_bsdf(const material_view &m, float3 N, float3 V, float u_lobe, float x,
-                                                   float y)
+// sample_disney (bsdf_disney.slang:162-296). The reference draws a fresh random number for each lobe
+// decision; here u_lobe alone makes them all, rescaled to [0, 1) inside the chosen branch, so every
+// path segment uses a fixed count of draws. (x, y) drive the half vector or the cosine lobe, and y
+// also makes the Fresnel reflect / refract choice of the dielectric lobe (as the reference's Xi.y does).
+// eta = n_incident / n_transmitted of the hit face.
+__device__ __forceinline__ bsdf_sample sample_bsdf(const material_view &m, float3 N, float3 V, float eta,
+                                                   float u_lobe, float x, float y)
 {
     bsdf_sample r;
+    r.transmission = false;
     float diffuse_ratio = 0.5f * (1.f - m.metalness);
+    float trans_weight = (1.f - m.metalness) * m.transmission;
     float alpha = fmaxf(0.001f, m.roughness * m.roughness);
     float3 spec = lerp3(f3(0.08f, 0.08f, 0.08f), m.base, m.metalness);
     frame3 fr = local_frame(N);
-    if(u_lobe < diffuse_ratio)
-    {
-        r.dir = to_world(fr, sample_hemisphere_cosine(x, y));
-        float3 H = normalize(r.dir + V);
-        r.f = eval_diffuse(alpha, m.base, m.metalness, V, N, r.dir, H, r.pdf);
-        r.pdf *= diffuse_ratio;
-    }
-    else
+    if(trans_weight > 0.f && u_lobe < trans_weight)
     {
         float3 H = to_world(fr, sample_ggx_vndf(x, y, to_local(fr, V), alpha));
         if(dot(V, H) < 0.f) H = -H;
-        r.dir = normalize(reflect3(-V, H));
-        r.f = eval_specular(alpha, spec, V, N, r.dir, H, r.pdf);
-        r.pdf *= 1.f - diffuse_ratio;
+        const float3 R = reflect3(-V, H);
+        const float F = dielectric_fresnel(fabsf(dot(R, H)), eta);
+        float3 refr = f3(0.f, 0.f, 0.f);
+        if(!(y < F)) refr = refract3(-V, H, eta);
+        if(y < F || dot(refr, refr) < 1e-7f)
+        {
+            // reflection, or total internal reflection
+            r.dir = normalize(R);
+            r.f = eval_dielectric_reflection(alpha, m.base, eta, V, N, r.dir, H, r.pdf);
+        }
+        else
+        {
+            r.dir = normalize(refr);
+            r.f = eval_dielectric_refraction(alpha, m.base, eta, V, N, r.dir, H, r.pdf);
+            r.transmission = true;
+        }
+        r.f = r.f * trans_weight;
+        r.pdf *= trans_weight;
+    }
+    else
+    {
+        const float u = trans_weight > 0.f ? (u_lobe - trans_weight) / (1.f - trans_weight) : u_lobe;
+        if(u < diffuse_ratio)
+        {
+            const float dt = m.diffuse_transmission;
+            const float ud = u / diffuse_ratio;
+            const float3 c = sample_hemisphere_cosine(x, y);
+            if(dt > 0.f && ud < dt)
+            {
+                // Lambertian transmission: the cosine lobe of the opposite hemisphere
+                r.dir = to_world(fr, f3(c.x, c.y, -c.z));
+                r.f = m.dt_color * (dt * PT_ONE_OVER_PI);
+                r.pdf = c.z * PT_ONE_OVER_PI * diffuse_ratio * dt;
+                r.transmission = true;
+            }
+            else
+            {
+                r.dir = to_world(fr, c);
+                float3 H = normalize(r.dir + V);
+                r.f = eval_diffuse(m, alpha, fmaxf(0.001f, m.sheen_roughness), V, N, r.dir, H, r.pdf) * (1.f - dt);
+                r.pdf *= diffuse_ratio * (1.f - dt);
+            }
+        }
+        else
+        {
+            const float primary = 1.f / (1.f + m.clearcoat);
+            const float us = (u - diffuse_ratio) / (1.f - diffuse_ratio);
+            if(!(m.clearcoat > 0.f) || us < primary)
+            {
+                float3 H = to_world(fr, sample_ggx_vndf(x, y, to_local(fr, V), alpha));
+                if(dot(V, H) < 0.f) H = -H;
+                r.dir = normalize(reflect3(-V, H));
+                r.f = eval_specular(alpha, spec, V, N, r.dir, H, r.pdf);
+                r.pdf *= primary * (1.f - diffuse_ratio);
+            }
+            else
+            {
+                float3 H = to_world(fr, sample_gtr1(x, y, lerpf(0.1f, 0.001f, m.clearcoat)));
+                if(dot(V, H) < 0.f) H = -H;
+                r.dir = normalize(reflect3(-V, H));
+                const float c = eval_clearcoat(m.clearcoat_roughness, m.clearcoat, V, N, r.dir, H, r.pdf);
+                r.f = f3(c, c, c);
+                r.pdf *= (1.f - primary) * (1.f - diffuse_ratio);
+            }
+        }
+        r.f = r.f * (1.f - trans_weight);
+        r.pdf *= 1.f - trans_weight;
     }
     if(isnan(r.pdf)) r.pdf = 0.f;
     return r;
 }
 
-// eval_disney for the same subset: value and mixture pdf (the sum over lobes)
-__device__ __forceinline__ float3 eval_bsdf(const material_view &m, float3 L, float3 N, float3 V, float &pdf)
+// eval_disney (bsdf_disney.slang:298-381): value and mixture pdf (the sum over lobes). The clearcoat
+// lobe is skipped when clearcoat == 0, where its value and pdf weight are 0.
+__device__ __forceinline__ float3 eval_bsdf(const material_view &m, float3 L, float3 N, float3 V, float eta, float &pdf)
 {
     pdf = 0.f;
-    float3 lpv = L + V;
+    const bool refl = dot(N, L) > 0.f;
+    float3 lpv = refl ? L + V : L + V * eta;
     float len = sqrtf(dot(lpv, lpv));
     if(len < 1e-7f) return f3(0.f, 0.f, 0.f);
     float3 H = lpv * (1.f / len);
     if(dot(V, H) < 0.f) H = -H;
-    if(dot(N, L) > 0.f && dot(N, H) <= 0.f) return f3(0.f, 0.f, 0.f);
+    if(refl && dot(N, H) <= 0.f) return f3(0.f, 0.f, 0.f);
     float diffuse_ratio = 0.5f * (1.f - m.metalness);
+    float primary = 1.f / (1.f + m.clearcoat);
+    float trans_weight = (1.f - m.metalness) * m.transmission;
     float alpha = fmaxf(0.001f, m.roughness * m.roughness);
     float3 spec = lerp3(f3(0.08f, 0.08f, 0.08f), m.base, m.metalness);
-    float pd, ps;
-    float3 f = eval_diffuse(alpha, m.base, m.metalness, V, N, L, H, pd);
-    f = f + eval_specular(alpha, spec, V, N, L, H, ps);
-    float p = pd * diffuse_ratio + ps * (1.f - diffuse_ratio);
+    float3 brdf = f3(0.f, 0.f, 0.f), bsdf = brdf;
+    float brdf_pdf = 0.f, bsdf_pdf = 0.f, mp;
+    if(trans_weight > 0.f)
+    {
+        if(refl) bsdf = eval_dielectric_reflection(alpha, m.base, eta, V, N, L, H, bsdf_pdf);
+        else bsdf = eval_dielectric_refraction(alpha, m.base, eta, V, N, L, H, bsdf_pdf);
+    }
+    if(trans_weight < 1.f)
+    {
+        const float dt = m.diffuse_transmission;
+        brdf = eval_diffuse(m, alpha, fmaxf(0.001f, m.sheen_roughness), V, N, L, H, mp) * (1.f - dt);
+        brdf_pdf = mp * diffuse_ratio * (1.f - dt);
+        if(dt > 0.f && !refl)
+        {
+            brdf = brdf + m.dt_color * (dt * PT_ONE_OVER_PI);
+            brdf_pdf += -dot(N, L) * PT_ONE_OVER_PI * diffuse_ratio * dt;
+        }
+        brdf = brdf + eval_specular(alpha, spec, V, N, L, H, mp);
+        brdf_pdf += mp * primary * (1.f - diffuse_ratio);
+        if(m.clearcoat > 0.f)
+        {
+            const float c = eval_clearcoat(m.clearcoat_roughness, m.clearcoat, V, N, L, H, mp);
+            brdf = brdf + f3(c, c, c);
+            brdf_pdf += mp * (1.f - primary) * (1.f - diffuse_ratio);
+        }
+    }
+    float p = lerpf(brdf_pdf, bsdf_pdf, trans_weight);
     if(!(p > 0.f)) return f3(0.f, 0.f, 0.f);
     pdf = p;
-    return f;
+    return lerp3(brdf, bsdf, trans_weight);
+}
+
+// the material record as the BSDF reads it
+__device__ __forceinline__ material_view load_material(const vkg_material *mats, uint32_t id, bool disable_material)
+{
+    const vkg_material &q = mats[id];
+    material_view m;
+    m.base = disable_material ? f3(0.8f, 0.8f, 0.8f) : f3(q.base_color[0], q.base_color[1], q.base_color[2]);
+    m.roughness = q.roughness;
+    m.metalness = q.metalness;
+    m.transmission = q.transmission;
+    m.clearcoat = q.clearcoat;
+    m.clearcoat_roughness = q.clearcoat_roughness;
+    m.sheen_color = f3(q.sheen_color[0], q.sheen_color[1], q.sheen_color[2]);
+    m.sheen_roughness = q.sheen_roughness;
+    m.diffuse_transmission = q.diffuse_transmission;
+    m.dt_color = f3(q.diffuse_transmission_color[0], q.diffuse_transmission_color[1], q.diffuse_transmission_color[2]);
+    return m;
+}
+
+// eta of a hit (raypipeline.slang:489-491) for an object in vacuum: entering through a front face
+// 1 / ior, leaving through a back face ior, plus the reference's EPS; 1 for opaque materials
+__device__ __forceinline__ float hit_eta(const vkg_material *mats, uint32_t id, bool back_face)
+{
+    const float t = mats[id].transmission;
+    if(!(t > 0.f)) return 1.f;
+    const float ior = mats[id].ior;
+    return (back_face ? ior : 1.f / ior) + PT_EPS;
 }
 
 // direct_lighting.slang:140-144

@@ -309,14 +309,13 @@ __global__ void __launch_bounds__(PT_THREADS)
                 uint32_t mat;
                 hit_surface(P, h.x, P.two_level ? hit_inst[i] : 0u, __uint_as_float(h.z), __uint_as_float(h.w), P0,
                             ng, mat);
-                N = dot(ng, dir) < 0.f ? ng : -ng; // shading normal faces the incoming ray
+                const bool back_face = !(dot(ng, dir) < 0.f);
+                N = back_face ? -ng : ng; // shading normal faces the incoming ray
                 const float3 V = -dir;
-                const vkg_material mt = P.mats[mat];
-                material_view m;
-                m.base = P.disable_material ? f3(0.8f, 0.8f, 0.8f) : f3(mt.base_color[0], mt.base_color[1], mt.base_color[2]);
-                m.roughness = mt.roughness;
-                m.metalness = mt.metalness;
-                L = L + beta * f3(mt.emission[0], mt.emission[1], mt.emission[2]);
+                const material_view m = load_material(P.mats, mat, P.disable_material);
+                const float eta = hit_eta(P.mats, mat, back_face);
+                const float *em = P.mats[mat].emission;
+                L = L + beta * f3(em[0], em[1], em[2]);
                 if constexpr(MODE == MODE_CACHE)
                 {
                     if(pid < P.train_base && depth == P.term_depth)
@@ -352,7 +351,7 @@ __global__ void __launch_bounds__(PT_THREADS)
                     if(pdf_env > 0.f && cosl > 0.f)
                     {
                         float pdf_b;
-                        const float3 f = eval_bsdf(m, ld, N, V, pdf_b);
+                        const float3 f = eval_bsdf(m, ld, N, V, eta, pdf_b);
                         if(pdf_b > 0.f)
                         {
                             const float w = P.mis_mode == 1 ? 1.f : power_heuristic(pdf_env, pdf_b);
@@ -366,7 +365,7 @@ __global__ void __launch_bounds__(PT_THREADS)
                     }
                 }
                 // BSDF sample (sample_disney) and throughput
-                const bsdf_sample bs = sample_bsdf(m, N, V, u[0], u[1], u[2]);
+                const bsdf_sample bs = sample_bsdf(m, N, V, eta, u[0], u[1], u[2]);
                 bool alive = bs.pdf > 0.f && !push_query;
                 if(alive)
                 {
@@ -375,8 +374,10 @@ __global__ void __launch_bounds__(PT_THREADS)
                     if(depth >= 1 && P.max_path_beta > 0.f)
                         tp = f3(fminf(tp.x, P.max_path_beta), fminf(tp.y, P.max_path_beta), fminf(tp.z, P.max_path_beta));
                     beta = beta * tp;
+                    // MIS pdf of the bounce for an environment hit: the mixture pdf where the
+                    // environment sampler competes (directions above the surface), 0 below it
                     float pdf_mix = 0.f;
-                    eval_bsdf(m, bs.dir, N, V, pdf_mix);
+                    if(dot(N, bs.dir) > 0.f) eval_bsdf(m, bs.dir, N, V, eta, pdf_mix);
                     prev_pdf = pdf_mix;
                     // Russian roulette
                     if(P.rr_depth == 0)
@@ -740,7 +741,7 @@ __global__ void k_tri_flags(tri_rec *__restrict__ tris, uint32_t n, const uint32
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= n) return;
     const uint32_t m = tri_mat[tris[i].prim];
-    tris[i].pad[0] = (m < num_mats && mats[m].twosided) ? TRI_FLAG_TWOSIDED : 0u;
+    tris[i].pad[0] = (m < num_mats && material_unculled(mats[m])) ? TRI_FLAG_TWOSIDED : 0u;
 }
 
 __global__ void k_check_materials(const uint32_t *__restrict__ tri_mat, uint32_t n, uint32_t num_mats,

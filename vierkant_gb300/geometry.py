@@ -14,8 +14,20 @@ import numpy as np
 from ._lib import check, lib, vkg_camera, vkg_material
 
 MATERIAL_DTYPE = np.dtype([("base_color", "<f4", 3), ("roughness", "<f4"), ("metalness", "<f4"),
-                           ("emission", "<f4", 3), ("twosided", "<u4"), ("pad", "<f4", 3)])
+                           ("emission", "<f4", 3), ("twosided", "<u4"), ("transmission", "<f4"), ("ior", "<f4"),
+                           ("clearcoat", "<f4"), ("clearcoat_roughness", "<f4"), ("sheen_color", "<f4", 3),
+                           ("sheen_roughness", "<f4"), ("diffuse_transmission", "<f4"),
+                           ("diffuse_transmission_color", "<f4", 3), ("pad", "<f4", 3)])
 assert MATERIAL_DTYPE.itemsize == C.sizeof(vkg_material)
+
+
+def default_materials(n: int) -> np.ndarray:
+    """n material records with the reference's defaults (base colour 1, roughness 1, ior 1.5,
+    diffuse-transmission colour 1, everything else 0), filled by the library."""
+    m = vkg_material()
+    check(lib().vkg_material_defaults(C.byref(m)))
+    one = np.frombuffer(bytes(m), MATERIAL_DTYPE, count=1)
+    return np.repeat(one, n).copy()
 
 
 def _p(a: np.ndarray):
@@ -43,6 +55,40 @@ def cornell_scene(seed: int = 0x5EED, stream: int = 2, num_spheres: int = 64, n:
     mats = np.zeros(nm.value, MATERIAL_DTYPE)
     check(L.vkg_scene_cornell(seed, stream, num_spheres, n, _p(xyz), _p(idx), _p(tm), _p(mats)))
     return {"xyz": xyz, "indices": idx, "tri_material": tm, "materials": mats}
+
+
+SHOWCASE_KINDS = ("metal-rough", "glass", "rough glass", "clearcoat", "sheen", "diffuse transmission")
+
+
+def showcase_materials(materials: np.ndarray) -> np.ndarray:
+    """The Cornell-box material table with its spheres cycled through the Disney lobes: sphere s
+    (material 3 + s) becomes SHOWCASE_KINDS[s % 6] and keeps its generated colour (lightened for glass);
+    the walls and the metal-rough spheres are unchanged."""
+    m = np.array(materials, MATERIAL_DTYPE, copy=True)
+    for s in range(len(m) - 3):
+        i, kind = 3 + s, s % len(SHOWCASE_KINDS)
+        c = m["base_color"][i].copy()
+        if kind == 0:
+            continue
+        m["metalness"][i] = 0.0
+        if kind in (1, 2):
+            m["transmission"][i] = 1.0
+            m["ior"][i] = 1.5 if kind == 1 else 1.33
+            m["roughness"][i] = 0.0 if kind == 1 else 0.35
+            m["base_color"][i] = 0.75 + 0.25 * c
+        elif kind == 3:
+            m["clearcoat"][i] = 1.0
+            m["clearcoat_roughness"][i] = 0.05
+            m["roughness"][i] = 0.6
+        elif kind == 4:
+            m["sheen_color"][i] = (0.9, 0.9, 0.9)
+            m["sheen_roughness"][i] = 0.5
+            m["roughness"][i] = 0.9
+        else:
+            m["diffuse_transmission"][i] = 0.6
+            m["diffuse_transmission_color"][i] = c
+            m["roughness"][i] = 0.7
+    return m
 
 
 def camera_lookat(eye, target, up, fovy_deg: float, width: int, height: int) -> vkg_camera:
