@@ -231,11 +231,12 @@ def run_ours(args):
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_baseline(sc, batch, budget_s=args.cpu_seconds)
-    pt_block = batch_block = stress = None
+    pt_block = batch_block = stress = features = None
     if rank == 0 and not args.no_pt:
         pt_block = path_tracer_block(ctx, frames=args.nrc_frames)
         batch_block = batched_block(ctx)
         stress = stress_block(ctx)
+        features = features_block(ctx)
 
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 1), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
@@ -257,6 +258,8 @@ def run_ours(args):
             line["batched"] = batch_block
         if stress is not None:
             line["stress"] = stress
+        if features is not None:
+            line["materials_lights"] = features
         print(json.dumps(line), flush=True)
     bvh.close()
     ctx.close()
@@ -350,6 +353,72 @@ def path_tracer_block(ctx, frames=256):
         "nrc_rmse_final": round(rmse, 4), "nrc_bias_final": round(bias, 5),
         "oracle": "FP64 4096 spp, 128x128 crop at (896, 824)",
         "protocol": "1 spp per frame, 65,536 training paths per frame, terminate after 2 bounces"}
+    return out
+
+
+def features_block(ctx):
+    """The full material and light set: the Cornell box with the showcase materials (glass, rough
+    glass, clearcoat, sheen, diffuse transmission, metal-rough), one light of every analytic type and
+    a sun disc, against the same box with metal-rough materials and no lights, both at 1280x720 x 64
+    spp, 8 segments (samples/s, Mrays/s). Parity: the 16-sphere lit scene at 256x144 x 1024 spp
+    against its FP64 oracle (4096 spp full frame)."""
+    import math
+    import numpy as np
+    import torch
+    from vierkant_gb300 import geometry
+    from vierkant_gb300.pathtracer import PBRPathTracer, Scene, cornell_lights
+
+    sun = dict(color=(1.0, 0.95, 0.9), intensity=3.0, coords=(math.radians(30), math.radians(200)), angular=0.05)
+
+    def settings(spp, w, h, lit):
+        s = PBRPathTracer.default_settings()
+        s.num_samples, s.max_trace_depth, s.rr_start_depth = spp, 8, 3
+        s.resolution[0], s.resolution[1] = w, h
+        if lit:
+            for c in range(3):
+                s.sun_color[c] = sun["color"][c]
+            s.sun_intensity = sun["intensity"]
+            s.sun_spherical_coords[0], s.sun_spherical_coords[1] = sun["coords"]
+            s.sun_angular_size = sun["angular"]
+        return s
+
+    env = torch.full((64, 128, 3), 0.1, dtype=torch.float32, device="cuda")
+    out = {}
+    sc = geometry.cornell_scene(SEED, 2, 64, 16)
+    cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, 1280, 720)
+    for name, mats, lit in (("plain_720p_64spp_8seg", sc["materials"], False),
+                            ("materials_lights_720p_64spp_8seg", geometry.showcase_materials(sc["materials"]), True)):
+        scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], mats, env)
+        if lit:
+            scene.set_lights(cornell_lights())
+        pt = PBRPathTracer(ctx, seed=SEED, settings=settings(64, 1280, 720, lit))
+        pt.render_scene(scene, cam)
+        pt.reset_accumulator()
+        pt.render_scene(scene, cam)
+        st = pt.statistics()
+        rays = st.extension_rays + st.shadow_rays
+        out[name] = {"ms": round(st.total_ms, 2), "samples_per_s": round(st.paths / st.total_ms * 1e3),
+                     "mrays_per_s": round(rays / st.total_ms / 1e3, 1), "rays": int(rays)}
+        pt.close()
+        scene.close()
+    out["materials_lights_time_vs_plain"] = round(out["materials_lights_720p_64spp_8seg"]["ms"] /
+                                                  out["plain_720p_64spp_8seg"]["ms"], 3)
+    g = np.load(ROOT / "tests" / "golden" / "pt_oracle_lights.npz")
+    sc = geometry.cornell_scene(SEED, 2, int(g["num_spheres"]), 16)
+    scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], geometry.showcase_materials(sc["materials"]),
+                  env)
+    scene.set_lights(cornell_lights())
+    cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, 256, 144)
+    pt = PBRPathTracer(ctx, seed=SEED, settings=settings(1024, 256, 144, True))
+    img = pt.render_scene(scene, cam).cpu().numpy().astype(np.float64)
+    pt.close()
+    scene.close()
+    ref = g["mean"].astype(np.float64)
+    rmse = math.sqrt(np.mean((_lum(img) - _lum(ref)) ** 2))
+    out["lights_parity_256x144_1024spp"] = {
+        "rmse": round(rmse, 4), "bias": round(float((img.sum() - ref.sum()) / ref.sum()), 5),
+        "expected_noise": round(math.sqrt(np.mean(g["lum_var"]) / 1024 + np.mean(g["lum_var"]) / int(g["spp"])), 4),
+        "oracle": "FP64 %d spp, full frame" % int(g["spp"])}
     return out
 
 

@@ -149,6 +149,52 @@ typedef struct vkg_material
     float diffuse_transmission_color[3];
     float pad[3];
 } vkg_material; /* 96 B */
+/* ---- analytic lights ----------------------------------------------------------------------
+ * The reference's LightType (punctual_light.hpp:20-34); AREA is reserved for emissive triangles and
+ * rejected here, as the reference leaves it out of the light list (PBRPathTracer.cpp:633-634). */
+enum
+{
+    VKG_LIGHT_OMNI = 0,
+    VKG_LIGHT_SPOT = 1,
+    VKG_LIGHT_DIRECTIONAL = 2,
+    VKG_LIGHT_AREA = 3,
+    VKG_LIGHT_RECT = 4,
+    VKG_LIGHT_SPHERE = 5,
+    VKG_LIGHT_TUBE = 6,
+    VKG_LIGHT_DISK = 7
+};
+/* the shader-side light record, same 80-byte layout as the reference's light_t
+   (punctual_light.hpp:67-90, ray_common.slang:109-131) */
+typedef struct vkg_light
+{
+    float position[3];
+    uint32_t type;
+    float color[3];
+    float intensity;
+    float direction[3];       /* propagation direction (unit); rect / disk emit along it, tube axis */
+    float range;              /* omni / spot range window, +inf: pure inverse square */
+    float spot_angle_scale;
+    float spot_angle_offset;
+    float angular_size;       /* directional: > 0 makes a sun disc of this cone half-angle (radians) */
+    float size_y;             /* rect half-height, tube half-length */
+    float tangent[3];         /* rect in-plane x axis (unit, orthogonal to direction) */
+    float size_x;             /* sphere / disk / tube radius, rect half-width */
+} vkg_light;                  /* 80 B */
+/* a light-source asset (lightsource_t, punctual_light.hpp:43-57) */
+typedef struct vkg_light_source
+{
+    uint32_t type;
+    float color[3];
+    float intensity;
+    float range;              /* <= 0: +inf */
+    float inner_cone_angle, outer_cone_angle;
+    float size[2];            /* x: radius or rect half-width, y: rect half-height or tube half-length */
+} vkg_light_source;
+/* convert_light (punctual_light.hpp:92-111): place an asset with an object transform (row-major
+   3x3 rotation, translation) */
+vkg_status vkg_light_convert(const vkg_light_source *src, const float rotation[9], const float translation[3],
+                             vkg_light *out);
+
 /* fills *m with the reference's defaults: base colour 1, roughness 1, ior 1.5, diffuse-transmission colour 1,
    everything else 0 */
 vkg_status vkg_material_defaults(vkg_material *m);
@@ -362,6 +408,9 @@ vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_de
 /* the two-level BVH of an instanced scene (NULL for a single-level scene) */
 vkg_status vkg_scene_tlas(const vkg_scene *scene, const vkg_tlas **out);
 vkg_status vkg_scene_destroy(vkg_ctx *ctx, vkg_scene *scene);
+/* the scene's analytic lights (host array, copied; n = 0 removes them). Directions and tangents are
+   normalised; the sun of the tracer settings comes first in the light list of a render. */
+vkg_status vkg_scene_set_lights(vkg_ctx *ctx, vkg_scene *scene, const vkg_light *lights, uint32_t n);
 /* the scene's BVH (owned by the scene) for direct ray queries */
 vkg_status vkg_scene_bvh(const vkg_scene *scene, const vkg_bvh **out);
 /* device views of the environment sampling tables: per texel normalised weight (mean 1, fp32) and
@@ -388,6 +437,13 @@ typedef struct vkg_settings
                                          max(beta) <= 0.05 * depth (raypipeline.slang:668-677) */
     uint32_t crop[4];                 /* x0, y0, width, height of the traced window (0 size: full) */
     uint32_t samples_per_wave;        /* paths in flight = pixels x this (0 = automatic) */
+    uint32_t suppress_refractive_caustics; /* drop light-body / sun hits on refractive-caustic paths */
+    /* sunlight_params_t (PBRPathTracer.hpp:23-33): a directional light folded in as light 0 when
+       sun_intensity > 0; direction from (elevation, azimuth) as the reference's quaternion does */
+    float sun_color[3];
+    float sun_intensity;
+    float sun_spherical_coords[2];    /* elevation, azimuth (radians) */
+    float sun_angular_size;           /* cone half-angle of the disc (radians); 0: a delta light */
 } vkg_settings;
 
 typedef struct vkg_tracer_create_info

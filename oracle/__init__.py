@@ -263,7 +263,33 @@ class orc_pt_settings(C.Structure):
     _fields_ = [("seed", C.c_uint32), ("batch", C.c_uint32), ("spp", C.c_uint32), ("max_depth", C.c_uint32),
                 ("rr_depth", C.c_uint32), ("mis_mode", C.c_uint32), ("disable_material", C.c_uint32),
                 ("draw_skybox", C.c_uint32), ("max_path_beta", C.c_float), ("environment", C.c_float),
-                ("crop", C.c_uint32 * 4)]
+                ("crop", C.c_uint32 * 4), ("num_lights", C.c_uint32), ("suppress_caustics", C.c_uint32),
+                ("lights", C.c_void_p)]
+
+
+# analytic light record (80 bytes, the layout of vkg_light)
+LIGHT_DTYPE = np.dtype([("position", "<f4", 3), ("type", "<u4"), ("color", "<f4", 3), ("intensity", "<f4"),
+                        ("direction", "<f4", 3), ("range", "<f4"), ("spot_angle_scale", "<f4"),
+                        ("spot_angle_offset", "<f4"), ("angular_size", "<f4"), ("size_y", "<f4"),
+                        ("tangent", "<f4", 3), ("size_x", "<f4")])
+
+
+def sun_light(color, intensity, spherical_coords, angular_size):
+    """the tracer settings' sun as a directional light record (oracle restatement)"""
+    out = np.zeros(1, LIGHT_DTYPE)
+    orc().orc_sun_light.argtypes = [C.c_void_p, C.c_float, C.c_void_p, C.c_float, C.c_void_p]
+    orc().orc_sun_light(ptr(np.asarray(color, np.float32)), intensity, ptr(np.asarray(spherical_coords, np.float32)),
+                        angular_size, ptr(out))
+    return out[0]
+
+
+def _settings(seed, batch, spp, max_depth, rr_depth, mis_mode, draw_skybox, max_path_beta, environment, crop, lights,
+              suppress_caustics):
+    arr = np.ascontiguousarray(np.asarray(lights if lights is not None else [], LIGHT_DTYPE).reshape(-1))
+    st = orc_pt_settings(seed, batch, spp, max_depth, rr_depth, mis_mode, 0, draw_skybox, max_path_beta, environment,
+                         (C.c_uint32 * 4)(*crop), len(arr), int(suppress_caustics),
+                         arr.ctypes.data_as(C.c_void_p) if len(arr) else None)
+    return st, arr
 
 
 def cornell_materials(seed=0x5EED, stream=2, num_spheres=64):
@@ -303,7 +329,7 @@ def env_tables_fp64(rgb):
 
 def pt_render(fp64, xyz, idx, tri_mat, mats, bvh: "CpuBVH", env_rgb, cam, spp, *, seed=0x5EED, batch=0, max_depth=6,
               rr_depth=3, mis_mode=0, crop=(0, 0, 0, 0), environment=1.0, draw_skybox=1, max_path_beta=0.0,
-              alias_prob=None, alias=None, weight=None, cdf=None, nthreads=0):
+              alias_prob=None, alias=None, weight=None, cdf=None, nthreads=0, lights=None, suppress_caustics=False):
     """Mean radiance per crop pixel ([h, w, 3] float64), mean squared luminance per pixel, (ext, shadow) rays."""
     L = orc()
     L.orc_pt_render.argtypes = [C.c_int, C.POINTER(orc_pt_scene), C.POINTER(orc_bvh), C.POINTER(orc_pt_env),
@@ -320,8 +346,8 @@ def pt_render(fp64, xyz, idx, tri_mat, mats, bvh: "CpuBVH", env_rgb, cam, spp, *
                      ptr(alias) if alias is not None else None, ptr(cdf) if cdf is not None else None, w, h)
     cw = crop[2] or cam.width
     ch = crop[3] or cam.height
-    st = orc_pt_settings(seed, batch, spp, max_depth, rr_depth, mis_mode, 0, draw_skybox, max_path_beta, environment,
-                         (C.c_uint32 * 4)(*crop))
+    st, _lights = _settings(seed, batch, spp, max_depth, rr_depth, mis_mode, draw_skybox, max_path_beta, environment,
+                            crop, lights, suppress_caustics)
     out = np.zeros((ch, cw, 3), np.float64)
     sq = np.zeros((ch, cw), np.float64)
     stats = np.zeros(2, np.uint64)
@@ -339,7 +365,7 @@ class orc_pt_instances(C.Structure):
 
 def pt_render_instanced(meshes, o2w, inst_mesh, inst_mat, mats, env_rgb, cam, spp, *, seed=0x5EED, batch=0,
                         max_depth=6, rr_depth=3, mis_mode=0, crop=(0, 0, 0, 0), environment=1.0, draw_skybox=1,
-                        nthreads=0, mesh_bvhs=None):
+                        nthreads=0, mesh_bvhs=None, lights=None, suppress_caustics=False):
     """FP64 oracle of an instanced scene: meshes [(xyz, idx, twosided)], o2w [N, 12] object -> world,
     mesh and material index per instance. Returns (mean radiance [h, w, 3], mean squared luminance,
     (ext, shadow) rays)."""
@@ -371,8 +397,8 @@ def pt_render_instanced(meshes, o2w, inst_mesh, inst_mat, mats, env_rgb, cam, sp
     env = orc_pt_env(ptr(rgb), ptr(np.ascontiguousarray(weight, np.float32)), None, None, ptr(cdf), w, h)
     cw = crop[2] or cam.width
     ch = crop[3] or cam.height
-    st = orc_pt_settings(seed, batch, spp, max_depth, rr_depth, mis_mode, 0, draw_skybox, 0.0, environment,
-                         (C.c_uint32 * 4)(*crop))
+    st, _lights = _settings(seed, batch, spp, max_depth, rr_depth, mis_mode, draw_skybox, 0.0, environment, crop,
+                            lights, suppress_caustics)
     out = np.zeros((ch, cw, 3), np.float64)
     sq = np.zeros((ch, cw), np.float64)
     stats = np.zeros(2, np.uint64)

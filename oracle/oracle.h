@@ -144,6 +144,16 @@ typedef struct {
     uint32_t w, h;
 } orc_pt_env;
 
+/* an analytic light, same 80-byte layout as vkg_light (the reference's light_t) */
+typedef struct {
+    float position[3];
+    uint32_t type; /* 0 omni, 1 spot, 2 directional, 4 rect, 5 sphere, 6 tube, 7 disk */
+    float color[3], intensity;
+    float direction[3], range;
+    float spot_angle_scale, spot_angle_offset, angular_size, size_y;
+    float tangent[3], size_x;
+} orc_pt_light;
+
 typedef struct {
     uint32_t seed;
     uint32_t batch;
@@ -151,7 +161,14 @@ typedef struct {
     uint32_t max_depth, rr_depth, mis_mode, disable_material, draw_skybox;
     float max_path_beta, environment;
     uint32_t crop[4]; /* x0, y0, w, h (pixels of the full resolution camera) */
+    uint32_t num_lights, suppress_caustics;
+    const orc_pt_light *lights; /* the sun (if any) first */
 } orc_pt_settings;
+
+/* the sun of the tracer settings as a directional light (PBRPathTracer.cpp:610-624): propagation
+   direction = +z rotated by the quaternion of the Euler angles (elevation, azimuth, 0) */
+void orc_sun_light(const float color[3], float intensity, const float spherical_coords[2], float angular_size,
+                   orc_pt_light *out);
 
 /* an instanced scene for the FP64 oracle: meshes (each with the oracle's BVH) and instances with an
    object -> world 3x4 transform, a mesh and a material index into the scene's materials */

@@ -31,6 +31,8 @@ typedef struct {
     const uint8_t *twosided; /* by triangle id */
     uint32_t seed, batch, spp, max_depth, rr_depth, mis_mode, disable_material, draw_skybox;
     float max_path_beta, environment;
+    const orc_pt_light *lights;
+    uint32_t num_lights, suppress_caustics;
     uint32_t cx0, cy0, cw, ch;
     double *out, *sq;
     const orc_pt_instances *inst; /* NULL: single-level scene */
@@ -44,7 +46,7 @@ typedef struct {
 static inline float f_draw_raw(orc_pcg32 *g) { return orc_u01(orc_pcg32_next(g)); }
 
 static void f_hit_raw(const orc_pt_job *J, float ox, float oy, float oz, float tmin, float dx, float dy, float dz,
-                      uint32_t *prim, uint32_t *inst, float *u, float *v)
+                      uint32_t *prim, uint32_t *inst, float *u, float *v, float *t)
 {
     *inst = 0;
     orc_ray r = {{ox, oy, oz}, tmin, {dx, dy, dz}, 1e4f};
@@ -53,6 +55,31 @@ static void f_hit_raw(const orc_pt_job *J, float ox, float oy, float oz, float t
     *prim = h.prim;
     *u = h.u;
     *v = h.v;
+    *t = h.t;
+}
+
+/* light-NEE visibility (visibility_test.slang:94-131): 0 at the first opaque surface in (tmin, tmax),
+   else transmission x base colour of every transmissive surface crossed, nearest first */
+static void f_transmit_raw(const orc_pt_job *J, float ox, float oy, float oz, float dx, float dy, float dz, float tmax,
+                           float T[3])
+{
+    T[0] = T[1] = T[2] = 1.f;
+    float tmin = 0.f;
+    for(int k = 0;; ++k)
+    {
+        orc_ray r = {{ox, oy, oz}, tmin, {dx, dy, dz}, tmax};
+        orc_hit h;
+        orc_bvh_trace1(J->bvh, &r, 0, NULL, 0, &h, NULL);
+        if(h.prim == ORC_MISS) return;
+        const orc_pt_material *m = &J->scene->mats[J->scene->tri_mat[h.prim]];
+        if(!(m->transmission > 0.f) || k + 1 >= 32)
+        {
+            T[0] = T[1] = T[2] = 0.f;
+            return;
+        }
+        for(int c = 0; c < 3; ++c) T[c] = T[c] * m->base[c] * m->transmission;
+        tmin = h.t;
+    }
 }
 
 static int f_occluded_raw(const orc_pt_job *J, float ox, float oy, float oz, float dx, float dy, float dz)
@@ -177,11 +204,10 @@ static int d_trace_bvh(const orc_bvh *b, const uint8_t *twosided, int all_twosid
     return best != ORC_MISS;
 }
 
-static int d_trace(const orc_pt_job *J, const double o[3], double tmin, const double d[3], int cull_mode, int any,
-                   uint32_t *prim_out, double *u_out, double *v_out)
+static int d_trace(const orc_pt_job *J, const double o[3], double tmin, const double d[3], double tmax, int cull_mode,
+                   int any, uint32_t *prim_out, double *t_out, double *u_out, double *v_out)
 {
-    double t;
-    return d_trace_bvh(J->bvh, J->twosided, 0, o, tmin, d, 1e4, cull_mode, any, prim_out, &t, u_out, v_out);
+    return d_trace_bvh(J->bvh, J->twosided, 0, o, tmin, d, tmax, cull_mode, any, prim_out, t_out, u_out, v_out);
 }
 
 /* ---- instanced scenes (FP64) ----------------------------------------------------------------
@@ -375,8 +401,9 @@ static int slab(const double lo[3], const double hi[3], const double o[3], const
     return tmin <= tmax;
 }
 
-static int d_trace_inst(const orc_pt_job *J, const double o[3], double tmin, const double d[3], int cull_mode,
-                        int any, uint32_t *prim_out, uint32_t *inst_out, double *u_out, double *v_out)
+static int d_trace_inst(const orc_pt_job *J, const double o[3], double tmin, const double d[3], double tmax,
+                        int cull_mode, int any, uint32_t *prim_out, uint32_t *inst_out, double *t_out, double *u_out,
+                        double *v_out)
 {
     const orc_pt_instances *I = J->inst;
     const inst_bvh *B = (const inst_bvh *)J->ibvh;
@@ -384,7 +411,7 @@ static int d_trace_inst(const orc_pt_job *J, const double o[3], double tmin, con
     if(I->num_instances == 0) return 0;
     double inv[3];
     for(int a = 0; a < 3; ++a) inv[a] = d[a] != 0.0 ? 1.0 / d[a] : copysign(1e300, d[a]);
-    double best_t = 1e4, bu = 0, bv = 0;
+    double best_t = tmax, bu = 0, bv = 0;
     uint32_t stack[256];
     int sp = 0;
     stack[sp++] = 0;
@@ -427,6 +454,7 @@ static int d_trace_inst(const orc_pt_job *J, const double o[3], double tmin, con
     }
     *u_out = bu;
     *v_out = bv;
+    *t_out = best_t;
     return *prim_out != ORC_MISS;
 }
 
@@ -457,21 +485,46 @@ static void d_env_sample_raw(const orc_pt_env *e, double u0, double u1, double u
 }
 
 static void d_hit_raw(const orc_pt_job *J, double ox, double oy, double oz, double tmin, double dx, double dy,
-                      double dz, uint32_t *prim, uint32_t *inst, double *u, double *v)
+                      double dz, uint32_t *prim, uint32_t *inst, double *u, double *v, double *t)
 {
     double o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz};
     *u = *v = 0;
+    *t = 1e4;
     *inst = 0;
-    if(J->inst) d_trace_inst(J, o, tmin, d, 2, 0, prim, inst, u, v);
-    else d_trace(J, o, tmin, d, 2, 0, prim, u, v);
+    if(J->inst) d_trace_inst(J, o, tmin, d, 1e4, 2, 0, prim, inst, t, u, v);
+    else d_trace(J, o, tmin, d, 1e4, 2, 0, prim, t, u, v);
 }
 
 static int d_occluded_raw(const orc_pt_job *J, double ox, double oy, double oz, double dx, double dy, double dz)
 {
-    double o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz}, u, v;
+    double o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz}, u, v, t;
     uint32_t prim, inst;
-    if(J->inst) return d_trace_inst(J, o, 0.0, d, 0, 1, &prim, &inst, &u, &v);
-    return d_trace(J, o, 0.0, d, 0, 1, &prim, &u, &v);
+    if(J->inst) return d_trace_inst(J, o, 0.0, d, 1e4, 0, 1, &prim, &inst, &t, &u, &v);
+    return d_trace(J, o, 0.0, d, 1e4, 0, 1, &prim, &t, &u, &v);
+}
+
+static void d_transmit_raw(const orc_pt_job *J, double ox, double oy, double oz, double dx, double dy, double dz,
+                           double tmax, double T[3])
+{
+    double o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz}, tmin = 0.0;
+    T[0] = T[1] = T[2] = 1.0;
+    for(int k = 0;; ++k)
+    {
+        uint32_t prim, inst = 0;
+        double t, u, v;
+        int hit = J->inst ? d_trace_inst(J, o, tmin, d, tmax, 0, 0, &prim, &inst, &t, &u, &v)
+                          : d_trace(J, o, tmin, d, tmax, 0, 0, &prim, &t, &u, &v);
+        if(!hit) return;
+        const uint32_t mat = J->inst ? J->inst->inst_mat[inst] : J->scene->tri_mat[prim];
+        const orc_pt_material *m = &J->scene->mats[mat];
+        if(!(m->transmission > 0.f) || k + 1 >= 32)
+        {
+            T[0] = T[1] = T[2] = 0.0;
+            return;
+        }
+        for(int c = 0; c < 3; ++c) T[c] = T[c] * (double)m->base[c] * (double)m->transmission;
+        tmin = t;
+    }
 }
 
 /* ---- instantiate the estimator ------------------------------------------------------------- */
@@ -489,6 +542,8 @@ static int d_occluded_raw(const orc_pt_job *J, double ox, double oy, double oz, 
 #define OCC_RAW f_occluded_raw
 #define ENV_RAW f_env_sample_raw
 #define DRAW_RAW f_draw_raw
+#define TRANS_RAW f_transmit_raw
+#define RASIN(x) asinf(x)
 #include "pt_core.inc"
 #undef REAL
 #undef SFX
@@ -504,6 +559,8 @@ static int d_occluded_raw(const orc_pt_job *J, double ox, double oy, double oz, 
 #undef OCC_RAW
 #undef ENV_RAW
 #undef DRAW_RAW
+#undef TRANS_RAW
+#undef RASIN
 
 #define REAL double
 #define SFX(n) d_##n
@@ -519,7 +576,25 @@ static int d_occluded_raw(const orc_pt_job *J, double ox, double oy, double oz, 
 #define OCC_RAW d_occluded_raw
 #define ENV_RAW d_env_sample_raw
 #define DRAW_RAW d_draw_raw
+#define TRANS_RAW d_transmit_raw
+#define RASIN(x) asin(x)
 #include "pt_core.inc"
+
+void orc_sun_light(const float color[3], float intensity, const float spherical_coords[2], float angular_size,
+                   orc_pt_light *out)
+{
+    memset(out, 0, sizeof(*out));
+    out->type = 2;
+    for(int c = 0; c < 3; ++c) out->color[c] = color[c];
+    out->intensity = intensity;
+    /* q = q_y(azimuth) q_x(elevation); direction = q (0,0,1) q^-1 = (cos el sin az, -sin el, cos el cos az) */
+    double el = spherical_coords[0], az = spherical_coords[1];
+    double d[3] = {cos(el) * sin(az), -sin(el), cos(el) * cos(az)};
+    double len = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    for(int c = 0; c < 3; ++c) out->direction[c] = (float)(d[c] / len);
+    out->range = INFINITY;
+    out->angular_size = angular_size;
+}
 
 /* ---- single BSDF evaluations (FP64), for the sampling / evaluation consistency tests ---------- */
 void orc_bsdf_sample(const orc_pt_material *mt, const double n[3], const double v[3], double eta, const double u[3],
@@ -616,6 +691,9 @@ int orc_pt_render(int fp64, const orc_pt_scene *scene, const orc_bvh *bvh, const
     J.draw_skybox = set->draw_skybox;
     J.max_path_beta = set->max_path_beta;
     J.environment = set->environment;
+    J.lights = set->lights;
+    J.num_lights = set->lights ? set->num_lights : 0;
+    J.suppress_caustics = set->suppress_caustics;
     J.cx0 = set->crop[0];
     J.cy0 = set->crop[1];
     J.cw = set->crop[2] ? set->crop[2] : cam->width;
@@ -661,6 +739,9 @@ int orc_pt_render_instanced(const orc_pt_scene *scene, const orc_pt_instances *i
     J.draw_skybox = set->draw_skybox;
     J.max_path_beta = set->max_path_beta;
     J.environment = set->environment;
+    J.lights = set->lights;
+    J.num_lights = set->lights ? set->num_lights : 0;
+    J.suppress_caustics = set->suppress_caustics;
     J.cx0 = set->crop[0];
     J.cy0 = set->crop[1];
     J.cw = set->crop[2] ? set->crop[2] : cam->width;
@@ -694,6 +775,10 @@ void orc_pt_env_tables(const float *rgb, uint32_t w, uint32_t h, float *weight, 
         wt[t] = lum > 0 ? lum * sin(theta) : 0;
         total += wt[t];
     }
+    /* a black map: uniform weights (the GPU table builder's fallback), so pdfs stay finite */
+    if(!(total > 0))
+        for(size_t t = 0; t < n; ++t) wt[t] = 1.0;
+    if(!(total > 0)) total = (double)n;
     double run = 0;
     for(size_t t = 0; t < n; ++t)
     {

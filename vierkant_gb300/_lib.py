@@ -60,7 +60,21 @@ class vkg_settings(C.Structure):
                 ("max_trace_depth", C.c_uint32), ("max_path_beta", C.c_float), ("suspend_trace_when_done", C.c_uint32),
                 ("disable_material", C.c_uint32), ("mis_mode", C.c_uint32), ("draw_skybox", C.c_uint32),
                 ("environment", C.c_float), ("rr_start_depth", C.c_uint32), ("crop", C.c_uint32 * 4),
-                ("samples_per_wave", C.c_uint32)]
+                ("samples_per_wave", C.c_uint32), ("suppress_refractive_caustics", C.c_uint32),
+                ("sun_color", C.c_float * 3), ("sun_intensity", C.c_float), ("sun_spherical_coords", C.c_float * 2),
+                ("sun_angular_size", C.c_float)]
+
+
+class vkg_light(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("type", C.c_uint32), ("color", C.c_float * 3), ("intensity", C.c_float),
+                ("direction", C.c_float * 3), ("range", C.c_float), ("spot_angle_scale", C.c_float),
+                ("spot_angle_offset", C.c_float), ("angular_size", C.c_float), ("size_y", C.c_float),
+                ("tangent", C.c_float * 3), ("size_x", C.c_float)]
+
+
+class vkg_light_source(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("color", C.c_float * 3), ("intensity", C.c_float), ("range", C.c_float),
+                ("inner_cone_angle", C.c_float), ("outer_cone_angle", C.c_float), ("size", C.c_float * 2)]
 
 
 class vkg_tracer_create_info(C.Structure):
@@ -181,6 +195,8 @@ SIGNATURES = {
     "vkg_env_procedural_sky": (I32, [P, U32, U32, P, F32, F32, P, P]),
     "vkg_scene_create": (I32, [P, C.POINTER(vkg_scene_desc), C.POINTER(P), P]),
     "vkg_scene_destroy": (I32, [P, P]),
+    "vkg_scene_set_lights": (I32, [P, P, P, U32]),
+    "vkg_light_convert": (I32, [C.POINTER(vkg_light_source), P, P, C.POINTER(vkg_light)]),
     "vkg_scene_bvh": (I32, [P, C.POINTER(P)]),
     "vkg_scene_env_tables": (I32, [P, C.POINTER(P), C.POINTER(P), C.POINTER(U32), C.POINTER(U32)]),
     "vkg_settings_default": (I32, [C.POINTER(vkg_settings)]),

@@ -332,7 +332,8 @@ vkg_status enqueue(vkg_batch *b, const std::vector<vkg_batch::wave> &waves, cuda
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_s, 0, sizeof(uint32_t), st));
             k_pt_shade<MODE_PLAIN><<<grid, bs, 0, st>>>(J, depth, b->q_ray[a], b->q_pid[a], b->hits, b->hit_inst, cnt_in,
                                                        b->q_ray[1 - a], b->q_pid[1 - a], cnt_out, b->s_ray, b->s_pid,
-                                                       b->s_contrib, cnt_s, b->rng, b->beta_pdf, b->radiance, io);
+                                                       b->s_contrib, cnt_s, b->rng, b->beta_pdf, b->radiance, io,
+                                                       light_queue{});
             if(T.extend_kernel == 2)
             {
                 VKG_TRY_CUDA(ctx, cudaMemsetAsync(b->counters + 3, 0, sizeof(uint32_t), st));
@@ -347,7 +348,7 @@ vkg_status enqueue(vkg_batch *b, const std::vector<vkg_batch::wave> &waves, cuda
                 k_pt_shadow<job_table, 64><<<grid, bs, 0, st>>>(J, b->s_ray, b->s_pid, b->s_contrib, cnt_s, b->radiance);
             else
                 k_pt_shadow<<<grid, bs, 0, st>>>(J, b->s_ray, b->s_pid, b->s_contrib, cnt_s, b->radiance);
-            k_pt_tally<<<1, 1, 0, st>>>(cnt_in, cnt_s, b->totals);
+            k_pt_tally<<<1, 1, 0, st>>>(cnt_in, cnt_s, nullptr, b->totals);
             a = 1 - a;
         }
         k_batch_accumulate<<<(w.npix + 255) / 256, 256, 0, st>>>(ch, w.nchunks, w.npix, b->d_jd, b->radiance, b->sum);
@@ -449,6 +450,9 @@ vkg_status vkg_batch_create(vkg_ctx *ctx, const vkg_batch_job *jobs, uint32_t nj
         const vkg_batch_job &jb = jobs[j];
         if(!jb.scene) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_batch_create: job %u has no scene", j);
         if(vkg_status s = check_tracer_settings(ctx, &jb.settings); s != VKG_OK) return s;
+        if(!jb.scene->lights.empty() || jb.settings.sun_intensity > 0.f)
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
+                             "vkg_batch_create: job %u: analytic lights and the sun are rendered by vkg_tracer_render", j);
         if(jb.camera.width != jb.settings.resolution[0] || jb.camera.height != jb.settings.resolution[1])
             return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_batch_create: job %u camera size != resolution", j);
         uint32_t x0, y0, w, h;

@@ -10,6 +10,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <vector>
 
 namespace vkg
@@ -678,6 +679,31 @@ vkg_status vkg_scene_cornell(uint64_t seed, uint64_t stream, uint32_t num_sphere
             materials[3 + s] = mat;
         }
     }
+    return VKG_OK;
+}
+
+vkg_status vkg_light_convert(const vkg_light_source *src, const float rotation[9], const float translation[3],
+                             vkg_light *out)
+{
+    if(!src || !rotation || !translation || !out) return VKG_ERR_INVALID_ARGUMENT;
+    // convert_light (punctual_light.hpp:92-111): position from the translation, direction = R (0,0,-1),
+    // tangent = R (1,0,0), the spot cone as scale / offset of the cosine
+    vkg_light l{};
+    for(int c = 0; c < 3; ++c)
+    {
+        l.position[c] = translation[c];
+        l.color[c] = src->color[c];
+        l.direction[c] = -rotation[3 * c + 2];
+        l.tangent[c] = rotation[3 * c];
+    }
+    l.type = src->type;
+    l.intensity = src->intensity;
+    l.range = src->range > 0.f ? src->range : std::numeric_limits<float>::infinity();
+    l.spot_angle_scale = 1.f / std::max(0.001f, std::cos(src->inner_cone_angle) - std::cos(src->outer_cone_angle));
+    l.spot_angle_offset = -std::cos(src->outer_cone_angle) * l.spot_angle_scale;
+    l.size_x = src->size[0];
+    l.size_y = src->size[1];
+    *out = l;
     return VKG_OK;
 }
 

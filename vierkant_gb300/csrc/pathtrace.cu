@@ -58,7 +58,8 @@ struct vkg_tracer
     float *sum = nullptr;
     float *accum = nullptr;
     uint32_t *counters = nullptr;           // [0..1] queue lengths, [2] shadow queue length, [3] cache queries,
-                                            // [4] training records, [5] training batch length
+                                            // [4] training records, [5] training batch length, [6] work
+                                            // counter, [7] light shadow queue length
     unsigned long long *totals = nullptr;   // [0] extension rays, [1] shadow rays, [2] cache queries
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_train = nullptr;
     uint64_t last_paths = 0;
@@ -74,6 +75,12 @@ struct vkg_tracer
     float4 *rec = nullptr;         // training records: rec_cap x 5 float4, path-major
     uint32_t *vcount = nullptr;    // recorded interactions per training path
     float *t_feat = nullptr, *t_target = nullptr; // compacted training set: rec_cap x 13, rec_cap x 3
+    // analytic lights: the light list of the last render and the light-NEE shadow queue
+    vkg_light *d_lights = nullptr;
+    size_t lights_cap = 0, lq_cap = 0;
+    vkg_ray *l_ray = nullptr;
+    uint32_t *l_pid = nullptr;
+    float4 *l_contrib = nullptr;
 };
 
 namespace vkg
@@ -114,8 +121,9 @@ __global__ void k_check_instance_materials(const vkg_instance *__restrict__ inst
 
 // the material fields the BSDF divides by or takes as probabilities must be in range
 vkg_status check_material_values(vkg_ctx *ctx, const vkg_material *d_mats, uint32_t n, cudaStream_t st,
-                                 const char *fn)
+                                 const char *fn, bool *any_transmissive)
 {
+    *any_transmissive = false;
     std::vector<vkg_material> h(n);
     cudaError_t e = cudaMemcpyAsync(h.data(), d_mats, n * sizeof(vkg_material), cudaMemcpyDeviceToHost, st);
     if(e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -134,6 +142,7 @@ vkg_status check_material_values(vkg_ctx *ctx, const vkg_material *d_mats, uint3
            !std::isfinite(m.clearcoat))
             return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
                              "%s: material %u: clearcoat, clearcoat_roughness and sheen_roughness must be >= 0", fn, i);
+        *any_transmissive = *any_transmissive || m.transmission > 0.f;
     }
     return VKG_OK;
 }
@@ -239,6 +248,38 @@ vkg_status tracer_ensure(vkg_tracer *t, size_t paths, size_t npix)
     return VKG_OK;
 }
 
+// the light list on the device and a light-NEE shadow queue for `paths` paths
+vkg_status tracer_ensure_lights(vkg_tracer *t, const std::vector<vkg_light> &lights, size_t paths, cudaStream_t st)
+{
+    if(lights.empty()) return VKG_OK;
+    cudaError_t e = cudaSuccess;
+    if(lights.size() > t->lights_cap)
+    {
+        cudaFree(t->d_lights);
+        t->d_lights = nullptr;
+        t->lights_cap = 0;
+        e = cudaMalloc(&t->d_lights, lights.size() * sizeof(vkg_light));
+        if(e != cudaSuccess) return cuda_check(t->ctx, e, "light list");
+        t->lights_cap = lights.size();
+    }
+    if(paths > t->lq_cap)
+    {
+        for(void *p: {(void *)t->l_ray, (void *)t->l_pid, (void *)t->l_contrib}) cudaFree(p);
+        t->l_ray = nullptr;
+        t->l_pid = nullptr;
+        t->l_contrib = nullptr;
+        t->lq_cap = 0;
+        if(e == cudaSuccess) e = cudaMalloc(&t->l_ray, paths * sizeof(vkg_ray));
+        if(e == cudaSuccess) e = cudaMalloc(&t->l_pid, paths * sizeof(uint32_t));
+        if(e == cudaSuccess) e = cudaMalloc(&t->l_contrib, paths * sizeof(float4));
+        if(e != cudaSuccess) return cuda_check(t->ctx, e, "light shadow queue");
+        t->lq_cap = paths;
+    }
+    // pageable source: the copy is staged before the call returns
+    e = cudaMemcpyAsync(t->d_lights, lights.data(), lights.size() * sizeof(vkg_light), cudaMemcpyHostToDevice, st);
+    return e == cudaSuccess ? VKG_OK : cuda_check(t->ctx, e, "light list");
+}
+
 }// namespace
 }// namespace vkg
 
@@ -255,6 +296,10 @@ vkg_status vkg::check_tracer_settings(vkg_ctx *ctx, const vkg_settings *s)
     if(s->crop[2] && s->crop[3] &&
        ((uint64_t)s->crop[0] + s->crop[2] > s->resolution[0] || (uint64_t)s->crop[1] + s->crop[3] > s->resolution[1]))
         return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "settings: crop window outside the resolution");
+    if(!std::isfinite(s->sun_intensity) || s->sun_intensity < 0.f || !std::isfinite(s->sun_angular_size) ||
+       s->sun_angular_size < 0.f || !std::isfinite(s->sun_spherical_coords[0]) ||
+       !std::isfinite(s->sun_spherical_coords[1]))
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "settings: invalid sun parameters");
     return VKG_OK;
 }
 
@@ -297,7 +342,9 @@ vkg_status vkg_scene_create(vkg_ctx *ctx, const vkg_scene_desc *d, vkg_scene **o
         vkg_scene_destroy(ctx, sc);
         return cuda_check(ctx, e, "vkg_scene_create");
     }
-    if(vkg_status s = check_material_values(ctx, sc->mats, d->num_materials, st, "vkg_scene_create"); s != VKG_OK)
+    if(vkg_status s = check_material_values(ctx, sc->mats, d->num_materials, st, "vkg_scene_create",
+                                                 &sc->any_transmissive);
+       s != VKG_OK)
     {
         vkg_scene_destroy(ctx, sc);
         return s;
@@ -334,6 +381,46 @@ vkg_status vkg_scene_create(vkg_ctx *ctx, const vkg_scene_desc *d, vkg_scene **o
         return e != cudaSuccess ? cuda_check(ctx, e, "vkg_scene_create") : s;
     }
     *out = sc;
+    return VKG_OK;
+}
+
+vkg_status vkg_scene_set_lights(vkg_ctx *ctx, vkg_scene *sc, const vkg_light *lights, uint32_t n)
+{
+    if(!ctx) return VKG_ERR_INVALID_ARGUMENT;
+    if(!sc || (n && !lights)) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_set_lights: NULL argument");
+    std::vector<vkg_light> v(lights, lights + n);
+    auto finite = [](const float *p, int k) {
+        for(int i = 0; i < k; ++i)
+            if(!std::isfinite(p[i])) return false;
+        return true;
+    };
+    auto unit = [](float *p) {
+        const float l2 = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
+        if(!(l2 > 0.f) || !std::isfinite(l2)) return false;
+        const float inv = 1.f / std::sqrt(l2);
+        for(int i = 0; i < 3; ++i) p[i] *= inv;
+        return true;
+    };
+    for(uint32_t i = 0; i < n; ++i)
+    {
+        vkg_light &l = v[i];
+        const uint32_t ty = l.type;
+        if(ty > VKG_LIGHT_DISK || ty == VKG_LIGHT_AREA)
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_set_lights: light %u: unsupported type %u", i, ty);
+        if(!finite(l.position, 3) || !finite(l.color, 3) || !std::isfinite(l.intensity) || l.intensity < 0.f ||
+           !(l.range > 0.f) || !std::isfinite(l.spot_angle_scale) || !std::isfinite(l.spot_angle_offset) ||
+           !std::isfinite(l.angular_size) || l.angular_size < 0.f)
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_set_lights: light %u: invalid parameters", i);
+        const bool area = ty >= VKG_LIGHT_RECT;
+        if(ty != VKG_LIGHT_OMNI && ty != VKG_LIGHT_SPHERE && !unit(l.direction))
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_set_lights: light %u: zero direction", i);
+        if(ty == VKG_LIGHT_RECT && !unit(l.tangent))
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_set_lights: light %u: zero tangent", i);
+        if(area && (!(l.size_x > 0.f) || !std::isfinite(l.size_x) ||
+                    ((ty == VKG_LIGHT_RECT || ty == VKG_LIGHT_TUBE) && (!(l.size_y > 0.f) || !std::isfinite(l.size_y)))))
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_set_lights: light %u: area lights need sizes > 0", i);
+    }
+    sc->lights = std::move(v);
     return VKG_OK;
 }
 
@@ -383,7 +470,8 @@ vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_de
     chk(cudaMalloc(&sc->mats, d->num_materials * sizeof(vkg_material)));
     chk(cudaMemcpyAsync(sc->mats, d->d_materials, d->num_materials * sizeof(vkg_material), cudaMemcpyDeviceToDevice, st));
     if(e != cudaSuccess) return fail(cuda_check(ctx, e, "vkg_scene_create_instanced"));
-    if(vkg_status s = check_material_values(ctx, sc->mats, d->num_materials, st, "vkg_scene_create_instanced");
+    if(vkg_status s = check_material_values(ctx, sc->mats, d->num_materials, st, "vkg_scene_create_instanced",
+                                                 &sc->any_transmissive);
        s != VKG_OK)
         return fail(s);
     std::vector<mesh_ref> refs(d->num_meshes);
@@ -589,7 +677,13 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
     if(ccfg)
         if(vkg_status s = tracer_ensure_cache(t, cache_render ? paths : 0u); s != VKG_OK) return s;
 
+    const std::vector<vkg_light> lights = render_lights(sc, S);
+    if(vkg_status s = tracer_ensure_lights(t, lights, paths + train_paths, st); s != VKG_OK) return s;
     pt_params P = make_params(sc, *cam, S, t->seed, t->batch);
+    P.lights = lights.empty() ? nullptr : t->d_lights;
+    P.num_lights = (uint32_t)lights.size();
+    uint32_t *cnt_l = lights.empty() ? nullptr : t->counters + 7;
+    const light_queue lq{t->l_ray, t->l_pid, t->l_contrib, cnt_l};
     P.term_depth = cache_render ? ccfg->terminate_depth : 0xFFFFFFFFu;
     P.rec_depth = rec_depth;
     P.train_paths = train_paths;
@@ -648,11 +742,12 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
                 k_pt_extend<<<grid, PT_THREADS, 0, st>>>(SS, t->q_ray[a], t->q_pid[a], cnt_in, t->hits, t->hit_inst);
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_out, 0, sizeof(uint32_t), st));
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_s, 0, sizeof(uint32_t), st));
+            if(cnt_l) VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_l, 0, sizeof(uint32_t), st));
 #define VKG_SHADE(M)                                                                                                   \
     k_pt_shade<M><<<grid, PT_THREADS, 0, st>>>(SS, depth, t->q_ray[a], t->q_pid[a], t->hits, t->hit_inst, cnt_in,        \
                                                t->q_ray[1 - a],                                                          \
                                                t->q_pid[1 - a], cnt_out, t->s_ray, t->s_pid, t->s_contrib, cnt_s,         \
-                                               t->rng, t->beta_pdf, t->radiance, io)
+                                               t->rng, t->beta_pdf, t->radiance, io, lq)
             if(mode == MODE_PLAIN) VKG_SHADE(MODE_PLAIN);
             else VKG_SHADE(MODE_CACHE);
 #undef VKG_SHADE
@@ -668,7 +763,14 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
             else if(!empty)
                 k_pt_shadow<<<grid, PT_THREADS, 0, st>>>(SS, t->s_ray, t->s_pid, t->s_contrib, cnt_s,
                                                          t->radiance);
-            k_pt_tally<<<1, 1, 0, st>>>(cnt_in, cnt_s, t->totals);
+            if(cnt_l && !empty)
+            {
+                if(small_stack)
+                    k_pt_light_shadow<single_scene, 64><<<grid, PT_THREADS, 0, st>>>(SS, lq, t->radiance);
+                else
+                    k_pt_light_shadow<<<grid, PT_THREADS, 0, st>>>(SS, lq, t->radiance);
+            }
+            k_pt_tally<<<1, 1, 0, st>>>(cnt_in, cnt_s, cnt_l, t->totals);
             a = 1 - a;
         }
         if(cache_render)
@@ -760,6 +862,7 @@ vkg_status vkg_tracer_destroy(vkg_tracer *t)
     tracer_free_buffers(t);
     tracer_free_cache_buffers(t);
     cudaFree(t->counters);
+    for(void *p: {(void *)t->d_lights, (void *)t->l_ray, (void *)t->l_pid, (void *)t->l_contrib}) cudaFree(p);
     cudaFree(t->totals);
     if(t->ev0) cudaEventDestroy(t->ev0);
     if(t->ev1) cudaEventDestroy(t->ev1);

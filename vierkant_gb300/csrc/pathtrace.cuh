@@ -23,6 +23,11 @@ constexpr float PT_ONE_OVER_PI = 0.31830988618379067154f;
 constexpr float PT_EPS = 1e-4f;     // ray::EPS (ray_common.slang:12)
 constexpr float PT_PDF_EPS = 1e-3f; // ray::PDF_EPS (ray_common.slang:13)
 constexpr float PT_TMAX = 1e4f;     // ray::DEFAULT_TMAX (ray_common.slang:15)
+constexpr float PT_REGULARIZE_PDF_THRESHOLD = 1e3f; // raypipeline.slang:24
+constexpr float PT_REGULARIZE_MIN_ROUGHNESS = 0.25f; // raypipeline.slang:25
+// path flag bits (stored in the .w word of the path's radiance record)
+constexpr uint32_t PATH_REGULARIZE = 1u; // a bounce with pdf < PT_REGULARIZE_PDF_THRESHOLD happened
+constexpr uint32_t PATH_CAUSTIC = 2u;    // the reference's caustic_path marker
 
 struct env_alias
 {

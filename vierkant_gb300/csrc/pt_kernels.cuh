@@ -6,10 +6,13 @@
 #pragma once
 
 #include "nrc.cuh"
+#include "light.cuh"
 #include "pathtrace.cuh"
 #include "tlas.cuh"
 #include "traverse.cuh"
 
+#include <cmath>
+#include <limits>
 #include <vector>
 
 namespace vkg
@@ -39,6 +42,8 @@ struct vkg_scene
     std::vector<uint32_t *> mesh_idx;
     vkg::mesh_ref *d_meshes = nullptr;
     uint32_t num_instances = 0;
+    bool any_transmissive = false;  // a material with transmission > 0 (light shadow rays pass through it)
+    std::vector<vkg_light> lights;  // analytic lights (host copy; the tracer uploads them per render)
 };
 
 namespace vkg
@@ -74,6 +79,9 @@ struct pt_params
     uint32_t rec_depth;   // interactions recorded per training path
     uint32_t train_base;  // paths [train_base, train_base + train_paths) of the wave are training paths
     uint32_t train_paths;
+    // analytic lights (the sun first) and the switches of their estimators
+    const vkg_light *lights;
+    uint32_t num_lights, suppress_caustics, transmissive;
 };
 
 // the shade kernel's two modes
@@ -93,6 +101,15 @@ struct cache_io
 };
 
 constexpr int REC_F4 = 5; // float4 per training record
+
+// the light-NEE shadow queue (count == nullptr: the scene has no lights)
+struct light_queue
+{
+    vkg_ray *ray;
+    uint32_t *pid;
+    float4 *contrib;
+    uint32_t *count;
+};
 
 __device__ __forceinline__ uint64_t path_seq(const pt_params &P, uint32_t pid)
 {
@@ -260,7 +277,7 @@ __global__ void __launch_bounds__(PT_THREADS)
                    uint32_t *__restrict__ out_pid, uint32_t *__restrict__ out_count, vkg_ray *__restrict__ s_ray,
                    uint32_t *__restrict__ s_pid, float4 *__restrict__ s_contrib, uint32_t *__restrict__ s_count,
                    uint64_t *__restrict__ rng, float4 *__restrict__ beta_pdf, float4 *__restrict__ radiance,
-                   cache_io io)
+                   cache_io io, light_queue lq)
 {
     const uint32_t n = *in_count;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -268,10 +285,10 @@ __global__ void __launch_bounds__(PT_THREADS)
     {
         const uint32_t i = base + threadIdx.x;
         const bool active = i < n;
-        bool push_ext = false, push_shadow = false, push_query = false;
+        bool push_ext = false, push_shadow = false, push_query = false, push_light = false;
         float3 P0 = f3(0.f, 0.f, 0.f), ndir = P0, sdir = P0, N = P0;
-        float3 contrib = P0, qbeta = P0, albedo = P0, vq = P0;
-        float rough = 0.f;
+        float3 contrib = P0, qbeta = P0, albedo = P0, vq = P0, ldir_s = P0, lcontrib = P0;
+        float rough = 0.f, ldist = 0.f;
         uint32_t pid = 0;
         if(active)
         {
@@ -282,15 +299,50 @@ __global__ void __launch_bounds__(PT_THREADS)
             const float3 dir = f3(r1.x, r1.y, r1.z);
             const uint4 h = reinterpret_cast<const uint4 *>(hits)[i];
             pcg32 g{rng[pid], S.inc(pid)};
-            float u[8];
-            for(int k = 0; k < 8; ++k) u[k] = u01(pcg32_next(g));
+            // 8 draws per segment; 3 more (light pick, point on the light) when the scene has lights
+            float u[11];
+            const int nu = P.num_lights ? 11 : 8;
+            for(int k = 0; k < 11; ++k) u[k] = k < nu ? u01(pcg32_next(g)) : 0.f;
             const float4 bp = beta_pdf[pid];
             float3 beta = f3(bp.x, bp.y, bp.z);
             float prev_pdf = bp.w;
             const float4 lr = radiance[pid];
             float3 L = f3(lr.x, lr.y, lr.z);
+            uint32_t flags = __float_as_uint(lr.w); // PATH_REGULARIZE | PATH_CAUSTIC
+            const bool light_hits = P.num_lights && !(P.suppress_caustics && (flags & PATH_CAUSTIC));
+            if(light_hits)
+            {
+                // light bodies the segment passed (raypipeline.slang:196-224): additive emitters,
+                // MIS-weighted against their NEE strategy
+                const float4 r0 = rp[0];
+                const float3 o = f3(r0.x, r0.y, r0.z);
+                const float t_end = h.x == VKG_MISS ? r1.w : __uint_as_float(h.y);
+                const float inv_n = 1.f / (float)P.num_lights;
+                for(uint32_t li = 0; li < P.num_lights; ++li)
+                {
+                    const vkg_light &l = P.lights[li];
+                    const float2 lh = intersect_light(l, o, dir);
+                    if(lh.x <= r0.w || lh.x >= t_end) continue;
+                    const float w = mis_weight_hit(P.mis_mode, prev_pdf, light_pdf(l, o, dir) * inv_n);
+                    L = L + beta * lv3(l.color) * (w * l.intensity);
+                }
+            }
             if(h.x == VKG_MISS)
             {
+                if(light_hits)
+                {
+                    // sun discs seen by the ray (eval_distant_lights, raypipeline.slang:728-744)
+                    const float inv_n = 1.f / (float)P.num_lights;
+                    for(uint32_t li = 0; li < P.num_lights; ++li)
+                    {
+                        const vkg_light &l = P.lights[li];
+                        if(l.type != VKG_LIGHT_DIRECTIONAL) continue;
+                        const float pdf = light_pdf(l, f3(0.f, 0.f, 0.f), dir);
+                        if(pdf <= 0.f) continue;
+                        const float w = mis_weight_hit(P.mis_mode, prev_pdf, pdf * inv_n);
+                        L = L + beta * lv3(l.color) * (w * l.intensity);
+                    }
+                }
                 // miss_environment (raypipeline.slang:764-781) with the hit-side MIS weight
                 const uint32_t t = env_texel(dir, P.env.w, P.env.h);
                 float3 le = env_radiance(P.env, t);
@@ -312,7 +364,10 @@ __global__ void __launch_bounds__(PT_THREADS)
                 const bool back_face = !(dot(ng, dir) < 0.f);
                 N = back_face ? -ng : ng; // shading normal faces the incoming ray
                 const float3 V = -dir;
-                const material_view m = load_material(P.mats, mat, P.disable_material);
+                material_view m = load_material(P.mats, mat, P.disable_material);
+                // path regularisation (raypipeline.slang:611): after a non-peaked bounce, later vertices
+                // shade (sample and NEE) with roughness >= 0.25
+                if(flags & PATH_REGULARIZE) m.roughness = fmaxf(m.roughness, PT_REGULARIZE_MIN_ROUGHNESS);
                 const float eta = hit_eta(P.mats, mat, back_face);
                 const float *em = P.mats[mat].emission;
                 L = L + beta * f3(em[0], em[1], em[2]);
@@ -364,11 +419,40 @@ __global__ void __launch_bounds__(PT_THREADS)
                         }
                     }
                 }
+                // next-event estimation against one uniformly picked light (nee_surface,
+                // direct_lighting.slang:297-332); its shadow ray passes transmissive surfaces
+                if(!push_query && P.num_lights)
+                {
+                    const uint32_t nl = P.num_lights;
+                    const uint32_t li = nl > 1 ? min((uint32_t)(u[8] * (float)nl), nl - 1u) : 0u;
+                    const vkg_light &l = P.lights[li];
+                    const light_sample ls = sample_light(l, P0, u[9], u[10]);
+                    if(max3(ls.radiance) > 0.f)
+                    {
+                        const float cosl = fmaxf(dot(N, ls.dir), 0.f);
+                        float pdf_b = 0.f;
+                        const float3 f = eval_bsdf(m, ls.dir, N, V, eta, pdf_b);
+                        const float w = bsdf_reachable(l) ? mis_weight_nee(P.mis_mode, ls.pdf / (float)nl, pdf_b) : 1.f;
+                        lcontrib = beta * f * ls.radiance * (w * (float)nl * cosl / ls.pdf);
+                        if(max3(lcontrib) > 0.f)
+                        {
+                            push_light = true;
+                            ldir_s = ls.dir;
+                            ldist = ls.dist;
+                        }
+                    }
+                }
                 // BSDF sample (sample_disney) and throughput
                 const bsdf_sample bs = sample_bsdf(m, N, V, eta, u[0], u[1], u[2]);
                 bool alive = bs.pdf > 0.f && !push_query;
                 if(alive)
                 {
+                    // raypipeline.slang:632-637: a bounce with pdf below the threshold turns
+                    // regularisation on; the refractive-caustic marker follows the same test
+                    const bool below = bs.pdf < PT_REGULARIZE_PDF_THRESHOLD;
+                    const bool caustic = below && ((flags & PATH_CAUSTIC) || bs.transmission);
+                    flags = (flags | (below ? PATH_REGULARIZE : 0u)) & ~PATH_CAUSTIC;
+                    if(caustic) flags |= PATH_CAUSTIC;
                     const float cost = fabsf(dot(N, bs.dir));
                     float3 tp = bs.f * (cost / fmaxf(bs.pdf, PT_PDF_EPS));
                     if(depth >= 1 && P.max_path_beta > 0.f)
@@ -404,7 +488,7 @@ __global__ void __launch_bounds__(PT_THREADS)
             }
             rng[pid] = g.state;
             beta_pdf[pid] = make_float4(beta.x, beta.y, beta.z, prev_pdf);
-            radiance[pid] = make_float4(L.x, L.y, L.z, 0.f);
+            radiance[pid] = make_float4(L.x, L.y, L.z, __uint_as_float(flags));
         }
         const uint32_t pe = warp_push(out_count, push_ext);
         if(push_ext)
@@ -423,6 +507,19 @@ __global__ void __launch_bounds__(PT_THREADS)
             o[1] = make_float4(sdir.x, sdir.y, sdir.z, PT_TMAX);
             s_pid[ps] = pid;
             s_contrib[ps] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
+        }
+        if(lq.count)
+        {
+            const uint32_t pl = warp_push(lq.count, push_light);
+            if(push_light)
+            {
+                const float3 so = P0 + N * PT_EPS;
+                float4 *o = reinterpret_cast<float4 *>(lq.ray + pl);
+                o[0] = make_float4(so.x, so.y, so.z, 0.f);
+                o[1] = make_float4(ldir_s.x, ldir_s.y, ldir_s.z, ldist);
+                lq.pid[pl] = pid;
+                lq.contrib[pl] = make_float4(lcontrib.x, lcontrib.y, lcontrib.z, 0.f);
+            }
         }
         if constexpr(MODE == MODE_CACHE)
         {
@@ -476,6 +573,83 @@ __global__ void __launch_bounds__(PT_THREADS)
             L.x += c.x;
             L.y += c.y;
             L.z += c.z;
+            radiance[pid] = L;
+        }
+    }
+}
+
+// light-NEE visibility (transmittance_test, visibility_test.slang:94-131): 0 at the first opaque
+// surface on the segment, else the product of transmission x base colour over the transmissive
+// surfaces it crosses, found nearest first by repeated closest-hit queries from the last crossing
+// (at most PT_MAX_CROSSINGS; more count as blocked). Scenes without transmissive materials take
+// one any-hit query. Runs after the environment shadow kernel, so each path's radiance has one
+// writer at a time.
+constexpr int PT_MAX_CROSSINGS = 32;
+
+template<class J, int STACK = (int)TRAVERSAL_STACK>
+__global__ void __launch_bounds__(PT_THREADS) k_pt_light_shadow(J S, light_queue lq, float4 *__restrict__ radiance)
+{
+    const uint32_t n = *lq.count;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        const uint32_t pid = lq.pid[i];
+        const pt_params &P = S.params(J::per_path ? pid : 0u);
+        const float4 *rp = reinterpret_cast<const float4 *>(lq.ray + i);
+        const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
+        float3 T = f3(1.f, 1.f, 1.f);
+        unsigned long long v = 0, c = 0;
+        if(!P.transmissive)
+        {
+            const bool occ = P.two_level ? trace_tlas<true>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z, r0.w,
+                                                            r1.x, r1.y, r1.z, r1.w, CULL_NONE)
+                                                   .occluded
+                                         : trace_ray<true, false, STACK>(P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x,
+                                                                         r1.y, r1.z, r1.w, CULL_NONE, v, c, nullptr)
+                                                   .occluded;
+            if(occ) T = f3(0.f, 0.f, 0.f);
+        }
+        else
+        {
+            float tmin = r0.w;
+            for(int k = 0;; ++k)
+            {
+                uint32_t prim, mat;
+                float t;
+                if(P.two_level)
+                {
+                    const tlas_result r = trace_tlas<false>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z, tmin,
+                                                            r1.x, r1.y, r1.z, r1.w, CULL_NONE);
+                    prim = r.prim;
+                    t = r.t;
+                    mat = prim == VKG_MISS ? 0u : __ldg(&P.tl_by_id[r.inst].material);
+                }
+                else
+                {
+                    const trace_result r = trace_ray<false, false, STACK>(P.nodes, P.tris, r0.x, r0.y, r0.z, tmin, r1.x,
+                                                                          r1.y, r1.z, r1.w, CULL_NONE, v, c, nullptr);
+                    prim = r.prim;
+                    t = r.t;
+                    mat = prim == VKG_MISS ? 0u : __ldg(&P.tri_mat[prim]);
+                }
+                if(prim == VKG_MISS) break;
+                const vkg_material &q = P.mats[mat];
+                if(!(q.transmission > 0.f) || k + 1 >= PT_MAX_CROSSINGS)
+                {
+                    T = f3(0.f, 0.f, 0.f);
+                    break;
+                }
+                T = T * f3(q.base_color[0], q.base_color[1], q.base_color[2]) * q.transmission;
+                tmin = t;
+            }
+        }
+        if(max3(T) > 0.f)
+        {
+            const float4 cc = lq.contrib[i];
+            float4 L = radiance[pid];
+            L.x += T.x * cc.x;
+            L.y += T.y * cc.y;
+            L.z += T.z * cc.z;
             radiance[pid] = L;
         }
     }
@@ -634,10 +808,10 @@ __global__ void k_fill_miss_queue(const uint32_t *__restrict__ count, vkg_hit *_
 }
 
 __global__ void k_pt_tally(const uint32_t *__restrict__ ext_count, const uint32_t *__restrict__ s_count,
-                           unsigned long long *__restrict__ totals)
+                           const uint32_t *__restrict__ l_count, unsigned long long *__restrict__ totals)
 {
     totals[0] += *ext_count;
-    totals[1] += *s_count;
+    totals[1] += *s_count + (l_count ? *l_count : 0u);
 }
 
 // rendering with a cache: path radiance += throughput x prediction (negative outputs clamped)
@@ -802,6 +976,44 @@ inline pt_params make_params(const vkg_scene *sc, const vkg_camera &cam, const v
     P.rec_depth = 0;
     P.train_base = 0xFFFFFFFFu;
     P.train_paths = 0;
+    P.lights = nullptr;
+    P.num_lights = 0;
+    P.suppress_caustics = S.suppress_refractive_caustics;
+    P.transmissive = sc->any_transmissive ? 1u : 0u;
     return P;
+}
+
+// the light list of a render: the settings' sun (PBRPathTracer.cpp:610-624) first, then the scene's
+inline std::vector<vkg_light> render_lights(const vkg_scene *sc, const vkg_settings &S)
+{
+    std::vector<vkg_light> out;
+    if(S.sun_intensity > 0.f)
+    {
+        vkg_light sun{};
+        sun.type = VKG_LIGHT_DIRECTIONAL;
+        for(int c = 0; c < 3; ++c) sun.color[c] = S.sun_color[c];
+        sun.intensity = S.sun_intensity;
+        // the propagation direction: +z rotated by the quaternion of the Euler angles
+        // (elevation, azimuth, 0), normalised
+        const float hx = 0.5f * S.sun_spherical_coords[0], hy = 0.5f * S.sun_spherical_coords[1];
+        const float cx = std::cos(hx), sx = std::sin(hx), cy = std::cos(hy), sy = std::sin(hy);
+        const float qw = cx * cy, qx = sx * cy, qy = cx * sy, qz = -sx * sy;
+        // v' = v + 2 w (q x v) + 2 q x (q x v) for v = (0, 0, 1)
+        const float ax = qy, ay = -qx, az = 0.f;                                  // q x v
+        const float bx = qy * az - qz * ay, by = qz * ax - qx * az, bz = qx * ay - qy * ax; // q x (q x v)
+        float d[3] = {2.f * qw * ax + 2.f * bx, 2.f * qw * ay + 2.f * by, 1.f + 2.f * qw * az + 2.f * bz};
+        const float len2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if(len2 > 0.f)
+        {
+            const float inv = 1.f / std::sqrt(len2);
+            for(float &x: d) x *= inv;
+        }
+        for(int c = 0; c < 3; ++c) sun.direction[c] = d[c];
+        sun.range = std::numeric_limits<float>::infinity();
+        sun.angular_size = S.sun_angular_size;
+        out.push_back(sun);
+    }
+    out.insert(out.end(), sc->lights.begin(), sc->lights.end());
+    return out;
 }
 }// namespace vkg

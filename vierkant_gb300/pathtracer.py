@@ -17,7 +17,8 @@ import math
 import numpy as np
 import torch
 
-from ._lib import (check, lib, vkg_bvh_info, vkg_camera, vkg_scene_desc, vkg_settings, vkg_tracer_create_info,
+from ._lib import (check, lib, vkg_bvh_info, vkg_camera, vkg_light, vkg_light_source, vkg_scene_desc, vkg_settings,
+                   vkg_tracer_create_info,
                    vkg_tracer_stats)
 from .raytracing import Context
 
@@ -43,7 +44,70 @@ def procedural_sky(ctx: Context, width=2048, height=1024, sun_dir=None, sun_peak
     return out
 
 
-class Scene:
+# analytic lights: the reference's LightType values and the 80-byte light record
+LIGHT_OMNI, LIGHT_SPOT, LIGHT_DIRECTIONAL, LIGHT_RECT, LIGHT_SPHERE, LIGHT_TUBE, LIGHT_DISK = 0, 1, 2, 4, 5, 6, 7
+LIGHT_DTYPE = np.dtype([("position", "<f4", 3), ("type", "<u4"), ("color", "<f4", 3), ("intensity", "<f4"),
+                        ("direction", "<f4", 3), ("range", "<f4"), ("spot_angle_scale", "<f4"),
+                        ("spot_angle_offset", "<f4"), ("angular_size", "<f4"), ("size_y", "<f4"),
+                        ("tangent", "<f4", 3), ("size_x", "<f4")])
+assert LIGHT_DTYPE.itemsize == C.sizeof(vkg_light)
+
+
+def convert_light(type, color=(1.0, 1.0, 1.0), intensity=1.0, range=math.inf, inner_cone_angle=0.0,
+                  outer_cone_angle=math.pi / 4, size=(1.0, 1.0), rotation=None, translation=(0.0, 0.0, 0.0)):
+    """A light record from a light-source asset placed by an object transform (row-major 3x3 rotation,
+    translation), as the reference's convert_light does; returns one LIGHT_DTYPE element."""
+    src = vkg_light_source(type, (C.c_float * 3)(*color), intensity, range, inner_cone_angle, outer_cone_angle,
+                           (C.c_float * 2)(*size))
+    rot = np.ascontiguousarray(np.eye(3) if rotation is None else rotation, np.float32).reshape(9)
+    tr = np.ascontiguousarray(translation, np.float32)
+    out = vkg_light()
+    check(lib().vkg_light_convert(C.byref(src), rot.ctypes.data_as(C.c_void_p), tr.ctypes.data_as(C.c_void_p),
+                                  C.byref(out)))
+    return np.frombuffer(bytes(out), LIGHT_DTYPE, count=1)[0]
+
+
+def cornell_lights(intensity_scale: float = 1.0) -> np.ndarray:
+    """One light of every analytic type inside the Cornell box ([-1, 1]^3, open toward +z): a rect on
+    the ceiling facing down, a sphere, a spot, a tube along x, a disk on the back wall and an omni."""
+    L = np.zeros(6, LIGHT_DTYPE)
+    rows = [
+        dict(type=LIGHT_RECT, position=(0.0, 0.98, 0.0), direction=(0, -1, 0), tangent=(1, 0, 0), size_x=0.25,
+             size_y=0.25, color=(1.0, 0.9, 0.8), intensity=8.0),
+        dict(type=LIGHT_SPHERE, position=(-0.6, 0.6, -0.5), size_x=0.15, color=(0.9, 0.9, 1.0), intensity=6.0),
+        dict(type=LIGHT_SPOT, position=(0.6, 0.9, 0.3), direction=(-0.2, -1, 0), color=(1.0, 1.0, 0.9),
+             intensity=3.0),
+        dict(type=LIGHT_TUBE, position=(0.3, 0.2, -0.8), direction=(1, 0, 0), size_x=0.06, size_y=0.3,
+             color=(0.8, 1.0, 0.8), intensity=5.0),
+        dict(type=LIGHT_DISK, position=(0.0, 0.5, -0.99), direction=(0, 0, 1), size_x=0.15, color=(1.0, 0.8, 0.8),
+             intensity=6.0),
+        dict(type=LIGHT_OMNI, position=(-0.7, -0.5, 0.5), color=(1.0, 1.0, 1.0), intensity=0.5),
+    ]
+    for i, r in enumerate(rows):
+        L[i]["range"] = np.inf
+        L[i]["spot_angle_scale"], L[i]["spot_angle_offset"] = 1.0, 0.0
+        for k, v in r.items():
+            L[i][k] = v
+        d = np.asarray(L[i]["direction"], np.float64)
+        if np.any(d):
+            L[i]["direction"] = d / np.linalg.norm(d)
+        L[i]["intensity"] *= intensity_scale
+    # the spot cone: inner 0.3 rad, outer 0.6 rad (convert_light's scale / offset)
+    sc = 1.0 / max(0.001, math.cos(0.3) - math.cos(0.6))
+    L[2]["spot_angle_scale"], L[2]["spot_angle_offset"] = sc, -math.cos(0.6) * sc
+    return L
+
+
+class _Lights:
+    def set_lights(self, lights):
+        """Analytic lights of the scene (LIGHT_DTYPE records; empty removes them)."""
+        arr = np.ascontiguousarray(np.asarray(lights, LIGHT_DTYPE).reshape(-1))
+        check(lib().vkg_scene_set_lights(self.ctx.handle, self.handle,
+                                         arr.ctypes.data_as(C.c_void_p) if len(arr) else None, len(arr)),
+              self.ctx.handle, "vkg_scene_set_lights")
+
+
+class Scene(_Lights):
     def __init__(self, ctx: Context, xyz, indices, tri_material, materials, env_rgb, leaf_max=4):
         dev = f"cuda:{ctx.device}"
 
@@ -95,7 +159,7 @@ class Scene:
             pass
 
 
-class InstancedScene:
+class InstancedScene(_Lights):
     """A two-level scene: meshes [(xyz, indices, twosided)] each with its own BVH, instances
     (raytracing.INSTANCE_DTYPE: object -> world transform, mesh, material) under a top-level BVH,
     materials (MATERIAL_DTYPE) and the environment map. Renders with PBRPathTracer like Scene."""
