@@ -144,6 +144,7 @@ struct vkg_batch
     std::vector<batch_job_dev> jdev;
     uint32_t njobs = 0, total_pix = 0, max_depth = 0;
     bool any_instanced = false;
+    bool any_full = false; // a job scene with materials beyond metal-roughness
     uint32_t max_bvh_depth = 0;
     uint64_t total_paths = 0;
     vkg_batch_tuning tuning{};
@@ -330,7 +331,15 @@ vkg_status enqueue(vkg_batch *b, const std::vector<vkg_batch::wave> &waves, cuda
                 k_pt_extend<<<grid, bs, 0, st>>>(J, b->q_ray[a], b->q_pid[a], cnt_in, b->hits, b->hit_inst);
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_out, 0, sizeof(uint32_t), st));
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_s, 0, sizeof(uint32_t), st));
-            k_pt_shade<MODE_PLAIN><<<grid, bs, 0, st>>>(J, depth, b->q_ray[a], b->q_pid[a], b->hits, b->hit_inst, cnt_in,
+            if(b->any_full)
+                k_pt_shade<MODE_PLAIN, job_table, true><<<grid, bs, 0, st>>>(J, depth, b->q_ray[a], b->q_pid[a], b->hits,
+                                                                             b->hit_inst, cnt_in, b->q_ray[1 - a],
+                                                                             b->q_pid[1 - a], cnt_out, b->s_ray,
+                                                                             b->s_pid, b->s_contrib, cnt_s, b->rng,
+                                                                             b->beta_pdf, b->radiance, io,
+                                                                             light_queue{});
+            else
+            k_pt_shade<MODE_PLAIN, job_table, false><<<grid, bs, 0, st>>>(J, depth, b->q_ray[a], b->q_pid[a], b->hits, b->hit_inst, cnt_in,
                                                        b->q_ray[1 - a], b->q_pid[1 - a], cnt_out, b->s_ray, b->s_pid,
                                                        b->s_contrib, cnt_s, b->rng, b->beta_pdf, b->radiance, io,
                                                        light_queue{});
@@ -472,6 +481,7 @@ vkg_status vkg_batch_create(vkg_ctx *ctx, const vkg_batch_job *jobs, uint32_t nj
         const vkg_batch_job &jb = jobs[j];
         b->params.push_back(make_params(jb.scene, jb.camera, jb.settings, jb.seed, 0));
         b->any_instanced = b->any_instanced || jb.scene->tlas != nullptr;
+        b->any_full = b->any_full || jb.scene->any_full;
         if(jb.scene->bvh) b->max_bvh_depth = std::max(b->max_bvh_depth, jb.scene->bvh->depth);
         const uint32_t npix = b->params.back().npix;
         b->jdev.push_back(batch_job_dev{npix, jb.settings.num_samples, off, jb.d_rgb_out});

@@ -121,9 +121,10 @@ __global__ void k_check_instance_materials(const vkg_instance *__restrict__ inst
 
 // the material fields the BSDF divides by or takes as probabilities must be in range
 vkg_status check_material_values(vkg_ctx *ctx, const vkg_material *d_mats, uint32_t n, cudaStream_t st,
-                                 const char *fn, bool *any_transmissive)
+                                 const char *fn, bool *any_transmissive, bool *any_full)
 {
     *any_transmissive = false;
+    *any_full = false;
     std::vector<vkg_material> h(n);
     cudaError_t e = cudaMemcpyAsync(h.data(), d_mats, n * sizeof(vkg_material), cudaMemcpyDeviceToHost, st);
     if(e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -143,6 +144,7 @@ vkg_status check_material_values(vkg_ctx *ctx, const vkg_material *d_mats, uint3
             return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
                              "%s: material %u: clearcoat, clearcoat_roughness and sheen_roughness must be >= 0", fn, i);
         *any_transmissive = *any_transmissive || m.transmission > 0.f;
+        *any_full = *any_full || material_full(m);
     }
     return VKG_OK;
 }
@@ -343,7 +345,7 @@ vkg_status vkg_scene_create(vkg_ctx *ctx, const vkg_scene_desc *d, vkg_scene **o
         return cuda_check(ctx, e, "vkg_scene_create");
     }
     if(vkg_status s = check_material_values(ctx, sc->mats, d->num_materials, st, "vkg_scene_create",
-                                                 &sc->any_transmissive);
+                                                 &sc->any_transmissive, &sc->any_full);
        s != VKG_OK)
     {
         vkg_scene_destroy(ctx, sc);
@@ -471,7 +473,7 @@ vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_de
     chk(cudaMemcpyAsync(sc->mats, d->d_materials, d->num_materials * sizeof(vkg_material), cudaMemcpyDeviceToDevice, st));
     if(e != cudaSuccess) return fail(cuda_check(ctx, e, "vkg_scene_create_instanced"));
     if(vkg_status s = check_material_values(ctx, sc->mats, d->num_materials, st, "vkg_scene_create_instanced",
-                                                 &sc->any_transmissive);
+                                                 &sc->any_transmissive, &sc->any_full);
        s != VKG_OK)
         return fail(s);
     std::vector<mesh_ref> refs(d->num_meshes);
@@ -684,6 +686,8 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
     P.num_lights = (uint32_t)lights.size();
     uint32_t *cnt_l = lights.empty() ? nullptr : t->counters + 7;
     const light_queue lq{t->l_ray, t->l_pid, t->l_contrib, cnt_l};
+    // the shade variant: the full Disney model and the light terms, or metal-roughness only
+    const bool full = sc->any_full || !lights.empty();
     P.term_depth = cache_render ? ccfg->terminate_depth : 0xFFFFFFFFu;
     P.rec_depth = rec_depth;
     P.train_paths = train_paths;
@@ -743,13 +747,15 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_out, 0, sizeof(uint32_t), st));
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_s, 0, sizeof(uint32_t), st));
             if(cnt_l) VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_l, 0, sizeof(uint32_t), st));
-#define VKG_SHADE(M)                                                                                                   \
-    k_pt_shade<M><<<grid, PT_THREADS, 0, st>>>(SS, depth, t->q_ray[a], t->q_pid[a], t->hits, t->hit_inst, cnt_in,        \
+#define VKG_SHADE(M, F)                                                                                                \
+    k_pt_shade<M, single_scene, F><<<grid, PT_THREADS, 0, st>>>(SS, depth, t->q_ray[a], t->q_pid[a], t->hits, t->hit_inst, cnt_in,        \
                                                t->q_ray[1 - a],                                                          \
                                                t->q_pid[1 - a], cnt_out, t->s_ray, t->s_pid, t->s_contrib, cnt_s,         \
                                                t->rng, t->beta_pdf, t->radiance, io, lq)
-            if(mode == MODE_PLAIN) VKG_SHADE(MODE_PLAIN);
-            else VKG_SHADE(MODE_CACHE);
+            if(mode == MODE_PLAIN && full) VKG_SHADE(MODE_PLAIN, true);
+            else if(mode == MODE_PLAIN) VKG_SHADE(MODE_PLAIN, false);
+            else if(full) VKG_SHADE(MODE_CACHE, true);
+            else VKG_SHADE(MODE_CACHE, false);
 #undef VKG_SHADE
             if(!empty && tl_persistent)
             {

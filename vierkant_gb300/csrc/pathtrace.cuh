@@ -55,6 +55,13 @@ __host__ __device__ inline bool material_unculled(const vkg_material &m)
     return m.twosided != 0u || m.transmission > 0.f || m.diffuse_transmission > 0.f;
 }
 
+// a material that uses a lobe beyond metal-roughness (the shade kernels' FULL variant)
+__host__ __device__ inline bool material_full(const vkg_material &m)
+{
+    return m.transmission > 0.f || m.clearcoat > 0.f || m.diffuse_transmission > 0.f || m.sheen_color[0] > 0.f ||
+           m.sheen_color[1] > 0.f || m.sheen_color[2] > 0.f;
+}
+
 __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
 __device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
 __device__ __forceinline__ float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
@@ -459,7 +466,9 @@ __device__ __forceinline__ float3 eval_bsdf(const material_view &m, float3 L, fl
     return lerp3(brdf, bsdf, trans_weight);
 }
 
-// the material record as the BSDF reads it
+// the material record as the BSDF reads it; FULL = false reads only the metal-roughness fields and
+// makes the other lobes compile-time zero (for scenes whose materials have none of them)
+template<bool FULL = true>
 __device__ __forceinline__ material_view load_material(const vkg_material *mats, uint32_t id, bool disable_material)
 {
     const vkg_material &q = mats[id];
@@ -467,6 +476,12 @@ __device__ __forceinline__ material_view load_material(const vkg_material *mats,
     m.base = disable_material ? f3(0.8f, 0.8f, 0.8f) : f3(q.base_color[0], q.base_color[1], q.base_color[2]);
     m.roughness = q.roughness;
     m.metalness = q.metalness;
+    if constexpr(!FULL)
+    {
+        m.transmission = m.clearcoat = m.clearcoat_roughness = m.sheen_roughness = m.diffuse_transmission = 0.f;
+        m.sheen_color = m.dt_color = f3(0.f, 0.f, 0.f);
+        return m;
+    }
     m.transmission = q.transmission;
     m.clearcoat = q.clearcoat;
     m.clearcoat_roughness = q.clearcoat_roughness;

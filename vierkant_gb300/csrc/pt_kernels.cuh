@@ -43,6 +43,7 @@ struct vkg_scene
     vkg::mesh_ref *d_meshes = nullptr;
     uint32_t num_instances = 0;
     bool any_transmissive = false;  // a material with transmission > 0 (light shadow rays pass through it)
+    bool any_full = false;          // a material with a lobe beyond metal-roughness
     std::vector<vkg_light> lights;  // analytic lights (host copy; the tracer uploads them per render)
 };
 
@@ -268,7 +269,9 @@ __device__ __forceinline__ void hit_surface(const pt_params &P, uint32_t prim, u
     ng = normalize(n);
 }
 
-template<int MODE, class J>
+// FULL = false: a scene without lights whose materials are metal-roughness only; the light terms and
+// the other lobes compile away
+template<int MODE, class J, bool FULL = true>
 __global__ void __launch_bounds__(PT_THREADS)
         k_pt_shade(J S, uint32_t depth, const vkg_ray *__restrict__ in_ray,
                    const uint32_t *__restrict__ in_pid, const vkg_hit *__restrict__ hits,
@@ -300,8 +303,9 @@ __global__ void __launch_bounds__(PT_THREADS)
             const uint4 h = reinterpret_cast<const uint4 *>(hits)[i];
             pcg32 g{rng[pid], S.inc(pid)};
             // 8 draws per segment; 3 more (light pick, point on the light) when the scene has lights
+            const uint32_t num_lights = FULL ? P.num_lights : 0u;
             float u[11];
-            const int nu = P.num_lights ? 11 : 8;
+            const int nu = num_lights ? 11 : 8;
             for(int k = 0; k < 11; ++k) u[k] = k < nu ? u01(pcg32_next(g)) : 0.f;
             const float4 bp = beta_pdf[pid];
             float3 beta = f3(bp.x, bp.y, bp.z);
@@ -309,7 +313,7 @@ __global__ void __launch_bounds__(PT_THREADS)
             const float4 lr = radiance[pid];
             float3 L = f3(lr.x, lr.y, lr.z);
             uint32_t flags = __float_as_uint(lr.w); // PATH_REGULARIZE | PATH_CAUSTIC
-            const bool light_hits = P.num_lights && !(P.suppress_caustics && (flags & PATH_CAUSTIC));
+            const bool light_hits = num_lights && !(P.suppress_caustics && (flags & PATH_CAUSTIC));
             if(light_hits)
             {
                 // light bodies the segment passed (raypipeline.slang:196-224): additive emitters,
@@ -317,8 +321,8 @@ __global__ void __launch_bounds__(PT_THREADS)
                 const float4 r0 = rp[0];
                 const float3 o = f3(r0.x, r0.y, r0.z);
                 const float t_end = h.x == VKG_MISS ? r1.w : __uint_as_float(h.y);
-                const float inv_n = 1.f / (float)P.num_lights;
-                for(uint32_t li = 0; li < P.num_lights; ++li)
+                const float inv_n = 1.f / (float)num_lights;
+                for(uint32_t li = 0; li < num_lights; ++li)
                 {
                     const vkg_light &l = P.lights[li];
                     const float2 lh = intersect_light(l, o, dir);
@@ -332,8 +336,8 @@ __global__ void __launch_bounds__(PT_THREADS)
                 if(light_hits)
                 {
                     // sun discs seen by the ray (eval_distant_lights, raypipeline.slang:728-744)
-                    const float inv_n = 1.f / (float)P.num_lights;
-                    for(uint32_t li = 0; li < P.num_lights; ++li)
+                    const float inv_n = 1.f / (float)num_lights;
+                    for(uint32_t li = 0; li < num_lights; ++li)
                     {
                         const vkg_light &l = P.lights[li];
                         if(l.type != VKG_LIGHT_DIRECTIONAL) continue;
@@ -364,11 +368,11 @@ __global__ void __launch_bounds__(PT_THREADS)
                 const bool back_face = !(dot(ng, dir) < 0.f);
                 N = back_face ? -ng : ng; // shading normal faces the incoming ray
                 const float3 V = -dir;
-                material_view m = load_material(P.mats, mat, P.disable_material);
+                material_view m = load_material<FULL>(P.mats, mat, P.disable_material);
                 // path regularisation (raypipeline.slang:611): after a non-peaked bounce, later vertices
                 // shade (sample and NEE) with roughness >= 0.25
                 if(flags & PATH_REGULARIZE) m.roughness = fmaxf(m.roughness, PT_REGULARIZE_MIN_ROUGHNESS);
-                const float eta = hit_eta(P.mats, mat, back_face);
+                const float eta = FULL ? hit_eta(P.mats, mat, back_face) : 1.f;
                 const float *em = P.mats[mat].emission;
                 L = L + beta * f3(em[0], em[1], em[2]);
                 if constexpr(MODE == MODE_CACHE)
@@ -421,9 +425,9 @@ __global__ void __launch_bounds__(PT_THREADS)
                 }
                 // next-event estimation against one uniformly picked light (nee_surface,
                 // direct_lighting.slang:297-332); its shadow ray passes transmissive surfaces
-                if(!push_query && P.num_lights)
+                if(!push_query && num_lights)
                 {
-                    const uint32_t nl = P.num_lights;
+                    const uint32_t nl = num_lights;
                     const uint32_t li = nl > 1 ? min((uint32_t)(u[8] * (float)nl), nl - 1u) : 0u;
                     const vkg_light &l = P.lights[li];
                     const light_sample ls = sample_light(l, P0, u[9], u[10]);
@@ -508,7 +512,7 @@ __global__ void __launch_bounds__(PT_THREADS)
             s_pid[ps] = pid;
             s_contrib[ps] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
         }
-        if(lq.count)
+        if(FULL && lq.count)
         {
             const uint32_t pl = warp_push(lq.count, push_light);
             if(push_light)
@@ -580,10 +584,10 @@ __global__ void __launch_bounds__(PT_THREADS)
 
 // light-NEE visibility (transmittance_test, visibility_test.slang:94-131): 0 at the first opaque
 // surface on the segment, else the product of transmission x base colour over the transmissive
-// surfaces it crosses, found nearest first by repeated closest-hit queries from the last crossing
-// (at most PT_MAX_CROSSINGS; more count as blocked). Scenes without transmissive materials take
-// one any-hit query. Runs after the environment shadow kernel, so each path's radiance has one
-// writer at a time.
+// surfaces it crosses. Scenes without transmissive materials take one any-hit query; single-level
+// scenes one pass over the crossed triangles (trace_transmit); instanced scenes repeated closest-hit
+// queries from the last crossing (at most PT_MAX_CROSSINGS; more count as blocked). Runs after the
+// environment shadow kernel, so each path's radiance has one writer at a time.
 constexpr int PT_MAX_CROSSINGS = 32;
 
 template<class J, int STACK = (int)TRAVERSAL_STACK>
@@ -609,8 +613,18 @@ __global__ void __launch_bounds__(PT_THREADS) k_pt_light_shadow(J S, light_queue
                                                    .occluded;
             if(occ) T = f3(0.f, 0.f, 0.f);
         }
+        else if(!P.two_level)
+        {
+            const bool open = trace_transmit<STACK>(
+                    P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, T, [&](uint32_t prim) {
+                        const vkg_material &q = P.mats[__ldg(&P.tri_mat[prim])];
+                        return f3(q.base_color[0], q.base_color[1], q.base_color[2]) * q.transmission;
+                    });
+            if(!open) T = f3(0.f, 0.f, 0.f);
+        }
         else
         {
+            // instanced scenes: a material per instance, so crossings are found one closest hit at a time
             float tmin = r0.w;
             for(int k = 0;; ++k)
             {
@@ -915,7 +929,8 @@ __global__ void k_tri_flags(tri_rec *__restrict__ tris, uint32_t n, const uint32
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= n) return;
     const uint32_t m = tri_mat[tris[i].prim];
-    tris[i].pad[0] = (m < num_mats && material_unculled(mats[m])) ? TRI_FLAG_TWOSIDED : 0u;
+    tris[i].pad[0] = (m < num_mats && material_unculled(mats[m]) ? TRI_FLAG_TWOSIDED : 0u) |
+                     (m < num_mats && mats[m].transmission > 0.f ? TRI_FLAG_TRANSMISSIVE : 0u);
 }
 
 __global__ void k_check_materials(const uint32_t *__restrict__ tri_mat, uint32_t n, uint32_t num_mats,

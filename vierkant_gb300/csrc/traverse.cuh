@@ -24,6 +24,7 @@ enum cull_mode : int
     CULL_BACK_UNLESS_TWOSIDED = 2
 };
 constexpr uint32_t TRI_FLAG_TWOSIDED = 1u;
+constexpr uint32_t TRI_FLAG_TRANSMISSIVE = 2u; // the triangle's material has transmission > 0
 
 struct trace_result
 {
@@ -242,6 +243,56 @@ __device__ __forceinline__ trace_result ray_result(const ray_state_t<STACK> &s)
     r.u = s.best == VKG_MISS ? 0.f : s.bu;
     r.v = s.best == VKG_MISS ? 0.f : s.bv;
     return r;
+}
+
+// transmittance of a segment (light-NEE visibility): one pass over every triangle the ray crosses in
+// (tmin, tmax), no culling, in traversal order; false at the first triangle without
+// TRI_FLAG_TRANSMISSIVE, else T is multiplied by tint(prim) of each crossed transmissive triangle.
+// Every triangle sits in one leaf and every node is visited at most once, so each crossing counts
+// once; the children need no ordering.
+template<int STACK, class Tint>
+__device__ __forceinline__ bool trace_transmit(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
+                                               float ox, float oy, float oz, float tmin, float dx, float dy, float dz,
+                                               float tmax, float3 &T, Tint tint)
+{
+    const float ix = safe_rcp(dx), iy = safe_rcp(dy), iz = safe_rcp(dz);
+    uint32_t st[STACK];
+    int sp = 1;
+    st[0] = 0u;
+    while(sp > 0)
+    {
+        const uint32_t ni = st[--sp];
+        uint32_t key[8];
+        uint4 w4, w5;
+        node_keys(nodes, ni, ox, oy, oz, ix, iy, iz, tmin, tmax, key, w4, w5);
+#pragma unroll
+        for(int k = 0; k < 8; ++k)
+        {
+            if(key[k] == 0xFFFFFFFFu) continue;
+            const uint32_t c = (k & 4) ? sel4(w5, k & 3) : sel4(w4, k & 3);
+            if(!(c & LEAF_BIT))
+            {
+                if(sp < STACK) st[sp++] = c;
+                continue;
+            }
+            const uint32_t start = c & 0x07FFFFFFu, cnt = ((c >> 27) & 0xFu) + 1u;
+            for(uint32_t ti = start; ti < start + cnt; ++ti)
+            {
+                const float4 *tp = reinterpret_cast<const float4 *>(tris + ti);
+                const float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
+                float t, u, v;
+                if(!tri_test(a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, cc.x, ox, oy, oz, dx, dy, dz, 0, t, u, v))
+                    continue;
+                if(!(t > tmin && t < tmax)) continue;
+                if(!(__float_as_uint(cc.z) & TRI_FLAG_TRANSMISSIVE)) return false;
+                const float3 m = tint(__float_as_uint(cc.y));
+                T.x *= m.x;
+                T.y *= m.y;
+                T.z *= m.z;
+            }
+        }
+    }
+    return true;
 }
 
 template<bool ANY, bool STATS, int STACK = (int)TRAVERSAL_STACK>
