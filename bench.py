@@ -280,6 +280,29 @@ def _crop_error(img, golden):
     return math.sqrt(float(np.mean((_lum(c) - _lum(ref)) ** 2))), float((c.sum() - ref.sum()) / ref.sum())
 
 
+def denoise_timing(ctx, pixels, w, h, reps=20):
+    """The a-trous denoise pass (5 passes) over a frame of pixel records: CUDA-event time per call on
+    the context's stream, and its bytes against the measured HBM copy bandwidth. Bytes per pixel: the
+    32-byte record read once, per pass the demodulated colour written and read (2 x 16 B), the
+    geometry and albedo float4s (32 B) and the output (16 B) — the 25 taps per pass are L1/L2 hits."""
+    import torch
+    from vierkant_gb300.pathtracer import denoise
+    for _ in range(3):
+        denoise(ctx, pixels, w, h)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(torch.cuda.current_stream())
+    for _ in range(reps):
+        denoise(ctx, pixels, w, h)
+    e1.record(torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    byts = w * h * (32 + 5 * (2 * 16 + 32 + 16) + 16)
+    peak, src = measured_peaks()
+    return {"ms": round(ms, 4), "mpix_per_s": round(w * h / ms / 1e3, 1), "bytes_per_pixel": byts // (w * h),
+            "gbs": round(byts / ms / 1e6, 1), "frac_of_hbm": round(byts / ms / 1e6 / peak, 3), "peak": src}
+
+
 def path_tracer_block(ctx, frames=256):
     """The radiance estimator on the same scene: the plain tracer at 1280x720 x 64 spp (samples/s,
     Mrays/s, RMSE / bias against the FP64 oracle crop), and the equal-RMSE comparison at 1920x1080:
@@ -315,6 +338,7 @@ def path_tracer_block(ctx, frames=256):
                                "mrays_per_s": round(rays / st.total_ms / 1e3, 1), "rays": int(rays),
                                "rmse": round(rmse, 4), "bias": round(bias, 5),
                                "oracle": "FP64 4096 spp, 128x128 crop at (576, 528)"}
+    out["denoise_720p"] = denoise_timing(ctx, pt.pixel_data(), 1280, 720)
     pt.close()
 
     cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, 1920, 1080)

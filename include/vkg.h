@@ -444,7 +444,24 @@ typedef struct vkg_settings
     float sun_intensity;
     float sun_spherical_coords[2];    /* elevation, azimuth (radians) */
     float sun_angular_size;           /* cone half-angle of the disc (radians); 0: a delta light */
+    uint32_t denoising;               /* settings_t::denoising: the output is the a-trous filtered image */
+    float clip_near;                  /* the camera's near clipping distance, for the pixel depth
+                                         near / view-space distance (camera_params.hpp:37); 0: 0.1 */
 } vkg_settings;
+
+/* per-pixel output record, the layout of the reference's pixel_data_t (pixel_data.slang:9-21):
+   accumulated radiance, coverage of the last batch, reversed-z depth, primary-hit normal
+   (octahedral, two snorm16), object id (0xFFFF on a miss), primary-hit albedo (RGBA8) — the
+   G-buffer fields come from each pixel's last sample, as the reference's raygen loop leaves them */
+typedef struct vkg_pixel_data
+{
+    float radiance[3];
+    float alpha;
+    float depth;
+    uint32_t normal;
+    uint32_t object_id;
+    uint32_t albedo;
+} vkg_pixel_data; /* 32 B */
 
 typedef struct vkg_tracer_create_info
 {
@@ -469,6 +486,14 @@ typedef struct vkg_tracer_stats
 
 typedef struct vkg_tracer vkg_tracer;
 vkg_status vkg_settings_default(vkg_settings *out);
+/* the pixel records of the traced window (crop) after the last render: d_out holds width x height */
+vkg_status vkg_tracer_pixel_data(vkg_tracer *tracer, vkg_pixel_data *d_out, void *stream);
+/* the reference's denoise pass (PBRPathTracer.cpp:346-403, denoise.slang): five edge-avoiding
+   a-trous passes (steps 1, 2, 4, 8, 16) over albedo-demodulated radiance with luminance, normal and
+   depth weights; d_out_rgba: width x height x 4 floats (alpha 0, as the shader writes), d_out_depth
+   (may be NULL): the pixels' depth */
+vkg_status vkg_denoise(vkg_ctx *ctx, const vkg_pixel_data *d_pixels, uint32_t width, uint32_t height,
+                       float *d_out_rgba, float *d_out_depth, void *stream);
 /* PBRPathTracer::create (PBRPathTracer.hpp:144) */
 vkg_status vkg_tracer_create(vkg_ctx *ctx, const vkg_tracer_create_info *info, vkg_tracer **out);
 vkg_status vkg_tracer_set_settings(vkg_tracer *tracer, const vkg_settings *settings);

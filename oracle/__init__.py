@@ -264,7 +264,22 @@ class orc_pt_settings(C.Structure):
                 ("rr_depth", C.c_uint32), ("mis_mode", C.c_uint32), ("disable_material", C.c_uint32),
                 ("draw_skybox", C.c_uint32), ("max_path_beta", C.c_float), ("environment", C.c_float),
                 ("crop", C.c_uint32 * 4), ("num_lights", C.c_uint32), ("suppress_caustics", C.c_uint32),
-                ("lights", C.c_void_p)]
+                ("lights", C.c_void_p), ("pixels", C.c_void_p), ("clip_near", C.c_float)]
+
+
+# per-pixel record (32 bytes, the layout of vkg_pixel_data)
+PIXEL_DTYPE = np.dtype([("radiance", "<f4", 3), ("alpha", "<f4"), ("depth", "<f4"), ("normal", "<u4"),
+                        ("object_id", "<u4"), ("albedo", "<u4")])
+
+
+def denoise(pixels):
+    """the a-trous denoise pass over pixel records [h, w] (PIXEL_DTYPE); returns rgba [h, w, 4] float32"""
+    px = np.ascontiguousarray(pixels, PIXEL_DTYPE)
+    h, w = px.shape
+    out = np.zeros((h, w, 4), np.float32)
+    orc().orc_denoise.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]
+    orc().orc_denoise(ptr(px), w, h, ptr(out))
+    return out
 
 
 # analytic light record (80 bytes, the layout of vkg_light)
@@ -284,11 +299,12 @@ def sun_light(color, intensity, spherical_coords, angular_size):
 
 
 def _settings(seed, batch, spp, max_depth, rr_depth, mis_mode, draw_skybox, max_path_beta, environment, crop, lights,
-              suppress_caustics):
+              suppress_caustics, pixels=None, clip_near=0.1):
     arr = np.ascontiguousarray(np.asarray(lights if lights is not None else [], LIGHT_DTYPE).reshape(-1))
     st = orc_pt_settings(seed, batch, spp, max_depth, rr_depth, mis_mode, 0, draw_skybox, max_path_beta, environment,
                          (C.c_uint32 * 4)(*crop), len(arr), int(suppress_caustics),
-                         arr.ctypes.data_as(C.c_void_p) if len(arr) else None)
+                         arr.ctypes.data_as(C.c_void_p) if len(arr) else None,
+                         pixels.ctypes.data_as(C.c_void_p) if pixels is not None else None, clip_near)
     return st, arr
 
 
@@ -329,8 +345,11 @@ def env_tables_fp64(rgb):
 
 def pt_render(fp64, xyz, idx, tri_mat, mats, bvh: "CpuBVH", env_rgb, cam, spp, *, seed=0x5EED, batch=0, max_depth=6,
               rr_depth=3, mis_mode=0, crop=(0, 0, 0, 0), environment=1.0, draw_skybox=1, max_path_beta=0.0,
-              alias_prob=None, alias=None, weight=None, cdf=None, nthreads=0, lights=None, suppress_caustics=False):
-    """Mean radiance per crop pixel ([h, w, 3] float64), mean squared luminance per pixel, (ext, shadow) rays."""
+              alias_prob=None, alias=None, weight=None, cdf=None, nthreads=0, lights=None, suppress_caustics=False,
+              pixels=None, clip_near=0.1):
+    """Mean radiance per crop pixel ([h, w, 3] float64), mean squared luminance per pixel, (ext, shadow) rays.
+    pixels: optional PIXEL_DTYPE array [h, w] of the crop, filled with the pixel records (radiance left 0)
+    the tracer writes."""
     L = orc()
     L.orc_pt_render.argtypes = [C.c_int, C.POINTER(orc_pt_scene), C.POINTER(orc_bvh), C.POINTER(orc_pt_env),
                                 C.POINTER(orc_camera), C.POINTER(orc_pt_settings), C.c_void_p, C.c_void_p, C.c_void_p,
@@ -347,7 +366,7 @@ def pt_render(fp64, xyz, idx, tri_mat, mats, bvh: "CpuBVH", env_rgb, cam, spp, *
     cw = crop[2] or cam.width
     ch = crop[3] or cam.height
     st, _lights = _settings(seed, batch, spp, max_depth, rr_depth, mis_mode, draw_skybox, max_path_beta, environment,
-                            crop, lights, suppress_caustics)
+                            crop, lights, suppress_caustics, pixels, clip_near)
     out = np.zeros((ch, cw, 3), np.float64)
     sq = np.zeros((ch, cw), np.float64)
     stats = np.zeros(2, np.uint64)

@@ -154,6 +154,12 @@ typedef struct {
     float tangent[3], size_x;
 } orc_pt_light;
 
+/* the per-pixel record, same 32-byte layout as vkg_pixel_data (the reference's pixel_data_t) */
+typedef struct {
+    float radiance[3], alpha, depth;
+    uint32_t normal, object_id, albedo;
+} orc_pixel;
+
 typedef struct {
     uint32_t seed;
     uint32_t batch;
@@ -163,6 +169,8 @@ typedef struct {
     uint32_t crop[4]; /* x0, y0, w, h (pixels of the full resolution camera) */
     uint32_t num_lights, suppress_caustics;
     const orc_pt_light *lights; /* the sun (if any) first */
+    orc_pixel *pixels;          /* optional: the crop's pixel records (radiance left 0), as the tracer writes them */
+    float clip_near;            /* near clipping distance for the records' depth */
 } orc_pt_settings;
 
 /* the sun of the tracer settings as a directional light (PBRPathTracer.cpp:610-624): propagation
@@ -193,6 +201,15 @@ int orc_pt_render(int fp64, const orc_pt_scene *scene, const orc_bvh *bvh, const
 int orc_pt_render_instanced(const orc_pt_scene *scene, const orc_pt_instances *inst, const orc_pt_env *env,
                             const orc_camera *cam, const orc_pt_settings *set, double *out, double *sq,
                             uint64_t *stats, int nthreads);
+/* pixel-record packing and the a-trous denoise pass (denoise.c) */
+void orc_oct_encode(const float n[3], float p[2]);
+void orc_oct_decode(const float p[2], float n[3]);
+uint32_t orc_pack_snorm_2x16(float x, float y);
+void orc_unpack_snorm_2x16(uint32_t p, float out[2]);
+uint32_t orc_pack_rgba8(float r, float g, float b, float a);
+void orc_unpack_rgb8(uint32_t c, float out[3]);
+void orc_denoise(const orc_pixel *px, uint32_t w, uint32_t h, float *out_rgba);
+
 /* one BSDF sample / evaluation in FP64 (sample_disney / eval_disney): u = (lobe, x, y); the return
    value of orc_bsdf_eval is the mixture pdf */
 void orc_bsdf_sample(const orc_pt_material *m, const double n[3], const double v[3], double eta, const double u[3],

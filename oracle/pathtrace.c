@@ -33,6 +33,8 @@ typedef struct {
     float max_path_beta, environment;
     const orc_pt_light *lights;
     uint32_t num_lights, suppress_caustics;
+    orc_pixel *pixels;
+    float clip_near;
     uint32_t cx0, cy0, cw, ch;
     double *out, *sq;
     const orc_pt_instances *inst; /* NULL: single-level scene */
@@ -632,20 +634,24 @@ static void *pt_worker(void *arg)
         if(pix >= npix) break;
         uint32_t x = J->cx0 + pix % J->cw, y = J->cy0 + pix / J->cw;
         double acc[3] = {0, 0, 0}, sq = 0;
+        int covered = 0;
         for(uint32_t s = 0; s < J->spp; ++s)
         {
             uint64_t seq = ((uint64_t)J->batch << 40) ^ ((uint64_t)s * npix + pix);
             double L[3];
+            /* the pixel record: coverage from every sample, the G-buffer from the last one */
+            orc_pixel *rec = (J->pixels && s + 1 == J->spp) ? &J->pixels[pix] : NULL;
+            int hit0 = 0;
             if(J->fp64)
             {
-                d_v3 r = d_trace_path(J, x, y, seq, st);
+                d_v3 r = d_trace_path(J, x, y, seq, st, rec, &hit0);
                 L[0] = r.x;
                 L[1] = r.y;
                 L[2] = r.z;
             }
             else
             {
-                f_v3 r = f_trace_path(J, x, y, seq, st);
+                f_v3 r = f_trace_path(J, x, y, seq, st, rec, &hit0);
                 L[0] = r.x;
                 L[1] = r.y;
                 L[2] = r.z;
@@ -654,7 +660,9 @@ static void *pt_worker(void *arg)
             for(int c = 0; c < 3; ++c) acc[c] = J->fp64 ? acc[c] + L[c] : (double)((float)acc[c] + (float)L[c]);
             double lum = 0.2126 * L[0] + 0.7152 * L[1] + 0.0722 * L[2];
             sq += lum * lum;
+            covered = covered || hit0;
         }
+        if(J->pixels) J->pixels[pix].alpha = covered ? 1.f : 0.f;
         for(int c = 0; c < 3; ++c)
             J->out[3 * (size_t)pix + c] = J->fp64 ? acc[c] / J->spp : (double)((float)acc[c] / (float)J->spp);
         if(J->sq) J->sq[pix] = sq / J->spp;
@@ -694,6 +702,8 @@ int orc_pt_render(int fp64, const orc_pt_scene *scene, const orc_bvh *bvh, const
     J.lights = set->lights;
     J.num_lights = set->lights ? set->num_lights : 0;
     J.suppress_caustics = set->suppress_caustics;
+    J.pixels = set->pixels;
+    J.clip_near = set->clip_near > 0.f ? set->clip_near : 0.1f;
     J.cx0 = set->crop[0];
     J.cy0 = set->crop[1];
     J.cw = set->crop[2] ? set->crop[2] : cam->width;
@@ -742,6 +752,8 @@ int orc_pt_render_instanced(const orc_pt_scene *scene, const orc_pt_instances *i
     J.lights = set->lights;
     J.num_lights = set->lights ? set->num_lights : 0;
     J.suppress_caustics = set->suppress_caustics;
+    J.pixels = set->pixels;
+    J.clip_near = set->clip_near > 0.f ? set->clip_near : 0.1f;
     J.cx0 = set->crop[0];
     J.cy0 = set->crop[1];
     J.cw = set->crop[2] ? set->crop[2] : cam->width;

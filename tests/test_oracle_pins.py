@@ -319,3 +319,54 @@ def test_sun_light_direction():
     e, a = math.radians(30), math.radians(20)
     assert np.allclose(s["direction"], (math.cos(e) * math.sin(a), -math.sin(e), math.cos(e) * math.cos(a)), atol=1e-6)
     assert s["type"] == 2 and s["intensity"] == 2.0 and np.isinf(s["range"])
+
+
+def test_pixel_record_packing():
+    """octahedral snorm16 normals and RGBA8 colours (octahedral_map.slang:9-55, color.slang:6-18)"""
+    rng = np.random.default_rng(3)
+    v = rng.normal(size=(2000, 3)).astype(np.float32)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    L = oracle.orc()
+    L.orc_oct_encode.argtypes = [C.c_void_p, C.c_void_p]
+    L.orc_oct_decode.argtypes = [C.c_void_p, C.c_void_p]
+    L.orc_pack_snorm_2x16.argtypes = [C.c_float, C.c_float]
+    L.orc_pack_snorm_2x16.restype = C.c_uint32
+    L.orc_unpack_snorm_2x16.argtypes = [C.c_uint32, C.c_void_p]
+    L.orc_pack_rgba8.argtypes = [C.c_float] * 4
+    L.orc_pack_rgba8.restype = C.c_uint32
+    worst = 0.0
+    for n in v:
+        p = np.zeros(2, np.float32)
+        L.orc_oct_encode(ptr(np.ascontiguousarray(n)), ptr(p))
+        q = np.zeros(2, np.float32)
+        L.orc_unpack_snorm_2x16(L.orc_pack_snorm_2x16(float(p[0]), float(p[1])), ptr(q))
+        d = np.zeros(3, np.float32)
+        L.orc_oct_decode(ptr(q), ptr(d))
+        worst = max(worst, float(np.linalg.norm(d - n)))
+    assert worst < 1e-4, worst
+    assert L.orc_pack_snorm_2x16(float("nan"), 0.0) == 0
+    assert L.orc_pack_rgba8(1.0, 0.5, 0.0, 1.0) == 0xFF007FFF
+    assert L.orc_pack_rgba8(2.0, -1.0, 0.25, 0.0) == 0x003F00FF
+
+
+def test_denoise_restatement_properties():
+    """the a-trous restatement keeps a constant image constant (the weights are normalised), and
+    with the reference's albedo demodulation a flat image of any albedo too"""
+    h, w = 23, 31
+    px = np.zeros((h, w), oracle.PIXEL_DTYPE)
+    px["radiance"] = (0.3, 0.5, 0.7)
+    px["depth"] = np.linspace(0.01, 0.05, w, dtype=np.float32)[None, :]
+    px["albedo"] = 0xFF804020
+    out = oracle.denoise(px)
+    assert np.allclose(out[..., :3], (0.3, 0.5, 0.7), rtol=1e-5)
+    assert np.all(out[..., 3] == 0)
+    # low-amplitude noise is smoothed (its spread shrinks, its mean stays); an isolated bright pixel
+    # is an edge for the luminance weight and survives, as the filter intends
+    rng = np.random.default_rng(5)
+    px["radiance"] = (0.5 + 0.05 * rng.standard_normal((h, w, 1))).astype(np.float32)
+    out = oracle.denoise(px)
+    assert out[..., 0].std() < 0.3 * px["radiance"][..., 0].std()
+    assert abs(out[..., 0].mean() - px["radiance"][..., 0].mean()) < 0.01
+    px["radiance"][11, 15] = (10.0, 10.0, 10.0)
+    out = oracle.denoise(px)
+    assert out[11, 15, 0] > 9.0

@@ -62,7 +62,12 @@ class vkg_settings(C.Structure):
                 ("environment", C.c_float), ("rr_start_depth", C.c_uint32), ("crop", C.c_uint32 * 4),
                 ("samples_per_wave", C.c_uint32), ("suppress_refractive_caustics", C.c_uint32),
                 ("sun_color", C.c_float * 3), ("sun_intensity", C.c_float), ("sun_spherical_coords", C.c_float * 2),
-                ("sun_angular_size", C.c_float)]
+                ("sun_angular_size", C.c_float), ("denoising", C.c_uint32), ("clip_near", C.c_float)]
+
+
+class vkg_pixel_data(C.Structure):
+    _fields_ = [("radiance", C.c_float * 3), ("alpha", C.c_float), ("depth", C.c_float), ("normal", C.c_uint32),
+                ("object_id", C.c_uint32), ("albedo", C.c_uint32)]
 
 
 class vkg_light(C.Structure):
@@ -196,6 +201,8 @@ SIGNATURES = {
     "vkg_scene_create": (I32, [P, C.POINTER(vkg_scene_desc), C.POINTER(P), P]),
     "vkg_scene_destroy": (I32, [P, P]),
     "vkg_scene_set_lights": (I32, [P, P, P, U32]),
+    "vkg_tracer_pixel_data": (I32, [P, P, P]),
+    "vkg_denoise": (I32, [P, P, U32, U32, P, P, P]),
     "vkg_light_convert": (I32, [C.POINTER(vkg_light_source), P, P, C.POINTER(vkg_light)]),
     "vkg_scene_bvh": (I32, [P, C.POINTER(P)]),
     "vkg_scene_env_tables": (I32, [P, C.POINTER(P), C.POINTER(P), C.POINTER(U32), C.POINTER(U32)]),

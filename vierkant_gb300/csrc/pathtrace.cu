@@ -57,6 +57,7 @@ struct vkg_tracer
     float4 *radiance = nullptr;
     float *sum = nullptr;
     float *accum = nullptr;
+    vkg_pixel_data *gbuf = nullptr; // pixel records of the traced window
     uint32_t *counters = nullptr;           // [0..1] queue lengths, [2] shadow queue length, [3] cache queries,
                                             // [4] training records, [5] training batch length, [6] work
                                             // counter, [7] light shadow queue length
@@ -85,6 +86,8 @@ struct vkg_tracer
 
 namespace vkg
 {
+vkg_status denoise_run(vkg_ctx *ctx, const vkg_pixel_data *px, uint32_t w, uint32_t h, float *out_rgba,
+                       float *out_rgb, float *out_depth, cudaStream_t st);
 namespace
 {
 
@@ -154,7 +157,7 @@ void tracer_free_buffers(vkg_tracer *t)
     for(void *p: {(void *)t->q_ray[0], (void *)t->q_ray[1], (void *)t->q_pid[0], (void *)t->q_pid[1], (void *)t->hits,
                   (void *)t->hit_inst,
                   (void *)t->s_ray, (void *)t->s_pid, (void *)t->s_contrib, (void *)t->rng, (void *)t->beta_pdf,
-                  (void *)t->radiance, (void *)t->sum, (void *)t->accum})
+                  (void *)t->radiance, (void *)t->sum, (void *)t->accum, (void *)t->gbuf})
         cudaFree(p);
     t->q_ray[0] = t->q_ray[1] = nullptr;
     t->q_pid[0] = t->q_pid[1] = nullptr;
@@ -165,6 +168,7 @@ void tracer_free_buffers(vkg_tracer *t)
     t->s_contrib = nullptr;
     t->rng = nullptr;
     t->beta_pdf = t->radiance = nullptr;
+    t->gbuf = nullptr;
     t->sum = t->accum = nullptr;
     t->capacity = t->npix_cap = 0;
 }
@@ -239,6 +243,7 @@ vkg_status tracer_ensure(vkg_tracer *t, size_t paths, size_t npix)
     al((void **)&t->radiance, paths * sizeof(float4));
     al((void **)&t->sum, npix * 3 * sizeof(float));
     al((void **)&t->accum, npix * 3 * sizeof(float));
+    al((void **)&t->gbuf, npix * sizeof(vkg_pixel_data));
     if(e != cudaSuccess)
     {
         tracer_free_buffers(t);
@@ -589,6 +594,8 @@ vkg_status vkg_settings_default(vkg_settings *s)
     s->draw_skybox = 1;
     s->environment = 1.f;
     s->rr_start_depth = 0;
+    s->denoising = 0;
+    s->clip_near = 0.1f; // camera_params.hpp:37
     return VKG_OK;
 }
 
@@ -688,6 +695,7 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
     const light_queue lq{t->l_ray, t->l_pid, t->l_contrib, cnt_l};
     // the shade variant: the full Disney model and the light terms, or metal-roughness only
     const bool full = sc->any_full || !lights.empty();
+    P.gbuf = t->gbuf;
     P.term_depth = cache_render ? ccfg->terminate_depth : 0xFFFFFFFFu;
     P.rec_depth = rec_depth;
     P.train_paths = train_paths;
@@ -709,6 +717,7 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
     cache_io io{t->q_feat, t->q_beta, cnt_q, t->rec, t->vcount};
 
     VKG_TRY_CUDA(ctx, cudaMemsetAsync(t->sum, 0, (size_t)npix * 3 * sizeof(float), st));
+    VKG_TRY_CUDA(ctx, cudaMemsetAsync(t->gbuf, 0, (size_t)npix * sizeof(vkg_pixel_data), st));
     VKG_TRY_CUDA(ctx, cudaMemsetAsync(t->totals, 0, 3 * sizeof(unsigned long long), st));
     VKG_TRY_CUDA(ctx, cudaEventRecord(t->ev0, st));
     for(uint32_t s0 = 0; s0 < S.num_samples; s0 += spw)
@@ -814,11 +823,25 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
     if(!train_paths) VKG_TRY_CUDA(ctx, cudaEventRecord(t->ev_train, st));
     t->trained = train_paths > 0;
     k_pt_finalize<<<(3 * npix + 255) / 256, 256, 0, st>>>(npix, S.num_samples, t->batch, t->sum, t->accum, d_rgb_out);
+    k_pixel_radiance<<<(npix + 255) / 256, 256, 0, st>>>(t->accum, npix, t->gbuf);
+    if(S.denoising && d_rgb_out)
+        if(vkg_status s = denoise_run(ctx, t->gbuf, cw, ch, nullptr, d_rgb_out, nullptr, st); s != VKG_OK) return s;
     VKG_TRY_CUDA(ctx, cudaEventRecord(t->ev1, st));
     VKG_TRY_CUDA(ctx, cudaGetLastError());
     t->last_paths = (uint64_t)npix * S.num_samples;
     t->rendered = true;
     t->batch += 1;
+    return VKG_OK;
+}
+
+vkg_status vkg_tracer_pixel_data(vkg_tracer *t, vkg_pixel_data *d_out, void *stream)
+{
+    if(!t) return VKG_ERR_INVALID_ARGUMENT;
+    if(!d_out) return set_error(t->ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_tracer_pixel_data: NULL buffer");
+    if(!t->rendered) return set_error(t->ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_tracer_pixel_data: nothing rendered yet");
+    if(vkg_status s = bind_device(t->ctx); s != VKG_OK) return s;
+    VKG_TRY_CUDA(t->ctx, cudaMemcpyAsync(d_out, t->gbuf, t->npix_cap * sizeof(vkg_pixel_data), cudaMemcpyDeviceToDevice,
+                                         static_cast<cudaStream_t>(stream)));
     return VKG_OK;
 }
 

@@ -8,6 +8,7 @@
 #include "nrc.cuh"
 #include "light.cuh"
 #include "pathtrace.cuh"
+#include "pixel.cuh"
 #include "tlas.cuh"
 #include "traverse.cuh"
 
@@ -83,6 +84,11 @@ struct pt_params
     // analytic lights (the sun first) and the switches of their estimators
     const vkg_light *lights;
     uint32_t num_lights, suppress_caustics, transmissive;
+    // per-pixel records of the traced window (nullptr: none): coverage from every sample, the
+    // G-buffer fields from sample last_sample's primary hit; clip_near for the reversed-z depth
+    vkg_pixel_data *gbuf;
+    uint32_t last_sample;
+    float clip_near;
 };
 
 // the shade kernel's two modes
@@ -331,6 +337,17 @@ __global__ void __launch_bounds__(PT_THREADS)
                     L = L + beta * lv3(l.color) * (w * l.intensity);
                 }
             }
+            // the pixel record of a camera ray (raypipeline.slang:224-236, :250-268)
+            const bool record = depth == 0 && P.gbuf && pid < P.train_base &&
+                                P.s0 + pid / P.npix == P.last_sample;
+            if(record && h.x == VKG_MISS)
+            {
+                vkg_pixel_data &px = P.gbuf[pid % P.npix];
+                px.depth = 0.f;
+                px.normal = 0u;
+                px.object_id = 0xFFFFu;
+                px.albedo = pack_rgba8(0.f, 0.f, 0.f, 1.f);
+            }
             if(h.x == VKG_MISS)
             {
                 if(light_hits)
@@ -375,6 +392,23 @@ __global__ void __launch_bounds__(PT_THREADS)
                 const float eta = FULL ? hit_eta(P.mats, mat, back_face) : 1.f;
                 const float *em = P.mats[mat].emission;
                 L = L + beta * f3(em[0], em[1], em[2]);
+                if(depth == 0 && P.gbuf && pid < P.train_base)
+                {
+                    vkg_pixel_data &px = P.gbuf[pid % P.npix];
+                    px.alpha = 1.f; // coverage: any sample of the batch hit geometry
+                    if(record)
+                    {
+                        // reversed-z depth near / (distance along the view axis); normal and albedo
+                        // of the primary hit
+                        const float3 fwd = f3(-P.cam.back[0], -P.cam.back[1], -P.cam.back[2]);
+                        const float3 rel = P0 - f3(P.cam.eye[0], P.cam.eye[1], P.cam.eye[2]);
+                        px.depth = P.clip_near / dot(rel, fwd);
+                        const float2 oc = oct_encode(N.x, N.y, N.z);
+                        px.normal = pack_snorm_2x16(oc.x, oc.y);
+                        px.object_id = P.two_level ? hit_inst[i] : 0u;
+                        px.albedo = pack_rgba8(m.base.x, m.base.y, m.base.z, 1.f);
+                    }
+                }
                 if constexpr(MODE == MODE_CACHE)
                 {
                     if(pid < P.train_base && depth == P.term_depth)
@@ -923,6 +957,16 @@ __global__ void k_pt_finalize(uint32_t npix, uint32_t spp, uint32_t batch, const
     if(out) out[k] = a;
 }
 
+// the accumulated radiance into the pixel records
+__global__ void k_pixel_radiance(const float *__restrict__ accum, uint32_t npix, vkg_pixel_data *__restrict__ px)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= npix) return;
+    px[i].radiance[0] = accum[3 * (size_t)i];
+    px[i].radiance[1] = accum[3 * (size_t)i + 1];
+    px[i].radiance[2] = accum[3 * (size_t)i + 2];
+}
+
 __global__ void k_tri_flags(tri_rec *__restrict__ tris, uint32_t n, const uint32_t *__restrict__ tri_mat,
                             const vkg_material *__restrict__ mats, uint32_t num_mats)
 {
@@ -995,6 +1039,9 @@ inline pt_params make_params(const vkg_scene *sc, const vkg_camera &cam, const v
     P.num_lights = 0;
     P.suppress_caustics = S.suppress_refractive_caustics;
     P.transmissive = sc->any_transmissive ? 1u : 0u;
+    P.gbuf = nullptr;
+    P.last_sample = S.num_samples ? S.num_samples - 1 : 0u;
+    P.clip_near = S.clip_near > 0.f ? S.clip_near : 0.1f;
     return P;
 }
 

@@ -17,8 +17,8 @@ import math
 import numpy as np
 import torch
 
-from ._lib import (check, lib, vkg_bvh_info, vkg_camera, vkg_light, vkg_light_source, vkg_scene_desc, vkg_settings,
-                   vkg_tracer_create_info,
+from ._lib import (check, lib, vkg_bvh_info, vkg_camera, vkg_light, vkg_light_source, vkg_pixel_data,
+                   vkg_scene_desc, vkg_settings, vkg_tracer_create_info,
                    vkg_tracer_stats)
 from .raytracing import Context
 
@@ -96,6 +96,23 @@ def cornell_lights(intensity_scale: float = 1.0) -> np.ndarray:
     sc = 1.0 / max(0.001, math.cos(0.3) - math.cos(0.6))
     L[2]["spot_angle_scale"], L[2]["spot_angle_offset"] = sc, -math.cos(0.6) * sc
     return L
+
+
+# the per-pixel record (pixel_data_t layout): radiance, coverage, depth, octahedral normal, object id, RGBA8 albedo
+PIXEL_DTYPE = np.dtype([("radiance", "<f4", 3), ("alpha", "<f4"), ("depth", "<f4"), ("normal", "<u4"),
+                        ("object_id", "<u4"), ("albedo", "<u4")])
+assert PIXEL_DTYPE.itemsize == C.sizeof(vkg_pixel_data)
+
+
+def denoise(ctx: Context, pixels: torch.Tensor, width: int, height: int, with_depth: bool = False):
+    """The reference's a-trous denoise pass over pixel records (a uint8 CUDA tensor of width x height
+    x 32 bytes, e.g. PBRPathTracer.pixel_data()); returns the rgba image (and the depth)."""
+    out = torch.empty((height, width, 4), dtype=torch.float32, device=pixels.device)
+    dep = torch.empty((height, width), dtype=torch.float32, device=pixels.device) if with_depth else None
+    check(lib().vkg_denoise(ctx.handle, C.c_void_p(pixels.data_ptr()), width, height, C.c_void_p(out.data_ptr()),
+                            C.c_void_p(dep.data_ptr()) if dep is not None else None, C.c_void_p(ctx.stream())),
+          ctx.handle, "vkg_denoise")
+    return (out, dep) if with_depth else out
 
 
 class _Lights:
@@ -248,6 +265,15 @@ class PBRPathTracer:
             out = torch.empty((h, w, 3), dtype=torch.float32, device=f"cuda:{self.ctx.device}")
         check(lib().vkg_tracer_render(self.handle, scene.handle, C.byref(camera), C.c_void_p(out.data_ptr()),
                                       C.c_void_p(self.ctx.stream())), self.ctx.handle, "vkg_tracer_render")
+        return out
+
+    def pixel_data(self) -> torch.Tensor:
+        """The pixel records of the traced window after the last render (uint8 [h, w, 32]; view the
+        host copy with PIXEL_DTYPE)."""
+        w, h = self._crop()
+        out = torch.empty((h, w, 32), dtype=torch.uint8, device=f"cuda:{self.ctx.device}")
+        check(lib().vkg_tracer_pixel_data(self.handle, C.c_void_p(out.data_ptr()), C.c_void_p(self.ctx.stream())),
+              self.ctx.handle, "vkg_tracer_pixel_data")
         return out
 
     def reset_accumulator(self):
