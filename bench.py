@@ -303,6 +303,30 @@ def denoise_timing(ctx, pixels, w, h, reps=20):
             "gbs": round(byts / ms / 1e6, 1), "frac_of_hbm": round(byts / ms / 1e6 / peak, 3), "peak": src}
 
 
+def post_fx_timing(ctx, rgb, w, h, reps=20):
+    """Bloom + tonemap (threshold to half resolution, 3 x 2 blur passes, composition) of one frame:
+    CUDA-event time per call. Bytes per full-resolution pixel: the HDR image read twice (16 B each:
+    threshold, composition) and the output (16 B); per half-resolution pixel the threshold write and
+    2 x 3 blur passes reading and writing RGBA16F (8 B each) and the composition's read."""
+    import torch
+    from vierkant_gb300.pathtracer import post_fx
+    hdr = torch.cat([rgb, torch.ones_like(rgb[..., :1])], dim=-1).contiguous()
+    for _ in range(3):
+        post_fx(ctx, hdr)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(torch.cuda.current_stream())
+    for _ in range(reps):
+        post_fx(ctx, hdr)
+    e1.record(torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    byts = w * h * 48 + (w // 2) * (h // 2) * (8 + 6 * 16 + 8)
+    peak, src = measured_peaks()
+    return {"ms": round(ms, 4), "mpix_per_s": round(w * h / ms / 1e3, 1), "gbs": round(byts / ms / 1e6, 1),
+            "frac_of_hbm": round(byts / ms / 1e6 / peak, 3), "peak": src}
+
+
 def path_tracer_block(ctx, frames=256):
     """The radiance estimator on the same scene: the plain tracer at 1280x720 x 64 spp (samples/s,
     Mrays/s, RMSE / bias against the FP64 oracle crop), and the equal-RMSE comparison at 1920x1080:
@@ -339,6 +363,7 @@ def path_tracer_block(ctx, frames=256):
                                "rmse": round(rmse, 4), "bias": round(bias, 5),
                                "oracle": "FP64 4096 spp, 128x128 crop at (576, 528)"}
     out["denoise_720p"] = denoise_timing(ctx, pt.pixel_data(), 1280, 720)
+    out["post_fx_720p"] = post_fx_timing(ctx, pt.render_scene(scene, cam), 1280, 720)
     pt.close()
 
     cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, 1920, 1080)

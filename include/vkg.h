@@ -488,6 +488,21 @@ typedef struct vkg_tracer vkg_tracer;
 vkg_status vkg_settings_default(vkg_settings *out);
 /* the pixel records of the traced window (crop) after the last render: d_out holds width x height */
 vkg_status vkg_tracer_pixel_data(vkg_tracer *tracer, vkg_pixel_data *d_out, void *stream);
+/* bloom + tonemap composition of an HDR rgba image (PBRPathTracer.cpp:405-465): bloom of the
+   half-resolution luma-thresholded image blurred by `blur_iterations` separable 9-tap Gaussian passes
+   (RGBA16F intermediates), then 1 - exp(-(hdr + bloom) * exposure) and pow(., 1 / gamma); tonemap = 0
+   copies the HDR image */
+typedef struct vkg_post_fx_settings
+{
+    uint32_t tonemap, bloom;   /* settings_t::tonemap / bloom */
+    float exposure, gamma;     /* settings_t::exposure (2) / gamma (1) */
+    float brightness_thresh[2]; /* Bloom::create_info_t::brightness_thresh (0.95, 1.1) */
+    uint32_t blur_iterations;  /* 3 (PBRPathTracer.cpp:799) */
+} vkg_post_fx_settings;
+vkg_status vkg_post_fx_default(vkg_post_fx_settings *s);
+vkg_status vkg_post_fx(vkg_ctx *ctx, const float *d_hdr_rgba, uint32_t width, uint32_t height,
+                       const vkg_post_fx_settings *s, float *d_out_rgba, void *stream);
+
 /* the reference's denoise pass (PBRPathTracer.cpp:346-403, denoise.slang): five edge-avoiding
    a-trous passes (steps 1, 2, 4, 8, 16) over albedo-demodulated radiance with luminance, normal and
    depth weights; d_out_rgba: width x height x 4 floats (alpha 0, as the shader writes), d_out_depth

@@ -272,6 +272,19 @@ PIXEL_DTYPE = np.dtype([("radiance", "<f4", 3), ("alpha", "<f4"), ("depth", "<f4
                         ("object_id", "<u4"), ("albedo", "<u4")])
 
 
+def post_fx(hdr_rgba, tonemap=True, bloom=True, exposure=2.0, gamma=1.0, brightness_thresh=(0.95, 1.1),
+            iterations=3):
+    """bloom + tonemap composition of an HDR image [h, w, 4] float32 (oracle/postfx.c)"""
+    src = np.ascontiguousarray(hdr_rgba, np.float32)
+    h, w = src.shape[:2]
+    out = np.zeros_like(src)
+    orc().orc_post_fx.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_int, C.c_int, C.c_float, C.c_float,
+                                  C.c_float, C.c_float, C.c_uint32, C.c_void_p]
+    orc().orc_post_fx(ptr(src), w, h, int(tonemap), int(bloom), exposure, gamma, brightness_thresh[0],
+                      brightness_thresh[1], iterations, ptr(out))
+    return out
+
+
 def denoise(pixels):
     """the a-trous denoise pass over pixel records [h, w] (PIXEL_DTYPE); returns rgba [h, w, 4] float32"""
     px = np.ascontiguousarray(pixels, PIXEL_DTYPE)

@@ -209,6 +209,9 @@ void orc_unpack_snorm_2x16(uint32_t p, float out[2]);
 uint32_t orc_pack_rgba8(float r, float g, float b, float a);
 void orc_unpack_rgb8(uint32_t c, float out[3]);
 void orc_denoise(const orc_pixel *px, uint32_t w, uint32_t h, float *out_rgba);
+/* bloom + tonemap composition of an HDR rgba image (postfx.c) */
+void orc_post_fx(const float *hdr, uint32_t w, uint32_t h, int tonemap, int bloom, float exposure, float gamma,
+                 float lo, float hi, uint32_t iterations, float *out);
 
 /* one BSDF sample / evaluation in FP64 (sample_disney / eval_disney): u = (lobe, x, y); the return
    value of orc_bsdf_eval is the mixture pdf */

@@ -65,6 +65,11 @@ class vkg_settings(C.Structure):
                 ("sun_angular_size", C.c_float), ("denoising", C.c_uint32), ("clip_near", C.c_float)]
 
 
+class vkg_post_fx_settings(C.Structure):
+    _fields_ = [("tonemap", C.c_uint32), ("bloom", C.c_uint32), ("exposure", C.c_float), ("gamma", C.c_float),
+                ("brightness_thresh", C.c_float * 2), ("blur_iterations", C.c_uint32)]
+
+
 class vkg_pixel_data(C.Structure):
     _fields_ = [("radiance", C.c_float * 3), ("alpha", C.c_float), ("depth", C.c_float), ("normal", C.c_uint32),
                 ("object_id", C.c_uint32), ("albedo", C.c_uint32)]
@@ -203,6 +208,8 @@ SIGNATURES = {
     "vkg_scene_set_lights": (I32, [P, P, P, U32]),
     "vkg_tracer_pixel_data": (I32, [P, P, P]),
     "vkg_denoise": (I32, [P, P, U32, U32, P, P, P]),
+    "vkg_post_fx_default": (I32, [C.POINTER(vkg_post_fx_settings)]),
+    "vkg_post_fx": (I32, [P, P, U32, U32, C.POINTER(vkg_post_fx_settings), P, P]),
     "vkg_light_convert": (I32, [C.POINTER(vkg_light_source), P, P, C.POINTER(vkg_light)]),
     "vkg_scene_bvh": (I32, [P, C.POINTER(P)]),
     "vkg_scene_env_tables": (I32, [P, C.POINTER(P), C.POINTER(P), C.POINTER(U32), C.POINTER(U32)]),

@@ -18,7 +18,7 @@ import numpy as np
 import torch
 
 from ._lib import (check, lib, vkg_bvh_info, vkg_camera, vkg_light, vkg_light_source, vkg_pixel_data,
-                   vkg_scene_desc, vkg_settings, vkg_tracer_create_info,
+                   vkg_post_fx_settings, vkg_scene_desc, vkg_settings, vkg_tracer_create_info,
                    vkg_tracer_stats)
 from .raytracing import Context
 
@@ -113,6 +113,30 @@ def denoise(ctx: Context, pixels: torch.Tensor, width: int, height: int, with_de
                             C.c_void_p(dep.data_ptr()) if dep is not None else None, C.c_void_p(ctx.stream())),
           ctx.handle, "vkg_denoise")
     return (out, dep) if with_depth else out
+
+
+def post_fx_settings(**kw) -> vkg_post_fx_settings:
+    """the reference's post-FX defaults (tonemap and bloom on, exposure 2, gamma 1, brightness threshold
+    (0.95, 1.1), 3 blur iterations), with keyword overrides"""
+    s = vkg_post_fx_settings()
+    check(lib().vkg_post_fx_default(C.byref(s)))
+    for k, v in kw.items():
+        if k == "brightness_thresh":
+            s.brightness_thresh[0], s.brightness_thresh[1] = v
+        else:
+            setattr(s, k, v)
+    return s
+
+
+def post_fx(ctx: Context, hdr_rgba: torch.Tensor, settings: vkg_post_fx_settings | None = None) -> torch.Tensor:
+    """Bloom + tonemap composition of an HDR [h, w, 4] float32 CUDA image."""
+    h, w = hdr_rgba.shape[:2]
+    src = hdr_rgba.contiguous()
+    out = torch.empty_like(src)
+    s = settings if settings is not None else post_fx_settings()
+    check(lib().vkg_post_fx(ctx.handle, C.c_void_p(src.data_ptr()), w, h, C.byref(s), C.c_void_p(out.data_ptr()),
+                            C.c_void_p(ctx.stream())), ctx.handle, "vkg_post_fx")
+    return out
 
 
 class _Lights:
