@@ -384,12 +384,13 @@ vkg_status vkg_scene_create(vkg_ctx *ctx, const vkg_scene_desc *desc, vkg_scene 
  * d_materials) a two-level BVH. Mesh triangles are one-sided unless the mesh is flagged two-sided. */
 typedef struct vkg_mesh_desc
 {
-    const float *d_xyz;
+    const float *d_xyz;     /* position of vertex k at byte offset k * vertex_stride */
     uint32_t num_vertices;
     const uint32_t *d_indices;
     uint32_t num_tris;
     uint32_t twosided;
-    uint32_t pad;
+    uint32_t vertex_stride; /* bytes between positions, a multiple of 4 (0: 12, packed xyz; 24: the
+                               reference's packed_vertex_t, packed_vertex.slang:17-23) */
 } vkg_mesh_desc;
 typedef struct vkg_instanced_scene_desc
 {
@@ -448,6 +449,27 @@ typedef struct vkg_settings
     float clip_near;                  /* the camera's near clipping distance, for the pixel depth
                                          near / view-space distance (camera_params.hpp:37); 0: 0.1 */
 } vkg_settings;
+
+/* ---- glTF 2.0 ingestion (host only; the reference's model/gltf.cpp path) --------------------
+ * vkg_gltf_load reads a .gltf (base64 or file buffers) or .glb file into meshes (one per triangle
+ * primitive; float positions, uint32 indices), instances (node placements, object -> world 3x4,
+ * mesh index in `blas`, material), materials (vkg_material) and KHR_lights_punctual lights
+ * (vkg_light); those feed vkg_scene_create_instanced and vkg_scene_set_lights. Errors: a status and
+ * the message in err (may be NULL). The mesh pointers stay valid until vkg_gltf_destroy. */
+typedef struct vkg_gltf vkg_gltf;
+typedef struct vkg_gltf_counts
+{
+    uint32_t num_meshes, num_instances, num_materials, num_lights;
+    uint32_t skipped_primitives; /* non-triangle primitives left out */
+} vkg_gltf_counts;
+vkg_status vkg_gltf_load(const char *path, vkg_gltf **out, char *err, size_t err_len);
+vkg_status vkg_gltf_counts_get(const vkg_gltf *g, vkg_gltf_counts *out);
+vkg_status vkg_gltf_mesh(const vkg_gltf *g, uint32_t index, const float **xyz, uint32_t *num_vertices,
+                         const uint32_t **indices, uint32_t *num_tris);
+vkg_status vkg_gltf_instances(const vkg_gltf *g, vkg_instance *out);
+vkg_status vkg_gltf_materials(const vkg_gltf *g, vkg_material *out);
+vkg_status vkg_gltf_lights(const vkg_gltf *g, vkg_light *out);
+vkg_status vkg_gltf_destroy(vkg_gltf *g);
 
 /* per-pixel output record, the layout of the reference's pixel_data_t (pixel_data.slang:9-21):
    accumulated radiance, coverage of the last batch, reversed-z depth, primary-hit normal

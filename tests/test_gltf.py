@@ -1,0 +1,155 @@
+"""glTF 2.0 ingestion (vkg_gltf_*; host only, no GPU): the loader against assets written by
+tests/gltf_writer.py — the three container forms, node hierarchies with matrix and TRS transforms
+(checked against numpy compositions), uint16 / uint32 / absent indices, skipped non-triangle
+primitives, materials with the KHR extensions, KHR_lights_punctual placement (convert_light), and
+malformed inputs that must fail with a message."""
+import json
+import math
+
+import numpy as np
+import pytest
+
+from gltf_writer import write
+from vierkant_gb300.gltf import load_gltf
+from vierkant_gb300.pathtracer import LIGHT_DIRECTIONAL, LIGHT_OMNI, LIGHT_SPOT
+
+TRI = (np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), np.array([[0, 1, 2]]))
+QUAD = (np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]], np.float32), np.array([[0, 1, 2], [0, 2, 3]]))
+
+
+def quat(axis, angle):
+    a = np.asarray(axis, np.float64) / np.linalg.norm(axis)
+    s = math.sin(angle / 2)
+    return [a[0] * s, a[1] * s, a[2] * s, math.cos(angle / 2)]
+
+
+def trs_matrix(t=(0, 0, 0), q=(0, 0, 0, 1), s=(1, 1, 1)):
+    x, y, z, w = q
+    R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                  [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                  [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+    M = np.eye(4)
+    M[:3, :3] = R * np.asarray(s)[None, :]
+    M[:3, 3] = t
+    return M
+
+
+@pytest.mark.parametrize("mode", ["embedded", "external", "glb"])
+def test_containers_and_hierarchy(tmp_path, mode):
+    child_m = trs_matrix((0.5, -1, 2), quat((0, 1, 0), 0.3), (2, 2, 2))
+    nodes = [dict(mesh=0, translation=[1, 2, 3], rotation=quat((1, 1, 0), 0.7), scale=[0.5, 0.5, 0.5],
+                  children=[1, 2]),
+             dict(mesh=1, matrix=list(child_m.T.reshape(-1))),   # column-major
+             dict(children=[3], translation=[0, 0, -4]),
+             dict(mesh=0)]
+    path = tmp_path / ("a.glb" if mode == "glb" else "a.gltf")
+    write(path, [[(*TRI, None, None)], [(*QUAD, None, None), (*TRI, None, None)]], nodes, [0], mode=mode)
+    a = load_gltf(str(path))
+    assert len(a["meshes"]) == 3  # mesh 0: one primitive, mesh 1: two
+    assert np.array_equal(a["meshes"][0][0], TRI[0]) and np.array_equal(a["meshes"][1][1], QUAD[1])
+    W0 = trs_matrix((1, 2, 3), quat((1, 1, 0), 0.7), (0.5, 0.5, 0.5))
+    # breadth first: node 0, node 1 (two primitives), node 2 (no mesh), node 3
+    expect = [(W0, 0), (W0 @ child_m, 1), (W0 @ child_m, 2), (W0 @ trs_matrix((0, 0, -4)), 0)]
+    inst = a["instances"]
+    assert len(inst) == len(expect)
+    for k, (M, mesh) in enumerate(expect):
+        assert inst[k]["blas"] == mesh and inst[k]["material"] == 0
+        assert np.allclose(inst[k]["transform"].reshape(3, 4), M[:3, :], atol=1e-6)
+    assert len(a["materials"]) == 1 and a["materials"][0]["ior"] == np.float32(1.5)  # the default material
+
+
+@pytest.mark.parametrize("itype", [np.uint32, np.uint16, np.uint8])
+def test_index_types_and_skipped_primitives(tmp_path, itype):
+    path = tmp_path / "b.gltf"
+    write(path, [[(*QUAD, None, None), (*QUAD, None, 1), (*TRI, 5, None), (TRI[0], None, None, None)]],
+          [dict(mesh=0)], [0], index_type=itype)
+    a = load_gltf(str(path))
+    assert a["skipped_primitives"] == 1  # mode 1 (LINES) is left out
+    assert len(a["meshes"]) == 3
+    assert np.array_equal(a["meshes"][0][1], QUAD[1])
+    assert np.array_equal(a["meshes"][1][1], TRI[1])
+    assert np.array_equal(a["meshes"][2][1], [[0, 1, 2]])  # no indices: sequential
+    assert list(a["instances"]["material"]) == [0, 0, 0]  # material 5 does not exist -> 0
+
+
+def test_materials(tmp_path):
+    mats = [
+        {"pbrMetallicRoughness": {"baseColorFactor": [0.2, 0.4, 0.6, 1], "metallicFactor": 0.25,
+                                  "roughnessFactor": 0.75},
+         "emissiveFactor": [1, 0.5, 0.25], "doubleSided": True,
+         "extensions": {"KHR_materials_emissive_strength": {"emissiveStrength": 4.0}}},
+        {"extensions": {"KHR_materials_transmission": {"transmissionFactor": 0.9},
+                        "KHR_materials_ior": {"ior": 1.33},
+                        "KHR_materials_clearcoat": {"clearcoatFactor": 0.5, "clearcoatRoughnessFactor": 0.1},
+                        "KHR_materials_sheen": {"sheenColorFactor": [0.1, 0.2, 0.3], "sheenRoughnessFactor": 0.4},
+                        "KHR_materials_diffuse_transmission": {"diffuseTransmissionFactor": 0.3,
+                                                               "diffuseTransmissionColorFactor": [1, 0.5, 0]}}},
+        {},
+    ]
+    path = tmp_path / "m.gltf"
+    write(path, [[(*TRI, 0, None), (*TRI, 1, None), (*TRI, None, None)]], [dict(mesh=0)], [0], materials=mats)
+    a = load_gltf(str(path))
+    m = a["materials"]
+    assert np.allclose(m[0]["base_color"], (0.2, 0.4, 0.6)) and m[0]["metalness"] == np.float32(0.25)
+    assert m[0]["roughness"] == np.float32(0.75) and m[0]["twosided"] == 1
+    assert np.allclose(m[0]["emission"], (4.0, 2.0, 1.0))
+    assert m[1]["transmission"] == np.float32(0.9) and m[1]["ior"] == np.float32(1.33)
+    assert m[1]["clearcoat"] == np.float32(0.5) and m[1]["clearcoat_roughness"] == np.float32(0.1)
+    assert np.allclose(m[1]["sheen_color"], (0.1, 0.2, 0.3)) and m[1]["sheen_roughness"] == np.float32(0.4)
+    assert m[1]["diffuse_transmission"] == np.float32(0.3)
+    assert np.allclose(m[1]["diffuse_transmission_color"], (1, 0.5, 0))
+    # glTF defaults: metallic 1, roughness 1, white
+    assert m[2]["metalness"] == 1 and m[2]["roughness"] == 1 and np.all(m[2]["base_color"] == 1)
+    assert list(a["instances"]["material"]) == [0, 1, 0]  # no material -> index 0, as the reference
+
+
+def test_lights(tmp_path):
+    lights = [{"type": "point", "color": [1, 0.5, 0.25], "intensity": 3.0, "range": 10.0},
+              {"type": "spot", "intensity": 2.0, "spot": {"innerConeAngle": 0.2, "outerConeAngle": 0.5}},
+              {"type": "directional"}]
+    q = quat((1, 0, 0), -math.pi / 2)  # -z -> -y: a light pointing down
+    nodes = [dict(light=0, translation=[1, 2, 3]), dict(light=1, rotation=q, translation=[0, 5, 0]),
+             dict(light=2, rotation=quat((0, 1, 0), 0.4))]
+    path = tmp_path / "l.gltf"
+    write(path, [[(*TRI, None, None)]], nodes, [0, 1, 2], lights=lights)
+    L = load_gltf(str(path))["lights"]
+    assert len(L) == 3
+    assert L[0]["type"] == LIGHT_OMNI and np.allclose(L[0]["position"], (1, 2, 3)) and L[0]["range"] == 10
+    assert np.allclose(L[0]["color"], (1, 0.5, 0.25)) and L[0]["intensity"] == 3
+    assert L[1]["type"] == LIGHT_SPOT and np.allclose(L[1]["direction"], (0, -1, 0), atol=1e-6)
+    sc = 1.0 / max(0.001, math.cos(0.2) - math.cos(0.5))
+    assert np.isclose(L[1]["spot_angle_scale"], sc, rtol=1e-5)
+    assert np.isclose(L[1]["spot_angle_offset"], -math.cos(0.5) * sc, rtol=1e-5)
+    assert L[2]["type"] == LIGHT_DIRECTIONAL and np.isinf(L[2]["range"])
+    assert np.allclose(L[2]["direction"], (-math.sin(0.4), 0, -math.cos(0.4)), atol=1e-6)
+
+
+@pytest.mark.parametrize("kind", ["missing", "notjson", "version", "oob_index", "short_buffer", "no_position",
+                                  "bad_glb", "deep"])
+def test_malformed_inputs_fail(tmp_path, kind):
+    path = tmp_path / "x.gltf"
+    if kind == "missing":
+        path = tmp_path / "nope.gltf"
+    elif kind == "notjson":
+        path.write_text("{\"asset\": {\"version\": \"2.0\"},")
+    elif kind == "version":
+        path.write_text(json.dumps({"asset": {"version": "1.0"}}))
+    elif kind == "oob_index":
+        write(path, [[(TRI[0], np.array([[0, 1, 7]]), None, None)]], [dict(mesh=0)], [0])
+    elif kind == "short_buffer":
+        write(path, [[(*TRI, None, None)]], [dict(mesh=0)], [0])
+        d = json.loads(path.read_text())
+        d["buffers"][0]["byteLength"] += 100
+        path.write_text(json.dumps(d))
+    elif kind == "no_position":
+        write(path, [[(*TRI, None, None)]], [dict(mesh=0)], [0])
+        d = json.loads(path.read_text())
+        d["meshes"][0]["primitives"][0]["attributes"] = {}
+        path.write_text(json.dumps(d))
+    elif kind == "bad_glb":
+        path = tmp_path / "x.glb"
+        path.write_bytes(b"glTF" + (2).to_bytes(4, "little") + (10 ** 6).to_bytes(4, "little"))
+    elif kind == "deep":
+        path.write_text("[" * 5000 + "]" * 5000)
+    with pytest.raises(ValueError):
+        load_gltf(str(path))

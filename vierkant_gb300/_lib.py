@@ -70,6 +70,11 @@ class vkg_post_fx_settings(C.Structure):
                 ("brightness_thresh", C.c_float * 2), ("blur_iterations", C.c_uint32)]
 
 
+class vkg_gltf_counts(C.Structure):
+    _fields_ = [("num_meshes", C.c_uint32), ("num_instances", C.c_uint32), ("num_materials", C.c_uint32),
+                ("num_lights", C.c_uint32), ("skipped_primitives", C.c_uint32)]
+
+
 class vkg_pixel_data(C.Structure):
     _fields_ = [("radiance", C.c_float * 3), ("alpha", C.c_float), ("depth", C.c_float), ("normal", C.c_uint32),
                 ("object_id", C.c_uint32), ("albedo", C.c_uint32)]
@@ -100,7 +105,7 @@ class vkg_tlas_info(C.Structure):
 
 class vkg_mesh_desc(C.Structure):
     _fields_ = [("d_xyz", C.c_void_p), ("num_vertices", C.c_uint32), ("d_indices", C.c_void_p),
-                ("num_tris", C.c_uint32), ("twosided", C.c_uint32), ("pad", C.c_uint32)]
+                ("num_tris", C.c_uint32), ("twosided", C.c_uint32), ("vertex_stride", C.c_uint32)]
 
 
 class vkg_instanced_scene_desc(C.Structure):
@@ -209,6 +214,14 @@ SIGNATURES = {
     "vkg_tracer_pixel_data": (I32, [P, P, P]),
     "vkg_denoise": (I32, [P, P, U32, U32, P, P, P]),
     "vkg_post_fx_default": (I32, [C.POINTER(vkg_post_fx_settings)]),
+    "vkg_gltf_load": (I32, [C.c_char_p, C.POINTER(P), C.c_char_p, C.c_size_t]),
+    "vkg_gltf_counts_get": (I32, [P, C.POINTER(vkg_gltf_counts)]),
+    "vkg_gltf_mesh": (I32, [P, U32, C.POINTER(C.POINTER(C.c_float)), C.POINTER(U32), C.POINTER(C.POINTER(U32)),
+                            C.POINTER(U32)]),
+    "vkg_gltf_instances": (I32, [P, P]),
+    "vkg_gltf_materials": (I32, [P, P]),
+    "vkg_gltf_lights": (I32, [P, P]),
+    "vkg_gltf_destroy": (I32, [P]),
     "vkg_post_fx": (I32, [P, P, U32, U32, C.POINTER(vkg_post_fx_settings), P, P]),
     "vkg_light_convert": (I32, [C.POINTER(vkg_light_source), P, P, C.POINTER(vkg_light)]),
     "vkg_scene_bvh": (I32, [P, C.POINTER(P)]),

@@ -488,6 +488,10 @@ vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_de
         const vkg_mesh_desc &M = d->meshes[m];
         if(M.num_tris && (!M.d_xyz || !M.d_indices || M.num_vertices == 0))
             return fail(set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_create_instanced: mesh %u has no geometry", m));
+        const size_t stride = M.vertex_stride ? M.vertex_stride : 12u;
+        if(stride < 12u || stride % 4u)
+            return fail(set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
+                                  "vkg_scene_create_instanced: mesh %u: vertex_stride must be 0 or a multiple of 4 >= 12", m));
         float *xyz = nullptr;
         uint32_t *idx = nullptr;
         chk(cudaMalloc(&xyz, std::max<size_t>(M.num_vertices, 1) * 3 * sizeof(float)));
@@ -496,7 +500,10 @@ vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_de
         sc->mesh_idx.push_back(idx);
         if(M.num_tris)
         {
-            chk(cudaMemcpyAsync(xyz, M.d_xyz, (size_t)M.num_vertices * 3 * sizeof(float), cudaMemcpyDeviceToDevice, st));
+            if(stride == 12u)
+                chk(cudaMemcpyAsync(xyz, M.d_xyz, (size_t)M.num_vertices * 3 * sizeof(float), cudaMemcpyDeviceToDevice, st));
+            else // positions out of interleaved vertex records
+                chk(cudaMemcpy2DAsync(xyz, 12, M.d_xyz, stride, 12, M.num_vertices, cudaMemcpyDeviceToDevice, st));
             chk(cudaMemcpyAsync(idx, M.d_indices, (size_t)M.num_tris * 3 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
         }
         if(e != cudaSuccess) break;

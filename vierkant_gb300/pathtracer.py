@@ -200,8 +200,15 @@ class Scene(_Lights):
             pass
 
 
+# the reference's packed_vertex_t (packed_vertex.slang:17-23): position, octahedral normal and tangent,
+# fp16 texture coordinates; 24 bytes
+PACKED_VERTEX_DTYPE = np.dtype([("position", "<f4", 3), ("normal", "<u4"), ("tangent", "<u4"),
+                                ("texcoord", "<f2", 2)])
+
+
 class InstancedScene(_Lights):
-    """A two-level scene: meshes [(xyz, indices, twosided)] each with its own BVH, instances
+    """A two-level scene: meshes [(xyz, indices, twosided)] each with its own BVH (xyz: float [V, 3] or
+    PACKED_VERTEX_DTYPE records), instances
     (raytracing.INSTANCE_DTYPE: object -> world transform, mesh, material) under a top-level BVH,
     materials (MATERIAL_DTYPE) and the environment map. Renders with PBRPathTracer like Scene."""
 
@@ -213,10 +220,16 @@ class InstancedScene(_Lights):
         self._keep = []
         descs = (vkg_mesh_desc * max(1, len(meshes)))()
         for k, (xyz, idx, twosided) in enumerate(meshes):
-            x = torch.from_numpy(np.ascontiguousarray(xyz, np.float32)).to(dev)
+            if xyz.dtype == PACKED_VERTEX_DTYPE:
+                # the reference's packed_vertex_t records: positions read with a 24-byte stride
+                x = torch.from_numpy(np.ascontiguousarray(xyz).view(np.uint8).copy()).to(dev)
+                nv, stride = len(xyz), PACKED_VERTEX_DTYPE.itemsize
+            else:
+                x = torch.from_numpy(np.ascontiguousarray(xyz, np.float32)).to(dev)
+                nv, stride = x.shape[0], 0
             i = torch.from_numpy(np.ascontiguousarray(idx, np.uint32).view(np.int32)).to(dev)
             self._keep += [x, i]
-            descs[k] = vkg_mesh_desc(x.data_ptr(), x.shape[0], i.data_ptr(), i.shape[0], int(twosided), 0)
+            descs[k] = vkg_mesh_desc(x.data_ptr(), nv, i.data_ptr(), i.shape[0], int(twosided), stride)
         inst = torch.from_numpy(np.ascontiguousarray(instances, INSTANCE_DTYPE).view(np.uint8).copy()).to(dev)
         mats = torch.from_numpy(np.frombuffer(np.ascontiguousarray(materials).tobytes(), np.uint8).copy()).to(dev)
         env = env_rgb.to(dev, torch.float32).contiguous()
