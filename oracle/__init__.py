@@ -246,7 +246,8 @@ MATERIAL_DTYPE = np.dtype([("base_color", "<f4", 3), ("roughness", "<f4"), ("met
                            ("emission", "<f4", 3), ("twosided", "<u4"), ("transmission", "<f4"), ("ior", "<f4"),
                            ("clearcoat", "<f4"), ("clearcoat_roughness", "<f4"), ("sheen_color", "<f4", 3),
                            ("sheen_roughness", "<f4"), ("diffuse_transmission", "<f4"),
-                           ("diffuse_transmission_color", "<f4", 3), ("pad", "<f4", 3)])
+                           ("diffuse_transmission_color", "<f4", 3), ("iridescence", "<f4"),
+                           ("iridescence_ior", "<f4"), ("iridescence_thickness", "<f4")])
 
 
 class orc_pt_scene(C.Structure):

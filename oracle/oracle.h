@@ -124,7 +124,7 @@ typedef struct {
     float transmission, ior, clearcoat, clearcoat_roughness;
     float sheen_color[3], sheen_roughness;
     float diffuse_transmission, diffuse_transmission_color[3];
-    float pad[3];
+    float iridescence, iridescence_ior, iridescence_thickness;
 } orc_pt_material; /* same 96-byte layout as vkg_material */
 
 typedef struct {
@@ -217,6 +217,8 @@ void orc_post_fx(const float *hdr, uint32_t w, uint32_t h, int tonemap, int bloo
    value of orc_bsdf_eval is the mixture pdf */
 void orc_bsdf_sample(const orc_pt_material *m, const double n[3], const double v[3], double eta, const double u[3],
                      double dir[3], double *pdf, double f[3], int *transmission);
+void orc_iridescent_fresnel(double outside, double film, const double f0[3], double thickness, double cos1,
+                            double out[3]);
 double orc_bsdf_eval(const orc_pt_material *m, const double l[3], const double n[3], const double v[3], double eta,
                      double f[3]);
 /* FP64 env tables from an rgb map: weights (mean 1, as float) and the CDF (w*h+1 doubles) */

@@ -546,6 +546,7 @@ static void d_transmit_raw(const orc_pt_job *J, double ox, double oy, double oz,
 #define DRAW_RAW f_draw_raw
 #define TRANS_RAW f_transmit_raw
 #define RASIN(x) asinf(x)
+#define REXP(x) expf(x)
 #include "pt_core.inc"
 #undef REAL
 #undef SFX
@@ -563,6 +564,7 @@ static void d_transmit_raw(const orc_pt_job *J, double ox, double oy, double oz,
 #undef DRAW_RAW
 #undef TRANS_RAW
 #undef RASIN
+#undef REXP
 
 #define REAL double
 #define SFX(n) d_##n
@@ -580,6 +582,7 @@ static void d_transmit_raw(const orc_pt_job *J, double ox, double oy, double oz,
 #define DRAW_RAW d_draw_raw
 #define TRANS_RAW d_transmit_raw
 #define RASIN(x) asin(x)
+#define REXP(x) exp(x)
 #include "pt_core.inc"
 
 void orc_sun_light(const float color[3], float intensity, const float spherical_coords[2], float angular_size,
@@ -609,6 +612,13 @@ void orc_bsdf_sample(const orc_pt_material *mt, const double n[3], const double 
                   transmission);
     dir[0] = d.x, dir[1] = d.y, dir[2] = d.z;
     f[0] = fv.x, f[1] = fv.y, f[2] = fv.z;
+}
+
+void orc_iridescent_fresnel(double outside, double film, const double f0[3], double thickness, double cos1,
+                            double out[3])
+{
+    d_v3 r = d_iridescent_fresnel(outside, film, d_mk(f0[0], f0[1], f0[2]), thickness, cos1);
+    out[0] = r.x, out[1] = r.y, out[2] = r.z;
 }
 
 double orc_bsdf_eval(const orc_pt_material *mt, const double l[3], const double n[3], const double v[3], double eta,

@@ -83,7 +83,10 @@ def test_materials(tmp_path):
                         "KHR_materials_clearcoat": {"clearcoatFactor": 0.5, "clearcoatRoughnessFactor": 0.1},
                         "KHR_materials_sheen": {"sheenColorFactor": [0.1, 0.2, 0.3], "sheenRoughnessFactor": 0.4},
                         "KHR_materials_diffuse_transmission": {"diffuseTransmissionFactor": 0.3,
-                                                               "diffuseTransmissionColorFactor": [1, 0.5, 0]}}},
+                                                               "diffuseTransmissionColorFactor": [1, 0.5, 0]},
+                        "KHR_materials_iridescence": {"iridescenceFactor": 0.8, "iridescenceIOR": 1.4,
+                                                      "iridescenceThicknessMinimum": 150,
+                                                      "iridescenceThicknessMaximum": 520}}},
         {},
     ]
     path = tmp_path / "m.gltf"
@@ -98,6 +101,9 @@ def test_materials(tmp_path):
     assert np.allclose(m[1]["sheen_color"], (0.1, 0.2, 0.3)) and m[1]["sheen_roughness"] == np.float32(0.4)
     assert m[1]["diffuse_transmission"] == np.float32(0.3)
     assert np.allclose(m[1]["diffuse_transmission_color"], (1, 0.5, 0))
+    assert m[1]["iridescence"] == np.float32(0.8) and m[1]["iridescence_ior"] == np.float32(1.4)
+    assert m[1]["iridescence_thickness"] == 520  # the range's maximum, as the shader reads it
+    assert m[0]["iridescence"] == 0 and m[0]["iridescence_ior"] == np.float32(1.3)
     # glTF defaults: metallic 1, roughness 1, white
     assert m[2]["metalness"] == 1 and m[2]["roughness"] == 1 and np.all(m[2]["base_color"] == 1)
     assert list(a["instances"]["material"]) == [0, 1, 0]  # no material -> index 0, as the reference

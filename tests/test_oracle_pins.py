@@ -245,7 +245,8 @@ def test_fp64_oracle_glass_white_furnace():
     assert 0.9 < rough.mean() < 1.0
 
 
-@pytest.mark.parametrize("kind", ["diffuse", "sheen", "metal", "plastic", "diffuse_transmission", "clearcoat"])
+@pytest.mark.parametrize("kind", ["diffuse", "sheen", "metal", "plastic", "diffuse_transmission", "clearcoat",
+                                  "iridescent_metal"])
 def test_fp64_bsdf_sampling_matches_evaluation(kind):
     """sample_disney and eval_disney describe the same BSDF (bsdf_disney.slang:162-381): the albedo
     integral of f |cos| estimated from the sampler's f / pdf equals the one integrated over uniform
@@ -268,6 +269,9 @@ def test_fp64_bsdf_sampling_matches_evaluation(kind):
         m["diffuse_transmission"][0], m["diffuse_transmission_color"][0] = 0.6, (0.5, 0.7, 0.9)
     elif kind == "clearcoat":
         m["clearcoat"][0], m["clearcoat_roughness"][0] = 1.0, 0.3
+    elif kind == "iridescent_metal":
+        m["iridescence"][0], m["iridescence_ior"][0], m["iridescence_thickness"][0] = 0.7, 1.3, 400.0
+        m["metalness"][0] = 1.0
     rng = np.random.default_rng(1)
     n_ = np.array([0.0, 0.0, 1.0])
     th = math.radians(40)
@@ -278,12 +282,22 @@ def test_fp64_bsdf_sampling_matches_evaluation(kind):
         d, pdf, f, _ = oracle.bsdf_sample(m, n_, v, 1.0, rng.random(3))
         if pdf > 0:
             a += f * abs(d[2]) / max(pdf, 1e-3)
+    # the reference picks the thin-film or the plain specular lobe with probability s / 1 - s and puts
+    # it into the pdf but leaves the lobe's value unweighted (bsdf_disney.slang:195-206, :266-277), while
+    # eval_disney weights the values by s / 1 - s: for a metal the sampled albedo is therefore
+    # eval(s) + eval(1 - s). Restated as written.
+    flips = [m]
+    if kind == "iridescent_metal":
+        m2 = m.copy()
+        m2["iridescence"][0] = 1.0 - m["iridescence"][0]
+        flips.append(m2)
     b = np.zeros(3)
     for _ in range(count):
         z, p = 2 * rng.random() - 1, 2 * math.pi * rng.random()
         r = math.sqrt(max(0.0, 1 - z * z))
-        f, _ = oracle.bsdf_eval(m, np.array([r * math.cos(p), r * math.sin(p), z]), n_, v, 1.0)
-        b += f * abs(z) * 4 * math.pi
+        for mm in flips:
+            f, _ = oracle.bsdf_eval(mm, np.array([r * math.cos(p), r * math.sin(p), z]), n_, v, 1.0)
+            b += f * abs(z) * 4 * math.pi
     ratio = a / b
     assert np.all(np.abs(ratio - 1.0) < 0.03), ratio
 
@@ -370,3 +384,61 @@ def test_denoise_restatement_properties():
     px["radiance"][11, 15] = (10.0, 10.0, 10.0)
     out = oracle.denoise(px)
     assert out[11, 15, 0] > 9.0
+
+
+
+def _iridescent_fresnel_numpy(outside, film, f0, thickness, cos1):
+    """an independent transcription of utils/bsdf.slang:83-150 (thin film over a base of reflectance f0)"""
+    xyz_to_rgb = np.array([[3.2404542, -0.9692660, 0.0556434], [-1.5371385, 1.8760108, -0.2040259],
+                           [-0.4985314, 0.0415560, 1.0572252]])  # rows: the shader's float3x3 rows
+
+    def sensitivity(opd, shift):
+        phase = 2 * math.pi * opd * 1e-9
+        val = np.array([5.4856e-13, 4.4201e-13, 5.2481e-13])
+        pos = np.array([1.6810e+06, 1.7953e+06, 2.2084e+06])
+        var = np.array([4.3278e+09, 9.3046e+09, 6.6121e+09])
+        xyz = val * np.sqrt(2 * math.pi * var) * np.cos(pos * phase + shift) * np.exp(-phase ** 2 * var)
+        xyz[0] += 9.7470e-14 * math.sqrt(2 * math.pi * 4.5282e+09) * math.cos(2.2399e+06 * phase + shift[0]) * \
+            math.exp(-4.5282e+09 * phase ** 2)
+        return (xyz / 1.0685e-7) @ xyz_to_rgb
+
+    schlick = lambda c, r0: r0 + (1 - r0) * (1 - c) ** 5
+    R12 = schlick(cos1, ((film - outside) / (film + outside)) ** 2)
+    T121 = 1 - R12
+    cos2sq = 1 - (outside / film) ** 2 * (1 - cos1 ** 2)
+    if cos2sq < 0:
+        return np.ones(3)
+    cos2 = math.sqrt(cos2sq)
+    q = np.sqrt(np.clip(f0, 0, 0.9999) + 0.0001)
+    base = (1 + q) / (1 - q)
+    R23 = schlick(cos2, ((base - film) / (base + film)) ** 2)
+    phi = (math.pi - (math.pi if film < outside else 0.0)) + np.where(base < film, math.pi, 0.0)
+    opd = 2 * film * thickness * cos2
+    R123 = np.clip(R12 * R23, 1e-5, 0.9999)
+    Rs = T121 ** 2 * R23 / (1 - R123)
+    I = R12 + Rs
+    Cm = Rs - T121
+    for k in (1, 2):
+        Cm = Cm * np.sqrt(R123)
+        I = I + Cm * 2 * sensitivity(k * opd, k * phi)
+    return np.maximum(I, 0)
+
+
+def test_iridescent_fresnel_against_independent_transcription():
+    """the oracle's thin-film Fresnel (pt_core.inc, double) equals a second transcription of the
+    reference's formula in numpy over films, bases, thicknesses and angles (total internal
+    reflection in the film included)"""
+    L = oracle.orc()
+    L.orc_iridescent_fresnel.argtypes = [C.c_double, C.c_double, C.c_void_p, C.c_double, C.c_double, C.c_void_p]
+    rng = np.random.default_rng(8)
+    for _ in range(300):
+        film = rng.uniform(1.0, 2.2)
+        outside = 1.0 if rng.random() < 0.8 else rng.uniform(1.0, 2.5)
+        f0 = rng.uniform(0.0, 1.0, 3)
+        thick = rng.uniform(0.0, 1200.0)
+        cos1 = rng.uniform(0.0, 1.0)
+        out = np.zeros(3)
+        L.orc_iridescent_fresnel(outside, film, ptr(np.ascontiguousarray(f0)), thick, cos1, ptr(out))
+        ref = _iridescent_fresnel_numpy(outside, film, f0, thick, cos1)
+        # the oracle keeps the shader's single-precision constants (as the GPU does): ~1e-7 of the O(1) terms
+        assert np.allclose(out, ref, rtol=2e-6, atol=1e-6), (out, ref)

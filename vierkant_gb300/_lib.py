@@ -47,7 +47,8 @@ class vkg_material(C.Structure):
                 ("emission", C.c_float * 3), ("twosided", C.c_uint32), ("transmission", C.c_float),
                 ("ior", C.c_float), ("clearcoat", C.c_float), ("clearcoat_roughness", C.c_float),
                 ("sheen_color", C.c_float * 3), ("sheen_roughness", C.c_float), ("diffuse_transmission", C.c_float),
-                ("diffuse_transmission_color", C.c_float * 3), ("pad", C.c_float * 3)]
+                ("diffuse_transmission_color", C.c_float * 3), ("iridescence", C.c_float),
+                ("iridescence_ior", C.c_float), ("iridescence_thickness", C.c_float)]
 
 
 class vkg_camera(C.Structure):

@@ -715,6 +715,8 @@ vkg_status vkg_material_defaults(vkg_material *m)
     for(int c = 0; c < 3; ++c) m->base_color[c] = m->diffuse_transmission_color[c] = 1.f;
     m->roughness = 1.f;
     m->ior = 1.5f;
+    m->iridescence_ior = 1.3f;
+    m->iridescence_thickness = 400.f;
     return VKG_OK;
 }
 

@@ -12,13 +12,14 @@
 //     the primitive's material, 0 when it has none (the reference's default index);
 //   * the materials (gltf.cpp:316-560): base colour, metallic (default 1), roughness (default 1),
 //     emissive x KHR_materials_emissive_strength, doubleSided, KHR_materials_transmission,
-//     KHR_materials_ior, KHR_materials_clearcoat, KHR_materials_sheen,
-//     KHR_materials_diffuse_transmission; a default material when the asset has none;
+//     KHR_materials_ior, KHR_materials_clearcoat, KHR_materials_sheen, KHR_materials_iridescence (the
+//     film thickness is the range's maximum, as the shader reads it), KHR_materials_diffuse_transmission;
+//     a default material when the asset has none;
 //   * KHR_lights_punctual lights placed by their nodes (gltf.cpp:1043-1061, :1182-1190), converted as
 //     convert_light does (punctual_light.hpp:92-111): position = translation, direction = R (0,0,-1),
 //     tangent = R (1,0,0), R the node's rotation (its world matrix's columns normalised).
 // Not read: textures and texture transforms, skins, morph targets, animations, cameras, volumes,
-// specular, iridescence, sparse accessors, quantised positions. The reference composes transforms as
+// specular, sparse accessors, quantised positions. The reference composes transforms as
 // translation / quaternion / scale triples and projects shear away (transform.hpp:106-128); the
 // matrix composition here is the same for every chain without shear.
 #include "internal.hpp"
@@ -562,6 +563,12 @@ struct loader
                 r.sheen_color[0] = r.sheen_color[1] = r.sheen_color[2] = 0.f;
                 rd(e, "sheenColorFactor", r.sheen_color, 3);
                 r.sheen_roughness = (float)std::max(0.0, e->num("sheenRoughnessFactor", 0.0));
+            }
+            if(const jv *e = ext->get("KHR_materials_iridescence"))
+            {
+                r.iridescence = clampf(e->num("iridescenceFactor", 0.0), 0, 1);
+                r.iridescence_ior = (float)e->num("iridescenceIOR", 1.3);
+                r.iridescence_thickness = (float)e->num("iridescenceThicknessMaximum", 400.0);
             }
             if(const jv *e = ext->get("KHR_materials_diffuse_transmission"))
             {

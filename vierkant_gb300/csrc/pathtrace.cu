@@ -139,6 +139,11 @@ vkg_status check_material_values(vkg_ctx *ctx, const vkg_material *d_mats, uint3
         if(!unit(m.transmission) || !unit(m.diffuse_transmission) || !unit(m.metalness))
             return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
                              "%s: material %u: metalness, transmission and diffuse_transmission must be in [0, 1]", fn, i);
+        if(!unit(m.iridescence) ||
+           (m.iridescence > 0.f && (!(m.iridescence_ior > 0.f) || !(m.iridescence_thickness >= 0.f) ||
+                                    !std::isfinite(m.iridescence_ior) || !std::isfinite(m.iridescence_thickness))))
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
+                             "%s: material %u: iridescence in [0, 1] needs an ior > 0 and a thickness >= 0", fn, i);
         if(m.transmission > 0.f && !(m.ior > 0.f && std::isfinite(m.ior)))
             return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "%s: material %u: a transmissive material needs ior > 0",
                              fn, i);

@@ -1,5 +1,5 @@
 // Device math of the path tracer: environment lookup / importance sampling, vierkant's Disney BSDF
-// (all lobes but iridescence), sampling helpers and MIS weights.
+// (all lobes, iridescence included), sampling helpers and MIS weights.
 //
 // Restated from the reference shaders:
 //   sample_disney / eval_disney   shaders/slang/ray/bsdf_disney.slang:162-296, :298-381
@@ -59,7 +59,7 @@ __host__ __device__ inline bool material_unculled(const vkg_material &m)
 __host__ __device__ inline bool material_full(const vkg_material &m)
 {
     return m.transmission > 0.f || m.clearcoat > 0.f || m.diffuse_transmission > 0.f || m.sheen_color[0] > 0.f ||
-           m.sheen_color[1] > 0.f || m.sheen_color[2] > 0.f;
+           m.sheen_color[1] > 0.f || m.sheen_color[2] > 0.f || m.iridescence > 0.f;
 }
 
 __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
@@ -147,7 +147,7 @@ __device__ __forceinline__ float3 env_sample(const env_view &e, float u0, float 
     return d;
 }
 
-// ---- BSDF (bsdf_disney.slang without iridescence) -------------------------------------------
+// ---- BSDF (bsdf_disney.slang) --------------------------------------------------------------------
 struct material_view
 {
     float3 base;
@@ -158,6 +158,7 @@ struct material_view
     float sheen_roughness;
     float diffuse_transmission;
     float3 dt_color;
+    float iridescence, iri_ior, iri_thickness;
 };
 
 __device__ __forceinline__ float schlick_fresnel(float u)
@@ -241,6 +242,72 @@ __device__ __forceinline__ float3 sample_gtr1(float x, float y, float roughness)
     return f3(st * cosf(phi), st * sinf(phi), ct);
 }
 
+// ---- thin-film iridescence (utils/bsdf.slang:15-17, :34-48, :83-150) ------------------------------
+__device__ __forceinline__ float f_schlick(float c, float f0) { return f0 + (1.f - f0) * powf(1.f - c, 5.f); }
+__device__ __forceinline__ float ior_to_f0(float t, float i)
+{
+    float v = (t - i) / (t + i);
+    return v * v;
+}
+// XYZ -> linear Rec.709 (row vector times the reference's XYZ_TO_REC709 rows)
+__device__ __forceinline__ float3 xyz_to_rec709(float x, float y, float z)
+{
+    return f3(x * 3.2404542f + y * -1.5371385f + z * -0.4985314f, x * -0.9692660f + y * 1.8760108f + z * 0.0415560f,
+              x * 0.0556434f + y * -0.2040259f + z * 1.0572252f);
+}
+// evalSensitivity: the Fourier transform of the CIE colour matching functions as Gaussians
+__device__ __forceinline__ float3 eval_sensitivity(float opd, float3 shift)
+{
+    const float phase = 2.f * PT_PI * opd * 1.0e-9f, phase2 = phase * phase;
+    const float vx = 5.4856e-13f, vy = 4.4201e-13f, vz = 5.2481e-13f;
+    const float px = 1.6810e+06f, py = 1.7953e+06f, pz = 2.2084e+06f;
+    const float sx = 4.3278e+09f, sy = 9.3046e+09f, sz = 6.6121e+09f;
+    float x = vx * sqrtf(2.f * PT_PI * sx) * cosf(px * phase + shift.x) * expf(-phase2 * sx);
+    float y = vy * sqrtf(2.f * PT_PI * sy) * cosf(py * phase + shift.y) * expf(-phase2 * sy);
+    float z = vz * sqrtf(2.f * PT_PI * sz) * cosf(pz * phase + shift.z) * expf(-phase2 * sz);
+    x += 9.7470e-14f * sqrtf(2.f * PT_PI * 4.5282e+09f) * cosf(2.2399e+06f * phase + shift.x) *
+         expf(-4.5282e+09f * phase2);
+    const float inv = 1.f / 1.0685e-7f;
+    return xyz_to_rec709(x * inv, y * inv, z * inv);
+}
+// Fresnel of a thin film of ior `film` over a base of reflectance f0, seen from outside ior `outside`
+__device__ __forceinline__ float3 iridescent_fresnel(float outside, float film, float3 f0, float thickness, float cos1)
+{
+    const float R0 = ior_to_f0(film, outside);
+    const float R12 = f_schlick(cos1, R0);
+    const float T121 = 1.f - R12;
+    const float r = outside / film;
+    const float sin2sq = r * r * (1.f - cos1 * cos1);
+    const float cos2sq = 1.f - sin2sq;
+    if(cos2sq < 0.f) return f3(1.f, 1.f, 1.f);
+    const float cos2 = sqrtf(cos2sq);
+    auto base_ior = [](float f) {
+        const float q = sqrtf(fminf(fmaxf(f, 0.f), 0.9999f) + 0.0001f);
+        return (1.f + q) / (1.f - q);
+    };
+    const float3 bi = f3(base_ior(f0.x), base_ior(f0.y), base_ior(f0.z));
+    const float3 R23 = f3(f_schlick(cos2, ior_to_f0(bi.x, film)), f_schlick(cos2, ior_to_f0(bi.y, film)),
+                          f_schlick(cos2, ior_to_f0(bi.z, film)));
+    const float phi12 = film < outside ? PT_PI : 0.f, phi21 = PT_PI - phi12;
+    const float3 phi = f3(phi21 + (bi.x < film ? PT_PI : 0.f), phi21 + (bi.y < film ? PT_PI : 0.f),
+                          phi21 + (bi.z < film ? PT_PI : 0.f));
+    const float opd = 2.f * film * thickness * cos2;
+    auto cl = [](float v) { return fminf(fmaxf(v, 1e-5f), 0.9999f); };
+    const float3 R123 = f3(cl(R12 * R23.x), cl(R12 * R23.y), cl(R12 * R23.z));
+    const float3 r123 = f3(sqrtf(R123.x), sqrtf(R123.y), sqrtf(R123.z));
+    const float3 Rs = f3(T121 * T121 * R23.x / (1.f - R123.x), T121 * T121 * R23.y / (1.f - R123.y),
+                         T121 * T121 * R23.z / (1.f - R123.z));
+    float3 I = f3(R12, R12, R12) + Rs;
+    float3 Cm = Rs - f3(T121, T121, T121);
+    for(int k = 1; k <= 2; ++k)
+    {
+        Cm = Cm * r123;
+        const float3 Sm = eval_sensitivity((float)k * opd, phi * (float)k) * 2.f;
+        I = I + Cm * Sm;
+    }
+    return f3(fmaxf(I.x, 0.f), fmaxf(I.y, 0.f), fmaxf(I.z, 0.f));
+}
+
 // EvalDiffuse with the sheen term (bsdf_disney.slang:142-160)
 __device__ __forceinline__ float3 eval_diffuse(const material_view &m, float alpha, float sheen_r, float3 V, float3 N,
                                                float3 L, float3 H, float &pdf)
@@ -318,6 +385,38 @@ __device__ __forceinline__ float3 eval_dielectric_refraction(float alpha, float3
     return color * ((1.f - F) * d * g * fabsf(voh) * 4.f * jac);
 }
 
+// EvalSpecularIridescence (bsdf_disney.slang:112-127)
+__device__ __forceinline__ float3 eval_specular_iridescence(float alpha, float film_ior, float thickness, float3 cspec0,
+                                                            float3 V, float3 N, float3 L, float3 H, float &pdf)
+{
+    pdf = 0.f;
+    if(dot(N, L) <= 0.f) return f3(0.f, 0.f, 0.f);
+    float d = gtr2(dot(N, H), alpha);
+    float sv = smith_ggx(fabsf(dot(N, V)), alpha);
+    pdf = 0.5f * d * sv;
+    const float3 F = iridescent_fresnel(1.f, film_ior, cspec0, thickness, dot(V, H));
+    float g = smith_ggx(fabsf(dot(N, L)), alpha) * sv;
+    return F * (d * g);
+}
+
+// EvalDielectricReflectionIridescence (bsdf_disney.slang:60-77)
+__device__ __forceinline__ float3 eval_dielectric_reflection_iridescence(float alpha, float3 color, float film_ior,
+                                                                         float thickness, float3 cspec0, float eta,
+                                                                         float3 V, float3 N, float3 L, float3 H,
+                                                                         float &pdf)
+{
+    pdf = 0.f;
+    if(dot(N, L) <= 0.f) return f3(0.f, 0.f, 0.f);
+    const float voh = dot(V, H);
+    float F = dielectric_fresnel(voh, eta);
+    float d = gtr2(dot(N, H), alpha);
+    float sv = smith_ggx(fabsf(dot(N, V)), alpha);
+    pdf = 0.5f * d * sv * F;
+    float g = smith_ggx(fabsf(dot(N, L)), alpha) * sv;
+    const float3 irF = iridescent_fresnel(1.f, film_ior, cspec0, thickness, voh);
+    return color * irF * (d * g);
+}
+
 struct bsdf_sample
 {
     float3 dir;
@@ -349,9 +448,26 @@ __device__ __forceinline__ bsdf_sample sample_bsdf(const material_view &m, float
         const float F = dielectric_fresnel(fabsf(dot(R, H)), eta);
         float3 refr = f3(0.f, 0.f, 0.f);
         if(!(y < F)) refr = refract3(-V, H, eta);
-        if(y < F || dot(refr, refr) < 1e-7f)
+        if(y < F)
         {
-            // reflection, or total internal reflection
+            // reflection: plain or thin-film, by the rescaled lobe uniform
+            r.dir = normalize(R);
+            const float ut = u_lobe / trans_weight;
+            if(m.iridescence > 0.f && ut < m.iridescence)
+            {
+                r.f = eval_dielectric_reflection_iridescence(alpha, m.base, m.iri_ior, m.iri_thickness, spec, eta, V, N,
+                                                             r.dir, H, r.pdf);
+                r.pdf *= m.iridescence;
+            }
+            else
+            {
+                r.f = eval_dielectric_reflection(alpha, m.base, eta, V, N, r.dir, H, r.pdf);
+                if(m.iridescence > 0.f) r.pdf *= 1.f - m.iridescence;
+            }
+        }
+        else if(dot(refr, refr) < 1e-7f)
+        {
+            // total internal reflection
             r.dir = normalize(R);
             r.f = eval_dielectric_reflection(alpha, m.base, eta, V, N, r.dir, H, r.pdf);
         }
@@ -397,8 +513,18 @@ __device__ __forceinline__ bsdf_sample sample_bsdf(const material_view &m, float
                 float3 H = to_world(fr, sample_ggx_vndf(x, y, to_local(fr, V), alpha));
                 if(dot(V, H) < 0.f) H = -H;
                 r.dir = normalize(reflect3(-V, H));
-                r.f = eval_specular(alpha, spec, V, N, r.dir, H, r.pdf);
-                r.pdf *= primary * (1.f - diffuse_ratio);
+                const float ui = us / primary;
+                if(m.iridescence > 0.f && ui < m.iridescence)
+                {
+                    r.f = eval_specular_iridescence(alpha, m.iri_ior, m.iri_thickness, spec, V, N, r.dir, H, r.pdf);
+                    r.pdf *= primary * (1.f - diffuse_ratio) * m.iridescence;
+                }
+                else
+                {
+                    r.f = eval_specular(alpha, spec, V, N, r.dir, H, r.pdf);
+                    r.pdf *= m.iridescence > 0.f ? primary * (1.f - diffuse_ratio) * (1.f - m.iridescence)
+                                                 : primary * (1.f - diffuse_ratio);
+                }
             }
             else
             {
@@ -436,9 +562,22 @@ __device__ __forceinline__ float3 eval_bsdf(const material_view &m, float3 L, fl
     float3 spec = lerp3(f3(0.08f, 0.08f, 0.08f), m.base, m.metalness);
     float3 brdf = f3(0.f, 0.f, 0.f), bsdf = brdf;
     float brdf_pdf = 0.f, bsdf_pdf = 0.f, mp;
+    const float s_ir = m.iridescence;
     if(trans_weight > 0.f)
     {
-        if(refl) bsdf = eval_dielectric_reflection(alpha, m.base, eta, V, N, L, H, bsdf_pdf);
+        if(refl)
+        {
+            bsdf = eval_dielectric_reflection(alpha, m.base, eta, V, N, L, H, bsdf_pdf);
+            if(s_ir > 0.f)
+            {
+                bsdf = bsdf * (1.f - s_ir);
+                bsdf_pdf *= 1.f - s_ir;
+                const float3 b2 = eval_dielectric_reflection_iridescence(alpha, m.base, m.iri_ior, m.iri_thickness,
+                                                                         spec, eta, V, N, L, H, mp);
+                bsdf = bsdf + b2 * s_ir;
+                bsdf_pdf += mp * s_ir;
+            }
+        }
         else bsdf = eval_dielectric_refraction(alpha, m.base, eta, V, N, L, H, bsdf_pdf);
     }
     if(trans_weight < 1.f)
@@ -451,8 +590,18 @@ __device__ __forceinline__ float3 eval_bsdf(const material_view &m, float3 L, fl
             brdf = brdf + m.dt_color * (dt * PT_ONE_OVER_PI);
             brdf_pdf += -dot(N, L) * PT_ONE_OVER_PI * diffuse_ratio * dt;
         }
-        brdf = brdf + eval_specular(alpha, spec, V, N, L, H, mp);
-        brdf_pdf += mp * primary * (1.f - diffuse_ratio);
+        if(s_ir > 0.f)
+        {
+            brdf = brdf + eval_specular(alpha, spec, V, N, L, H, mp) * (1.f - s_ir);
+            brdf_pdf += mp * primary * (1.f - diffuse_ratio) * (1.f - s_ir);
+            brdf = brdf + eval_specular_iridescence(alpha, m.iri_ior, m.iri_thickness, spec, V, N, L, H, mp) * s_ir;
+            brdf_pdf += mp * primary * (1.f - diffuse_ratio) * s_ir;
+        }
+        else
+        {
+            brdf = brdf + eval_specular(alpha, spec, V, N, L, H, mp);
+            brdf_pdf += mp * primary * (1.f - diffuse_ratio);
+        }
         if(m.clearcoat > 0.f)
         {
             const float c = eval_clearcoat(m.clearcoat_roughness, m.clearcoat, V, N, L, H, mp);
@@ -480,8 +629,12 @@ __device__ __forceinline__ material_view load_material(const vkg_material *mats,
     {
         m.transmission = m.clearcoat = m.clearcoat_roughness = m.sheen_roughness = m.diffuse_transmission = 0.f;
         m.sheen_color = m.dt_color = f3(0.f, 0.f, 0.f);
+        m.iridescence = m.iri_ior = m.iri_thickness = 0.f;
         return m;
     }
+    m.iridescence = q.iridescence;
+    m.iri_ior = q.iridescence_ior;
+    m.iri_thickness = q.iridescence_thickness;
     m.transmission = q.transmission;
     m.clearcoat = q.clearcoat;
     m.clearcoat_roughness = q.clearcoat_roughness;

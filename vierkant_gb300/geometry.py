@@ -17,7 +17,8 @@ MATERIAL_DTYPE = np.dtype([("base_color", "<f4", 3), ("roughness", "<f4"), ("met
                            ("emission", "<f4", 3), ("twosided", "<u4"), ("transmission", "<f4"), ("ior", "<f4"),
                            ("clearcoat", "<f4"), ("clearcoat_roughness", "<f4"), ("sheen_color", "<f4", 3),
                            ("sheen_roughness", "<f4"), ("diffuse_transmission", "<f4"),
-                           ("diffuse_transmission_color", "<f4", 3), ("pad", "<f4", 3)])
+                           ("diffuse_transmission_color", "<f4", 3), ("iridescence", "<f4"),
+                           ("iridescence_ior", "<f4"), ("iridescence_thickness", "<f4")])
 assert MATERIAL_DTYPE.itemsize == C.sizeof(vkg_material)
 
 
@@ -57,13 +58,14 @@ def cornell_scene(seed: int = 0x5EED, stream: int = 2, num_spheres: int = 64, n:
     return {"xyz": xyz, "indices": idx, "tri_material": tm, "materials": mats}
 
 
-SHOWCASE_KINDS = ("metal-rough", "glass", "rough glass", "clearcoat", "sheen", "diffuse transmission")
+SHOWCASE_KINDS = ("metal-rough", "glass", "rough glass", "clearcoat", "sheen", "diffuse transmission", "iridescent")
 
 
 def showcase_materials(materials: np.ndarray) -> np.ndarray:
     """The Cornell-box material table with its spheres cycled through the Disney lobes: sphere s
-    (material 3 + s) becomes SHOWCASE_KINDS[s % 6] and keeps its generated colour (lightened for glass);
-    the walls and the metal-rough spheres are unchanged."""
+    (material 3 + s) becomes SHOWCASE_KINDS[s % 7] and keeps its generated colour (lightened for glass;
+    iridescent spheres alternate between dielectric and metal); the walls and the metal-rough spheres
+    are unchanged."""
     m = np.array(materials, MATERIAL_DTYPE, copy=True)
     for s in range(len(m) - 3):
         i, kind = 3 + s, s % len(SHOWCASE_KINDS)
@@ -84,10 +86,16 @@ def showcase_materials(materials: np.ndarray) -> np.ndarray:
             m["sheen_color"][i] = (0.9, 0.9, 0.9)
             m["sheen_roughness"][i] = 0.5
             m["roughness"][i] = 0.9
-        else:
+        elif kind == 5:
             m["diffuse_transmission"][i] = 0.6
             m["diffuse_transmission_color"][i] = c
             m["roughness"][i] = 0.7
+        else:
+            m["iridescence"][i] = 1.0
+            m["iridescence_ior"][i] = 1.3
+            m["iridescence_thickness"][i] = 400.0
+            m["roughness"][i] = 0.25
+            m["metalness"][i] = 1.0 if s % 2 else 0.0
     return m
 
 
