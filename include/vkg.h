@@ -129,8 +129,7 @@ vkg_status vkg_geometry_icosphere(float radius, uint32_t tess, float *xyz, uint3
 /* Cornell box (5 quads over [-1,1]^3, open toward +z) + `num_spheres` cube-spheres of
  * 12 * n^2 triangles each with PCG32-drawn radius / centre / GGX material. Counts first, then
  * fill. per-triangle material id -> tri_material; materials: see vkg_material. */
-/* Disney material record (the reference's material_struct_t, RayBuilder.hpp:40-80, without textures
-   and media). A triangle whose material has transmission > 0 or diffuse_transmission > 0
+/* Disney material record (the reference's material_struct_t, RayBuilder.hpp:40-80, without textures). A triangle whose material has transmission > 0 or diffuse_transmission > 0
    is never culled: rays leave such objects through their back faces. */
 typedef struct vkg_material
 {
@@ -150,7 +149,17 @@ typedef struct vkg_material
     float iridescence;          /* iridescence_strength: weight of the thin-film specular lobes, [0, 1] */
     float iridescence_ior;      /* the thin film's index of refraction (1.3) */
     float iridescence_thickness; /* film thickness in nm (the reference's thickness_range.y, 400) */
-} vkg_material; /* 96 B */
+    /* homogeneous interior medium (Material.hpp:101-120): sigma_t = -log(attenuation_color) /
+       attenuation_distance, single-scattering albedo from scatter_factor * scatter_color; a finite
+       attenuation_distance or null_surface makes the material a medium boundary */
+    float attenuation_color[3];  /* (0, 1], 1: no extinction */
+    float attenuation_distance;  /* > 0, +inf: no medium */
+    float scatter_color[3];      /* multi-scatter albedo tint, [0, 1] */
+    float scatter_factor;        /* [0, 1] */
+    float phase_g;               /* Henyey-Greenstein asymmetry, (-1, 1) */
+    uint32_t null_surface;       /* 1: no surface interaction; emission becomes the medium's */
+    float pad[2];
+} vkg_material; /* 144 B */
 /* ---- analytic lights ----------------------------------------------------------------------
  * The reference's LightType (punctual_light.hpp:20-34); AREA is reserved for emissive triangles and
  * rejected here, as the reference leaves it out of the light list (PBRPathTracer.cpp:633-634). */
@@ -198,7 +207,8 @@ vkg_status vkg_light_convert(const vkg_light_source *src, const float rotation[9
                              vkg_light *out);
 
 /* fills *m with the reference's defaults: base colour 1, roughness 1, ior 1.5, diffuse-transmission colour 1,
-   iridescence ior 1.3 and thickness 400 nm, everything else 0 */
+   iridescence ior 1.3 and thickness 400 nm, attenuation colour 1 at +inf distance, scatter colour 1,
+   everything else 0 */
 vkg_status vkg_material_defaults(vkg_material *m);
 vkg_status vkg_scene_cornell_counts(uint32_t num_spheres, uint32_t n, uint32_t *num_vertices, uint32_t *num_tris,
                                     uint32_t *num_materials);

@@ -247,7 +247,9 @@ MATERIAL_DTYPE = np.dtype([("base_color", "<f4", 3), ("roughness", "<f4"), ("met
                            ("clearcoat", "<f4"), ("clearcoat_roughness", "<f4"), ("sheen_color", "<f4", 3),
                            ("sheen_roughness", "<f4"), ("diffuse_transmission", "<f4"),
                            ("diffuse_transmission_color", "<f4", 3), ("iridescence", "<f4"),
-                           ("iridescence_ior", "<f4"), ("iridescence_thickness", "<f4")])
+                           ("iridescence_ior", "<f4"), ("iridescence_thickness", "<f4"), ("attenuation_color", "<f4", 3),
+                           ("attenuation_distance", "<f4"), ("scatter_color", "<f4", 3), ("scatter_factor", "<f4"),
+                           ("phase_g", "<f4"), ("null_surface", "<u4"), ("pad", "<f4", 2)])
 
 
 class orc_pt_scene(C.Structure):
@@ -438,6 +440,24 @@ def pt_render_instanced(meshes, o2w, inst_mesh, inst_mat, mats, env_rgb, cam, sp
     L.orc_pt_render_instanced(C.byref(scene), C.byref(inst), C.byref(env), C.byref(cam), C.byref(st), ptr(out),
                               ptr(sq), ptr(stats), nthreads)
     return out, sq, (int(stats[0]), int(stats[1]))
+
+
+def phase_hg(cos_theta, g):
+    """FP64 Henyey-Greenstein phase function value (phase_function.slang:10-14)"""
+    L = orc()
+    L.orc_phase_hg.argtypes = [C.c_double, C.c_double]
+    L.orc_phase_hg.restype = C.c_double
+    return L.orc_phase_hg(float(cos_theta), float(g))
+
+
+def phase_hg_sample(x, y, g):
+    """one FP64 phase-function sample around +z: (direction, pdf)"""
+    L = orc()
+    L.orc_phase_hg_sample.argtypes = [C.c_double, C.c_double, C.c_double, C.c_void_p, C.c_void_p]
+    d = np.zeros(3)
+    pdf = C.c_double()
+    L.orc_phase_hg_sample(float(x), float(y), float(g), ptr(d), C.byref(pdf))
+    return d, pdf.value
 
 
 def bsdf_sample(material, n, v, eta, u):

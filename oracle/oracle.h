@@ -125,7 +125,10 @@ typedef struct {
     float sheen_color[3], sheen_roughness;
     float diffuse_transmission, diffuse_transmission_color[3];
     float iridescence, iridescence_ior, iridescence_thickness;
-} orc_pt_material; /* same 96-byte layout as vkg_material */
+    float attenuation_color[3], attenuation_distance, scatter_color[3], scatter_factor, phase_g;
+    uint32_t null_surface;
+    float pad[2];
+} orc_pt_material; /* same 144-byte layout as vkg_material */
 
 typedef struct {
     const float *xyz;
@@ -217,6 +220,8 @@ void orc_post_fx(const float *hdr, uint32_t w, uint32_t h, int tonemap, int bloo
    value of orc_bsdf_eval is the mixture pdf */
 void orc_bsdf_sample(const orc_pt_material *m, const double n[3], const double v[3], double eta, const double u[3],
                      double dir[3], double *pdf, double f[3], int *transmission);
+void orc_phase_hg_sample(double x, double y, double g, double dir[3], double *pdf);
+double orc_phase_hg(double cos_theta, double g);
 void orc_iridescent_fresnel(double outside, double film, const double f0[3], double thickness, double cos1,
                             double out[3]);
 double orc_bsdf_eval(const orc_pt_material *m, const double l[3], const double n[3], const double v[3], double eta,

@@ -23,6 +23,31 @@ int orc__run_threads(void *(*fn)(void *), void *arg, int nthreads);
 
 #define LEAF_BIT 0x80000000u
 
+/* the medium a boundary material defines (raypipeline.slang:493-511), computed in float as the
+   product's host code does; flags: 1 finite attenuation distance, 2 null surface */
+typedef struct {
+    float sigma_s[3], g, sigma_a[3], ior, emission[3];
+    uint32_t flags;
+} orc_medium;
+
+static void orc_medium_from(const orc_pt_material *m, orc_medium *r)
+{
+    int vol = m->attenuation_distance > 0.f && m->attenuation_distance < 3.0e38f;
+    for(int c = 0; c < 3; ++c)
+    {
+        float st = vol ? -logf(m->attenuation_color[c]) / m->attenuation_distance : 0.f;
+        float ms = m->scatter_factor * m->scatter_color[c];
+        float kc = 4.09712f + 4.20863f * ms - sqrtf(9.59217f + 41.6808f * ms + 17.7126f * ms * ms);
+        float ss = 1.f - kc * kc;
+        r->sigma_s[c] = ss * st;
+        r->sigma_a[c] = (1.f - ss) * st;
+        r->emission[c] = m->null_surface ? m->emission[c] : 0.f;
+    }
+    r->g = m->phase_g;
+    r->ior = m->ior;
+    r->flags = (vol ? 1u : 0u) | (m->null_surface ? 2u : 0u);
+}
+
 typedef struct {
     const orc_pt_scene *scene;
     const orc_bvh *bvh;
@@ -35,6 +60,7 @@ typedef struct {
     uint32_t num_lights, suppress_caustics;
     orc_pixel *pixels;
     float clip_near;
+    const orc_medium *media; /* per material, NULL: the scene has no media */
     uint32_t cx0, cy0, cw, ch;
     double *out, *sq;
     const orc_pt_instances *inst; /* NULL: single-level scene */
@@ -61,34 +87,59 @@ static void f_hit_raw(const orc_pt_job *J, float ox, float oy, float oz, float t
 }
 
 /* light-NEE visibility (visibility_test.slang:94-131): 0 at the first opaque surface in (tmin, tmax),
-   else transmission x base colour of every transmissive surface crossed, nearest first */
-static void f_transmit_raw(const orc_pt_job *J, float ox, float oy, float oz, float dx, float dy, float dz, float tmax,
-                           float T[3])
+   else transmission x base colour of every transmissive surface crossed, nearest first; null surfaces
+   pass unattenuated */
+static void f_transmit_raw(const orc_pt_job *J, float ox, float oy, float oz, float tmin, float dx, float dy, float dz,
+                           float tmax, int cull, float T[3])
 {
     T[0] = T[1] = T[2] = 1.f;
-    float tmin = 0.f;
+    float od[3] = {0.f, 0.f, 0.f};
     for(int k = 0;; ++k)
     {
         orc_ray r = {{ox, oy, oz}, tmin, {dx, dy, dz}, tmax};
         orc_hit h;
-        orc_bvh_trace1(J->bvh, &r, 0, NULL, 0, &h, NULL);
-        if(h.prim == ORC_MISS) return;
-        const orc_pt_material *m = &J->scene->mats[J->scene->tri_mat[h.prim]];
+        orc_bvh_trace1(J->bvh, &r, cull ? 1 : 0, NULL, 0, &h, NULL);
+        if(h.prim == ORC_MISS) break;
+        const uint32_t mi = J->scene->tri_mat[h.prim];
+        const orc_pt_material *m = &J->scene->mats[mi];
+        if(m->null_surface && k + 1 < 32)
+        {
+            tmin = h.t; /* null surfaces pass unattenuated (visibility_test.slang:113) */
+            continue;
+        }
         if(!(m->transmission > 0.f) || k + 1 >= 32)
         {
             T[0] = T[1] = T[2] = 0.f;
             return;
         }
         for(int c = 0; c < 3; ++c) T[c] = T[c] * m->base[c] * m->transmission;
+        if(J->media && (J->media[mi].flags & 1u))
+        {
+            /* Beer-Lambert: -sigma_t t entering (front face), +sigma_t t leaving */
+            const float *xyz = J->scene->xyz;
+            const uint32_t *ix = J->scene->idx + 3 * (size_t)h.prim;
+            const float *a = xyz + 3 * (size_t)ix[0], *b = xyz + 3 * (size_t)ix[1], *c2 = xyz + 3 * (size_t)ix[2];
+            float e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, e2[3] = {c2[0] - a[0], c2[1] - a[1], c2[2] - a[2]};
+            float n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+            int front = n[0] * dx + n[1] * dy + n[2] * dz < 0.f;
+            for(int c = 0; c < 3; ++c)
+            {
+                float st = J->media[mi].sigma_s[c] + J->media[mi].sigma_a[c];
+                od[c] += st * (front ? -h.t : h.t);
+            }
+        }
         tmin = h.t;
     }
+    if(J->media)
+        for(int c = 0; c < 3; ++c) T[c] *= expf(-fmaxf(od[c], 0.f));
 }
 
-static int f_occluded_raw(const orc_pt_job *J, float ox, float oy, float oz, float dx, float dy, float dz)
+static int f_occluded_raw(const orc_pt_job *J, float ox, float oy, float oz, float tmin, float dx, float dy, float dz,
+                          int cull)
 {
-    orc_ray r = {{ox, oy, oz}, 0.f, {dx, dy, dz}, 1e4f};
+    orc_ray r = {{ox, oy, oz}, tmin, {dx, dy, dz}, 1e4f};
     uint32_t occ = 0;
-    orc_bvh_trace1(J->bvh, &r, 0, NULL, 1, NULL, &occ);
+    orc_bvh_trace1(J->bvh, &r, cull ? 1 : 0, NULL, 1, NULL, &occ);
     return (int)occ;
 }
 
@@ -267,7 +318,8 @@ static int ib_key_cmp(const void *a, const void *b)
 /* back faces are traced for two-sided surfaces and for objects rays enter and leave (transmission) */
 static int orc_material_unculled(const orc_pt_material *m)
 {
-    return m->twosided != 0u || m->transmission > 0.f || m->diffuse_transmission > 0.f;
+    return m->twosided != 0u || m->transmission > 0.f || m->diffuse_transmission > 0.f || m->null_surface != 0u ||
+           (m->attenuation_distance > 0.f && m->attenuation_distance < 3.0e38f);
 }
 
 static inst_bvh *build_inst_bvh(const orc_pt_instances *I)
@@ -497,36 +549,60 @@ static void d_hit_raw(const orc_pt_job *J, double ox, double oy, double oz, doub
     else d_trace(J, o, tmin, d, 1e4, 2, 0, prim, t, u, v);
 }
 
-static int d_occluded_raw(const orc_pt_job *J, double ox, double oy, double oz, double dx, double dy, double dz)
+static int d_occluded_raw(const orc_pt_job *J, double ox, double oy, double oz, double tmin, double dx, double dy,
+                          double dz, int cull)
 {
     double o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz}, u, v, t;
     uint32_t prim, inst;
-    if(J->inst) return d_trace_inst(J, o, 0.0, d, 1e4, 0, 1, &prim, &inst, &t, &u, &v);
-    return d_trace(J, o, 0.0, d, 1e4, 0, 1, &prim, &t, &u, &v);
+    if(J->inst) return d_trace_inst(J, o, tmin, d, 1e4, cull ? 1 : 0, 1, &prim, &inst, &t, &u, &v);
+    return d_trace(J, o, tmin, d, 1e4, cull ? 1 : 0, 1, &prim, &t, &u, &v);
 }
 
-static void d_transmit_raw(const orc_pt_job *J, double ox, double oy, double oz, double dx, double dy, double dz,
-                           double tmax, double T[3])
+static void d_transmit_raw(const orc_pt_job *J, double ox, double oy, double oz, double tmin, double dx, double dy,
+                           double dz, double tmax, int cull, double T[3])
 {
-    double o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz}, tmin = 0.0;
+    double o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz}, od[3] = {0, 0, 0};
     T[0] = T[1] = T[2] = 1.0;
     for(int k = 0;; ++k)
     {
         uint32_t prim, inst = 0;
         double t, u, v;
-        int hit = J->inst ? d_trace_inst(J, o, tmin, d, tmax, 0, 0, &prim, &inst, &t, &u, &v)
-                          : d_trace(J, o, tmin, d, tmax, 0, 0, &prim, &t, &u, &v);
-        if(!hit) return;
+        int hit = J->inst ? d_trace_inst(J, o, tmin, d, tmax, cull ? 1 : 0, 0, &prim, &inst, &t, &u, &v)
+                          : d_trace(J, o, tmin, d, tmax, cull ? 1 : 0, 0, &prim, &t, &u, &v);
+        if(!hit) break;
         const uint32_t mat = J->inst ? J->inst->inst_mat[inst] : J->scene->tri_mat[prim];
         const orc_pt_material *m = &J->scene->mats[mat];
+        if(m->null_surface && k + 1 < 32)
+        {
+            tmin = t;
+            continue;
+        }
         if(!(m->transmission > 0.f) || k + 1 >= 32)
         {
             T[0] = T[1] = T[2] = 0.0;
             return;
         }
         for(int c = 0; c < 3; ++c) T[c] = T[c] * (double)m->base[c] * (double)m->transmission;
+        if(J->media && !J->inst && (J->media[mat].flags & 1u))
+        {
+            /* Beer-Lambert through transmissive volumes of a single-level scene (as the GPU) */
+            const float *xyz = J->scene->xyz;
+            const uint32_t *ix = J->scene->idx + 3 * (size_t)prim;
+            const float *a = xyz + 3 * (size_t)ix[0], *b = xyz + 3 * (size_t)ix[1], *c2 = xyz + 3 * (size_t)ix[2];
+            double e1[3] = {(double)b[0] - a[0], (double)b[1] - a[1], (double)b[2] - a[2]};
+            double e2[3] = {(double)c2[0] - a[0], (double)c2[1] - a[1], (double)c2[2] - a[2]};
+            double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+            int front = n[0] * dx + n[1] * dy + n[2] * dz < 0.0;
+            for(int c = 0; c < 3; ++c)
+            {
+                double st = (double)J->media[mat].sigma_s[c] + (double)J->media[mat].sigma_a[c];
+                od[c] += st * (front ? -t : t);
+            }
+        }
         tmin = t;
     }
+    if(J->media)
+        for(int c = 0; c < 3; ++c) T[c] *= exp(-(od[c] > 0 ? od[c] : 0));
 }
 
 /* ---- instantiate the estimator ------------------------------------------------------------- */
@@ -547,6 +623,7 @@ static void d_transmit_raw(const orc_pt_job *J, double ox, double oy, double oz,
 #define TRANS_RAW f_transmit_raw
 #define RASIN(x) asinf(x)
 #define REXP(x) expf(x)
+#define RLOG(x) logf(x)
 #include "pt_core.inc"
 #undef REAL
 #undef SFX
@@ -565,6 +642,7 @@ static void d_transmit_raw(const orc_pt_job *J, double ox, double oy, double oz,
 #undef TRANS_RAW
 #undef RASIN
 #undef REXP
+#undef RLOG
 
 #define REAL double
 #define SFX(n) d_##n
@@ -583,6 +661,7 @@ static void d_transmit_raw(const orc_pt_job *J, double ox, double oy, double oz,
 #define TRANS_RAW d_transmit_raw
 #define RASIN(x) asin(x)
 #define REXP(x) exp(x)
+#define RLOG(x) log(x)
 #include "pt_core.inc"
 
 void orc_sun_light(const float color[3], float intensity, const float spherical_coords[2], float angular_size,
@@ -613,6 +692,15 @@ void orc_bsdf_sample(const orc_pt_material *mt, const double n[3], const double 
     dir[0] = d.x, dir[1] = d.y, dir[2] = d.z;
     f[0] = fv.x, f[1] = fv.y, f[2] = fv.z;
 }
+
+/* one FP64 Henyey-Greenstein phase sample around +z (phase_function.slang:17-31): direction and pdf */
+void orc_phase_hg_sample(double x, double y, double g, double dir[3], double *pdf)
+{
+    d_v3 d = d_sample_phase_hg(x, y, g, pdf);
+    dir[0] = d.x, dir[1] = d.y, dir[2] = d.z;
+}
+
+double orc_phase_hg(double cos_theta, double g) { return d_phase_hg(cos_theta, g); }
 
 void orc_iridescent_fresnel(double outside, double film, const double f0[3], double thickness, double cos1,
                             double out[3])
@@ -714,6 +802,19 @@ int orc_pt_render(int fp64, const orc_pt_scene *scene, const orc_bvh *bvh, const
     J.suppress_caustics = set->suppress_caustics;
     J.pixels = set->pixels;
     J.clip_near = set->clip_near > 0.f ? set->clip_near : 0.1f;
+    orc_medium *media = NULL;
+    for(uint32_t i = 0; i < scene->nmat; ++i)
+    {
+        const orc_pt_material *m = &scene->mats[i];
+        if(m->null_surface || (m->attenuation_distance > 0.f && m->attenuation_distance < 3.0e38f))
+        {
+            media = (orc_medium *)calloc(scene->nmat, sizeof(orc_medium));
+            break;
+        }
+    }
+    if(media)
+        for(uint32_t i = 0; i < scene->nmat; ++i) orc_medium_from(&scene->mats[i], &media[i]);
+    J.media = media;
     J.cx0 = set->crop[0];
     J.cy0 = set->crop[1];
     J.cw = set->crop[2] ? set->crop[2] : cam->width;
@@ -731,6 +832,7 @@ int orc_pt_render(int fp64, const orc_pt_scene *scene, const orc_bvh *bvh, const
         stats[1] = atomic_load(&J.shadow);
     }
     free(ts);
+    free(media);
     return n;
 }
 
@@ -764,6 +866,19 @@ int orc_pt_render_instanced(const orc_pt_scene *scene, const orc_pt_instances *i
     J.suppress_caustics = set->suppress_caustics;
     J.pixels = set->pixels;
     J.clip_near = set->clip_near > 0.f ? set->clip_near : 0.1f;
+    orc_medium *media = NULL;
+    for(uint32_t i = 0; i < scene->nmat; ++i)
+    {
+        const orc_pt_material *m = &scene->mats[i];
+        if(m->null_surface || (m->attenuation_distance > 0.f && m->attenuation_distance < 3.0e38f))
+        {
+            media = (orc_medium *)calloc(scene->nmat, sizeof(orc_medium));
+            break;
+        }
+    }
+    if(media)
+        for(uint32_t i = 0; i < scene->nmat; ++i) orc_medium_from(&scene->mats[i], &media[i]);
+    J.media = media;
     J.cx0 = set->crop[0];
     J.cy0 = set->crop[1];
     J.cw = set->crop[2] ? set->crop[2] : cam->width;
@@ -781,6 +896,7 @@ int orc_pt_render_instanced(const orc_pt_scene *scene, const orc_pt_instances *i
         stats[1] = atomic_load(&J.shadow);
     }
     free_inst_bvh(B);
+    free(media);
     return n;
 }
 

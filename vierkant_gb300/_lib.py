@@ -48,7 +48,10 @@ class vkg_material(C.Structure):
                 ("ior", C.c_float), ("clearcoat", C.c_float), ("clearcoat_roughness", C.c_float),
                 ("sheen_color", C.c_float * 3), ("sheen_roughness", C.c_float), ("diffuse_transmission", C.c_float),
                 ("diffuse_transmission_color", C.c_float * 3), ("iridescence", C.c_float),
-                ("iridescence_ior", C.c_float), ("iridescence_thickness", C.c_float)]
+                ("iridescence_ior", C.c_float), ("iridescence_thickness", C.c_float),
+                ("attenuation_color", C.c_float * 3), ("attenuation_distance", C.c_float),
+                ("scatter_color", C.c_float * 3), ("scatter_factor", C.c_float), ("phase_g", C.c_float),
+                ("null_surface", C.c_uint32), ("pad", C.c_float * 2)]
 
 
 class vkg_camera(C.Structure):

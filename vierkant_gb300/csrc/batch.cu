@@ -459,9 +459,10 @@ vkg_status vkg_batch_create(vkg_ctx *ctx, const vkg_batch_job *jobs, uint32_t nj
         const vkg_batch_job &jb = jobs[j];
         if(!jb.scene) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_batch_create: job %u has no scene", j);
         if(vkg_status s = check_tracer_settings(ctx, &jb.settings); s != VKG_OK) return s;
-        if(!jb.scene->lights.empty() || jb.settings.sun_intensity > 0.f)
+        if(!jb.scene->lights.empty() || jb.settings.sun_intensity > 0.f || jb.scene->d_media)
             return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
-                             "vkg_batch_create: job %u: analytic lights and the sun are rendered by vkg_tracer_render", j);
+                             "vkg_batch_create: job %u: analytic lights, the sun and media are rendered by "
+                             "vkg_tracer_render", j);
         if(jb.camera.width != jb.settings.resolution[0] || jb.camera.height != jb.settings.resolution[1])
             return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_batch_create: job %u camera size != resolution", j);
         uint32_t x0, y0, w, h;

@@ -717,6 +717,8 @@ vkg_status vkg_material_defaults(vkg_material *m)
     m->ior = 1.5f;
     m->iridescence_ior = 1.3f;
     m->iridescence_thickness = 400.f;
+    for(int c = 0; c < 3; ++c) m->attenuation_color[c] = m->scatter_color[c] = 1.f;
+    m->attenuation_distance = std::numeric_limits<float>::infinity();
     return VKG_OK;
 }
 

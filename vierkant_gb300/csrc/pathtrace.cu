@@ -58,6 +58,8 @@ struct vkg_tracer
     float *sum = nullptr;
     float *accum = nullptr;
     vkg_pixel_data *gbuf = nullptr; // pixel records of the traced window
+    uint4 *mstack = nullptr;        // per-path medium stacks (scenes with media)
+    size_t mstack_cap = 0;
     uint32_t *counters = nullptr;           // [0..1] queue lengths, [2] shadow queue length, [3] cache queries,
                                             // [4] training records, [5] training batch length, [6] work
                                             // counter, [7] light shadow queue length
@@ -124,10 +126,13 @@ __global__ void k_check_instance_materials(const vkg_instance *__restrict__ inst
 
 // the material fields the BSDF divides by or takes as probabilities must be in range
 vkg_status check_material_values(vkg_ctx *ctx, const vkg_material *d_mats, uint32_t n, cudaStream_t st,
-                                 const char *fn, bool *any_transmissive, bool *any_full)
+                                 const char *fn, bool *any_transmissive, bool *any_full, medium_rec **d_media)
 {
     *any_transmissive = false;
     *any_full = false;
+    *d_media = nullptr;
+    std::vector<medium_rec> media(n);
+    bool any_medium = false;
     std::vector<vkg_material> h(n);
     cudaError_t e = cudaMemcpyAsync(h.data(), d_mats, n * sizeof(vkg_material), cudaMemcpyDeviceToHost, st);
     if(e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -151,8 +156,27 @@ vkg_status check_material_values(vkg_ctx *ctx, const vkg_material *d_mats, uint3
            !std::isfinite(m.clearcoat))
             return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
                              "%s: material %u: clearcoat, clearcoat_roughness and sheen_roughness must be >= 0", fn, i);
-        *any_transmissive = *any_transmissive || m.transmission > 0.f;
+        const bool vol = material_has_volume(m);
+        auto unit_open = [](float x) { return x > 0.f && x <= 1.f; };
+        if((vol && (!unit_open(m.attenuation_color[0]) || !unit_open(m.attenuation_color[1]) ||
+                    !unit_open(m.attenuation_color[2]))) ||
+           !unit(m.scatter_factor) || !unit(m.scatter_color[0]) || !unit(m.scatter_color[1]) ||
+           !unit(m.scatter_color[2]) || !(m.phase_g > -1.f && m.phase_g < 1.f))
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
+                             "%s: material %u: attenuation colour in (0, 1], scatter factor / colour in [0, 1], "
+                             "phase g in (-1, 1)", fn, i);
+        *any_transmissive = *any_transmissive || m.transmission > 0.f || m.null_surface;
         *any_full = *any_full || material_full(m);
+        media[i] = medium_from_material(m);
+        any_medium = any_medium || vol || m.null_surface;
+    }
+    if(any_medium)
+    {
+        e = cudaMalloc(d_media, n * sizeof(medium_rec));
+        if(e == cudaSuccess)
+            e = cudaMemcpyAsync(*d_media, media.data(), n * sizeof(medium_rec), cudaMemcpyHostToDevice, st);
+        if(e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if(e != cudaSuccess) return cuda_check(ctx, e, fn);
     }
     return VKG_OK;
 }
@@ -355,7 +379,7 @@ vkg_status vkg_scene_create(vkg_ctx *ctx, const vkg_scene_desc *d, vkg_scene **o
         return cuda_check(ctx, e, "vkg_scene_create");
     }
     if(vkg_status s = check_material_values(ctx, sc->mats, d->num_materials, st, "vkg_scene_create",
-                                                 &sc->any_transmissive, &sc->any_full);
+                                                 &sc->any_transmissive, &sc->any_full, &sc->d_media);
        s != VKG_OK)
     {
         vkg_scene_destroy(ctx, sc);
@@ -450,6 +474,7 @@ vkg_status vkg_scene_destroy(vkg_ctx *ctx, vkg_scene *sc)
     cudaFree(sc->idx);
     cudaFree(sc->tri_mat);
     cudaFree(sc->mats);
+    cudaFree(sc->d_media);
     env_free(sc->env);
     delete sc;
     return VKG_OK;
@@ -483,7 +508,7 @@ vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_de
     chk(cudaMemcpyAsync(sc->mats, d->d_materials, d->num_materials * sizeof(vkg_material), cudaMemcpyDeviceToDevice, st));
     if(e != cudaSuccess) return fail(cuda_check(ctx, e, "vkg_scene_create_instanced"));
     if(vkg_status s = check_material_values(ctx, sc->mats, d->num_materials, st, "vkg_scene_create_instanced",
-                                                 &sc->any_transmissive, &sc->any_full);
+                                                 &sc->any_transmissive, &sc->any_full, &sc->d_media);
        s != VKG_OK)
         return fail(s);
     std::vector<mesh_ref> refs(d->num_meshes);
@@ -706,8 +731,21 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
     uint32_t *cnt_l = lights.empty() ? nullptr : t->counters + 7;
     const light_queue lq{t->l_ray, t->l_pid, t->l_contrib, cnt_l};
     // the shade variant: the full Disney model and the light terms, or metal-roughness only
-    const bool full = sc->any_full || !lights.empty();
+    const bool full = sc->any_full || !lights.empty() || sc->d_media;
     P.gbuf = t->gbuf;
+    if(sc->d_media)
+    {
+        if(ccfg) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_tracer_render: media with a radiance cache");
+        if(t->mstack_cap < paths + train_paths)
+        {
+            cudaFree(t->mstack);
+            t->mstack = nullptr;
+            t->mstack_cap = 0;
+            VKG_TRY_CUDA(ctx, cudaMalloc(&t->mstack, (paths + train_paths) * sizeof(uint4)));
+            t->mstack_cap = paths + train_paths;
+        }
+        P.mstack = t->mstack;
+    }
     P.term_depth = cache_render ? ccfg->terminate_depth : 0xFFFFFFFFu;
     P.rec_depth = rec_depth;
     P.train_paths = train_paths;
@@ -716,7 +754,7 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
     uint32_t *cnt_q = t->counters + 3, *cnt_rec = t->counters + 4, *cnt_b = t->counters + 5, *cnt_work = t->counters + 6;
     // instanced scenes: grid-stride two-level tracers (faster on the stress scene: 274 vs 252 Mrays/s);
     // VKG_TL_KERNEL=persistent selects the refilling persistent ones
-    const bool tl_persistent = sc->tlas && tl_persistent_selected();
+    const bool tl_persistent = sc->tlas && tl_persistent_selected() && !sc->d_media;
     // a 64-entry traversal stack serves BVHs up to 10 levels deep (7 (depth - 1) + 1 entries)
     const bool small_stack = sc->bvh && sc->bvh->depth <= 10;
     uint32_t tl_grid = 0;
@@ -768,15 +806,16 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_out, 0, sizeof(uint32_t), st));
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_s, 0, sizeof(uint32_t), st));
             if(cnt_l) VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_l, 0, sizeof(uint32_t), st));
-#define VKG_SHADE(M, F)                                                                                                \
-    k_pt_shade<M, single_scene, F><<<grid, PT_THREADS, 0, st>>>(SS, depth, t->q_ray[a], t->q_pid[a], t->hits, t->hit_inst, cnt_in,        \
+#define VKG_SHADE(M, F, MD)                                                                                            \
+    k_pt_shade<M, single_scene, F, MD><<<grid, PT_THREADS, 0, st>>>(SS, depth, t->q_ray[a], t->q_pid[a], t->hits, t->hit_inst, cnt_in,        \
                                                t->q_ray[1 - a],                                                          \
                                                t->q_pid[1 - a], cnt_out, t->s_ray, t->s_pid, t->s_contrib, cnt_s,         \
                                                t->rng, t->beta_pdf, t->radiance, io, lq)
-            if(mode == MODE_PLAIN && full) VKG_SHADE(MODE_PLAIN, true);
-            else if(mode == MODE_PLAIN) VKG_SHADE(MODE_PLAIN, false);
-            else if(full) VKG_SHADE(MODE_CACHE, true);
-            else VKG_SHADE(MODE_CACHE, false);
+            if(mode == MODE_PLAIN && sc->d_media) VKG_SHADE(MODE_PLAIN, true, true);
+            else if(mode == MODE_PLAIN && full) VKG_SHADE(MODE_PLAIN, true, false);
+            else if(mode == MODE_PLAIN) VKG_SHADE(MODE_PLAIN, false, false);
+            else if(full) VKG_SHADE(MODE_CACHE, true, false);
+            else VKG_SHADE(MODE_CACHE, false, false);
 #undef VKG_SHADE
             if(!empty && tl_persistent)
             {
@@ -903,7 +942,8 @@ vkg_status vkg_tracer_destroy(vkg_tracer *t)
     tracer_free_buffers(t);
     tracer_free_cache_buffers(t);
     cudaFree(t->counters);
-    for(void *p: {(void *)t->d_lights, (void *)t->l_ray, (void *)t->l_pid, (void *)t->l_contrib}) cudaFree(p);
+    for(void *p: {(void *)t->d_lights, (void *)t->l_ray, (void *)t->l_pid, (void *)t->l_contrib, (void *)t->mstack})
+        cudaFree(p);
     cudaFree(t->totals);
     if(t->ev0) cudaEventDestroy(t->ev0);
     if(t->ev1) cudaEventDestroy(t->ev1);

@@ -52,14 +52,16 @@ void env_free(env_tables &t);
 // rays enter and leave (dielectric or diffuse transmission)
 __host__ __device__ inline bool material_unculled(const vkg_material &m)
 {
-    return m.twosided != 0u || m.transmission > 0.f || m.diffuse_transmission > 0.f;
+    return m.twosided != 0u || m.transmission > 0.f || m.diffuse_transmission > 0.f || m.null_surface != 0u ||
+           (m.attenuation_distance > 0.f && m.attenuation_distance < 3.0e38f);
 }
 
 // a material that uses a lobe beyond metal-roughness (the shade kernels' FULL variant)
 __host__ __device__ inline bool material_full(const vkg_material &m)
 {
     return m.transmission > 0.f || m.clearcoat > 0.f || m.diffuse_transmission > 0.f || m.sheen_color[0] > 0.f ||
-           m.sheen_color[1] > 0.f || m.sheen_color[2] > 0.f || m.iridescence > 0.f;
+           m.sheen_color[1] > 0.f || m.sheen_color[2] > 0.f || m.iridescence > 0.f || m.null_surface != 0u ||
+           (m.attenuation_distance > 0.f && m.attenuation_distance < 3.0e38f);
 }
 
 __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }

@@ -7,6 +7,7 @@
 
 #include "nrc.cuh"
 #include "light.cuh"
+#include "medium.cuh"
 #include "pathtrace.cuh"
 #include "pixel.cuh"
 #include "tlas.cuh"
@@ -43,8 +44,9 @@ struct vkg_scene
     std::vector<uint32_t *> mesh_idx;
     vkg::mesh_ref *d_meshes = nullptr;
     uint32_t num_instances = 0;
-    bool any_transmissive = false;  // a material with transmission > 0 (light shadow rays pass through it)
+    bool any_transmissive = false;  // a material with transmission > 0 or a null surface (light shadow rays pass)
     bool any_full = false;          // a material with a lobe beyond metal-roughness
+    vkg::medium_rec *d_media = nullptr; // per-material medium records, when a material bounds a medium
     std::vector<vkg_light> lights;  // analytic lights (host copy; the tracer uploads them per render)
 };
 
@@ -89,6 +91,10 @@ struct pt_params
     vkg_pixel_data *gbuf;
     uint32_t last_sample;
     float clip_near;
+    // homogeneous media: the per-material medium table (nullptr: no material bounds a medium) and
+    // the per-path medium stacks
+    const medium_rec *media;
+    uint4 *mstack;
 };
 
 // the shade kernel's two modes
@@ -199,6 +205,7 @@ __global__ void __launch_bounds__(PT_THREADS)
         rng[p] = g.state;
         beta_pdf[p] = make_float4(1.f, 1.f, 1.f, 0.f);
         radiance[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if(P.mstack) P.mstack[p] = make_uint4(0u, 0u, 0u, 0u); // the camera starts in vacuum
     }
     if(blockIdx.x == 0 && threadIdx.x == 0) counters[0] = n;
 }
@@ -276,8 +283,8 @@ __device__ __forceinline__ void hit_surface(const pt_params &P, uint32_t prim, u
 }
 
 // FULL = false: a scene without lights whose materials are metal-roughness only; the light terms and
-// the other lobes compile away
-template<int MODE, class J, bool FULL = true>
+// the other lobes compile away. MEDIA = true (with FULL): the homogeneous-media terms
+template<int MODE, class J, bool FULL = true, bool MEDIA = false>
 __global__ void __launch_bounds__(PT_THREADS)
         k_pt_shade(J S, uint32_t depth, const vkg_ray *__restrict__ in_ray,
                    const uint32_t *__restrict__ in_pid, const vkg_hit *__restrict__ hits,
@@ -295,6 +302,7 @@ __global__ void __launch_bounds__(PT_THREADS)
         const uint32_t i = base + threadIdx.x;
         const bool active = i < n;
         bool push_ext = false, push_shadow = false, push_query = false, push_light = false;
+        bool cull_back_shadow = false; // shadow rays from inside a medium leave it through back faces
         float3 P0 = f3(0.f, 0.f, 0.f), ndir = P0, sdir = P0, N = P0;
         float3 contrib = P0, qbeta = P0, albedo = P0, vq = P0, ldir_s = P0, lcontrib = P0;
         float rough = 0.f, ldist = 0.f;
@@ -308,25 +316,72 @@ __global__ void __launch_bounds__(PT_THREADS)
             const float3 dir = f3(r1.x, r1.y, r1.z);
             const uint4 h = reinterpret_cast<const uint4 *>(hits)[i];
             pcg32 g{rng[pid], S.inc(pid)};
-            // 8 draws per segment; 3 more (light pick, point on the light) when the scene has lights
+            // 8 draws per segment; 3 more (light pick, point on the light) when the scene has lights,
+            // 4 more (channel, distance, phase direction) when it has media
             const uint32_t num_lights = FULL ? P.num_lights : 0u;
-            float u[11];
-            const int nu = num_lights ? 11 : 8;
-            for(int k = 0; k < 11; ++k) u[k] = k < nu ? u01(pcg32_next(g)) : 0.f;
+            const bool media = FULL && MEDIA && P.media;
+            float u[15];
+            const int nu = media ? 15 : (num_lights ? 11 : 8);
+            for(int k = 0; k < 15; ++k) u[k] = k < nu ? u01(pcg32_next(g)) : 0.f;
             const float4 bp = beta_pdf[pid];
             float3 beta = f3(bp.x, bp.y, bp.z);
+            const float3 seg_beta = beta;
             float prev_pdf = bp.w;
             const float4 lr = radiance[pid];
             float3 L = f3(lr.x, lr.y, lr.z);
             uint32_t flags = __float_as_uint(lr.w); // PATH_REGULARIZE | PATH_CAUSTIC
+            const float4 r0 = rp[0];
+            float t_end = h.x == VKG_MISS ? r1.w : __uint_as_float(h.y);
+            // the medium the segment runs through (raypipeline.slang:388-474, homogeneous branch)
+            uint4 mst = make_uint4(0u, 0u, 0u, 0u);
+            bool scattered = false;
+            float scatter_g = 0.f;
+            if(media)
+            {
+                // only a segment that ends on a surface runs through a medium: the reference samples it
+                // in the closest-hit stage, an escaping ray goes straight to the miss stage
+                mst = P.mstack[pid];
+                const uint32_t top = stack_top(mst);
+                if(top != 0xFFFFFFFFu && h.x != VKG_MISS)
+                {
+                    const medium_rec &M = P.media[top];
+                    const float3 ss = f3(M.sigma_s[0], M.sigma_s[1], M.sigma_s[2]);
+                    const float3 sa = f3(M.sigma_a[0], M.sigma_a[1], M.sigma_a[2]);
+                    const float3 st = ss + sa;
+                    if(st.x > 0.f || st.y > 0.f || st.z > 0.f)
+                    {
+                        const float T = t_end;
+                        const float3 le = f3(M.emission[0], M.emission[1], M.emission[2]);
+                        if(le.x > 0.f || le.y > 0.f || le.z > 0.f)
+                        {
+                            // emission over the segment: sigma_a Le (1 - exp(-sigma_t T)) / sigma_t
+                            const float3 ti = f3((1.f - expf(-st.x * T)) / fmaxf(st.x, PT_EPS),
+                                                 (1.f - expf(-st.y * T)) / fmaxf(st.y, PT_EPS),
+                                                 (1.f - expf(-st.z * T)) / fmaxf(st.z, PT_EPS));
+                            L = L + beta * sa * le * ti;
+                        }
+                        const int ch = (int)fminf(u[11] * 3.f, 2.f);
+                        const float stc = ch == 0 ? st.x : (ch == 1 ? st.y : st.z);
+                        const float t = fminf(-logf(1.f - u[12]) / fmaxf(stc, PT_EPS), T);
+                        scattered = t < T;
+                        const float3 tr = f3(expf(-st.x * t), expf(-st.y * t), expf(-st.z * t));
+                        const float3 dens = scattered ? tr * st : tr;
+                        const float pdf = fmaxf((dens.x + dens.y + dens.z) / 3.f, PT_PDF_EPS);
+                        beta = scattered ? beta * (ss * tr * (1.f / pdf)) : beta * (tr * (1.f / pdf));
+                        if(scattered)
+                        {
+                            t_end = t;
+                            scatter_g = M.g;
+                        }
+                    }
+                }
+            }
             const bool light_hits = num_lights && !(P.suppress_caustics && (flags & PATH_CAUSTIC));
             if(light_hits)
             {
                 // light bodies the segment passed (raypipeline.slang:196-224): additive emitters,
-                // MIS-weighted against their NEE strategy
-                const float4 r0 = rp[0];
+                // MIS-weighted against their NEE strategy, with the throughput at the segment's start
                 const float3 o = f3(r0.x, r0.y, r0.z);
-                const float t_end = h.x == VKG_MISS ? r1.w : __uint_as_float(h.y);
                 const float inv_n = 1.f / (float)num_lights;
                 for(uint32_t li = 0; li < num_lights; ++li)
                 {
@@ -334,13 +389,78 @@ __global__ void __launch_bounds__(PT_THREADS)
                     const float2 lh = intersect_light(l, o, dir);
                     if(lh.x <= r0.w || lh.x >= t_end) continue;
                     const float w = mis_weight_hit(P.mis_mode, prev_pdf, light_pdf(l, o, dir) * inv_n);
-                    L = L + beta * lv3(l.color) * (w * l.intensity);
+                    L = L + seg_beta * lv3(l.color) * (w * l.intensity);
                 }
+            }
+            if(scattered)
+            {
+                // a scattering event: NEE toward one light and the environment with the phase function
+                // (nee_volume, direct_lighting.slang:334-366), then a phase-function bounce
+                P0 = f3(r0.x, r0.y, r0.z) + dir * t_end;
+                cull_back_shadow = true;
+                if(P.mis_mode != 2)
+                {
+                    float pdf_env;
+                    uint32_t texel;
+                    const float3 ld = env_sample(P.env, u[3], u[4], u[5], u[6], pdf_env, texel);
+                    if(pdf_env > 0.f)
+                    {
+                        const float ph = phase_hg(dot(dir, ld), scatter_g);
+                        const float w = P.mis_mode == 1 ? 1.f : power_heuristic(pdf_env, ph);
+                        contrib = beta * env_radiance(P.env, texel) * (w * ph / pdf_env);
+                        if(max3(contrib) > 0.f)
+                        {
+                            push_shadow = true;
+                            sdir = ld;
+                        }
+                    }
+                }
+                if(num_lights)
+                {
+                    const uint32_t nl = num_lights;
+                    const uint32_t li = nl > 1 ? min((uint32_t)(u[8] * (float)nl), nl - 1u) : 0u;
+                    const vkg_light &l = P.lights[li];
+                    const light_sample ls = sample_light(l, P0, u[9], u[10]);
+                    if(max3(ls.radiance) > 0.f)
+                    {
+                        const float ph = phase_hg(dot(dir, ls.dir), scatter_g);
+                        const float w = bsdf_reachable(l) ? mis_weight_nee(P.mis_mode, ls.pdf / (float)nl, ph) : 1.f;
+                        lcontrib = beta * ls.radiance * (w * (float)nl * ph / ls.pdf);
+                        if(max3(lcontrib) > 0.f)
+                        {
+                            push_light = true;
+                            ldir_s = ls.dir;
+                            ldist = ls.dist;
+                        }
+                    }
+                }
+                float ppdf;
+                const float3 loc = sample_phase_hg(u[13], u[14], scatter_g, ppdf);
+                ndir = to_world(local_frame(dir), loc);
+                prev_pdf = ppdf;
+                if(ppdf < PT_REGULARIZE_PDF_THRESHOLD) flags |= PATH_REGULARIZE;
+                bool alive = true;
+                if(P.rr_depth == 0)
+                {
+                    if(max3(beta) <= 0.05f * (float)depth)
+                    {
+                        const float q = 1.f - max3(beta);
+                        if(u[7] < q) alive = false;
+                        else beta = beta * (1.f / (1.f - q));
+                    }
+                }
+                else if(depth + 1 >= P.rr_depth)
+                {
+                    const float q = fmaxf(0.f, 1.f - max3(beta));
+                    if(u[7] < q) alive = false;
+                    else beta = beta * (1.f / (1.f - q));
+                }
+                push_ext = alive && depth + 1 < P.max_depth && max3(beta) > 0.f;
             }
             // the pixel record of a camera ray (raypipeline.slang:224-236, :250-268)
             const bool record = depth == 0 && P.gbuf && pid < P.train_base &&
                                 P.s0 + pid / P.npix == P.last_sample;
-            if(record && h.x == VKG_MISS)
+            if(record && h.x == VKG_MISS && !scattered)
             {
                 vkg_pixel_data &px = P.gbuf[pid % P.npix];
                 px.depth = 0.f;
@@ -348,7 +468,8 @@ __global__ void __launch_bounds__(PT_THREADS)
                 px.object_id = 0xFFFFu;
                 px.albedo = pack_rgba8(0.f, 0.f, 0.f, 1.f);
             }
-            if(h.x == VKG_MISS)
+            if(scattered) {}
+            else if(h.x == VKG_MISS)
             {
                 if(light_hits)
                 {
@@ -385,11 +506,52 @@ __global__ void __launch_bounds__(PT_THREADS)
                 const bool back_face = !(dot(ng, dir) < 0.f);
                 N = back_face ? -ng : ng; // shading normal faces the incoming ray
                 const float3 V = -dir;
+                // media: a boundary pushes its medium on a transmission through a front face and pops
+                // on one through a back face (raypipeline.slang:516-523, :656-664)
+                const bool boundary = media && ((P.media[mat].flags & MEDIUM_VOLUME) || P.mats[mat].transmission > 0.f);
+                if(media && (P.media[mat].flags & MEDIUM_NULL))
+                {
+                    // a null surface: no interaction, the path crosses it (raypipeline.slang:478, :524);
+                    // it enters / leaves a medium only when it bounds one
+                    if(boundary)
+                    {
+                        if(back_face) stack_pop(mst);
+                        else stack_push(mst, mat);
+                    }
+                    bool alive = true;
+                    if(P.rr_depth == 0)
+                    {
+                        if(max3(beta) <= 0.05f * (float)depth)
+                        {
+                            const float q = 1.f - max3(beta);
+                            if(u[7] < q) alive = false;
+                            else beta = beta * (1.f / (1.f - q));
+                        }
+                    }
+                    else if(depth + 1 >= P.rr_depth)
+                    {
+                        const float q = fmaxf(0.f, 1.f - max3(beta));
+                        if(u[7] < q) alive = false;
+                        else beta = beta * (1.f / (1.f - q));
+                    }
+                    push_ext = alive && depth + 1 < P.max_depth;
+                    ndir = dir;
+                    goto done;
+                }
+                {
                 material_view m = load_material<FULL>(P.mats, mat, P.disable_material);
                 // path regularisation (raypipeline.slang:611): after a non-peaked bounce, later vertices
                 // shade (sample and NEE) with roughness >= 0.25
                 if(flags & PATH_REGULARIZE) m.roughness = fmaxf(m.roughness, PT_REGULARIZE_MIN_ROUGHNESS);
-                const float eta = FULL ? hit_eta(P.mats, mat, back_face) : 1.f;
+                float eta = FULL ? hit_eta(P.mats, mat, back_face) : 1.f;
+                if(media && P.mats[mat].transmission > 0.f)
+                {
+                    // eta from the media stack: the current medium's ior over the surface's entering,
+                    // the surface's over the enclosing medium's leaving (raypipeline.slang:489-491)
+                    const float ior = P.mats[mat].ior;
+                    eta = (back_face ? ior / stack_ior(P.media, mst, mst.x ? mst.x - 1 : 0)
+                                     : stack_ior(P.media, mst, mst.x) / ior) + PT_EPS;
+                }
                 const float *em = P.mats[mat].emission;
                 L = L + beta * f3(em[0], em[1], em[2]);
                 if(depth == 0 && P.gbuf && pid < P.train_base)
@@ -522,8 +684,16 @@ __global__ void __launch_bounds__(PT_THREADS)
                         push_ext = true;
                         ndir = bs.dir;
                     }
+                    if(boundary && bs.transmission)
+                    {
+                        if(back_face) stack_pop(mst);
+                        else stack_push(mst, mat);
+                    }
+                }
                 }
             }
+        done:
+            if(media) P.mstack[pid] = mst;
             rng[pid] = g.state;
             beta_pdf[pid] = make_float4(beta.x, beta.y, beta.z, prev_pdf);
             radiance[pid] = make_float4(L.x, L.y, L.z, __uint_as_float(flags));
@@ -539,24 +709,26 @@ __global__ void __launch_bounds__(PT_THREADS)
         const uint32_t ps = warp_push(s_count, push_shadow);
         if(push_shadow)
         {
-            const float3 so = P0 + N * PT_EPS;
+            // from a surface: offset along the normal, tmin 0; from inside a medium: the scattering
+            // point, tmin EPS, back faces culled (flag in the contribution's w)
+            const float3 so = cull_back_shadow ? P0 : P0 + N * PT_EPS;
             float4 *o = reinterpret_cast<float4 *>(s_ray + ps);
-            o[0] = make_float4(so.x, so.y, so.z, 0.f);
+            o[0] = make_float4(so.x, so.y, so.z, cull_back_shadow ? PT_EPS : 0.f);
             o[1] = make_float4(sdir.x, sdir.y, sdir.z, PT_TMAX);
             s_pid[ps] = pid;
-            s_contrib[ps] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
+            s_contrib[ps] = make_float4(contrib.x, contrib.y, contrib.z, cull_back_shadow ? 1.f : 0.f);
         }
         if(FULL && lq.count)
         {
             const uint32_t pl = warp_push(lq.count, push_light);
             if(push_light)
             {
-                const float3 so = P0 + N * PT_EPS;
+                const float3 so = cull_back_shadow ? P0 : P0 + N * PT_EPS;
                 float4 *o = reinterpret_cast<float4 *>(lq.ray + pl);
-                o[0] = make_float4(so.x, so.y, so.z, 0.f);
+                o[0] = make_float4(so.x, so.y, so.z, cull_back_shadow ? PT_EPS : 0.f);
                 o[1] = make_float4(ldir_s.x, ldir_s.y, ldir_s.z, ldist);
                 lq.pid[pl] = pid;
-                lq.contrib[pl] = make_float4(lcontrib.x, lcontrib.y, lcontrib.z, 0.f);
+                lq.contrib[pl] = make_float4(lcontrib.x, lcontrib.y, lcontrib.z, cull_back_shadow ? 1.f : 0.f);
             }
         }
         if constexpr(MODE == MODE_CACHE)
@@ -591,22 +763,23 @@ __global__ void __launch_bounds__(PT_THREADS)
         const pt_params &P = S.params(J::per_path ? s_pid[i] : 0u);
         const float4 *rp = reinterpret_cast<const float4 *>(s_ray + i);
         const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
+        const float4 c = s_contrib[i];
+        const int cull = c.w != 0.f ? CULL_BACK : CULL_NONE; // from inside a medium: back faces culled
         bool occluded;
         if(P.two_level)
             occluded = trace_tlas<true>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w,
-                                        CULL_NONE)
+                                        cull)
                                .occluded;
         else
         {
             unsigned long long v = 0, t = 0;
             occluded = trace_ray<true, false, STACK>(P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w,
-                                                     CULL_NONE, v, t, nullptr)
+                                                     cull, v, t, nullptr)
                                .occluded;
         }
         if(!occluded)
         {
             const uint32_t pid = s_pid[i];
-            const float4 c = s_contrib[i];
             float4 L = radiance[pid];
             L.x += c.x;
             L.y += c.y;
@@ -618,7 +791,7 @@ __global__ void __launch_bounds__(PT_THREADS)
 
 // light-NEE visibility (transmittance_test, visibility_test.slang:94-131): 0 at the first opaque
 // surface on the segment, else the product of transmission x base colour over the transmissive
-// surfaces it crosses. Scenes without transmissive materials take one any-hit query; single-level
+// surfaces it crosses; null surfaces pass unattenuated. Scenes without transmissive materials take one any-hit query; single-level
 // scenes one pass over the crossed triangles (trace_transmit); instanced scenes repeated closest-hit
 // queries from the last crossing (at most PT_MAX_CROSSINGS; more count as blocked). Runs after the
 // environment shadow kernel, so each path's radiance has one writer at a time.
@@ -635,26 +808,44 @@ __global__ void __launch_bounds__(PT_THREADS) k_pt_light_shadow(J S, light_queue
         const pt_params &P = S.params(J::per_path ? pid : 0u);
         const float4 *rp = reinterpret_cast<const float4 *>(lq.ray + i);
         const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
+        const float4 cc = lq.contrib[i];
+        // rays from inside a medium cull back faces (nee_volume, direct_lighting.slang:348-354)
+        const int cull = cc.w != 0.f ? CULL_BACK : CULL_NONE;
         float3 T = f3(1.f, 1.f, 1.f);
         unsigned long long v = 0, c = 0;
         if(!P.transmissive)
         {
             const bool occ = P.two_level ? trace_tlas<true>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z, r0.w,
-                                                            r1.x, r1.y, r1.z, r1.w, CULL_NONE)
+                                                            r1.x, r1.y, r1.z, r1.w, cull)
                                                    .occluded
                                          : trace_ray<true, false, STACK>(P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x,
-                                                                         r1.y, r1.z, r1.w, CULL_NONE, v, c, nullptr)
+                                                                         r1.y, r1.z, r1.w, cull, v, c, nullptr)
                                                    .occluded;
             if(occ) T = f3(0.f, 0.f, 0.f);
         }
         else if(!P.two_level)
         {
+            // Beer-Lambert through transmissive volumes: optical depth -sigma_t t at an entry (front
+            // face), +sigma_t t at an exit, clamped at 0 (visibility_test.slang:123-129, :161-162)
+            float3 od = f3(0.f, 0.f, 0.f);
             const bool open = trace_transmit<STACK>(
-                    P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, T, [&](uint32_t prim) {
-                        const vkg_material &q = P.mats[__ldg(&P.tri_mat[prim])];
+                    P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, cull, T,
+                    [&](uint32_t prim, float t, bool front) {
+                        const uint32_t mi = __ldg(&P.tri_mat[prim]);
+                        const vkg_material &q = P.mats[mi];
+                        if(q.null_surface) return f3(1.f, 1.f, 1.f); // null surfaces pass unattenuated
+                        if(P.media && (P.media[mi].flags & MEDIUM_VOLUME))
+                        {
+                            const medium_rec &M = P.media[mi];
+                            const float3 st = f3(M.sigma_s[0] + M.sigma_a[0], M.sigma_s[1] + M.sigma_a[1],
+                                                 M.sigma_s[2] + M.sigma_a[2]);
+                            od = od + st * (front ? -t : t);
+                        }
                         return f3(q.base_color[0], q.base_color[1], q.base_color[2]) * q.transmission;
                     });
             if(!open) T = f3(0.f, 0.f, 0.f);
+            else if(P.media)
+                T = T * f3(expf(-fmaxf(od.x, 0.f)), expf(-fmaxf(od.y, 0.f)), expf(-fmaxf(od.z, 0.f)));
         }
         else
         {
@@ -667,7 +858,7 @@ __global__ void __launch_bounds__(PT_THREADS) k_pt_light_shadow(J S, light_queue
                 if(P.two_level)
                 {
                     const tlas_result r = trace_tlas<false>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z, tmin,
-                                                            r1.x, r1.y, r1.z, r1.w, CULL_NONE);
+                                                            r1.x, r1.y, r1.z, r1.w, cull);
                     prim = r.prim;
                     t = r.t;
                     mat = prim == VKG_MISS ? 0u : __ldg(&P.tl_by_id[r.inst].material);
@@ -675,13 +866,18 @@ __global__ void __launch_bounds__(PT_THREADS) k_pt_light_shadow(J S, light_queue
                 else
                 {
                     const trace_result r = trace_ray<false, false, STACK>(P.nodes, P.tris, r0.x, r0.y, r0.z, tmin, r1.x,
-                                                                          r1.y, r1.z, r1.w, CULL_NONE, v, c, nullptr);
+                                                                          r1.y, r1.z, r1.w, cull, v, c, nullptr);
                     prim = r.prim;
                     t = r.t;
                     mat = prim == VKG_MISS ? 0u : __ldg(&P.tri_mat[prim]);
                 }
                 if(prim == VKG_MISS) break;
                 const vkg_material &q = P.mats[mat];
+                if(q.null_surface && k + 1 < PT_MAX_CROSSINGS)
+                {
+                    tmin = t;
+                    continue;
+                }
                 if(!(q.transmission > 0.f) || k + 1 >= PT_MAX_CROSSINGS)
                 {
                     T = f3(0.f, 0.f, 0.f);
@@ -693,7 +889,6 @@ __global__ void __launch_bounds__(PT_THREADS) k_pt_light_shadow(J S, light_queue
         }
         if(max3(T) > 0.f)
         {
-            const float4 cc = lq.contrib[i];
             float4 L = radiance[pid];
             L.x += T.x * cc.x;
             L.y += T.y * cc.y;
@@ -974,7 +1169,7 @@ __global__ void k_tri_flags(tri_rec *__restrict__ tris, uint32_t n, const uint32
     if(i >= n) return;
     const uint32_t m = tri_mat[tris[i].prim];
     tris[i].pad[0] = (m < num_mats && material_unculled(mats[m]) ? TRI_FLAG_TWOSIDED : 0u) |
-                     (m < num_mats && mats[m].transmission > 0.f ? TRI_FLAG_TRANSMISSIVE : 0u);
+                     (m < num_mats && (mats[m].transmission > 0.f || mats[m].null_surface) ? TRI_FLAG_TRANSMISSIVE : 0u);
 }
 
 __global__ void k_check_materials(const uint32_t *__restrict__ tri_mat, uint32_t n, uint32_t num_mats,
@@ -1040,6 +1235,8 @@ inline pt_params make_params(const vkg_scene *sc, const vkg_camera &cam, const v
     P.suppress_caustics = S.suppress_refractive_caustics;
     P.transmissive = sc->any_transmissive ? 1u : 0u;
     P.gbuf = nullptr;
+    P.media = sc->d_media;
+    P.mstack = nullptr;
     P.last_sample = S.num_samples ? S.num_samples - 1 : 0u;
     P.clip_near = S.clip_near > 0.f ? S.clip_near : 0.1f;
     return P;

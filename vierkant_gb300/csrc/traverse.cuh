@@ -24,7 +24,7 @@ enum cull_mode : int
     CULL_BACK_UNLESS_TWOSIDED = 2
 };
 constexpr uint32_t TRI_FLAG_TWOSIDED = 1u;
-constexpr uint32_t TRI_FLAG_TRANSMISSIVE = 2u; // the triangle's material has transmission > 0
+constexpr uint32_t TRI_FLAG_TRANSMISSIVE = 2u; // light shadow rays pass: transmission > 0 or a null surface
 
 struct trace_result
 {
@@ -246,14 +246,15 @@ __device__ __forceinline__ trace_result ray_result(const ray_state_t<STACK> &s)
 }
 
 // transmittance of a segment (light-NEE visibility): one pass over every triangle the ray crosses in
-// (tmin, tmax), no culling, in traversal order; false at the first triangle without
-// TRI_FLAG_TRANSMISSIVE, else T is multiplied by tint(prim) of each crossed transmissive triangle.
+// (tmin, tmax) (back faces culled when cull == CULL_BACK), in traversal order; false at the first
+// triangle without TRI_FLAG_TRANSMISSIVE, else T is multiplied by tint(prim, t, front face) of each
+// crossed transmissive triangle.
 // Every triangle sits in one leaf and every node is visited at most once, so each crossing counts
 // once; the children need no ordering.
 template<int STACK, class Tint>
 __device__ __forceinline__ bool trace_transmit(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
                                                float ox, float oy, float oz, float tmin, float dx, float dy, float dz,
-                                               float tmax, float3 &T, Tint tint)
+                                               float tmax, int cull, float3 &T, Tint tint)
 {
     const float ix = safe_rcp(dx), iy = safe_rcp(dy), iz = safe_rcp(dz);
     uint32_t st[STACK];
@@ -281,11 +282,14 @@ __device__ __forceinline__ bool trace_transmit(const node8 *__restrict__ nodes, 
                 const float4 *tp = reinterpret_cast<const float4 *>(tris + ti);
                 const float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
                 float t, u, v;
-                if(!tri_test(a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, cc.x, ox, oy, oz, dx, dy, dz, 0, t, u, v))
+                if(!tri_test(a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, cc.x, ox, oy, oz, dx, dy, dz,
+                             cull == CULL_BACK ? 1 : 0, t, u, v))
                     continue;
                 if(!(t > tmin && t < tmax)) continue;
                 if(!(__float_as_uint(cc.z) & TRI_FLAG_TRANSMISSIVE)) return false;
-                const float3 m = tint(__float_as_uint(cc.y));
+                // front face: the ray runs against the normal e1 x e2
+                const float nx = b.x * cc.x - b.y * b.w, ny = b.y * b.z - a.w * cc.x, nz = a.w * b.w - b.x * b.z;
+                const float3 m = tint(__float_as_uint(cc.y), t, nx * dx + ny * dy + nz * dz < 0.f);
                 T.x *= m.x;
                 T.y *= m.y;
                 T.z *= m.z;

@@ -18,7 +18,9 @@ MATERIAL_DTYPE = np.dtype([("base_color", "<f4", 3), ("roughness", "<f4"), ("met
                            ("clearcoat", "<f4"), ("clearcoat_roughness", "<f4"), ("sheen_color", "<f4", 3),
                            ("sheen_roughness", "<f4"), ("diffuse_transmission", "<f4"),
                            ("diffuse_transmission_color", "<f4", 3), ("iridescence", "<f4"),
-                           ("iridescence_ior", "<f4"), ("iridescence_thickness", "<f4")])
+                           ("iridescence_ior", "<f4"), ("iridescence_thickness", "<f4"), ("attenuation_color", "<f4", 3),
+                           ("attenuation_distance", "<f4"), ("scatter_color", "<f4", 3), ("scatter_factor", "<f4"),
+                           ("phase_g", "<f4"), ("null_surface", "<u4"), ("pad", "<f4", 2)])
 assert MATERIAL_DTYPE.itemsize == C.sizeof(vkg_material)
 
 
@@ -96,6 +98,52 @@ def showcase_materials(materials: np.ndarray) -> np.ndarray:
             m["iridescence_thickness"][i] = 400.0
             m["roughness"][i] = 0.25
             m["metalness"][i] = 1.0 if s % 2 else 0.0
+    return m
+
+
+MEDIA_KINDS = ("metal-rough", "fog", "absorbing glass", "emissive gas", "scattering glass")
+
+
+def media_materials(materials: np.ndarray) -> np.ndarray:
+    """The Cornell-box material table with its spheres cycled through homogeneous media: sphere s
+    (material 3 + s) becomes MEDIA_KINDS[s % 5] with its generated colour c as the medium's tint —
+    fog (a null surface around a forward-scattering medium), absorbing glass (Beer-Lambert inside a
+    smooth dielectric), emissive gas (a null surface around an absorbing medium that emits 4 c) and
+    scattering glass (a rough dielectric around a scattering medium). Attenuation distances are 0.25,
+    about one sphere radius. Overlapping spheres nest their media on the per-path stack."""
+    m = np.array(materials, MATERIAL_DTYPE, copy=True)
+    for s in range(len(m) - 3):
+        i, kind = 3 + s, s % len(MEDIA_KINDS)
+        c = m["base_color"][i].copy()
+        if kind == 0:
+            continue
+        m["metalness"][i] = 0.0
+        m["attenuation_distance"][i] = 0.25
+        if kind == 1:
+            m["null_surface"][i] = 1
+            m["attenuation_color"][i] = 0.35 + 0.5 * c
+            m["scatter_factor"][i] = 1.0
+            m["scatter_color"][i] = 0.6 + 0.4 * c
+            m["phase_g"][i] = 0.5
+        elif kind == 2:
+            m["transmission"][i] = 1.0
+            m["ior"][i] = 1.5
+            m["roughness"][i] = 0.0
+            m["base_color"][i] = 1.0
+            m["attenuation_color"][i] = 0.2 + 0.8 * c
+        elif kind == 3:
+            m["null_surface"][i] = 1
+            m["attenuation_color"][i] = (0.5, 0.5, 0.5)
+            m["emission"][i] = 4.0 * c
+        else:
+            m["transmission"][i] = 1.0
+            m["ior"][i] = 1.33
+            m["roughness"][i] = 0.2
+            m["base_color"][i] = 1.0
+            m["attenuation_color"][i] = 0.3 + 0.6 * c
+            m["scatter_factor"][i] = 1.0
+            m["scatter_color"][i] = 0.5 + 0.5 * c
+            m["phase_g"][i] = -0.2
     return m
 
 
