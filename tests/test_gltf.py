@@ -109,6 +109,33 @@ def test_materials(tmp_path):
     assert list(a["instances"]["material"]) == [0, 1, 0]  # no material -> index 0, as the reference
 
 
+def test_volume_and_scatter_materials(tmp_path):
+    """KHR_materials_volume gives the attenuation colour / distance (absent distance: infinite, no
+    medium); KHR_materials_scatter has a scatter factor defaulting to 0, the older
+    KHR_materials_volume_scatter none (implicitly 1) (gltf.cpp:476-500, :634-657)"""
+    mats = [
+        {"extensions": {"KHR_materials_volume": {"thicknessFactor": 0.1, "attenuationColor": [0.5, 0.6, 0.7],
+                                                 "attenuationDistance": 2.5},
+                        "KHR_materials_scatter": {"multiscatterColorFactor": [0.9, 0.8, 0.7],
+                                                  "scatterAnisotropy": 0.3, "scatterFactor": 0.6}}},
+        {"extensions": {"KHR_materials_volume": {"attenuationColor": [0.2, 0.2, 0.2]},
+                        "KHR_materials_scatter": {"multiscatterColorFactor": [0.1, 0.2, 0.3]}}},
+        {"extensions": {"KHR_materials_volume": {"attenuationDistance": 0.5},
+                        "KHR_materials_volume_scatter": {"scatterAnisotropy": -0.5}}},
+    ]
+    path = tmp_path / "v.gltf"
+    write(path, [[(*TRI, 0, None), (*TRI, 1, None), (*TRI, 2, None)]], [dict(mesh=0)], [0], materials=mats)
+    m = load_gltf(str(path))["materials"]
+    assert np.allclose(m[0]["attenuation_color"], (0.5, 0.6, 0.7)) and m[0]["attenuation_distance"] == 2.5
+    assert np.allclose(m[0]["scatter_color"], (0.9, 0.8, 0.7)) and np.isclose(m[0]["phase_g"], 0.3)
+    assert np.isclose(m[0]["scatter_factor"], 0.6)
+    assert np.isinf(m[1]["attenuation_distance"]) and m[1]["scatter_factor"] == 0  # unified: default 0
+    assert np.allclose(m[1]["scatter_color"], (0.1, 0.2, 0.3))
+    assert np.all(m[2]["attenuation_color"] == 1) and m[2]["attenuation_distance"] == 0.5
+    assert m[2]["scatter_factor"] == 1 and np.isclose(m[2]["phase_g"], -0.5)  # legacy: implicit 1
+    assert np.all(m[2]["scatter_color"] == 1)
+
+
 def test_lights(tmp_path):
     lights = [{"type": "point", "color": [1, 0.5, 0.25], "intensity": 3.0, "range": 10.0},
               {"type": "spot", "intensity": 2.0, "spot": {"innerConeAngle": 0.2, "outerConeAngle": 0.5}},

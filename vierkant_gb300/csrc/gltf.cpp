@@ -13,13 +13,15 @@
 //   * the materials (gltf.cpp:316-560): base colour, metallic (default 1), roughness (default 1),
 //     emissive x KHR_materials_emissive_strength, doubleSided, KHR_materials_transmission,
 //     KHR_materials_ior, KHR_materials_clearcoat, KHR_materials_sheen, KHR_materials_iridescence (the
-//     film thickness is the range's maximum, as the shader reads it), KHR_materials_diffuse_transmission;
-//     a default material when the asset has none;
+//     film thickness is the range's maximum, as the shader reads it), KHR_materials_diffuse_transmission,
+//     KHR_materials_volume (attenuation colour / distance) and KHR_materials_scatter /
+//     KHR_materials_volume_scatter (gltf.cpp:476-500, :634-657); a default material when the asset
+//     has none;
 //   * KHR_lights_punctual lights placed by their nodes (gltf.cpp:1043-1061, :1182-1190), converted as
 //     convert_light does (punctual_light.hpp:92-111): position = translation, direction = R (0,0,-1),
 //     tangent = R (1,0,0), R the node's rotation (its world matrix's columns normalised).
-// Not read: textures and texture transforms, skins, morph targets, animations, cameras, volumes,
-// specular, sparse accessors, quantised positions. The reference composes transforms as
+// Not read: textures and texture transforms, skins, morph targets, animations, cameras, volume
+// thickness, specular, sparse accessors, quantised positions. The reference composes transforms as
 // translation / quaternion / scale triples and projects shear away (transform.hpp:106-128); the
 // matrix composition here is the same for every chain without shear.
 #include "internal.hpp"
@@ -574,6 +576,24 @@ struct loader
             {
                 r.diffuse_transmission = clampf(e->num("diffuseTransmissionFactor", 0.0), 0, 1);
                 rd(e, "diffuseTransmissionColorFactor", r.diffuse_transmission_color, 3);
+            }
+            if(const jv *e = ext->get("KHR_materials_volume"))
+            {
+                // attenuation colour / distance (absent distance: infinite, no medium); the
+                // thickness factor drives no part of the path tracer and is not stored
+                rd(e, "attenuationColor", r.attenuation_color, 3);
+                r.attenuation_distance = (float)e->num("attenuationDistance", (double)r.attenuation_distance);
+            }
+            // KHR_materials_scatter (scatterFactor, default 0) or the older KHR_materials_volume_scatter
+            // (no factor: implicitly 1): multi-scatter colour and Henyey-Greenstein anisotropy
+            const jv *sc = ext->get("KHR_materials_scatter");
+            const bool unified = sc != nullptr;
+            if(!sc) sc = ext->get("KHR_materials_volume_scatter");
+            if(sc)
+            {
+                rd(sc, "multiscatterColorFactor", r.scatter_color, 3);
+                r.phase_g = (float)sc->num("scatterAnisotropy", 0.0);
+                r.scatter_factor = (float)sc->num("scatterFactor", unified ? 0.0 : 1.0);
             }
         }
         for(int c = 0; c < 3; ++c) r.emission[c] = em[c] * strength;
