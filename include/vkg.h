@@ -432,6 +432,30 @@ vkg_status vkg_scene_env_tables(const vkg_scene *scene, const float **d_weights,
                                 uint32_t *width, uint32_t *height);
 
 /* ---- path tracer (replaces PBRPathTracer, include/vierkant/PBRPathTracer.hpp:37-386) ---------- */
+/* a homogeneous medium given directly (the reference's medium_params_t, include/vierkant/media.hpp:26-49,
+   converted as to_media does, src/media.cpp:6-23): sigma_t = -log(attenuation_color) /
+   attenuation_distance, single-scattering albedo from scatter_factor x scatter_color (Kulla-Conty),
+   emitted radiance emission_color x emission_intensity */
+typedef struct vkg_medium_params
+{
+    float attenuation_color[3]; /* (0.7, 0.7, 0.7), each in (0, 1] */
+    float attenuation_distance; /* 1, finite and > 0 */
+    float scatter_factor;       /* 0, in [0, 1] */
+    float scatter_color[3];     /* (1, 1, 1), each in [0, 1] */
+    float phase_g;              /* 0, in (-1, 1) */
+    float ior;                  /* 1 */
+    float emission_color[3];    /* (1, 1, 1) */
+    float emission_intensity;   /* 0 */
+} vkg_medium_params;            /* 56 B */
+vkg_status vkg_medium_params_default(vkg_medium_params *out);
+enum
+{
+    VKG_CAMERA_MEDIUM_DETECT = 0, /* the reference's default (PBRPathTracer.cpp:471-525, :598-605): in an
+                                     instanced scene, the material of the smallest instance whose world
+                                     box (its mesh's box under the instance transform) contains the eye
+                                     and whose material has a finite attenuation distance; else vacuum */
+    VKG_CAMERA_MEDIUM_GIVEN = 1,  /* settings.camera_medium (settings_t::camera_medium set) */
+};
 /* PBRPathTracer::settings_t (PBRPathTracer.hpp:42-110): the fields of the traced path */
 typedef struct vkg_settings
 {
@@ -460,7 +484,14 @@ typedef struct vkg_settings
     uint32_t denoising;               /* settings_t::denoising: the output is the a-trous filtered image */
     float clip_near;                  /* the camera's near clipping distance, for the pixel depth
                                          near / view-space distance (camera_params.hpp:37); 0: 0.1 */
+    /* the medium the camera sits in (paths start with it on their media stack,
+       raypipeline.slang:128-135): VKG_CAMERA_MEDIUM_DETECT or VKG_CAMERA_MEDIUM_GIVEN */
+    uint32_t camera_medium_mode;
+    vkg_medium_params camera_medium;  /* used when camera_medium_mode = VKG_CAMERA_MEDIUM_GIVEN */
 } vkg_settings;
+/* the camera medium a render of `scene` seen from `eye` would detect: the material index, or
+   0xFFFFFFFF for vacuum (always vacuum for single-level scenes, which have no objects) */
+vkg_status vkg_scene_camera_medium(const vkg_scene *scene, const float eye[3], uint32_t *material);
 
 /* ---- glTF 2.0 ingestion (host only; the reference's model/gltf.cpp path) --------------------
  * vkg_gltf_load reads a .gltf (base64 or file buffers) or .glb file into meshes (one per triangle

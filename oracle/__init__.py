@@ -267,7 +267,8 @@ class orc_pt_settings(C.Structure):
                 ("rr_depth", C.c_uint32), ("mis_mode", C.c_uint32), ("disable_material", C.c_uint32),
                 ("draw_skybox", C.c_uint32), ("max_path_beta", C.c_float), ("environment", C.c_float),
                 ("crop", C.c_uint32 * 4), ("num_lights", C.c_uint32), ("suppress_caustics", C.c_uint32),
-                ("lights", C.c_void_p), ("pixels", C.c_void_p), ("clip_near", C.c_float)]
+                ("lights", C.c_void_p), ("pixels", C.c_void_p), ("clip_near", C.c_float),
+                ("camera_medium", C.c_void_p), ("camera_material", C.c_uint32)]
 
 
 # per-pixel record (32 bytes, the layout of vkg_pixel_data)
@@ -314,14 +315,31 @@ def sun_light(color, intensity, spherical_coords, angular_size):
     return out[0]
 
 
+MEDIUM_PARAMS = ("attenuation_color", "attenuation_distance", "scatter_factor", "scatter_color", "phase_g", "ior",
+                 "emission_color", "emission_intensity")
+MEDIUM_DEFAULTS = dict(attenuation_color=(0.7, 0.7, 0.7), attenuation_distance=1.0, scatter_factor=0.0,
+                       scatter_color=(1, 1, 1), phase_g=0.0, ior=1.0, emission_color=(1, 1, 1),
+                       emission_intensity=0.0)
+
+
+def medium_params(**kw):
+    """the 14 floats of a camera medium (medium_params_t order) from keyword fields over the defaults"""
+    d = dict(MEDIUM_DEFAULTS, **kw)
+    return np.concatenate([np.atleast_1d(np.asarray(d[k], np.float32)) for k in MEDIUM_PARAMS]).astype(np.float32)
+
+
 def _settings(seed, batch, spp, max_depth, rr_depth, mis_mode, draw_skybox, max_path_beta, environment, crop, lights,
-              suppress_caustics, pixels=None, clip_near=0.1):
+              suppress_caustics, pixels=None, clip_near=0.1, camera_medium=None, camera_material=None):
     arr = np.ascontiguousarray(np.asarray(lights if lights is not None else [], LIGHT_DTYPE).reshape(-1))
+    cm = np.ascontiguousarray(camera_medium, np.float32) if camera_medium is not None else None
+    assert cm is None or cm.shape == (14,)
     st = orc_pt_settings(seed, batch, spp, max_depth, rr_depth, mis_mode, 0, draw_skybox, max_path_beta, environment,
                          (C.c_uint32 * 4)(*crop), len(arr), int(suppress_caustics),
                          arr.ctypes.data_as(C.c_void_p) if len(arr) else None,
-                         pixels.ctypes.data_as(C.c_void_p) if pixels is not None else None, clip_near)
-    return st, arr
+                         pixels.ctypes.data_as(C.c_void_p) if pixels is not None else None, clip_near,
+                         cm.ctypes.data_as(C.c_void_p) if cm is not None else None,
+                         0xFFFFFFFF if camera_material is None else int(camera_material))
+    return st, (arr, cm)
 
 
 def cornell_materials(seed=0x5EED, stream=2, num_spheres=64):
@@ -362,7 +380,7 @@ def env_tables_fp64(rgb):
 def pt_render(fp64, xyz, idx, tri_mat, mats, bvh: "CpuBVH", env_rgb, cam, spp, *, seed=0x5EED, batch=0, max_depth=6,
               rr_depth=3, mis_mode=0, crop=(0, 0, 0, 0), environment=1.0, draw_skybox=1, max_path_beta=0.0,
               alias_prob=None, alias=None, weight=None, cdf=None, nthreads=0, lights=None, suppress_caustics=False,
-              pixels=None, clip_near=0.1):
+              pixels=None, clip_near=0.1, camera_medium=None, camera_material=None):
     """Mean radiance per crop pixel ([h, w, 3] float64), mean squared luminance per pixel, (ext, shadow) rays.
     pixels: optional PIXEL_DTYPE array [h, w] of the crop, filled with the pixel records (radiance left 0)
     the tracer writes."""
@@ -381,8 +399,8 @@ def pt_render(fp64, xyz, idx, tri_mat, mats, bvh: "CpuBVH", env_rgb, cam, spp, *
                      ptr(alias) if alias is not None else None, ptr(cdf) if cdf is not None else None, w, h)
     cw = crop[2] or cam.width
     ch = crop[3] or cam.height
-    st, _lights = _settings(seed, batch, spp, max_depth, rr_depth, mis_mode, draw_skybox, max_path_beta, environment,
-                            crop, lights, suppress_caustics, pixels, clip_near)
+    st, _keep = _settings(seed, batch, spp, max_depth, rr_depth, mis_mode, draw_skybox, max_path_beta, environment,
+                          crop, lights, suppress_caustics, pixels, clip_near, camera_medium, camera_material)
     out = np.zeros((ch, cw, 3), np.float64)
     sq = np.zeros((ch, cw), np.float64)
     stats = np.zeros(2, np.uint64)
@@ -400,10 +418,12 @@ class orc_pt_instances(C.Structure):
 
 def pt_render_instanced(meshes, o2w, inst_mesh, inst_mat, mats, env_rgb, cam, spp, *, seed=0x5EED, batch=0,
                         max_depth=6, rr_depth=3, mis_mode=0, crop=(0, 0, 0, 0), environment=1.0, draw_skybox=1,
-                        nthreads=0, mesh_bvhs=None, lights=None, suppress_caustics=False):
+                        nthreads=0, mesh_bvhs=None, lights=None, suppress_caustics=False, camera_medium=None,
+                        camera_material=None):
     """FP64 oracle of an instanced scene: meshes [(xyz, idx, twosided)], o2w [N, 12] object -> world,
     mesh and material index per instance. Returns (mean radiance [h, w, 3], mean squared luminance,
-    (ext, shadow) rays)."""
+    (ext, shadow) rays). camera_medium: medium_params(...) floats; camera_material: the material whose
+    medium the camera sits in."""
     L = orc()
     L.orc_pt_render_instanced.argtypes = [C.POINTER(orc_pt_scene), C.POINTER(orc_pt_instances),
                                           C.POINTER(orc_pt_env), C.POINTER(orc_camera),
@@ -432,8 +452,8 @@ def pt_render_instanced(meshes, o2w, inst_mesh, inst_mat, mats, env_rgb, cam, sp
     env = orc_pt_env(ptr(rgb), ptr(np.ascontiguousarray(weight, np.float32)), None, None, ptr(cdf), w, h)
     cw = crop[2] or cam.width
     ch = crop[3] or cam.height
-    st, _lights = _settings(seed, batch, spp, max_depth, rr_depth, mis_mode, draw_skybox, 0.0, environment, crop,
-                            lights, suppress_caustics)
+    st, _keep = _settings(seed, batch, spp, max_depth, rr_depth, mis_mode, draw_skybox, 0.0, environment, crop,
+                          lights, suppress_caustics, None, 0.1, camera_medium, camera_material)
     out = np.zeros((ch, cw, 3), np.float64)
     sq = np.zeros((ch, cw), np.float64)
     stats = np.zeros(2, np.uint64)

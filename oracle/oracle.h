@@ -174,6 +174,12 @@ typedef struct {
     const orc_pt_light *lights; /* the sun (if any) first */
     orc_pixel *pixels;          /* optional: the crop's pixel records (radiance left 0), as the tracer writes them */
     float clip_near;            /* near clipping distance for the records' depth */
+    /* the camera's medium (raypipeline.slang:128-135): camera_medium = 14 floats in the order of the
+       reference's medium_params_t (attenuation colour, distance, scatter factor, scatter colour, g,
+       ior, emission colour, intensity), or camera_material = a material whose medium it is (its own
+       ior also for a null surface); NULL / 0xFFFFFFFF: vacuum */
+    const float *camera_medium;
+    uint32_t camera_material;
 } orc_pt_settings;
 
 /* the sun of the tracer settings as a directional light (PBRPathTracer.cpp:610-624): propagation

@@ -48,6 +48,53 @@ static void orc_medium_from(const orc_pt_material *m, orc_medium *r)
     r->flags = (vol ? 1u : 0u) | (m->null_surface ? 2u : 0u);
 }
 
+/* a medium given directly (media.hpp:26-49 converted as to_media, media.cpp:6-23): p = attenuation
+   colour[3], distance, scatter factor, scatter colour[3], g, ior, emission colour[3], intensity */
+static void orc_medium_from_params(const float *p, orc_medium *r)
+{
+    for(int c = 0; c < 3; ++c)
+    {
+        float st = -logf(p[c]) / p[3];
+        float ms = p[4] * p[5 + c];
+        float kc = 4.09712f + 4.20863f * ms - sqrtf(9.59217f + 41.6808f * ms + 17.7126f * ms * ms);
+        float ss = 1.f - kc * kc;
+        r->sigma_s[c] = ss * st;
+        r->sigma_a[c] = (1.f - ss) * st;
+        r->emission[c] = p[10 + c] * p[13];
+    }
+    r->g = p[8];
+    r->ior = p[9];
+    r->flags = 1u;
+}
+
+/* the medium table of a render: one record per material, plus the camera's medium as the last one;
+   NULL when no material bounds a medium and the camera sits in vacuum */
+static orc_medium *orc_media_table(const orc_pt_scene *scene, const orc_pt_settings *set, uint32_t *cam)
+{
+    int any = set->camera_medium != NULL || set->camera_material < scene->nmat;
+    for(uint32_t i = 0; i < scene->nmat && !any; ++i)
+    {
+        const orc_pt_material *m = &scene->mats[i];
+        any = m->null_surface || (m->attenuation_distance > 0.f && m->attenuation_distance < 3.0e38f);
+    }
+    *cam = 0xFFFFFFFFu;
+    if(!any) return NULL;
+    orc_medium *media = (orc_medium *)calloc(scene->nmat + 1, sizeof(orc_medium));
+    for(uint32_t i = 0; i < scene->nmat; ++i) orc_medium_from(&scene->mats[i], &media[i]);
+    if(set->camera_medium)
+    {
+        orc_medium_from_params(set->camera_medium, &media[scene->nmat]);
+        *cam = scene->nmat;
+    }
+    else if(set->camera_material < scene->nmat)
+    {
+        media[scene->nmat] = media[set->camera_material];
+        media[scene->nmat].flags = 1u;
+        *cam = scene->nmat;
+    }
+    return media;
+}
+
 typedef struct {
     const orc_pt_scene *scene;
     const orc_bvh *bvh;
@@ -60,7 +107,8 @@ typedef struct {
     uint32_t num_lights, suppress_caustics;
     orc_pixel *pixels;
     float clip_near;
-    const orc_medium *media; /* per material, NULL: the scene has no media */
+    const orc_medium *media; /* per material (+ the camera's), NULL: no media */
+    uint32_t cam_medium;     /* index of the camera's medium, 0xFFFFFFFF: vacuum */
     uint32_t cx0, cy0, cw, ch;
     double *out, *sq;
     const orc_pt_instances *inst; /* NULL: single-level scene */
@@ -802,18 +850,7 @@ int orc_pt_render(int fp64, const orc_pt_scene *scene, const orc_bvh *bvh, const
     J.suppress_caustics = set->suppress_caustics;
     J.pixels = set->pixels;
     J.clip_near = set->clip_near > 0.f ? set->clip_near : 0.1f;
-    orc_medium *media = NULL;
-    for(uint32_t i = 0; i < scene->nmat; ++i)
-    {
-        const orc_pt_material *m = &scene->mats[i];
-        if(m->null_surface || (m->attenuation_distance > 0.f && m->attenuation_distance < 3.0e38f))
-        {
-            media = (orc_medium *)calloc(scene->nmat, sizeof(orc_medium));
-            break;
-        }
-    }
-    if(media)
-        for(uint32_t i = 0; i < scene->nmat; ++i) orc_medium_from(&scene->mats[i], &media[i]);
+    orc_medium *media = orc_media_table(scene, set, &J.cam_medium);
     J.media = media;
     J.cx0 = set->crop[0];
     J.cy0 = set->crop[1];
@@ -866,18 +903,7 @@ int orc_pt_render_instanced(const orc_pt_scene *scene, const orc_pt_instances *i
     J.suppress_caustics = set->suppress_caustics;
     J.pixels = set->pixels;
     J.clip_near = set->clip_near > 0.f ? set->clip_near : 0.1f;
-    orc_medium *media = NULL;
-    for(uint32_t i = 0; i < scene->nmat; ++i)
-    {
-        const orc_pt_material *m = &scene->mats[i];
-        if(m->null_surface || (m->attenuation_distance > 0.f && m->attenuation_distance < 3.0e38f))
-        {
-            media = (orc_medium *)calloc(scene->nmat, sizeof(orc_medium));
-            break;
-        }
-    }
-    if(media)
-        for(uint32_t i = 0; i < scene->nmat; ++i) orc_medium_from(&scene->mats[i], &media[i]);
+    orc_medium *media = orc_media_table(scene, set, &J.cam_medium);
     J.media = media;
     J.cx0 = set->crop[0];
     J.cy0 = set->crop[1];

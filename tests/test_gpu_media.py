@@ -141,11 +141,11 @@ def test_emissive_box_matches_emission_integral(ctx):
     assert abs(img.sum() / expect.sum() - 1) < 0.01
 
 
-@pytest.mark.parametrize("g", [0.0, 0.6, -0.4])
-def test_white_scattering_furnace(ctx, g):
+@pytest.mark.parametrize("g,mis", [(0.0, 2), (0.6, 2), (-0.4, 2), (0.3, 0), (0.3, 1)])
+def test_white_scattering_furnace(ctx, g, mis):
     mat = null_box_material(attenuation_color=(0.3, 0.3, 0.3), attenuation_distance=1.0, scatter_factor=1.0,
                             scatter_color=(1, 1, 1), phase_g=g)
-    img = _box_render(ctx, mat, 1.0, 1024, mis=2, max_depth=64)
+    img = _box_render(ctx, mat, 1.0, 1024, mis=mis, max_depth=64)
     assert abs(img.mean() - 1) < 0.005, img.mean()
 
 
@@ -183,3 +183,114 @@ def test_invalid_media_rejected(ctx, field, value):
     env = torch.ones((8, 16, 3), dtype=torch.float32, device="cuda")
     with pytest.raises(_lib.VkgError):
         Scene(ctx, xyz, idx, np.zeros(len(idx), np.uint32), mat, env)
+
+
+def test_camera_medium_given_twin(ctx):
+    """a camera inside a scattering box whose medium is given in the settings: the FP32 twin with the
+    same camera medium reproduces the GPU image path for path"""
+    from vierkant_gb300.pathtracer import CAMERA_MEDIUM_GIVEN, medium_params
+    fields = dict(attenuation_color=(0.5, 0.7, 0.9), attenuation_distance=4.0, scatter_factor=0.8,
+                  scatter_color=(0.9, 0.8, 0.7), phase_g=0.3)
+    xyz, idx = box_mesh(5.0)
+    mat = null_box_material(**fields)
+    env = torch.full((32, 64, 3), 0.8, dtype=torch.float32, device="cuda")
+    scene = Scene(ctx, xyz, idx, np.zeros(len(idx), np.uint32), mat, env)
+    tan_half = 0.2679
+    cam = geometry.camera_lookat((0.3, 0.2, 4.0), (0, 0, 0), (0, 1, 0), math.degrees(2 * math.atan(tan_half)), 64, 64)
+    s = settings(16, max_depth=8, res=(64, 64))
+    s.camera_medium_mode = CAMERA_MEDIUM_GIVEN
+    s.camera_medium = medium_params(**fields)
+    pt = PBRPathTracer(ctx, seed=11, settings=s)
+    img = pt.render_scene(scene, cam).cpu().numpy().astype(np.float64)
+    st = pt.statistics()
+    pt.close()
+    wptr, aptr, EW, EH = scene.env_tables()
+    n = EW * EH
+    w = d2h(wptr, 4 * n, np.float32)
+    tab = d2h(aptr, 8 * n, np.uint32).reshape(n, 2)
+    ocam = oracle.camera((0.3, 0.2, 4.0), (0, 0, 0), (0, 1, 0), float(cam.tan_half_fovy), 64, 64)
+    twin, _, rays = oracle.pt_render(False, xyz, idx, np.zeros(len(idx), np.uint32), mat, oracle.CpuBVH(xyz, idx, 4),
+                                     env.cpu().numpy(), ocam, 16, seed=11, max_depth=8, rr_depth=3,
+                                     alias_prob=np.ascontiguousarray(tab[:, 0].view(np.float32)),
+                                     alias=np.ascontiguousarray(tab[:, 1]), weight=w,
+                                     camera_medium=oracle.medium_params(**fields))
+    scene.close()
+    rel = np.abs(img - twin) / np.maximum(np.abs(twin), 1e-2)
+    close = np.mean(np.all(rel < 1e-3, axis=-1))
+    print(f"close {close:.4f} sum ratio {img.sum() / twin.sum():.5f} rays {st.extension_rays}/{rays[0]}")
+    assert close > 0.9 and abs(img.sum() / twin.sum() - 1) < 0.02
+    assert abs(st.extension_rays / rays[0] - 1.0) < 0.01
+    assert img.mean() < 0.8  # the medium's absorption dims the environment
+
+
+def test_camera_medium_detected_in_instanced_scene(ctx):
+    """PBRPathTracer.cpp:471-525: of the instances whose oriented world box contains the eye and whose
+    material has a finite attenuation distance, the smallest; a render that detects it equals one given
+    the same medium"""
+    from vierkant_gb300.pathtracer import CAMERA_MEDIUM_GIVEN, InstancedScene, medium_params
+    from vierkant_gb300.raytracing import INSTANCE_DTYPE
+    fields = dict(attenuation_color=(0.6, 0.7, 0.8), attenuation_distance=3.0, scatter_factor=0.5,
+                  scatter_color=(0.9, 0.9, 0.9), phase_g=0.2)
+    mats = np.concatenate([null_box_material(), null_box_material(attenuation_color=(0.9, 0.9, 0.9),
+                                                                  attenuation_distance=20.0),
+                           null_box_material(attenuation_color=(0.5, 0.5, 0.5), attenuation_distance=2.0),
+                           null_box_material(attenuation_color=(0.5, 0.5, 0.5), attenuation_distance=1.0),
+                           null_box_material(**fields)])
+    xyz, idx = box_mesh(1.0)
+
+    def place(scale, t=(0, 0, 0), rot_z=False):
+        M = np.diag(np.asarray(scale, np.float64))
+        if rot_z:
+            M = np.array([[0, -1, 0], [1, 0, 0], [0, 0, 1]], np.float64) @ M
+        return np.concatenate([M, np.asarray(t, np.float64)[:, None]], axis=1).reshape(-1)
+
+    inst = np.zeros(5, INSTANCE_DTYPE)
+    rows = [(place((10, 10, 10)), 1),            # a large volume around the eye
+            (place((3, 3, 3)), 2),               # a smaller one
+            (place((2, 2, 2)), 0),               # smaller still, but no volume: skipped
+            (place((1.5, 1.5, 1.5), (10, 0, 0)), 3),  # a volume away from the eye
+            (place((4, 0.5, 4), rot_z=True), 4)]  # rotated: world half extents (0.5, 4, 4), the smallest
+    for k, (T, m) in enumerate(rows):
+        inst["transform"][k], inst["blas"][k], inst["material"][k] = T, 0, m
+    env = torch.full((16, 32, 3), 0.8, dtype=torch.float32, device="cuda")
+    scene = InstancedScene(ctx, [(xyz, idx, 0)], inst, mats, env)
+    eye = (0.3, 0.2, 2.5)
+    assert scene.camera_medium(eye) == 4
+    assert scene.camera_medium((1.0, 0.0, 0.0)) == 2   # outside the rotated box, inside the 3-box
+    assert scene.camera_medium((30.0, 0.0, 0.0)) is None
+    cam = geometry.camera_lookat(eye, (0, 0, 0), (0, 1, 0), 40.0, 32, 32)
+    images = []
+    for given in (False, True):
+        s = settings(8, max_depth=8, res=(32, 32))
+        if given:
+            s.camera_medium_mode = CAMERA_MEDIUM_GIVEN
+            s.camera_medium = medium_params(**fields)
+        pt = PBRPathTracer(ctx, seed=5, settings=s)
+        images.append(pt.render_scene(scene, cam).clone())
+        pt.close()
+    scene.close()
+    assert torch.equal(images[0], images[1])
+
+
+def test_camera_medium_validated(ctx):
+    from vierkant_gb300.pathtracer import CAMERA_MEDIUM_GIVEN, medium_params
+    xyz, idx = box_mesh(1.0)
+    env = torch.ones((8, 16, 3), dtype=torch.float32, device="cuda")
+    scene = Scene(ctx, xyz, idx, np.zeros(len(idx), np.uint32), null_box_material(), env)
+    cam = geometry.camera_lookat((0, 0, 4), (0, 0, 0), (0, 1, 0), 30.0, 8, 8)
+    for bad in (dict(attenuation_color=(0, 1, 1)), dict(attenuation_distance=0.0), dict(phase_g=1.0),
+                dict(scatter_factor=2.0), dict(ior=-1.0)):
+        s = settings(1, res=(8, 8))
+        s.camera_medium_mode = CAMERA_MEDIUM_GIVEN
+        s.camera_medium = medium_params(**bad)
+        pt = PBRPathTracer(ctx, seed=1, settings=s)
+        with pytest.raises(_lib.VkgError):
+            pt.render_scene(scene, cam)
+        pt.close()
+    s = settings(1, res=(8, 8))
+    s.camera_medium_mode = 7
+    pt = PBRPathTracer(ctx, seed=1, settings=s)
+    with pytest.raises(_lib.VkgError):
+        pt.render_scene(scene, cam)
+    pt.close()
+    scene.close()

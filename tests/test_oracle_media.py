@@ -124,16 +124,17 @@ def test_emissive_box_matches_emission_integral():
     assert np.all(img[~(Lc > 0).any(axis=2)] == 0)
 
 
-@pytest.mark.parametrize("g", [0.0, 0.6, -0.4])
-def test_white_scattering_furnace(g):
+@pytest.mark.parametrize("g,mis", [(0.0, 2), (0.6, 2), (-0.4, 2), (0.3, 0), (0.3, 1)])
+def test_white_scattering_furnace(g, mis):
     """a non-absorbing scatterer (scatter colour 1 at scatter factor 1: single-scattering albedo 1 by the
-    Kulla-Conty inversion) in a constant unit environment, phase-function sampling only: every path
-    escapes eventually, so radiance 1 comes back at every pixel"""
+    Kulla-Conty inversion) in a constant unit environment: every path escapes eventually, so radiance 1
+    comes back at every pixel. Scattering events take no environment NEE sample, so MIS and NEE-only
+    collect the environment from the phase-sampled paths like BSDF-only does."""
     mat = null_box_material(attenuation_color=(0.3, 0.3, 0.3), attenuation_distance=1.0, scatter_factor=1.0,
                             scatter_color=(1, 1, 1), phase_g=g)
     ss, sa = medium_of(mat)
     assert np.all(sa < 1e-6 * ss)
-    img = render(mat, 1.0, 128, mis_mode=2, max_depth=64)
+    img = render(mat, 1.0, 128, mis_mode=mis, max_depth=64)
     assert abs(img.mean() - 1) < 0.01, img.mean()
     inside = (chords(64) > 0).all(axis=2)
     assert abs(img[inside].mean() - 1) < 0.015
@@ -171,3 +172,32 @@ def test_null_surface_without_medium_is_invisible():
     attenuates: the environment comes through unchanged"""
     img = render(null_box_material(), 0.75, 4)
     assert np.allclose(img, 0.75, rtol=0, atol=1e-12)
+
+
+def test_camera_inside_medium():
+    """a camera inside an absorbing box (raypipeline.slang:128-135): paths start with the camera's medium
+    on their stack, so a ray that leaves through the box wall at distance t carries exp(-sigma_t t);
+    the medium given as parameters and as the box material's render identically; without a camera
+    medium the exit wall pops nothing and the environment comes through unattenuated"""
+    big = 5.0
+    xyz, idx = box_mesh(big)
+    mat = null_box_material(attenuation_color=(0.5, 0.7, 0.9), attenuation_distance=6.0)
+    env = np.ones((32, 64, 3), np.float32)
+    args = (True, xyz, idx, np.zeros(len(idx), np.uint32), mat, oracle.CpuBVH(xyz, idx, 4), env, cam(), 16)
+    kw = dict(max_depth=4, rr_depth=64, mis_mode=0)
+    given, _, _ = oracle.pt_render(*args, camera_medium=oracle.medium_params(attenuation_color=(0.5, 0.7, 0.9),
+                                                                             attenuation_distance=6.0), **kw)
+    by_mat, _, _ = oracle.pt_render(*args, camera_material=0, **kw)
+    vacuum, _, _ = oracle.pt_render(*args, **kw)
+    assert np.array_equal(given, by_mat)
+    assert np.all(vacuum == 1.0)
+    r = oracle.camera_rays(cam(), 7, 3, 256)
+    o, d = r["o"].astype(np.float64), r["d"].astype(np.float64)
+    d = d / np.linalg.norm(d, axis=1, keepdims=True)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        tf = np.nanmin(np.maximum((-big - o) / d, (big - o) / d), axis=1)
+    st = -np.log(np.array([0.5, 0.7, 0.9])) / 6.0
+    expect = np.exp(-st[None, :] * tf[:, None]).reshape(256, RES, RES, 3).mean(axis=0)
+    # free-flight escapes weigh tr / mean(tr): per channel unbiased, 16 spp x 256 pixels
+    for c in range(3):
+        assert abs(given[..., c].mean() / expect[..., c].mean() - 1) < 0.03, c

@@ -59,6 +59,12 @@ class vkg_camera(C.Structure):
                 ("tan_half_fovy", C.c_float), ("aspect", C.c_float), ("width", C.c_uint32), ("height", C.c_uint32)]
 
 
+class vkg_medium_params(C.Structure):
+    _fields_ = [("attenuation_color", C.c_float * 3), ("attenuation_distance", C.c_float),
+                ("scatter_factor", C.c_float), ("scatter_color", C.c_float * 3), ("phase_g", C.c_float),
+                ("ior", C.c_float), ("emission_color", C.c_float * 3), ("emission_intensity", C.c_float)]
+
+
 class vkg_settings(C.Structure):
     _fields_ = [("resolution", C.c_uint32 * 2), ("max_num_batches", C.c_uint32), ("num_samples", C.c_uint32),
                 ("max_trace_depth", C.c_uint32), ("max_path_beta", C.c_float), ("suspend_trace_when_done", C.c_uint32),
@@ -66,7 +72,8 @@ class vkg_settings(C.Structure):
                 ("environment", C.c_float), ("rr_start_depth", C.c_uint32), ("crop", C.c_uint32 * 4),
                 ("samples_per_wave", C.c_uint32), ("suppress_refractive_caustics", C.c_uint32),
                 ("sun_color", C.c_float * 3), ("sun_intensity", C.c_float), ("sun_spherical_coords", C.c_float * 2),
-                ("sun_angular_size", C.c_float), ("denoising", C.c_uint32), ("clip_near", C.c_float)]
+                ("sun_angular_size", C.c_float), ("denoising", C.c_uint32), ("clip_near", C.c_float),
+                ("camera_medium_mode", C.c_uint32), ("camera_medium", vkg_medium_params)]
 
 
 class vkg_post_fx_settings(C.Structure):
@@ -231,6 +238,8 @@ SIGNATURES = {
     "vkg_scene_bvh": (I32, [P, C.POINTER(P)]),
     "vkg_scene_env_tables": (I32, [P, C.POINTER(P), C.POINTER(P), C.POINTER(U32), C.POINTER(U32)]),
     "vkg_settings_default": (I32, [C.POINTER(vkg_settings)]),
+    "vkg_medium_params_default": (I32, [C.POINTER(vkg_medium_params)]),
+    "vkg_scene_camera_medium": (I32, [P, C.POINTER(C.c_float), C.POINTER(U32)]),
     "vkg_tracer_create": (I32, [P, C.POINTER(vkg_tracer_create_info), C.POINTER(P)]),
     "vkg_tracer_set_settings": (I32, [P, C.POINTER(vkg_settings)]),
     "vkg_tracer_get_settings": (I32, [P, C.POINTER(vkg_settings)]),

@@ -459,7 +459,8 @@ vkg_status vkg_batch_create(vkg_ctx *ctx, const vkg_batch_job *jobs, uint32_t nj
         const vkg_batch_job &jb = jobs[j];
         if(!jb.scene) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_batch_create: job %u has no scene", j);
         if(vkg_status s = check_tracer_settings(ctx, &jb.settings); s != VKG_OK) return s;
-        if(!jb.scene->lights.empty() || jb.settings.sun_intensity > 0.f || jb.scene->d_media)
+        if(!jb.scene->lights.empty() || jb.settings.sun_intensity > 0.f || jb.scene->d_media ||
+           jb.settings.camera_medium_mode != VKG_CAMERA_MEDIUM_DETECT)
             return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
                              "vkg_batch_create: job %u: analytic lights, the sun and media are rendered by "
                              "vkg_tracer_render", j);

@@ -54,6 +54,39 @@ inline medium_rec medium_from_material(const vkg_material &m)
     return r;
 }
 
+// a medium given directly (media.hpp:26-49 converted as to_media, media.cpp:6-23): always a volume,
+// emission colour x intensity
+inline medium_rec medium_from_params(const vkg_medium_params &p)
+{
+    medium_rec r{};
+    for(int c = 0; c < 3; ++c)
+    {
+        const float st = -std::log(p.attenuation_color[c]) / p.attenuation_distance;
+        const float ms = p.scatter_factor * p.scatter_color[c];
+        const float kc = 4.09712f + 4.20863f * ms - std::sqrt(9.59217f + 41.6808f * ms + 17.7126f * ms * ms);
+        const float ss = 1.f - kc * kc;
+        r.sigma_s[c] = ss * st;
+        r.sigma_a[c] = (1.f - ss) * st;
+        r.emission[c] = p.emission_color[c] * p.emission_intensity;
+    }
+    r.g = p.phase_g;
+    r.ior = p.ior;
+    r.flags = MEDIUM_VOLUME;
+    return r;
+}
+
+inline bool medium_params_valid(const vkg_medium_params &p)
+{
+    auto unit = [](float x) { return x >= 0.f && x <= 1.f; };
+    for(int c = 0; c < 3; ++c)
+        if(!(p.attenuation_color[c] > 0.f && p.attenuation_color[c] <= 1.f) || !unit(p.scatter_color[c]) ||
+           !(p.emission_color[c] >= 0.f) || !std::isfinite(p.emission_color[c]))
+            return false;
+    return p.attenuation_distance > 0.f && std::isfinite(p.attenuation_distance) && unit(p.scatter_factor) &&
+           p.phase_g > -1.f && p.phase_g < 1.f && p.ior > 0.f && std::isfinite(p.ior) &&
+           p.emission_intensity >= 0.f && std::isfinite(p.emission_intensity);
+}
+
 #if defined(__CUDACC__)
 
 constexpr float PT_ONE_OVER_FOUR_PI = 0.07957747154594766788f;

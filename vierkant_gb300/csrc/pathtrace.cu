@@ -84,6 +84,9 @@ struct vkg_tracer
     vkg_ray *l_ray = nullptr;
     uint32_t *l_pid = nullptr;
     float4 *l_contrib = nullptr;
+    // medium table of renders with a camera medium: the scene's records + the camera's (last upload kept)
+    vkg::medium_rec *d_media_cam = nullptr;
+    std::vector<vkg::medium_rec> media_cam;
 };
 
 namespace vkg
@@ -92,6 +95,51 @@ vkg_status denoise_run(vkg_ctx *ctx, const vkg_pixel_data *px, uint32_t w, uint3
                        float *out_rgb, float *out_depth, cudaStream_t st);
 namespace
 {
+
+// the camera medium of PBRPathTracer.cpp:471-525: of the instances whose world box (the mesh's box
+// under the instance transform: an oriented box) contains the eye and whose material has a finite
+// attenuation distance, the one with the smallest box volume (the first on ties); single-level
+// scenes have no objects and start in vacuum
+uint32_t detect_camera_medium(const vkg_scene *sc, const float eye[3])
+{
+    uint32_t best = 0xFFFFFFFFu;
+    double best_volume = std::numeric_limits<double>::max();
+    if(!sc->tlas) return best;
+    for(const vkg_instance &in: sc->h_inst)
+    {
+        if(in.material >= sc->h_mats.size() || in.blas >= sc->blas.size()) continue;
+        if(!material_has_volume(sc->h_mats[in.material])) continue;
+        const vkg_bvh *b = sc->blas[in.blas];
+        const float *M = in.transform;
+        // object-space eye: solve A x = eye - t for the 3x3 part A (Cramer's rule in double)
+        const double a[9] = {M[0], M[1], M[2], M[4], M[5], M[6], M[8], M[9], M[10]};
+        const double r[3] = {eye[0] - (double)M[3], eye[1] - (double)M[7], eye[2] - (double)M[11]};
+        const double det = a[0] * (a[4] * a[8] - a[5] * a[7]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
+                           a[2] * (a[3] * a[7] - a[4] * a[6]);
+        if(!(std::fabs(det) > 0.0)) continue;
+        double x[3];
+        for(int k = 0; k < 3; ++k)
+        {
+            double c[9];
+            std::memcpy(c, a, sizeof(c));
+            for(int row = 0; row < 3; ++row) c[3 * row + k] = r[row];
+            x[k] = (c[0] * (c[4] * c[8] - c[5] * c[7]) - c[1] * (c[3] * c[8] - c[5] * c[6]) +
+                    c[2] * (c[3] * c[7] - c[4] * c[6])) / det;
+        }
+        bool inside = true;
+        double volume = 8.0;
+        for(int k = 0; k < 3; ++k)
+        {
+            inside = inside && x[k] >= b->scene_min[k] && x[k] <= b->scene_max[k];
+            const double col = std::sqrt(a[k] * a[k] + a[3 + k] * a[3 + k] + a[6 + k] * a[6 + k]);
+            volume *= 0.5 * ((double)b->scene_max[k] - b->scene_min[k]) * col;
+        }
+        if(!inside || volume >= best_volume) continue;
+        best_volume = volume;
+        best = in.material;
+    }
+    return best;
+}
 
 bool tl_persistent_selected()
 {
@@ -126,7 +174,8 @@ __global__ void k_check_instance_materials(const vkg_instance *__restrict__ inst
 
 // the material fields the BSDF divides by or takes as probabilities must be in range
 vkg_status check_material_values(vkg_ctx *ctx, const vkg_material *d_mats, uint32_t n, cudaStream_t st,
-                                 const char *fn, bool *any_transmissive, bool *any_full, medium_rec **d_media)
+                                 const char *fn, bool *any_transmissive, bool *any_full, medium_rec **d_media,
+                                 std::vector<medium_rec> *h_media, std::vector<vkg_material> *h_mats)
 {
     *any_transmissive = false;
     *any_full = false;
@@ -178,6 +227,8 @@ vkg_status check_material_values(vkg_ctx *ctx, const vkg_material *d_mats, uint3
         if(e == cudaSuccess) e = cudaStreamSynchronize(st);
         if(e != cudaSuccess) return cuda_check(ctx, e, fn);
     }
+    *h_media = std::move(media);
+    *h_mats = std::move(h);
     return VKG_OK;
 }
 
@@ -379,7 +430,8 @@ vkg_status vkg_scene_create(vkg_ctx *ctx, const vkg_scene_desc *d, vkg_scene **o
         return cuda_check(ctx, e, "vkg_scene_create");
     }
     if(vkg_status s = check_material_values(ctx, sc->mats, d->num_materials, st, "vkg_scene_create",
-                                                 &sc->any_transmissive, &sc->any_full, &sc->d_media);
+                                                 &sc->any_transmissive, &sc->any_full, &sc->d_media,
+                                                 &sc->h_media, &sc->h_mats);
        s != VKG_OK)
     {
         vkg_scene_destroy(ctx, sc);
@@ -508,7 +560,8 @@ vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_de
     chk(cudaMemcpyAsync(sc->mats, d->d_materials, d->num_materials * sizeof(vkg_material), cudaMemcpyDeviceToDevice, st));
     if(e != cudaSuccess) return fail(cuda_check(ctx, e, "vkg_scene_create_instanced"));
     if(vkg_status s = check_material_values(ctx, sc->mats, d->num_materials, st, "vkg_scene_create_instanced",
-                                                 &sc->any_transmissive, &sc->any_full, &sc->d_media);
+                                                 &sc->any_transmissive, &sc->any_full, &sc->d_media,
+                                                 &sc->h_media, &sc->h_mats);
        s != VKG_OK)
         return fail(s);
     std::vector<mesh_ref> refs(d->num_meshes);
@@ -567,6 +620,11 @@ vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_de
         chk(cudaStreamSynchronize(st));
         if(e != cudaSuccess) return fail(cuda_check(ctx, e, "vkg_scene_create_instanced"));
         if(hf[0]) return fail(set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_create_instanced: an instance material >= num_materials"));
+        sc->h_inst.resize(d->num_instances);
+        chk(cudaMemcpyAsync(sc->h_inst.data(), d->d_instances, d->num_instances * sizeof(vkg_instance),
+                            cudaMemcpyDeviceToHost, st));
+        chk(cudaStreamSynchronize(st));
+        if(e != cudaSuccess) return fail(cuda_check(ctx, e, "vkg_scene_create_instanced"));
         // rays enter and leave transmissive instances through back faces: their meshes are not culled
         for(uint32_t m = 0; m < d->num_meshes; ++m)
             if(hf[1 + m] && !d->meshes[m].twosided && d->meshes[m].num_tris)
@@ -633,6 +691,30 @@ vkg_status vkg_settings_default(vkg_settings *s)
     s->rr_start_depth = 0;
     s->denoising = 0;
     s->clip_near = 0.1f; // camera_params.hpp:37
+    s->camera_medium_mode = VKG_CAMERA_MEDIUM_DETECT;
+    vkg_medium_params_default(&s->camera_medium);
+    return VKG_OK;
+}
+
+vkg_status vkg_medium_params_default(vkg_medium_params *p)
+{
+    if(!p) return VKG_ERR_INVALID_ARGUMENT;
+    *p = vkg_medium_params{}; // media.hpp:26-49
+    for(int c = 0; c < 3; ++c)
+    {
+        p->attenuation_color[c] = 0.7f;
+        p->scatter_color[c] = 1.f;
+        p->emission_color[c] = 1.f;
+    }
+    p->attenuation_distance = 1.f;
+    p->ior = 1.f;
+    return VKG_OK;
+}
+
+vkg_status vkg_scene_camera_medium(const vkg_scene *scene, const float eye[3], uint32_t *material)
+{
+    if(!scene || !eye || !material) return VKG_ERR_INVALID_ARGUMENT;
+    *material = detect_camera_medium(scene, eye);
     return VKG_OK;
 }
 
@@ -730,10 +812,57 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
     P.num_lights = (uint32_t)lights.size();
     uint32_t *cnt_l = lights.empty() ? nullptr : t->counters + 7;
     const light_queue lq{t->l_ray, t->l_pid, t->l_contrib, cnt_l};
+    // the camera's medium (raypipeline.slang:128-135, PBRPathTracer.cpp:598-605): given, or the
+    // medium of the smallest volume instance around the eye; its record follows the scene's
+    uint32_t cam_mat = 0xFFFFFFFFu;
+    medium_rec cam_rec{};
+    if(S.camera_medium_mode == VKG_CAMERA_MEDIUM_GIVEN)
+    {
+        if(!medium_params_valid(S.camera_medium))
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
+                             "vkg_tracer_render: camera medium: attenuation colour in (0, 1], finite distance > 0, "
+                             "scatter factor / colour in [0, 1], phase g in (-1, 1), ior > 0, emission >= 0");
+        cam_rec = medium_from_params(S.camera_medium);
+        cam_mat = 0u;
+    }
+    else if(S.camera_medium_mode != VKG_CAMERA_MEDIUM_DETECT)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_tracer_render: unknown camera_medium_mode %u",
+                         S.camera_medium_mode);
+    else if((cam_mat = detect_camera_medium(sc, cam->eye)) != 0xFFFFFFFFu)
+    {
+        cam_rec = sc->h_media[cam_mat];
+        cam_rec.flags = MEDIUM_VOLUME; // keeps its own ior, also for a null-surface material
+    }
+    const bool cam_medium = cam_mat != 0xFFFFFFFFu;
+    const bool has_media = sc->d_media || cam_medium;
+    if(cam_medium)
+    {
+        const size_t n = sc->h_media.size();
+        std::vector<medium_rec> table(sc->h_media);
+        table.push_back(cam_rec);
+        const bool same = t->media_cam.size() == table.size() &&
+                          std::memcmp(t->media_cam.data(), table.data(), table.size() * sizeof(medium_rec)) == 0;
+        if(!same)
+        {
+            if(t->media_cam.size() < table.size())
+            {
+                cudaFree(t->d_media_cam);
+                t->d_media_cam = nullptr;
+                t->media_cam.clear();
+                VKG_TRY_CUDA(ctx, cudaMalloc(&t->d_media_cam, table.size() * sizeof(medium_rec)));
+            }
+            VKG_TRY_CUDA(ctx, cudaMemcpyAsync(t->d_media_cam, table.data(), table.size() * sizeof(medium_rec),
+                                              cudaMemcpyHostToDevice, st));
+            VKG_TRY_CUDA(ctx, cudaStreamSynchronize(st));
+            t->media_cam = std::move(table);
+        }
+        P.media = t->d_media_cam;
+        P.cam_medium = (uint32_t)n;
+    }
     // the shade variant: the full Disney model and the light terms, or metal-roughness only
-    const bool full = sc->any_full || !lights.empty() || sc->d_media;
+    const bool full = sc->any_full || !lights.empty() || has_media;
     P.gbuf = t->gbuf;
-    if(sc->d_media)
+    if(has_media)
     {
         if(ccfg) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_tracer_render: media with a radiance cache");
         if(t->mstack_cap < paths + train_paths)
@@ -754,7 +883,7 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
     uint32_t *cnt_q = t->counters + 3, *cnt_rec = t->counters + 4, *cnt_b = t->counters + 5, *cnt_work = t->counters + 6;
     // instanced scenes: grid-stride two-level tracers (faster on the stress scene: 274 vs 252 Mrays/s);
     // VKG_TL_KERNEL=persistent selects the refilling persistent ones
-    const bool tl_persistent = sc->tlas && tl_persistent_selected() && !sc->d_media;
+    const bool tl_persistent = sc->tlas && tl_persistent_selected() && !has_media;
     // a 64-entry traversal stack serves BVHs up to 10 levels deep (7 (depth - 1) + 1 entries)
     const bool small_stack = sc->bvh && sc->bvh->depth <= 10;
     uint32_t tl_grid = 0;
@@ -811,7 +940,7 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
                                                t->q_ray[1 - a],                                                          \
                                                t->q_pid[1 - a], cnt_out, t->s_ray, t->s_pid, t->s_contrib, cnt_s,         \
                                                t->rng, t->beta_pdf, t->radiance, io, lq)
-            if(mode == MODE_PLAIN && sc->d_media) VKG_SHADE(MODE_PLAIN, true, true);
+            if(mode == MODE_PLAIN && has_media) VKG_SHADE(MODE_PLAIN, true, true);
             else if(mode == MODE_PLAIN && full) VKG_SHADE(MODE_PLAIN, true, false);
             else if(mode == MODE_PLAIN) VKG_SHADE(MODE_PLAIN, false, false);
             else if(full) VKG_SHADE(MODE_CACHE, true, false);
@@ -942,7 +1071,8 @@ vkg_status vkg_tracer_destroy(vkg_tracer *t)
     tracer_free_buffers(t);
     tracer_free_cache_buffers(t);
     cudaFree(t->counters);
-    for(void *p: {(void *)t->d_lights, (void *)t->l_ray, (void *)t->l_pid, (void *)t->l_contrib, (void *)t->mstack})
+    for(void *p: {(void *)t->d_lights, (void *)t->l_ray, (void *)t->l_pid, (void *)t->l_contrib, (void *)t->mstack,
+                  (void *)t->d_media_cam})
         cudaFree(p);
     cudaFree(t->totals);
     if(t->ev0) cudaEventDestroy(t->ev0);

@@ -28,6 +28,7 @@ constexpr float PT_REGULARIZE_MIN_ROUGHNESS = 0.25f; // raypipeline.slang:25
 // path flag bits (stored in the .w word of the path's radiance record)
 constexpr uint32_t PATH_REGULARIZE = 1u; // a bounce with pdf < PT_REGULARIZE_PDF_THRESHOLD happened
 constexpr uint32_t PATH_CAUSTIC = 2u;    // the reference's caustic_path marker
+constexpr uint32_t PATH_NO_ENV_NEE = 4u; // the last vertex was a scattering event (no environment NEE there)
 
 struct env_alias
 {

@@ -47,6 +47,9 @@ struct vkg_scene
     bool any_transmissive = false;  // a material with transmission > 0 or a null surface (light shadow rays pass)
     bool any_full = false;          // a material with a lobe beyond metal-roughness
     vkg::medium_rec *d_media = nullptr; // per-material medium records, when a material bounds a medium
+    std::vector<vkg::medium_rec> h_media; // the same records for every material (host)
+    std::vector<vkg_material> h_mats;     // host copy of the materials
+    std::vector<vkg_instance> h_inst;     // host copy of the instances (instanced scenes)
     std::vector<vkg_light> lights;  // analytic lights (host copy; the tracer uploads them per render)
 };
 
@@ -95,6 +98,7 @@ struct pt_params
     // the per-path medium stacks
     const medium_rec *media;
     uint4 *mstack;
+    uint32_t cam_medium; // medium table index of the camera's medium (0xFFFFFFFF: vacuum)
 };
 
 // the shade kernel's two modes
@@ -205,7 +209,9 @@ __global__ void __launch_bounds__(PT_THREADS)
         rng[p] = g.state;
         beta_pdf[p] = make_float4(1.f, 1.f, 1.f, 0.f);
         radiance[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if(P.mstack) P.mstack[p] = make_uint4(0u, 0u, 0u, 0u); // the camera starts in vacuum
+        // the camera's medium seeds the stack (raypipeline.slang:128-135)
+        if(P.mstack)
+            P.mstack[p] = P.cam_medium != 0xFFFFFFFFu ? make_uint4(1u, P.cam_medium, 0u, 0u) : make_uint4(0u, 0u, 0u, 0u);
     }
     if(blockIdx.x == 0 && threadIdx.x == 0) counters[0] = n;
 }
@@ -394,27 +400,14 @@ __global__ void __launch_bounds__(PT_THREADS)
             }
             if(scattered)
             {
-                // a scattering event: NEE toward one light and the environment with the phase function
-                // (nee_volume, direct_lighting.slang:334-366), then a phase-function bounce
+                // a scattering event: NEE toward one light with the phase function (nee_volume,
+                // direct_lighting.slang:334-366), then a phase-function bounce. The environment gets no
+                // NEE sample here (as in the reference): a shadow ray would not see the medium's
+                // attenuation, so the environment is left to the phase-sampled path, whose miss then
+                // takes MIS weight 1 (PATH_NO_ENV_NEE)
                 P0 = f3(r0.x, r0.y, r0.z) + dir * t_end;
                 cull_back_shadow = true;
-                if(P.mis_mode != 2)
-                {
-                    float pdf_env;
-                    uint32_t texel;
-                    const float3 ld = env_sample(P.env, u[3], u[4], u[5], u[6], pdf_env, texel);
-                    if(pdf_env > 0.f)
-                    {
-                        const float ph = phase_hg(dot(dir, ld), scatter_g);
-                        const float w = P.mis_mode == 1 ? 1.f : power_heuristic(pdf_env, ph);
-                        contrib = beta * env_radiance(P.env, texel) * (w * ph / pdf_env);
-                        if(max3(contrib) > 0.f)
-                        {
-                            push_shadow = true;
-                            sdir = ld;
-                        }
-                    }
-                }
+                flags |= PATH_NO_ENV_NEE;
                 if(num_lights)
                 {
                     const uint32_t nl = num_lights;
@@ -490,7 +483,7 @@ __global__ void __launch_bounds__(PT_THREADS)
                 float3 le = env_radiance(P.env, t);
                 if(depth == 0 && !P.draw_skybox) le = f3(0.f, 0.f, 0.f);
                 float w = 1.f;
-                if(prev_pdf > 0.f)
+                if(prev_pdf > 0.f && !(flags & PATH_NO_ENV_NEE))
                 {
                     if(P.mis_mode == 1) w = 0.f;
                     else if(P.mis_mode == 0) w = power_heuristic(prev_pdf, env_pdf(P.env, dir, t));
@@ -651,7 +644,7 @@ __global__ void __launch_bounds__(PT_THREADS)
                     // regularisation on; the refractive-caustic marker follows the same test
                     const bool below = bs.pdf < PT_REGULARIZE_PDF_THRESHOLD;
                     const bool caustic = below && ((flags & PATH_CAUSTIC) || bs.transmission);
-                    flags = (flags | (below ? PATH_REGULARIZE : 0u)) & ~PATH_CAUSTIC;
+                    flags = (flags | (below ? PATH_REGULARIZE : 0u)) & ~(PATH_CAUSTIC | PATH_NO_ENV_NEE);
                     if(caustic) flags |= PATH_CAUSTIC;
                     const float cost = fabsf(dot(N, bs.dir));
                     float3 tp = bs.f * (cost / fmaxf(bs.pdf, PT_PDF_EPS));
@@ -1237,6 +1230,7 @@ inline pt_params make_params(const vkg_scene *sc, const vkg_camera &cam, const v
     P.gbuf = nullptr;
     P.media = sc->d_media;
     P.mstack = nullptr;
+    P.cam_medium = 0xFFFFFFFFu;
     P.last_sample = S.num_samples ? S.num_samples - 1 : 0u;
     P.clip_near = S.clip_near > 0.f ? S.clip_near : 0.1f;
     return P;

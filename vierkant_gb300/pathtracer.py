@@ -17,8 +17,8 @@ import math
 import numpy as np
 import torch
 
-from ._lib import (check, lib, vkg_bvh_info, vkg_camera, vkg_light, vkg_light_source, vkg_pixel_data,
-                   vkg_post_fx_settings, vkg_scene_desc, vkg_settings, vkg_tracer_create_info,
+from ._lib import (check, lib, vkg_bvh_info, vkg_camera, vkg_light, vkg_light_source, vkg_medium_params,
+                   vkg_pixel_data, vkg_post_fx_settings, vkg_scene_desc, vkg_settings, vkg_tracer_create_info,
                    vkg_tracer_stats)
 from .raytracing import Context
 
@@ -139,7 +139,31 @@ def post_fx(ctx: Context, hdr_rgba: torch.Tensor, settings: vkg_post_fx_settings
     return out
 
 
+CAMERA_MEDIUM_DETECT, CAMERA_MEDIUM_GIVEN = 0, 1
+
+
+def medium_params(**kw) -> vkg_medium_params:
+    """A vkg_medium_params with the reference's defaults (medium_params_t) and the given fields."""
+    p = vkg_medium_params()
+    check(lib().vkg_medium_params_default(C.byref(p)))
+    for k, v in kw.items():
+        f = getattr(p, k)
+        if isinstance(f, C.Array):
+            for i, x in enumerate(v):
+                f[i] = x
+        else:
+            setattr(p, k, v)
+    return p
+
+
 class _Lights:
+    def camera_medium(self, eye) -> int | None:
+        """The material of the medium a render from `eye` starts in (camera_medium_mode DETECT), or None."""
+        e = (C.c_float * 3)(*[float(x) for x in eye])
+        m = C.c_uint32()
+        check(lib().vkg_scene_camera_medium(self.handle, e, C.byref(m)))
+        return None if m.value == 0xFFFFFFFF else m.value
+
     def set_lights(self, lights):
         """Analytic lights of the scene (LIGHT_DTYPE records; empty removes them)."""
         arr = np.ascontiguousarray(np.asarray(lights, LIGHT_DTYPE).reshape(-1))
