@@ -407,10 +407,12 @@ def path_tracer_block(ctx, frames=256):
 
 def features_block(ctx):
     """The full material and light set: the Cornell box with the showcase materials (glass, rough
-    glass, clearcoat, sheen, diffuse transmission, metal-rough), one light of every analytic type and
-    a sun disc, against the same box with metal-rough materials and no lights, both at 1280x720 x 64
-    spp, 8 segments (samples/s, Mrays/s). Parity: the 16-sphere lit scene at 256x144 x 1024 spp
-    against its FP64 oracle (4096 spp full frame)."""
+    glass, clearcoat, sheen, diffuse transmission, iridescence, metal-rough), one light of every
+    analytic type and a sun disc, and the same box with its spheres cycled through homogeneous media
+    (fog, absorbing glass, emissive gas, scattering glass) and the same lights, against the box with
+    metal-rough materials and no lights, all at 1280x720 x 64 spp, 8 segments (samples/s, Mrays/s).
+    Parity: the 16-sphere lit scene and the 16-sphere media scene at 256x144 x 1024 spp against their
+    FP64 oracles (4096 spp full frame)."""
     import math
     import numpy as np
     import torch
@@ -436,7 +438,8 @@ def features_block(ctx):
     sc = geometry.cornell_scene(SEED, 2, 64, 16)
     cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, 1280, 720)
     for name, mats, lit in (("plain_720p_64spp_8seg", sc["materials"], False),
-                            ("materials_lights_720p_64spp_8seg", geometry.showcase_materials(sc["materials"]), True)):
+                            ("materials_lights_720p_64spp_8seg", geometry.showcase_materials(sc["materials"]), True),
+                            ("media_lights_720p_64spp_8seg", geometry.media_materials(sc["materials"]), True)):
         scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], mats, env)
         if lit:
             scene.set_lights(cornell_lights())
@@ -452,6 +455,8 @@ def features_block(ctx):
         scene.close()
     out["materials_lights_time_vs_plain"] = round(out["materials_lights_720p_64spp_8seg"]["ms"] /
                                                   out["plain_720p_64spp_8seg"]["ms"], 3)
+    out["media_lights_time_vs_plain"] = round(out["media_lights_720p_64spp_8seg"]["ms"] /
+                                              out["plain_720p_64spp_8seg"]["ms"], 3)
     g = np.load(ROOT / "tests" / "golden" / "pt_oracle_lights.npz")
     sc = geometry.cornell_scene(SEED, 2, int(g["num_spheres"]), 16)
     scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], geometry.showcase_materials(sc["materials"]),
@@ -465,6 +470,25 @@ def features_block(ctx):
     ref = g["mean"].astype(np.float64)
     rmse = math.sqrt(np.mean((_lum(img) - _lum(ref)) ** 2))
     out["lights_parity_256x144_1024spp"] = {
+        "rmse": round(rmse, 4), "bias": round(float((img.sum() - ref.sum()) / ref.sum()), 5),
+        "expected_noise": round(math.sqrt(np.mean(g["lum_var"]) / 1024 + np.mean(g["lum_var"]) / int(g["spp"])), 4),
+        "oracle": "FP64 %d spp, full frame" % int(g["spp"])}
+    # media: fog, absorbing glass, emissive gas and scattering glass spheres, the analytic lights, a
+    # constant 0.2 environment, 10 segments, against its FP64 oracle
+    g = np.load(ROOT / "tests" / "golden" / "pt_oracle_media.npz")
+    sc = geometry.cornell_scene(SEED, 2, int(g["num_spheres"]), 16)
+    env_m = torch.full((64, 128, 3), float(g["env"]), dtype=torch.float32, device="cuda")
+    scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], geometry.media_materials(sc["materials"]), env_m)
+    scene.set_lights(cornell_lights())
+    s = settings(1024, 256, 144, False)
+    s.max_trace_depth = int(g["max_depth"])
+    pt = PBRPathTracer(ctx, seed=SEED, settings=s)
+    img = pt.render_scene(scene, cam).cpu().numpy().astype(np.float64)
+    pt.close()
+    scene.close()
+    ref = g["mean"].astype(np.float64)
+    rmse = math.sqrt(np.mean((_lum(img) - _lum(ref)) ** 2))
+    out["media_parity_256x144_1024spp"] = {
         "rmse": round(rmse, 4), "bias": round(float((img.sum() - ref.sum()) / ref.sum()), 5),
         "expected_noise": round(math.sqrt(np.mean(g["lum_var"]) / 1024 + np.mean(g["lum_var"]) / int(g["spp"])), 4),
         "oracle": "FP64 %d spp, full frame" % int(g["spp"])}
@@ -683,6 +707,17 @@ def profile_case(name: str):
         s.sun_intensity, s.sun_angular_size = 3.0, 0.05
         s.sun_spherical_coords[0], s.sun_spherical_coords[1] = math.radians(30), math.radians(200)
         PBRPathTracer(ctx, seed=SEED, settings=s).render_scene(scene, cam)
+    elif name == "media":
+        from vierkant_gb300.pathtracer import cornell_lights
+        sc = geometry.cornell_scene(SEED, 2, 64, 16)
+        envc = torch.full((64, 128, 3), 0.1, dtype=torch.float32, device="cuda")
+        scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], geometry.media_materials(sc["materials"]),
+                      envc)
+        scene.set_lights(cornell_lights())
+        cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, 1280, 720)
+        s = PBRPathTracer.default_settings()
+        s.num_samples, s.max_trace_depth, s.rr_start_depth = 4, 8, 3
+        PBRPathTracer(ctx, seed=SEED, settings=s).render_scene(scene, cam)
     else:
         raise SystemExit(f"unknown profile case {name}")
     torch.cuda.synchronize()
@@ -774,7 +809,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-pt", action="store_true", help="skip the path-tracer / radiance-cache block")
     ap.add_argument("--nrc-frames", type=int, default=256)
-    ap.add_argument("--profile-case", choices=["pt-frame", "nrc", "batch", "stress", "features"], default=None,
+    ap.add_argument("--profile-case", choices=["pt-frame", "nrc", "batch", "stress", "features", "media"], default=None,
                     help="run one small workload for a profiler capture and exit (no JSON line)")
     args = ap.parse_args()
     if args.profile_case:

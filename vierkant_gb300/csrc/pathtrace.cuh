@@ -258,23 +258,55 @@ __device__ __forceinline__ float3 xyz_to_rec709(float x, float y, float z)
     return f3(x * 3.2404542f + y * -1.5371385f + z * -0.4985314f, x * -0.9692660f + y * 1.8760108f + z * 0.0415560f,
               x * 0.0556434f + y * -0.2040259f + z * 1.0572252f);
 }
-// evalSensitivity: the Fourier transform of the CIE colour matching functions as Gaussians
-__device__ __forceinline__ float3 eval_sensitivity(float opd, float3 shift)
+// evalSensitivity (utils/bsdf.slang:83-100): the Fourier transform of the CIE colour matching
+// functions as Gaussians, val * sqrt(2 pi var) * cos(pos * phase + shift) * exp(-phase^2 var) per
+// component (two Gaussians for X). Kept as its cosines c and Gaussians e so that the term of twice the
+// optical path difference and phase shift follows without further transcendentals.
+struct sensitivity_terms
+{
+    float c[4], e[4]; // X, Y, Z, second X Gaussian
+};
+__device__ __forceinline__ sensitivity_terms sensitivity_cos_exp(float opd, float3 shift)
 {
     const float phase = 2.f * PT_PI * opd * 1.0e-9f, phase2 = phase * phase;
+    sensitivity_terms t;
+    t.c[0] = cosf(1.6810e+06f * phase + shift.x);
+    t.c[1] = cosf(1.7953e+06f * phase + shift.y);
+    t.c[2] = cosf(2.2084e+06f * phase + shift.z);
+    t.c[3] = cosf(2.2399e+06f * phase + shift.x);
+    t.e[0] = expf(-phase2 * 4.3278e+09f);
+    t.e[1] = expf(-phase2 * 9.3046e+09f);
+    t.e[2] = expf(-phase2 * 6.6121e+09f);
+    t.e[3] = expf(-phase2 * 4.5282e+09f);
+    return t;
+}
+// the terms at twice the path difference and phase shift
+__device__ __forceinline__ sensitivity_terms sensitivity_double(const sensitivity_terms &t)
+{
+    sensitivity_terms d;
+    for(int k = 0; k < 4; ++k)
+    {
+        d.c[k] = 2.f * t.c[k] * t.c[k] - 1.f;
+        const float e2 = t.e[k] * t.e[k];
+        d.e[k] = e2 * e2;
+    }
+    return d;
+}
+__device__ __forceinline__ float3 sensitivity_rgb(const sensitivity_terms &t)
+{
     const float vx = 5.4856e-13f, vy = 4.4201e-13f, vz = 5.2481e-13f;
-    const float px = 1.6810e+06f, py = 1.7953e+06f, pz = 2.2084e+06f;
     const float sx = 4.3278e+09f, sy = 9.3046e+09f, sz = 6.6121e+09f;
-    float x = vx * sqrtf(2.f * PT_PI * sx) * cosf(px * phase + shift.x) * expf(-phase2 * sx);
-    float y = vy * sqrtf(2.f * PT_PI * sy) * cosf(py * phase + shift.y) * expf(-phase2 * sy);
-    float z = vz * sqrtf(2.f * PT_PI * sz) * cosf(pz * phase + shift.z) * expf(-phase2 * sz);
-    x += 9.7470e-14f * sqrtf(2.f * PT_PI * 4.5282e+09f) * cosf(2.2399e+06f * phase + shift.x) *
-         expf(-4.5282e+09f * phase2);
+    float x = vx * sqrtf(2.f * PT_PI * sx) * t.c[0] * t.e[0];
+    float y = vy * sqrtf(2.f * PT_PI * sy) * t.c[1] * t.e[1];
+    float z = vz * sqrtf(2.f * PT_PI * sz) * t.c[2] * t.e[2];
+    x += 9.7470e-14f * sqrtf(2.f * PT_PI * 4.5282e+09f) * t.c[3] * t.e[3];
     const float inv = 1.f / 1.0685e-7f;
     return xyz_to_rec709(x * inv, y * inv, z * inv);
 }
-// Fresnel of a thin film of ior `film` over a base of reflectance f0, seen from outside ior `outside`
-__device__ __forceinline__ float3 iridescent_fresnel(float outside, float film, float3 f0, float thickness, float cos1)
+// Fresnel of a thin film of ior `film` over a base of reflectance f0, seen from outside ior `outside`.
+// Not inlined: its eight cosines and exponentials would otherwise be copied into every lobe evaluation
+// of every caller, and the shade kernel's code then outgrows the instruction cache
+static __device__ __noinline__ float3 iridescent_fresnel(float outside, float film, float3 f0, float thickness, float cos1)
 {
     const float R0 = ior_to_f0(film, outside);
     const float R12 = f_schlick(cos1, R0);
@@ -302,12 +334,14 @@ __device__ __forceinline__ float3 iridescent_fresnel(float outside, float film, 
                          T121 * T121 * R23.z / (1.f - R123.z));
     float3 I = f3(R12, R12, R12) + Rs;
     float3 Cm = Rs - f3(T121, T121, T121);
-    for(int k = 1; k <= 2; ++k)
-    {
-        Cm = Cm * r123;
-        const float3 Sm = eval_sensitivity((float)k * opd, phi * (float)k) * 2.f;
-        I = I + Cm * Sm;
-    }
+    // the two terms m = 1, 2 of the reference's loop: the m = 2 term's cosines and Gaussians follow from
+    // the m = 1 term's (cos 2a = 2 cos^2 a - 1, exp(-4 p^2 s) = exp(-p^2 s)^4), halving the
+    // transcendental calls
+    const sensitivity_terms t1 = sensitivity_cos_exp(opd, phi);
+    Cm = Cm * r123;
+    I = I + Cm * (sensitivity_rgb(t1) * 2.f);
+    Cm = Cm * r123;
+    I = I + Cm * (sensitivity_rgb(sensitivity_double(t1)) * 2.f);
     return f3(fmaxf(I.x, 0.f), fmaxf(I.y, 0.f), fmaxf(I.z, 0.f));
 }
 
@@ -390,13 +424,15 @@ __device__ __forceinline__ float3 eval_dielectric_refraction(float alpha, float3
 
 // EvalSpecularIridescence (bsdf_disney.slang:112-127)
 __device__ __forceinline__ float3 eval_specular_iridescence(float alpha, float film_ior, float thickness, float3 cspec0,
-                                                            float3 V, float3 N, float3 L, float3 H, float &pdf)
+                                                            float3 V, float3 N, float3 L, float3 H, float &pdf,
+                                                            bool with_value = true)
 {
     pdf = 0.f;
     if(dot(N, L) <= 0.f) return f3(0.f, 0.f, 0.f);
     float d = gtr2(dot(N, H), alpha);
     float sv = smith_ggx(fabsf(dot(N, V)), alpha);
     pdf = 0.5f * d * sv;
+    if(!with_value) return f3(0.f, 0.f, 0.f);
     const float3 F = iridescent_fresnel(1.f, film_ior, cspec0, thickness, dot(V, H));
     float g = smith_ggx(fabsf(dot(N, L)), alpha) * sv;
     return F * (d * g);
@@ -406,7 +442,7 @@ __device__ __forceinline__ float3 eval_specular_iridescence(float alpha, float f
 __device__ __forceinline__ float3 eval_dielectric_reflection_iridescence(float alpha, float3 color, float film_ior,
                                                                          float thickness, float3 cspec0, float eta,
                                                                          float3 V, float3 N, float3 L, float3 H,
-                                                                         float &pdf)
+                                                                         float &pdf, bool with_value = true)
 {
     pdf = 0.f;
     if(dot(N, L) <= 0.f) return f3(0.f, 0.f, 0.f);
@@ -415,6 +451,7 @@ __device__ __forceinline__ float3 eval_dielectric_reflection_iridescence(float a
     float d = gtr2(dot(N, H), alpha);
     float sv = smith_ggx(fabsf(dot(N, V)), alpha);
     pdf = 0.5f * d * sv * F;
+    if(!with_value) return f3(0.f, 0.f, 0.f);
     float g = smith_ggx(fabsf(dot(N, L)), alpha) * sv;
     const float3 irF = iridescent_fresnel(1.f, film_ior, cspec0, thickness, voh);
     return color * irF * (d * g);
@@ -548,6 +585,9 @@ __device__ __forceinline__ bsdf_sample sample_bsdf(const material_view &m, float
 
 // eval_disney (bsdf_disney.slang:298-381): value and mixture pdf (the sum over lobes). The clearcoat
 // lobe is skipped when clearcoat == 0, where its value and pdf weight are 0.
+// VALUE = false: the mixture pdf only (the thin-film Fresnel is skipped; every other value term is
+// dead code the compiler removes)
+template<bool VALUE = true>
 __device__ __forceinline__ float3 eval_bsdf(const material_view &m, float3 L, float3 N, float3 V, float eta, float &pdf)
 {
     pdf = 0.f;
@@ -576,7 +616,7 @@ __device__ __forceinline__ float3 eval_bsdf(const material_view &m, float3 L, fl
                 bsdf = bsdf * (1.f - s_ir);
                 bsdf_pdf *= 1.f - s_ir;
                 const float3 b2 = eval_dielectric_reflection_iridescence(alpha, m.base, m.iri_ior, m.iri_thickness,
-                                                                         spec, eta, V, N, L, H, mp);
+                                                                         spec, eta, V, N, L, H, mp, VALUE);
                 bsdf = bsdf + b2 * s_ir;
                 bsdf_pdf += mp * s_ir;
             }
@@ -597,7 +637,7 @@ __device__ __forceinline__ float3 eval_bsdf(const material_view &m, float3 L, fl
         {
             brdf = brdf + eval_specular(alpha, spec, V, N, L, H, mp) * (1.f - s_ir);
             brdf_pdf += mp * primary * (1.f - diffuse_ratio) * (1.f - s_ir);
-            brdf = brdf + eval_specular_iridescence(alpha, m.iri_ior, m.iri_thickness, spec, V, N, L, H, mp) * s_ir;
+            brdf = brdf + eval_specular_iridescence(alpha, m.iri_ior, m.iri_thickness, spec, V, N, L, H, mp, VALUE) * s_ir;
             brdf_pdf += mp * primary * (1.f - diffuse_ratio) * s_ir;
         }
         else
@@ -616,6 +656,22 @@ __device__ __forceinline__ float3 eval_bsdf(const material_view &m, float3 L, fl
     if(!(p > 0.f)) return f3(0.f, 0.f, 0.f);
     pdf = p;
     return lerp3(brdf, bsdf, trans_weight);
+}
+
+// eval_bsdf as one out-of-line copy: the full-material shade kernel evaluates the BSDF at three places
+// (environment NEE, light NEE, the MIS pdf of the bounce), and three inlined copies of every lobe
+// overflow the instruction cache
+static __device__ __noinline__ float3 eval_bsdf_ool(material_view m, float3 L, float3 N, float3 V, float eta,
+                                                    float &pdf)
+{
+    return eval_bsdf(m, L, N, V, eta, pdf);
+}
+// the mixture pdf alone (the MIS pdf of a bounce), out of line for the same reason
+static __device__ __noinline__ float pdf_bsdf_ool(material_view m, float3 L, float3 N, float3 V, float eta)
+{
+    float pdf;
+    eval_bsdf<false>(m, L, N, V, eta, pdf);
+    return pdf;
 }
 
 // the material record as the BSDF reads it; FULL = false reads only the metal-roughness fields and

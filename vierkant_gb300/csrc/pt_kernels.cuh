@@ -599,7 +599,7 @@ __global__ void __launch_bounds__(PT_THREADS)
                     if(pdf_env > 0.f && cosl > 0.f)
                     {
                         float pdf_b;
-                        const float3 f = eval_bsdf(m, ld, N, V, eta, pdf_b);
+                        const float3 f = FULL ? eval_bsdf_ool(m, ld, N, V, eta, pdf_b) : eval_bsdf(m, ld, N, V, eta, pdf_b);
                         if(pdf_b > 0.f)
                         {
                             const float w = P.mis_mode == 1 ? 1.f : power_heuristic(pdf_env, pdf_b);
@@ -624,7 +624,7 @@ __global__ void __launch_bounds__(PT_THREADS)
                     {
                         const float cosl = fmaxf(dot(N, ls.dir), 0.f);
                         float pdf_b = 0.f;
-                        const float3 f = eval_bsdf(m, ls.dir, N, V, eta, pdf_b);
+                        const float3 f = FULL ? eval_bsdf_ool(m, ls.dir, N, V, eta, pdf_b) : eval_bsdf(m, ls.dir, N, V, eta, pdf_b);
                         const float w = bsdf_reachable(l) ? mis_weight_nee(P.mis_mode, ls.pdf / (float)nl, pdf_b) : 1.f;
                         lcontrib = beta * f * ls.radiance * (w * (float)nl * cosl / ls.pdf);
                         if(max3(lcontrib) > 0.f)
@@ -654,7 +654,11 @@ __global__ void __launch_bounds__(PT_THREADS)
                     // MIS pdf of the bounce for an environment hit: the mixture pdf where the
                     // environment sampler competes (directions above the surface), 0 below it
                     float pdf_mix = 0.f;
-                    if(dot(N, bs.dir) > 0.f) eval_bsdf(m, bs.dir, N, V, eta, pdf_mix);
+                    if(dot(N, bs.dir) > 0.f)
+                    {
+                        if constexpr(FULL) pdf_mix = pdf_bsdf_ool(m, bs.dir, N, V, eta);
+                        else eval_bsdf<false>(m, bs.dir, N, V, eta, pdf_mix);
+                    }
                     prev_pdf = pdf_mix;
                     // Russian roulette
                     if(P.rr_depth == 0)
