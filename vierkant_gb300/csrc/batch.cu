@@ -337,12 +337,12 @@ vkg_status enqueue(vkg_batch *b, const std::vector<vkg_batch::wave> &waves, cuda
                                                                              b->q_pid[1 - a], cnt_out, b->s_ray,
                                                                              b->s_pid, b->s_contrib, cnt_s, b->rng,
                                                                              b->beta_pdf, b->radiance, io,
-                                                                             light_queue{});
+                                                                             light_queue{}, nullptr);
             else
             k_pt_shade<MODE_PLAIN, job_table, false><<<grid, bs, 0, st>>>(J, depth, b->q_ray[a], b->q_pid[a], b->hits, b->hit_inst, cnt_in,
                                                        b->q_ray[1 - a], b->q_pid[1 - a], cnt_out, b->s_ray, b->s_pid,
                                                        b->s_contrib, cnt_s, b->rng, b->beta_pdf, b->radiance, io,
-                                                       light_queue{});
+                                                       light_queue{}, nullptr);
             if(T.extend_kernel == 2)
             {
                 VKG_TRY_CUDA(ctx, cudaMemsetAsync(b->counters + 3, 0, sizeof(uint32_t), st));

@@ -58,6 +58,8 @@ struct vkg_tracer
     float *sum = nullptr;
     float *accum = nullptr;
     vkg_pixel_data *gbuf = nullptr; // pixel records of the traced window
+    uint32_t *order = nullptr;      // queue slots grouped by material class (full material set)
+    uint32_t *bins = nullptr;       // class counts [0..7] and fill cursors [8..15]
     uint4 *mstack = nullptr;        // per-path medium stacks (scenes with media)
     size_t mstack_cap = 0;
     uint32_t *counters = nullptr;           // [0..1] queue lengths, [2] shadow queue length, [3] cache queries,
@@ -139,6 +141,18 @@ uint32_t detect_camera_medium(const vkg_scene *sc, const float eye[3])
         best = in.material;
     }
     return best;
+}
+
+// shading-coherence binning of the full material set (on unless VKG_PT_BINNING=0)
+bool pt_binning_selected()
+{
+    static int v = -1;
+    if(v < 0)
+    {
+        const char *s = std::getenv("VKG_PT_BINNING");
+        v = (s && std::strcmp(s, "0") == 0) ? 0 : 1;
+    }
+    return v == 1;
 }
 
 bool tl_persistent_selected()
@@ -237,8 +251,10 @@ void tracer_free_buffers(vkg_tracer *t)
     for(void *p: {(void *)t->q_ray[0], (void *)t->q_ray[1], (void *)t->q_pid[0], (void *)t->q_pid[1], (void *)t->hits,
                   (void *)t->hit_inst,
                   (void *)t->s_ray, (void *)t->s_pid, (void *)t->s_contrib, (void *)t->rng, (void *)t->beta_pdf,
-                  (void *)t->radiance, (void *)t->sum, (void *)t->accum, (void *)t->gbuf})
+                  (void *)t->radiance, (void *)t->sum, (void *)t->accum, (void *)t->gbuf, (void *)t->order,
+                  (void *)t->bins})
         cudaFree(p);
+    t->order = t->bins = nullptr;
     t->q_ray[0] = t->q_ray[1] = nullptr;
     t->q_pid[0] = t->q_pid[1] = nullptr;
     t->hits = nullptr;
@@ -324,6 +340,8 @@ vkg_status tracer_ensure(vkg_tracer *t, size_t paths, size_t npix)
     al((void **)&t->sum, npix * 3 * sizeof(float));
     al((void **)&t->accum, npix * 3 * sizeof(float));
     al((void **)&t->gbuf, npix * sizeof(vkg_pixel_data));
+    al((void **)&t->order, paths * sizeof(uint32_t));
+    al((void **)&t->bins, 2 * PT_BIN_CLASSES * sizeof(uint32_t));
     if(e != cudaSuccess)
     {
         tracer_free_buffers(t);
@@ -884,6 +902,7 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
     // instanced scenes: grid-stride two-level tracers (faster on the stress scene: 274 vs 252 Mrays/s);
     // VKG_TL_KERNEL=persistent selects the refilling persistent ones
     const bool tl_persistent = sc->tlas && tl_persistent_selected() && !has_media;
+    const bool bin_materials = pt_binning_selected();
     // a 64-entry traversal stack serves BVHs up to 10 levels deep (7 (depth - 1) + 1 entries)
     const bool small_stack = sc->bvh && sc->bvh->depth <= 10;
     uint32_t tl_grid = 0;
@@ -935,11 +954,22 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_out, 0, sizeof(uint32_t), st));
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_s, 0, sizeof(uint32_t), st));
             if(cnt_l) VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_l, 0, sizeof(uint32_t), st));
+            // the full material set: group the queue by material class first, so that warps shade
+            // coherently (k_pt_bin_count / k_pt_bin_scatter, two light passes over the hits)
+            const uint32_t *order = nullptr;
+            if(full && bin_materials)
+            {
+                VKG_TRY_CUDA(ctx, cudaMemsetAsync(t->bins, 0, 2 * PT_BIN_CLASSES * sizeof(uint32_t), st));
+                k_pt_bin_count<<<grid, PT_THREADS, 0, st>>>(SS, t->q_pid[a], t->hits, t->hit_inst, cnt_in, t->bins);
+                k_pt_bin_scatter<<<grid, PT_THREADS, 0, st>>>(SS, t->q_pid[a], t->hits, t->hit_inst, cnt_in, t->bins,
+                                                              t->order);
+                order = t->order;
+            }
 #define VKG_SHADE(M, F, MD)                                                                                            \
     k_pt_shade<M, single_scene, F, MD><<<grid, PT_THREADS, 0, st>>>(SS, depth, t->q_ray[a], t->q_pid[a], t->hits, t->hit_inst, cnt_in,        \
                                                t->q_ray[1 - a],                                                          \
                                                t->q_pid[1 - a], cnt_out, t->s_ray, t->s_pid, t->s_contrib, cnt_s,         \
-                                               t->rng, t->beta_pdf, t->radiance, io, lq)
+                                               t->rng, t->beta_pdf, t->radiance, io, lq, order)
             if(mode == MODE_PLAIN && has_media) VKG_SHADE(MODE_PLAIN, true, true);
             else if(mode == MODE_PLAIN && full) VKG_SHADE(MODE_PLAIN, true, false);
             else if(mode == MODE_PLAIN) VKG_SHADE(MODE_PLAIN, false, false);

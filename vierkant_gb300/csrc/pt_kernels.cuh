@@ -290,6 +290,84 @@ __device__ __forceinline__ void hit_surface(const pt_params &P, uint32_t prim, u
 
 // FULL = false: a scene without lights whose materials are metal-roughness only; the light terms and
 // the other lobes compile away. MEDIA = true (with FULL): the homogeneous-media terms
+// material classes of a queue entry for shading coherence: 0 miss, then by the costliest lobe the
+// material takes (thin film, dielectric, medium boundary / null surface, clearcoat, sheen, diffuse
+// transmission, metal-roughness only)
+constexpr uint32_t PT_BIN_CLASSES = 8;
+__device__ __forceinline__ uint32_t material_class(const vkg_material &m)
+{
+    if(m.iridescence > 0.f) return 1;
+    if(m.transmission > 0.f) return 2;
+    if(m.null_surface || (m.attenuation_distance > 0.f && m.attenuation_distance < 3.0e38f)) return 3;
+    if(m.clearcoat > 0.f) return 4;
+    if(m.sheen_color[0] > 0.f || m.sheen_color[1] > 0.f || m.sheen_color[2] > 0.f) return 5;
+    if(m.diffuse_transmission > 0.f) return 6;
+    return 7;
+}
+template<class J>
+__device__ __forceinline__ uint32_t entry_class(const J &S, const uint32_t *__restrict__ in_pid,
+                                                const vkg_hit *__restrict__ hits, const uint32_t *__restrict__ hit_inst,
+                                                uint32_t i)
+{
+    const uint32_t prim = __ldg(&hits[i].prim);
+    if(prim == VKG_MISS) return 0;
+    const pt_params &P = S.params(__ldg(&in_pid[i]));
+    const uint32_t mat = P.two_level ? __ldg(&P.tl_by_id[__ldg(&hit_inst[i])].material) : __ldg(&P.tri_mat[prim]);
+    return material_class(P.mats[mat]);
+}
+// counts per class of the queue (bins[0..7]; zero at launch)
+template<class J>
+__global__ void __launch_bounds__(PT_THREADS)
+        k_pt_bin_count(J S, const uint32_t *__restrict__ in_pid, const vkg_hit *__restrict__ hits,
+                       const uint32_t *__restrict__ hit_inst, const uint32_t *__restrict__ in_count,
+                       uint32_t *__restrict__ bins)
+{
+    __shared__ uint32_t h[PT_BIN_CLASSES];
+    if(threadIdx.x < PT_BIN_CLASSES) h[threadIdx.x] = 0u;
+    __syncthreads();
+    const uint32_t n = *in_count;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(&h[entry_class(S, in_pid, hits, hit_inst, i)], 1u);
+    __syncthreads();
+    if(threadIdx.x < PT_BIN_CLASSES && h[threadIdx.x]) atomicAdd(&bins[threadIdx.x], h[threadIdx.x]);
+}
+// order[k] = queue entry of the k-th slot, classes in ascending order (bins[8..15] are the classes'
+// fill cursors, zero at launch); within a class the order is arbitrary — each path's result does not
+// depend on its slot
+template<class J>
+__global__ void __launch_bounds__(PT_THREADS)
+        k_pt_bin_scatter(J S, const uint32_t *__restrict__ in_pid, const vkg_hit *__restrict__ hits,
+                         const uint32_t *__restrict__ hit_inst, const uint32_t *__restrict__ in_count,
+                         uint32_t *__restrict__ bins, uint32_t *__restrict__ order)
+{
+    __shared__ uint32_t start[PT_BIN_CLASSES];
+    if(threadIdx.x == 0)
+    {
+        uint32_t acc = 0;
+        for(uint32_t c = 0; c < PT_BIN_CLASSES; ++c)
+        {
+            start[c] = acc;
+            acc += bins[c];
+        }
+    }
+    __syncthreads();
+    const uint32_t n = *in_count;
+    const uint32_t lane = threadIdx.x & 31u;
+    for(uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x)
+    {
+        const uint32_t i = base + threadIdx.x;
+        const bool active = i < n;
+        const uint32_t c = active ? entry_class(S, in_pid, hits, hit_inst, i) : PT_BIN_CLASSES;
+        // one atomic per class present in the warp
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, c);
+        const uint32_t leader = __ffs(peers) - 1u;
+        uint32_t pos = 0;
+        if(active && lane == leader) pos = atomicAdd(&bins[PT_BIN_CLASSES + c], (uint32_t)__popc(peers));
+        pos = __shfl_sync(0xFFFFFFFFu, pos, (int)leader);
+        if(active) order[start[c] + pos + (uint32_t)__popc(peers & ((1u << lane) - 1u))] = i;
+    }
+}
+
 template<int MODE, class J, bool FULL = true, bool MEDIA = false>
 __global__ void __launch_bounds__(PT_THREADS)
         k_pt_shade(J S, uint32_t depth, const vkg_ray *__restrict__ in_ray,
@@ -299,14 +377,17 @@ __global__ void __launch_bounds__(PT_THREADS)
                    uint32_t *__restrict__ out_pid, uint32_t *__restrict__ out_count, vkg_ray *__restrict__ s_ray,
                    uint32_t *__restrict__ s_pid, float4 *__restrict__ s_contrib, uint32_t *__restrict__ s_count,
                    uint64_t *__restrict__ rng, float4 *__restrict__ beta_pdf, float4 *__restrict__ radiance,
-                   cache_io io, light_queue lq)
+                   cache_io io, light_queue lq, const uint32_t *__restrict__ order)
 {
     const uint32_t n = *in_count;
     const uint32_t stride = gridDim.x * blockDim.x;
     for(uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride)
     {
-        const uint32_t i = base + threadIdx.x;
-        const bool active = i < n;
+        // order (may be null): queue entries grouped by material class, so that a warp's lanes take
+        // the same lobes (k_pt_bin_count / k_pt_bin_scatter)
+        const uint32_t j = base + threadIdx.x;
+        const bool active = j < n;
+        const uint32_t i = active && order ? __ldg(&order[j]) : j;
         bool push_ext = false, push_shadow = false, push_query = false, push_light = false;
         bool cull_back_shadow = false; // shadow rays from inside a medium leave it through back faces
         float3 P0 = f3(0.f, 0.f, 0.f), ndir = P0, sdir = P0, N = P0;
