@@ -294,3 +294,44 @@ def test_camera_medium_validated(ctx):
         pt.render_scene(scene, cam)
     pt.close()
     scene.close()
+
+
+def test_instanced_media_against_fp64_oracle(ctx):
+    """the media showcase as a two-level scene (one identity instance per wall quad and sphere, its
+    material per instance) against the instanced FP64 oracle on a crop: media, null surfaces and the
+    media stack through the two-level traversal (light shadow rays of instanced scenes tint through
+    glass without optical depth, in both)"""
+    from scene_helpers import split_cornell
+    from vierkant_gb300.pathtracer import InstancedScene
+    sc = geometry.cornell_scene(0x5EED, 2, NUM_SPHERES, 16)
+    sc["materials"] = geometry.media_materials(sc["materials"])
+    meshes, inst = split_cornell(sc)
+    env = torch.full((64, 128, 3), ENV, dtype=torch.float32, device="cuda")
+    scene = InstancedScene(ctx, meshes, inst, sc["materials"], env)
+    scene.set_lights(cornell_lights())
+    cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, W, HT)
+    crop = (96, 40, 64, 64)
+    s = settings(256)
+    for k in range(4):
+        s.crop[k] = crop[k]
+    pt = PBRPathTracer(ctx, seed=0x5EED, settings=s)
+    for _ in range(4):
+        img = pt.render_scene(scene, cam)
+    img = img.cpu().numpy().astype(np.float64)
+    pt.close()
+    scene.close()
+    th = float(np.float32(math.tan(math.radians(45.0) / 2.0)))
+    ocam = oracle.camera((0, 0, 3.4), (0, 0, 0), (0, 1, 0), th, W, HT)
+    spp = 256
+    ref, sq, _ = oracle.pt_render_instanced(meshes, inst["transform"], inst["blas"], inst["material"],
+                                            sc["materials"], env.cpu().numpy(), ocam, spp, seed=77,
+                                            max_depth=MAX_DEPTH, rr_depth=3, crop=crop,
+                                            lights=cornell_lights().astype(oracle.LIGHT_DTYPE))
+    lum = lambda a: 0.2126 * a[..., 0] + 0.7152 * a[..., 1] + 0.0722 * a[..., 2]
+    var = np.maximum(sq - lum(ref) ** 2, 0.0)
+    rmse = math.sqrt(np.mean((lum(img) - lum(ref)) ** 2))
+    expected = math.sqrt(np.mean(var) / spp + np.mean(var) / 1024)
+    bias = (img.sum() - ref.sum()) / ref.sum()
+    print(f"instanced media vs FP64 oracle: bias {bias:+.4f} rmse {rmse:.4f} expected noise {expected:.4f}")
+    assert rmse < 2.0 * expected, (rmse, expected)
+    assert abs(bias) < 0.03, bias
