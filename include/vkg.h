@@ -514,6 +514,32 @@ vkg_status vkg_gltf_materials(const vkg_gltf *g, vkg_material *out);
 vkg_status vkg_gltf_lights(const vkg_gltf *g, vkg_light *out);
 vkg_status vkg_gltf_destroy(vkg_gltf *g);
 
+/* ---- RayBuilder wire records (host only) ----------------------------------------------------
+ * The byte images RayBuilder uploads for its ray pipeline, read as they are: the C++ layouts of
+ * RayBuilder::material_struct_t (RayBuilder.hpp:40-116) and RayBuilder::entry_t (RayBuilder.hpp:24-37)
+ * with glm's default packing, which equal their shader twins' std430 layouts (ray/types.slang:17-32,
+ * :64-110; the shader pads both to a multiple of 16 bytes). */
+#define VKG_WIRE_MATERIAL_BYTES 208u
+#define VKG_WIRE_ENTRY_BYTES 192u
+/* material_struct_t -> vkg_material: colour rgb, emission rgb x emission.a (the emissive strength, as
+   the closest-hit shader multiplies them), the scalar lobes, sheen colour rgb, iridescence strength /
+   ior and the thickness range's maximum (what the shader reads), the media fields and two_sided.
+   Texture indices, blend mode, alpha cutoff and dispersion have no counterpart and are dropped;
+   *dropped (may be NULL) counts the records that use any of them. */
+vkg_status vkg_materials_from_wire(const void *records, uint32_t n, vkg_material *out, uint32_t *dropped);
+/* per entry: where its triangles are in the mesh buffers */
+typedef struct vkg_wire_entry_info
+{
+    uint32_t buffer_index;  /* the mesh (vertex / index buffer pair) */
+    uint32_t base_index;    /* first index of the entry in the index buffer */
+    int32_t vertex_offset;  /* added to every index */
+    float aabb_min[3], aabb_max[3]; /* object-space box */
+} vkg_wire_entry_info;
+/* entry_t -> vkg_instance: object -> world = T R S of the entry's transform_t (translation, rotation
+   quaternion stored x y z w, scale; the shader's apply_transform, utils/transform.slang:19-24) as a
+   row-major 3x4, blas = buffer_index, material = material_index. info (may be NULL): n records. */
+vkg_status vkg_instances_from_wire(const void *records, uint32_t n, vkg_instance *out, vkg_wire_entry_info *info);
+
 /* per-pixel output record, the layout of the reference's pixel_data_t (pixel_data.slang:9-21):
    accumulated radiance, coverage of the last batch, reversed-z depth, primary-hit normal
    (octahedral, two snorm16), object id (0xFFFF on a miss), primary-hit albedo (RGBA8) — the

@@ -86,6 +86,11 @@ class vkg_gltf_counts(C.Structure):
                 ("num_lights", C.c_uint32), ("skipped_primitives", C.c_uint32)]
 
 
+class vkg_wire_entry_info(C.Structure):
+    _fields_ = [("buffer_index", C.c_uint32), ("base_index", C.c_uint32), ("vertex_offset", C.c_int32),
+                ("aabb_min", C.c_float * 3), ("aabb_max", C.c_float * 3)]
+
+
 class vkg_pixel_data(C.Structure):
     _fields_ = [("radiance", C.c_float * 3), ("alpha", C.c_float), ("depth", C.c_float), ("normal", C.c_uint32),
                 ("object_id", C.c_uint32), ("albedo", C.c_uint32)]
@@ -238,6 +243,8 @@ SIGNATURES = {
     "vkg_scene_bvh": (I32, [P, C.POINTER(P)]),
     "vkg_scene_env_tables": (I32, [P, C.POINTER(P), C.POINTER(P), C.POINTER(U32), C.POINTER(U32)]),
     "vkg_settings_default": (I32, [C.POINTER(vkg_settings)]),
+    "vkg_materials_from_wire": (I32, [P, U32, P, C.POINTER(U32)]),
+    "vkg_instances_from_wire": (I32, [P, U32, P, P]),
     "vkg_medium_params_default": (I32, [C.POINTER(vkg_medium_params)]),
     "vkg_scene_camera_medium": (I32, [P, C.POINTER(C.c_float), C.POINTER(U32)]),
     "vkg_tracer_create": (I32, [P, C.POINTER(vkg_tracer_create_info), C.POINTER(P)]),

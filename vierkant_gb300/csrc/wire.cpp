@@ -1,0 +1,131 @@
+// RayBuilder's wire records (material_struct_t, entry_t) read into the library's scene records.
+//
+// Layouts restated from the reference's struct definitions (RayBuilder.hpp:24-116 with glm's default
+// packing: vec4 16 B, vec3 12 B, vec2 8 B, quat 16 B stored x y z w, all 4-byte aligned; the structs
+// are alignas(16)) and checked against the shader twins' std430 layouts (ray/types.slang:17-32, :64-110).
+#include "internal.hpp"
+
+#include <cmath>
+#include <cstring>
+
+namespace
+{
+
+// byte offsets in RayBuilder::material_struct_t
+namespace mat_off
+{
+constexpr size_t color = 0, emission = 16, metalness = 32, roughness = 36, transmission = 40, null_surface = 44;
+constexpr size_t attenuation_color = 48, attenuation_distance = 60, ior = 64, clearcoat = 68,
+                 clearcoat_roughness = 72, sheen_roughness = 76, sheen_color = 80;
+constexpr size_t iridescence_strength = 96, iridescence_ior = 100, iridescence_thickness_range = 104;
+constexpr size_t albedo_index = 112, texture_type_flags = 132, blend_mode = 136, two_sided = 144,
+                 phase_g = 148, scatter_factor = 152, dispersion = 156, scatter_color = 160,
+                 diffuse_transmission = 172, diffuse_transmission_color = 176;
+}// namespace mat_off
+
+// byte offsets in RayBuilder::entry_t
+namespace entry_off
+{
+constexpr size_t texture_matrix = 0, transform = 64, inv_transform = 104, aabb = 144, material_index = 168,
+                 vertex_offset = 172, base_index = 176, buffer_index = 180;
+}// namespace entry_off
+
+template<class T>
+T rd(const unsigned char *p, size_t off)
+{
+    T v;
+    std::memcpy(&v, p + off, sizeof(T));
+    return v;
+}
+
+void rd3(const unsigned char *p, size_t off, float *dst)
+{
+    std::memcpy(dst, p + off, 3 * sizeof(float));
+}
+
+}// namespace
+
+extern "C" {
+
+vkg_status vkg_materials_from_wire(const void *records, uint32_t n, vkg_material *out, uint32_t *dropped)
+{
+    if(n && (!records || !out)) return VKG_ERR_INVALID_ARGUMENT;
+    uint32_t nd = 0;
+    const auto *base = static_cast<const unsigned char *>(records);
+    for(uint32_t i = 0; i < n; ++i)
+    {
+        const unsigned char *r = base + (size_t)i * VKG_WIRE_MATERIAL_BYTES;
+        vkg_material m;
+        vkg_material_defaults(&m);
+        rd3(r, mat_off::color, m.base_color);
+        float em[4];
+        std::memcpy(em, r + mat_off::emission, sizeof(em));
+        for(int c = 0; c < 3; ++c) m.emission[c] = em[c] * em[3];
+        m.metalness = rd<float>(r, mat_off::metalness);
+        m.roughness = rd<float>(r, mat_off::roughness);
+        m.transmission = rd<float>(r, mat_off::transmission);
+        m.null_surface = rd<uint32_t>(r, mat_off::null_surface) ? 1u : 0u;
+        rd3(r, mat_off::attenuation_color, m.attenuation_color);
+        m.attenuation_distance = rd<float>(r, mat_off::attenuation_distance);
+        m.ior = rd<float>(r, mat_off::ior);
+        m.clearcoat = rd<float>(r, mat_off::clearcoat);
+        m.clearcoat_roughness = rd<float>(r, mat_off::clearcoat_roughness);
+        m.sheen_roughness = rd<float>(r, mat_off::sheen_roughness);
+        rd3(r, mat_off::sheen_color, m.sheen_color);
+        m.iridescence = rd<float>(r, mat_off::iridescence_strength);
+        m.iridescence_ior = rd<float>(r, mat_off::iridescence_ior);
+        m.iridescence_thickness = rd<float>(r, mat_off::iridescence_thickness_range + 4); // range.y
+        m.twosided = rd<uint32_t>(r, mat_off::two_sided) ? 1u : 0u;
+        m.phase_g = rd<float>(r, mat_off::phase_g);
+        m.scatter_factor = rd<float>(r, mat_off::scatter_factor);
+        rd3(r, mat_off::scatter_color, m.scatter_color);
+        m.diffuse_transmission = rd<float>(r, mat_off::diffuse_transmission);
+        rd3(r, mat_off::diffuse_transmission_color, m.diffuse_transmission_color);
+        bool unused = rd<uint32_t>(r, mat_off::texture_type_flags) != 0 || rd<uint32_t>(r, mat_off::blend_mode) != 0 ||
+                      rd<float>(r, mat_off::dispersion) != 0.f;
+        nd += unused ? 1u : 0u;
+        out[i] = m;
+    }
+    if(dropped) *dropped = nd;
+    return VKG_OK;
+}
+
+vkg_status vkg_instances_from_wire(const void *records, uint32_t n, vkg_instance *out, vkg_wire_entry_info *info)
+{
+    if(n && (!records || !out)) return VKG_ERR_INVALID_ARGUMENT;
+    const auto *base = static_cast<const unsigned char *>(records);
+    for(uint32_t i = 0; i < n; ++i)
+    {
+        const unsigned char *r = base + (size_t)i * VKG_WIRE_ENTRY_BYTES;
+        float t[3], q[4], s[3];
+        rd3(r, entry_off::transform, t);
+        std::memcpy(q, r + entry_off::transform + 12, sizeof(q)); // x y z w
+        rd3(r, entry_off::transform + 28, s);
+        // rotation matrix of the unit quaternion (x, y, z, w), in double, columns scaled by s
+        const double x = q[0], y = q[1], z = q[2], w = q[3];
+        const double R[3][3] = {{1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)},
+                                {2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)},
+                                {2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)}};
+        vkg_instance in{};
+        for(int row = 0; row < 3; ++row)
+        {
+            for(int c = 0; c < 3; ++c) in.transform[4 * row + c] = (float)(R[row][c] * (double)s[c]);
+            in.transform[4 * row + 3] = t[row];
+        }
+        in.blas = rd<uint32_t>(r, entry_off::buffer_index);
+        in.material = rd<uint32_t>(r, entry_off::material_index);
+        out[i] = in;
+        if(info)
+        {
+            vkg_wire_entry_info &e = info[i];
+            e.buffer_index = in.blas;
+            e.base_index = rd<uint32_t>(r, entry_off::base_index);
+            e.vertex_offset = rd<int32_t>(r, entry_off::vertex_offset);
+            rd3(r, entry_off::aabb, e.aabb_min);
+            rd3(r, entry_off::aabb + 12, e.aabb_max);
+        }
+    }
+    return VKG_OK;
+}
+
+}// extern "C"
