@@ -176,10 +176,12 @@ def test_cornell_primary_and_secondary_bit_exact(ctx):
     b.close()
 
 
-def test_host_buffer_variant_equals_device(ctx):
+@pytest.mark.parametrize("w,h,spp", [(320, 180, 1), (1280, 720, 3)])
+def test_host_buffer_variant_equals_device(ctx, w, h, spp):
+    """one chunk, and 2.76 M rays: three chunks of the two-stream copy / trace pipeline, the last ragged"""
     sc, b = cornell(ctx)
-    cam_p = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, 320, 180)
-    rays = ctx.camera_rays(cam_p, 0x5EED, 2, 1)
+    cam_p = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, w, h)
+    rays = ctx.camera_rays(cam_p, 0x5EED, 2, spp)
     dev = hits_np(b.closest_hit(rays))
     rh = rays.cpu().pin_memory()
     hh = torch.empty((rays.shape[0], 4), dtype=torch.int32).pin_memory()

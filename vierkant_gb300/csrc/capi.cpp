@@ -81,6 +81,10 @@ vkg_status vkg_ctx_destroy(vkg_ctx *ctx)
     cudaFree(ctx->d_work);
     cudaFree(ctx->d_stage_rays);
     cudaFree(ctx->d_stage_hits);
+    for(cudaStream_t s: ctx->pipe)
+        if(s) cudaStreamDestroy(s);
+    for(cudaEvent_t e: ctx->pipe_ev)
+        if(e) cudaEventDestroy(e);
     delete ctx;
     return VKG_OK;
 }

@@ -23,6 +23,9 @@ struct vkg_ctx
     void *d_stage_rays = nullptr;
     void *d_stage_hits = nullptr;
     size_t stage_rays_bytes = 0, stage_hits_bytes = 0;
+    // the host variant's copy / trace pipeline: two streams and a fork + two join events (first use)
+    cudaStream_t pipe[2] = {nullptr, nullptr};
+    cudaEvent_t pipe_ev[3] = {nullptr, nullptr, nullptr};
 };
 
 struct vkg_bvh

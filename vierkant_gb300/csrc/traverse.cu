@@ -8,6 +8,7 @@
 // 96 B per node visit and 48 B per triangle test from L2/L1.
 #include "traverse.cuh"
 
+#include <algorithm>
 #include <cstdlib>
 #include <string>
 
@@ -271,12 +272,56 @@ extern "C" vkg_status vkg_closest_hit_host(vkg_ctx *ctx, const vkg_bvh *bvh, con
         VKG_TRY_CUDA(ctx, cudaMalloc(&ctx->d_stage_hits, hb));
         ctx->stage_hits_bytes = hb;
     }
-    VKG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->d_stage_rays, h_rays, rb, cudaMemcpyHostToDevice, st));
-    vkg_status s = launch_trace(ctx, bvh, static_cast<const vkg_ray *>(ctx->d_stage_rays), num_rays,
-                                static_cast<vkg_hit *>(ctx->d_stage_hits), nullptr, flags, st);
-    if(s != VKG_OK) return s;
-    VKG_TRY_CUDA(ctx, cudaMemcpyAsync(h_hits, ctx->d_stage_hits, hb, cudaMemcpyDeviceToHost, st));
-    VKG_TRY_CUDA(ctx, cudaStreamSynchronize(st));
+    // Chunks of HOST_CHUNK rays alternate between two streams: chunk c's upload, trace and download
+    // are ordered on its stream, so the upload of c + 1 and the download of c - 1 (two copy engines)
+    // run under the trace of c. Each chunk has its own region of the staging buffers.
+    constexpr uint32_t HOST_CHUNK = 1u << 20;
+    const uint32_t chunks = (num_rays + HOST_CHUNK - 1) / HOST_CHUNK;
+    auto *d_rays = static_cast<vkg_ray *>(ctx->d_stage_rays);
+    auto *d_hits = static_cast<vkg_hit *>(ctx->d_stage_hits);
+    // (the persistent kernels share one work counter, so they are not run on two streams at once)
+    if(chunks == 1 || use_persistent())
+    {
+        VKG_TRY_CUDA(ctx, cudaMemcpyAsync(d_rays, h_rays, rb, cudaMemcpyHostToDevice, st));
+        vkg_status s = launch_trace(ctx, bvh, d_rays, num_rays, d_hits, nullptr, flags, st);
+        if(s != VKG_OK) return s;
+        VKG_TRY_CUDA(ctx, cudaMemcpyAsync(h_hits, d_hits, hb, cudaMemcpyDeviceToHost, st));
+        VKG_TRY_CUDA(ctx, cudaStreamSynchronize(st));
+        return VKG_OK;
+    }
+    for(int k = 0; k < 2; ++k)
+        if(!ctx->pipe[k]) VKG_TRY_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->pipe[k], cudaStreamNonBlocking));
+    for(int k = 0; k < 3; ++k)
+        if(!ctx->pipe_ev[k]) VKG_TRY_CUDA(ctx, cudaEventCreateWithFlags(&ctx->pipe_ev[k], cudaEventDisableTiming));
+    // fork: both streams start after the work already queued on the caller's stream
+    VKG_TRY_CUDA(ctx, cudaEventRecord(ctx->pipe_ev[0], st));
+    for(int k = 0; k < 2; ++k) VKG_TRY_CUDA(ctx, cudaStreamWaitEvent(ctx->pipe[k], ctx->pipe_ev[0], 0));
+    vkg_status status = VKG_OK;
+    for(uint32_t c = 0; c < chunks && status == VKG_OK; ++c)
+    {
+        cudaStream_t ps = ctx->pipe[c & 1u];
+        const size_t first = (size_t)c * HOST_CHUNK;
+        const uint32_t n = (uint32_t)std::min<size_t>(HOST_CHUNK, num_rays - first);
+        cudaError_t e = cudaMemcpyAsync(d_rays + first, h_rays + first, n * sizeof(vkg_ray), cudaMemcpyHostToDevice, ps);
+        if(e != cudaSuccess)
+        {
+            status = cuda_check(ctx, e, "vkg_closest_hit_host");
+            break;
+        }
+        status = launch_trace(ctx, bvh, d_rays + first, n, d_hits + first, nullptr, flags, ps);
+        if(status != VKG_OK) break;
+        e = cudaMemcpyAsync(h_hits + first, d_hits + first, n * sizeof(vkg_hit), cudaMemcpyDeviceToHost, ps);
+        if(e != cudaSuccess) status = cuda_check(ctx, e, "vkg_closest_hit_host");
+    }
+    // join: the caller's stream waits for both (also after an error, so nothing is left in flight)
+    for(int k = 0; k < 2; ++k)
+    {
+        cudaEventRecord(ctx->pipe_ev[1 + k], ctx->pipe[k]);
+        cudaStreamWaitEvent(st, ctx->pipe_ev[1 + k], 0);
+    }
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if(status != VKG_OK) return status;
+    if(e != cudaSuccess) return cuda_check(ctx, e, "vkg_closest_hit_host");
     return VKG_OK;
 }
 
