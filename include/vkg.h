@@ -242,7 +242,7 @@ typedef struct vkg_bvh vkg_bvh;
 
 typedef struct vkg_bvh_build_options
 {
-    uint32_t leaf_max; /* max triangles per leaf range, 1..16 (0 -> default 4) */
+    uint32_t leaf_max; /* max triangles per leaf range, 1..16 (0 -> default 2) */
 } vkg_bvh_build_options;
 
 typedef struct vkg_bvh_info
@@ -388,7 +388,7 @@ typedef struct vkg_scene_desc
     uint32_t num_materials;
     const float *d_env_rgb; /* equirect map, env_width x env_height x 3 fp32 */
     uint32_t env_width, env_height;
-    uint32_t leaf_max; /* BVH leaf size (0 -> 4) */
+    uint32_t leaf_max; /* BVH leaf size (0 -> 2) */
 } vkg_scene_desc;
 vkg_status vkg_scene_create(vkg_ctx *ctx, const vkg_scene_desc *desc, vkg_scene **out, void *stream);
 /* instanced scenes (RayBuilder's BLAS-per-mesh + TLAS-over-entries layout, RayBuilder.cpp:98-300,
@@ -414,7 +414,7 @@ typedef struct vkg_instanced_scene_desc
     uint32_t num_materials;
     const float *d_env_rgb;
     uint32_t env_width, env_height;
-    uint32_t leaf_max; /* BVH leaf size of the meshes (0 -> 4) */
+    uint32_t leaf_max; /* BVH leaf size of the meshes (0 -> 2) */
 } vkg_instanced_scene_desc;
 vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_desc *desc, vkg_scene **out,
                                       void *stream);

@@ -111,7 +111,7 @@ def test_config1_closest_hit_full(ctx, golden):
     hits = b.closest_hit(rays, flags=RAY_COUNT_STATS)
     visits, tests = ctx.stats(reset=True)
     h = hits_np(hits)
-    cb = oracle.CpuBVH(xyz, idx, 4)
+    cb = oracle.CpuBVH(xyz, idx, DEFAULT_LEAF)
     ref_rays = oracle.camera_rays(cam_o, 0x5EED, 1, 1)
     ch, st = cb.closest_hit(ref_rays, stats=True)
     assert h.tobytes() == ch.tobytes()
@@ -122,6 +122,9 @@ def test_config1_closest_hit_full(ctx, golden):
     h2 = hits_np(b.closest_hit(rays))
     assert h2.tobytes() == h.tobytes()
     b.close()
+
+
+DEFAULT_LEAF = 2  # the library's default BVH leaf size
 
 
 def cornell(ctx):
@@ -151,7 +154,7 @@ def test_cornell_primary_and_secondary_bit_exact(ctx):
     rays = ctx.camera_rays(cam_p, 0x5EED, 2, 1)
     ref_rays = oracle.camera_rays(cam_o, 0x5EED, 2, 1)
     assert rays.cpu().numpy().tobytes() == ref_rays.tobytes()
-    cb = oracle.CpuBVH(sc["xyz"], sc["indices"], 4)
+    cb = oracle.CpuBVH(sc["xyz"], sc["indices"], DEFAULT_LEAF)
     assert b.info().num_nodes == cb.b.num_nodes
     h = hits_np(b.closest_hit(rays))
     assert h.tobytes() == cb.closest_hit(ref_rays).tobytes()

@@ -36,7 +36,7 @@ def _copy_out(ptr, nbytes):
     return out.cpu().numpy().tobytes()
 
 
-def _noalloc(xyz, idx, leaf_max=4):
+def _noalloc(xyz, idx, leaf_max=0):  # 0: the library default, as the regular build
     n = idx.shape[0]
     nodes = torch.zeros((max(1, n) * 96,), dtype=torch.uint8, device="cuda")
     tris = torch.zeros((max(1, n) * 48,), dtype=torch.uint8, device="cuda")

@@ -769,7 +769,7 @@ extern "C" vkg_status vkg_bvh_build(vkg_ctx *ctx, const float *d_xyz, uint32_t n
     if(num_tris >= MAX_TRIS)
         return set_error(ctx, VKG_ERR_CAPACITY, "vkg_bvh_build: %u triangles exceed the maximum of %u", num_tris,
                          MAX_TRIS - 1);
-    uint32_t leaf_max = (opts && opts->leaf_max) ? opts->leaf_max : 4u;
+    uint32_t leaf_max = (opts && opts->leaf_max) ? opts->leaf_max : 2u;
     if(leaf_max > LEAF_MAX_LIMIT)
         return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_bvh_build: leaf_max %u > %u", leaf_max, LEAF_MAX_LIMIT);
     if(vkg_status s = bind_device(ctx); s != VKG_OK) return s;
@@ -867,7 +867,7 @@ extern "C" vkg_status vkg_tlas_build(vkg_ctx *ctx, const vkg_bvh *const *blas, u
         if(!blas[b]) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_tlas_build: BLAS %u is NULL", b);
     if(num_instances >= MAX_TRIS)
         return set_error(ctx, VKG_ERR_CAPACITY, "vkg_tlas_build: %u instances exceed the maximum", num_instances);
-    const uint32_t leaf_max = (opts && opts->leaf_max) ? opts->leaf_max : 4u;
+    const uint32_t leaf_max = (opts && opts->leaf_max) ? opts->leaf_max : 2u;
     if(leaf_max > LEAF_MAX_LIMIT)
         return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_tlas_build: leaf_max %u > %u", leaf_max, LEAF_MAX_LIMIT);
     if(vkg_status s = bind_device(ctx); s != VKG_OK) return s;
@@ -1074,7 +1074,7 @@ extern "C" vkg_status vkg_bvh_build_noalloc(const float *d_xyz, uint32_t num_ver
 {
     if(num_tris > NOALLOC_MAX_TRIS) return VKG_ERR_CAPACITY;
     if(!d_info) return VKG_ERR_INVALID_ARGUMENT;
-    if(leaf_max == 0) leaf_max = 4u;
+    if(leaf_max == 0) leaf_max = 2u;
     if(leaf_max > LEAF_MAX_LIMIT) return VKG_ERR_INVALID_ARGUMENT;
     if(num_tris > 0 && (!d_xyz || !d_indices || num_vertices == 0 || !d_nodes || !d_tris)) return VKG_ERR_INVALID_ARGUMENT;
     if(num_tris > 0 && node_capacity < num_tris) return VKG_ERR_INVALID_ARGUMENT;

@@ -173,7 +173,7 @@ class _Lights:
 
 
 class Scene(_Lights):
-    def __init__(self, ctx: Context, xyz, indices, tri_material, materials, env_rgb, leaf_max=4):
+    def __init__(self, ctx: Context, xyz, indices, tri_material, materials, env_rgb, leaf_max=2):
         dev = f"cuda:{ctx.device}"
 
         def t(a, dt):
@@ -236,7 +236,7 @@ class InstancedScene(_Lights):
     (raytracing.INSTANCE_DTYPE: object -> world transform, mesh, material) under a top-level BVH,
     materials (MATERIAL_DTYPE) and the environment map. Renders with PBRPathTracer like Scene."""
 
-    def __init__(self, ctx: Context, meshes, instances, materials, env_rgb, leaf_max=4):
+    def __init__(self, ctx: Context, meshes, instances, materials, env_rgb, leaf_max=2):
         from ._lib import vkg_instanced_scene_desc, vkg_mesh_desc
         from .raytracing import INSTANCE_DTYPE
         dev = f"cuda:{ctx.device}"

@@ -81,7 +81,7 @@ class Context:
 class BVH:
     """8-wide quantised BVH built on the GPU from fp32 xyz vertices and uint32 triangle indices."""
 
-    def __init__(self, ctx: Context, xyz: torch.Tensor, indices: torch.Tensor, leaf_max: int = 4):
+    def __init__(self, ctx: Context, xyz: torch.Tensor, indices: torch.Tensor, leaf_max: int = 2):
         self.ctx = ctx
         dev = f"cuda:{ctx.device}"
         xyz = xyz.to(device=dev, dtype=torch.float32).contiguous()
