@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(PT_THREADS)
 }
 
 template<class J, int STACK = (int)TRAVERSAL_STACK>
-__global__ void __launch_bounds__(PT_THREADS)
+__global__ void __launch_bounds__(PT_THREADS, 8) // 64 registers: 8 blocks per SM
         k_pt_extend(J S, const vkg_ray *__restrict__ q_ray, const uint32_t *__restrict__ q_pid,
                     const uint32_t *__restrict__ count, vkg_hit *__restrict__ hits, uint32_t *__restrict__ hit_inst)
 {
@@ -829,7 +829,7 @@ __global__ void __launch_bounds__(PT_THREADS)
 }
 
 template<class J, int STACK = (int)TRAVERSAL_STACK>
-__global__ void __launch_bounds__(PT_THREADS)
+__global__ void __launch_bounds__(PT_THREADS, 8) // 64 registers: 8 blocks per SM
         k_pt_shadow(J S, const vkg_ray *__restrict__ s_ray, const uint32_t *__restrict__ s_pid,
                     const float4 *__restrict__ s_contrib, const uint32_t *__restrict__ count,
                     float4 *__restrict__ radiance)
@@ -992,6 +992,8 @@ __global__ void __launch_bounds__(PT_THREADS)
     const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
     unsigned long long v = 0, t = 0;
     ray_state_t<STACK> s;
+    uint2 stack[STACK];
+    s.st = stack;
     const node8 *nodes = nullptr;
     const tri_rec *tris = nullptr;
     uint32_t cur = 0xFFFFFFFFu;
@@ -1065,6 +1067,8 @@ __global__ void __launch_bounds__(PT_THREADS)
     const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
     const int cull = SHADOW ? CULL_NONE : CULL_BACK_UNLESS_TWOSIDED;
     tl_state s;
+    uint2 stack[TL_STACK];
+    s.st = stack;
     uint32_t cur = 0xFFFFFFFFu;
     bool exhausted = false;
     for(;;)

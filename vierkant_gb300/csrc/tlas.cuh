@@ -48,7 +48,8 @@ struct tl_state
     const tri_rec *tris;
     int sp;
     bool in_blas, done;
-    uint2 st[TL_STACK]; // {entry, entry distance (float bits)}
+    uint2 *st; // uint2[TL_STACK] {entry, entry distance (float bits)}, a separate local array so that
+               // the fields stay in registers (see ray_state_t)
 };
 
 __device__ __forceinline__ void tl_init(tl_state &s, const node8 *tnodes, float ox, float oy, float oz, float tmin,
@@ -202,6 +203,8 @@ __device__ __forceinline__ tlas_result trace_tlas(const node8 *__restrict__ tnod
                                                   float tmin, float dx, float dy, float dz, float tmax, int cull)
 {
     tl_state s;
+    uint2 stack[TL_STACK];
+    s.st = stack;
     tl_init(s, tnodes, ox, oy, oz, tmin, dx, dy, dz, tmax);
     while(tl_step<ANY>(s, tnodes, inst, blas, cull)) {}
     tlas_result R;

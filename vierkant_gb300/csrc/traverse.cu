@@ -70,6 +70,8 @@ __global__ void __launch_bounds__(TRACE_THREADS)
     const uint32_t lt = (1u << lane) - 1u;
     unsigned long long visits = 0, tests = 0;
     ray_state s;
+    uint2 stack[TRAVERSAL_STACK];
+    s.st = stack;
     uint32_t cur = 0xFFFFFFFFu;
     bool exhausted = false;
     for(;;)

@@ -77,7 +77,10 @@ __device__ __forceinline__ float safe_rcp(float d)
 __device__ __forceinline__ float qbyte(uint32_t w, int k) { return (float)((w >> (8 * (k & 3))) & 0xFFu); }
 
 
-// per-ray traversal state (the stack lives in local memory; only its used top is touched)
+// per-ray traversal state. The stack (STACK entries) is a separate local-memory array the state
+// points to: a struct that holds the array itself is placed in local memory as a whole, fields
+// included, and every field access then costs a local-memory access; with the array outside, the
+// fields stay in registers.
 template<int STACK = (int)TRAVERSAL_STACK>
 struct ray_state_t
 {
@@ -86,7 +89,7 @@ struct ray_state_t
     uint32_t best;
     int sp;
     bool done;
-    uint2 st[STACK]; // {node, entry distance (float bits)}: one 64-bit access per push / pop
+    uint2 *st; // uint2[STACK] {node, entry distance (float bits)}: one 64-bit access per push / pop
 };
 using ray_state = ray_state_t<>;
 
@@ -307,6 +310,8 @@ __device__ __forceinline__ trace_result trace_ray(const node8 *__restrict__ node
                                                   unsigned long long *__restrict__ counters)
 {
     ray_state_t<STACK> s;
+    uint2 stack[STACK];
+    s.st = stack;
     ray_init(s, ox, oy, oz, tmin, dx, dy, dz, tmax);
     while(ray_step<ANY, STATS>(s, nodes, tris, cull, visits, tests, counters)) {}
     return ray_result(s);
