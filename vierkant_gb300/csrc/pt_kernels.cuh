@@ -876,7 +876,7 @@ __global__ void __launch_bounds__(PT_THREADS, 8) // 64 registers: 8 blocks per S
 constexpr int PT_MAX_CROSSINGS = 32;
 
 template<class J, int STACK = (int)TRAVERSAL_STACK>
-__global__ void __launch_bounds__(PT_THREADS) k_pt_light_shadow(J S, light_queue lq, float4 *__restrict__ radiance)
+__global__ void __launch_bounds__(PT_THREADS, 8) k_pt_light_shadow(J S, light_queue lq, float4 *__restrict__ radiance)
 {
     const uint32_t n = *lq.count;
     const uint32_t stride = gridDim.x * blockDim.x;
