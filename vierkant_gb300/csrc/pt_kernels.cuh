@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(PT_THREADS)
 }
 
 template<class J, int STACK = (int)TRAVERSAL_STACK>
-__global__ void __launch_bounds__(PT_THREADS, 8) // 64 registers: 8 blocks per SM
+__global__ void __launch_bounds__(PT_THREADS, STACK <= 64 ? 8 : 6) // 64 / 85 registers
         k_pt_extend(J S, const vkg_ray *__restrict__ q_ray, const uint32_t *__restrict__ q_pid,
                     const uint32_t *__restrict__ count, vkg_hit *__restrict__ hits, uint32_t *__restrict__ hit_inst)
 {
@@ -829,7 +829,7 @@ __global__ void __launch_bounds__(PT_THREADS)
 }
 
 template<class J, int STACK = (int)TRAVERSAL_STACK>
-__global__ void __launch_bounds__(PT_THREADS, 8) // 64 registers: 8 blocks per SM
+__global__ void __launch_bounds__(PT_THREADS, STACK <= 64 ? 8 : 6) // 64 / 85 registers
         k_pt_shadow(J S, const vkg_ray *__restrict__ s_ray, const uint32_t *__restrict__ s_pid,
                     const float4 *__restrict__ s_contrib, const uint32_t *__restrict__ count,
                     float4 *__restrict__ radiance)
