@@ -631,16 +631,31 @@ static void d_transmit_raw(const orc_pt_job *J, double ox, double oy, double oz,
             return;
         }
         for(int c = 0; c < 3; ++c) T[c] = T[c] * (double)m->base[c] * (double)m->transmission;
-        if(J->media && !J->inst && (J->media[mat].flags & 1u))
+        if(J->media && (J->media[mat].flags & 1u))
         {
-            /* Beer-Lambert through transmissive volumes of a single-level scene (as the GPU) */
-            const float *xyz = J->scene->xyz;
-            const uint32_t *ix = J->scene->idx + 3 * (size_t)prim;
+            /* Beer-Lambert through transmissive volumes: the face from the triangle's normal against
+               the ray, in object space for an instance (the world-to-object map of the direction) */
+            const float *xyz;
+            const uint32_t *ix;
+            double dd[3] = {dx, dy, dz};
+            if(!J->inst)
+            {
+                xyz = J->scene->xyz;
+                ix = J->scene->idx + 3 * (size_t)prim;
+            }
+            else
+            {
+                const uint32_t m = J->inst->inst_mesh[inst];
+                xyz = J->inst->mesh_xyz[m];
+                ix = J->inst->mesh_idx[m] + 3 * (size_t)prim;
+                const double *w = ((const inst_bvh *)J->ibvh)->w2o + 12 * (size_t)inst;
+                for(int r = 0; r < 3; ++r) dd[r] = w[4 * r] * dx + w[4 * r + 1] * dy + w[4 * r + 2] * dz;
+            }
             const float *a = xyz + 3 * (size_t)ix[0], *b = xyz + 3 * (size_t)ix[1], *c2 = xyz + 3 * (size_t)ix[2];
             double e1[3] = {(double)b[0] - a[0], (double)b[1] - a[1], (double)b[2] - a[2]};
             double e2[3] = {(double)c2[0] - a[0], (double)c2[1] - a[1], (double)c2[2] - a[2]};
             double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
-            int front = n[0] * dx + n[1] * dy + n[2] * dz < 0.0;
+            int front = n[0] * dd[0] + n[1] * dd[1] + n[2] * dd[2] < 0.0;
             for(int c = 0; c < 3; ++c)
             {
                 double st = (double)J->media[mat].sigma_s[c] + (double)J->media[mat].sigma_a[c];

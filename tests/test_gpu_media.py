@@ -299,8 +299,8 @@ def test_camera_medium_validated(ctx):
 def test_instanced_media_against_fp64_oracle(ctx):
     """the media showcase as a two-level scene (one identity instance per wall quad and sphere, its
     material per instance) against the instanced FP64 oracle on a crop: media, null surfaces and the
-    media stack through the two-level traversal (light shadow rays of instanced scenes tint through
-    glass without optical depth, in both)"""
+    media stack through the two-level traversal, and light shadow rays that take the optical depth of
+    absorbing glass instances crossing by crossing"""
     from scene_helpers import split_cornell
     from vierkant_gb300.pathtracer import InstancedScene
     sc = geometry.cornell_scene(0x5EED, 2, NUM_SPHERES, 16)

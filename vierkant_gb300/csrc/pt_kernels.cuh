@@ -927,18 +927,24 @@ __global__ void __launch_bounds__(PT_THREADS, 8) k_pt_light_shadow(J S, light_qu
         }
         else
         {
-            // instanced scenes: a material per instance, so crossings are found one closest hit at a time
+            // instanced scenes: a material per instance, so crossings are found one closest hit at a time;
+            // Beer-Lambert optical depth as in the single-level pass, the face taken from the hit's
+            // world-space geometric normal
             float tmin = r0.w;
+            float3 od = f3(0.f, 0.f, 0.f);
             for(int k = 0;; ++k)
             {
-                uint32_t prim, mat;
-                float t;
+                uint32_t prim, mat, inst = 0;
+                float t, hu = 0.f, hv = 0.f;
                 if(P.two_level)
                 {
                     const tlas_result r = trace_tlas<false>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z, tmin,
                                                             r1.x, r1.y, r1.z, r1.w, cull);
                     prim = r.prim;
                     t = r.t;
+                    inst = r.inst;
+                    hu = r.u;
+                    hv = r.v;
                     mat = prim == VKG_MISS ? 0u : __ldg(&P.tl_by_id[r.inst].material);
                 }
                 else
@@ -947,6 +953,8 @@ __global__ void __launch_bounds__(PT_THREADS, 8) k_pt_light_shadow(J S, light_qu
                                                                           r1.y, r1.z, r1.w, cull, v, c, nullptr);
                     prim = r.prim;
                     t = r.t;
+                    hu = r.u;
+                    hv = r.v;
                     mat = prim == VKG_MISS ? 0u : __ldg(&P.tri_mat[prim]);
                 }
                 if(prim == VKG_MISS) break;
@@ -962,8 +970,20 @@ __global__ void __launch_bounds__(PT_THREADS, 8) k_pt_light_shadow(J S, light_qu
                     break;
                 }
                 T = T * f3(q.base_color[0], q.base_color[1], q.base_color[2]) * q.transmission;
+                if(P.media && (P.media[mat].flags & MEDIUM_VOLUME))
+                {
+                    float3 hp, ng;
+                    uint32_t hm;
+                    hit_surface(P, prim, inst, hu, hv, hp, ng, hm);
+                    const medium_rec &M = P.media[mat];
+                    const float3 st = f3(M.sigma_s[0] + M.sigma_a[0], M.sigma_s[1] + M.sigma_a[1],
+                                         M.sigma_s[2] + M.sigma_a[2]);
+                    od = od + st * (dot(ng, f3(r1.x, r1.y, r1.z)) < 0.f ? -t : t);
+                }
                 tmin = t;
             }
+            if(P.media && max3(T) > 0.f)
+                T = T * f3(expf(-fmaxf(od.x, 0.f)), expf(-fmaxf(od.y, 0.f)), expf(-fmaxf(od.z, 0.f)));
         }
         if(max3(T) > 0.f)
         {
