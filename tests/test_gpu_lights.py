@@ -9,7 +9,7 @@
   NEE competitor);
 * MIS, NEE-only and BSDF-only converge to the same image when paths are long enough that the last
   vertex's untraced BSDF ray carries no light;
-* invalid light records are rejected; the batch renderer refuses lights.
+* invalid light records are rejected; the batch renderer renders lit jobs like the tracer.
 """
 import math
 
@@ -175,8 +175,33 @@ def test_invalid_lights_rejected(ctx, lit, field, value):
     lit["scene"].set_lights(cornell_lights())  # the scene keeps working
 
 
-def test_batch_refuses_lights(ctx, lit):
+@pytest.mark.parametrize("extend,stack", [(1, 64), (2, 128)])
+def test_batch_renders_lights_like_the_tracer(ctx, lit, extend, stack):
+    """the batch renderer with lit jobs (scene lights, with and without the sun) next to an unlit one:
+    the lit jobs' images equal the single-scene tracer's bit for bit, over two accumulated batches. A
+    batch shades all its jobs with one kernel variant, here the full one, so the metal-rough job —
+    which the tracer alone shades with the metal-roughness variant — agrees up to the rounding of
+    the out-of-line BSDF evaluation (FMA contraction across the call)"""
     from vierkant_gb300.batch import BatchJob, BatchRenderer
-    job = BatchJob(lit["scene"], lit["cam"], settings(1, sun=False), seed=1)
-    with pytest.raises(_lib.VkgError):
-        BatchRenderer(ctx, [job])
+    sc = lit["sc"]
+    plain = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], sc["materials"], lit["env"])
+    cam_s = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, 96, 64)
+    jobs = [BatchJob(lit["scene"], cam_s, settings(3, res=(96, 64), sun=True), seed=1),
+            BatchJob(plain, cam_s, settings(2, res=(96, 64), sun=False), seed=2),
+            BatchJob(lit["scene"], cam_s, settings(4, res=(96, 64), sun=False, mis=1), seed=3)]
+    t = BatchRenderer.default_tuning()
+    t.extend_kernel, t.stack_depth = extend, stack
+    br = BatchRenderer(ctx, jobs, t)
+    for r in (1, 2):
+        imgs = [i.clone() for i in br.render()]
+        for k, job in enumerate(jobs):
+            pt = PBRPathTracer(ctx, seed=job.seed, settings=job.settings)
+            for _ in range(r):
+                ref = pt.render_scene(job.scene, job.camera).clone()
+            pt.close()
+            if k == 1:
+                assert torch.allclose(imgs[k], ref, rtol=1e-5, atol=1e-6), (k, r, (imgs[k] - ref).abs().max().item())
+            else:
+                assert torch.equal(imgs[k], ref), (k, r, (imgs[k] - ref).abs().max().item())
+    br.close()
+    plain.close()

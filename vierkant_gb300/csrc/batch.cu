@@ -19,6 +19,12 @@
 // (grid-stride vs persistent work-stealing queue tracers, grid size, wave size, block size, traversal
 // stack depth) on a one-sample render and keeps the fastest; tunings change timing only, never the
 // images.
+//
+// Analytic lights and the settings' sun: every job's light list in one device array, the light-NEE
+// shadow queue per wave and the light-shadow launch after the environment shadow launch, as the
+// tracer does. One shade variant serves all jobs of a batch: the full one when any job needs it
+// (materials beyond metal-roughness or lights), so a metal-rough job in such a batch equals its
+// tracer render up to the rounding of the out-of-line BSDF evaluation. Media are refused.
 #include "pt_kernels.cuh"
 
 #include <algorithm>
@@ -173,6 +179,13 @@ struct vkg_batch
     uint64_t *rng = nullptr, *pinc = nullptr;
     uint32_t *pjob = nullptr;
     float4 *beta_pdf = nullptr, *radiance = nullptr;
+    // analytic lights: every job's light list (the settings' sun first) in one array, and the
+    // light-NEE shadow queue of a wave (allocated when a job has lights)
+    bool any_lights = false;
+    vkg_light *d_lights = nullptr;
+    vkg_ray *l_ray = nullptr;
+    uint32_t *l_pid = nullptr;
+    float4 *l_contrib = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -188,8 +201,12 @@ void free_waves(vkg_batch *b)
     for(void *p: {(void *)b->q_ray[0], (void *)b->q_ray[1], (void *)b->q_pid[0], (void *)b->q_pid[1], (void *)b->hits,
                   (void *)b->hit_inst,
                   (void *)b->s_ray, (void *)b->s_pid, (void *)b->s_contrib, (void *)b->rng, (void *)b->pinc,
-                  (void *)b->pjob, (void *)b->beta_pdf, (void *)b->radiance, (void *)b->d_chunks})
+                  (void *)b->pjob, (void *)b->beta_pdf, (void *)b->radiance, (void *)b->d_chunks, (void *)b->l_ray,
+                  (void *)b->l_pid, (void *)b->l_contrib})
         cudaFree(p);
+    b->l_ray = nullptr;
+    b->l_pid = nullptr;
+    b->l_contrib = nullptr;
     b->q_ray[0] = b->q_ray[1] = nullptr;
     b->q_pid[0] = b->q_pid[1] = nullptr;
     b->hits = nullptr;
@@ -277,6 +294,12 @@ vkg_status ensure_waves(vkg_batch *b, const std::vector<vkg_batch::wave> &waves,
         al((void **)&b->pjob, need * sizeof(uint32_t));
         al((void **)&b->beta_pdf, need * sizeof(float4));
         al((void **)&b->radiance, need * sizeof(float4));
+        if(b->any_lights)
+        {
+            al((void **)&b->l_ray, need * sizeof(vkg_ray));
+            al((void **)&b->l_pid, need * sizeof(uint32_t));
+            al((void **)&b->l_contrib, need * sizeof(float4));
+        }
         if(e != cudaSuccess)
         {
             free_waves(b);
@@ -300,6 +323,8 @@ vkg_status enqueue(vkg_batch *b, const std::vector<vkg_batch::wave> &waves, cuda
     // a 64-entry stack serves BVHs of depth <= 10 (7 (depth - 1) + 1 entries at most)
     if(b->max_bvh_depth > 10) T.stack_depth = 128;
     const job_table J{b->d_params, b->pjob, b->pinc};
+    uint32_t *cnt_l = b->any_lights ? b->counters + 4 : nullptr;
+    const light_queue lq{b->l_ray, b->l_pid, b->l_contrib, cnt_l};
     VKG_TRY_CUDA(ctx, cudaMemsetAsync(b->sum, 0, (size_t)b->total_pix * 3 * sizeof(float), st));
     cache_io io{};
     const uint32_t bs = T.block_size;
@@ -331,13 +356,13 @@ vkg_status enqueue(vkg_batch *b, const std::vector<vkg_batch::wave> &waves, cuda
                 k_pt_extend<<<grid, bs, 0, st>>>(J, b->q_ray[a], b->q_pid[a], cnt_in, b->hits, b->hit_inst);
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_out, 0, sizeof(uint32_t), st));
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_s, 0, sizeof(uint32_t), st));
-            if(b->any_full)
+            if(cnt_l) VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_l, 0, sizeof(uint32_t), st));
+            if(b->any_full || b->any_lights)
                 k_pt_shade<MODE_PLAIN, job_table, true><<<grid, bs, 0, st>>>(J, depth, b->q_ray[a], b->q_pid[a], b->hits,
                                                                              b->hit_inst, cnt_in, b->q_ray[1 - a],
                                                                              b->q_pid[1 - a], cnt_out, b->s_ray,
                                                                              b->s_pid, b->s_contrib, cnt_s, b->rng,
-                                                                             b->beta_pdf, b->radiance, io,
-                                                                             light_queue{}, nullptr);
+                                                                             b->beta_pdf, b->radiance, io, lq, nullptr);
             else
             k_pt_shade<MODE_PLAIN, job_table, false><<<grid, bs, 0, st>>>(J, depth, b->q_ray[a], b->q_pid[a], b->hits, b->hit_inst, cnt_in,
                                                        b->q_ray[1 - a], b->q_pid[1 - a], cnt_out, b->s_ray, b->s_pid,
@@ -357,7 +382,12 @@ vkg_status enqueue(vkg_batch *b, const std::vector<vkg_batch::wave> &waves, cuda
                 k_pt_shadow<job_table, 64><<<grid, bs, 0, st>>>(J, b->s_ray, b->s_pid, b->s_contrib, cnt_s, b->radiance);
             else
                 k_pt_shadow<<<grid, bs, 0, st>>>(J, b->s_ray, b->s_pid, b->s_contrib, cnt_s, b->radiance);
-            k_pt_tally<<<1, 1, 0, st>>>(cnt_in, cnt_s, nullptr, b->totals);
+            // light NEE after the environment shadow launch: one writer per path at a time
+            if(cnt_l && T.stack_depth == 64)
+                k_pt_light_shadow<job_table, 64><<<grid, bs, 0, st>>>(J, lq, b->radiance);
+            else if(cnt_l)
+                k_pt_light_shadow<job_table><<<grid, bs, 0, st>>>(J, lq, b->radiance);
+            k_pt_tally<<<1, 1, 0, st>>>(cnt_in, cnt_s, cnt_l, b->totals);
             a = 1 - a;
         }
         k_batch_accumulate<<<(w.npix + 255) / 256, 256, 0, st>>>(ch, w.nchunks, w.npix, b->d_jd, b->radiance, b->sum);
@@ -459,11 +489,9 @@ vkg_status vkg_batch_create(vkg_ctx *ctx, const vkg_batch_job *jobs, uint32_t nj
         const vkg_batch_job &jb = jobs[j];
         if(!jb.scene) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_batch_create: job %u has no scene", j);
         if(vkg_status s = check_tracer_settings(ctx, &jb.settings); s != VKG_OK) return s;
-        if(!jb.scene->lights.empty() || jb.settings.sun_intensity > 0.f || jb.scene->d_media ||
-           jb.settings.camera_medium_mode != VKG_CAMERA_MEDIUM_DETECT)
+        if(jb.scene->d_media || jb.settings.camera_medium_mode != VKG_CAMERA_MEDIUM_DETECT)
             return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
-                             "vkg_batch_create: job %u: analytic lights, the sun and media are rendered by "
-                             "vkg_tracer_render", j);
+                             "vkg_batch_create: job %u: media are rendered by vkg_tracer_render", j);
         if(jb.camera.width != jb.settings.resolution[0] || jb.camera.height != jb.settings.resolution[1])
             return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_batch_create: job %u camera size != resolution", j);
         uint32_t x0, y0, w, h;
@@ -478,10 +506,16 @@ vkg_status vkg_batch_create(vkg_ctx *ctx, const vkg_batch_job *jobs, uint32_t nj
     b->njobs = njobs;
     b->jobs.assign(jobs, jobs + njobs);
     uint32_t off = 0;
+    std::vector<vkg_light> all_lights;
+    std::vector<uint32_t> light_off;
     for(uint32_t j = 0; j < njobs; ++j)
     {
         const vkg_batch_job &jb = jobs[j];
         b->params.push_back(make_params(jb.scene, jb.camera, jb.settings, jb.seed, 0));
+        const std::vector<vkg_light> jl = render_lights(jb.scene, jb.settings);
+        light_off.push_back((uint32_t)all_lights.size());
+        b->params.back().num_lights = (uint32_t)jl.size();
+        all_lights.insert(all_lights.end(), jl.begin(), jl.end());
         b->any_instanced = b->any_instanced || jb.scene->tlas != nullptr;
         b->any_full = b->any_full || jb.scene->any_full;
         if(jb.scene->bvh) b->max_bvh_depth = std::max(b->max_bvh_depth, jb.scene->bvh->depth);
@@ -501,8 +535,17 @@ vkg_status vkg_batch_create(vkg_ctx *ctx, const vkg_batch_job *jobs, uint32_t nj
     al((void **)&b->sum, (size_t)off * 3 * sizeof(float));
     al((void **)&b->accum, (size_t)off * 3 * sizeof(float));
     al((void **)&b->d_batch, sizeof(uint32_t));
-    al((void **)&b->counters, 4 * sizeof(uint32_t));
+    al((void **)&b->counters, 5 * sizeof(uint32_t));
     al((void **)&b->totals, 2 * sizeof(unsigned long long));
+    b->any_lights = !all_lights.empty();
+    if(b->any_lights)
+    {
+        al((void **)&b->d_lights, all_lights.size() * sizeof(vkg_light));
+        if(e == cudaSuccess)
+            e = cudaMemcpy(b->d_lights, all_lights.data(), all_lights.size() * sizeof(vkg_light), cudaMemcpyHostToDevice);
+        for(uint32_t j = 0; j < njobs; ++j)
+            b->params[j].lights = b->params[j].num_lights ? b->d_lights + light_off[j] : nullptr;
+    }
     if(e == cudaSuccess) e = cudaMemcpy(b->d_params, b->params.data(), njobs * sizeof(pt_params), cudaMemcpyHostToDevice);
     if(e == cudaSuccess) e = cudaMemcpy(b->d_jd, b->jdev.data(), njobs * sizeof(batch_job_dev), cudaMemcpyHostToDevice);
     if(e == cudaSuccess) e = cudaMemset(b->d_batch, 0, sizeof(uint32_t));
@@ -621,7 +664,7 @@ vkg_status vkg_batch_destroy(vkg_batch *b)
     drop_graph(b);
     free_waves(b);
     for(void *p: {(void *)b->d_params, (void *)b->d_jd, (void *)b->sum, (void *)b->accum, (void *)b->d_batch,
-                  (void *)b->counters, (void *)b->totals})
+                  (void *)b->counters, (void *)b->totals, (void *)b->d_lights})
         cudaFree(p);
     if(b->ev0) cudaEventDestroy(b->ev0);
     if(b->ev1) cudaEventDestroy(b->ev1);
