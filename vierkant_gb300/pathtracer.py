@@ -22,7 +22,7 @@ from ._lib import (check, lib, vkg_bvh_info, vkg_camera, vkg_light, vkg_light_so
                    vkg_tracer_stats)
 from .raytracing import Context
 
-# BASELINE sun: 30 deg elevation, 20 deg azimuth (measured from +z toward +x), 5e4 peak, width 3.8e-5
+# the benchmark sky's sun: 30 deg elevation, 20 deg azimuth (measured from +z toward +x), 5e4 peak, width 3.8e-5
 SUN_ELEVATION_DEG = 30.0
 SUN_AZIMUTH_DEG = 20.0
 
