@@ -44,6 +44,24 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, device) -> float:
+    """The largest of every rank's x: the slowest replica sets the whole job's time (a no-op without
+    an initialised process group of more than one rank)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank: int, world_size: int, ms: float) -> float:
+    """Whole-job throughput of weak-scaled replicas in millions of units per second: every rank
+    processed units_per_rank units in at most ms milliseconds."""
+    return units_per_rank * world_size / (ms * 1e-3) / 1e6
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -188,13 +206,8 @@ def run_ours(args):
         dist.barrier()
     ms_total = e0.elapsed_time(e1)
     clk = clocks.stop()
-    ms_step = ms_total / args.steps
-    if ws > 1:
-        t = torch.tensor([ms_step], device=batch.device, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    rays_all = n * ws
-    value = rays_all / (ms_step * 1e-3) / 1e6
+    ms_step = max_over_ranks(ms_total / args.steps, batch.device)
+    value = replica_throughput(n, ws, ms_step)
 
     # end to end through the host-buffer entry point: H2D rays, trace, D2H hits, synchronise
     rays_host = batch.cpu().pin_memory()
@@ -207,12 +220,8 @@ def run_ours(args):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         bvh.closest_hit_host(rays_host, hits_host)
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
-    if ws > 1:
-        t = torch.tensor([e2e_ms], device=batch.device, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = rays_all / (e2e_ms * 1e-3) / 1e6
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / e2e_steps, batch.device)
+    e2e_value = replica_throughput(n, ws, e2e_ms)
     # the host-buffer results must equal the device results
     dev_hits = hits.cpu()
     e2e_ok = bool(torch.equal(dev_hits, hits_host))
