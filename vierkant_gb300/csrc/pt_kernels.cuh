@@ -876,7 +876,8 @@ __global__ void __launch_bounds__(PT_THREADS, STACK <= 64 ? 8 : 6) // 64 / 85 re
 constexpr int PT_MAX_CROSSINGS = 32;
 
 template<class J, int STACK = (int)TRAVERSAL_STACK>
-__global__ void __launch_bounds__(PT_THREADS, 8) k_pt_light_shadow(J S, light_queue lq, float4 *__restrict__ radiance)
+__global__ void __launch_bounds__(PT_THREADS, STACK <= 64 ? 8 : 6) // 64 / 85 registers
+        k_pt_light_shadow(J S, light_queue lq, float4 *__restrict__ radiance)
 {
     const uint32_t n = *lq.count;
     const uint32_t stride = gridDim.x * blockDim.x;
