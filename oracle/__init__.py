@@ -5,8 +5,8 @@ the checker / the timed CPU reference. The product (vierkant_gb300, libvkg.so) n
 
 - ``orc()``  -> liboracle.so: C restatement of the reference's algorithms (see oracle.h)
 - ``ref()``  -> _ref/libvkref.so: the reference's own src/intersection.cpp compiled unmodified
-               against the project-written shim (None if it was not built: it needs the reference
-               checkout, which only exists where the fixtures are generated)
+               against the project-written shim from the copy in baseline/_ref (None if that copy
+               is absent)
 """
 from __future__ import annotations
 
@@ -18,7 +18,8 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-REF_ROOT = Path(os.environ.get("VKG_REFERENCE_ROOT", "/root/reference"))
+# the reference's files this oracle compiles, copied unmodified into baseline/_ref by `make -C oracle stage`
+REF_ROOT = Path(os.environ.get("VKG_REFERENCE_ROOT", str(HERE.parent / "baseline" / "_ref")))
 
 RAY_DTYPE = np.dtype([("o", "<f4", 3), ("tmin", "<f4"), ("d", "<f4", 3), ("tmax", "<f4")])
 HIT_DTYPE = np.dtype([("prim", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])
@@ -73,6 +74,7 @@ def orc() -> C.CDLL:
             "orc_intersect_ray_aabb": (i32, [vp, vp, vp, vp, C.POINTER(f32)]),
             "orc_closest_hit_bruteforce": (i32, [vp, vp, u32, vp, u32, vp, i32, i32]),
             "orc_any_hit_bruteforce": (i32, [vp, vp, u32, vp, u32, vp, i32, i32]),
+            "orc_bvh_closest_hit_fn": (i32, [vp, vp, u32, vp, i32, vp, vp, vp]),
             "orc_icosphere_counts": (u32, [u32, C.POINTER(u32)]),
             "orc_icosphere": (None, [f32, u32, vp, vp]),
             "orc_cornell_sphere_params": (None, [u64, u64, u32, vp]),
@@ -108,6 +110,8 @@ def ref() -> C.CDLL | None:
             "vkref_triangle_aabb_overlap": (u32, [vp, vp, vp]),
             "vkref_triangle_triangle_overlap": (u32, [vp, vp]),
             "vkref_closest_hit_bruteforce": (i32, [vp, vp, u32, vp, u32, vp, i32, i32]),
+            "vkref_mesh_create": (vp, [vp, vp, u32]),
+            "vkref_mesh_destroy": (None, [vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -216,6 +220,34 @@ class CpuBVH:
         occ = np.zeros(len(rays), np.uint32)
         orc().orc_bvh_any_hit(C.byref(self.b), ptr(rays), len(rays), ptr(occ), nthreads, int(cull))
         return occ
+
+    def closest_hit_ref(self, mesh: "RefMesh", rays, nthreads=0, stats=False):
+        """Closest hit over this BVH with every triangle test done by the reference's own
+        vierkant::intersect (intersection.cpp:114-129) on the original triangle; no culling. Returns
+        (hits, threads used) or (hits, threads, (visits, tests)) with stats."""
+        hits = np.zeros(len(rays), HIT_DTYPE)
+        st = np.zeros(2, np.uint64)
+        used = orc().orc_bvh_closest_hit_fn(C.byref(self.b), ptr(rays), len(rays), ptr(hits), nthreads, mesh.fn,
+                                            mesh.handle, ptr(st))
+        return (hits, used, (int(st[0]), int(st[1]))) if stats else (hits, used)
+
+
+class RefMesh:
+    """The reference's vierkant::Triangle array of an indexed mesh (needs oracle/_ref)."""
+
+    def __init__(self, xyz, idx):
+        R = ref()
+        if R is None:
+            raise RuntimeError("oracle/_ref/libvkref.so was not built")
+        xyz, idx = np.ascontiguousarray(xyz, np.float32), np.ascontiguousarray(idx, np.uint32)
+        self.handle = R.vkref_mesh_create(ptr(xyz), ptr(idx), idx.shape[0])
+        self.fn = C.cast(R.vkref_mesh_intersect, C.c_void_p)
+
+    def __del__(self):
+        try:
+            ref().vkref_mesh_destroy(self.handle)
+        except Exception:
+            pass
 
 
 INST_HIT_DTYPE = np.dtype([("prim", "<u4"), ("inst", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4"),

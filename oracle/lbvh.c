@@ -400,6 +400,8 @@ typedef struct {
     int cull;
     atomic_uint next;
     atomic_ullong visits, tests;
+    orc_tri_fn tri_fn; /* NULL: the restated test on the precomputed record */
+    void *tri_ctx;
 } tr_job;
 
 /* Moeller-Trumbore on the precomputed record (same ops as intersection.cpp:114-129) */
@@ -427,11 +429,11 @@ static inline int tri_test(const float *r, const float o[3], const float d[3], i
 
 /* cull: 0 none, 1 every back face, 2 back faces of triangles not flagged in twosided[prim] */
 static void trace_one_ex(const orc_bvh *b, const orc_ray *ray, int cull, const uint8_t *twosided, int any,
-                         orc_hit *hit, uint32_t *occ, uint64_t *nv, uint64_t *nt);
+                         orc_hit *hit, uint32_t *occ, uint64_t *nv, uint64_t *nt, orc_tri_fn fn, void *fn_ctx);
 static void trace_one(const orc_bvh *b, const orc_ray *ray, int cull, int any, orc_hit *hit, uint32_t *occ,
-                      uint64_t *nv, uint64_t *nt)
+                      uint64_t *nv, uint64_t *nt, orc_tri_fn fn, void *fn_ctx)
 {
-    trace_one_ex(b, ray, cull ? 1 : 0, NULL, any, hit, occ, nv, nt);
+    trace_one_ex(b, ray, cull ? 1 : 0, NULL, any, hit, occ, nv, nt, fn, fn_ctx);
 }
 
 void orc_bvh_trace1(const orc_bvh *b, const orc_ray *ray, int cull_mode, const uint8_t *twosided, int any,
@@ -444,11 +446,11 @@ void orc_bvh_trace1(const orc_bvh *b, const orc_ray *ray, int cull_mode, const u
         if(occ) *occ = 0;
         return;
     }
-    trace_one_ex(b, ray, cull_mode, twosided, any, hit, occ, &nv, &nt);
+    trace_one_ex(b, ray, cull_mode, twosided, any, hit, occ, &nv, &nt, NULL, NULL);
 }
 
 static void trace_one_ex(const orc_bvh *b, const orc_ray *ray, int cull_mode, const uint8_t *twosided, int any,
-                         orc_hit *hit, uint32_t *occ, uint64_t *nv, uint64_t *nt)
+                         orc_hit *hit, uint32_t *occ, uint64_t *nv, uint64_t *nt, orc_tri_fn fn, void *fn_ctx)
 {
     float inv_d[3];
     int neg[3];
@@ -530,7 +532,16 @@ static void trace_one_ex(const orc_bvh *b, const orc_ray *ray, int cull_mode, co
                 float t, u, v;
                 ++tests;
                 int cull = cull_mode == 1 || (cull_mode == 2 && !(twosided && twosided[prim]));
-                if(!tri_test(r, ray->o, ray->d, cull, &t, &u, &v)) continue;
+                if(fn)
+                {
+                    /* caller's triangle test on the original triangle (no culling on this path) */
+                    float tuv[3];
+                    if(fn(fn_ctx, prim, ray->o, ray->d, tuv) != 1) continue;
+                    t = tuv[0];
+                    u = tuv[1];
+                    v = tuv[2];
+                }
+                else if(!tri_test(r, ray->o, ray->d, cull, &t, &u, &v)) continue;
                 if(!(t > ray->tmin && t < ray->tmax)) continue;
                 if(any)
                 {
@@ -579,7 +590,7 @@ static void *tr_worker(void *arg)
         uint32_t end = begin + 64u < j->nray ? begin + 64u : j->nray;
         for(uint32_t r = begin; r < end; ++r)
             trace_one(j->b, &j->rays[r], j->cull, j->occluded != NULL, j->hits ? &j->hits[r] : NULL,
-                      j->occluded ? &j->occluded[r] : NULL, &nv, &nt);
+                      j->occluded ? &j->occluded[r] : NULL, &nv, &nt, j->tri_fn, j->tri_ctx);
     }
     atomic_fetch_add(&j->visits, nv);
     atomic_fetch_add(&j->tests, nt);
@@ -595,7 +606,21 @@ int orc_bvh_closest_hit(const orc_bvh *b, const orc_ray *rays, uint32_t nray, or
         if(stats) stats[0] = stats[1] = 0;
         return 1;
     }
-    tr_job j = {b, rays, nray, hits, NULL, cull_back, 0, 0, 0};
+    tr_job j = {b, rays, nray, hits, NULL, cull_back, 0, 0, 0, NULL, NULL};
+    int n = orc__run_threads(tr_worker, &j, nthreads);
+    if(stats)
+    {
+        stats[0] = atomic_load(&j.visits);
+        stats[1] = atomic_load(&j.tests);
+    }
+    return n;
+}
+
+int orc_bvh_closest_hit_fn(const orc_bvh *b, const orc_ray *rays, uint32_t nray, orc_hit *hits, int nthreads,
+                           orc_tri_fn fn, void *fn_ctx, uint64_t *stats)
+{
+    if(b->num_tris == 0 || fn == NULL) return orc_bvh_closest_hit(b, rays, nray, hits, nthreads, 0, stats);
+    tr_job j = {b, rays, nray, hits, NULL, 0, 0, 0, 0, fn, fn_ctx};
     int n = orc__run_threads(tr_worker, &j, nthreads);
     if(stats)
     {
@@ -613,6 +638,6 @@ int orc_bvh_any_hit(const orc_bvh *b, const orc_ray *rays, uint32_t nray, uint32
         memset(occluded, 0, 4 * (size_t)nray);
         return 1;
     }
-    tr_job j = {b, rays, nray, NULL, occluded, cull_back, 0, 0, 0};
+    tr_job j = {b, rays, nray, NULL, occluded, cull_back, 0, 0, 0, NULL, NULL};
     return orc__run_threads(tr_worker, &j, nthreads);
 }

@@ -106,6 +106,11 @@ int orc_bvh_closest_hit(const orc_bvh *b, const orc_ray *rays, uint32_t nray, or
                         int cull_back, uint64_t *stats /* [2]: node visits, tri tests; may be NULL */);
 int orc_bvh_any_hit(const orc_bvh *b, const orc_ray *rays, uint32_t nray, uint32_t *occluded, int nthreads,
                     int cull_back);
+/* closest hit over the same BVH with the triangle test supplied by the caller: fn(ctx, prim, o, d, tuv)
+   returns 1 (INTERSECT) with tuv = {t, u, v} for the triangle with original index prim. No culling. */
+typedef int (*orc_tri_fn)(void *ctx, uint32_t prim, const float o[3], const float d[3], float tuv[3]);
+int orc_bvh_closest_hit_fn(const orc_bvh *b, const orc_ray *rays, uint32_t nray, orc_hit *hits, int nthreads,
+                           orc_tri_fn fn, void *fn_ctx, uint64_t *stats);
 /* single ray; cull_mode 0 none, 1 all back faces, 2 back faces of triangles with twosided[prim] == 0 */
 void orc_bvh_trace1(const orc_bvh *b, const orc_ray *ray, int cull_mode, const uint8_t *twosided, int any,
                     orc_hit *hit, uint32_t *occ);

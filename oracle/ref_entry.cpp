@@ -109,6 +109,40 @@ uint32_t vkref_triangle_triangle_overlap(const float a[9], const float b[9])
     return vierkant::intersect(t1, t2);
 }
 
+// Triangle soup for the CPU BVH traversal (oracle/lbvh.c, orc_bvh_closest_hit_fn): the oracle's BVH
+// decides which triangles a ray meets, and every triangle test is the reference's
+// vierkant::intersect(const Triangle&, const Ray&) (intersection.cpp:114-129) on the original vertices.
+void *vkref_mesh_create(const float *xyz, const uint32_t *indices, uint32_t num_tris)
+{
+    auto *tris = new std::vector<vierkant::Triangle>(num_tris);
+    for(uint32_t i = 0; i < num_tris; ++i)
+    {
+        for(int k = 0; k < 3; ++k)
+        {
+            const float *p = xyz + 3 * size_t(indices[3 * size_t(i) + k]);
+            (*tris)[i][k] = glm::vec3(p[0], p[1], p[2]);
+        }
+    }
+    return tris;
+}
+
+void vkref_mesh_destroy(void *mesh) { delete static_cast<std::vector<vierkant::Triangle> *>(mesh); }
+
+// orc_tri_fn: 1 (INTERSECT) with {t, u, v}, else 0; the stored direction is used as given
+int vkref_mesh_intersect(void *mesh, uint32_t prim, const float o[3], const float d[3], float tuv[3])
+{
+    const auto &tris = *static_cast<const std::vector<vierkant::Triangle> *>(mesh);
+    vierkant::Ray ray;
+    ray.origin = glm::vec3(o[0], o[1], o[2]);
+    ray.direction = glm::vec3(d[0], d[1], d[2]);
+    auto res = vierkant::intersect(tris[prim], ray);
+    if(res.type != vierkant::INTERSECT) { return 0; }
+    tuv[0] = res.distance;
+    tuv[1] = res.u;
+    tuv[2] = res.v;
+    return 1;
+}
+
 // Brute-force closest hit over all host threads (num_threads <= 0: hardware_concurrency).
 // Triangles are gathered from an indexed mesh (fp32 xyz, uint32 indices, Geometry.hpp:14).
 int vkref_closest_hit_bruteforce(const float *xyz, const uint32_t *indices, uint32_t num_tris, const void *rays_v,
