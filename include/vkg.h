@@ -730,12 +730,6 @@ vkg_status vkg_nrc_load_params(vkg_nrc *nrc, const float *d_mlp, const float *d_
  * records their first train_depth interactions together with the radiance that followed each,
  * and runs train_steps optimiser steps on batches of batch_size records, all on `stream`. */
 vkg_status vkg_tracer_attach_cache(vkg_tracer *tracer, vkg_nrc *cache);
-/* diagnostic: D (128 x n FP32, row-major) = A (128 x k BF16, row-major) * B^T (n x k BF16, row-major)
- * with one tcgen05.mma chain through the library's shared-memory descriptors (16 <= n <= 64,
- * k <= 256, both multiples of 16); *d_err (device) gets bit 0 if the completion wait ran out */
-vkg_status vkg_diag_tc_gemm(vkg_ctx *ctx, const uint16_t *d_a, const uint16_t *d_b, uint32_t k, uint32_t n, float *d_d,
-                            uint32_t *d_err, void *stream);
-
 #ifdef __cplusplus
 }
 #endif

@@ -1,27 +1,31 @@
-"""The C ABI library loads and exports every entry point declared in include/vkg.h (no GPU calls)."""
+"""The C ABI library loads and exports every entry point declared in include/*.h (the drop-in vkg.h and
+the test-only vkg_diag.h), with no GPU calls."""
 import re
 from pathlib import Path
 
 from vierkant_gb300 import _lib
 
-HEADER = Path(__file__).resolve().parents[1] / "include" / "vkg.h"
+HEADERS = sorted((Path(__file__).resolve().parents[1] / "include").glob("*.h"))
 
 
 def declared_functions():
-    text = HEADER.read_text()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(vkg_[a-z0-9_]+)\s*\(", text)))
+    names = set()
+    for h in HEADERS:
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names |= set(re.findall(r"\b(vkg_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
 
 
 def test_header_declares_entry_points():
     names = declared_functions()
     assert "vkg_closest_hit" in names and "vkg_bvh_build" in names and "vkg_intersect_ray_triangle" in names
+    assert "vkg_diag_wait_timeout" in names and len(HEADERS) >= 2
 
 
 def test_library_exports_every_declared_symbol():
     L = _lib.lib()
     missing = [n for n in declared_functions() if not hasattr(L, n)]
-    assert not missing, f"declared in vkg.h but not exported: {missing}"
+    assert not missing, f"declared in include/*.h but not exported: {missing}"
 
 
 def test_bindings_cover_header():

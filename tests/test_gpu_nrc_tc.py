@@ -128,3 +128,33 @@ def test_tc_training_fits_like_fp32(ctx):
         c.close()
     print("held-out relative error fp32 / tcgen05 weight gradients:", errs)
     assert errs[1] < 0.18 and abs(errs[1] - errs[0]) < 0.06
+
+
+def _wait_probe(ctx, num_ctas, limit_ns):
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    elapsed = torch.zeros(1, dtype=torch.int64, device="cuda")
+    _lib.check(_lib.lib().vkg_diag_wait_timeout(ctx.handle, num_ctas, limit_ns, C.c_void_p(err.data_ptr()),
+                                                C.c_void_p(elapsed.data_ptr()), C.c_void_p(ctx.stream())),
+               ctx.handle, "vkg_diag_wait_timeout")
+    torch.cuda.synchronize()
+    return err.item(), elapsed.item()
+
+
+def test_bounded_wait_runs_out_and_returns(ctx):
+    """A wait that nothing ends gives up after its limit: the kernel sets the error bit, takes the
+    second bounded wait of the error path, frees its TMEM and returns; the context stays usable and
+    the tcgen05 kernels that follow allocate TMEM and run normally."""
+    limit = 2_000_000  # 2 ms instead of the kernels' 1 s
+    for num_ctas in (1, 2 * 152):
+        err, elapsed = _wait_probe(ctx, num_ctas, limit)
+        assert err == 1
+        # both waits of a CTA ran to their limit, and no CTA hung beyond it
+        assert 2 * limit <= elapsed < 50 * limit, elapsed
+    # TMEM was freed: tcgen05 kernels after the probe still allocate, multiply and finish in time
+    test_tc_gemm_matches_fp32_matmul(ctx, 64, 64)
+    cache = NeuralRadianceCache(ctx, NeuralRadianceCache.default_config())
+    x, _ = random_features(4096, seed=3)
+    cache.infer(x)
+    torch.cuda.synchronize()
+    assert cache.info().kernel_error == 0
+    cache.close()

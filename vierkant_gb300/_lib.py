@@ -275,6 +275,7 @@ SIGNATURES = {
     "vkg_batch_statistics": (I32, [P, C.POINTER(vkg_batch_stats)]),
     "vkg_batch_destroy": (I32, [P]),
     "vkg_diag_tc_gemm": (I32, [P, P, P, U32, U32, P, P, P]),
+    "vkg_diag_wait_timeout": (I32, [P, U32, U64, P, P, P]),
     "vkg_nrc_config_default": (I32, [C.POINTER(vkg_nrc_config)]),
     "vkg_nrc_create": (I32, [P, C.POINTER(vkg_nrc_config), C.POINTER(P)]),
     "vkg_nrc_destroy": (I32, [P]),

@@ -2,6 +2,7 @@
 #pragma once
 
 #include "../../include/vkg.h"
+#include "../../include/vkg_diag.h"
 #include "vkg_common.cuh"
 
 #include <cuda_runtime.h>

@@ -251,6 +251,38 @@ __global__ void __launch_bounds__(TC_THREADS)
     if(warp == 0) tc::tmem_dealloc(tmem, TC_TMEM_COLS);
 }
 
+// diagnostic: the error path every tcgen05 kernel here takes when a wait runs out, run to its end on
+// purpose. Each CTA allocates TMEM and waits on an mbarrier that nothing arrives on, with a limit of
+// limit_ns instead of the kernels' 1 s; the wait gives up, the CTA sets TC_TIMEOUT, waits a second
+// time (bounded, as the kernels do for MMAs in flight), frees its TMEM and returns. elapsed_ns: the
+// longest time one CTA spent in the two waits.
+constexpr uint32_t PROBE_TMEM_COLS = 32;
+__global__ void __launch_bounds__(TC_THREADS)
+        k_wait_probe(uint64_t limit_ns, uint32_t *__restrict__ err, unsigned long long *__restrict__ elapsed_ns)
+{
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tslot;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    if(warp == 0) tc::tmem_alloc(&tslot, PROBE_TMEM_COLS);
+    if(tid == 0) tc::mbar_init(&mbar, 1);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tslot;
+    const uint64_t t0 = tc::global_ns();
+    const bool ok = tc::mbar_wait_for(&mbar, 0, tc::WAIT_LIMIT, limit_ns);
+    if(__syncthreads_or(!ok))
+    {
+        if(tid == 0) atomicOr(err, TC_TIMEOUT);
+        tc::mbar_wait_for(&mbar, 0, tc::WAIT_LIMIT, limit_ns);
+    }
+    if(tid == 0) atomicMax(elapsed_ns, (unsigned long long)(tc::global_ns() - t0));
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if(warp == 0) tc::tmem_dealloc(tmem, PROBE_TMEM_COLS);
+}
+
 // ---- weight gradients on tcgen05 --------------------------------------------------------------
 // dW_l[k][o] = sum over records s of H_l[s][k] * G_l[s][o] (H_0 = the encoded inputs X, G_l the
 // gradient of layer l's pre-activation, both BF16 as the backward stored them). As one UMMA chain per
@@ -454,6 +486,19 @@ vkg_status nrc_infer_tc(vkg_ctx *ctx, const grid_config &gc, const __half2 *grid
 }// namespace vkg
 
 using namespace vkg;
+
+extern "C" vkg_status vkg_diag_wait_timeout(vkg_ctx *ctx, uint32_t num_ctas, uint64_t limit_ns, uint32_t *d_err,
+                                            uint64_t *d_elapsed_ns, void *stream)
+{
+    if(!ctx) return VKG_ERR_INVALID_ARGUMENT;
+    if(!d_err || !d_elapsed_ns || num_ctas == 0 || num_ctas > 4096 || limit_ns == 0 || limit_ns > 100000000ull)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
+                         "vkg_diag_wait_timeout: need 1 <= num_ctas <= 4096 and 0 < limit_ns <= 1e8");
+    if(vkg_status s = bind_device(ctx); s != VKG_OK) return s;
+    nrc::k_wait_probe<<<num_ctas, nrc::TC_THREADS, 0, static_cast<cudaStream_t>(stream)>>>(
+            limit_ns, d_err, reinterpret_cast<unsigned long long *>(d_elapsed_ns));
+    return cuda_check(ctx, cudaGetLastError(), "k_wait_probe");
+}
 
 extern "C" vkg_status vkg_diag_tc_gemm(vkg_ctx *ctx, const uint16_t *d_a, const uint16_t *d_b, uint32_t k,
                                        uint32_t n, float *d_d, uint32_t *d_err, void *stream)

@@ -47,17 +47,23 @@ __device__ __forceinline__ uint64_t global_ns()
     return t;
 }
 
-// true once the phase with the given parity completed; false when the wait runs out
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+// true once the phase with the given parity completed; false after max_tries attempts or max_ns
+__device__ __forceinline__ bool mbar_wait_for(uint64_t *bar, uint32_t parity, uint32_t max_tries, uint64_t max_ns)
 {
     if(mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = global_ns();
-    for(uint32_t i = 0; i < WAIT_LIMIT; ++i)
+    for(uint32_t i = 0; i < max_tries; ++i)
     {
         if(mbar_try_wait(bar, parity)) return true;
-        if((i & 255u) == 255u && global_ns() - t0 > WAIT_NS) return false;
+        if((i & 255u) == 255u && global_ns() - t0 > max_ns) return false;
     }
     return false;
+}
+
+// the kernels' wait: at most WAIT_LIMIT attempts or WAIT_NS
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    return mbar_wait_for(bar, parity, WAIT_LIMIT, WAIT_NS);
 }
 
 // ---- TMEM ----------------------------------------------------------------------------------------
