@@ -329,7 +329,8 @@ def run_ours(args):
         c1 = config1_block(ctx, args, run_cpu=(ws == 1 and not args.no_cpu))
     pt_block = batch_block = stress = features = None
     if rank == 0 and not args.no_pt:
-        pt_block = path_tracer_block(ctx, frames=args.nrc_frames)
+        pt_block = path_tracer_block(ctx, frames=args.nrc_frames, bytes_per_ray=bytes_per_launch / n,
+                                     cpu=(ws == 1 and not args.no_cpu))
         batch_block = batched_block(ctx)
         stress = stress_block(ctx)
         features = features_block(ctx)
@@ -425,7 +426,48 @@ def post_fx_timing(ctx, rgb, w, h, reps=20):
             "frac_of_hbm": round(byts / ms / 1e6 / peak, 3), "peak": src}
 
 
-def path_tracer_block(ctx, frames=256):
+def pt_cpu_baseline(sc, scene, env, pt_settings_crop, spp=4, budget_s=12.0):
+    """The estimator on the host cores: the oracle's FP32 twin of the tracer (the same arithmetic,
+    BVH hits, alias-table environment sampling and PCG32 streams, oracle/pathtrace.c) over all threads
+    on the 128x128 crop of the 1280x720 frame, 6 segments, roulette from the 3rd interaction; samples
+    (paths) per second, repeated until about budget_s."""
+    import numpy as np
+    import oracle
+    from vierkant_gb300.raytracing import _cudart
+    import ctypes as C
+
+    def d2h(ptr_, nbytes, dtype):
+        a = np.empty(nbytes // np.dtype(dtype).itemsize, dtype)
+        _cudart().cudaMemcpy(a.ctypes.data_as(C.c_void_p), C.c_void_p(ptr_), C.c_size_t(nbytes), 2)
+        return a
+
+    wptr, aptr, W, H = scene.env_tables()
+    n = W * H
+    w = d2h(wptr, 4 * n, np.float32)
+    tab = d2h(aptr, 8 * n, np.uint32).reshape(n, 2)
+    prob = np.ascontiguousarray(tab[:, 0].view(np.float32))
+    alias = np.ascontiguousarray(tab[:, 1])
+    env = env.cpu().numpy()
+    bvh = oracle.CpuBVH(sc["xyz"], sc["indices"], 2)
+    th = float(np.float32(math.tan(math.radians(45.0) / 2.0)))
+    cam = oracle.camera((0, 0, 3.4), (0, 0, 0), (0, 1, 0), th, 1280, 720)
+    total, paths, batches = 0.0, 0, 0
+    while total < budget_s or batches < 2:
+        t0 = time.perf_counter()
+        oracle.pt_render(False, sc["xyz"], sc["indices"], sc["tri_material"], sc["materials"], bvh, env, cam, spp,
+                         seed=SEED, batch=batches, rr_depth=3, crop=pt_settings_crop, alias_prob=prob, alias=alias,
+                         weight=w)
+        total += time.perf_counter() - t0
+        paths += pt_settings_crop[2] * pt_settings_crop[3] * spp
+        batches += 1
+    return {"value": round(paths / total, 1), "unit": "samples/s", "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": f"{batches} x {spp} spp on the 128x128 crop at ({pt_settings_crop[0]}, {pt_settings_crop[1]}), "
+                      f"{total:.1f} s",
+            "method": "the oracle's FP32 twin of the tracer (oracle/pathtrace.c) on all host threads; the reference "
+                      "has no CPU path tracer (its estimator runs in Vulkan ray-tracing shaders)"}
+
+
+def path_tracer_block(ctx, frames=256, bytes_per_ray=None, cpu=True):
     """The radiance estimator on the same scene: the plain tracer at 1280x720 x 64 spp (samples/s,
     Mrays/s, RMSE / bias against the FP64 oracle crop), and the equal-RMSE comparison at 1920x1080:
     GPU time for the plain tracer's 64-spp image vs the radiance-cache tracer (1 spp per frame, trained
@@ -460,6 +502,18 @@ def path_tracer_block(ctx, frames=256):
                                "mrays_per_s": round(rays / st.total_ms / 1e3, 1), "rays": int(rays),
                                "rmse": round(rmse, 4), "bias": round(bias, 5),
                                "oracle": "FP64 4096 spp, 128x128 crop at (576, 528)"}
+    if bytes_per_ray:
+        peak, src = measured_peaks()
+        gbs = rays * bytes_per_ray / (st.total_ms * 1e-3) / 1e9
+        out["plain_720p_64spp"]["traversal_roofline"] = {
+            "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s", "frac": round(gbs / peak, 4), "peak_source": src,
+            "bytes_per_ray": round(bytes_per_ray, 1),
+            "note": "extension + shadow rays x the algorithmic bytes per ray of the closest-hit batch (camera and "
+                    "bounce rays of this scene) over the whole frame time, shading included: a lower bound for "
+                    "the traversal kernels alone (their share of a frame: "
+                    "profiles/path_tracer_cornell_720p_4spp_launches.md)"}
+    if cpu:
+        out["plain_720p_64spp"]["cpu_baseline"] = pt_cpu_baseline(sc, scene, env, pt_settings_crop=(576, 528, 128, 128))
     out["denoise_720p"] = denoise_timing(ctx, pt.pixel_data(), 1280, 720)
     out["post_fx_720p"] = post_fx_timing(ctx, pt.render_scene(scene, cam), 1280, 720)
     pt.close()

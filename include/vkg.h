@@ -272,10 +272,14 @@ vkg_status vkg_bvh_info_get(const vkg_bvh *bvh, vkg_bvh_info *out);
  *   - at most VKG_NOALLOC_MAX_TRIS triangles; larger inputs return VKG_ERR_CAPACITY
  *   - the caller provides d_nodes (node_capacity >= num_tris nodes of 96 B, 16-byte aligned),
  *     d_tris (num_tris records of 48 B, 16-byte aligned) and d_info (16 uint32 words, device):
- *     [0] node count, [1] depth, [2] error flags (1: an index >= num_vertices, 2: node capacity),
- *     [3] box margin (float bits), [4..6] scene min, [7..9] scene max (float bits)
+ *     [0] node count, [1] depth, [2] error flags (1: an index >= num_vertices, 2: node capacity,
+ *     4: the tree is deeper than the library's traversal supports -- vkg_bvh_build refuses such a
+ *     tree with VKG_ERR_CAPACITY), [3] box margin (float bits), [4..6] scene min, [7..9] scene max
  *   - works on the current CUDA device; its first call on a device looks up the array's device
- *     address (cudaGetSymbolAddress), so make that first call before any stream capture
+ *     address (cudaGetSymbolAddress), so make that first call before any stream capture; the
+ *     address is kept per device for the life of the process and assumes the device's primary
+ *     context (after cudaDeviceReset, or under another context made current through the driver
+ *     API, it is stale)
  *   - all calls share the one array: calls that overlap on the GPU (other streams, other threads)
  *     race and must be serialised by the caller
  *   - asynchronous on `stream`; no vkg_ctx (no error message: the status code says what failed) */

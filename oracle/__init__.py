@@ -441,6 +441,33 @@ def pt_render(fp64, xyz, idx, tri_mat, mats, bvh: "CpuBVH", env_rgb, cam, spp, *
     return out, sq, (int(stats[0]), int(stats[1]))
 
 
+def pt_variance_split(xyz, idx, tri_mat, mats, bvh: "CpuBVH", env_rgb, cam, spp, fork_depth, *, seed=0x5EED,
+                      max_depth=6, rr_depth=3, mis_mode=0, crop=(0, 0, 0, 0), nthreads=0):
+    """FP64 variance split at the surface reached by segment fork_depth (orc_pt_variance_split):
+    [h, w, 4] float64 {mean luminance, per-sample variance of the plain estimator, the tail variance an
+    exact cache there would remove, fraction of samples reaching it}, and (extension, shadow) rays of
+    one trace per sample."""
+    L = orc()
+    L.orc_pt_variance_split.argtypes = [C.POINTER(orc_pt_scene), C.POINTER(orc_bvh), C.POINTER(orc_pt_env),
+                                        C.POINTER(orc_camera), C.POINTER(orc_pt_settings), C.c_uint32, C.c_void_p,
+                                        C.c_void_p, C.c_int]
+    keep = [np.ascontiguousarray(a) for a in (xyz, idx, tri_mat, mats)]
+    scene = orc_pt_scene(ptr(keep[0]), ptr(keep[1]), ptr(keep[2]), ptr(keep[3]), keep[1].shape[0], len(mats))
+    rgb = np.ascontiguousarray(env_rgb, np.float32)
+    h, w = rgb.shape[:2]
+    weight, cdf = env_tables_fp64(rgb)
+    env = orc_pt_env(ptr(rgb), ptr(np.ascontiguousarray(weight, np.float32)), None, None, ptr(cdf), w, h)
+    cw = crop[2] or cam.width
+    ch = crop[3] or cam.height
+    st, _keep = _settings(seed, 0, spp, max_depth, rr_depth, mis_mode, 1, 0.0, 1.0, crop, None, False, None, 0.1,
+                          None, None)
+    out = np.zeros((ch, cw, 4), np.float64)
+    stats = np.zeros(2, np.uint64)
+    L.orc_pt_variance_split(C.byref(scene), C.byref(bvh.b), C.byref(env), C.byref(cam), C.byref(st), fork_depth,
+                            ptr(out), ptr(stats), nthreads)
+    return out, (int(stats[0]), int(stats[1]))
+
+
 class orc_pt_instances(C.Structure):
     _fields_ = [("mesh_bvh", C.c_void_p), ("mesh_xyz", C.c_void_p), ("mesh_idx", C.c_void_p),
                 ("mesh_nvert", C.c_void_p), ("mesh_twosided", C.c_void_p), ("num_meshes", C.c_uint32),

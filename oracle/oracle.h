@@ -212,6 +212,13 @@ int orc_pt_render(int fp64, const orc_pt_scene *scene, const orc_bvh *bvh, const
                   const orc_camera *cam, const orc_pt_settings *set, double *out, double *sq, uint64_t *stats,
                   int nthreads);
 /* the same for an instanced scene (FP64 oracle only; scene supplies the materials) */
+/* variance split of the FP64 estimator at the surface reached by segment fork_depth (a radiance cache
+   ending paths there): split[pixel] = {mean luminance, per-sample variance, tail variance an exact cache
+   would remove, fraction of samples reaching the fork}; stats: extension / shadow rays of the first
+   trace of each sample */
+int orc_pt_variance_split(const orc_pt_scene *scene, const orc_bvh *bvh, const orc_pt_env *env, const orc_camera *cam,
+                          const orc_pt_settings *set, uint32_t fork_depth, double *split, uint64_t *stats,
+                          int nthreads);
 int orc_pt_render_instanced(const orc_pt_scene *scene, const orc_pt_instances *inst, const orc_pt_env *env,
                             const orc_camera *cam, const orc_pt_settings *set, double *out, double *sq,
                             uint64_t *stats, int nthreads);

@@ -116,6 +116,8 @@ typedef struct {
     atomic_uint next;
     atomic_ullong ext, shadow;
     int fp64;
+    uint32_t fork_depth; /* the variance split's fork segment (orc_pt_variance_split) */
+    double *split;       /* [pixels][4] of orc_pt_variance_split */
 } orc_pt_job;
 
 /* ---- FP32 twin hooks ------------------------------------------------------------------------ */
@@ -805,14 +807,14 @@ static void *pt_worker(void *arg)
             int hit0 = 0;
             if(J->fp64)
             {
-                d_v3 r = d_trace_path(J, x, y, seq, st, rec, &hit0);
+                d_v3 r = d_trace_path(J, x, y, seq, st, rec, &hit0, NULL);
                 L[0] = r.x;
                 L[1] = r.y;
                 L[2] = r.z;
             }
             else
             {
-                f_v3 r = f_trace_path(J, x, y, seq, st, rec, &hit0);
+                f_v3 r = f_trace_path(J, x, y, seq, st, rec, &hit0, NULL);
                 L[0] = r.x;
                 L[1] = r.y;
                 L[2] = r.z;
@@ -878,6 +880,105 @@ int orc_pt_render(int fp64, const orc_pt_scene *scene, const orc_bvh *bvh, const
     atomic_init(&J.ext, 0ull);
     atomic_init(&J.shadow, 0ull);
     int n = orc__run_threads(pt_worker, &J, nthreads);
+    if(stats)
+    {
+        stats[0] = atomic_load(&J.ext);
+        stats[1] = atomic_load(&J.shadow);
+    }
+    free(ts);
+    free(media);
+    return n;
+}
+
+/* ---- variance split (FP64): how much of a pixel's variance a radiance cache could remove --------
+   Each sample traces its path twice with the same random numbers up to the surface that segment
+   fork_depth reaches, and with independent streams after it (d_fork). With L = prefix + tail:
+     var_plain = Var(lum L)                      per-sample variance of the plain estimator
+     var_tail  = E[(lum L_a - lum L_b)^2 / 2]    = E[Var(lum tail | prefix)], the part an exact cache
+                                                  at that surface (zero variance) would remove
+   split[pix] = {mean lum L_a, var_plain, var_tail, fraction of samples that reached the fork}. */
+static void *pt_split_worker(void *arg)
+{
+    orc_pt_job *J = (orc_pt_job *)arg;
+    const uint32_t npix = J->cw * J->ch;
+    uint64_t st[2] = {0, 0};
+    for(;;)
+    {
+        uint32_t pix = atomic_fetch_add(&J->next, 1u);
+        if(pix >= npix) break;
+        uint32_t x = J->cx0 + pix % J->cw, y = J->cy0 + pix / J->cw;
+        double s1 = 0, s2 = 0, tail = 0, forks = 0;
+        for(uint32_t s = 0; s < J->spp; ++s)
+        {
+            uint64_t seq = ((uint64_t)J->batch << 40) ^ ((uint64_t)s * npix + pix);
+            uint64_t fseq = (1ull << 61) | (2ull * ((uint64_t)s * npix + pix));
+            int hit0 = 0;
+            d_fork fa = {fseq, {0, 0, 0}, 0}, fb = {fseq + 1, {0, 0, 0}, 0};
+            d_v3 a = d_trace_path(J, x, y, seq, st, NULL, &hit0, &fa);
+            d_v3 b = d_trace_path(J, x, y, seq, NULL, NULL, &hit0, &fb);
+            double la = 0.2126 * a.x + 0.7152 * a.y + 0.0722 * a.z;
+            double lb = 0.2126 * b.x + 0.7152 * b.y + 0.0722 * b.z;
+            s1 += la;
+            s2 += la * la;
+            tail += 0.5 * (la - lb) * (la - lb);
+            forks += fa.forked ? 1 : 0;
+        }
+        double n = (double)J->spp, m = s1 / n;
+        double *o = J->split + 4 * (size_t)pix;
+        o[0] = m;
+        o[1] = n > 1 ? (s2 - n * m * m) / (n - 1) : 0;
+        o[2] = tail / n;
+        o[3] = forks / n;
+    }
+    atomic_fetch_add(&J->ext, st[0]);
+    atomic_fetch_add(&J->shadow, st[1]);
+    return NULL;
+}
+
+int orc_pt_variance_split(const orc_pt_scene *scene, const orc_bvh *bvh, const orc_pt_env *env, const orc_camera *cam,
+                          const orc_pt_settings *set, uint32_t fork_depth, double *split, uint64_t *stats,
+                          int nthreads)
+{
+    uint8_t *ts = (uint8_t *)calloc(scene->ntri ? scene->ntri : 1, 1);
+    for(uint32_t i = 0; i < scene->ntri; ++i)
+    {
+        uint32_t m = scene->tri_mat[i];
+        ts[i] = (m < scene->nmat && orc_material_unculled(&scene->mats[m])) ? 1 : 0;
+    }
+    orc_pt_job J;
+    memset(&J, 0, sizeof(J));
+    J.scene = scene;
+    J.bvh = bvh;
+    J.env = env;
+    J.cam = cam;
+    J.twosided = ts;
+    J.seed = set->seed;
+    J.batch = set->batch;
+    J.spp = set->spp;
+    J.max_depth = set->max_depth;
+    J.rr_depth = set->rr_depth;
+    J.mis_mode = set->mis_mode;
+    J.disable_material = set->disable_material;
+    J.draw_skybox = set->draw_skybox;
+    J.max_path_beta = set->max_path_beta;
+    J.environment = set->environment;
+    J.lights = set->lights;
+    J.num_lights = set->lights ? set->num_lights : 0;
+    J.suppress_caustics = set->suppress_caustics;
+    J.clip_near = set->clip_near > 0.f ? set->clip_near : 0.1f;
+    orc_medium *media = orc_media_table(scene, set, &J.cam_medium);
+    J.media = media;
+    J.cx0 = set->crop[0];
+    J.cy0 = set->crop[1];
+    J.cw = set->crop[2] ? set->crop[2] : cam->width;
+    J.ch = set->crop[3] ? set->crop[3] : cam->height;
+    J.fp64 = 1;
+    J.fork_depth = fork_depth;
+    J.split = split;
+    atomic_init(&J.next, 0u);
+    atomic_init(&J.ext, 0ull);
+    atomic_init(&J.shadow, 0ull);
+    int n = orc__run_threads(pt_split_worker, &J, nthreads);
     if(stats)
     {
         stats[0] = atomic_load(&J.ext);

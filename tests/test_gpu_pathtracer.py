@@ -17,6 +17,7 @@ import pytest
 import torch
 
 import oracle
+from radiance_stats import check, compare, render_batches, report
 from vierkant_gb300 import _lib, geometry
 from vierkant_gb300.pathtracer import PBRPathTracer, Scene, procedural_sky, sun_direction
 
@@ -120,23 +121,15 @@ def test_twin_parity_path_for_path(ctx, world):
 
 
 def test_radiance_against_fp64_oracle(ctx, world, golden):
+    """16 independent 64-spp batches against the FP64 crop (4096 spp): the luminance bias is within 3
+    standard errors of zero and the RMSE within 1.2x the noise of the two estimates (radiance_stats)"""
     g = golden("pt_oracle_crop")
-    ref = g["mean"].astype(np.float64)
     assert tuple(g["crop"]) == CROP
-    pt = PBRPathTracer(ctx, seed=0x5EED, settings=settings(64, CROP))
-    for _ in range(4):  # 4 batches x 64 spp, running mean
-        img = pt.render_scene(world["scene"], world["cam"])
-    assert pt.current_batch() == 4
-    img = img.cpu().numpy().astype(np.float64)
-    pt.close()
-    spp = 256
-    bias = (img.sum() - ref.sum()) / ref.sum()
-    lum = lambda a: 0.2126 * a[..., 0] + 0.7152 * a[..., 1] + 0.0722 * a[..., 2]
-    rmse = math.sqrt(np.mean((lum(img) - lum(ref)) ** 2))
-    expected = math.sqrt(np.mean(g["lum_var"]) / spp + np.mean(g["lum_var"]) / int(g["spp"]))
-    print(f"bias {bias:+.4f}  rmse {rmse:.4f}  expected noise {expected:.4f}")
-    assert abs(bias) < 0.02, bias
-    assert rmse < 2.5 * expected, (rmse, expected)
+    imgs = render_batches(lambda seed: PBRPathTracer(ctx, seed=seed, settings=settings(64, CROP)),
+                          world["scene"], world["cam"], 16)
+    st = compare(imgs, g["mean"], g["lum_var"], int(g["spp"]))
+    report("Cornell crop vs FP64 oracle", st)
+    check(st)
 
 
 def test_mis_modes_converge_on_low_dynamic_range_env(ctx, world):

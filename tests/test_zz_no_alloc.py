@@ -96,3 +96,45 @@ def test_noalloc_rejects_oversize_and_reports_bad_indices():
     idx = torch.tensor([[0, 1, 9]], dtype=torch.int32, device="cuda")
     st, _, _, info = _noalloc(xyz, idx)
     assert st == 0 and (info[2] & 1) == 1
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 9])
+@pytest.mark.parametrize("leaf_max", [1, 2, 4])
+def test_noalloc_small_meshes_and_leaf_sizes(n, leaf_max):
+    """1, 2 and 3 triangles (a root leaf, and trees without an internal binary level to refit) and the
+    leaf sizes 1 and 4 give the same bytes as vkg_bvh_build"""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    ctx = Context(0)
+    rng = np.random.default_rng(100 + n)
+    xyz_np = rng.normal(size=(3 * n, 3)).astype(np.float32)
+    idx_np = np.arange(3 * n, dtype=np.int32).reshape(n, 3)
+    xyz, idx = torch.from_numpy(xyz_np).cuda(), torch.from_numpy(idx_np).cuda()
+    ref = BVH(ctx, xyz, idx, leaf_max=leaf_max)
+    inf = ref.info()
+    ref_nodes = _copy_out(inf.d_nodes, inf.num_nodes * 96)
+    ref_tris = _copy_out(inf.d_tris, inf.num_tris * 48)
+    st, nodes, tris, info = _noalloc(xyz, idx, leaf_max)
+    assert st == 0 and info[2] == 0
+    assert info[0] == inf.num_nodes and info[1] == inf.depth
+    assert nodes.cpu().numpy().tobytes()[: inf.num_nodes * 96] == ref_nodes
+    assert tris.cpu().numpy().tobytes()[: inf.num_tris * 48] == ref_tris
+    ref.close()
+    ctx.close()
+
+
+def test_noalloc_rejects_small_node_capacity():
+    """a node buffer for fewer than num_tris nodes is refused before any work (num_tris nodes always
+    suffice: an 8-wide tree over n triangles has fewer than n nodes)"""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    xyz, idx = _mesh("ico")
+    n = idx.shape[0]
+    nodes = torch.zeros(((n - 1) * 96,), dtype=torch.uint8, device="cuda")
+    tris = torch.zeros((n * 48,), dtype=torch.uint8, device="cuda")
+    info = torch.zeros(16, dtype=torch.int32, device="cuda")
+    st = _lib.lib().vkg_bvh_build_noalloc(C.c_void_p(xyz.data_ptr()), xyz.shape[0], C.c_void_p(idx.data_ptr()), n,
+                                          1, C.c_void_p(nodes.data_ptr()), n - 1, C.c_void_p(tris.data_ptr()),
+                                          C.c_void_p(info.data_ptr()),
+                                          C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 1  # VKG_ERR_INVALID_ARGUMENT

@@ -1049,6 +1049,8 @@ __global__ void k_noalloc_reset(noalloc_scratch *s, uint32_t n)
 
 // info words: [0] nodes, [1] depth, [2] error flags (1 = index >= num_vertices, 2 = node capacity),
 // [3] margin (float bits), [4..6] scene min, [7..9] scene max (float bits)
+constexpr uint32_t NOALLOC_FLAG_DEPTH = 4u;
+
 __global__ void k_noalloc_info(const noalloc_scratch *s, uint32_t n, uint32_t *info)
 {
     if(threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -1057,6 +1059,8 @@ __global__ void k_noalloc_info(const noalloc_scratch *s, uint32_t n, uint32_t *i
     info[0] = s->small[8];
     info[1] = s->small[9];
     info[2] = s->small[10] | s->small[6];
+    // deeper than the traversal stack supports (the limit vkg_bvh_build enforces)
+    if(s->small[9] > (TRAVERSAL_STACK - 1) / 7 + 1) info[2] |= NOALLOC_FLAG_DEPTH;
     info[3] = __float_as_uint(s->margin[0]);
     for(int a = 0; a < 3; ++a)
     {
