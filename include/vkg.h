@@ -492,7 +492,25 @@ typedef struct vkg_settings
        raypipeline.slang:128-135): VKG_CAMERA_MEDIUM_DETECT or VKG_CAMERA_MEDIUM_GIVEN */
     uint32_t camera_medium_mode;
     vkg_medium_params camera_medium;  /* used when camera_medium_mode = VKG_CAMERA_MEDIUM_GIVEN */
+    /* random streams: VKG_RNG_PCG32 (0, default): PCG32 per path, initstate = the create-info seed,
+       initseq = (batch << 40) ^ (sample * pixels + pixel); VKG_RNG_REFERENCE (1): the reference
+       shaders' streams. In the latter, render call k takes the k-th output of the create-info
+       seed's std::minstd_rand0 (std::default_random_engine of libstdc++ and libc++,
+       PBRPathTracer.cpp:32, :588) as the batch seed; a pixel (x, y) of the full resolution starts
+       the chain xxhash32(batch seed, width * y + x) (raypipeline.slang:95), draws its sub-pixel
+       offset 2 rnd() - 1 (:100); each sample s of N draws the lens sample (2 rnd(), unused by a
+       pinhole) and jitters by frac(Hammersley(s, N) + offset) (:102-108, sampling.slang:9-13); segment
+       i hashes the chain with i (:150) and takes its uniforms from the LCG rnd() started at the
+       chain (random.slang:27-36). The samples of a pixel continue one chain, so one sample per pixel
+       is traced per wave (samples_per_wave is ignored). Not with a radiance cache. The estimator's
+       use of the uniforms (8 per segment, one per decision) is the library's either way. */
+    uint32_t rng_mode;
 } vkg_settings;
+enum
+{
+    VKG_RNG_PCG32 = 0,
+    VKG_RNG_REFERENCE = 1
+};
 /* the camera medium a render of `scene` seen from `eye` would detect: the material index, or
    0xFFFFFFFF for vacuum (always vacuum for single-level scenes, which have no objects) */
 vkg_status vkg_scene_camera_medium(const vkg_scene *scene, const float eye[3], uint32_t *material);
@@ -726,6 +744,17 @@ vkg_status vkg_nrc_train_step(vkg_nrc *nrc, const float *d_features, const float
                               float *h_loss, void *stream);
 /* overwrite the FP32 master parameters (either may be NULL) */
 vkg_status vkg_nrc_load_params(vkg_nrc *nrc, const float *d_mlp, const float *d_grid, void *stream);
+/* checkpoints (not in the reference): vkg_nrc_save writes the cache's training state -- FP32 MLP
+ * weights and hash-grid features with both Adam moments and the step count -- to one file: a
+ * 128-byte little-endian header (magic "VKGNRC01", version 1, the grid layout: levels,
+ * log2_table_size, base and max resolution, the scene box, the parameter counts, the step, the
+ * optimiser constants, the payload size and an FNV-1a 64 checksum of the payload), then the
+ * payload: MLP weights, first and second moments (num_mlp_params floats each), grid features,
+ * first and second moments (num_grid_params floats each). vkg_nrc_load reads such a file into a
+ * cache created with the same grid layout (else VKG_ERR_INVALID_ARGUMENT), checks the checksum and
+ * restores the BF16 / FP16 operand copies. Both synchronise `stream`. */
+vkg_status vkg_nrc_save(vkg_nrc *nrc, const char *path, void *stream);
+vkg_status vkg_nrc_load(vkg_nrc *nrc, const char *path, void *stream);
 /* Attach a radiance cache to a path tracer (NULL detaches; the cache must outlive its use). With a
  * cache attached, vkg_tracer_render ends every rendering path at its terminate_depth-th surface
  * interaction in the cache: the path adds throughput x (emission + predicted outgoing radiance)

@@ -153,7 +153,7 @@ def test_bounded_wait_runs_out_and_returns(ctx):
     # TMEM was freed: tcgen05 kernels after the probe still allocate, multiply and finish in time
     test_tc_gemm_matches_fp32_matmul(ctx, 64, 64)
     cache = NeuralRadianceCache(ctx, NeuralRadianceCache.default_config())
-    x, _ = random_features(4096, seed=3)
+    x = random_features(4096, seed=3)
     cache.infer(x)
     torch.cuda.synchronize()
     assert cache.info().kernel_error == 0

@@ -20,6 +20,9 @@ RAY_CULL_BACK_FACES = 1
 RAY_COUNT_STATS = 2
 
 
+RNG_PCG32, RNG_REFERENCE = 0, 1
+
+
 class VkgError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
@@ -73,7 +76,7 @@ class vkg_settings(C.Structure):
                 ("samples_per_wave", C.c_uint32), ("suppress_refractive_caustics", C.c_uint32),
                 ("sun_color", C.c_float * 3), ("sun_intensity", C.c_float), ("sun_spherical_coords", C.c_float * 2),
                 ("sun_angular_size", C.c_float), ("denoising", C.c_uint32), ("clip_near", C.c_float),
-                ("camera_medium_mode", C.c_uint32), ("camera_medium", vkg_medium_params)]
+                ("camera_medium_mode", C.c_uint32), ("camera_medium", vkg_medium_params), ("rng_mode", C.c_uint32)]
 
 
 class vkg_post_fx_settings(C.Structure):
@@ -276,6 +279,7 @@ SIGNATURES = {
     "vkg_batch_destroy": (I32, [P]),
     "vkg_diag_tc_gemm": (I32, [P, P, P, U32, U32, P, P, P]),
     "vkg_diag_wait_timeout": (I32, [P, U32, U64, P, P, P]),
+    "vkg_diag_tracer_uniforms": (I32, [P, P, U32]),
     "vkg_nrc_config_default": (I32, [C.POINTER(vkg_nrc_config)]),
     "vkg_nrc_create": (I32, [P, C.POINTER(vkg_nrc_config), C.POINTER(P)]),
     "vkg_nrc_destroy": (I32, [P]),
@@ -285,6 +289,8 @@ SIGNATURES = {
     "vkg_nrc_adam_step": (I32, [P, P]),
     "vkg_nrc_train_step": (I32, [P, P, P, U32, C.POINTER(F32), P]),
     "vkg_nrc_load_params": (I32, [P, P, P, P]),
+    "vkg_nrc_save": (I32, [P, C.c_char_p, P]),
+    "vkg_nrc_load": (I32, [P, C.c_char_p, P]),
 }
 
 _lib = None

@@ -489,6 +489,9 @@ vkg_status vkg_batch_create(vkg_ctx *ctx, const vkg_batch_job *jobs, uint32_t nj
         const vkg_batch_job &jb = jobs[j];
         if(!jb.scene) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_batch_create: job %u has no scene", j);
         if(vkg_status s = check_tracer_settings(ctx, &jb.settings); s != VKG_OK) return s;
+        if(jb.settings.rng_mode != VKG_RNG_PCG32)
+            return set_error(ctx, VKG_ERR_NOT_SUPPORTED, "vkg_batch_create: job %u: VKG_RNG_REFERENCE is a tracer mode",
+                             (unsigned)j);
         if(jb.scene->d_media || jb.settings.camera_medium_mode != VKG_CAMERA_MEDIUM_DETECT)
             return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
                              "vkg_batch_create: job %u: media are rendered by vkg_tracer_render", j);

@@ -10,6 +10,7 @@
 #include "nrc_encode.cuh"
 
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -827,6 +828,153 @@ vkg_status vkg_nrc_load_params(vkg_nrc *c, const float *d_mlp, const float *d_gr
     k_pack<<<(NFRAG + 255) / 256, 256, 0, st>>>(c->w, c->frag, c->fragT);
     if(vkg_status s = nrc_pack_tc(c->ctx, c->w, c->wtc, st); s != VKG_OK) return s;
     return cuda_check(c->ctx, cudaGetLastError(), "vkg_nrc_load_params");
+}
+
+}// extern "C"
+
+namespace
+{
+// checkpoint file header, 128 bytes little-endian
+struct nrc_ckpt_header
+{
+    char magic[8];            // "VKGNRC01"
+    uint32_t version;         // 1
+    uint32_t header_bytes;    // 128
+    uint32_t levels, log2_table_size, base_resolution, max_resolution;
+    uint32_t num_mlp_params, step;
+    uint64_t num_grid_params;
+    float learning_rate, beta1, beta2, epsilon;
+    float scene_min[3], scene_max[3];
+    uint64_t payload_bytes;
+    uint64_t checksum;        // FNV-1a 64 of the payload
+    uint8_t reserved[24];
+};
+static_assert(sizeof(nrc_ckpt_header) == 128, "checkpoint header layout");
+
+uint64_t fnv1a64(const void *data, size_t n, uint64_t h = 1469598103934665603ull)
+{
+    const auto *p = static_cast<const uint8_t *>(data);
+    for(size_t i = 0; i < n; ++i)
+    {
+        h ^= p[i];
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+nrc_ckpt_header ckpt_header(const vkg_nrc *c, uint32_t step)
+{
+    nrc_ckpt_header h{};
+    std::memcpy(h.magic, "VKGNRC01", 8);
+    h.version = 1;
+    h.header_bytes = sizeof(nrc_ckpt_header);
+    h.levels = c->cfg.levels;
+    h.log2_table_size = c->cfg.log2_table_size;
+    h.base_resolution = c->cfg.base_resolution;
+    h.max_resolution = c->cfg.max_resolution;
+    h.num_mlp_params = NPARAM;
+    h.step = step;
+    h.num_grid_params = c->ngrid;
+    h.learning_rate = c->lr;
+    h.beta1 = c->b1;
+    h.beta2 = c->b2;
+    h.epsilon = c->eps;
+    for(int a = 0; a < 3; ++a)
+    {
+        h.scene_min[a] = c->cfg.scene_min[a];
+        h.scene_max[a] = c->cfg.scene_max[a];
+    }
+    h.payload_bytes = (3ull * NPARAM + 3ull * c->ngrid) * sizeof(float);
+    return h;
+}
+}// namespace
+
+extern "C" {
+
+vkg_status vkg_nrc_save(vkg_nrc *c, const char *path, void *stream)
+{
+    if(!c) return VKG_ERR_INVALID_ARGUMENT;
+    if(!path) return set_error(c->ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_nrc_save: NULL path");
+    if(vkg_status s = bind_device(c->ctx); s != VKG_OK) return s;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    uint32_t step = 0;
+    std::vector<float> buf(3ull * NPARAM + 3ull * c->ngrid);
+    float *dst = buf.data();
+    for(const float *src: {c->w, c->w_m, c->w_v})
+    {
+        VKG_TRY_CUDA(c->ctx, cudaMemcpyAsync(dst, src, NPARAM * sizeof(float), cudaMemcpyDeviceToHost, st));
+        dst += NPARAM;
+    }
+    for(const float *src: {c->grid, c->grid_m, c->grid_v})
+    {
+        VKG_TRY_CUDA(c->ctx, cudaMemcpyAsync(dst, src, c->ngrid * sizeof(float), cudaMemcpyDeviceToHost, st));
+        dst += c->ngrid;
+    }
+    VKG_TRY_CUDA(c->ctx, cudaMemcpyAsync(&step, c->d_state, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    VKG_TRY_CUDA(c->ctx, cudaStreamSynchronize(st));
+    nrc_ckpt_header h = ckpt_header(c, step);
+    h.checksum = fnv1a64(buf.data(), buf.size() * sizeof(float));
+    std::FILE *f = std::fopen(path, "wb");
+    if(!f) return set_error(c->ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_nrc_save: cannot open %s", path);
+    const bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 &&
+                    std::fwrite(buf.data(), sizeof(float), buf.size(), f) == buf.size();
+    const bool closed = std::fclose(f) == 0;
+    if(!ok || !closed) return set_error(c->ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_nrc_save: write to %s failed", path);
+    return VKG_OK;
+}
+
+vkg_status vkg_nrc_load(vkg_nrc *c, const char *path, void *stream)
+{
+    if(!c) return VKG_ERR_INVALID_ARGUMENT;
+    if(!path) return set_error(c->ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_nrc_load: NULL path");
+    if(vkg_status s = bind_device(c->ctx); s != VKG_OK) return s;
+    std::FILE *f = std::fopen(path, "rb");
+    if(!f) return set_error(c->ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_nrc_load: cannot open %s", path);
+    nrc_ckpt_header h{};
+    std::vector<float> buf;
+    const char *why = nullptr;
+    if(std::fread(&h, sizeof(h), 1, f) != 1) why = "short header";
+    else if(std::memcmp(h.magic, "VKGNRC01", 8) != 0 || h.version != 1 || h.header_bytes != sizeof(h))
+        why = "not a version-1 cache checkpoint";
+    else
+    {
+        const nrc_ckpt_header want = ckpt_header(c, 0);
+        bool same = h.levels == want.levels && h.log2_table_size == want.log2_table_size &&
+                    h.base_resolution == want.base_resolution && h.max_resolution == want.max_resolution &&
+                    h.num_mlp_params == want.num_mlp_params && h.num_grid_params == want.num_grid_params &&
+                    h.payload_bytes == want.payload_bytes;
+        for(int a = 0; a < 3; ++a)
+            same = same && h.scene_min[a] == want.scene_min[a] && h.scene_max[a] == want.scene_max[a];
+        if(!same) why = "grid layout or scene box differs from this cache's configuration";
+        else
+        {
+            buf.resize(h.payload_bytes / sizeof(float));
+            if(std::fread(buf.data(), sizeof(float), buf.size(), f) != buf.size()) why = "short payload";
+            else if(std::fgetc(f) != EOF) why = "trailing bytes after the payload";
+            else if(fnv1a64(buf.data(), buf.size() * sizeof(float)) != h.checksum) why = "checksum mismatch";
+        }
+    }
+    std::fclose(f);
+    if(why) return set_error(c->ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_nrc_load: %s: %s", path, why);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const float *src = buf.data();
+    for(float *dst: {c->w, c->w_m, c->w_v})
+    {
+        VKG_TRY_CUDA(c->ctx, cudaMemcpyAsync(dst, src, NPARAM * sizeof(float), cudaMemcpyHostToDevice, st));
+        src += NPARAM;
+    }
+    for(float *dst: {c->grid, c->grid_m, c->grid_v})
+    {
+        VKG_TRY_CUDA(c->ctx, cudaMemcpyAsync(dst, src, c->ngrid * sizeof(float), cudaMemcpyHostToDevice, st));
+        src += c->ngrid;
+    }
+    VKG_TRY_CUDA(c->ctx, cudaMemcpyAsync(c->d_state, &h.step, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    // the operand copies the kernels read
+    k_to_half<<<c->ctx->num_sms * 8, 256, 0, st>>>(c->grid, c->ngrid, c->grid_h);
+    k_pack<<<(NFRAG + 255) / 256, 256, 0, st>>>(c->w, c->frag, c->fragT);
+    if(vkg_status s = nrc_pack_tc(c->ctx, c->w, c->wtc, st); s != VKG_OK) return s;
+    VKG_TRY_CUDA(c->ctx, cudaStreamSynchronize(st));
+    return cuda_check(c->ctx, cudaGetLastError(), "vkg_nrc_load");
 }
 
 }// extern "C"

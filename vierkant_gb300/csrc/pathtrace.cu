@@ -35,12 +35,22 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <random>
 
 
 struct vkg_tracer
 {
     vkg_ctx *ctx = nullptr;
     uint32_t seed = 0;
+    // VKG_RNG_REFERENCE: the batch seeds (std::default_random_engine(seed), PBRPathTracer.cpp:32) and
+    // per window pixel the chain state and sub-pixel offset carried from sample to sample
+    std::minstd_rand0 ref_engine;
+    uint32_t *ref_chain = nullptr;
+    float *ref_offset = nullptr;
+    size_t ref_cap = 0;
+    // vkg_diag_tracer_uniforms
+    float *dbg_u = nullptr;
+    uint32_t dbg_segments = 0;
     vkg_settings settings{};
     uint32_t batch = 0;
     // buffers sized for `capacity` paths and `npix` pixels
@@ -398,6 +408,8 @@ vkg_status vkg::check_tracer_settings(vkg_ctx *ctx, const vkg_settings *s)
     if(s->max_trace_depth == 0 || s->max_trace_depth > 64)
         return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "settings: max_trace_depth must be 1..64");
     if(s->mis_mode > 2) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "settings: mis_mode must be 0, 1 or 2");
+    if(s->rng_mode > VKG_RNG_REFERENCE)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "settings: rng_mode must be VKG_RNG_PCG32 or VKG_RNG_REFERENCE");
     if(s->crop[2] && s->crop[3] &&
        ((uint64_t)s->crop[0] + s->crop[2] > s->resolution[0] || (uint64_t)s->crop[1] + s->crop[3] > s->resolution[1]))
         return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "settings: crop window outside the resolution");
@@ -747,6 +759,7 @@ vkg_status vkg_tracer_create(vkg_ctx *ctx, const vkg_tracer_create_info *info, v
     auto *t = new vkg_tracer();
     t->ctx = ctx;
     t->seed = info->seed;
+    t->ref_engine.seed(info->seed);
     t->settings = info->settings;
     if(cudaMalloc(&t->counters, 8 * sizeof(uint32_t)) != cudaSuccess ||
        cudaMalloc(&t->totals, 3 * sizeof(unsigned long long)) != cudaSuccess ||
@@ -808,6 +821,11 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
     uint32_t spw = S.samples_per_wave;
     if(spw == 0) spw = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(S.num_samples, (8u << 20) / npix));
     spw = std::min(spw, S.num_samples);
+    // the reference's streams chain a pixel's samples: one sample per pixel and wave
+    const bool ref_rng = S.rng_mode == VKG_RNG_REFERENCE;
+    if(ref_rng) spw = 1;
+    if(ref_rng && t->cache)
+        return set_error(ctx, VKG_ERR_NOT_SUPPORTED, "vkg_tracer_render: VKG_RNG_REFERENCE with a radiance cache");
     const size_t paths = (size_t)npix * spw;
     if(paths >= (1ull << 31)) return set_error(ctx, VKG_ERR_CAPACITY, "vkg_tracer_render: too many paths per wave");
     const vkg_nrc_config *ccfg = t->cache ? &nrc::nrc_config(t->cache) : nullptr;
@@ -826,6 +844,29 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
     const std::vector<vkg_light> lights = render_lights(sc, S);
     if(vkg_status s = tracer_ensure_lights(t, lights, paths + train_paths, st); s != VKG_OK) return s;
     pt_params P = make_params(sc, *cam, S, t->seed, t->batch);
+    if(ref_rng)
+    {
+        if(t->ref_cap < npix)
+        {
+            cudaFree(t->ref_chain);
+            cudaFree(t->ref_offset);
+            t->ref_chain = nullptr;
+            t->ref_offset = nullptr;
+            t->ref_cap = 0;
+            VKG_TRY_CUDA(ctx, cudaMalloc(&t->ref_chain, npix * sizeof(uint32_t)));
+            VKG_TRY_CUDA(ctx, cudaMalloc(&t->ref_offset, npix * sizeof(float)));
+            t->ref_cap = npix;
+        }
+        P.ref_rng = 1;
+        P.ref_seed = (uint32_t)t->ref_engine(); // trace_params.random_seed = m_random_engine() (PBRPathTracer.cpp:588)
+        P.ref_width = S.resolution[0];
+        P.ref_samples = S.num_samples;
+        P.ref_chain = t->ref_chain;
+        P.ref_offset = t->ref_offset;
+    }
+    P.dbg_u = t->dbg_u;
+    P.dbg_segments = t->dbg_segments;
+    P.dbg_stride = 2 + DBG_U_PER_SEGMENT * t->dbg_segments;
     P.lights = lights.empty() ? nullptr : t->d_lights;
     P.num_lights = (uint32_t)lights.size();
     uint32_t *cnt_l = lights.empty() ? nullptr : t->counters + 7;
@@ -1094,6 +1135,14 @@ vkg_status vkg_tracer_attach_cache(vkg_tracer *t, vkg_nrc *cache)
     return VKG_OK;
 }
 
+vkg_status vkg_diag_tracer_uniforms(vkg_tracer *t, float *d_buf, uint32_t max_segments)
+{
+    if(!t || (d_buf && (max_segments == 0 || max_segments > 64))) return VKG_ERR_INVALID_ARGUMENT;
+    t->dbg_u = d_buf;
+    t->dbg_segments = d_buf ? max_segments : 0u;
+    return VKG_OK;
+}
+
 vkg_status vkg_tracer_destroy(vkg_tracer *t)
 {
     if(!t) return VKG_OK;
@@ -1102,7 +1151,7 @@ vkg_status vkg_tracer_destroy(vkg_tracer *t)
     tracer_free_cache_buffers(t);
     cudaFree(t->counters);
     for(void *p: {(void *)t->d_lights, (void *)t->l_ray, (void *)t->l_pid, (void *)t->l_contrib, (void *)t->mstack,
-                  (void *)t->d_media_cam})
+                  (void *)t->d_media_cam, (void *)t->ref_chain, (void *)t->ref_offset})
         cudaFree(p);
     cudaFree(t->totals);
     if(t->ev0) cudaEventDestroy(t->ev0);

@@ -99,7 +99,18 @@ struct pt_params
     const medium_rec *media;
     uint4 *mstack;
     uint32_t cam_medium; // medium table index of the camera's medium (0xFFFFFFFF: vacuum)
+    // the reference's random streams (VKG_RNG_REFERENCE, one sample per pixel and wave): the batch
+    // seed, the full-resolution width and samples per batch, and per window pixel the chain state
+    // between samples and the sub-pixel offset of the batch
+    uint32_t ref_rng, ref_seed, ref_width, ref_samples;
+    uint32_t *ref_chain;
+    float *ref_offset;
+    // diagnostics: the drawn random numbers (vkg_diag_tracer_uniforms), records of dbg_stride floats
+    float *dbg_u;
+    uint32_t dbg_stride, dbg_segments;
 };
+
+constexpr uint32_t DBG_U_PER_SEGMENT = 15;
 
 // the shade kernel's two modes
 enum : int
@@ -203,7 +214,45 @@ __global__ void __launch_bounds__(PT_THREADS)
             vcount[k] = 0;
         }
         const uint32_t x = P.cx0 + pix % P.cw, y = P.cy0 + pix / P.cw;
-        const float jx = u01(pcg32_next(g)), jy = u01(pcg32_next(g));
+        float jx, jy;
+        if(P.ref_rng)
+        {
+            // the reference's raygen streams (raypipeline.slang:95-108): the pixel's chain runs through
+            // the batch's samples, one sample per wave
+            uint32_t chain;
+            float off;
+            if(P.s0 == 0)
+            {
+                chain = xxhash32(P.ref_seed, P.ref_width * y + x);
+                off = fsub(fmul(2.0f, rnd(chain)), 1.0f);
+                P.ref_offset[pix] = off;
+            }
+            else
+            {
+                chain = P.ref_chain[pix];
+                off = P.ref_offset[pix];
+            }
+            rnd(chain); // Xi, the lens sample: a pinhole camera does not use it
+            rnd(chain);
+            // frac(Hammersley(s, N) + offset), Hammersley(i, N) = (i / N, reversebits(i) 2^-32)
+            const float hx = fdiv((float)P.s0, (float)P.ref_samples);
+            const float hy = fmul((float)__brev(P.s0), 2.3283064365386963e-10f);
+            const float ax = fadd(hx, off), ay = fadd(hy, off);
+            jx = fsub(ax, floorf(ax));
+            jy = fsub(ay, floorf(ay));
+            g.state = chain;
+        }
+        else
+        {
+            jx = u01(pcg32_next(g));
+            jy = u01(pcg32_next(g));
+        }
+        if(P.dbg_u)
+        {
+            float *d = P.dbg_u + ((size_t)P.s0 * P.npix + p) * P.dbg_stride;
+            d[0] = jx;
+            d[1] = jy;
+        }
         camera_ray(P.cam, x, y, jx, jy, reinterpret_cast<float4 *>(q_ray + p));
         q_pid[p] = p;
         rng[p] = g.state;
@@ -409,7 +458,22 @@ __global__ void __launch_bounds__(PT_THREADS)
             const bool media = FULL && MEDIA && P.media;
             float u[15];
             const int nu = media ? 15 : (num_lights ? 11 : 8);
-            for(int k = 0; k < 15; ++k) u[k] = k < nu ? u01(pcg32_next(g)) : 0.f;
+            if(P.ref_rng)
+            {
+                // the reference's per-segment stream: chain = xxhash32(chain, i) (raypipeline.slang:150),
+                // the hit shader's rnd() LCG started at it (random.slang:27-36)
+                const uint32_t chain = xxhash32((uint32_t)g.state, depth);
+                uint32_t l = chain;
+                for(int k = 0; k < 15; ++k) u[k] = k < nu ? rnd(l) : 0.f;
+                g.state = chain;
+            }
+            else
+                for(int k = 0; k < 15; ++k) u[k] = k < nu ? u01(pcg32_next(g)) : 0.f;
+            if(P.dbg_u && depth < P.dbg_segments)
+            {
+                float *d = P.dbg_u + ((size_t)P.s0 * P.npix + pid) * P.dbg_stride + 2 + DBG_U_PER_SEGMENT * depth;
+                for(int k = 0; k < nu; ++k) d[k] = u[k];
+            }
             const float4 bp = beta_pdf[pid];
             float3 beta = f3(bp.x, bp.y, bp.z);
             const float3 seg_beta = beta;
@@ -773,6 +837,8 @@ __global__ void __launch_bounds__(PT_THREADS)
         done:
             if(media) P.mstack[pid] = mst;
             rng[pid] = g.state;
+            // the reference's chain of a finished path continues with the pixel's next sample
+            if(P.ref_rng && !push_ext) P.ref_chain[pid] = (uint32_t)g.state;
             beta_pdf[pid] = make_float4(beta.x, beta.y, beta.z, prev_pdf);
             radiance[pid] = make_float4(L.x, L.y, L.z, __uint_as_float(flags));
         }

@@ -76,20 +76,6 @@ __device__ __forceinline__ float safe_rcp(float d)
 
 __device__ __forceinline__ float qbyte(uint32_t w, int k) { return (float)((w >> (8 * (k & 3))) & 0xFFu); }
 
-// three-input minimum / maximum (PTX min.f32 / max.f32 with three sources, sm_100 and later): exact,
-// so max3(a, b, c) equals fmaxf(fmaxf(a, b), c) for the non-NaN values the slab test produces
-__device__ __forceinline__ float fmax3(float a, float b, float c)
-{
-    float r;
-    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
-}
-__device__ __forceinline__ float fmin3(float a, float b, float c)
-{
-    float r;
-    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
-}
 
 
 // per-ray traversal state. The stack (STACK entries) is a separate local-memory array the state
@@ -171,8 +157,8 @@ __device__ __forceinline__ void node_keys(const node8 *__restrict__ nodes, uint3
             const float tnx = fmaf(qbyte(wnx, k), sx, tox), tfx = fmaf(qbyte(wfx, k), sx, tox);
             const float tny = fmaf(qbyte(wny, k), sy, toy), tfy = fmaf(qbyte(wfy, k), sy, toy);
             const float tnz = fmaf(qbyte(wnz, k), sz, toz), tfz = fmaf(qbyte(wfz, k), sz, toz);
-            const float tn = fmax3(tnx, tny, fmaxf(tnz, tmin));
-            const float tf = fmin3(tfx, tfy, fminf(tfz, tmax));
+            const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+            const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
             if(tn <= tf) key[k] = (tenc(tn) & ~7u) | (uint32_t)k;
         }
     }

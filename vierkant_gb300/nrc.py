@@ -63,6 +63,14 @@ class NeuralRadianceCache:
                                         C.c_void_p(grid.data_ptr()) if grid is not None else None, self._s()),
               self.ctx.handle, "vkg_nrc_load_params")
 
+    def save(self, path: str):
+        """checkpoint: weights, grid, both Adam moments and the step count (vkg_nrc_save)"""
+        check(lib().vkg_nrc_save(self.handle, str(path).encode(), self._s()), self.ctx.handle, "vkg_nrc_save")
+
+    def load(self, path: str):
+        """restore a checkpoint of a cache with the same grid layout (vkg_nrc_load)"""
+        check(lib().vkg_nrc_load(self.handle, str(path).encode(), self._s()), self.ctx.handle, "vkg_nrc_load")
+
     def close(self):
         if getattr(self, "handle", None) and getattr(self.ctx, "handle", None):
             lib().vkg_nrc_destroy(self.handle)
