@@ -30,6 +30,7 @@ constexpr uint32_t TC_W_BYTES = NPARAM * 2;      // all six layers, BF16 B opera
 constexpr uint32_t TC_A_BYTES = TC_TILE * IN * 2; // one A operand (20,480 B)
 constexpr uint32_t TC_SMEM = TC_W_BYTES + TC_A_BYTES;
 constexpr uint32_t TC_TIMEOUT = 1u;
+constexpr int TC_INFER_WG = 4;                    // warpgroups (tiles in flight) of the pipelined kernel
 
 namespace
 {
@@ -251,6 +252,117 @@ __global__ void __launch_bounds__(TC_THREADS)
     if(warp == 0) tc::tmem_dealloc(tmem, TC_TMEM_COLS);
 }
 
+// ---- pipelined inference: independent warpgroups ------------------------------------------------
+// The single-tile kernel above leaves the tensor core idle while a layer's epilogue (TMEM -> registers
+// -> ReLU / BF16 -> shared memory) runs, and the epilogue, not the MMA, sets its time. Here a CTA of
+// NWG warpgroups (128 threads each) runs NWG tiles at once: warpgroup g owns 64 TMEM columns
+// [64 g, 64 g + 64), one A operand in shared memory, one mbarrier and named barrier g + 1, and its
+// thread 0 issues its own MMAs; so while one warpgroup drains its accumulator the tensor core works
+// on another's layer. The weights (all six layers, 45 KB) are shared. Thread r of a warpgroup owns
+// row r of its tile (TMEM lane r: warp w reads lanes 32 (w mod 4) .. + 31). Inputs are the encoded
+// BF16 records of k_encode.
+template<int NWG>
+__global__ void __launch_bounds__(NWG * 128)
+        k_infer_tc_wg(const uint32_t *__restrict__ X, uint32_t n_cap, const uint32_t *__restrict__ d_n,
+                      const uint16_t *__restrict__ wtc, float *__restrict__ Y, uint32_t *__restrict__ err)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t mbar[NWG];
+    __shared__ uint32_t tslot;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, g = tid >> 7, r = tid & 127u;
+    uint8_t *sw = smem, *sa = smem + TC_W_BYTES + g * TC_A_BYTES;
+    for(uint32_t i = tid; i < TC_W_BYTES / 16; i += NWG * 128)
+        reinterpret_cast<uint4 *>(sw)[i] = reinterpret_cast<const uint4 *>(wtc)[i];
+    constexpr uint32_t COLS = NWG * 64 <= 32 ? 32 : (NWG * 64 <= 64 ? 64 : (NWG * 64 <= 128 ? 128 : 256));
+    if(warp == 0) tc::tmem_alloc(&tslot, COLS);
+    if(tid < NWG) tc::mbar_init(&mbar[tid], 1);
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tslot + 64u * g, lane_base = ((warp & 3u) * 32u) << 16;
+    const uint32_t sw_addr = tc::smem_addr(sw), sa_addr = tc::smem_addr(sa);
+    const uint32_t n = eff_n(n_cap, d_n), tiles = (n + TC_TILE - 1) / TC_TILE;
+    const uint32_t bar_id = g + 1;
+    uint32_t phase = 0;
+    bool failed = false;
+
+    for(uint32_t tile = blockIdx.x * NWG + g; tile < tiles && !failed; tile += gridDim.x * NWG)
+    {
+        const uint32_t q = tile * TC_TILE + r;
+        const uint4 *src = reinterpret_cast<const uint4 *>(X + (size_t)(IN / 2) * q);
+#pragma unroll
+        for(int j = 0; j < IN / 8; ++j)
+            *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 8 * j, IN)) = q < n ? src[j] : make_uint4(0u, 0u, 0u, 0u);
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        tc::wg_sync(bar_id);
+#pragma unroll 1
+        for(int l = 0; l < NLAYER; ++l)
+        {
+            const uint32_t K = layer_in(l), N = layer_out(l);
+            if(r == 0)
+            {
+                tc::fence_after_sync();
+                const uint32_t idesc = tc::idesc_bf16(TC_TILE, N);
+                const uint32_t wb = sw_addr + (uint32_t)layer_off(l) * 2u;
+                for(uint32_t s = 0; s < K / 16; ++s)
+                    tc::mma_bf16(tmem, tc::smem_desc(sa_addr + 256u * s, 128u, K * 16u),
+                                 tc::smem_desc(wb + 256u * s, 128u, K * 16u), idesc, s > 0);
+                tc::mma_commit(&mbar[g]);
+            }
+            const bool ok = tc::mbar_wait(&mbar[g], phase);
+            if(tc::wg_sync_or(bar_id, !ok))
+            {
+                failed = true;
+                break;
+            }
+            phase ^= 1u;
+            tc::fence_after_sync();
+            if(l + 1 < NLAYER)
+            {
+#pragma unroll
+                for(int c = 0; c < 4; ++c)
+                {
+                    float v[16];
+                    tc::tmem_ld16(tmem + lane_base + 16u * c, v);
+                    tc::tmem_ld_wait();
+                    uint32_t hv[8];
+#pragma unroll
+                    for(int j = 0; j < 8; ++j) hv[j] = pack_bf16(fmaxf(v[2 * j], 0.f), fmaxf(v[2 * j + 1], 0.f));
+                    *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 16 * c, HID)) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
+                    *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 16 * c + 8, HID)) =
+                            make_uint4(hv[4], hv[5], hv[6], hv[7]);
+                }
+                tc::fence_async_smem();
+            }
+            else
+            {
+                float v[16];
+                tc::tmem_ld16(tmem + lane_base, v);
+                tc::tmem_ld_wait();
+                if(q < n)
+                {
+                    Y[3 * (size_t)q] = v[0];
+                    Y[3 * (size_t)q + 1] = v[1];
+                    Y[3 * (size_t)q + 2] = v[2];
+                }
+            }
+            tc::fence_before_sync();
+            tc::wg_sync(bar_id);
+        }
+    }
+    if(failed)
+    {
+        if(r == 0) atomicOr(err, TC_TIMEOUT);
+        tc::mbar_wait(&mbar[g], phase); // this warpgroup's MMAs in flight, if any
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if(warp == 0) tc::tmem_dealloc(tslot, COLS);
+}
+
 // diagnostic: the error path every tcgen05 kernel here takes when a wait runs out, run to its end on
 // purpose. Each CTA allocates TMEM and waits on an mbarrier that nothing arrives on, with a limit of
 // limit_ns instead of the kernels' 1 s; the wait gives up, the CTA sets TC_TIMEOUT, waits a second
@@ -470,6 +582,17 @@ vkg_status nrc_infer_tc(vkg_ctx *ctx, const grid_config &gc, const __half2 *grid
                         cudaStream_t st)
 {
     if(n == 0) return VKG_OK;
+    if(X)
+    {
+        // encoded inputs: the pipelined kernel, four warpgroups (four tiles in flight) per SM
+        constexpr int NWG = TC_INFER_WG;
+        const uint32_t smem = TC_W_BYTES + NWG * TC_A_BYTES;
+        VKG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_infer_tc_wg<NWG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const uint32_t tiles = (n + TC_TILE - 1) / TC_TILE;
+        const uint32_t grid_n = std::min<uint32_t>((tiles + NWG - 1) / NWG, (uint32_t)ctx->num_sms);
+        k_infer_tc_wg<NWG><<<grid_n, NWG * 128, smem, st>>>(X, n, d_n, wtc, Y, err);
+        return cuda_check(ctx, cudaGetLastError(), "k_infer_tc_wg");
+    }
     auto kern = X ? k_infer_tc<false> : k_infer_tc<true>;
     VKG_TRY_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
     int per_sm = 0;

@@ -66,6 +66,21 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
     return mbar_wait_for(bar, parity, WAIT_LIMIT, WAIT_NS);
 }
 
+// ---- named barriers over one warpgroup (128 threads); id 0 is __syncthreads' ----------------------
+__device__ __forceinline__ void wg_sync(uint32_t id) { asm volatile("barrier.sync %0, 128;\n" ::"r"(id) : "memory"); }
+
+// barrier over the warpgroup that also ORs a predicate across its threads
+__device__ __forceinline__ bool wg_sync_or(uint32_t id, bool pred)
+{
+    uint32_t out;
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbarrier.red.or.pred p, %2, 128, q;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(out)
+                 : "r"((uint32_t)pred), "r"(id)
+                 : "memory");
+    return out != 0;
+}
+
 // ---- TMEM ----------------------------------------------------------------------------------------
 // one full warp; the base address is written to *slot (shared memory)
 __device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t ncols)
