@@ -711,7 +711,9 @@ typedef struct vkg_nrc_config
     uint32_t train_depth;     /* training targets are recorded at the first this-many interactions (4) */
     uint32_t train_steps;     /* optimiser steps per frame; 0: ceil(train_paths * train_depth / batch_size) */
     uint32_t infer_kernel;    /* 0: default, 1: mma.sync MLP, 2: tcgen05 MLP, 3: tcgen05 MLP with the encoding fused */
-    uint32_t train_kernel;    /* weight gradients: 0: default (tcgen05), 1: FP32 CUDA cores, 2: tcgen05 */
+    uint32_t train_kernel;    /* 0: default (2), 1: mma.sync forward + FP32 CUDA-core weight gradients,
+                                 2: mma.sync forward + tcgen05 weight gradients, 3: tcgen05 forward and
+                                 weight gradients (the backward through the layers is mma.sync in all) */
 } vkg_nrc_config;
 typedef struct vkg_nrc_info_t
 {
@@ -727,7 +729,7 @@ typedef struct vkg_nrc_info_t
     uint32_t step;            /* optimiser steps taken */
     uint32_t kernel_error;    /* nonzero: a tensor-core kernel gave up waiting (its results are void) */
     uint32_t infer_kernel;    /* the inference kernel in use (1..3, see vkg_nrc_config) */
-    uint32_t train_kernel;    /* the weight-gradient kernel in use (1, 2) */
+    uint32_t train_kernel;    /* the training kernels in use (1..3) */
 } vkg_nrc_info_t;
 vkg_status vkg_nrc_config_default(vkg_nrc_config *out);
 vkg_status vkg_nrc_create(vkg_ctx *ctx, const vkg_nrc_config *cfg, vkg_nrc **out);

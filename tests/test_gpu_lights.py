@@ -98,13 +98,14 @@ def test_twin_parity_path_for_path(ctx, lit, suppress):
 
 
 def test_radiance_against_fp64_oracle(ctx, lit, golden):
-    """32 independent 512-spp batches (16,384 spp) against the FP64 fixture (full frame): the luminance
-    bias is within 3 standard errors of zero, with 3 standard errors below 0.5 %, and the RMSE within 1.2x
-    the noise of the two estimates (radiance_stats)"""
+    """64 independent 512-spp batches (32,768 spp) against the FP64 fixture (full frame, 16,384 spp): the
+    luminance bias is within 3 standard errors of zero, with 3 standard errors below 0.5 % (the caustics
+    through the glass spheres are heavy-tailed, so this scene needs the most samples), and the RMSE
+    within 1.2x the noise of the two estimates (radiance_stats)"""
     g = golden("pt_oracle_lights")
     assert tuple(g["size"]) == (W, H) and int(g["max_depth"]) == 8 and int(g["num_spheres"]) == NUM_SPHERES
     imgs = render_batches(lambda seed: PBRPathTracer(ctx, seed=seed, settings=settings(512)), lit["scene"],
-                          lit["cam"], 32)
+                          lit["cam"], 64)
     st = compare(imgs, g["mean"], g["lum_var"], int(g["spp"]))
     report("lit showcase vs FP64 oracle", st)
     check(st)

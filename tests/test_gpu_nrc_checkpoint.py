@@ -1,7 +1,9 @@
 """Radiance-cache checkpoints (vkg_nrc_save / vkg_nrc_load): a trained cache saved and loaded into a
-fresh cache gives the same parameters, Adam moments, step count and predictions bit for bit, and
-training continues identically from the loaded state; a corrupted payload, a truncated file and a
-cache with another grid layout are refused."""
+fresh cache gives the same parameters, Adam moments, step count and predictions bit for bit (saving
+the loaded cache writes the same bytes), and training continues from the loaded state as from the
+original (the hash-grid gradients are summed with atomics, so two training runs agree to rounding,
+not bit for bit); a corrupted payload, a truncated file and a cache with another grid layout are
+refused."""
 import ctypes as C
 
 import numpy as np
@@ -58,12 +60,19 @@ def test_checkpoint_round_trip_and_resume(ctx, tmp_path):
     assert ma.tobytes() == mb.tobytes() and ga.tobytes() == gb.tobytes()
     q = random_features(4096, seed=99)
     assert torch.equal(a.infer(q), b.infer(q))
-    # the Adam moments came along: the next steps match bit for bit
+    # the whole training state came along, Adam moments included: saving it again gives the same file
+    path2 = tmp_path / "again.vkgnrc"
+    b.save(path2)
+    assert path.read_bytes() == path2.read_bytes()
+    # and training continues from it as from the original
     _train(a, 3, 50)
     _train(b, 3, 50)
-    ma, ga, _ = _params(a)
-    mb, gb, _ = _params(b)
-    assert ma.tobytes() == mb.tobytes() and ga.tobytes() == gb.tobytes()
+    ma, ga, sa = _params(a)
+    mb, gb, sb = _params(b)
+    assert sa == sb == 8
+    assert np.allclose(ma, mb, rtol=0, atol=2e-3) and np.allclose(ga, gb, rtol=0, atol=2e-3)
+    pa, pb = a.infer(q), b.infer(q)
+    assert (pa - pb).abs().max().item() <= 1e-2 * max(1.0, pa.abs().max().item())
     assert a.info().kernel_error == 0 and b.info().kernel_error == 0
     a.close()
     b.close()

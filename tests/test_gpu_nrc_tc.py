@@ -158,3 +158,26 @@ def test_bounded_wait_runs_out_and_returns(ctx):
     torch.cuda.synchronize()
     assert cache.info().kernel_error == 0
     cache.close()
+
+
+def test_tc_training_forward_matches_mma_forward(ctx):
+    """train_kernel 3 runs the training forward on the pipelined tcgen05 kernel: its activations feed the
+    same backward, so the gradients equal train_kernel 2's up to the BF16 rounding of activations whose
+    FP32 sums differ in summation order"""
+    n = 20_000
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    cfg = NeuralRadianceCache.default_config()
+    cfg.log2_table_size = 16
+    probe = NeuralRadianceCache(ctx, cfg)
+    i = probe.info()
+    w = torch.randn(i.num_mlp_params, device="cuda", generator=gen) * 0.2
+    g = torch.randn(i.num_grid_params, device="cuda", generator=gen) * 0.5
+    probe.close()
+    feats = random_features(n, 77)
+    targets = torch.rand((n, 3), device="cuda", generator=gen)
+    w2, g2, i2 = _grads(ctx, 2, feats, targets, w, g)
+    w3, g3, i3 = _grads(ctx, 3, feats, targets, w, g)
+    assert i2.train_kernel == 2 and i3.train_kernel == 3 and i3.kernel_error == 0
+    cos = lambda a, b: float((a * b).sum() / (a.norm() * b.norm()))
+    assert cos(w2, w3) > 0.9999 and cos(g2, g3) > 0.9999, (cos(w2, w3), cos(g2, g3))
+    assert (w2 - w3).abs().max().item() <= 2e-2 * w2.abs().max().item()

@@ -31,6 +31,7 @@ struct vkg_nrc
     uint32_t *d_err = nullptr;   // tensor-core kernel error word
     uint32_t tc_infer = 1;       // 1: mma.sync MLP, 2: tcgen05 MLP, 3: tcgen05 MLP with the encoding fused
     bool tc_train = false;       // weight gradients on tcgen05 (else FP32 CUDA cores)
+    bool tc_forward = false;     // the training forward on tcgen05 (else the mma.sync twin)
     // training / inference scratch, sized for `cap` samples
     uint32_t cap = 0;
     uint32_t *X = nullptr, *H = nullptr, *G = nullptr;
@@ -561,7 +562,13 @@ vkg_status nrc_backward(vkg_nrc *c, const float *feats, const float *targets, ui
     if(vkg_status s = nrc_encode(c, feats, n, d_n, c->X, st); s != VKG_OK) return s;
     const uint32_t tiles = (n + 15) / 16, per_cta = MLP_THREADS / 32;
     const uint32_t grid = std::min<uint32_t>((tiles + per_cta - 1) / per_cta, (uint32_t)c->ctx->num_sms * 8);
-    k_forward<true><<<grid, MLP_THREADS, 0, st>>>(c->X, n, d_n, c->frag, c->Y, c->H);
+    // the training forward: on tcgen05 (train_kernel 3), else the mma.sync twin
+    if(c->tc_forward)
+    {
+        if(vkg_status s = nrc_forward_tc(c->ctx, c->wtc, c->X, n, d_n, c->Y, c->H, c->d_err, st); s != VKG_OK) return s;
+    }
+    else
+        k_forward<true><<<grid, MLP_THREADS, 0, st>>>(c->X, n, d_n, c->frag, c->Y, c->H);
     k_backward<<<grid, MLP_THREADS, 0, st>>>(c->H, c->Y, targets, n, d_n, c->fragT, c->G, c->dXg, c->loss);
     if(c->tc_train)
     {
@@ -655,13 +662,14 @@ vkg_status vkg_nrc_create(vkg_ctx *ctx, const vkg_nrc_config *cfg, vkg_nrc **out
         return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_nrc_create: invalid training configuration");
     if(cfg->infer_kernel > 3)
         return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_nrc_create: infer_kernel must be 0..3");
-    if(cfg->train_kernel > 2)
-        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_nrc_create: train_kernel must be 0..2");
+    if(cfg->train_kernel > 3)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_nrc_create: train_kernel must be 0..3");
     auto *c = new vkg_nrc();
     c->ctx = ctx;
     c->cfg = *cfg;
     c->tc_infer = cfg->infer_kernel ? cfg->infer_kernel : 1u;
     c->tc_train = cfg->train_kernel != 1; // default: tcgen05 (479 vs 577 us per 65,536-record step)
+    c->tc_forward = cfg->train_kernel == 3;
     c->gc.levels = cfg->levels;
     c->gc.log2_t = cfg->log2_table_size;
     c->gc.base_res = cfg->base_resolution;
@@ -762,7 +770,7 @@ vkg_status vkg_nrc_info(const vkg_nrc *c, vkg_nrc_info_t *out)
     VKG_TRY_CUDA(c->ctx, cudaMemcpy(&out->step, c->d_state, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     VKG_TRY_CUDA(c->ctx, cudaMemcpy(&out->kernel_error, c->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     out->infer_kernel = c->tc_infer;
-    out->train_kernel = c->tc_train ? 2u : 1u;
+    out->train_kernel = c->tc_forward ? 3u : (c->tc_train ? 2u : 1u);
     return VKG_OK;
 }
 

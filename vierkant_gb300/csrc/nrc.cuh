@@ -89,6 +89,8 @@ vkg_status nrc_infer_tc(vkg_ctx *ctx, const grid_config &gc, const __half2 *grid
                         const float *feats, const uint32_t *X, uint32_t n, const uint32_t *d_n, float *Y, uint32_t *err,
                         cudaStream_t st);
 // weight gradients of n records on tcgen05 (accumulated into dW); err receives 1 if a wait ran out
+vkg_status nrc_forward_tc(vkg_ctx *ctx, const uint16_t *wtc, const uint32_t *X, uint32_t n, const uint32_t *d_n,
+                          float *Y, uint32_t *H, uint32_t *err, cudaStream_t st);
 vkg_status nrc_wgrad_tc(vkg_ctx *ctx, const uint32_t *X, const uint32_t *H, const uint32_t *G, uint32_t n,
                         const uint32_t *d_n, float *dW, uint32_t *err, cudaStream_t st);
 // one optimiser step (backward + Adam) on n records; records past *d_n contribute nothing

@@ -30,7 +30,7 @@ constexpr uint32_t TC_W_BYTES = NPARAM * 2;      // all six layers, BF16 B opera
 constexpr uint32_t TC_A_BYTES = TC_TILE * IN * 2; // one A operand (20,480 B)
 constexpr uint32_t TC_SMEM = TC_W_BYTES + TC_A_BYTES;
 constexpr uint32_t TC_TIMEOUT = 1u;
-constexpr int TC_INFER_WG = 4;                    // warpgroups (tiles in flight) of the pipelined kernel
+constexpr int TC_INFER_WG = 8;                    // warpgroups (tiles in flight) of the pipelined kernel
 
 namespace
 {
@@ -261,10 +261,13 @@ __global__ void __launch_bounds__(TC_THREADS)
 // on another's layer. The weights (all six layers, 45 KB) are shared. Thread r of a warpgroup owns
 // row r of its tile (TMEM lane r: warp w reads lanes 32 (w mod 4) .. + 31). Inputs are the encoded
 // BF16 records of k_encode.
-template<int NWG>
+// TRAIN: also store the hidden activations H1..H5 (BF16, 5 x 64 per record in natural column order,
+// the layout the backward reads) as the training forward.
+template<int NWG, bool TRAIN>
 __global__ void __launch_bounds__(NWG * 128)
         k_infer_tc_wg(const uint32_t *__restrict__ X, uint32_t n_cap, const uint32_t *__restrict__ d_n,
-                      const uint16_t *__restrict__ wtc, float *__restrict__ Y, uint32_t *__restrict__ err)
+                      const uint16_t *__restrict__ wtc, float *__restrict__ Y, uint32_t *__restrict__ err,
+                      uint32_t *__restrict__ H)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint64_t mbar[NWG];
@@ -273,7 +276,9 @@ __global__ void __launch_bounds__(NWG * 128)
     uint8_t *sw = smem, *sa = smem + TC_W_BYTES + g * TC_A_BYTES;
     for(uint32_t i = tid; i < TC_W_BYTES / 16; i += NWG * 128)
         reinterpret_cast<uint4 *>(sw)[i] = reinterpret_cast<const uint4 *>(wtc)[i];
-    constexpr uint32_t COLS = NWG * 64 <= 32 ? 32 : (NWG * 64 <= 64 ? 64 : (NWG * 64 <= 128 ? 128 : 256));
+    // TMEM columns: 64 per warpgroup, allocated as a power of two of at least 32
+    static_assert(NWG >= 1 && NWG <= 8, "at most 512 TMEM columns");
+    constexpr uint32_t COLS = NWG * 64 <= 64 ? 64 : (NWG * 64 <= 128 ? 128 : (NWG * 64 <= 256 ? 256 : 512));
     if(warp == 0) tc::tmem_alloc(&tslot, COLS);
     if(tid < NWG) tc::mbar_init(&mbar[tid], 1);
     tc::fence_async_smem();
@@ -333,6 +338,12 @@ __global__ void __launch_bounds__(NWG * 128)
                     *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 16 * c, HID)) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
                     *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 16 * c + 8, HID)) =
                             make_uint4(hv[4], hv[5], hv[6], hv[7]);
+                    if(TRAIN && q < n)
+                    {
+                        uint4 *hp = reinterpret_cast<uint4 *>(H + (size_t)q * (5 * HID / 2) + l * (HID / 2) + 8 * c);
+                        hp[0] = make_uint4(hv[0], hv[1], hv[2], hv[3]);
+                        hp[1] = make_uint4(hv[4], hv[5], hv[6], hv[7]);
+                    }
                 }
                 tc::fence_async_smem();
             }
@@ -577,22 +588,28 @@ vkg_status nrc_pack_tc(vkg_ctx *ctx, const float *W, uint16_t *wtc, cudaStream_t
     return cuda_check(ctx, cudaGetLastError(), "k_pack_tc");
 }
 
+// the pipelined MLP over encoded inputs X: inference (H null) or the training forward (H receives the
+// activations); TC_INFER_WG warpgroups (tiles in flight) per SM
+vkg_status nrc_forward_tc(vkg_ctx *ctx, const uint16_t *wtc, const uint32_t *X, uint32_t n, const uint32_t *d_n,
+                          float *Y, uint32_t *H, uint32_t *err, cudaStream_t st)
+{
+    if(n == 0) return VKG_OK;
+    constexpr int NWG = TC_INFER_WG;
+    const uint32_t smem = TC_W_BYTES + NWG * TC_A_BYTES;
+    auto kern = H ? k_infer_tc_wg<NWG, true> : k_infer_tc_wg<NWG, false>;
+    VKG_TRY_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const uint32_t tiles = (n + TC_TILE - 1) / TC_TILE;
+    const uint32_t grid_n = std::min<uint32_t>((tiles + NWG - 1) / NWG, (uint32_t)ctx->num_sms);
+    kern<<<grid_n, NWG * 128, smem, st>>>(X, n, d_n, wtc, Y, err, H);
+    return cuda_check(ctx, cudaGetLastError(), "k_infer_tc_wg");
+}
+
 vkg_status nrc_infer_tc(vkg_ctx *ctx, const grid_config &gc, const __half2 *grid, const uint16_t *wtc,
                         const float *feats, const uint32_t *X, uint32_t n, const uint32_t *d_n, float *Y, uint32_t *err,
                         cudaStream_t st)
 {
     if(n == 0) return VKG_OK;
-    if(X)
-    {
-        // encoded inputs: the pipelined kernel, four warpgroups (four tiles in flight) per SM
-        constexpr int NWG = TC_INFER_WG;
-        const uint32_t smem = TC_W_BYTES + NWG * TC_A_BYTES;
-        VKG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_infer_tc_wg<NWG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        const uint32_t tiles = (n + TC_TILE - 1) / TC_TILE;
-        const uint32_t grid_n = std::min<uint32_t>((tiles + NWG - 1) / NWG, (uint32_t)ctx->num_sms);
-        k_infer_tc_wg<NWG><<<grid_n, NWG * 128, smem, st>>>(X, n, d_n, wtc, Y, err);
-        return cuda_check(ctx, cudaGetLastError(), "k_infer_tc_wg");
-    }
+    if(X) return nrc_forward_tc(ctx, wtc, X, n, d_n, Y, nullptr, err, st);
     auto kern = X ? k_infer_tc<false> : k_infer_tc<true>;
     VKG_TRY_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
     int per_sm = 0;
