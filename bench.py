@@ -781,8 +781,9 @@ def stress_block(ctx):
 def profile_case(name: str):
     """Small workloads for profiler captures (ncu): one case per call, no JSON line.
     pt-frame   plain path tracer, Cornell scene, 1280x720 x 4 spp
-    nrc        radiance-cache kernels: 4 training steps of 65,536 records, inference of 262,144 queries
-               with the mma.sync, tcgen05 and fused tcgen05 kernels
+    nrc        radiance-cache kernels: 2 training steps of 65,536 records with each training forward
+               (mma.sync, tcgen05), inference of 262,144 queries with the mma.sync, tcgen05 and fused
+               tcgen05 kernels
     batch      batched renderer, 4 scenes of the batched workload at 1 spp
     stress     instanced scene: 512^2 terrain + 10,000 instances, 960x540 x 2 spp, 8 segments
     features   Cornell scene with the showcase materials, the six analytic lights and a sun disc,
@@ -815,10 +816,12 @@ def profile_case(name: str):
         for kind in (1, 2, 3):
             cfg = NeuralRadianceCache.default_config()
             cfg.infer_kernel = kind
+            cfg.train_kernel = 3 if kind == 2 else 2
             caches.append(NeuralRadianceCache(ctx, cfg))
         x, t = feats(65536), torch.rand((65536, 3), device="cuda", generator=g)
-        for _ in range(4):
-            caches[0].train_step(x, t)
+        for _ in range(2):
+            caches[0].train_step(x, t)  # mma.sync forward, tcgen05 weight gradients
+            caches[1].train_step(x, t)  # tcgen05 forward and weight gradients
         q = feats(262144)
         for c in caches:
             c.infer(q)

@@ -26,10 +26,11 @@ def tensor_from(ptr, n, dtype=torch.float32):
     return out
 
 
-@pytest.fixture
-def cache(ctx):
+@pytest.fixture(params=[2, 3], ids=["mma_fwd_bwd", "tcgen05_fwd_bwd"])
+def cache(ctx, request):
     cfg = NeuralRadianceCache.default_config()
     cfg.log2_table_size = 14  # small tables keep the FP64 reference quick
+    cfg.train_kernel = request.param  # forward / backward on mma.sync (2) or tcgen05 (3)
     c = NeuralRadianceCache(ctx, cfg)
     yield c
     c.close()

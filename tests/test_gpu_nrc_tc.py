@@ -160,10 +160,10 @@ def test_bounded_wait_runs_out_and_returns(ctx):
     cache.close()
 
 
-def test_tc_training_forward_matches_mma_forward(ctx):
-    """train_kernel 3 runs the training forward on the pipelined tcgen05 kernel: its activations feed the
-    same backward, so the gradients equal train_kernel 2's up to the BF16 rounding of activations whose
-    FP32 sums differ in summation order"""
+def test_tc_training_forward_backward_match_mma(ctx):
+    """train_kernel 3 runs the training forward and the backward through the layers on the pipelined
+    tcgen05 kernels: the gradients equal train_kernel 2's (mma.sync) up to the BF16 rounding of
+    activations and layer gradients whose FP32 sums differ in summation order"""
     n = 20_000
     gen = torch.Generator(device="cuda").manual_seed(5)
     cfg = NeuralRadianceCache.default_config()

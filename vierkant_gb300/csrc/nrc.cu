@@ -28,6 +28,7 @@ struct vkg_nrc
     float *w = nullptr, *w_g = nullptr, *w_m = nullptr, *w_v = nullptr;
     uint2 *frag = nullptr, *fragT = nullptr;
     uint16_t *wtc = nullptr;     // BF16 weights in the tcgen05 operand layout
+    uint16_t *wtc_t = nullptr;   // the same, transposed per layer (the backward's operands)
     uint32_t *d_err = nullptr;   // tensor-core kernel error word
     uint32_t tc_infer = 1;       // 1: mma.sync MLP, 2: tcgen05 MLP, 3: tcgen05 MLP with the encoding fused
     bool tc_train = false;       // weight gradients on tcgen05 (else FP32 CUDA cores)
@@ -562,14 +563,22 @@ vkg_status nrc_backward(vkg_nrc *c, const float *feats, const float *targets, ui
     if(vkg_status s = nrc_encode(c, feats, n, d_n, c->X, st); s != VKG_OK) return s;
     const uint32_t tiles = (n + 15) / 16, per_cta = MLP_THREADS / 32;
     const uint32_t grid = std::min<uint32_t>((tiles + per_cta - 1) / per_cta, (uint32_t)c->ctx->num_sms * 8);
-    // the training forward: on tcgen05 (train_kernel 3), else the mma.sync twin
+    // the training forward and backward: on tcgen05 (train_kernel 3), else the mma.sync twins
     if(c->tc_forward)
     {
         if(vkg_status s = nrc_forward_tc(c->ctx, c->wtc, c->X, n, d_n, c->Y, c->H, c->d_err, st); s != VKG_OK) return s;
     }
     else
         k_forward<true><<<grid, MLP_THREADS, 0, st>>>(c->X, n, d_n, c->frag, c->Y, c->H);
-    k_backward<<<grid, MLP_THREADS, 0, st>>>(c->H, c->Y, targets, n, d_n, c->fragT, c->G, c->dXg, c->loss);
+    if(c->tc_forward)
+    {
+        if(vkg_status s = nrc_backward_tc(c->ctx, c->wtc_t, c->H, c->Y, targets, n, d_n, c->G, c->dXg, c->loss,
+                                          c->d_err, st);
+           s != VKG_OK)
+            return s;
+    }
+    else
+        k_backward<<<grid, MLP_THREADS, 0, st>>>(c->H, c->Y, targets, n, d_n, c->fragT, c->G, c->dXg, c->loss);
     if(c->tc_train)
     {
         if(vkg_status s = nrc_wgrad_tc(c->ctx, c->X, c->H, c->G, n, d_n, c->w_g, c->d_err, st); s != VKG_OK) return s;
@@ -592,7 +601,7 @@ vkg_status nrc_adam(vkg_nrc *c, const uint32_t *d_n, cudaStream_t st)
                                    c->d_state, c->grid_h);
     k_adam<<<64, 256, 0, st>>>(c->w, c->w_g, c->w_m, c->w_v, NPARAM, c->lr, c->b1, c->b2, c->eps, c->d_state, nullptr);
     k_pack<<<(NFRAG + 255) / 256, 256, 0, st>>>(c->w, c->frag, c->fragT);
-    if(vkg_status s = nrc_pack_tc(c->ctx, c->w, c->wtc, st); s != VKG_OK) return s;
+    if(vkg_status s = nrc_pack_tc(c->ctx, c->w, c->wtc, st, c->wtc_t); s != VKG_OK) return s;
     return cuda_check(c->ctx, cudaGetLastError(), "nrc adam");
 }
 
@@ -706,6 +715,7 @@ vkg_status vkg_nrc_create(vkg_ctx *ctx, const vkg_nrc_config *cfg, vkg_nrc **out
     al((void **)&c->loss, 4 * 4);
     al((void **)&c->d_state, 2 * sizeof(uint32_t));
     al((void **)&c->wtc, NPARAM * 2);
+    al((void **)&c->wtc_t, NPARAM * 2);
     al((void **)&c->d_err, sizeof(uint32_t));
     if(e == cudaSuccess)
     {
@@ -724,7 +734,7 @@ vkg_status vkg_nrc_create(vkg_ctx *ctx, const vkg_nrc_config *cfg, vkg_nrc **out
     }
     k_init<<<ctx->num_sms * 8, 256>>>(c->grid, c->grid_h, c->ngrid, c->w, cfg->seed);
     k_pack<<<(NFRAG + 255) / 256, 256>>>(c->w, c->frag, c->fragT);
-    if(vkg_status s = nrc_pack_tc(ctx, c->w, c->wtc, nullptr); s != VKG_OK)
+    if(vkg_status s = nrc_pack_tc(ctx, c->w, c->wtc, nullptr, c->wtc_t); s != VKG_OK)
     {
         vkg_nrc_destroy(c);
         return s;
@@ -745,7 +755,7 @@ vkg_status vkg_nrc_destroy(vkg_nrc *c)
     if(c->ctx) bind_device(c->ctx);
     for(void *p: {(void *)c->grid, (void *)c->grid_g, (void *)c->grid_m, (void *)c->grid_v, (void *)c->grid_h,
                   (void *)c->w, (void *)c->w_g, (void *)c->w_m, (void *)c->w_v, (void *)c->frag, (void *)c->fragT,
-                  (void *)c->loss, (void *)c->d_state, (void *)c->wtc, (void *)c->d_err, (void *)c->X, (void *)c->H, (void *)c->G, (void *)c->Y,
+                  (void *)c->loss, (void *)c->d_state, (void *)c->wtc, (void *)c->wtc_t, (void *)c->d_err, (void *)c->X, (void *)c->H, (void *)c->G, (void *)c->Y,
                   (void *)c->dXg})
         cudaFree(p);
     delete c;
@@ -834,7 +844,7 @@ vkg_status vkg_nrc_load_params(vkg_nrc *c, const float *d_mlp, const float *d_gr
         k_to_half<<<c->ctx->num_sms * 8, 256, 0, st>>>(c->grid, c->ngrid, c->grid_h);
     }
     k_pack<<<(NFRAG + 255) / 256, 256, 0, st>>>(c->w, c->frag, c->fragT);
-    if(vkg_status s = nrc_pack_tc(c->ctx, c->w, c->wtc, st); s != VKG_OK) return s;
+    if(vkg_status s = nrc_pack_tc(c->ctx, c->w, c->wtc, st, c->wtc_t); s != VKG_OK) return s;
     return cuda_check(c->ctx, cudaGetLastError(), "vkg_nrc_load_params");
 }
 
@@ -980,7 +990,7 @@ vkg_status vkg_nrc_load(vkg_nrc *c, const char *path, void *stream)
     // the operand copies the kernels read
     k_to_half<<<c->ctx->num_sms * 8, 256, 0, st>>>(c->grid, c->ngrid, c->grid_h);
     k_pack<<<(NFRAG + 255) / 256, 256, 0, st>>>(c->w, c->frag, c->fragT);
-    if(vkg_status s = nrc_pack_tc(c->ctx, c->w, c->wtc, st); s != VKG_OK) return s;
+    if(vkg_status s = nrc_pack_tc(c->ctx, c->w, c->wtc, st, c->wtc_t); s != VKG_OK) return s;
     VKG_TRY_CUDA(c->ctx, cudaStreamSynchronize(st));
     return cuda_check(c->ctx, cudaGetLastError(), "vkg_nrc_load");
 }

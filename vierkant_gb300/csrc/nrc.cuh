@@ -82,7 +82,10 @@ constexpr size_t ENCODED_BYTES = IN * 2;
 vkg_status nrc_predict(vkg_nrc *c, const float *feats, uint32_t n, const uint32_t *d_n, uint32_t *X, float *Y,
                        cudaStream_t st);
 // tcgen05 inference (nrc_tc.cu): BF16 B operands of all layers (NPARAM x 2 bytes, canonical K-major)
-vkg_status nrc_pack_tc(vkg_ctx *ctx, const float *W, uint16_t *wtc, cudaStream_t st);
+vkg_status nrc_pack_tc(vkg_ctx *ctx, const float *W, uint16_t *wtc, cudaStream_t st, uint16_t *wtc_t = nullptr);
+vkg_status nrc_backward_tc(vkg_ctx *ctx, const uint16_t *wtc_t, const uint32_t *H, const float *Y, const float *T,
+                           uint32_t n, const uint32_t *d_n, uint32_t *G, float *dXg, float *loss, uint32_t *err,
+                           cudaStream_t st);
 // MLP on tcgen05 over the encoded inputs X (n x 40 u32), or, with X == nullptr, encoding + MLP fused;
 // err receives 1 if a tensor-core wait ran out
 vkg_status nrc_infer_tc(vkg_ctx *ctx, const grid_config &gc, const __half2 *grid, const uint16_t *wtc,

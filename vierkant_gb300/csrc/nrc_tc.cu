@@ -30,7 +30,6 @@ constexpr uint32_t TC_W_BYTES = NPARAM * 2;      // all six layers, BF16 B opera
 constexpr uint32_t TC_A_BYTES = TC_TILE * IN * 2; // one A operand (20,480 B)
 constexpr uint32_t TC_SMEM = TC_W_BYTES + TC_A_BYTES;
 constexpr uint32_t TC_TIMEOUT = 1u;
-constexpr int TC_INFER_WG = 8;                    // warpgroups (tiles in flight) of the pipelined kernel
 
 namespace
 {
@@ -48,6 +47,20 @@ __global__ void k_pack_tc(const float *__restrict__ W, uint16_t *__restrict__ wt
     const int k = local / N, n = local - k * N;
     const __nv_bfloat16 b = __float2bfloat16_rn(W[e]);
     wtc[(layer_off(l) * 2 + tc::canon_offset(n, k, K)) / 2] = *reinterpret_cast<const uint16_t *>(&b);
+}
+
+// FP32 master weights -> BF16 operands of the backward: layer l as K_l x N_l (rows = the layer's
+// inputs, K = its outputs), K-major, so that D (128 x K_l) = G_l (128 x N_l) W_l^T is one UMMA chain
+__global__ void k_pack_tc_t(const float *__restrict__ W, uint16_t *__restrict__ wtc_t)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if(e >= NPARAM) return;
+    int l = 0;
+    while(l + 1 < NLAYER && e >= layer_off(l + 1)) ++l;
+    const int N = layer_out(l), local = e - layer_off(l);
+    const int k = local / N, n = local - k * N;
+    const __nv_bfloat16 b = __float2bfloat16_rn(W[e]);
+    wtc_t[(layer_off(l) * 2 + tc::canon_offset(k, n, N)) / 2] = *reinterpret_cast<const uint16_t *>(&b);
 }
 
 // FUSED: encode the feature records here; else read the encoded inputs X (n x 40 u32) written by k_encode
@@ -374,6 +387,165 @@ __global__ void __launch_bounds__(NWG * 128)
     if(warp == 0) tc::tmem_dealloc(tslot, COLS);
 }
 
+// ---- backward through the layers on tcgen05 ------------------------------------------------------
+// The mma.sync k_backward restated on the tensor cores with the warpgroup pipeline of k_infer_tc_wg:
+// per tile of 128 records, thread r owns record q = 128 tile + r:
+//   dy = dL/dy of the relative L2 loss (|y - t|^2 / (y^2 + 0.01), mean over 3n) -> G block 5 and the
+//   BF16 A operand (128 x 16);
+//   for l = 5 .. 1: D = G_l W_l^T (UMMA, TMEM), G_{l-1} = D * [H_l > 0] rounded to BF16 -> G block
+//   l - 1 and the next A operand (128 x 64);
+//   dX (the 32 hash-grid features) = G_0 W_0^T (N = 32) -> dXg in FP32.
+// Quantisation points equal k_backward's (FP32 sums, mask in FP32, BF16 rounding of each G); only
+// the summation order inside an MMA differs. Weights: wtc_t (k_pack_tc_t), resident in shared memory.
+constexpr uint32_t TC_G_BYTES = TC_TILE * HID * 2; // one A operand of the backward (16,384 B)
+template<int NWG>
+__global__ void __launch_bounds__(NWG * 128)
+        k_backward_tc_wg(const uint32_t *__restrict__ H, const float *__restrict__ Y, const float *__restrict__ T,
+                         uint32_t n_cap, const uint32_t *__restrict__ d_n, const uint16_t *__restrict__ wtc_t,
+                         uint32_t *__restrict__ G, float *__restrict__ dXg, float *__restrict__ loss_sum,
+                         uint32_t *__restrict__ err)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t mbar[NWG];
+    __shared__ uint32_t tslot;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, g = tid >> 7, r = tid & 127u;
+    uint8_t *sw = smem, *sa = smem + TC_W_BYTES + g * TC_G_BYTES;
+    for(uint32_t i = tid; i < TC_W_BYTES / 16; i += NWG * 128)
+        reinterpret_cast<uint4 *>(sw)[i] = reinterpret_cast<const uint4 *>(wtc_t)[i];
+    static_assert(NWG >= 1 && NWG <= 8, "at most 512 TMEM columns");
+    constexpr uint32_t COLS = NWG * 64 <= 64 ? 64 : (NWG * 64 <= 128 ? 128 : (NWG * 64 <= 256 ? 256 : 512));
+    if(warp == 0) tc::tmem_alloc(&tslot, COLS);
+    if(tid < NWG) tc::mbar_init(&mbar[tid], 1);
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tslot + 64u * g, lane_base = ((warp & 3u) * 32u) << 16;
+    const uint32_t sw_addr = tc::smem_addr(sw), sa_addr = tc::smem_addr(sa);
+    const uint32_t n = eff_n(n_cap, d_n), tiles = (n + TC_TILE - 1) / TC_TILE;
+    const float inv_count = n ? 1.f / (3.f * (float)n) : 0.f;
+    const uint32_t bar_id = g + 1;
+    uint32_t phase = 0;
+    bool failed = false;
+    float loss = 0.f;
+
+    for(uint32_t tile = blockIdx.x * NWG + g; tile < tiles && !failed; tile += gridDim.x * NWG)
+    {
+        const uint32_t q = tile * TC_TILE + r;
+        const bool valid = q < n;
+        // dL/dy (raw columns 0..2 of 16)
+        float dy[3] = {0.f, 0.f, 0.f};
+        if(valid)
+            for(int c = 0; c < 3; ++c)
+            {
+                const float y = Y[(size_t)q * 3 + c], t = T[(size_t)q * 3 + c];
+                const float den = y * y + 0.01f;
+                const float e = y - t;
+                loss += e * e / den;
+                dy[c] = 2.f * e / den * inv_count;
+            }
+        const uint32_t gy0 = pack_bf16(dy[0], dy[1]), gy1 = pack_bf16(dy[2], 0.f);
+        if(valid)
+        {
+            uint4 *gp = reinterpret_cast<uint4 *>(G + (size_t)q * 168 + 160);
+            gp[0] = make_uint4(gy0, gy1, 0u, 0u);
+            gp[1] = make_uint4(0u, 0u, 0u, 0u);
+        }
+        // A operand 128 x 16 (K = 16): columns 0..7 and 8..15
+        *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 0, 16)) = make_uint4(gy0, gy1, 0u, 0u);
+        *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        tc::wg_sync(bar_id);
+#pragma unroll 1
+        for(int l = NLAYER - 1; l >= 0; --l)
+        {
+            // D (128 x rows) = A (128 x K') * B^T with B = W_l as rows = inputs, K' = outputs
+            const uint32_t Kp = layer_out(l), rows = l == 0 ? 32u : (uint32_t)layer_in(l);
+            if(r == 0)
+            {
+                tc::fence_after_sync();
+                const uint32_t idesc = tc::idesc_bf16(TC_TILE, rows);
+                const uint32_t wb = sw_addr + (uint32_t)layer_off(l) * 2u;
+                for(uint32_t s = 0; s < Kp / 16; ++s)
+                    tc::mma_bf16(tmem, tc::smem_desc(sa_addr + 256u * s, 128u, Kp * 16u),
+                                 tc::smem_desc(wb + 256u * s, 128u, Kp * 16u), idesc, s > 0);
+                tc::mma_commit(&mbar[g]);
+            }
+            const bool ok = tc::mbar_wait(&mbar[g], phase);
+            if(tc::wg_sync_or(bar_id, !ok))
+            {
+                failed = true;
+                break;
+            }
+            phase ^= 1u;
+            tc::fence_after_sync();
+            if(l > 0)
+            {
+                // G_{l-1} = dH_l * [H_l > 0]; H_l is block l - 1 of H
+                const uint4 *hp = reinterpret_cast<const uint4 *>(H + (size_t)q * 160 + (l - 1) * 32);
+#pragma unroll
+                for(int c = 0; c < 4; ++c)
+                {
+                    float v[16];
+                    tc::tmem_ld16(tmem + lane_base + 16u * c, v);
+                    tc::tmem_ld_wait();
+                    const uint4 h0 = valid ? hp[2 * c] : make_uint4(0u, 0u, 0u, 0u);
+                    const uint4 h1 = valid ? hp[2 * c + 1] : make_uint4(0u, 0u, 0u, 0u);
+                    const uint32_t hw[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+                    uint32_t gv[8];
+#pragma unroll
+                    for(int j = 0; j < 8; ++j)
+                    {
+                        const float m0 = (hw[j] & 0x7FFFu) ? 1.f : 0.f, m1 = ((hw[j] >> 16) & 0x7FFFu) ? 1.f : 0.f;
+                        gv[j] = pack_bf16(v[2 * j] * m0, v[2 * j + 1] * m1);
+                    }
+                    *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 16 * c, HID)) = make_uint4(gv[0], gv[1], gv[2], gv[3]);
+                    *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 16 * c + 8, HID)) =
+                            make_uint4(gv[4], gv[5], gv[6], gv[7]);
+                    if(valid)
+                    {
+                        uint4 *gp = reinterpret_cast<uint4 *>(G + (size_t)q * 168 + (l - 1) * 32 + 8 * c);
+                        gp[0] = make_uint4(gv[0], gv[1], gv[2], gv[3]);
+                        gp[1] = make_uint4(gv[4], gv[5], gv[6], gv[7]);
+                    }
+                }
+                tc::fence_async_smem();
+            }
+            else
+            {
+                // dX of the 32 hash-grid features, FP32
+#pragma unroll
+                for(int c = 0; c < 2; ++c)
+                {
+                    float v[16];
+                    tc::tmem_ld16(tmem + lane_base + 16u * c, v);
+                    tc::tmem_ld_wait();
+                    if(valid)
+                    {
+                        float4 *dp = reinterpret_cast<float4 *>(dXg + (size_t)q * 32 + 16 * c);
+#pragma unroll
+                        for(int j = 0; j < 4; ++j) dp[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+                    }
+                }
+            }
+            tc::fence_before_sync();
+            tc::wg_sync(bar_id);
+        }
+    }
+    for(int o = 16; o > 0; o >>= 1) loss += __shfl_down_sync(0xffffffffu, loss, o);
+    if((tid & 31u) == 0 && loss_sum) atomicAdd(loss_sum, loss * inv_count);
+    if(failed)
+    {
+        if(r == 0) atomicOr(err, TC_TIMEOUT);
+        tc::mbar_wait(&mbar[g], phase);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if(warp == 0) tc::tmem_dealloc(tslot, COLS);
+}
+
 // diagnostic: the error path every tcgen05 kernel here takes when a wait runs out, run to its end on
 // purpose. Each CTA allocates TMEM and waits on an mbarrier that nothing arrives on, with a limit of
 // limit_ns instead of the kernels' 1 s; the wait gives up, the CTA sets TC_TIMEOUT, waits a second
@@ -582,26 +754,68 @@ vkg_status nrc_wgrad_tc(vkg_ctx *ctx, const uint32_t *X, const uint32_t *H, cons
     return cuda_check(ctx, cudaGetLastError(), "k_wgrad_tc");
 }
 
-vkg_status nrc_pack_tc(vkg_ctx *ctx, const float *W, uint16_t *wtc, cudaStream_t st)
+vkg_status nrc_pack_tc(vkg_ctx *ctx, const float *W, uint16_t *wtc, cudaStream_t st, uint16_t *wtc_t)
 {
     k_pack_tc<<<(NPARAM + 255) / 256, 256, 0, st>>>(W, wtc);
+    if(wtc_t) k_pack_tc_t<<<(NPARAM + 255) / 256, 256, 0, st>>>(W, wtc_t);
     return cuda_check(ctx, cudaGetLastError(), "k_pack_tc");
 }
 
 // the pipelined MLP over encoded inputs X: inference (H null) or the training forward (H receives the
-// activations); TC_INFER_WG warpgroups (tiles in flight) per SM
+// activations)
+template<int NWG>
+vkg_status launch_forward_tc(vkg_ctx *ctx, const uint16_t *wtc, const uint32_t *X, uint32_t n, const uint32_t *d_n,
+                             float *Y, uint32_t *H, uint32_t *err, cudaStream_t st)
+{
+    const uint32_t smem = TC_W_BYTES + NWG * TC_A_BYTES;
+    auto kern = H ? k_infer_tc_wg<NWG, true> : k_infer_tc_wg<NWG, false>;
+    VKG_TRY_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    VKG_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NWG * 128, smem));
+    // TMEM: a resident CTA holds NWG x 64 of the SM's 512 columns
+    per_sm = std::max(1, std::min(per_sm, 512 / (NWG * 64)));
+    const uint32_t tiles = (n + TC_TILE - 1) / TC_TILE;
+    const uint32_t grid_n = std::min<uint32_t>((tiles + NWG - 1) / NWG, (uint32_t)(ctx->num_sms * per_sm));
+    kern<<<grid_n, NWG * 128, smem, st>>>(X, n, d_n, wtc, Y, err, H);
+    return cuda_check(ctx, cudaGetLastError(), "k_infer_tc_wg");
+}
+
 vkg_status nrc_forward_tc(vkg_ctx *ctx, const uint16_t *wtc, const uint32_t *X, uint32_t n, const uint32_t *d_n,
                           float *Y, uint32_t *H, uint32_t *err, cudaStream_t st)
 {
     if(n == 0) return VKG_OK;
-    constexpr int NWG = TC_INFER_WG;
-    const uint32_t smem = TC_W_BYTES + NWG * TC_A_BYTES;
-    auto kern = H ? k_infer_tc_wg<NWG, true> : k_infer_tc_wg<NWG, false>;
-    VKG_TRY_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // as many tiles in flight per SM as the batch fills: eight warpgroups once every SM gets eight tiles
+    const uint32_t tiles = (n + TC_TILE - 1) / TC_TILE, sms = (uint32_t)ctx->num_sms;
+    if(tiles >= 8 * sms) return launch_forward_tc<8>(ctx, wtc, X, n, d_n, Y, H, err, st);
+    if(tiles >= 4 * sms) return launch_forward_tc<4>(ctx, wtc, X, n, d_n, Y, H, err, st);
+    return launch_forward_tc<2>(ctx, wtc, X, n, d_n, Y, H, err, st);
+}
+
+template<int NWG>
+vkg_status launch_backward_tc(vkg_ctx *ctx, const uint16_t *wtc_t, const uint32_t *H, const float *Y, const float *T,
+                              uint32_t n, const uint32_t *d_n, uint32_t *G, float *dXg, float *loss, uint32_t *err,
+                              cudaStream_t st)
+{
+    const uint32_t smem = TC_W_BYTES + NWG * TC_G_BYTES;
+    VKG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_backward_tc_wg<NWG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    VKG_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_backward_tc_wg<NWG>, NWG * 128, smem));
+    per_sm = std::max(1, std::min(per_sm, 512 / (NWG * 64)));
     const uint32_t tiles = (n + TC_TILE - 1) / TC_TILE;
-    const uint32_t grid_n = std::min<uint32_t>((tiles + NWG - 1) / NWG, (uint32_t)ctx->num_sms);
-    kern<<<grid_n, NWG * 128, smem, st>>>(X, n, d_n, wtc, Y, err, H);
-    return cuda_check(ctx, cudaGetLastError(), "k_infer_tc_wg");
+    const uint32_t grid_n = std::min<uint32_t>((tiles + NWG - 1) / NWG, (uint32_t)(ctx->num_sms * per_sm));
+    k_backward_tc_wg<NWG><<<grid_n, NWG * 128, smem, st>>>(H, Y, T, n, d_n, wtc_t, G, dXg, loss, err);
+    return cuda_check(ctx, cudaGetLastError(), "k_backward_tc_wg");
+}
+
+vkg_status nrc_backward_tc(vkg_ctx *ctx, const uint16_t *wtc_t, const uint32_t *H, const float *Y, const float *T,
+                           uint32_t n, const uint32_t *d_n, uint32_t *G, float *dXg, float *loss, uint32_t *err,
+                           cudaStream_t st)
+{
+    if(n == 0) return VKG_OK;
+    const uint32_t tiles = (n + TC_TILE - 1) / TC_TILE, sms = (uint32_t)ctx->num_sms;
+    if(tiles >= 8 * sms) return launch_backward_tc<8>(ctx, wtc_t, H, Y, T, n, d_n, G, dXg, loss, err, st);
+    if(tiles >= 4 * sms) return launch_backward_tc<4>(ctx, wtc_t, H, Y, T, n, d_n, G, dXg, loss, err, st);
+    return launch_backward_tc<2>(ctx, wtc_t, H, Y, T, n, d_n, G, dXg, loss, err, st);
 }
 
 vkg_status nrc_infer_tc(vkg_ctx *ctx, const grid_config &gc, const __half2 *grid, const uint16_t *wtc,
