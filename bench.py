@@ -557,6 +557,60 @@ def path_tracer_block(ctx, frames=256, bytes_per_ray=None, cpu=True):
     return out
 
 
+def nrc_cut_sweep(frames=256):
+    """The radiance cache's cut point on the 1920x1080 Cornell workload: for terminate_depth 0, 1 and 2
+    (the surface interaction at which rendering paths end in the cache; 2 is the workload's), the GPU
+    time the cache tracer (1 spp per frame, 65,536 training paths per frame) needs to reach the plain
+    tracer's 64-spp crop RMSE against the FP64 oracle, over the plain tracer's time. Prints one JSON
+    line; not part of the default run."""
+    import numpy as np
+    from vierkant_gb300 import geometry
+    from vierkant_gb300.nrc import NeuralRadianceCache, cache_for_scene
+    from vierkant_gb300.pathtracer import PBRPathTracer, Scene, procedural_sky, sun_direction
+    from vierkant_gb300.raytracing import Context
+    ctx = Context(0)
+    g1080 = np.load(ROOT / "tests" / "golden" / "pt_oracle_crop_1080.npz")
+    sc = geometry.cornell_scene(SEED, 2, 64, 16)
+    env = procedural_sky(ctx, 2048, 1024, sun_direction(), 5e4, 3.8e-5)
+    scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], sc["materials"], env)
+
+    def settings(spp):
+        s = PBRPathTracer.default_settings()
+        s.num_samples, s.max_trace_depth, s.rr_start_depth = spp, 6, 3
+        s.resolution[0], s.resolution[1] = 1920, 1080
+        return s
+
+    cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, 1920, 1080)
+    pt = PBRPathTracer(ctx, seed=SEED, settings=settings(64))
+    pt.render_scene(scene, cam)
+    pt.reset_accumulator()
+    target, _ = _crop_error(pt.render_scene(scene, cam).cpu().numpy(), g1080)
+    plain_ms = pt.statistics().total_ms
+    pt.close()
+    out = {"plain_64spp_ms": round(plain_ms, 2), "rmse_target": round(target, 4), "frames": frames, "cuts": []}
+    for term in (0, 1, 2):
+        cfg = NeuralRadianceCache.default_config()
+        cfg.terminate_depth = term
+        pt = PBRPathTracer(ctx, seed=SEED + 1, settings=settings(1))
+        cache = cache_for_scene(ctx, scene, cfg)
+        pt.attach_cache(cache)
+        tot, reached, rmse, bias = 0.0, None, None, None
+        for f in range(frames):
+            im = pt.render_scene(scene, cam)
+            tot += pt.statistics().total_ms
+            rmse, bias = _crop_error(im.cpu().numpy(), g1080)
+            if reached is None and rmse <= target:
+                reached = {"frames": f + 1, "ms": round(tot, 1)}
+        out["cuts"].append({"terminate_depth": term, "reached": reached,
+                            "time_vs_plain": round(reached["ms"] / plain_ms, 3) if reached else None,
+                            "ms_per_frame": round(tot / frames, 3), "rmse_last": round(rmse, 4),
+                            "bias_last": round(bias, 4), "kernel_error": int(cache.info().kernel_error)})
+        pt.close()
+        cache.close()
+    scene.close()
+    print(json.dumps(out), flush=True)
+
+
 def features_block(ctx):
     """The full material and light set: the Cornell box with the showcase materials (glass, rough
     glass, clearcoat, sheen, diffuse transmission, iridescence, metal-rough), one light of every
@@ -1086,7 +1140,12 @@ def main():
     ap.add_argument("--nrc-frames", type=int, default=256)
     ap.add_argument("--profile-case", choices=["pt-frame", "nrc", "batch", "stress", "features", "media"], default=None,
                     help="run one small workload for a profiler capture and exit (no JSON line)")
+    ap.add_argument("--nrc-cut-sweep", action="store_true",
+                    help="measure the radiance cache's equal-RMSE time for terminate_depth 0, 1, 2 and exit")
     args = ap.parse_args()
+    if args.nrc_cut_sweep:
+        nrc_cut_sweep(args.nrc_frames)
+        return
     if args.profile_case:
         profile_case(args.profile_case)
         return

@@ -339,23 +339,32 @@ __global__ void __launch_bounds__(NWG * 128)
             tc::fence_after_sync();
             if(l + 1 < NLAYER)
             {
+                // two TMEM loads in flight per wait
 #pragma unroll
-                for(int c = 0; c < 4; ++c)
+                for(int c2 = 0; c2 < 2; ++c2)
                 {
-                    float v[16];
-                    tc::tmem_ld16(tmem + lane_base + 16u * c, v);
+                    float v[2][16];
+                    tc::tmem_ld16(tmem + lane_base + 32u * c2, v[0]);
+                    tc::tmem_ld16(tmem + lane_base + 32u * c2 + 16u, v[1]);
                     tc::tmem_ld_wait();
-                    uint32_t hv[8];
 #pragma unroll
-                    for(int j = 0; j < 8; ++j) hv[j] = pack_bf16(fmaxf(v[2 * j], 0.f), fmaxf(v[2 * j + 1], 0.f));
-                    *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 16 * c, HID)) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
-                    *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 16 * c + 8, HID)) =
-                            make_uint4(hv[4], hv[5], hv[6], hv[7]);
-                    if(TRAIN && q < n)
+                    for(int cc = 0; cc < 2; ++cc)
                     {
-                        uint4 *hp = reinterpret_cast<uint4 *>(H + (size_t)q * (5 * HID / 2) + l * (HID / 2) + 8 * c);
-                        hp[0] = make_uint4(hv[0], hv[1], hv[2], hv[3]);
-                        hp[1] = make_uint4(hv[4], hv[5], hv[6], hv[7]);
+                        const int c = 2 * c2 + cc;
+                        uint32_t hv[8];
+#pragma unroll
+                        for(int j = 0; j < 8; ++j)
+                            hv[j] = pack_bf16(fmaxf(v[cc][2 * j], 0.f), fmaxf(v[cc][2 * j + 1], 0.f));
+                        *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 16 * c, HID)) =
+                                make_uint4(hv[0], hv[1], hv[2], hv[3]);
+                        *reinterpret_cast<uint4 *>(sa + tc::canon_offset(r, 16 * c + 8, HID)) =
+                                make_uint4(hv[4], hv[5], hv[6], hv[7]);
+                        if(TRAIN && q < n)
+                        {
+                            uint4 *hp = reinterpret_cast<uint4 *>(H + (size_t)q * (5 * HID / 2) + l * (HID / 2) + 8 * c);
+                            hp[0] = make_uint4(hv[0], hv[1], hv[2], hv[3]);
+                            hp[1] = make_uint4(hv[4], hv[5], hv[6], hv[7]);
+                        }
                     }
                 }
                 tc::fence_async_smem();
