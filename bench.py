@@ -289,11 +289,16 @@ def run_ours(args):
         bvh.closest_hit_host(rays_host, hits_host)
     if ws > 1:
         dist.barrier()
-    e2e_steps = max(3, args.steps // 2)
-    t0 = time.perf_counter()
+    # per-call wall times (each call synchronises); the median call, so that one slow host-side call
+    # does not set the figure; the mean is reported beside it
+    e2e_steps = max(10, args.steps)
+    e2e_times = []
     for _ in range(e2e_steps):
+        t0 = time.perf_counter()
         bvh.closest_hit_host(rays_host, hits_host)
-    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / e2e_steps, batch.device)
+        e2e_times.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = max_over_ranks(statistics.median(e2e_times), batch.device)
+    e2e_mean_ms = max_over_ranks(statistics.mean(e2e_times), batch.device)
     e2e_value = replica_throughput(n, ws, e2e_ms)
     # the host-buffer results must equal the device results
     dev_hits = hits.cpu()
@@ -345,7 +350,9 @@ def run_ours(args):
                                "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
                 "hits_sha256_16": hits_digest,
                 "e2e": {"value": round(e2e_value, 1), "unit": "Mrays/s", "h2d_bytes_per_step": n * RAY_BYTES,
-                        "d2h_bytes_per_step": n * HIT_BYTES, "matches_device": e2e_ok},
+                        "d2h_bytes_per_step": n * HIT_BYTES, "matches_device": e2e_ok,
+                        "timing": f"median of {e2e_steps} host-buffer calls (wall clock, each synchronised)",
+                        "mean_value": round(replica_throughput(n, ws, e2e_mean_ms), 1)},
                 "gpu_launches": args.steps, "roofline": roofline, "clocks": clk}
         if cpu is not None:
             line["cpu_baseline"] = cpu
@@ -377,6 +384,22 @@ def _crop_error(img, golden):
     x0, y0, w, h = (int(v) for v in golden["crop"])
     c = img[y0:y0 + h, x0:x0 + w].astype(np.float64)
     return math.sqrt(float(np.mean((_lum(c) - _lum(ref)) ** 2))), float((c.sum() - ref.sum()) / ref.sum())
+
+
+def _parity(img, g, spp):
+    """one render of `spp` samples per pixel against an FP64 full-frame fixture, on luminance: relative
+    bias, its z-score and RMSE against the noise both estimates carry, the GPU's per-sample variance
+    taken as the fixture's (the statistical tests in tests/ measure it from independent batches)"""
+    import numpy as np
+    ref = g["mean"].astype(np.float64)
+    lv = g["lum_var"].astype(np.float64)
+    lg, lr = _lum(img.astype(np.float64)), _lum(ref)
+    var = lv / spp + lv / int(g["spp"])
+    return {"rmse": round(math.sqrt(float(np.mean((lg - lr) ** 2))), 4),
+            "expected_noise": round(math.sqrt(float(np.mean(var))), 4),
+            "bias": round(float((lg.sum() - lr.sum()) / lr.sum()), 5),
+            "z": round(float((lg.sum() - lr.sum()) / math.sqrt(var.sum())), 2),
+            "oracle": "FP64 %d spp, full frame" % int(g["spp"])}
 
 
 def denoise_timing(ctx, pixels, w, h, reps=20):
@@ -673,12 +696,7 @@ def features_block(ctx):
     img = pt.render_scene(scene, cam).cpu().numpy().astype(np.float64)
     pt.close()
     scene.close()
-    ref = g["mean"].astype(np.float64)
-    rmse = math.sqrt(np.mean((_lum(img) - _lum(ref)) ** 2))
-    out["lights_parity_256x144_1024spp"] = {
-        "rmse": round(rmse, 4), "bias": round(float((img.sum() - ref.sum()) / ref.sum()), 5),
-        "expected_noise": round(math.sqrt(np.mean(g["lum_var"]) / 1024 + np.mean(g["lum_var"]) / int(g["spp"])), 4),
-        "oracle": "FP64 %d spp, full frame" % int(g["spp"])}
+    out["lights_parity_256x144_1024spp"] = _parity(img, g, 1024)
     # media: fog, absorbing glass, emissive gas and scattering glass spheres, the analytic lights, a
     # constant 0.2 environment, 10 segments, against its FP64 oracle
     g = np.load(ROOT / "tests" / "golden" / "pt_oracle_media.npz")
@@ -692,12 +710,7 @@ def features_block(ctx):
     img = pt.render_scene(scene, cam).cpu().numpy().astype(np.float64)
     pt.close()
     scene.close()
-    ref = g["mean"].astype(np.float64)
-    rmse = math.sqrt(np.mean((_lum(img) - _lum(ref)) ** 2))
-    out["media_parity_256x144_1024spp"] = {
-        "rmse": round(rmse, 4), "bias": round(float((img.sum() - ref.sum()) / ref.sum()), 5),
-        "expected_noise": round(math.sqrt(np.mean(g["lum_var"]) / 1024 + np.mean(g["lum_var"]) / int(g["spp"])), 4),
-        "oracle": "FP64 %d spp, full frame" % int(g["spp"])}
+    out["media_parity_256x144_1024spp"] = _parity(img, g, 1024)
     return out
 
 

@@ -710,7 +710,7 @@ typedef struct vkg_nrc_config
     uint32_t terminate_depth; /* rendering paths end in the cache at this surface interaction (2) */
     uint32_t train_depth;     /* training targets are recorded at the first this-many interactions (4) */
     uint32_t train_steps;     /* optimiser steps per frame; 0: ceil(train_paths * train_depth / batch_size) */
-    uint32_t infer_kernel;    /* 0: default, 1: mma.sync MLP, 2: tcgen05 MLP, 3: tcgen05 MLP with the encoding fused */
+    uint32_t infer_kernel;    /* 0: default (2), 1: mma.sync MLP, 2: tcgen05 MLP, 3: tcgen05 MLP with the encoding fused */
     uint32_t train_kernel;    /* 0: default (3), 1: mma.sync forward / backward + FP32 CUDA-core weight
                                  gradients, 2: mma.sync forward / backward + tcgen05 weight gradients,
                                  3: everything on tcgen05 (forward, backward through the layers, weight
