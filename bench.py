@@ -337,7 +337,23 @@ def run_ours(args):
         pt_block = path_tracer_block(ctx, frames=args.nrc_frames, bytes_per_ray=bytes_per_launch / n,
                                      cpu=(ws == 1 and not args.no_cpu))
         batch_block = batched_block(ctx)
-        stress = stress_block(ctx)
+        stress = stress_block(ctx, cpu=(ws == 1 and not args.no_cpu))
+        twin = pt_block.get("plain_720p_64spp", {}).get("cpu_baseline")
+        if twin:
+            # the batched jobs on the host cores, extrapolated from the FP32 twin's per-sample rate on
+            # the Cornell crop (the same scene family, 6 segments)
+            cpu_s = batch_block["paths"] / twin["value"]
+            batch_block["cpu_baseline"] = {
+                "value": round(batch_block["rays"] / cpu_s / 1e6, 4), "unit": "Mrays/s", "cores": twin["cores"],
+                "kind": "port", "sample": "extrapolated: %d paths at the FP32 twin's %.0f samples/s on the Cornell "
+                                          "crop = %.0f s" % (batch_block["paths"], twin["value"], cpu_s)}
+        batch_block["traversal_roofline"] = {
+            "achieved": round(batch_block["rays"] * bytes_per_launch / n / (batch_block["render_ms"] * 1e-3) / 1e9, 1),
+            "unit": "GB/s", "peak": measured_peaks()[0], "peak_source": measured_peaks()[1],
+            "bytes_per_ray": round(bytes_per_launch / n, 1),
+            "note": "rays x the closest-hit batch's algorithmic bytes per ray over the whole render time"}
+        batch_block["traversal_roofline"]["frac"] = round(batch_block["traversal_roofline"]["achieved"] /
+                                                          batch_block["traversal_roofline"]["peak"], 4)
         features = features_block(ctx)
 
     if rank == 0:
@@ -771,7 +787,38 @@ def batched_block(ctx):
             "one_scene_at_a_time_ms": round(seq_ms, 2), "speedup_vs_one_at_a_time": round(seq_ms / best, 3)}
 
 
-def stress_block(ctx):
+def stress_cpu_baseline(st, env_rgb, budget_s=15.0):
+    """The stress scene on the host cores: the oracle's FP64 instanced estimator (a BVH per mesh, an
+    instance BVH, double arithmetic) on a 32x32 crop of the 3840x2160 frame at 1 spp per pass, 8
+    segments, all threads; samples/s (the FP32 twin has no instanced mode)."""
+    import numpy as np
+    import oracle
+    W, H, crop = 3840, 2160, (1856, 1016, 32, 32)
+    th = float(np.float32(math.tan(math.radians(40.0) / 2.0)))
+    cam = oracle.camera((0, 120, 300), (0, 0, 0), (0, 1, 0), th, W, H)
+    inst = st["instances"]
+    t0 = time.perf_counter()
+    bvhs = [oracle.CpuBVH(m[0], m[1], 2) for m in st["meshes"]]
+    build_s = time.perf_counter() - t0
+    total, paths, passes, rays = 0.0, 0, 0, 0
+    while total < budget_s or passes < 2:
+        t0 = time.perf_counter()
+        _, _, r = oracle.pt_render_instanced(st["meshes"], inst["transform"], inst["blas"], inst["material"],
+                                             st["materials"], env_rgb, cam, 1, seed=SEED, batch=passes, max_depth=8,
+                                             rr_depth=3, crop=crop, mesh_bvhs=bvhs)
+        total += time.perf_counter() - t0
+        paths += crop[2] * crop[3]
+        rays += r[0] + r[1]
+        passes += 1
+    return {"value": round(paths / total, 1), "unit": "samples/s", "cores": os.cpu_count() or 1, "kind": "port",
+            "mrays_per_s": round(rays / total / 1e6, 4),
+            "sample": f"{passes} passes x 1 spp on the 32x32 crop at (1856, 1016), {total:.1f} s "
+                      f"(+ {build_s:.1f} s building the mesh BVHs, untimed)",
+            "method": "the oracle's FP64 instanced estimator (oracle/pathtrace.c) on all host threads; the "
+                      "reference has no CPU path tracer"}
+
+
+def stress_block(ctx, cpu=False):
     """The stress workload: an 8,380,418-triangle fBm terrain (2048^2 vertices) plus 100,000 instances of
     20 cube-spheres (5,292 to 50,700 triangles) under a two-level BVH, rendered at 3840x2160 x 16 spp,
     8 segments, Russian roulette from the 3rd interaction, environment as the Cornell workload."""
@@ -841,6 +888,8 @@ def stress_block(ctx):
                              "nrc_vs_plain_time": round(reached["ms"] / best.total_ms, 3) if reached else None,
                              "nrc_frames_run": f + 1, "nrc_ms_total": round(tot, 1),
                              "nrc_rmse_last": round(rmse, 4), "nrc_bias_last": round(bias, 5)}
+    if cpu:
+        out["cpu_baseline"] = stress_cpu_baseline(st, env.cpu().numpy())
     scene.close()
     return out
 
