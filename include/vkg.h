@@ -158,7 +158,13 @@ typedef struct vkg_material
     float scatter_factor;        /* [0, 1] */
     float phase_g;               /* Henyey-Greenstein asymmetry, (-1, 1) */
     uint32_t null_surface;       /* 1: no surface interaction; emission becomes the medium's */
-    float pad[2];
+    /* chromatic dispersion (KHR_materials_dispersion, the reference's material_struct_t::dispersion,
+       RayBuilder.hpp:99-100): 20 / Abbe number, >= 0; with transmission > 0 a path samples one
+       wavelength in [400, 700] nm at such a surface and refracts with the Cauchy ior of that
+       wavelength (ior at the d-line); the first transmission locks the wavelength for the rest of the
+       path and tints its throughput by the wavelength's colour (raypipeline.slang:481-491, :651-659) */
+    float dispersion;
+    float pad;
 } vkg_material; /* 144 B */
 /* ---- analytic lights ----------------------------------------------------------------------
  * The reference's LightType (punctual_light.hpp:20-34); AREA is reserved for emissive triangles and
@@ -546,8 +552,8 @@ vkg_status vkg_gltf_destroy(vkg_gltf *g);
 /* material_struct_t -> vkg_material: colour rgb, emission rgb x emission.a (the emissive strength, as
    the closest-hit shader multiplies them), the scalar lobes, sheen colour rgb, iridescence strength /
    ior and the thickness range's maximum (what the shader reads), the media fields and two_sided.
-   Texture indices, blend mode, alpha cutoff and dispersion have no counterpart and are dropped;
-   *dropped (may be NULL) counts the records that use any of them. */
+   Texture indices, blend mode and alpha cutoff have no counterpart and are dropped; *dropped (may
+   be NULL) counts the records that use any of them. Dispersion is read into vkg_material::dispersion. */
 vkg_status vkg_materials_from_wire(const void *records, uint32_t n, vkg_material *out, uint32_t *dropped);
 /* per entry: where its triangles are in the mesh buffers */
 typedef struct vkg_wire_entry_info

@@ -29,8 +29,9 @@ vkg_status vkg_diag_wait_timeout(vkg_ctx *ctx, uint32_t num_ctas, uint64_t limit
 /* record the random numbers the tracer's kernels draw (d_buf NULL: stop). From the next render on,
  * the path of sample s through window pixel p writes record r = s * pixels + p of d_buf (floats):
  * [0..1] the camera jitter, then per segment i < max_segments the segment's uniforms at
- * 2 + 15 i (8, 11 or 15 of them; the rest of the record is left as it was). d_buf must hold
- * samples x pixels x (2 + 15 max_segments) floats for the largest render made while set. */
+ * 2 + 16 i (8, 11 or 15 of them, one more when a material disperses; the rest of the record is left
+ * as it was). d_buf must hold samples x pixels x (2 + 16 max_segments) floats for the largest render
+ * made while set. */
 vkg_status vkg_diag_tracer_uniforms(vkg_tracer *tracer, float *d_buf, uint32_t max_segments);
 
 #ifdef __cplusplus

@@ -281,7 +281,8 @@ MATERIAL_DTYPE = np.dtype([("base_color", "<f4", 3), ("roughness", "<f4"), ("met
                            ("diffuse_transmission_color", "<f4", 3), ("iridescence", "<f4"),
                            ("iridescence_ior", "<f4"), ("iridescence_thickness", "<f4"), ("attenuation_color", "<f4", 3),
                            ("attenuation_distance", "<f4"), ("scatter_color", "<f4", 3), ("scatter_factor", "<f4"),
-                           ("phase_g", "<f4"), ("null_surface", "<u4"), ("pad", "<f4", 2)])
+                           ("phase_g", "<f4"), ("null_surface", "<u4"), ("dispersion", "<f4"),
+                           ("pad", "<f4")])
 
 
 class orc_pt_scene(C.Structure):
@@ -519,6 +520,21 @@ def pt_render_instanced(meshes, o2w, inst_mesh, inst_mat, mats, env_rgb, cam, sp
     L.orc_pt_render_instanced(C.byref(scene), C.byref(inst), C.byref(env), C.byref(cam), C.byref(st), ptr(out),
                               ptr(sq), ptr(stats), nthreads)
     return out, sq, (int(stats[0]), int(stats[1]))
+
+
+def cauchy_ior(ior, dispersion, lam):
+    L = orc()
+    L.orc_cauchy_ior.restype = C.c_double
+    L.orc_cauchy_ior.argtypes = [C.c_double, C.c_double, C.c_double]
+    return L.orc_cauchy_ior(ior, dispersion, lam)
+
+
+def lambda_rgb(lam):
+    L = orc()
+    L.orc_lambda_rgb.argtypes = [C.c_double, C.c_void_p]
+    out = np.zeros(3)
+    L.orc_lambda_rgb(lam, ptr(out))
+    return out
 
 
 def phase_hg(cos_theta, g):

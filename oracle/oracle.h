@@ -132,7 +132,8 @@ typedef struct {
     float iridescence, iridescence_ior, iridescence_thickness;
     float attenuation_color[3], attenuation_distance, scatter_color[3], scatter_factor, phase_g;
     uint32_t null_surface;
-    float pad[2];
+    float dispersion; /* KHR_materials_dispersion: 20 / Abbe number (with transmission > 0) */
+    float pad;
 } orc_pt_material; /* same 144-byte layout as vkg_material */
 
 typedef struct {
@@ -240,6 +241,8 @@ void orc_bsdf_sample(const orc_pt_material *m, const double n[3], const double v
                      double dir[3], double *pdf, double f[3], int *transmission);
 void orc_phase_hg_sample(double x, double y, double g, double dir[3], double *pdf);
 double orc_phase_hg(double cos_theta, double g);
+double orc_cauchy_ior(double ior, double dispersion, double lambda);
+void orc_lambda_rgb(double lambda, double out[3]);
 void orc_iridescent_fresnel(double outside, double film, const double f0[3], double thickness, double cos1,
                             double out[3]);
 double orc_bsdf_eval(const orc_pt_material *m, const double l[3], const double n[3], const double v[3], double eta,

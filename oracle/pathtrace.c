@@ -95,6 +95,13 @@ static orc_medium *orc_media_table(const orc_pt_scene *scene, const orc_pt_setti
     return media;
 }
 
+static uint32_t orc__any_dispersive(const orc_pt_scene *scene)
+{
+    for(uint32_t i = 0; i < scene->nmat; ++i)
+        if(scene->mats[i].dispersion > 0.f && scene->mats[i].transmission > 0.f) return 1u;
+    return 0u;
+}
+
 typedef struct {
     const orc_pt_scene *scene;
     const orc_bvh *bvh;
@@ -116,6 +123,7 @@ typedef struct {
     atomic_uint next;
     atomic_ullong ext, shadow;
     int fp64;
+    uint32_t dispersion; /* a transmissive material disperses: one more uniform per segment */
     uint32_t fork_depth; /* the variance split's fork segment (orc_pt_variance_split) */
     double *split;       /* [pixels][4] of orc_pt_variance_split */
 } orc_pt_job;
@@ -767,6 +775,14 @@ void orc_phase_hg_sample(double x, double y, double g, double dir[3], double *pd
 
 double orc_phase_hg(double cos_theta, double g) { return d_phase_hg(cos_theta, g); }
 
+/* chromatic dispersion (FP64): the Cauchy ior of a wavelength and its Rec.709 colour */
+double orc_cauchy_ior(double ior, double dispersion, double lambda) { return d_cauchy_ior(ior, dispersion, lambda); }
+void orc_lambda_rgb(double lambda, double out[3])
+{
+    d_v3 c = d_lambda_rgb(lambda);
+    out[0] = c.x, out[1] = c.y, out[2] = c.z;
+}
+
 void orc_iridescent_fresnel(double outside, double film, const double f0[3], double thickness, double cos1,
                             double out[3])
 {
@@ -848,6 +864,7 @@ int orc_pt_render(int fp64, const orc_pt_scene *scene, const orc_bvh *bvh, const
     orc_pt_job J;
     memset(&J, 0, sizeof(J));
     J.scene = scene;
+    J.dispersion = orc__any_dispersive(scene);
     J.bvh = bvh;
     J.env = env;
     J.cam = cam;
@@ -948,6 +965,7 @@ int orc_pt_variance_split(const orc_pt_scene *scene, const orc_bvh *bvh, const o
     orc_pt_job J;
     memset(&J, 0, sizeof(J));
     J.scene = scene;
+    J.dispersion = orc__any_dispersive(scene);
     J.bvh = bvh;
     J.env = env;
     J.cam = cam;
@@ -1000,6 +1018,7 @@ int orc_pt_render_instanced(const orc_pt_scene *scene, const orc_pt_instances *i
     orc_pt_job J;
     memset(&J, 0, sizeof(J));
     J.scene = scene;
+    J.dispersion = orc__any_dispersive(scene);
     J.inst = inst;
     J.ibvh = B;
     J.env = env;

@@ -18,7 +18,7 @@ from vierkant_gb300.pathtracer import PBRPathTracer, Scene, procedural_sky, sun_
 pytestmark = pytest.mark.gpu
 
 W, H, CROP, SPP, DEPTH = 64, 36, (8, 4, 16, 12), 4, 6
-STRIDE = 2 + 15 * DEPTH
+STRIDE = 2 + 16 * DEPTH
 
 
 def minstd_rand0(seed, k):
@@ -61,9 +61,9 @@ def expected_check(rec, bseed, x, y, rs):
         jx, jy = f(ax - f(math.floor(ax))), f(ay - f(math.floor(ay)))
         assert d[0].tobytes() == jx.tobytes() and d[1].tobytes() == jy.tobytes(), (x, y, s)
         for i in range(DEPTH):
-            seg = d[2 + 15 * i: 2 + 15 * i + 8]
+            seg = d[2 + 16 * i: 2 + 16 * i + 8]
             if np.isnan(seg[0]):
-                assert np.all(np.isnan(d[2 + 15 * i:])), (x, y, s, i)
+                assert np.all(np.isnan(d[2 + 16 * i:])), (x, y, s, i)
                 break
             chain = rs.xxhash(chain, i)
             l = chain

@@ -442,3 +442,24 @@ def test_iridescent_fresnel_against_independent_transcription():
         ref = _iridescent_fresnel_numpy(outside, film, f0, thick, cos1)
         # the oracle keeps the shader's single-precision constants (as the GPU does): ~1e-7 of the O(1) terms
         assert np.allclose(out, ref, rtol=2e-6, atol=1e-6), (out, ref)
+
+
+def test_dispersion_cauchy_and_white_balance():
+    """chromatic dispersion (utils/bsdf.slang:46-91): the Cauchy ior equals the material's ior at the
+    sodium d-line and spreads (ior - 1) dispersion / 20 between the F and C lines (the
+    KHR_materials_dispersion definition, dispersion = 20 / Abbe number); the white balance makes a
+    uniform wavelength in [400, 700] nm average to white"""
+    for ior, disp in ((1.5, 1.0), (1.33, 3.0), (2.4, 0.5)):
+        assert abs(oracle.cauchy_ior(ior, disp, 587.6) - ior) < 1e-6
+        spread = oracle.cauchy_ior(ior, disp, 486.1) - oracle.cauchy_ior(ior, disp, 656.3)
+        assert abs(spread - (ior - 1) * disp / 20) < 1e-6 * max(1.0, spread)
+        # shorter wavelengths refract more
+        assert oracle.cauchy_ior(ior, disp, 420.0) > ior > oracle.cauchy_ior(ior, disp, 680.0)
+    lam = np.linspace(400.0, 700.0, 3001)
+    rgb = np.array([oracle.lambda_rgb(x) for x in lam])
+    assert np.all(rgb >= 0)
+    mean = np.trapezoid(rgb, lam, axis=0) / 300.0 * np.array([1.703734, 2.601105, 2.757475])
+    assert np.allclose(mean, 1.0, atol=2e-3), mean
+    # red at 650 nm, green at 540 nm, blue at 450 nm dominate
+    assert np.argmax(oracle.lambda_rgb(650.0)) == 0 and np.argmax(oracle.lambda_rgb(540.0)) == 1
+    assert np.argmax(oracle.lambda_rgb(450.0)) == 2

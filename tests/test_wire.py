@@ -57,7 +57,8 @@ def test_materials_from_wire():
     w["texture_type_flags"][3] = 0x1
     w["dispersion"][4] = 0.2
     m, dropped = materials_from_wire(w.tobytes())
-    assert dropped == 2
+    assert dropped == 1  # the texture flags; dispersion is read
+    assert np.array_equal(m["dispersion"], w["dispersion"])
     assert np.array_equal(m["base_color"], w["color"][:, :3])
     assert np.allclose(m["emission"], w["emission"][:, :3] * w["emission"][:, 3:4], rtol=1e-7, atol=0)
     for ours, theirs in (("metalness", "metalness"), ("roughness", "roughness"), ("transmission", "transmission"),

@@ -54,7 +54,7 @@ class vkg_material(C.Structure):
                 ("iridescence_ior", C.c_float), ("iridescence_thickness", C.c_float),
                 ("attenuation_color", C.c_float * 3), ("attenuation_distance", C.c_float),
                 ("scatter_color", C.c_float * 3), ("scatter_factor", C.c_float), ("phase_g", C.c_float),
-                ("null_surface", C.c_uint32), ("pad", C.c_float * 2)]
+                ("null_surface", C.c_uint32), ("dispersion", C.c_float), ("pad", C.c_float)]
 
 
 class vkg_camera(C.Structure):

@@ -12,7 +12,7 @@
 //     the primitive's material, 0 when it has none (the reference's default index);
 //   * the materials (gltf.cpp:316-560): base colour, metallic (default 1), roughness (default 1),
 //     emissive x KHR_materials_emissive_strength, doubleSided, KHR_materials_transmission,
-//     KHR_materials_ior, KHR_materials_clearcoat, KHR_materials_sheen, KHR_materials_iridescence (the
+//     KHR_materials_ior, KHR_materials_dispersion, KHR_materials_clearcoat, KHR_materials_sheen, KHR_materials_iridescence (the
 //     film thickness is the range's maximum, as the shader reads it), KHR_materials_diffuse_transmission,
 //     KHR_materials_volume (attenuation colour / distance) and KHR_materials_scatter /
 //     KHR_materials_volume_scatter (gltf.cpp:476-500, :634-657); a default material when the asset
@@ -555,6 +555,7 @@ struct loader
             if(const jv *e = ext->get("KHR_materials_transmission"))
                 r.transmission = clampf(e->num("transmissionFactor", 0.0), 0, 1);
             if(const jv *e = ext->get("KHR_materials_ior")) r.ior = (float)e->num("ior", 1.5);
+            if(const jv *e = ext->get("KHR_materials_dispersion")) r.dispersion = (float)e->num("dispersion", 0.0);
             if(const jv *e = ext->get("KHR_materials_clearcoat"))
             {
                 r.clearcoat = (float)std::max(0.0, e->num("clearcoatFactor", 0.0));

@@ -225,6 +225,8 @@ vkg_status check_material_values(vkg_ctx *ctx, const vkg_material *d_mats, uint3
         if(m.transmission > 0.f && !(m.ior > 0.f && std::isfinite(m.ior)))
             return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "%s: material %u: a transmissive material needs ior > 0",
                              fn, i);
+        if(!(m.dispersion >= 0.f) || !std::isfinite(m.dispersion))
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "%s: material %u: dispersion must be finite and >= 0", fn, i);
         if(!(m.clearcoat >= 0.f) || !(m.clearcoat_roughness >= 0.f) || !(m.sheen_roughness >= 0.f) ||
            !std::isfinite(m.clearcoat))
             return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
@@ -467,6 +469,7 @@ vkg_status vkg_scene_create(vkg_ctx *ctx, const vkg_scene_desc *d, vkg_scene **o
         vkg_scene_destroy(ctx, sc);
         return s;
     }
+    for(const vkg_material &m: sc->h_mats) sc->any_dispersion = sc->any_dispersion || material_dispersive(m);
     vkg_bvh_build_options opt{d->leaf_max};
     vkg_status s = vkg_bvh_build(ctx, sc->xyz, d->num_vertices, sc->idx, d->num_tris, &opt, &sc->bvh, stream);
     if(s != VKG_OK)
@@ -594,6 +597,7 @@ vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_de
                                                  &sc->h_media, &sc->h_mats);
        s != VKG_OK)
         return fail(s);
+    for(const vkg_material &m: sc->h_mats) sc->any_dispersion = sc->any_dispersion || material_dispersive(m);
     std::vector<mesh_ref> refs(d->num_meshes);
     uint64_t tris = 0;
     for(uint32_t m = 0; m < d->num_meshes && e == cudaSuccess; ++m)

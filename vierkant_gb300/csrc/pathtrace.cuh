@@ -15,6 +15,8 @@
 
 #include "internal.hpp"
 
+#include <cuda_fp16.h>
+
 namespace vkg
 {
 
@@ -149,6 +151,48 @@ __device__ __forceinline__ float3 env_sample(const env_view &e, float u0, float 
     texel = t;
     return d;
 }
+
+// ---- chromatic dispersion (utils/bsdf.slang:46-91) -------------------------------------------------
+__host__ __device__ inline bool material_dispersive(const vkg_material &m) { return m.dispersion > 0.f && m.transmission > 0.f; }
+
+// Cauchy n(lambda) = A + B / lambda^2 (lambda in nm): B from the KHR_materials_dispersion spread
+// n_F - n_C = (ior - 1) dispersion / 20 between the F (486.1 nm) and C (656.3 nm) lines, A so that
+// n(587.6 nm, the d-line) = ior
+__device__ __forceinline__ float cauchy_ior(float ior, float dispersion, float lambda)
+{
+    const float lambda_d = 587.6f;
+    const float half_spread = fmul(fmul(fsub(ior, 1.f), 0.025f), dispersion);
+    const float B = fmul(1046907.5f, half_spread); // 2 half_spread / (1/486.1^2 - 1/656.3^2)
+    const float A = fsub(ior, fdiv(B, fmul(lambda_d, lambda_d)));
+    return fadd(A, fdiv(B, fmul(lambda, lambda)));
+}
+
+// piecewise Gaussian of the CIE 1931 colour-matching fit (Wyman, Sloan & Shirley, JCGT 2013)
+__device__ __forceinline__ float gaussian_lobe(float x, float mu, float sigma1, float sigma2)
+{
+    const float t = fmul(fsub(x, mu), x < mu ? fdiv(1.f, sigma1) : fdiv(1.f, sigma2));
+    return expf(fmul(fmul(-0.5f, t), t));
+}
+
+// one wavelength (nm) -> linear Rec.709 RGB, negatives clamped (the fit's out-of-gamut colours)
+__device__ __forceinline__ float3 lambda_to_rgb(float lambda)
+{
+    const float x = fsub(fadd(fmul(1.056f, gaussian_lobe(lambda, 599.8f, 37.9f, 31.0f)),
+                              fmul(0.362f, gaussian_lobe(lambda, 442.0f, 16.0f, 26.7f))),
+                         fmul(0.065f, gaussian_lobe(lambda, 501.1f, 20.4f, 26.2f)));
+    const float y = fadd(fmul(0.821f, gaussian_lobe(lambda, 568.8f, 46.9f, 40.5f)),
+                         fmul(0.286f, gaussian_lobe(lambda, 530.9f, 16.3f, 31.1f)));
+    const float z = fadd(fmul(1.217f, gaussian_lobe(lambda, 437.0f, 11.8f, 36.0f)),
+                         fmul(0.681f, gaussian_lobe(lambda, 459.0f, 26.0f, 13.8f)));
+    // XYZ -> Rec.709 (row vector times the matrix, as the shader's mul(xyz, XYZ_TO_REC709))
+    const float r = fadd(fadd(fmul(x, 3.2404542f), fmul(y, -1.5371385f)), fmul(z, -0.4985314f));
+    const float g = fadd(fadd(fmul(x, -0.9692660f), fmul(y, 1.8760108f)), fmul(z, 0.0415560f));
+    const float b = fadd(fadd(fmul(x, 0.0556434f), fmul(y, -0.2040259f)), fmul(z, 1.0572252f));
+    return make_float3(fmaxf(r, 0.f), fmaxf(g, 0.f), fmaxf(b, 0.f));
+}
+
+// white balance of a uniform wavelength in [400, 700] nm (utils/bsdf.slang:79-80)
+constexpr float LAMBDA_RGB_NORM_R = 1.703734f, LAMBDA_RGB_NORM_G = 2.601105f, LAMBDA_RGB_NORM_B = 2.757475f;
 
 // ---- BSDF (bsdf_disney.slang) --------------------------------------------------------------------
 struct material_view
@@ -713,6 +757,9 @@ __device__ __forceinline__ float hit_eta(const vkg_material *mats, uint32_t id, 
     const float ior = mats[id].ior;
     return (back_face ? ior : 1.f / ior) + PT_EPS;
 }
+
+// the same for a surface whose ior is given (a dispersive surface's Cauchy ior)
+__device__ __forceinline__ float hit_eta_ior(float ior, bool back_face) { return (back_face ? ior : 1.f / ior) + PT_EPS; }
 
 // direct_lighting.slang:140-144
 __device__ __forceinline__ float power_heuristic(float pa, float pb)

@@ -46,6 +46,7 @@ struct vkg_scene
     uint32_t num_instances = 0;
     bool any_transmissive = false;  // a material with transmission > 0 or a null surface (light shadow rays pass)
     bool any_full = false;          // a material with a lobe beyond metal-roughness
+    bool any_dispersion = false;    // a transmissive material with dispersion > 0
     vkg::medium_rec *d_media = nullptr; // per-material medium records, when a material bounds a medium
     std::vector<vkg::medium_rec> h_media; // the same records for every material (host)
     std::vector<vkg_material> h_mats;     // host copy of the materials
@@ -99,6 +100,7 @@ struct pt_params
     const medium_rec *media;
     uint4 *mstack;
     uint32_t cam_medium; // medium table index of the camera's medium (0xFFFFFFFF: vacuum)
+    uint32_t dispersion; // a material disperses: every segment draws one more uniform (the wavelength)
     // the reference's random streams (VKG_RNG_REFERENCE, one sample per pixel and wave): the batch
     // seed, the full-resolution width and samples per batch, and per window pixel the chain state
     // between samples and the sub-pixel offset of the batch
@@ -110,7 +112,7 @@ struct pt_params
     uint32_t dbg_stride, dbg_segments;
 };
 
-constexpr uint32_t DBG_U_PER_SEGMENT = 15;
+constexpr uint32_t DBG_U_PER_SEGMENT = 16;
 
 // the shade kernel's two modes
 enum : int
@@ -456,19 +458,22 @@ __global__ void __launch_bounds__(PT_THREADS)
             // 4 more (channel, distance, phase direction) when it has media
             const uint32_t num_lights = FULL ? P.num_lights : 0u;
             const bool media = FULL && MEDIA && P.media;
-            float u[15];
-            const int nu = media ? 15 : (num_lights ? 11 : 8);
+            // one more (the wavelength) when a material disperses, after the others
+            float u[16];
+            const bool disp = FULL && P.dispersion;
+            const int nu = (media ? 15 : (num_lights ? 11 : 8)) + (disp ? 1 : 0);
             if(P.ref_rng)
             {
                 // the reference's per-segment stream: chain = xxhash32(chain, i) (raypipeline.slang:150),
                 // the hit shader's rnd() LCG started at it (random.slang:27-36)
                 const uint32_t chain = xxhash32((uint32_t)g.state, depth);
                 uint32_t l = chain;
-                for(int k = 0; k < 15; ++k) u[k] = k < nu ? rnd(l) : 0.f;
+                for(int k = 0; k < 16; ++k) u[k] = k < nu ? rnd(l) : 0.f;
                 g.state = chain;
             }
             else
-                for(int k = 0; k < 15; ++k) u[k] = k < nu ? u01(pcg32_next(g)) : 0.f;
+                for(int k = 0; k < 16; ++k) u[k] = k < nu ? u01(pcg32_next(g)) : 0.f;
+            const float u_lambda = media ? u[15] : (num_lights ? u[11] : u[8]);
             if(P.dbg_u && depth < P.dbg_segments)
             {
                 float *d = P.dbg_u + ((size_t)P.s0 * P.npix + pid) * P.dbg_stride + 2 + DBG_U_PER_SEGMENT * depth;
@@ -681,12 +686,24 @@ __global__ void __launch_bounds__(PT_THREADS)
                 // path regularisation (raypipeline.slang:611): after a non-peaked bounce, later vertices
                 // shade (sample and NEE) with roughness >= 0.25
                 if(flags & PATH_REGULARIZE) m.roughness = fmaxf(m.roughness, PT_REGULARIZE_MIN_ROUGHNESS);
-                float eta = FULL ? hit_eta(P.mats, mat, back_face) : 1.f;
+                // chromatic dispersion (raypipeline.slang:485-488): a wavelength, locked by the path's
+                // first transmission through a dispersive surface (bits 16..31 of the path flags, FP16
+                // as the reference's payload keeps it) or drawn here, and the surface's Cauchy ior
+                const bool dispersive = disp && material_dispersive(P.mats[mat]);
+                const bool lambda_locked = (flags >> 16) != 0u;
+                float lambda = 0.f, surf_ior = FULL ? P.mats[mat].ior : 1.f;
+                if(dispersive)
+                {
+                    lambda = lambda_locked ? __half2float(__ushort_as_half((unsigned short)(flags >> 16)))
+                                           : fadd(400.0f, fmul(u_lambda, 300.0f));
+                    surf_ior = cauchy_ior(P.mats[mat].ior, P.mats[mat].dispersion, lambda);
+                }
+                float eta = FULL ? (dispersive ? hit_eta_ior(surf_ior, back_face) : hit_eta(P.mats, mat, back_face)) : 1.f;
                 if(media && P.mats[mat].transmission > 0.f)
                 {
                     // eta from the media stack: the current medium's ior over the surface's entering,
                     // the surface's over the enclosing medium's leaving (raypipeline.slang:489-491)
-                    const float ior = P.mats[mat].ior;
+                    const float ior = surf_ior;
                     eta = (back_face ? ior / stack_ior(P.media, mst, mst.x ? mst.x - 1 : 0)
                                      : stack_ior(P.media, mst, mst.x) / ior) + PT_EPS;
                 }
@@ -796,6 +813,15 @@ __global__ void __launch_bounds__(PT_THREADS)
                     if(depth >= 1 && P.max_path_beta > 0.f)
                         tp = f3(fminf(tp.x, P.max_path_beta), fminf(tp.y, P.max_path_beta), fminf(tp.z, P.max_path_beta));
                     beta = beta * tp;
+                    // the first transmission through a dispersive surface locks the wavelength and tints
+                    // the throughput by its white-balanced colour (raypipeline.slang:651-659)
+                    if(dispersive && bs.transmission && !lambda_locked)
+                    {
+                        flags |= (uint32_t)__half_as_ushort(__float2half_rn(lambda)) << 16;
+                        const float3 c = lambda_to_rgb(lambda);
+                        beta = beta * f3(fmul(LAMBDA_RGB_NORM_R, c.x), fmul(LAMBDA_RGB_NORM_G, c.y),
+                                         fmul(LAMBDA_RGB_NORM_B, c.z));
+                    }
                     // MIS pdf of the bounce for an environment hit: the mixture pdf where the
                     // environment sampler competes (directions above the surface), 0 below it
                     float pdf_mix = 0.f;
@@ -1395,6 +1421,7 @@ inline pt_params make_params(const vkg_scene *sc, const vkg_camera &cam, const v
     P.max_path_beta = S.max_path_beta;
     P.seed = seed;
     P.batch = batch;
+    P.dispersion = sc->any_dispersion ? 1u : 0u;
     P.term_depth = 0xFFFFFFFFu;
     P.rec_depth = 0;
     P.train_base = 0xFFFFFFFFu;

@@ -81,8 +81,8 @@ vkg_status vkg_materials_from_wire(const void *records, uint32_t n, vkg_material
         rd3(r, mat_off::scatter_color, m.scatter_color);
         m.diffuse_transmission = rd<float>(r, mat_off::diffuse_transmission);
         rd3(r, mat_off::diffuse_transmission_color, m.diffuse_transmission_color);
-        bool unused = rd<uint32_t>(r, mat_off::texture_type_flags) != 0 || rd<uint32_t>(r, mat_off::blend_mode) != 0 ||
-                      rd<float>(r, mat_off::dispersion) != 0.f;
+        m.dispersion = rd<float>(r, mat_off::dispersion);
+        bool unused = rd<uint32_t>(r, mat_off::texture_type_flags) != 0 || rd<uint32_t>(r, mat_off::blend_mode) != 0;
         nd += unused ? 1u : 0u;
         out[i] = m;
     }

@@ -20,7 +20,8 @@ MATERIAL_DTYPE = np.dtype([("base_color", "<f4", 3), ("roughness", "<f4"), ("met
                            ("diffuse_transmission_color", "<f4", 3), ("iridescence", "<f4"),
                            ("iridescence_ior", "<f4"), ("iridescence_thickness", "<f4"), ("attenuation_color", "<f4", 3),
                            ("attenuation_distance", "<f4"), ("scatter_color", "<f4", 3), ("scatter_factor", "<f4"),
-                           ("phase_g", "<f4"), ("null_surface", "<u4"), ("pad", "<f4", 2)])
+                           ("phase_g", "<f4"), ("null_surface", "<u4"), ("dispersion", "<f4"),
+                           ("pad", "<f4")])
 assert MATERIAL_DTYPE.itemsize == C.sizeof(vkg_material)
 
 
@@ -102,6 +103,14 @@ def showcase_materials(materials: np.ndarray) -> np.ndarray:
 
 
 MEDIA_KINDS = ("metal-rough", "fog", "absorbing glass", "emissive gas", "scattering glass")
+
+
+def dispersive_materials(materials: np.ndarray, dispersion: float = 3.0) -> np.ndarray:
+    """a copy of `materials` whose transmissive materials disperse (KHR_materials_dispersion value;
+    3.0 is an Abbe number of about 6.7, strongly coloured)"""
+    m = materials.copy()
+    m["dispersion"][m["transmission"] > 0] = np.float32(dispersion)
+    return m
 
 
 def media_materials(materials: np.ndarray) -> np.ndarray:

@@ -28,7 +28,7 @@ def _bytes(records, size):
 
 def materials_from_wire(records) -> tuple[np.ndarray, int]:
     """material_struct_t records (bytes or any array of them) -> (MATERIAL_DTYPE array, number of
-    records that use textures, a blend mode or dispersion, which are dropped)"""
+    records that use textures or a blend mode, which are dropped)"""
     b, n = _bytes(records, WIRE_MATERIAL_BYTES)
     out = np.zeros(n, MATERIAL_DTYPE)
     dropped = C.c_uint32()
