@@ -121,10 +121,13 @@ __device__ __forceinline__ void ray_init(ray_state_t<STACK> &s, float ox, float 
 // interval [tmin, tmax]): key = ordered entry distance with its low 3 bits replaced by the slot,
 // 0xFFFFFFFF for a child the ray misses. Truncation only lowers the stored distance, so pruning with
 // it stays conservative. w4 / w5 receive the node's child words.
+// COUNT: also count the internal (non-leaf) children the ray hits into *n_int
+template<bool COUNT = false>
 __device__ __forceinline__ void node_keys(const node8 *__restrict__ nodes, uint32_t ni, float ox, float oy, float oz,
                                           float ix, float iy, float iz, float tmin, float tmax, uint32_t (&key)[8],
-                                          uint4 &w4, uint4 &w5)
+                                          uint4 &w4, uint4 &w5, uint32_t *n_int = nullptr)
 {
+    uint32_t nint = 0;
     const uint4 *np = reinterpret_cast<const uint4 *>(nodes + ni);
     const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2);
     const uint4 w3 = __ldg(np + 3);
@@ -159,9 +162,19 @@ __device__ __forceinline__ void node_keys(const node8 *__restrict__ nodes, uint3
             const float tnz = fmaf(qbyte(wnz, k), sz, toz), tfz = fmaf(qbyte(wfz, k), sz, toz);
             const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
             const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
-            if(tn <= tf) key[k] = (tenc(tn) & ~7u) | (uint32_t)k;
+            if(tn <= tf)
+            {
+                key[k] = (tenc(tn) & ~7u) | (uint32_t)k;
+                if(COUNT)
+                {
+                    const uint32_t c = k < 4 ? (k == 0 ? w4.x : k == 1 ? w4.y : k == 2 ? w4.z : w4.w)
+                                             : (k == 4 ? w5.x : k == 5 ? w5.y : k == 6 ? w5.z : w5.w);
+                    nint += (c & LEAF_BIT) ? 0u : 1u;
+                }
+            }
         }
     }
+    if(COUNT) *n_int = nint;
 }
 
 // one node of the traversal; returns false once the ray is finished
@@ -179,16 +192,30 @@ __device__ __forceinline__ bool ray_step(ray_state_t<STACK> &s, const node8 *__r
         if(STATS) ++visits;
         uint32_t key[8];
         uint4 w4, w5;
-        node_keys(nodes, ni, s.ox, s.oy, s.oz, s.ix, s.iy, s.iz, s.tmin, s.best_t, key, w4, w5);
+        uint32_t n_int;
+        node_keys<true>(nodes, ni, s.ox, s.oy, s.oz, s.ix, s.iy, s.iz, s.tmin, s.best_t, key, w4, w5, &n_int);
         sort8(key);
+        // one pass over the hit children, near to far: leaves are intersected as they come, internal
+        // children are written to the stack far-to-near (the r-th nearest at base + n_int - 1 - r) so
+        // that the nearest is popped first -- the order two separate passes would give
+        const int base = s.sp;
+        int r = 0;
 #pragma unroll
         for(int h = 0; h < 8; ++h)
         {
             if(key[h] == 0xFFFFFFFFu || s.done) break;
             const uint32_t k = key[h] & 7u;
             const uint32_t c = (k & 4u) ? sel4(w5, k & 3u) : sel4(w4, k & 3u);
-            if(!(c & LEAF_BIT)) continue;
-            if(tdec(key[h] & ~7u) > s.best_t) continue;
+            const float tentry = tdec(key[h] & ~7u);
+            if(!(c & LEAF_BIT))
+            {
+                const int pos = base + (int)n_int - 1 - r;
+                ++r;
+                if(pos < STACK) s.st[pos] = make_uint2(c, __float_as_uint(tentry));
+                else if(counters) { atomicOr(&counters[2], 1ull); }
+                continue;
+            }
+            if(tentry > s.best_t) continue;
             const uint32_t start = c & 0x07FFFFFFu, cnt = ((c >> 27) & 0xFu) + 1u;
             for(uint32_t ti = start; ti < start + cnt; ++ti)
             {
@@ -218,20 +245,7 @@ __device__ __forceinline__ bool ray_step(ray_state_t<STACK> &s, const node8 *__r
             }
         }
         if(s.done) break;
-#pragma unroll
-        for(int h = 7; h >= 0; --h)
-        {
-            if(key[h] == 0xFFFFFFFFu) continue;
-            const uint32_t k = key[h] & 7u;
-            const uint32_t c = (k & 4u) ? sel4(w5, k & 3u) : sel4(w4, k & 3u);
-            if(c & LEAF_BIT) continue;
-            if(s.sp < STACK)
-            {
-                s.st[s.sp] = make_uint2(c, __float_as_uint(tdec(key[h] & ~7u)));
-                ++s.sp;
-            }
-            else if(counters) { atomicOr(&counters[2], 1ull); }
-        }
+        s.sp = min(base + (int)n_int, STACK);
         return true; // one node processed
     }
     return false;
