@@ -302,8 +302,17 @@ vkg_status vkg_bvh_destroy(vkg_ctx *ctx, vkg_bvh *bvh);
 enum
 {
     VKG_RAY_CULL_BACK_FACES = 1u, /* RAY_FLAG_CULL_BACK_FACING_TRIANGLES: reject det < 0 (clockwise seen from origin) */
-    VKG_RAY_COUNT_STATS = 2u      /* also count node visits / triangle tests (slower; see vkg_ray_stats_get) */
+    VKG_RAY_COUNT_STATS = 2u,     /* also count node visits / triangle tests (slower; see vkg_ray_stats_get) */
+    VKG_RAY_KEEP_ORDER = 4u       /* trace in the given order: no binning of large batches (below) */
 };
+/* Batches of 2^19 rays or more are traced in bins: rays are grouped by the cell of the scene box
+ * (8 x 8 x 8) that holds their origin and by their direction (64 octahedral bins), and each group is
+ * traced together. Results, counters and error flags are those of tracing in the given order; only
+ * the speed differs. The context keeps the bins' scratch (12 B per ray plus 128 KB, grown on demand,
+ * one set for the caller's streams -- calls on different streams are ordered by an event -- and one
+ * per stream of the host variant's pipeline). Calls made while the stream is being captured into a
+ * CUDA graph, calls with VKG_RAY_KEEP_ORDER, and calls whose scratch cannot be allocated trace in the
+ * given order. */
 vkg_status vkg_closest_hit(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t num_rays,
                            vkg_hit *d_hits, uint32_t flags, void *stream);
 vkg_status vkg_any_hit(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t num_rays,

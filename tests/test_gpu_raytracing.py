@@ -11,7 +11,7 @@ import torch
 
 import oracle
 from vierkant_gb300 import geometry
-from vierkant_gb300._lib import RAY_COUNT_STATS, RAY_CULL_BACK_FACES, VkgError
+from vierkant_gb300._lib import RAY_COUNT_STATS, RAY_CULL_BACK_FACES, RAY_KEEP_ORDER, VkgError
 from vierkant_gb300.raytracing import BVH
 
 pytestmark = pytest.mark.gpu
@@ -176,6 +176,55 @@ def test_cornell_primary_and_secondary_bit_exact(ctx):
         assert hc.tobytes() == cb.closest_hit(sec, cull=bool(cull)).tobytes()
         occ = b.any_hit(rays_dev(sec), flags=cull).cpu().numpy().view(np.uint32)
         assert np.array_equal(occ, cb.any_hit(sec, cull=bool(cull)))
+    b.close()
+
+
+def test_binned_batches_equal_given_order(ctx):
+    """Batches of 2^19 rays or more are traced in bins (origin cell x direction). On a ragged mixed
+    batch (921,600 camera rays + 500,000 incoherent bounce rays): hits, any-hit flags and the work
+    counters equal tracing in the given order (VKG_RAY_KEEP_ORDER), with and without culling, the
+    bounce rays equal the CPU traversal bit for bit, and a call captured into a CUDA graph (traced
+    in the given order) replays to the same hits."""
+    sc, b = cornell(ctx)
+    cb = oracle.CpuBVH(sc["xyz"], sc["indices"], DEFAULT_LEAF)
+    th = float(np.float32(math.tan(math.radians(45.0) / 2.0)))
+    cam_o = oracle.camera((0, 0, 3.4), (0, 0, 0), (0, 1, 0), th, 1280, 720)
+    ref_rays = oracle.camera_rays(cam_o, 0x5EED, 2, 1)
+    h0 = np.ascontiguousarray(cb.closest_hit(ref_rays)).view(np.uint32).reshape(-1, 4)
+    sec = secondary_rays(np.random.default_rng(21), h0, ref_rays, 500000)
+    assert sec.shape[0] == 500000
+    batch = np.concatenate([ref_rays, sec])
+    assert batch.shape[0] % 256 != 0
+    d = rays_dev(batch)
+    for cull in (0, RAY_CULL_BACK_FACES):
+        ctx.stats(reset=True)
+        hb = hits_np(b.closest_hit(d, flags=cull | RAY_COUNT_STATS))
+        sb = ctx.stats(reset=True)
+        hk = hits_np(b.closest_hit(d, flags=cull | RAY_COUNT_STATS | RAY_KEEP_ORDER))
+        sk = ctx.stats(reset=True)
+        assert hb.tobytes() == hk.tobytes()
+        assert sb == sk
+        assert hits_np(b.closest_hit(d, flags=cull)).tobytes() == hb.tobytes()
+        if cull == 0:
+            h_plain = hb
+        assert hb[ref_rays.shape[0]:].tobytes() == cb.closest_hit(sec, cull=bool(cull)).tobytes()
+        ob = b.any_hit(d, flags=cull).cpu().numpy()
+        ok = b.any_hit(d, flags=cull | RAY_KEEP_ORDER).cpu().numpy()
+        assert np.array_equal(ob, ok)
+    # inside a stream capture the call traces in the given order
+    out = torch.empty((batch.shape[0], 4), dtype=torch.int32, device="cuda")
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        b.closest_hit(d, out)
+    torch.cuda.current_stream().wait_stream(side)
+    out.zero_()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        b.closest_hit(d, out)
+    g.replay()
+    torch.cuda.synchronize()
+    assert hits_np(out).tobytes() == h_plain.tobytes()
     b.close()
 
 

@@ -18,6 +18,7 @@ VKG_MISS = 0xFFFFFFFF
 REJECT, INTERSECT, INSIDE = 0, 1, 2
 RAY_CULL_BACK_FACES = 1
 RAY_COUNT_STATS = 2
+RAY_KEEP_ORDER = 4
 
 
 RNG_PCG32, RNG_REFERENCE = 0, 1

@@ -85,6 +85,14 @@ vkg_status vkg_ctx_destroy(vkg_ctx *ctx)
         if(s) cudaStreamDestroy(s);
     for(cudaEvent_t e: ctx->pipe_ev)
         if(e) cudaEventDestroy(e);
+    for(auto &b: ctx->bins)
+    {
+        cudaFree(b.keys);
+        cudaFree(b.perm);
+        cudaFree(b.tile_counts);
+        cudaFree(b.bin_totals);
+        if(b.done) cudaEventDestroy(b.done);
+    }
     delete ctx;
     return VKG_OK;
 }

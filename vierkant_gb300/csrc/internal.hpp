@@ -27,6 +27,21 @@ struct vkg_ctx
     // the host variant's copy / trace pipeline: two streams and a fork + two join events (first use)
     cudaStream_t pipe[2] = {nullptr, nullptr};
     cudaEvent_t pipe_ev[3] = {nullptr, nullptr, nullptr};
+    // ray-binning scratch of the bulk queries: [0] the caller's streams, [1], [2] the host variant's
+    // pipeline streams. keys: bin | rank in its tile << 16 per ray; perm: traced position -> ray
+    // index (its first half holds the 16-bit bins before that); tile_counts: rays per (tile, bin);
+    // bin_totals: rays per bin and the bins' first positions; done: recorded after the last use,
+    // waited for by the next
+    struct ray_bins
+    {
+        uint32_t *keys = nullptr;
+        uint32_t *perm = nullptr;
+        uint32_t *tile_counts = nullptr;
+        uint32_t *bin_totals = nullptr;
+        size_t cap = 0;
+        uint32_t tiles_cap = 0;
+        cudaEvent_t done = nullptr;
+    } bins[3];
 };
 
 struct vkg_bvh

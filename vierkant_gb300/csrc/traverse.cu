@@ -2,7 +2,9 @@
 // RT cores). Replaces the RT-core TraceRay of shaders/slang/raypipeline.slang:182 and the
 // RayQuery visibility test of shaders/slang/ray/visibility_test.slang:45-87.
 //
-// One thread per ray; the traversal itself is trace_ray() in traverse.cuh.
+// One thread per ray; the traversal itself is trace_ray() in traverse.cuh. Large batches are traced
+// in bins (origin cell x direction): neighbouring threads then follow similar paths through the tree,
+// so a warp's lanes stay busy together and share node loads in L1.
 //
 // Work per ray (the roofline's algorithmic unit): 32 B ray in + 16 B hit out from HBM, plus
 // 96 B per node visit and 48 B per triangle test from L2/L1.
@@ -24,12 +26,14 @@ template<bool ANY, bool STATS, int STACK>
 __global__ void __launch_bounds__(TRACE_THREADS)
         k_trace(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris, const vkg_ray *__restrict__ rays,
                 uint32_t n, vkg_hit *__restrict__ hits, uint32_t *__restrict__ occluded, int cull,
-                unsigned long long *__restrict__ counters)
+                unsigned long long *__restrict__ counters, const uint32_t *__restrict__ perm)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long visits = 0, tests = 0;
-    if(i < n)
+    if(j < n)
     {
+        // thread j traces ray perm[j] when the batch was binned
+        const uint32_t i = perm ? __ldg(perm + j) : j;
         const float4 *rp = reinterpret_cast<const float4 *>(rays + i);
         const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
         trace_result r = trace_ray<ANY, STATS, STACK>(nodes, tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w,
@@ -158,14 +162,332 @@ bool use_persistent()
 
 template<bool ANY, bool STATS>
 void launch_simple(bool small_stack, uint32_t grid, cudaStream_t st, const vkg_bvh *bvh, const vkg_ray *rays,
-                   uint32_t n, vkg_hit *hits, uint32_t *occ, int cull, unsigned long long *counters)
+                   uint32_t n, vkg_hit *hits, uint32_t *occ, int cull, unsigned long long *counters,
+                   const uint32_t *perm)
 {
     if(small_stack)
         k_trace<ANY, STATS, 64><<<grid, TRACE_THREADS, 0, st>>>(bvh->d_nodes, bvh->d_tris, rays, n, hits, occ, cull,
-                                                                counters);
+                                                                counters, perm);
     else
         k_trace<ANY, STATS, (int)TRAVERSAL_STACK><<<grid, TRACE_THREADS, 0, st>>>(bvh->d_nodes, bvh->d_tris, rays, n,
-                                                                                   hits, occ, cull, counters);
+                                                                                   hits, occ, cull, counters, perm);
+}
+
+// ---- ray binning -------------------------------------------------------------------------------
+// bin = (Morton index of the origin's cell in an 8 x 8 x 8 grid over the scene box) * 64 + direction
+// bin (8 x 8 cells of the octahedral map of the direction). Cell-major order keeps the rays of one
+// region of the scene together; within a cell, rays of similar direction. Within a bin the rays
+// keep roughly the order they came in (for a camera or bounce batch: pixel order, itself spatially
+// coherent): tiles keep their order, and within a tile the ranks follow the order in which its warps
+// reach the bin's counter, each warp walking a contiguous part of the tile. An order shuffled within
+// the bins traces slower than the given order.
+// Counting sort over T tiles of consecutive rays:
+//   k_bin_keys     every ray's bin (16 bits)
+//   k_bin_tiles    one CTA per tile: each ray's rank among the tile's rays of its bin (shared-memory
+//                  counters) and the tile's bin histogram -> M[t][bin]
+//   k_bin_columns  per bin, M[.][bin] scanned over the tiles in place (exclusive); S[bin] = total
+//   k_bin_offsets  F = exclusive scan of S: the bins' first positions
+//   k_bin_place    perm[F[bin] + M[t][bin] + rank] = ray
+constexpr int BIN_CELL_BITS = 3;                                            // per axis
+constexpr int BIN_DIR_BITS = 3;                                             // per octahedral axis
+constexpr uint32_t NUM_BINS = 1u << (3 * BIN_CELL_BITS + 2 * BIN_DIR_BITS); // 32,768
+constexpr uint32_t BIN_MIN_RAYS = 1u << 19;
+constexpr int BIN_THREADS = 1024;                                           // per tile CTA
+constexpr uint32_t BIN_MAX_TILE = 40u * BIN_THREADS;                        // ranks fit 16 bits
+constexpr size_t BIN_SMEM = sizeof(uint32_t) * NUM_BINS;                    // 128 KB
+static_assert(NUM_BINS == BIN_THREADS * 32, "32 bins per thread");
+static_assert(NUM_BINS <= 65536 && BIN_MAX_TILE <= 65536, "bin and rank are packed in 16 bits each");
+
+__device__ __forceinline__ uint32_t spread3(uint32_t v) { return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4); }
+
+__device__ __forceinline__ uint32_t cell_coord(float p, float lo, float scale)
+{
+    // NaN converts to 0; out-of-box origins clamp to the border cells
+    const int c = __float2int_rz((p - lo) * scale);
+    return (uint32_t)min(max(c, 0), (1 << BIN_CELL_BITS) - 1);
+}
+
+__device__ __forceinline__ uint32_t dir_bin(float dx, float dy, float dz)
+{
+    constexpr float R = (float)(1 << BIN_DIR_BITS);
+    const float a = fabsf(dx) + fabsf(dy) + fabsf(dz);
+    float u = 0.f, v = 0.f;
+    if(a > 0.f)
+    {
+        const float ia = 1.f / a;
+        u = dx * ia;
+        v = dy * ia;
+        if(dz < 0.f)
+        {
+            const float fu = (1.f - fabsf(v)) * copysignf(1.f, u), fv = (1.f - fabsf(u)) * copysignf(1.f, v);
+            u = fu;
+            v = fv;
+        }
+    }
+    const int qu = min(max(__float2int_rz((u + 1.f) * (0.5f * R)), 0), (1 << BIN_DIR_BITS) - 1);
+    const int qv = min(max(__float2int_rz((v + 1.f) * (0.5f * R)), 0), (1 << BIN_DIR_BITS) - 1);
+    return (uint32_t)qu | ((uint32_t)qv << BIN_DIR_BITS);
+}
+
+__device__ __forceinline__ uint32_t ray_bin(float4 r0, float4 r1, float3 lo, float3 scale)
+{
+    const uint32_t cell = spread3(cell_coord(r0.x, lo.x, scale.x)) | (spread3(cell_coord(r0.y, lo.y, scale.y)) << 1) |
+                          (spread3(cell_coord(r0.z, lo.z, scale.z)) << 2);
+    return (cell << (2 * BIN_DIR_BITS)) | dir_bin(r1.x, r1.y, r1.z);
+}
+
+__global__ void __launch_bounds__(256)
+        k_bin_keys(const vkg_ray *__restrict__ rays, uint32_t n, float3 lo, float3 scale, uint16_t *__restrict__ bins)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n) return;
+    const float4 *rp = reinterpret_cast<const float4 *>(rays + i);
+    bins[i] = (uint16_t)ray_bin(__ldg(rp), __ldg(rp + 1), lo, scale);
+}
+
+// Each warp walks its own contiguous 1/32 of the tile, 32 rays a step. Steps whose rays all share
+// one bin extend a run of that bin; a run takes its ranks with one atomic when it ends (its keys are
+// written then), so a stretch of coherent rays costs one atomic instead of one per step and warp
+// (all warps of a camera tile would otherwise queue on the same few counters). In other steps each
+// ray takes its rank with its own atomic.
+__global__ void __launch_bounds__(BIN_THREADS)
+        k_bin_tiles(const uint16_t *__restrict__ bins, uint32_t n, uint32_t tile, uint32_t *__restrict__ keys,
+                    uint32_t *__restrict__ M)
+{
+    extern __shared__ uint32_t h[];
+    for(uint32_t b = threadIdx.x; b < NUM_BINS; b += BIN_THREADS) h[b] = 0u;
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t start = blockIdx.x * tile, end = min(start + tile, n);
+    const uint32_t per_warp = tile / 32u; // a multiple of 32
+    const uint32_t w0 = start + warp * per_warp, w1 = min(w0 + per_warp, end);
+    uint32_t run_bin = 0xFFFFFFFFu, run_start = 0, run_len = 0;
+    // a run's ranks: one atomic, then its keys
+    auto flush = [&]() {
+        if(run_len == 0) return;
+        uint32_t base = 0;
+        if(lane == 0) base = atomicAdd(&h[run_bin], run_len);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        for(uint32_t j = lane; j < run_len; j += 32u) keys[run_start + j] = run_bin | ((base + j) << 16);
+        run_len = 0;
+        run_bin = 0xFFFFFFFFu;
+    };
+    constexpr int U = 8; // steps whose bins are loaded together
+    for(uint32_t r0 = w0; r0 < w1; r0 += 32u * U)
+    {
+        uint32_t bu[U];
+#pragma unroll
+        for(int u = 0; u < U; ++u)
+        {
+            const uint32_t i = r0 + 32u * u + lane;
+            bu[u] = i < w1 ? (uint32_t)__ldg(bins + i) : 0xFFFFFFFFu;
+        }
+#pragma unroll
+        for(int u = 0; u < U; ++u)
+        {
+            const uint32_t r = r0 + 32u * u;
+            if(r >= w1) break; // warp-uniform
+            const uint32_t i = r + lane;
+            const bool valid = i < w1;
+            const uint32_t bin = bu[u];
+            const uint32_t b0 = __shfl_sync(0xffffffffu, bin, 0); // lane 0 is always valid
+            if(__all_sync(0xffffffffu, !valid || bin == b0))
+            {
+                const uint32_t cnt = min(32u, w1 - r);
+                if(b0 != run_bin)
+                {
+                    flush();
+                    run_bin = b0;
+                    run_start = r;
+                }
+                run_len += cnt;
+                continue;
+            }
+            flush();
+            if(valid) keys[i] = bin | (atomicAdd(&h[bin], 1u) << 16);
+        }
+    }
+    flush();
+    __syncthreads();
+    uint32_t *row = M + (size_t)blockIdx.x * NUM_BINS;
+    for(uint32_t b = threadIdx.x; b < NUM_BINS; b += BIN_THREADS) row[b] = h[b];
+}
+
+// CTA = 32 bins (lanes) x 32 chunks of consecutive tiles (warps): chunk sums, their scan per bin in
+// shared memory, then the chunk's entries rewritten as the bin's running count before the tile
+__global__ void __launch_bounds__(1024) k_bin_columns(uint32_t *__restrict__ M, uint32_t tiles, uint32_t *__restrict__ S)
+{
+    __shared__ uint32_t part[32][33];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t b = blockIdx.x * 32u + lane;
+    const uint32_t per = (tiles + 31u) / 32u;
+    const uint32_t t0 = min(warp * per, tiles), t1 = min(t0 + per, tiles);
+    uint32_t sum = 0;
+    for(uint32_t t = t0; t < t1; ++t) sum += M[(size_t)t * NUM_BINS + b];
+    part[warp][lane] = sum;
+    __syncthreads();
+    if(warp == 0)
+    {
+        uint32_t run = 0;
+        for(int w = 0; w < 32; ++w)
+        {
+            const uint32_t c = part[w][lane];
+            part[w][lane] = run;
+            run += c;
+        }
+        S[b] = run;
+    }
+    __syncthreads();
+    uint32_t run = part[warp][lane];
+    for(uint32_t t = t0; t < t1; ++t)
+    {
+        uint32_t *p = M + (size_t)t * NUM_BINS + b;
+        const uint32_t c = *p;
+        *p = run;
+        run += c;
+    }
+}
+
+// F = exclusive scan of S, one CTA: S staged in shared memory (a pad word after every 32 keeps the
+// per-thread runs of 32 consecutive bins free of bank conflicts), 32 bins per thread
+constexpr size_t BIN_SCAN_SMEM = sizeof(uint32_t) * (NUM_BINS + NUM_BINS / 32);
+__global__ void __launch_bounds__(BIN_THREADS) k_bin_offsets(const uint32_t *__restrict__ S, uint32_t *__restrict__ F)
+{
+    extern __shared__ uint32_t sm[];
+    __shared__ uint32_t warp_sum[32];
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    for(uint32_t b = t; b < NUM_BINS; b += BIN_THREADS) sm[b + (b >> 5)] = __ldg(S + b);
+    __syncthreads();
+    uint32_t *mine = sm + t * 33u; // bins t*32 .. t*32+31
+    uint32_t total = 0;
+    for(int k = 0; k < 32; ++k) total += mine[k];
+    uint32_t x = total;
+    for(int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if(lane >= (uint32_t)o) x += y;
+    }
+    if(lane == 31) warp_sum[warp] = x;
+    __syncthreads();
+    if(warp == 0)
+    {
+        uint32_t w = warp_sum[lane];
+        for(int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if(lane >= (uint32_t)o) w += y;
+        }
+        warp_sum[lane] = w;
+    }
+    __syncthreads();
+    uint32_t acc = (warp ? warp_sum[warp - 1] : 0u) + x - total;
+    for(int k = 0; k < 32; ++k)
+    {
+        const uint32_t c = mine[k];
+        mine[k] = acc;
+        acc += c;
+    }
+    __syncthreads();
+    for(uint32_t b = t; b < NUM_BINS; b += BIN_THREADS) F[b] = sm[b + (b >> 5)];
+}
+
+__global__ void __launch_bounds__(256)
+        k_bin_place(const uint32_t *__restrict__ keys, uint32_t n, uint32_t tile, const uint32_t *__restrict__ M,
+                    const uint32_t *__restrict__ F, uint32_t *__restrict__ perm)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n) return;
+    const uint32_t k = keys[i], bin = k & 0xFFFFu, t = i / tile;
+    perm[__ldg(F + bin) + M[(size_t)t * NUM_BINS + bin] + (k >> 16)] = i;
+}
+
+// the traced order of a large batch (device pointer into the context's scratch), or nullptr to trace
+// in the given order
+const uint32_t *bin_rays(vkg_ctx *ctx, int slot, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t n,
+                         uint32_t flags, cudaStream_t st)
+{
+    if((flags & VKG_RAY_KEEP_ORDER) || n < BIN_MIN_RAYS) return nullptr;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if(cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+    {
+        cudaGetLastError();
+        return nullptr;
+    }
+    // the shared-memory opt-in is a per-device attribute
+    static uint64_t smem_set = 0;
+    const uint64_t dev_bit = 1ull << (ctx->device & 63);
+    if(!(smem_set & dev_bit))
+    {
+        if(cudaFuncSetAttribute(k_bin_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BIN_SMEM) != cudaSuccess ||
+           cudaFuncSetAttribute(k_bin_offsets, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BIN_SCAN_SMEM) !=
+                   cudaSuccess)
+        {
+            cudaGetLastError();
+            return nullptr;
+        }
+        smem_set |= dev_bit;
+    }
+    // tiles of whole 1024-ray rounds: one per SM, or more of BIN_MAX_TILE rays each for larger batches
+    const size_t per_sm = ((size_t)n + (size_t)ctx->num_sms - 1) / (size_t)ctx->num_sms;
+    const uint32_t tile =
+            (uint32_t)std::min<size_t>(BIN_MAX_TILE, (per_sm + BIN_THREADS - 1) / BIN_THREADS * BIN_THREADS);
+    const uint32_t tiles = (uint32_t)(((size_t)n + tile - 1) / tile);
+    auto &b = ctx->bins[slot];
+    if(!b.done && cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming) != cudaSuccess)
+    {
+        b.done = nullptr;
+        cudaGetLastError();
+        return nullptr;
+    }
+    // the previous call's kernels may still use the scratch (another stream)
+    if(cudaStreamWaitEvent(st, b.done, 0) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if(b.cap < n || b.tiles_cap < tiles)
+    {
+        // cudaFree waits for the device, so nothing in flight still uses the old buffers
+        cudaFree(b.keys);
+        cudaFree(b.perm);
+        cudaFree(b.tile_counts);
+        cudaFree(b.bin_totals);
+        b = vkg_ctx::ray_bins{nullptr, nullptr, nullptr, nullptr, 0, 0, b.done};
+        // bin_totals: S, F
+        if(cudaMalloc(&b.keys, sizeof(uint32_t) * (size_t)n) != cudaSuccess ||
+           cudaMalloc(&b.perm, sizeof(uint32_t) * (size_t)n) != cudaSuccess ||
+           cudaMalloc(&b.tile_counts, sizeof(uint32_t) * (size_t)NUM_BINS * tiles) != cudaSuccess ||
+           cudaMalloc(&b.bin_totals, sizeof(uint32_t) * 2 * (size_t)NUM_BINS) != cudaSuccess)
+        {
+            cudaFree(b.keys);
+            cudaFree(b.perm);
+            cudaFree(b.tile_counts);
+            cudaFree(b.bin_totals);
+            b = vkg_ctx::ray_bins{nullptr, nullptr, nullptr, nullptr, 0, 0, b.done};
+            cudaGetLastError();
+            return nullptr;
+        }
+        b.cap = n;
+        b.tiles_cap = tiles;
+    }
+    float3 lo, scale;
+    float *plo = &lo.x, *ps = &scale.x;
+    for(int a = 0; a < 3; ++a)
+    {
+        plo[a] = bvh->scene_min[a];
+        const float ext = bvh->scene_max[a] - bvh->scene_min[a];
+        ps[a] = ext > 0.f ? (float)(1 << BIN_CELL_BITS) / ext : 0.f;
+    }
+    uint32_t *S = b.bin_totals, *F = b.bin_totals + NUM_BINS;
+    // the 16-bit bins live in the first half of perm's storage until k_bin_place overwrites it
+    // (k_bin_tiles reads them before; k_bin_place reads only keys)
+    uint16_t *bins16 = reinterpret_cast<uint16_t *>(b.perm);
+    k_bin_keys<<<(n + 255) / 256, 256, 0, st>>>(d_rays, n, lo, scale, bins16);
+    k_bin_tiles<<<tiles, BIN_THREADS, BIN_SMEM, st>>>(bins16, n, tile, b.keys, b.tile_counts);
+    k_bin_columns<<<NUM_BINS / 32, 1024, 0, st>>>(b.tile_counts, tiles, S);
+    k_bin_offsets<<<1, BIN_THREADS, BIN_SCAN_SMEM, st>>>(S, F);
+    k_bin_place<<<(n + 255) / 256, 256, 0, st>>>(b.keys, n, tile, b.tile_counts, F, b.perm);
+    return b.perm;
 }
 
 __global__ void k_fill_miss(vkg_hit *hits, uint32_t *occluded, uint32_t n)
@@ -176,8 +498,9 @@ __global__ void k_fill_miss(vkg_hit *hits, uint32_t *occluded, uint32_t n)
     if(occluded) occluded[i] = 0u;
 }
 
+// slot: the binning scratch set (0 for the caller's streams, 1 / 2 for the host variant's pipeline)
 vkg_status launch_trace(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t n, vkg_hit *d_hits,
-                        uint32_t *d_occ, uint32_t flags, cudaStream_t st)
+                        uint32_t *d_occ, uint32_t flags, cudaStream_t st, int slot = 0)
 {
     const uint32_t grid = (n + TRACE_THREADS - 1) / TRACE_THREADS;
     if(bvh->num_tris == 0 || bvh->num_nodes == 0)
@@ -202,16 +525,18 @@ vkg_status launch_trace(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays,
         return cuda_check(ctx, cudaGetLastError(), "k_trace_persistent");
     }
     const bool small = bvh->depth <= 10;
+    const uint32_t *perm = bin_rays(ctx, slot, bvh, d_rays, n, flags, st);
     if(d_occ)
     {
-        if(stats) launch_simple<true, true>(small, grid, st, bvh, d_rays, n, nullptr, d_occ, cull, ctx->d_counters);
-        else launch_simple<true, false>(small, grid, st, bvh, d_rays, n, nullptr, d_occ, cull, ctx->d_counters);
+        if(stats) launch_simple<true, true>(small, grid, st, bvh, d_rays, n, nullptr, d_occ, cull, ctx->d_counters, perm);
+        else launch_simple<true, false>(small, grid, st, bvh, d_rays, n, nullptr, d_occ, cull, ctx->d_counters, perm);
     }
     else
     {
-        if(stats) launch_simple<false, true>(small, grid, st, bvh, d_rays, n, d_hits, nullptr, cull, ctx->d_counters);
-        else launch_simple<false, false>(small, grid, st, bvh, d_rays, n, d_hits, nullptr, cull, ctx->d_counters);
+        if(stats) launch_simple<false, true>(small, grid, st, bvh, d_rays, n, d_hits, nullptr, cull, ctx->d_counters, perm);
+        else launch_simple<false, false>(small, grid, st, bvh, d_rays, n, d_hits, nullptr, cull, ctx->d_counters, perm);
     }
+    if(perm) cudaEventRecord(ctx->bins[slot].done, st);
     return cuda_check(ctx, cudaGetLastError(), "k_trace");
 }
 
@@ -310,7 +635,7 @@ extern "C" vkg_status vkg_closest_hit_host(vkg_ctx *ctx, const vkg_bvh *bvh, con
             status = cuda_check(ctx, e, "vkg_closest_hit_host");
             break;
         }
-        status = launch_trace(ctx, bvh, d_rays + first, n, d_hits + first, nullptr, flags, ps);
+        status = launch_trace(ctx, bvh, d_rays + first, n, d_hits + first, nullptr, flags, ps, 1 + (int)(c & 1u));
         if(status != VKG_OK) break;
         e = cudaMemcpyAsync(h_hits + first, d_hits + first, n * sizeof(vkg_hit), cudaMemcpyDeviceToHost, ps);
         if(e != cudaSuccess) status = cuda_check(ctx, e, "vkg_closest_hit_host");

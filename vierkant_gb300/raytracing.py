@@ -13,10 +13,11 @@ import weakref
 import numpy as np
 import torch
 
-from ._lib import (RAY_COUNT_STATS, RAY_CULL_BACK_FACES, check, lib, vkg_bvh_build_options, vkg_bvh_info, vkg_tlas_info,
-                   vkg_camera)
+from ._lib import (RAY_COUNT_STATS, RAY_CULL_BACK_FACES, RAY_KEEP_ORDER, check, lib, vkg_bvh_build_options,
+                   vkg_bvh_info, vkg_tlas_info, vkg_camera)
 
-__all__ = ["Context", "BVH", "TLAS", "INSTANCE_DTYPE", "hits_view", "RAY_CULL_BACK_FACES", "RAY_COUNT_STATS"]
+__all__ = ["Context", "BVH", "TLAS", "INSTANCE_DTYPE", "hits_view", "RAY_CULL_BACK_FACES", "RAY_COUNT_STATS",
+           "RAY_KEEP_ORDER"]
 
 
 def _stream_ptr(device) -> int:
