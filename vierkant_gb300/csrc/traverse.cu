@@ -184,7 +184,9 @@ void launch_simple(bool small_stack, uint32_t grid, cudaStream_t st, const vkg_b
 // Counting sort over T tiles of consecutive rays:
 //   k_bin_keys     every ray's bin (16 bits)
 //   k_bin_tiles    one CTA per tile: each ray's rank among the tile's rays of its bin (shared-memory
-//                  counters) and the tile's bin histogram -> M[t][bin]
+//                  counters) and the tile's bin histogram -> M[t][bin]; a tile whose rays are
+//                  coherent already (most 32-ray steps in one bin: camera rays) keeps its order as
+//                  one run in an extra bin placed after all others
 //   k_bin_columns  per bin, M[.][bin] scanned over the tiles in place (exclusive); S[bin] = total
 //   k_bin_offsets  F = exclusive scan of S: the bins' first positions
 //   k_bin_place    perm[F[bin] + M[t][bin] + rank] = ray
@@ -194,9 +196,13 @@ constexpr uint32_t NUM_BINS = 1u << (3 * BIN_CELL_BITS + 2 * BIN_DIR_BITS); // 3
 constexpr uint32_t BIN_MIN_RAYS = 1u << 19;
 constexpr int BIN_THREADS = 1024;                                           // per tile CTA
 constexpr uint32_t BIN_MAX_TILE = 40u * BIN_THREADS;                        // ranks fit 16 bits
-constexpr size_t BIN_SMEM = sizeof(uint32_t) * NUM_BINS;                    // 128 KB
+// slot NUM_BINS (KEEP_BIN): the rays of tiles that keep their order; the count rows are padded to
+// whole groups of 32 slots
+constexpr uint32_t KEEP_BIN = NUM_BINS;
+constexpr uint32_t BIN_SLOTS = NUM_BINS + 32;
+constexpr size_t BIN_SMEM = sizeof(uint32_t) * BIN_SLOTS;                    // 128 KB + 128 B
 static_assert(NUM_BINS == BIN_THREADS * 32, "32 bins per thread");
-static_assert(NUM_BINS <= 65536 && BIN_MAX_TILE <= 65536, "bin and rank are packed in 16 bits each");
+static_assert(BIN_SLOTS <= 65536 && BIN_MAX_TILE <= 65536, "bin and rank are packed in 16 bits each");
 
 __device__ __forceinline__ uint32_t spread3(uint32_t v) { return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4); }
 
@@ -255,12 +261,51 @@ __global__ void __launch_bounds__(BIN_THREADS)
                     uint32_t *__restrict__ M)
 {
     extern __shared__ uint32_t h[];
-    for(uint32_t b = threadIdx.x; b < NUM_BINS; b += BIN_THREADS) h[b] = 0u;
+    __shared__ uint32_t uniform_steps;
+    for(uint32_t b = threadIdx.x; b < BIN_SLOTS; b += BIN_THREADS) h[b] = 0u;
+    if(threadIdx.x == 0) uniform_steps = 0u;
     __syncthreads();
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t start = blockIdx.x * tile, end = min(start + tile, n);
     const uint32_t per_warp = tile / 32u; // a multiple of 32
     const uint32_t w0 = start + warp * per_warp, w1 = min(w0 + per_warp, end);
+    // a tile most of whose 32-ray steps fall into one bin each is coherent already (camera rays):
+    // it keeps its order, as one run in KEEP_BIN
+    constexpr int U = 8; // steps whose bins are loaded together
+    {
+        uint32_t u_steps = 0;
+        for(uint32_t r0 = w0; r0 < w1; r0 += 32u * U)
+        {
+            uint32_t bu[U];
+#pragma unroll
+            for(int u = 0; u < U; ++u)
+            {
+                const uint32_t i = r0 + 32u * u + lane;
+                bu[u] = i < w1 ? (uint32_t)__ldg(bins + i) : 0xFFFFFFFFu;
+            }
+#pragma unroll
+            for(int u = 0; u < U; ++u)
+            {
+                const uint32_t r = r0 + 32u * u;
+                if(r >= w1) break; // warp-uniform
+                const bool valid = r + lane < w1;
+                const uint32_t b0 = __shfl_sync(0xffffffffu, bu[u], 0);
+                u_steps += __all_sync(0xffffffffu, !valid || bu[u] == b0) ? 1u : 0u;
+            }
+        }
+        if(lane == 0 && u_steps) atomicAdd(&uniform_steps, u_steps);
+    }
+    __syncthreads();
+    const uint32_t steps = (end - start + 31u) / 32u;
+    if(2u * uniform_steps >= steps)
+    {
+        for(uint32_t i = start + threadIdx.x; i < end; i += BIN_THREADS) keys[i] = KEEP_BIN | ((i - start) << 16);
+        if(threadIdx.x == 0) h[KEEP_BIN] = end - start;
+        __syncthreads();
+        uint32_t *row = M + (size_t)blockIdx.x * BIN_SLOTS;
+        for(uint32_t b = threadIdx.x; b < BIN_SLOTS; b += BIN_THREADS) row[b] = h[b];
+        return;
+    }
     uint32_t run_bin = 0xFFFFFFFFu, run_start = 0, run_len = 0;
     // a run's ranks: one atomic, then its keys
     auto flush = [&]() {
@@ -272,7 +317,6 @@ __global__ void __launch_bounds__(BIN_THREADS)
         run_len = 0;
         run_bin = 0xFFFFFFFFu;
     };
-    constexpr int U = 8; // steps whose bins are loaded together
     for(uint32_t r0 = w0; r0 < w1; r0 += 32u * U)
     {
         uint32_t bu[U];
@@ -309,8 +353,8 @@ __global__ void __launch_bounds__(BIN_THREADS)
     }
     flush();
     __syncthreads();
-    uint32_t *row = M + (size_t)blockIdx.x * NUM_BINS;
-    for(uint32_t b = threadIdx.x; b < NUM_BINS; b += BIN_THREADS) row[b] = h[b];
+    uint32_t *row = M + (size_t)blockIdx.x * BIN_SLOTS;
+    for(uint32_t b = threadIdx.x; b < BIN_SLOTS; b += BIN_THREADS) row[b] = h[b];
 }
 
 // CTA = 32 bins (lanes) x 32 chunks of consecutive tiles (warps): chunk sums, their scan per bin in
@@ -323,7 +367,7 @@ __global__ void __launch_bounds__(1024) k_bin_columns(uint32_t *__restrict__ M, 
     const uint32_t per = (tiles + 31u) / 32u;
     const uint32_t t0 = min(warp * per, tiles), t1 = min(t0 + per, tiles);
     uint32_t sum = 0;
-    for(uint32_t t = t0; t < t1; ++t) sum += M[(size_t)t * NUM_BINS + b];
+    for(uint32_t t = t0; t < t1; ++t) sum += M[(size_t)t * BIN_SLOTS + b];
     part[warp][lane] = sum;
     __syncthreads();
     if(warp == 0)
@@ -341,7 +385,7 @@ __global__ void __launch_bounds__(1024) k_bin_columns(uint32_t *__restrict__ M, 
     uint32_t run = part[warp][lane];
     for(uint32_t t = t0; t < t1; ++t)
     {
-        uint32_t *p = M + (size_t)t * NUM_BINS + b;
+        uint32_t *p = M + (size_t)t * BIN_SLOTS + b;
         const uint32_t c = *p;
         *p = run;
         run += c;
@@ -389,6 +433,7 @@ __global__ void __launch_bounds__(BIN_THREADS) k_bin_offsets(const uint32_t *__r
     }
     __syncthreads();
     for(uint32_t b = t; b < NUM_BINS; b += BIN_THREADS) F[b] = sm[b + (b >> 5)];
+    if(t == BIN_THREADS - 1) F[KEEP_BIN] = acc; // the kept rays follow all bins
 }
 
 __global__ void __launch_bounds__(256)
@@ -398,7 +443,7 @@ __global__ void __launch_bounds__(256)
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= n) return;
     const uint32_t k = keys[i], bin = k & 0xFFFFu, t = i / tile;
-    perm[__ldg(F + bin) + M[(size_t)t * NUM_BINS + bin] + (k >> 16)] = i;
+    perm[__ldg(F + bin) + M[(size_t)t * BIN_SLOTS + bin] + (k >> 16)] = i;
 }
 
 // the traced order of a large batch (device pointer into the context's scratch), or nullptr to trace
@@ -456,8 +501,8 @@ const uint32_t *bin_rays(vkg_ctx *ctx, int slot, const vkg_bvh *bvh, const vkg_r
         // bin_totals: S, F
         if(cudaMalloc(&b.keys, sizeof(uint32_t) * (size_t)n) != cudaSuccess ||
            cudaMalloc(&b.perm, sizeof(uint32_t) * (size_t)n) != cudaSuccess ||
-           cudaMalloc(&b.tile_counts, sizeof(uint32_t) * (size_t)NUM_BINS * tiles) != cudaSuccess ||
-           cudaMalloc(&b.bin_totals, sizeof(uint32_t) * 2 * (size_t)NUM_BINS) != cudaSuccess)
+           cudaMalloc(&b.tile_counts, sizeof(uint32_t) * (size_t)BIN_SLOTS * tiles) != cudaSuccess ||
+           cudaMalloc(&b.bin_totals, sizeof(uint32_t) * 2 * (size_t)BIN_SLOTS) != cudaSuccess)
         {
             cudaFree(b.keys);
             cudaFree(b.perm);
@@ -478,13 +523,13 @@ const uint32_t *bin_rays(vkg_ctx *ctx, int slot, const vkg_bvh *bvh, const vkg_r
         const float ext = bvh->scene_max[a] - bvh->scene_min[a];
         ps[a] = ext > 0.f ? (float)(1 << BIN_CELL_BITS) / ext : 0.f;
     }
-    uint32_t *S = b.bin_totals, *F = b.bin_totals + NUM_BINS;
+    uint32_t *S = b.bin_totals, *F = b.bin_totals + BIN_SLOTS;
     // the 16-bit bins live in the first half of perm's storage until k_bin_place overwrites it
     // (k_bin_tiles reads them before; k_bin_place reads only keys)
     uint16_t *bins16 = reinterpret_cast<uint16_t *>(b.perm);
     k_bin_keys<<<(n + 255) / 256, 256, 0, st>>>(d_rays, n, lo, scale, bins16);
     k_bin_tiles<<<tiles, BIN_THREADS, BIN_SMEM, st>>>(bins16, n, tile, b.keys, b.tile_counts);
-    k_bin_columns<<<NUM_BINS / 32, 1024, 0, st>>>(b.tile_counts, tiles, S);
+    k_bin_columns<<<BIN_SLOTS / 32, 1024, 0, st>>>(b.tile_counts, tiles, S);
     k_bin_offsets<<<1, BIN_THREADS, BIN_SCAN_SMEM, st>>>(S, F);
     k_bin_place<<<(n + 255) / 256, 256, 0, st>>>(b.keys, n, tile, b.tile_counts, F, b.perm);
     return b.perm;
