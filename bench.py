@@ -32,6 +32,7 @@ sys.path.insert(0, str(ROOT))
 WIDTH, HEIGHT, SPP = 1280, 720, 4
 SEED = 0x5EED
 NODE_BYTES, TRI_BYTES, RAY_BYTES, HIT_BYTES = 96, 48, 32, 16
+BIN_MIN_RAYS = 1 << 19  # vkg_closest_hit traces batches this large in bins
 METRIC = "Mrays/s closest-hit"
 WORKLOAD = ("closest-hit, Cornell box + 64 cube-spheres (196,618 triangles), 1280x720x4 spp camera rays "
             "+ one uniform bounce ray per primary hit")
@@ -305,6 +306,8 @@ def run_ours(args):
     e2e_ok = bool(torch.equal(dev_hits, hits_host))
     hits_digest = batch_digest(dev_hits.numpy())
 
+    # per call: five ray-binning kernels (batches of 2^19 rays or more) and the traversal kernel
+    launches_per_call = 6 if n >= BIN_MIN_RAYS else 1
     peak, peak_kind = measured_peaks()
     achieved = bytes_per_launch / (ms_step * 1e-3) / 1e9
     prof = profiled_counters()
@@ -313,9 +316,9 @@ def run_ours(args):
                 "algorithmic_bytes_per_ray": round(bytes_per_launch / n, 1),
                 "node_visits_per_ray": round(visits / n, 3), "tri_tests_per_ray": round(tests / n, 3),
                 "note": "achieved/frac: algorithmic bytes (48 B ray+hit, 96 B per node visit, 48 B per "
-                        "triangle test) per second against the measured HBM copy bandwidth; the node and "
-                        "triangle reads are L1/L2 hits, so the kernel's limiter is instruction issue, "
-                        "not DRAM (dram_frac)"}
+                        "triangle test) per second against the measured HBM copy bandwidth, over the whole "
+                        "call (the ray-binning kernels included); the node and triangle reads are L1/L2 "
+                        "hits, so the traversal's limiter is instruction issue, not DRAM (dram_frac)"}
     if prof is not None:
         dram = prof["dram_bytes_per_ray"] * n
         roofline.update({
@@ -323,7 +326,6 @@ def run_ours(args):
             "dram_frac": round(dram / (ms_step * 1e-3) / 1e9 / peak, 4),
             "threads_per_instruction": prof.get("threads_per_instruction"),
             "warp_instructions_per_ray": prof.get("warp_instructions_per_ray"),
-            "issue_active_pct": prof.get("issue_active_pct"),
             "alu_pipe_pct": prof.get("alu_pipe_pct")})
 
     cpu = None
@@ -369,7 +371,7 @@ def run_ours(args):
                         "d2h_bytes_per_step": n * HIT_BYTES, "matches_device": e2e_ok,
                         "timing": f"median of {e2e_steps} host-buffer calls (wall clock, each synchronised)",
                         "mean_value": round(replica_throughput(n, ws, e2e_mean_ms), 1)},
-                "gpu_launches": args.steps, "roofline": roofline, "clocks": clk}
+                "gpu_launches": args.steps * launches_per_call, "roofline": roofline, "clocks": clk}
         if cpu is not None:
             line["cpu_baseline"] = cpu
         if c1 is not None:

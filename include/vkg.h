@@ -307,12 +307,12 @@ enum
 };
 /* Batches of 2^19 rays or more are traced in bins: rays are grouped by the cell of the scene box
  * (8 x 8 x 8) that holds their origin and by their direction (64 octahedral bins), and each group is
- * traced together. Results, counters and error flags are those of tracing in the given order; only
- * the speed differs. The context keeps the bins' scratch (12 B per ray plus 128 KB, grown on demand,
- * one set for the caller's streams -- calls on different streams are ordered by an event -- and one
- * per stream of the host variant's pipeline). Calls made while the stream is being captured into a
- * CUDA graph, calls with VKG_RAY_KEEP_ORDER, and calls whose scratch cannot be allocated trace in the
- * given order. */
+ * traced together; tiles of rays that are coherent already (most runs of 32 consecutive rays in one
+ * bin, as camera rays are) keep their order. Results, counters and error flags are those of tracing
+ * in the given order; only the speed differs. The context keeps the scratch (8 B per ray plus 128 KB
+ * per SM-sized tile, grown on demand; calls on different streams are ordered by an event). Calls made
+ * while the stream is being captured into a CUDA graph, calls with VKG_RAY_KEEP_ORDER, calls whose
+ * scratch cannot be allocated, and the host variant's 2^20-ray chunks trace in the given order. */
 vkg_status vkg_closest_hit(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t num_rays,
                            vkg_hit *d_hits, uint32_t flags, void *stream);
 vkg_status vkg_any_hit(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t num_rays,

@@ -85,14 +85,11 @@ vkg_status vkg_ctx_destroy(vkg_ctx *ctx)
         if(s) cudaStreamDestroy(s);
     for(cudaEvent_t e: ctx->pipe_ev)
         if(e) cudaEventDestroy(e);
-    for(auto &b: ctx->bins)
-    {
-        cudaFree(b.keys);
-        cudaFree(b.perm);
-        cudaFree(b.tile_counts);
-        cudaFree(b.bin_totals);
-        if(b.done) cudaEventDestroy(b.done);
-    }
+    cudaFree(ctx->bins.keys);
+    cudaFree(ctx->bins.perm);
+    cudaFree(ctx->bins.tile_counts);
+    cudaFree(ctx->bins.bin_totals);
+    if(ctx->bins.done) cudaEventDestroy(ctx->bins.done);
     delete ctx;
     return VKG_OK;
 }

@@ -24,11 +24,12 @@ struct vkg_ctx
     void *d_stage_rays = nullptr;
     void *d_stage_hits = nullptr;
     size_t stage_rays_bytes = 0, stage_hits_bytes = 0;
-    // the host variant's copy / trace pipeline: two streams and a fork + two join events (first use)
-    cudaStream_t pipe[2] = {nullptr, nullptr};
-    cudaEvent_t pipe_ev[3] = {nullptr, nullptr, nullptr};
-    // ray-binning scratch of the bulk queries: [0] the caller's streams, [1], [2] the host variant's
-    // pipeline streams. keys: bin | rank in its tile << 16 per ray; perm: traced position -> ray
+    // the host variant's copy / trace pipeline (created on first use): streams [0], [1] trace
+    // alternate chunks, [2] uploads, [3] downloads; events: [0] fork, [1..4] joins, [5] a chunk's
+    // upload done, [6] a chunk's trace done
+    cudaStream_t pipe[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t pipe_ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    // ray-binning scratch of the bulk queries (calls on different streams are ordered by `done`). keys: bin | rank in its tile << 16 per ray; perm: traced position -> ray
     // index (its first half holds the 16-bit bins before that); tile_counts: rays per (tile, bin);
     // bin_totals: rays per bin and the bins' first positions; done: recorded after the last use,
     // waited for by the next
@@ -41,7 +42,7 @@ struct vkg_ctx
         size_t cap = 0;
         uint32_t tiles_cap = 0;
         cudaEvent_t done = nullptr;
-    } bins[3];
+    } bins;
 };
 
 struct vkg_bvh

@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <string>
+#include <vector>
 
 namespace vkg
 {
@@ -448,7 +449,7 @@ __global__ void __launch_bounds__(256)
 
 // the traced order of a large batch (device pointer into the context's scratch), or nullptr to trace
 // in the given order
-const uint32_t *bin_rays(vkg_ctx *ctx, int slot, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t n,
+const uint32_t *bin_rays(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t n,
                          uint32_t flags, cudaStream_t st)
 {
     if((flags & VKG_RAY_KEEP_ORDER) || n < BIN_MIN_RAYS) return nullptr;
@@ -477,7 +478,7 @@ const uint32_t *bin_rays(vkg_ctx *ctx, int slot, const vkg_bvh *bvh, const vkg_r
     const uint32_t tile =
             (uint32_t)std::min<size_t>(BIN_MAX_TILE, (per_sm + BIN_THREADS - 1) / BIN_THREADS * BIN_THREADS);
     const uint32_t tiles = (uint32_t)(((size_t)n + tile - 1) / tile);
-    auto &b = ctx->bins[slot];
+    auto &b = ctx->bins;
     if(!b.done && cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming) != cudaSuccess)
     {
         b.done = nullptr;
@@ -543,9 +544,8 @@ __global__ void k_fill_miss(vkg_hit *hits, uint32_t *occluded, uint32_t n)
     if(occluded) occluded[i] = 0u;
 }
 
-// slot: the binning scratch set (0 for the caller's streams, 1 / 2 for the host variant's pipeline)
 vkg_status launch_trace(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t n, vkg_hit *d_hits,
-                        uint32_t *d_occ, uint32_t flags, cudaStream_t st, int slot = 0)
+                        uint32_t *d_occ, uint32_t flags, cudaStream_t st)
 {
     const uint32_t grid = (n + TRACE_THREADS - 1) / TRACE_THREADS;
     if(bvh->num_tris == 0 || bvh->num_nodes == 0)
@@ -570,7 +570,7 @@ vkg_status launch_trace(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays,
         return cuda_check(ctx, cudaGetLastError(), "k_trace_persistent");
     }
     const bool small = bvh->depth <= 10;
-    const uint32_t *perm = bin_rays(ctx, slot, bvh, d_rays, n, flags, st);
+    const uint32_t *perm = bin_rays(ctx, bvh, d_rays, n, flags, st);
     if(d_occ)
     {
         if(stats) launch_simple<true, true>(small, grid, st, bvh, d_rays, n, nullptr, d_occ, cull, ctx->d_counters, perm);
@@ -581,7 +581,7 @@ vkg_status launch_trace(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays,
         if(stats) launch_simple<false, true>(small, grid, st, bvh, d_rays, n, d_hits, nullptr, cull, ctx->d_counters, perm);
         else launch_simple<false, false>(small, grid, st, bvh, d_rays, n, d_hits, nullptr, cull, ctx->d_counters, perm);
     }
-    if(perm) cudaEventRecord(ctx->bins[slot].done, st);
+    if(perm) cudaEventRecord(ctx->bins.done, st);
     return cuda_check(ctx, cudaGetLastError(), "k_trace");
 }
 
@@ -618,6 +618,45 @@ extern "C" vkg_status vkg_any_hit(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ra
     return launch_trace(ctx, bvh, d_rays, num_rays, nullptr, d_occluded, flags, static_cast<cudaStream_t>(stream));
 }
 
+namespace vkg
+{
+namespace
+{
+// Chunk sizes of the host variant's pipeline: 2^20 rays, with a ramp of 2^18 and 2^19 at the start
+// (the first trace waits only for a short upload; each upload still ends before the trace before it,
+// as uploads run about twice as fast as traces) and a 2^18 chunk at the end (a short last download).
+// One chunk up to 2^20 rays.
+std::vector<uint32_t> host_chunks(uint32_t n)
+{
+    constexpr uint32_t FULL = 1u << 20, SMALL = 1u << 18;
+    std::vector<uint32_t> out;
+    if(n <= FULL)
+    {
+        out.push_back(n);
+        return out;
+    }
+    uint32_t left = n;
+    for(uint32_t s: {SMALL, 2 * SMALL})
+    {
+        out.push_back(s);
+        left -= s;
+    }
+    while(left > FULL + SMALL)
+    {
+        out.push_back(FULL);
+        left -= FULL;
+    }
+    if(left > 2 * SMALL)
+    {
+        out.push_back(left - SMALL);
+        left = SMALL;
+    }
+    out.push_back(left);
+    return out;
+}
+}// namespace
+}// namespace vkg
+
 extern "C" vkg_status vkg_closest_hit_host(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *h_rays,
                                            uint32_t num_rays, vkg_hit *h_hits, uint32_t flags, void *stream)
 {
@@ -644,11 +683,13 @@ extern "C" vkg_status vkg_closest_hit_host(vkg_ctx *ctx, const vkg_bvh *bvh, con
         VKG_TRY_CUDA(ctx, cudaMalloc(&ctx->d_stage_hits, hb));
         ctx->stage_hits_bytes = hb;
     }
-    // Chunks of HOST_CHUNK rays alternate between two streams: chunk c's upload, trace and download
-    // are ordered on its stream, so the upload of c + 1 and the download of c - 1 (two copy engines)
-    // run under the trace of c. Each chunk has its own region of the staging buffers.
-    constexpr uint32_t HOST_CHUNK = 1u << 20;
-    const uint32_t chunks = (num_rays + HOST_CHUNK - 1) / HOST_CHUNK;
+    // Chunks flow through three engines at once: one stream uploads the chunks back to back, two
+    // streams trace alternate chunks (each chunk after its upload), one stream downloads each chunk's
+    // hits after its trace. Each chunk has its own region of the staging buffers, so nothing waits
+    // for a buffer to be free. The chunks are traced in their given order: binning a chunk costs more
+    // than it saves at this size (the one-call variant bins large batches).
+    const std::vector<uint32_t> sizes = host_chunks(num_rays);
+    const uint32_t chunks = (uint32_t)sizes.size();
     auto *d_rays = static_cast<vkg_ray *>(ctx->d_stage_rays);
     auto *d_hits = static_cast<vkg_hit *>(ctx->d_stage_hits);
     // (the persistent kernels share one work counter, so they are not run on two streams at once)
@@ -661,32 +702,40 @@ extern "C" vkg_status vkg_closest_hit_host(vkg_ctx *ctx, const vkg_bvh *bvh, con
         VKG_TRY_CUDA(ctx, cudaStreamSynchronize(st));
         return VKG_OK;
     }
-    for(int k = 0; k < 2; ++k)
-        if(!ctx->pipe[k]) VKG_TRY_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->pipe[k], cudaStreamNonBlocking));
-    for(int k = 0; k < 3; ++k)
-        if(!ctx->pipe_ev[k]) VKG_TRY_CUDA(ctx, cudaEventCreateWithFlags(&ctx->pipe_ev[k], cudaEventDisableTiming));
-    // fork: both streams start after the work already queued on the caller's stream
+    for(cudaStream_t &p: ctx->pipe)
+        if(!p) VKG_TRY_CUDA(ctx, cudaStreamCreateWithFlags(&p, cudaStreamNonBlocking));
+    for(cudaEvent_t &e: ctx->pipe_ev)
+        if(!e) VKG_TRY_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    cudaStream_t up = ctx->pipe[2], down = ctx->pipe[3];
+    cudaEvent_t up_done = ctx->pipe_ev[5], trace_done = ctx->pipe_ev[6];
+    // fork: every stream starts after the work already queued on the caller's stream
     VKG_TRY_CUDA(ctx, cudaEventRecord(ctx->pipe_ev[0], st));
-    for(int k = 0; k < 2; ++k) VKG_TRY_CUDA(ctx, cudaStreamWaitEvent(ctx->pipe[k], ctx->pipe_ev[0], 0));
+    for(cudaStream_t p: ctx->pipe) VKG_TRY_CUDA(ctx, cudaStreamWaitEvent(p, ctx->pipe_ev[0], 0));
+    // (an event is re-recorded for the next chunk only after the wait on its last record is queued)
     vkg_status status = VKG_OK;
-    for(uint32_t c = 0; c < chunks && status == VKG_OK; ++c)
+    size_t first = 0;
+    for(uint32_t c = 0; c < chunks && status == VKG_OK; first += sizes[c], ++c)
     {
-        cudaStream_t ps = ctx->pipe[c & 1u];
-        const size_t first = (size_t)c * HOST_CHUNK;
-        const uint32_t n = (uint32_t)std::min<size_t>(HOST_CHUNK, num_rays - first);
-        cudaError_t e = cudaMemcpyAsync(d_rays + first, h_rays + first, n * sizeof(vkg_ray), cudaMemcpyHostToDevice, ps);
+        cudaStream_t ts = ctx->pipe[c & 1u];
+        const uint32_t n = sizes[c];
+        cudaError_t e = cudaMemcpyAsync(d_rays + first, h_rays + first, n * sizeof(vkg_ray), cudaMemcpyHostToDevice, up);
+        if(e == cudaSuccess) e = cudaEventRecord(up_done, up);
+        if(e == cudaSuccess) e = cudaStreamWaitEvent(ts, up_done, 0);
         if(e != cudaSuccess)
         {
             status = cuda_check(ctx, e, "vkg_closest_hit_host");
             break;
         }
-        status = launch_trace(ctx, bvh, d_rays + first, n, d_hits + first, nullptr, flags, ps, 1 + (int)(c & 1u));
+        status = launch_trace(ctx, bvh, d_rays + first, n, d_hits + first, nullptr, flags | VKG_RAY_KEEP_ORDER, ts);
         if(status != VKG_OK) break;
-        e = cudaMemcpyAsync(h_hits + first, d_hits + first, n * sizeof(vkg_hit), cudaMemcpyDeviceToHost, ps);
+        e = cudaEventRecord(trace_done, ts);
+        if(e == cudaSuccess) e = cudaStreamWaitEvent(down, trace_done, 0);
+        if(e == cudaSuccess)
+            e = cudaMemcpyAsync(h_hits + first, d_hits + first, n * sizeof(vkg_hit), cudaMemcpyDeviceToHost, down);
         if(e != cudaSuccess) status = cuda_check(ctx, e, "vkg_closest_hit_host");
     }
-    // join: the caller's stream waits for both (also after an error, so nothing is left in flight)
-    for(int k = 0; k < 2; ++k)
+    // join: the caller's stream waits for every stream (also after an error, so nothing is left in flight)
+    for(int k = 0; k < 4; ++k)
     {
         cudaEventRecord(ctx->pipe_ev[1 + k], ctx->pipe[k]);
         cudaStreamWaitEvent(st, ctx->pipe_ev[1 + k], 0);
