@@ -389,6 +389,18 @@ static inline float fdec_(uint32_t u)
     memcpy(&f, &b, 4);
     return f;
 }
+static inline uint32_t fbits_(float f)
+{
+    uint32_t b;
+    memcpy(&b, &f, 4);
+    return b;
+}
+static inline float fval_(uint32_t b)
+{
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+}
 #define STACK_CAP 256
 
 typedef struct {
@@ -462,6 +474,7 @@ static void trace_one_ex(const orc_bvh *b, const orc_ray *ray, int cull_mode, co
         neg[a] = inv_d[a] < 0.f;
     }
     float best_t = ray->tmax, bu = 0.f, bv = 0.f;
+    const int pos = !(fbits_(ray->tmin) & 0x80000000u);
     uint32_t best = ORC_MISS;
     uint32_t st_node[STACK_CAP];
     float st_t[STACK_CAP];
@@ -502,8 +515,9 @@ static void trace_one_ex(const orc_bvh *b, const orc_ray *ray, int cull_mode, co
             float tf = fminf(fminf(tf3[0], tf3[1]), fminf(tf3[2], best_t));
             if(tn <= tf)
             {
-                /* 32-bit key as in the kernels: ordered entry distance, low 3 bits = slot */
-                uint32_t key = (fenc_(tn) & ~7u) | (uint32_t)k;
+                /* 32-bit key as in the kernels: ordered entry distance, low 3 bits = slot; a ray with
+                   tmin >= +0 keys the distance's bits with the sign cleared */
+                uint32_t key = pos ? ((fbits_(tn) & 0x7FFFFFF8u) | (uint32_t)k) : ((fenc_(tn) & ~7u) | (uint32_t)k);
                 int p = nh++;
                 while(p > 0 && hkey[p - 1] > key)
                 {
@@ -515,7 +529,7 @@ static void trace_one_ex(const orc_bvh *b, const orc_ray *ray, int cull_mode, co
         }
         for(int h = 0; h < nh; ++h)
         {
-            ht[h] = fdec_(hkey[h] & ~7u);
+            ht[h] = pos ? fval_(hkey[h] & 0x7FFFFFF8u) : fdec_(hkey[h] & ~7u);
             hk[h] = (int)(hkey[h] & 7u);
         }
         for(int h = 0; h < nh && !done; ++h)

@@ -37,8 +37,11 @@ __global__ void __launch_bounds__(TRACE_THREADS)
         const uint32_t i = perm ? __ldg(perm + j) : j;
         const float4 *rp = reinterpret_cast<const float4 *>(rays + i);
         const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
-        trace_result r = trace_ray<ANY, STATS, STACK>(nodes, tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w,
-                                                      cull, visits, tests, counters);
+        const trace_result r =
+                key_pos(r0.w) ? trace_ray_mode<ANY, STATS, STACK, true>(nodes, tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y,
+                                                                        r1.z, r1.w, cull, visits, tests, counters)
+                              : trace_ray_mode<ANY, STATS, STACK, false>(nodes, tris, r0.x, r0.y, r0.z, r0.w, r1.x,
+                                                                         r1.y, r1.z, r1.w, cull, visits, tests, counters);
         if(ANY) { occluded[i] = r.occluded ? 1u : 0u; }
         else
         {

@@ -43,6 +43,22 @@ __device__ __forceinline__ float tdec(uint32_t u)
     return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
 }
 
+// Child keys: an entry distance as an ordered 32-bit key with its low 3 bits replaced by the slot.
+// For a ray with tmin >= +0 every entry distance is >= +0, whose float bits order like the values:
+// the key is the bits with the sign cleared (so -0 and +0 agree). Other rays use tenc / tdec.
+template<bool POS>
+__device__ __forceinline__ uint32_t child_key(float tn, uint32_t k)
+{
+    return POS ? ((__float_as_uint(tn) & 0x7FFFFFF8u) | k) : ((tenc(tn) & ~7u) | k);
+}
+template<bool POS>
+__device__ __forceinline__ float key_dist(uint32_t key)
+{
+    return POS ? __uint_as_float(key & 0x7FFFFFF8u) : tdec(key & ~7u);
+}
+// the key mode of a ray: its tmin's sign bit clear
+__device__ __forceinline__ bool key_pos(float tmin) { return !(__float_as_uint(tmin) & 0x80000000u); }
+
 __device__ __forceinline__ void cswap(uint32_t &a, uint32_t &b)
 {
     const uint32_t lo = min(a, b), hi = max(a, b);
@@ -121,8 +137,9 @@ __device__ __forceinline__ void ray_init(ray_state_t<STACK> &s, float ox, float 
 // interval [tmin, tmax]): key = ordered entry distance with its low 3 bits replaced by the slot,
 // 0xFFFFFFFF for a child the ray misses. Truncation only lowers the stored distance, so pruning with
 // it stays conservative. w4 / w5 receive the node's child words.
-// COUNT: also count the internal (non-leaf) children the ray hits into *n_int
-template<bool COUNT = false>
+// COUNT: also count the internal (non-leaf) children the ray hits into *n_int; POS: the key mode of a
+// ray with tmin >= +0 (child_key)
+template<bool COUNT = false, bool POS = false>
 __device__ __forceinline__ void node_keys(const node8 *__restrict__ nodes, uint32_t ni, float ox, float oy, float oz,
                                           float ix, float iy, float iz, float tmin, float tmax, uint32_t (&key)[8],
                                           uint4 &w4, uint4 &w5, uint32_t *n_int = nullptr)
@@ -164,7 +181,7 @@ __device__ __forceinline__ void node_keys(const node8 *__restrict__ nodes, uint3
             const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
             if(tn <= tf)
             {
-                key[k] = (tenc(tn) & ~7u) | (uint32_t)k;
+                key[k] = child_key<POS>(tn, (uint32_t)k);
                 if(COUNT)
                 {
                     const uint32_t c = k < 4 ? (k == 0 ? w4.x : k == 1 ? w4.y : k == 2 ? w4.z : w4.w)
@@ -177,8 +194,9 @@ __device__ __forceinline__ void node_keys(const node8 *__restrict__ nodes, uint3
     if(COUNT) *n_int = nint;
 }
 
-// one node of the traversal; returns false once the ray is finished
-template<bool ANY, bool STATS, int STACK>
+// one node of the traversal; returns false once the ray is finished. POS: the ray's tmin is >= +0
+// (key_pos)
+template<bool ANY, bool STATS, int STACK, bool POS = false>
 __device__ __forceinline__ bool ray_step(ray_state_t<STACK> &s, const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
                                          int cull, unsigned long long &visits, unsigned long long &tests,
                                          unsigned long long *__restrict__ counters)
@@ -193,7 +211,7 @@ __device__ __forceinline__ bool ray_step(ray_state_t<STACK> &s, const node8 *__r
         uint32_t key[8];
         uint4 w4, w5;
         uint32_t n_int;
-        node_keys<true>(nodes, ni, s.ox, s.oy, s.oz, s.ix, s.iy, s.iz, s.tmin, s.best_t, key, w4, w5, &n_int);
+        node_keys<true, POS>(nodes, ni, s.ox, s.oy, s.oz, s.ix, s.iy, s.iz, s.tmin, s.best_t, key, w4, w5, &n_int);
         sort8(key);
         // one pass over the hit children, near to far: leaves are intersected as they come, internal
         // children are written to the stack far-to-near (the r-th nearest at base + n_int - 1 - r) so
@@ -206,7 +224,7 @@ __device__ __forceinline__ bool ray_step(ray_state_t<STACK> &s, const node8 *__r
             if(key[h] == 0xFFFFFFFFu || s.done) break;
             const uint32_t k = key[h] & 7u;
             const uint32_t c = (k & 4u) ? sel4(w5, k & 3u) : sel4(w4, k & 3u);
-            const float tentry = tdec(key[h] & ~7u);
+            const float tentry = key_dist<POS>(key[h]);
             if(!(c & LEAF_BIT))
             {
                 const int pos = base + (int)n_int - 1 - r;
@@ -317,6 +335,21 @@ __device__ __forceinline__ bool trace_transmit(const node8 *__restrict__ nodes, 
     return true;
 }
 
+template<bool ANY, bool STATS, int STACK, bool POS>
+__device__ __forceinline__ trace_result trace_ray_mode(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
+                                                       float ox, float oy, float oz, float tmin, float dx, float dy,
+                                                       float dz, float tmax, int cull, unsigned long long &visits,
+                                                       unsigned long long &tests,
+                                                       unsigned long long *__restrict__ counters)
+{
+    ray_state_t<STACK> s;
+    uint2 stack[STACK];
+    s.st = stack;
+    ray_init(s, ox, oy, oz, tmin, dx, dy, dz, tmax);
+    while(ray_step<ANY, STATS, STACK, POS>(s, nodes, tris, cull, visits, tests, counters)) {}
+    return ray_result(s);
+}
+
 template<bool ANY, bool STATS, int STACK = (int)TRAVERSAL_STACK>
 __device__ __forceinline__ trace_result trace_ray(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
                                                   float ox, float oy, float oz, float tmin, float dx, float dy,
@@ -324,12 +357,8 @@ __device__ __forceinline__ trace_result trace_ray(const node8 *__restrict__ node
                                                   unsigned long long &visits, unsigned long long &tests,
                                                   unsigned long long *__restrict__ counters)
 {
-    ray_state_t<STACK> s;
-    uint2 stack[STACK];
-    s.st = stack;
-    ray_init(s, ox, oy, oz, tmin, dx, dy, dz, tmax);
-    while(ray_step<ANY, STATS>(s, nodes, tris, cull, visits, tests, counters)) {}
-    return ray_result(s);
+    return trace_ray_mode<ANY, STATS, STACK, false>(nodes, tris, ox, oy, oz, tmin, dx, dy, dz, tmax, cull, visits,
+                                                     tests, counters);
 }
 
 }// namespace vkg
