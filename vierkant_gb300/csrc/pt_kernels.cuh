@@ -1141,7 +1141,7 @@ __global__ void __launch_bounds__(PT_THREADS)
         const bool active = cur != 0xFFFFFFFFu;
         if(!__any_sync(0xffffffffu, active)) break;
         if(active &&
-           !ray_step<SHADOW, false>(s, nodes, tris, SHADOW ? CULL_NONE : CULL_BACK_UNLESS_TWOSIDED, v, t, nullptr))
+           !ray_step_auto<SHADOW, false>(s, nodes, tris, SHADOW ? CULL_NONE : CULL_BACK_UNLESS_TWOSIDED, v, t, nullptr))
         {
             const trace_result r = ray_result(s);
             if constexpr(SHADOW)

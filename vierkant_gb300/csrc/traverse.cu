@@ -37,11 +37,8 @@ __global__ void __launch_bounds__(TRACE_THREADS)
         const uint32_t i = perm ? __ldg(perm + j) : j;
         const float4 *rp = reinterpret_cast<const float4 *>(rays + i);
         const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
-        const trace_result r =
-                key_pos(r0.w) ? trace_ray_mode<ANY, STATS, STACK, true>(nodes, tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y,
-                                                                        r1.z, r1.w, cull, visits, tests, counters)
-                              : trace_ray_mode<ANY, STATS, STACK, false>(nodes, tris, r0.x, r0.y, r0.z, r0.w, r1.x,
-                                                                         r1.y, r1.z, r1.w, cull, visits, tests, counters);
+        const trace_result r = trace_ray<ANY, STATS, STACK>(nodes, tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z,
+                                                            r1.w, cull, visits, tests, counters);
         if(ANY) { occluded[i] = r.occluded ? 1u : 0u; }
         else
         {
@@ -107,7 +104,7 @@ __global__ void __launch_bounds__(TRACE_THREADS)
         }
         const bool active = cur != 0xFFFFFFFFu;
         if(!__any_sync(0xffffffffu, active)) break;
-        if(active && !ray_step<ANY, STATS>(s, nodes, tris, cull, visits, tests, counters))
+        if(active && !ray_step_auto<ANY, STATS>(s, nodes, tris, cull, visits, tests, counters))
         {
             const trace_result r = ray_result(s);
             if(ANY) occluded[cur] = r.occluded ? 1u : 0u;

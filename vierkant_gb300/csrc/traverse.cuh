@@ -350,6 +350,7 @@ __device__ __forceinline__ trace_result trace_ray_mode(const node8 *__restrict__
     return ray_result(s);
 }
 
+// one ray, in the key mode its tmin allows
 template<bool ANY, bool STATS, int STACK = (int)TRAVERSAL_STACK>
 __device__ __forceinline__ trace_result trace_ray(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
                                                   float ox, float oy, float oz, float tmin, float dx, float dy,
@@ -357,8 +358,21 @@ __device__ __forceinline__ trace_result trace_ray(const node8 *__restrict__ node
                                                   unsigned long long &visits, unsigned long long &tests,
                                                   unsigned long long *__restrict__ counters)
 {
+    if(key_pos(tmin))
+        return trace_ray_mode<ANY, STATS, STACK, true>(nodes, tris, ox, oy, oz, tmin, dx, dy, dz, tmax, cull, visits,
+                                                        tests, counters);
     return trace_ray_mode<ANY, STATS, STACK, false>(nodes, tris, ox, oy, oz, tmin, dx, dy, dz, tmax, cull, visits,
                                                      tests, counters);
+}
+
+// one node of a ray's traversal (ray_step) in the key mode its tmin allows
+template<bool ANY, bool STATS, int STACK>
+__device__ __forceinline__ bool ray_step_auto(ray_state_t<STACK> &s, const node8 *__restrict__ nodes,
+                                              const tri_rec *__restrict__ tris, int cull, unsigned long long &visits,
+                                              unsigned long long &tests, unsigned long long *__restrict__ counters)
+{
+    return key_pos(s.tmin) ? ray_step<ANY, STATS, STACK, true>(s, nodes, tris, cull, visits, tests, counters)
+                           : ray_step<ANY, STATS, STACK, false>(s, nodes, tris, cull, visits, tests, counters);
 }
 
 }// namespace vkg
