@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(TRACE_THREADS)
         k_trace_persistent(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
                            const vkg_ray *__restrict__ rays, uint32_t n, vkg_hit *__restrict__ hits,
                            uint32_t *__restrict__ occluded, int cull, unsigned long long *__restrict__ counters,
-                           uint32_t *__restrict__ next_ray)
+                           uint32_t *__restrict__ next_ray, const uint32_t *__restrict__ perm)
 {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt = (1u << lane) - 1u;
@@ -91,9 +91,10 @@ __global__ void __launch_bounds__(TRACE_THREADS)
             base = __shfl_sync(0xffffffffu, base, leader);
             if(need)
             {
-                const uint32_t idx = base + __popc(m & lt);
-                if(idx < n)
+                const uint32_t pos = base + __popc(m & lt);
+                if(pos < n)
                 {
+                    const uint32_t idx = perm ? __ldg(perm + pos) : pos; // the ray at traced position pos
                     const float4 *rp = reinterpret_cast<const float4 *>(rays + idx);
                     const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
                     ray_init(s, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w);
@@ -131,7 +132,7 @@ __global__ void __launch_bounds__(TRACE_THREADS)
 
 template<bool ANY, bool STATS>
 void launch_persistent(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t n, vkg_hit *d_hits,
-                       uint32_t *d_occ, int cull, cudaStream_t st)
+                       uint32_t *d_occ, int cull, cudaStream_t st, const uint32_t *perm)
 {
     static int blocks_per_sm = 0;
     if(blocks_per_sm == 0)
@@ -145,7 +146,7 @@ void launch_persistent(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, 
     if(grid > need) grid = need;
     cudaMemsetAsync(ctx->d_work, 0, sizeof(uint32_t), st);
     k_trace_persistent<ANY, STATS><<<grid, TRACE_THREADS, 0, st>>>(bvh->d_nodes, bvh->d_tris, d_rays, n, d_hits, d_occ,
-                                                                   cull, ctx->d_counters, ctx->d_work);
+                                                                   cull, ctx->d_counters, ctx->d_work, perm);
 }
 
 // kernel choice: the one-thread-per-ray kernel by default (faster on mixed primary/bounce batches);
@@ -555,22 +556,23 @@ vkg_status launch_trace(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays,
     }
     const int cull = (flags & VKG_RAY_CULL_BACK_FACES) ? 1 : 0;
     const bool stats = (flags & VKG_RAY_COUNT_STATS) != 0;
+    const uint32_t *perm = bin_rays(ctx, bvh, d_rays, n, flags, st);
     if(use_persistent())
     {
         if(d_occ)
         {
-            if(stats) launch_persistent<true, true>(ctx, bvh, d_rays, n, nullptr, d_occ, cull, st);
-            else launch_persistent<true, false>(ctx, bvh, d_rays, n, nullptr, d_occ, cull, st);
+            if(stats) launch_persistent<true, true>(ctx, bvh, d_rays, n, nullptr, d_occ, cull, st, perm);
+            else launch_persistent<true, false>(ctx, bvh, d_rays, n, nullptr, d_occ, cull, st, perm);
         }
         else
         {
-            if(stats) launch_persistent<false, true>(ctx, bvh, d_rays, n, d_hits, nullptr, cull, st);
-            else launch_persistent<false, false>(ctx, bvh, d_rays, n, d_hits, nullptr, cull, st);
+            if(stats) launch_persistent<false, true>(ctx, bvh, d_rays, n, d_hits, nullptr, cull, st, perm);
+            else launch_persistent<false, false>(ctx, bvh, d_rays, n, d_hits, nullptr, cull, st, perm);
         }
+        if(perm) cudaEventRecord(ctx->bins.done, st);
         return cuda_check(ctx, cudaGetLastError(), "k_trace_persistent");
     }
     const bool small = bvh->depth <= 10;
-    const uint32_t *perm = bin_rays(ctx, bvh, d_rays, n, flags, st);
     if(d_occ)
     {
         if(stats) launch_simple<true, true>(small, grid, st, bvh, d_rays, n, nullptr, d_occ, cull, ctx->d_counters, perm);

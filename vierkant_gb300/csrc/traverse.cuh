@@ -223,7 +223,9 @@ __device__ __forceinline__ bool ray_step(ray_state_t<STACK> &s, const node8 *__r
         {
             if(key[h] == 0xFFFFFFFFu || s.done) break;
             const uint32_t k = key[h] & 7u;
-            const uint32_t c = (k & 4u) ? sel4(w5, k & 3u) : sel4(w4, k & 3u);
+            // the child word from L1 (the node's line was just read): one load instead of a select
+            // over eight registers
+            const uint32_t c = __ldg(&nodes[ni].child[k]);
             const float tentry = key_dist<POS>(key[h]);
             if(!(c & LEAF_BIT))
             {
