@@ -27,14 +27,15 @@ template<bool ANY, bool STATS, int STACK>
 __global__ void __launch_bounds__(TRACE_THREADS)
         k_trace(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris, const vkg_ray *__restrict__ rays,
                 uint32_t n, vkg_hit *__restrict__ hits, uint32_t *__restrict__ occluded, int cull,
-                unsigned long long *__restrict__ counters, const uint32_t *__restrict__ perm)
+                unsigned long long *__restrict__ counters, const uint32_t *__restrict__ perm,
+                const uint32_t *__restrict__ reordered)
 {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long visits = 0, tests = 0;
     if(j < n)
     {
-        // thread j traces ray perm[j] when the batch was binned
-        const uint32_t i = perm ? __ldg(perm + j) : j;
+        // thread j traces ray perm[j] when the batch was binned (and some tile did not keep its order)
+        const uint32_t i = (perm && __ldg(reordered)) ? __ldg(perm + j) : j;
         const float4 *rp = reinterpret_cast<const float4 *>(rays + i);
         const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
         const trace_result r = trace_ray<ANY, STATS, STACK>(nodes, tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z,
@@ -69,8 +70,10 @@ __global__ void __launch_bounds__(TRACE_THREADS)
         k_trace_persistent(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
                            const vkg_ray *__restrict__ rays, uint32_t n, vkg_hit *__restrict__ hits,
                            uint32_t *__restrict__ occluded, int cull, unsigned long long *__restrict__ counters,
-                           uint32_t *__restrict__ next_ray, const uint32_t *__restrict__ perm)
+                           uint32_t *__restrict__ next_ray, const uint32_t *__restrict__ perm,
+                           const uint32_t *__restrict__ reordered)
 {
+    if(perm && __ldg(reordered) == 0u) perm = nullptr;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt = (1u << lane) - 1u;
     unsigned long long visits = 0, tests = 0;
@@ -132,7 +135,7 @@ __global__ void __launch_bounds__(TRACE_THREADS)
 
 template<bool ANY, bool STATS>
 void launch_persistent(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t n, vkg_hit *d_hits,
-                       uint32_t *d_occ, int cull, cudaStream_t st, const uint32_t *perm)
+                       uint32_t *d_occ, int cull, cudaStream_t st, const uint32_t *perm, const uint32_t *reordered)
 {
     static int blocks_per_sm = 0;
     if(blocks_per_sm == 0)
@@ -146,7 +149,7 @@ void launch_persistent(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, 
     if(grid > need) grid = need;
     cudaMemsetAsync(ctx->d_work, 0, sizeof(uint32_t), st);
     k_trace_persistent<ANY, STATS><<<grid, TRACE_THREADS, 0, st>>>(bvh->d_nodes, bvh->d_tris, d_rays, n, d_hits, d_occ,
-                                                                   cull, ctx->d_counters, ctx->d_work, perm);
+                                                                   cull, ctx->d_counters, ctx->d_work, perm, reordered);
 }
 
 // kernel choice: the one-thread-per-ray kernel by default (faster on mixed primary/bounce batches);
@@ -165,14 +168,14 @@ bool use_persistent()
 template<bool ANY, bool STATS>
 void launch_simple(bool small_stack, uint32_t grid, cudaStream_t st, const vkg_bvh *bvh, const vkg_ray *rays,
                    uint32_t n, vkg_hit *hits, uint32_t *occ, int cull, unsigned long long *counters,
-                   const uint32_t *perm)
+                   const uint32_t *perm, const uint32_t *reordered)
 {
     if(small_stack)
         k_trace<ANY, STATS, 64><<<grid, TRACE_THREADS, 0, st>>>(bvh->d_nodes, bvh->d_tris, rays, n, hits, occ, cull,
-                                                                counters, perm);
+                                                                counters, perm, reordered);
     else
-        k_trace<ANY, STATS, (int)TRAVERSAL_STACK><<<grid, TRACE_THREADS, 0, st>>>(bvh->d_nodes, bvh->d_tris, rays, n,
-                                                                                   hits, occ, cull, counters, perm);
+        k_trace<ANY, STATS, (int)TRAVERSAL_STACK><<<grid, TRACE_THREADS, 0, st>>>(
+                bvh->d_nodes, bvh->d_tris, rays, n, hits, occ, cull, counters, perm, reordered);
 }
 
 // ---- ray binning -------------------------------------------------------------------------------
@@ -245,9 +248,11 @@ __device__ __forceinline__ uint32_t ray_bin(float4 r0, float4 r1, float3 lo, flo
 }
 
 __global__ void __launch_bounds__(256)
-        k_bin_keys(const vkg_ray *__restrict__ rays, uint32_t n, float3 lo, float3 scale, uint16_t *__restrict__ bins)
+        k_bin_keys(const vkg_ray *__restrict__ rays, uint32_t n, float3 lo, float3 scale, uint16_t *__restrict__ bins,
+                   uint32_t *__restrict__ reordered)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i == 0) *reordered = 0u; // k_bin_tiles counts the tiles that do not keep their order
     if(i >= n) return;
     const float4 *rp = reinterpret_cast<const float4 *>(rays + i);
     bins[i] = (uint16_t)ray_bin(__ldg(rp), __ldg(rp + 1), lo, scale);
@@ -260,7 +265,7 @@ __global__ void __launch_bounds__(256)
 // ray takes its rank with its own atomic.
 __global__ void __launch_bounds__(BIN_THREADS)
         k_bin_tiles(const uint16_t *__restrict__ bins, uint32_t n, uint32_t tile, uint32_t *__restrict__ keys,
-                    uint32_t *__restrict__ M)
+                    uint32_t *__restrict__ M, uint32_t *__restrict__ reordered)
 {
     extern __shared__ uint32_t h[];
     __shared__ uint32_t uniform_steps;
@@ -308,6 +313,7 @@ __global__ void __launch_bounds__(BIN_THREADS)
         for(uint32_t b = threadIdx.x; b < BIN_SLOTS; b += BIN_THREADS) row[b] = h[b];
         return;
     }
+    if(threadIdx.x == 0) atomicAdd(reordered, 1u);
     uint32_t run_bin = 0xFFFFFFFFu, run_start = 0, run_len = 0;
     // a run's ranks: one atomic, then its keys
     auto flush = [&]() {
@@ -361,8 +367,11 @@ __global__ void __launch_bounds__(BIN_THREADS)
 
 // CTA = 32 bins (lanes) x 32 chunks of consecutive tiles (warps): chunk sums, their scan per bin in
 // shared memory, then the chunk's entries rewritten as the bin's running count before the tile
-__global__ void __launch_bounds__(1024) k_bin_columns(uint32_t *__restrict__ M, uint32_t tiles, uint32_t *__restrict__ S)
+__global__ void __launch_bounds__(1024)
+        k_bin_columns(uint32_t *__restrict__ M, uint32_t tiles, uint32_t *__restrict__ S,
+                      const uint32_t *__restrict__ reordered)
 {
+    if(*reordered == 0u) return; // every tile keeps its order: the batch is traced as given
     __shared__ uint32_t part[32][33];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t b = blockIdx.x * 32u + lane;
@@ -397,8 +406,10 @@ __global__ void __launch_bounds__(1024) k_bin_columns(uint32_t *__restrict__ M, 
 // F = exclusive scan of S, one CTA: S staged in shared memory (a pad word after every 32 keeps the
 // per-thread runs of 32 consecutive bins free of bank conflicts), 32 bins per thread
 constexpr size_t BIN_SCAN_SMEM = sizeof(uint32_t) * (NUM_BINS + NUM_BINS / 32);
-__global__ void __launch_bounds__(BIN_THREADS) k_bin_offsets(const uint32_t *__restrict__ S, uint32_t *__restrict__ F)
+__global__ void __launch_bounds__(BIN_THREADS)
+        k_bin_offsets(const uint32_t *__restrict__ S, uint32_t *__restrict__ F, const uint32_t *__restrict__ reordered)
 {
+    if(*reordered == 0u) return;
     extern __shared__ uint32_t sm[];
     __shared__ uint32_t warp_sum[32];
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
@@ -440,8 +451,9 @@ __global__ void __launch_bounds__(BIN_THREADS) k_bin_offsets(const uint32_t *__r
 
 __global__ void __launch_bounds__(256)
         k_bin_place(const uint32_t *__restrict__ keys, uint32_t n, uint32_t tile, const uint32_t *__restrict__ M,
-                    const uint32_t *__restrict__ F, uint32_t *__restrict__ perm)
+                    const uint32_t *__restrict__ F, uint32_t *__restrict__ perm, const uint32_t *__restrict__ reordered)
 {
+    if(*reordered == 0u) return;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= n) return;
     const uint32_t k = keys[i], bin = k & 0xFFFFu, t = i / tile;
@@ -500,11 +512,11 @@ const uint32_t *bin_rays(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays
         cudaFree(b.tile_counts);
         cudaFree(b.bin_totals);
         b = vkg_ctx::ray_bins{nullptr, nullptr, nullptr, nullptr, 0, 0, b.done};
-        // bin_totals: S, F
+        // bin_totals: S, F, the count of reordered tiles
         if(cudaMalloc(&b.keys, sizeof(uint32_t) * (size_t)n) != cudaSuccess ||
            cudaMalloc(&b.perm, sizeof(uint32_t) * (size_t)n) != cudaSuccess ||
            cudaMalloc(&b.tile_counts, sizeof(uint32_t) * (size_t)BIN_SLOTS * tiles) != cudaSuccess ||
-           cudaMalloc(&b.bin_totals, sizeof(uint32_t) * 2 * (size_t)BIN_SLOTS) != cudaSuccess)
+           cudaMalloc(&b.bin_totals, sizeof(uint32_t) * (2 * (size_t)BIN_SLOTS + 1)) != cudaSuccess)
         {
             cudaFree(b.keys);
             cudaFree(b.perm);
@@ -529,11 +541,12 @@ const uint32_t *bin_rays(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays
     // the 16-bit bins live in the first half of perm's storage until k_bin_place overwrites it
     // (k_bin_tiles reads them before; k_bin_place reads only keys)
     uint16_t *bins16 = reinterpret_cast<uint16_t *>(b.perm);
-    k_bin_keys<<<(n + 255) / 256, 256, 0, st>>>(d_rays, n, lo, scale, bins16);
-    k_bin_tiles<<<tiles, BIN_THREADS, BIN_SMEM, st>>>(bins16, n, tile, b.keys, b.tile_counts);
-    k_bin_columns<<<BIN_SLOTS / 32, 1024, 0, st>>>(b.tile_counts, tiles, S);
-    k_bin_offsets<<<1, BIN_THREADS, BIN_SCAN_SMEM, st>>>(S, F);
-    k_bin_place<<<(n + 255) / 256, 256, 0, st>>>(b.keys, n, tile, b.tile_counts, F, b.perm);
+    uint32_t *reordered = b.bin_totals + 2 * BIN_SLOTS;
+    k_bin_keys<<<(n + 255) / 256, 256, 0, st>>>(d_rays, n, lo, scale, bins16, reordered);
+    k_bin_tiles<<<tiles, BIN_THREADS, BIN_SMEM, st>>>(bins16, n, tile, b.keys, b.tile_counts, reordered);
+    k_bin_columns<<<BIN_SLOTS / 32, 1024, 0, st>>>(b.tile_counts, tiles, S, reordered);
+    k_bin_offsets<<<1, BIN_THREADS, BIN_SCAN_SMEM, st>>>(S, F, reordered);
+    k_bin_place<<<(n + 255) / 256, 256, 0, st>>>(b.keys, n, tile, b.tile_counts, F, b.perm, reordered);
     return b.perm;
 }
 
@@ -557,17 +570,19 @@ vkg_status launch_trace(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays,
     const int cull = (flags & VKG_RAY_CULL_BACK_FACES) ? 1 : 0;
     const bool stats = (flags & VKG_RAY_COUNT_STATS) != 0;
     const uint32_t *perm = bin_rays(ctx, bvh, d_rays, n, flags, st);
+    // device word: the number of tiles the binning reordered (0: trace in the given order)
+    const uint32_t *reordered = perm ? ctx->bins.bin_totals + 2 * BIN_SLOTS : nullptr;
     if(use_persistent())
     {
         if(d_occ)
         {
-            if(stats) launch_persistent<true, true>(ctx, bvh, d_rays, n, nullptr, d_occ, cull, st, perm);
-            else launch_persistent<true, false>(ctx, bvh, d_rays, n, nullptr, d_occ, cull, st, perm);
+            if(stats) launch_persistent<true, true>(ctx, bvh, d_rays, n, nullptr, d_occ, cull, st, perm, reordered);
+            else launch_persistent<true, false>(ctx, bvh, d_rays, n, nullptr, d_occ, cull, st, perm, reordered);
         }
         else
         {
-            if(stats) launch_persistent<false, true>(ctx, bvh, d_rays, n, d_hits, nullptr, cull, st, perm);
-            else launch_persistent<false, false>(ctx, bvh, d_rays, n, d_hits, nullptr, cull, st, perm);
+            if(stats) launch_persistent<false, true>(ctx, bvh, d_rays, n, d_hits, nullptr, cull, st, perm, reordered);
+            else launch_persistent<false, false>(ctx, bvh, d_rays, n, d_hits, nullptr, cull, st, perm, reordered);
         }
         if(perm) cudaEventRecord(ctx->bins.done, st);
         return cuda_check(ctx, cudaGetLastError(), "k_trace_persistent");
@@ -575,13 +590,13 @@ vkg_status launch_trace(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays,
     const bool small = bvh->depth <= 10;
     if(d_occ)
     {
-        if(stats) launch_simple<true, true>(small, grid, st, bvh, d_rays, n, nullptr, d_occ, cull, ctx->d_counters, perm);
-        else launch_simple<true, false>(small, grid, st, bvh, d_rays, n, nullptr, d_occ, cull, ctx->d_counters, perm);
+        if(stats) launch_simple<true, true>(small, grid, st, bvh, d_rays, n, nullptr, d_occ, cull, ctx->d_counters, perm, reordered);
+        else launch_simple<true, false>(small, grid, st, bvh, d_rays, n, nullptr, d_occ, cull, ctx->d_counters, perm, reordered);
     }
     else
     {
-        if(stats) launch_simple<false, true>(small, grid, st, bvh, d_rays, n, d_hits, nullptr, cull, ctx->d_counters, perm);
-        else launch_simple<false, false>(small, grid, st, bvh, d_rays, n, d_hits, nullptr, cull, ctx->d_counters, perm);
+        if(stats) launch_simple<false, true>(small, grid, st, bvh, d_rays, n, d_hits, nullptr, cull, ctx->d_counters, perm, reordered);
+        else launch_simple<false, false>(small, grid, st, bvh, d_rays, n, d_hits, nullptr, cull, ctx->d_counters, perm, reordered);
     }
     if(perm) cudaEventRecord(ctx->bins.done, st);
     return cuda_check(ctx, cudaGetLastError(), "k_trace");
