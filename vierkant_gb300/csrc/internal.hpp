@@ -103,6 +103,17 @@ vkg_status bind_device(vkg_ctx *ctx);
 
 // traversal stack capacity (entries) of the traversal kernels; the build rejects deeper BVHs
 constexpr uint32_t TRAVERSAL_STACK = 128;
+
+// Ray binning (traverse.cu): the order in which to trace the rays d_rays[0, n) -- or [0, *d_n) when
+// d_n is a device-side count <= n -- so that neighbouring threads follow similar paths through bvh:
+// perm[position] = ray, valid when *reordered_out (a device word) is non-zero; otherwise the rays
+// are to be traced as given. Returns nullptr (trace as given) for VKG_RAY_KEEP_ORDER, batches below
+// 2^19 rays, a stream being captured, or scratch that cannot be allocated. The scratch is the
+// context's; calls on different streams are ordered by an event recorded by bin_rays_done().
+const uint32_t *bin_rays(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t n, const uint32_t *d_n,
+                         uint32_t flags, cudaStream_t st, const uint32_t **reordered_out);
+// after the launch that reads the order: the scratch may be reused once the stream reaches here
+inline void bin_rays_done(vkg_ctx *ctx, cudaStream_t st) { cudaEventRecord(ctx->bins.done, st); }
 }// namespace vkg
 
 #define VKG_TRY_CUDA(ctx, expr)                                                                                      \

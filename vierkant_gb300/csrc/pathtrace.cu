@@ -991,11 +991,24 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
                 k_pt_tl_persistent<false><<<tl_grid, PT_THREADS, 0, st>>>(SS, t->q_ray[a], t->q_pid[a], cnt_in, t->hits,
                                                                          t->hit_inst, nullptr, nullptr, cnt_work);
             }
-            else if(small_stack)
-                k_pt_extend<single_scene, 64><<<grid, PT_THREADS, 0, st>>>(SS, t->q_ray[a], t->q_pid[a], cnt_in, t->hits,
-                                                                            t->hit_inst);
             else
-                k_pt_extend<<<grid, PT_THREADS, 0, st>>>(SS, t->q_ray[a], t->q_pid[a], cnt_in, t->hits, t->hit_inst);
+            {
+                // the first bounce's rays (the longest incoherent queue) are traced in bins of origin
+                // cell x direction; the camera rays of depth 0 are coherent as they are, and the later
+                // queues, shortened by Russian roulette and escapes, gain less than binning costs
+                // (720p 64 spp: 69.1 ms binning depth 1, 69.3 ms binning every depth >= 1, 71.0 ms none)
+                const uint32_t *reordered = nullptr;
+                const uint32_t *perm = (depth == 1 && !P.two_level)
+                                               ? bin_rays(ctx, sc->bvh, t->q_ray[a], n, cnt_in, 0u, st, &reordered)
+                                               : nullptr;
+                if(small_stack)
+                    k_pt_extend<single_scene, 64><<<grid, PT_THREADS, 0, st>>>(SS, t->q_ray[a], t->q_pid[a], cnt_in,
+                                                                                t->hits, t->hit_inst, perm, reordered);
+                else
+                    k_pt_extend<<<grid, PT_THREADS, 0, st>>>(SS, t->q_ray[a], t->q_pid[a], cnt_in, t->hits, t->hit_inst,
+                                                             perm, reordered);
+                if(perm) bin_rays_done(ctx, st);
+            }
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_out, 0, sizeof(uint32_t), st));
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_s, 0, sizeof(uint32_t), st));
             if(cnt_l) VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_l, 0, sizeof(uint32_t), st));

@@ -248,11 +248,12 @@ __device__ __forceinline__ uint32_t ray_bin(float4 r0, float4 r1, float3 lo, flo
 }
 
 __global__ void __launch_bounds__(256)
-        k_bin_keys(const vkg_ray *__restrict__ rays, uint32_t n, float3 lo, float3 scale, uint16_t *__restrict__ bins,
-                   uint32_t *__restrict__ reordered)
+        k_bin_keys(const vkg_ray *__restrict__ rays, uint32_t n_cap, const uint32_t *__restrict__ d_n, float3 lo,
+                   float3 scale, uint16_t *__restrict__ bins, uint32_t *__restrict__ reordered)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i == 0) *reordered = 0u; // k_bin_tiles counts the tiles that do not keep their order
+    const uint32_t n = d_n ? min(*d_n, n_cap) : n_cap;
     if(i >= n) return;
     const float4 *rp = reinterpret_cast<const float4 *>(rays + i);
     bins[i] = (uint16_t)ray_bin(__ldg(rp), __ldg(rp + 1), lo, scale);
@@ -264,16 +265,18 @@ __global__ void __launch_bounds__(256)
 // (all warps of a camera tile would otherwise queue on the same few counters). In other steps each
 // ray takes its rank with its own atomic.
 __global__ void __launch_bounds__(BIN_THREADS)
-        k_bin_tiles(const uint16_t *__restrict__ bins, uint32_t n, uint32_t tile, uint32_t *__restrict__ keys,
-                    uint32_t *__restrict__ M, uint32_t *__restrict__ reordered)
+        k_bin_tiles(const uint16_t *__restrict__ bins, uint32_t n_cap, const uint32_t *__restrict__ d_n, uint32_t tile,
+                    uint32_t *__restrict__ keys, uint32_t *__restrict__ M, uint32_t *__restrict__ reordered)
 {
+    const uint32_t n = d_n ? min(*d_n, n_cap) : n_cap;
     extern __shared__ uint32_t h[];
     __shared__ uint32_t uniform_steps;
     for(uint32_t b = threadIdx.x; b < BIN_SLOTS; b += BIN_THREADS) h[b] = 0u;
     if(threadIdx.x == 0) uniform_steps = 0u;
     __syncthreads();
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const uint32_t start = blockIdx.x * tile, end = min(start + tile, n);
+    // (tiles past a device-side count are empty: they keep their order and write a zero row)
+    const uint32_t start = blockIdx.x * tile, end = start < n ? min(start + tile, n) : start;
     const uint32_t per_warp = tile / 32u; // a multiple of 32
     const uint32_t w0 = start + warp * per_warp, w1 = min(w0 + per_warp, end);
     // a tile most of whose 32-ray steps fall into one bin each is coherent already (camera rays):
@@ -450,22 +453,88 @@ __global__ void __launch_bounds__(BIN_THREADS)
 }
 
 __global__ void __launch_bounds__(256)
-        k_bin_place(const uint32_t *__restrict__ keys, uint32_t n, uint32_t tile, const uint32_t *__restrict__ M,
-                    const uint32_t *__restrict__ F, uint32_t *__restrict__ perm, const uint32_t *__restrict__ reordered)
+        k_bin_place(const uint32_t *__restrict__ keys, uint32_t n_cap, const uint32_t *__restrict__ d_n, uint32_t tile,
+                    const uint32_t *__restrict__ M, const uint32_t *__restrict__ F, uint32_t *__restrict__ perm,
+                    const uint32_t *__restrict__ reordered)
 {
     if(*reordered == 0u) return;
+    const uint32_t n = d_n ? min(*d_n, n_cap) : n_cap;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= n) return;
     const uint32_t k = keys[i], bin = k & 0xFFFFu, t = i / tile;
     perm[__ldg(F + bin) + M[(size_t)t * BIN_SLOTS + bin] + (k >> 16)] = i;
 }
 
-// the traced order of a large batch (device pointer into the context's scratch), or nullptr to trace
-// in the given order
-const uint32_t *bin_rays(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t n,
-                         uint32_t flags, cudaStream_t st)
+
+__global__ void k_fill_miss(vkg_hit *hits, uint32_t *occluded, uint32_t n)
 {
-    if((flags & VKG_RAY_KEEP_ORDER) || n < BIN_MIN_RAYS) return nullptr;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n) return;
+    if(hits) reinterpret_cast<uint4 *>(hits)[i] = make_uint4(VKG_MISS, 0u, 0u, 0u);
+    if(occluded) occluded[i] = 0u;
+}
+
+vkg_status launch_trace(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t n, vkg_hit *d_hits,
+                        uint32_t *d_occ, uint32_t flags, cudaStream_t st)
+{
+    const uint32_t grid = (n + TRACE_THREADS - 1) / TRACE_THREADS;
+    if(bvh->num_tris == 0 || bvh->num_nodes == 0)
+    {
+        k_fill_miss<<<grid, TRACE_THREADS, 0, st>>>(d_hits, d_occ, n);
+        return cuda_check(ctx, cudaGetLastError(), "k_fill_miss");
+    }
+    const int cull = (flags & VKG_RAY_CULL_BACK_FACES) ? 1 : 0;
+    const bool stats = (flags & VKG_RAY_COUNT_STATS) != 0;
+    // reordered: device word, the number of tiles the binning reordered (0: trace in the given order)
+    const uint32_t *reordered = nullptr;
+    const uint32_t *perm = bin_rays(ctx, bvh, d_rays, n, nullptr, flags, st, &reordered);
+    if(use_persistent())
+    {
+        if(d_occ)
+        {
+            if(stats) launch_persistent<true, true>(ctx, bvh, d_rays, n, nullptr, d_occ, cull, st, perm, reordered);
+            else launch_persistent<true, false>(ctx, bvh, d_rays, n, nullptr, d_occ, cull, st, perm, reordered);
+        }
+        else
+        {
+            if(stats) launch_persistent<false, true>(ctx, bvh, d_rays, n, d_hits, nullptr, cull, st, perm, reordered);
+            else launch_persistent<false, false>(ctx, bvh, d_rays, n, d_hits, nullptr, cull, st, perm, reordered);
+        }
+        if(perm) bin_rays_done(ctx, st);
+        return cuda_check(ctx, cudaGetLastError(), "k_trace_persistent");
+    }
+    const bool small = bvh->depth <= 10;
+    if(d_occ)
+    {
+        if(stats) launch_simple<true, true>(small, grid, st, bvh, d_rays, n, nullptr, d_occ, cull, ctx->d_counters, perm, reordered);
+        else launch_simple<true, false>(small, grid, st, bvh, d_rays, n, nullptr, d_occ, cull, ctx->d_counters, perm, reordered);
+    }
+    else
+    {
+        if(stats) launch_simple<false, true>(small, grid, st, bvh, d_rays, n, d_hits, nullptr, cull, ctx->d_counters, perm, reordered);
+        else launch_simple<false, false>(small, grid, st, bvh, d_rays, n, d_hits, nullptr, cull, ctx->d_counters, perm, reordered);
+    }
+    if(perm) bin_rays_done(ctx, st);
+    return cuda_check(ctx, cudaGetLastError(), "k_trace");
+}
+
+vkg_status check_common(vkg_ctx *ctx, const vkg_bvh *bvh, const void *rays, const void *out, const char *fn)
+{
+    if(!ctx) return VKG_ERR_INVALID_ARGUMENT;
+    if(!bvh) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "%s: bvh is NULL", fn);
+    if(!rays || !out) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "%s: NULL ray or output buffer", fn);
+    if((reinterpret_cast<uintptr_t>(rays) & 15u) || (reinterpret_cast<uintptr_t>(out) & 3u))
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "%s: ray buffer must be 16-byte aligned", fn);
+    return bind_device(ctx);
+}
+
+}// namespace
+
+const uint32_t *bin_rays(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t n, const uint32_t *d_n,
+                         uint32_t flags, cudaStream_t st, const uint32_t **reordered_out)
+{
+    *reordered_out = nullptr;
+    if((flags & VKG_RAY_KEEP_ORDER) || n < BIN_MIN_RAYS || !bvh) return nullptr;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     if(cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
     {
@@ -542,77 +611,15 @@ const uint32_t *bin_rays(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays
     // (k_bin_tiles reads them before; k_bin_place reads only keys)
     uint16_t *bins16 = reinterpret_cast<uint16_t *>(b.perm);
     uint32_t *reordered = b.bin_totals + 2 * BIN_SLOTS;
-    k_bin_keys<<<(n + 255) / 256, 256, 0, st>>>(d_rays, n, lo, scale, bins16, reordered);
-    k_bin_tiles<<<tiles, BIN_THREADS, BIN_SMEM, st>>>(bins16, n, tile, b.keys, b.tile_counts, reordered);
+    k_bin_keys<<<(n + 255) / 256, 256, 0, st>>>(d_rays, n, d_n, lo, scale, bins16, reordered);
+    k_bin_tiles<<<tiles, BIN_THREADS, BIN_SMEM, st>>>(bins16, n, d_n, tile, b.keys, b.tile_counts, reordered);
     k_bin_columns<<<BIN_SLOTS / 32, 1024, 0, st>>>(b.tile_counts, tiles, S, reordered);
     k_bin_offsets<<<1, BIN_THREADS, BIN_SCAN_SMEM, st>>>(S, F, reordered);
-    k_bin_place<<<(n + 255) / 256, 256, 0, st>>>(b.keys, n, tile, b.tile_counts, F, b.perm, reordered);
+    k_bin_place<<<(n + 255) / 256, 256, 0, st>>>(b.keys, n, d_n, tile, b.tile_counts, F, b.perm, reordered);
+    *reordered_out = reordered;
     return b.perm;
 }
 
-__global__ void k_fill_miss(vkg_hit *hits, uint32_t *occluded, uint32_t n)
-{
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if(i >= n) return;
-    if(hits) reinterpret_cast<uint4 *>(hits)[i] = make_uint4(VKG_MISS, 0u, 0u, 0u);
-    if(occluded) occluded[i] = 0u;
-}
-
-vkg_status launch_trace(vkg_ctx *ctx, const vkg_bvh *bvh, const vkg_ray *d_rays, uint32_t n, vkg_hit *d_hits,
-                        uint32_t *d_occ, uint32_t flags, cudaStream_t st)
-{
-    const uint32_t grid = (n + TRACE_THREADS - 1) / TRACE_THREADS;
-    if(bvh->num_tris == 0 || bvh->num_nodes == 0)
-    {
-        k_fill_miss<<<grid, TRACE_THREADS, 0, st>>>(d_hits, d_occ, n);
-        return cuda_check(ctx, cudaGetLastError(), "k_fill_miss");
-    }
-    const int cull = (flags & VKG_RAY_CULL_BACK_FACES) ? 1 : 0;
-    const bool stats = (flags & VKG_RAY_COUNT_STATS) != 0;
-    const uint32_t *perm = bin_rays(ctx, bvh, d_rays, n, flags, st);
-    // device word: the number of tiles the binning reordered (0: trace in the given order)
-    const uint32_t *reordered = perm ? ctx->bins.bin_totals + 2 * BIN_SLOTS : nullptr;
-    if(use_persistent())
-    {
-        if(d_occ)
-        {
-            if(stats) launch_persistent<true, true>(ctx, bvh, d_rays, n, nullptr, d_occ, cull, st, perm, reordered);
-            else launch_persistent<true, false>(ctx, bvh, d_rays, n, nullptr, d_occ, cull, st, perm, reordered);
-        }
-        else
-        {
-            if(stats) launch_persistent<false, true>(ctx, bvh, d_rays, n, d_hits, nullptr, cull, st, perm, reordered);
-            else launch_persistent<false, false>(ctx, bvh, d_rays, n, d_hits, nullptr, cull, st, perm, reordered);
-        }
-        if(perm) cudaEventRecord(ctx->bins.done, st);
-        return cuda_check(ctx, cudaGetLastError(), "k_trace_persistent");
-    }
-    const bool small = bvh->depth <= 10;
-    if(d_occ)
-    {
-        if(stats) launch_simple<true, true>(small, grid, st, bvh, d_rays, n, nullptr, d_occ, cull, ctx->d_counters, perm, reordered);
-        else launch_simple<true, false>(small, grid, st, bvh, d_rays, n, nullptr, d_occ, cull, ctx->d_counters, perm, reordered);
-    }
-    else
-    {
-        if(stats) launch_simple<false, true>(small, grid, st, bvh, d_rays, n, d_hits, nullptr, cull, ctx->d_counters, perm, reordered);
-        else launch_simple<false, false>(small, grid, st, bvh, d_rays, n, d_hits, nullptr, cull, ctx->d_counters, perm, reordered);
-    }
-    if(perm) cudaEventRecord(ctx->bins.done, st);
-    return cuda_check(ctx, cudaGetLastError(), "k_trace");
-}
-
-vkg_status check_common(vkg_ctx *ctx, const vkg_bvh *bvh, const void *rays, const void *out, const char *fn)
-{
-    if(!ctx) return VKG_ERR_INVALID_ARGUMENT;
-    if(!bvh) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "%s: bvh is NULL", fn);
-    if(!rays || !out) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "%s: NULL ray or output buffer", fn);
-    if((reinterpret_cast<uintptr_t>(rays) & 15u) || (reinterpret_cast<uintptr_t>(out) & 3u))
-        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "%s: ray buffer must be 16-byte aligned", fn);
-    return bind_device(ctx);
-}
-
-}// namespace
 }// namespace vkg
 
 using namespace vkg;
