@@ -1040,12 +1040,22 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
                 k_pt_tl_persistent<true><<<tl_grid, PT_THREADS, 0, st>>>(SS, t->s_ray, t->s_pid, cnt_s, nullptr, nullptr,
                                                                         t->s_contrib, t->radiance, cnt_work);
             }
-            else if(!empty && small_stack)
-                k_pt_shadow<single_scene, 64><<<grid, PT_THREADS, 0, st>>>(SS, t->s_ray, t->s_pid, t->s_contrib, cnt_s,
-                                                                            t->radiance);
             else if(!empty)
-                k_pt_shadow<<<grid, PT_THREADS, 0, st>>>(SS, t->s_ray, t->s_pid, t->s_contrib, cnt_s,
-                                                         t->radiance);
+            {
+                // the first two environment-shadow queues of a plain render are traced in bins too
+                // (720p 64 spp: 68.5 -> 67.5 ms; the radiance-cache frames gain nothing from it)
+                const uint32_t *s_reordered = nullptr;
+                const uint32_t *s_perm = (mode == MODE_PLAIN && depth <= 1 && !P.two_level)
+                                                 ? bin_rays(ctx, sc->bvh, t->s_ray, n, cnt_s, 0u, st, &s_reordered)
+                                                 : nullptr;
+                if(small_stack)
+                    k_pt_shadow<single_scene, 64><<<grid, PT_THREADS, 0, st>>>(SS, t->s_ray, t->s_pid, t->s_contrib,
+                                                                                cnt_s, t->radiance, s_perm, s_reordered);
+                else
+                    k_pt_shadow<<<grid, PT_THREADS, 0, st>>>(SS, t->s_ray, t->s_pid, t->s_contrib, cnt_s, t->radiance,
+                                                             s_perm, s_reordered);
+                if(s_perm) bin_rays_done(ctx, st);
+            }
             if(cnt_l && !empty)
             {
                 if(small_stack)

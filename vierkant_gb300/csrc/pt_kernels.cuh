@@ -928,12 +928,16 @@ template<class J, int STACK = (int)TRAVERSAL_STACK>
 __global__ void __launch_bounds__(PT_THREADS, STACK <= 64 ? 8 : 6) // 64 / 85 registers
         k_pt_shadow(J S, const vkg_ray *__restrict__ s_ray, const uint32_t *__restrict__ s_pid,
                     const float4 *__restrict__ s_contrib, const uint32_t *__restrict__ count,
-                    float4 *__restrict__ radiance)
+                    float4 *__restrict__ radiance, const uint32_t *__restrict__ perm = nullptr,
+                    const uint32_t *__restrict__ reordered = nullptr)
 {
     const uint32_t n = *count;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    // a binned queue (bin_rays): position j tests entry perm[j] (each path has one entry per launch)
+    if(perm && *reordered == 0u) perm = nullptr;
+    for(uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride)
     {
+        const uint32_t i = perm ? __ldg(perm + j) : j;
         const pt_params &P = S.params(J::per_path ? s_pid[i] : 0u);
         const float4 *rp = reinterpret_cast<const float4 *>(s_ray + i);
         const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
