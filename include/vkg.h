@@ -440,6 +440,21 @@ vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_de
 /* the two-level BVH of an instanced scene (NULL for a single-level scene) */
 vkg_status vkg_scene_tlas(const vkg_scene *scene, const vkg_tlas **out);
 vkg_status vkg_scene_destroy(vkg_ctx *ctx, vkg_scene *scene);
+/* Vertex normals for smooth shading (interpolate_vertex, raypipeline.slang:336-360): the shading
+ * normal of a hit is the vertex normals interpolated with the barycentric weights (1 - u - v, u, v),
+ * normalised and turned to the side the ray hit; without them (the default) it is the face normal.
+ * mesh: 0 for a single-level scene, the mesh index of an instanced scene. d_src: device records at
+ * `stride` bytes (0: packed) of `format` -- VKG_NORMALS_FLOAT3 (3 floats, normalised on upload) or
+ * VKG_NORMALS_OCT_SNORM16 (the octahedral snorm16 pair of packed_vertex_t, packed_vertex.slang:17-23:
+ * pass the vertex buffer + 12 and stride 24); one record per vertex of the mesh; NULL removes them.
+ * Copied; waits for the device, then synchronises `stream`. */
+enum
+{
+    VKG_NORMALS_FLOAT3 = 0u,
+    VKG_NORMALS_OCT_SNORM16 = 1u
+};
+vkg_status vkg_scene_set_normals(vkg_ctx *ctx, vkg_scene *scene, uint32_t mesh, const void *d_src, uint32_t stride,
+                                 uint32_t format, void *stream);
 /* the scene's analytic lights (host array, copied; n = 0 removes them). Directions and tangents are
    normalised; the sun of the tracer settings comes first in the light list of a render. */
 vkg_status vkg_scene_set_lights(vkg_ctx *ctx, vkg_scene *scene, const vkg_light *lights, uint32_t n);
@@ -546,6 +561,9 @@ vkg_status vkg_gltf_load(const char *path, vkg_gltf **out, char *err, size_t err
 vkg_status vkg_gltf_counts_get(const vkg_gltf *g, vkg_gltf_counts *out);
 vkg_status vkg_gltf_mesh(const vkg_gltf *g, uint32_t index, const float **xyz, uint32_t *num_vertices,
                          const uint32_t **indices, uint32_t *num_tris);
+/* the mesh's vertex normals (3 floats per vertex, the primitive's NORMAL attribute) or NULL when the
+   primitive has none; for vkg_scene_set_normals */
+vkg_status vkg_gltf_mesh_normals(const vkg_gltf *g, uint32_t index, const float **normals);
 vkg_status vkg_gltf_instances(const vkg_gltf *g, vkg_instance *out);
 vkg_status vkg_gltf_materials(const vkg_gltf *g, vkg_material *out);
 vkg_status vkg_gltf_lights(const vkg_gltf *g, vkg_light *out);

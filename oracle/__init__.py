@@ -287,7 +287,13 @@ MATERIAL_DTYPE = np.dtype([("base_color", "<f4", 3), ("roughness", "<f4"), ("met
 
 class orc_pt_scene(C.Structure):
     _fields_ = [("xyz", C.c_void_p), ("idx", C.c_void_p), ("tri_mat", C.c_void_p), ("mats", C.c_void_p),
-                ("ntri", C.c_uint32), ("nmat", C.c_uint32)]
+                ("ntri", C.c_uint32), ("nmat", C.c_uint32), ("nrm", C.c_void_p)]
+
+
+def _normals(normals):
+    """unit vertex normals as the tracers store them: float32 [V, 3], each normalised in float32"""
+    n = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+    return np.ascontiguousarray(n / np.sqrt((n * n).sum(axis=1, dtype=np.float32))[:, None], np.float32)
 
 
 class orc_pt_env(C.Structure):
@@ -413,16 +419,18 @@ def env_tables_fp64(rgb):
 def pt_render(fp64, xyz, idx, tri_mat, mats, bvh: "CpuBVH", env_rgb, cam, spp, *, seed=0x5EED, batch=0, max_depth=6,
               rr_depth=3, mis_mode=0, crop=(0, 0, 0, 0), environment=1.0, draw_skybox=1, max_path_beta=0.0,
               alias_prob=None, alias=None, weight=None, cdf=None, nthreads=0, lights=None, suppress_caustics=False,
-              pixels=None, clip_near=0.1, camera_medium=None, camera_material=None):
+              pixels=None, clip_near=0.1, camera_medium=None, camera_material=None, normals=None):
     """Mean radiance per crop pixel ([h, w, 3] float64), mean squared luminance per pixel, (ext, shadow) rays.
     pixels: optional PIXEL_DTYPE array [h, w] of the crop, filled with the pixel records (radiance left 0)
-    the tracer writes."""
+    the tracer writes. normals: optional vertex normals [V, 3] (smooth shading)."""
     L = orc()
     L.orc_pt_render.argtypes = [C.c_int, C.POINTER(orc_pt_scene), C.POINTER(orc_bvh), C.POINTER(orc_pt_env),
                                 C.POINTER(orc_camera), C.POINTER(orc_pt_settings), C.c_void_p, C.c_void_p, C.c_void_p,
                                 C.c_int]
     keep = [np.ascontiguousarray(a) for a in (xyz, idx, tri_mat, mats)]
-    scene = orc_pt_scene(ptr(keep[0]), ptr(keep[1]), ptr(keep[2]), ptr(keep[3]), keep[1].shape[0], len(mats))
+    nrm = _normals(normals) if normals is not None else None
+    scene = orc_pt_scene(ptr(keep[0]), ptr(keep[1]), ptr(keep[2]), ptr(keep[3]), keep[1].shape[0], len(mats),
+                         ptr(nrm) if nrm is not None else None)
     rgb = np.ascontiguousarray(env_rgb, np.float32)
     h, w = rgb.shape[:2]
     if fp64 and (weight is None or cdf is None):
@@ -473,15 +481,15 @@ class orc_pt_instances(C.Structure):
     _fields_ = [("mesh_bvh", C.c_void_p), ("mesh_xyz", C.c_void_p), ("mesh_idx", C.c_void_p),
                 ("mesh_nvert", C.c_void_p), ("mesh_twosided", C.c_void_p), ("num_meshes", C.c_uint32),
                 ("o2w", C.c_void_p), ("inst_mesh", C.c_void_p), ("inst_mat", C.c_void_p),
-                ("num_instances", C.c_uint32)]
+                ("num_instances", C.c_uint32), ("mesh_nrm", C.c_void_p)]
 
 
 def pt_render_instanced(meshes, o2w, inst_mesh, inst_mat, mats, env_rgb, cam, spp, *, seed=0x5EED, batch=0,
                         max_depth=6, rr_depth=3, mis_mode=0, crop=(0, 0, 0, 0), environment=1.0, draw_skybox=1,
                         nthreads=0, mesh_bvhs=None, lights=None, suppress_caustics=False, camera_medium=None,
-                        camera_material=None):
+                        camera_material=None, mesh_normals=None):
     """FP64 oracle of an instanced scene: meshes [(xyz, idx, twosided)], o2w [N, 12] object -> world,
-    mesh and material index per instance. Returns (mean radiance [h, w, 3], mean squared luminance,
+    mesh and material index per instance; mesh_normals: optional per-mesh vertex normals (or None). Returns (mean radiance [h, w, 3], mean squared luminance,
     (ext, shadow) rays). camera_medium: medium_params(...) floats; camera_material: the material whose
     medium the camera sits in."""
     L = orc()
@@ -503,8 +511,14 @@ def pt_render_instanced(meshes, o2w, inst_mesh, inst_mat, mats, env_rgb, cam, sp
     imat = np.ascontiguousarray(inst_mat, np.uint32)
     mats = np.ascontiguousarray(mats)
     keep += [nvert, twos, o2w, im, imat, mats]
+    nrm_arr = None
+    if mesh_normals is not None:
+        nrms = [_normals(n) if n is not None else None for n in mesh_normals]
+        keep += [n for n in nrms if n is not None]
+        nrm_arr = (C.c_void_p * len(meshes))(*[n.ctypes.data if n is not None else None for n in nrms])
     inst = orc_pt_instances(C.cast(bvh_arr, C.c_void_p), C.cast(xyz_arr, C.c_void_p), C.cast(idx_arr, C.c_void_p),
-                            ptr(nvert), ptr(twos), len(meshes), ptr(o2w), ptr(im), ptr(imat), len(im))
+                            ptr(nvert), ptr(twos), len(meshes), ptr(o2w), ptr(im), ptr(imat), len(im),
+                            C.cast(nrm_arr, C.c_void_p) if nrm_arr is not None else None)
     scene = orc_pt_scene(None, None, None, ptr(mats), 0, len(mats))
     rgb = np.ascontiguousarray(env_rgb, np.float32)
     h, w = rgb.shape[:2]

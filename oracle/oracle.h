@@ -142,6 +142,7 @@ typedef struct {
     const uint32_t *tri_mat;
     const orc_pt_material *mats;
     uint32_t ntri, nmat;
+    const float *nrm; /* unit vertex normals (3 per vertex) for smooth shading, or NULL: face normals */
 } orc_pt_scene;
 
 typedef struct {
@@ -205,6 +206,7 @@ typedef struct {
     const float *o2w;        /* [num_instances][12] */
     const uint32_t *inst_mesh, *inst_mat;
     uint32_t num_instances;
+    const float *const *mesh_nrm; /* per mesh: unit vertex normals or NULL (the array itself may be NULL) */
 } orc_pt_instances;
 
 /* mean radiance per crop pixel over spp paths (out: crop_w*crop_h*3 doubles); stats[0] extension

@@ -15,7 +15,8 @@ def _pad4(b: bytes, fill=b"\x00") -> bytes:
 
 def write(path, meshes, nodes, scene_roots, materials=None, lights=None, mode="embedded", index_type=np.uint32,
           extra=None):
-    """meshes: [[(xyz [V,3], indices [T,3] or None, material or None, prim_mode or None), ...], ...];
+    """meshes: [[(xyz [V,3], indices [T,3] or None, material or None, prim_mode or None[, normals [V,3]]),
+    ...], ...];
     nodes: [dict(mesh=, children=, matrix=[16] | translation=, rotation=(x,y,z,w), scale=, light=)]"""
     blob = b""
     views, accessors = [], []
@@ -36,8 +37,12 @@ def write(path, meshes, nodes, scene_roots, materials=None, lights=None, mode="e
     gm = []
     for prims in meshes:
         ps = []
-        for xyz, idx, mat, pmode in prims:
+        for prim in prims:
+            xyz, idx, mat, pmode = prim[:4]
             p = {"attributes": {"POSITION": add(np.asarray(xyz, np.float32), 34962, "VEC3", 5126)}}
+            if len(prim) > 4 and prim[4] is not None:
+                nrm = np.asarray(prim[4], np.float32)
+                p["attributes"]["NORMAL"] = add(nrm, 34962, "VEC3" if nrm.shape[1] == 3 else "VEC2", 5126)
             if idx is not None:
                 ct = {np.uint32: 5125, np.uint16: 5123, np.uint8: 5121}[index_type]
                 p["indices"] = add(np.asarray(idx, index_type).reshape(-1), 34963, "SCALAR", ct)

@@ -186,3 +186,18 @@ def test_malformed_inputs_fail(tmp_path, kind):
         path.write_text("[" * 5000 + "]" * 5000)
     with pytest.raises(ValueError):
         load_gltf(str(path))
+
+
+def test_vertex_normals(tmp_path):
+    """NORMAL attributes are read per primitive (None without one); a NORMAL that is not VEC3 fails"""
+    n_quad = np.array([[0, 0, 1], [0, 0.6, 0.8], [0.6, 0, 0.8], [0, 0, 1]], np.float32)
+    path = tmp_path / "n.gltf"
+    write(path, [[(*QUAD, None, None, n_quad), (*TRI, None, None)]], [dict(mesh=0)], [0])
+    a = load_gltf(str(path))
+    assert np.array_equal(a["normals"][0], n_quad)
+    assert a["normals"][1] is None
+    bad = tmp_path / "bad.gltf"
+    write(bad, [[(*TRI, None, None, np.zeros((3, 2), np.float32))]], [dict(mesh=0)], [0])
+    with pytest.raises(ValueError, match="NORMAL"):
+        load_gltf(str(bad))
+

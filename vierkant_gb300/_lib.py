@@ -19,6 +19,8 @@ REJECT, INTERSECT, INSIDE = 0, 1, 2
 RAY_CULL_BACK_FACES = 1
 RAY_COUNT_STATS = 2
 RAY_KEEP_ORDER = 4
+NORMALS_FLOAT3 = 0
+NORMALS_OCT_SNORM16 = 1
 
 
 RNG_PCG32, RNG_REFERENCE = 0, 1
@@ -231,6 +233,7 @@ SIGNATURES = {
     "vkg_scene_create": (I32, [P, C.POINTER(vkg_scene_desc), C.POINTER(P), P]),
     "vkg_scene_destroy": (I32, [P, P]),
     "vkg_scene_set_lights": (I32, [P, P, P, U32]),
+    "vkg_scene_set_normals": (I32, [P, P, U32, P, U32, U32, P]),
     "vkg_tracer_pixel_data": (I32, [P, P, P]),
     "vkg_denoise": (I32, [P, P, U32, U32, P, P, P]),
     "vkg_post_fx_default": (I32, [C.POINTER(vkg_post_fx_settings)]),
@@ -238,6 +241,7 @@ SIGNATURES = {
     "vkg_gltf_counts_get": (I32, [P, C.POINTER(vkg_gltf_counts)]),
     "vkg_gltf_mesh": (I32, [P, U32, C.POINTER(C.POINTER(C.c_float)), C.POINTER(U32), C.POINTER(C.POINTER(U32)),
                             C.POINTER(U32)]),
+    "vkg_gltf_mesh_normals": (I32, [P, U32, C.POINTER(C.POINTER(C.c_float))]),
     "vkg_gltf_instances": (I32, [P, P]),
     "vkg_gltf_materials": (I32, [P, P]),
     "vkg_gltf_lights": (I32, [P, P]),

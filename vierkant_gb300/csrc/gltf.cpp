@@ -277,6 +277,7 @@ struct mesh_t
 {
     std::vector<float> xyz;
     std::vector<uint32_t> idx;
+    std::vector<float> nrm; // the primitive's NORMAL attribute (3 per vertex), empty when it has none
 };
 
 }// namespace
@@ -639,6 +640,17 @@ struct loader
                 mesh_t M;
                 M.xyz.assign(p.begin(), p.end());
                 const size_t nv = p.size() / 3;
+                // vertex normals (the reference's loader reads them into its vertices, gltf.cpp:
+                // NORMAL -> Vertex::normal) for smooth shading
+                if(const long na = attr->idx("NORMAL"); na >= 0)
+                {
+                    std::vector<double> nn;
+                    int nc = 0;
+                    if(!accessor(na, "NORMAL", nn, nc, true)) return false;
+                    if(nc != 3 || nn.size() != p.size())
+                        return fail("mesh %zu primitive %zu: NORMAL is not VEC3 per vertex", mi, pi);
+                    M.nrm.assign(nn.begin(), nn.end());
+                }
                 const long ia = pr.idx("indices");
                 if(ia >= 0)
                 {
@@ -823,6 +835,14 @@ vkg_status vkg_gltf_mesh(const vkg_gltf *g, uint32_t i, const float **xyz, uint3
     *num_vertices = (uint32_t)(M.xyz.size() / 3);
     *indices = M.idx.data();
     *num_tris = (uint32_t)(M.idx.size() / 3);
+    return VKG_OK;
+}
+
+vkg_status vkg_gltf_mesh_normals(const vkg_gltf *g, uint32_t i, const float **normals)
+{
+    if(!g || i >= g->meshes.size() || !normals) return VKG_ERR_INVALID_ARGUMENT;
+    const auto &M = g->meshes[i];
+    *normals = M.nrm.empty() ? nullptr : M.nrm.data();
     return VKG_OK;
 }
 

@@ -545,6 +545,79 @@ vkg_status vkg_scene_set_lights(vkg_ctx *ctx, vkg_scene *sc, const vkg_light *li
     return VKG_OK;
 }
 
+namespace vkg
+{
+namespace
+{
+// unit vertex normals from the caller's records: three floats, or the octahedral snorm16 pair of the
+// reference's packed_vertex_t (packed_vertex.slang:17-23, unpacked as utils::unpack does with
+// octahedral_map.slang:28-49)
+__global__ void k_vertex_normals(const uint8_t *__restrict__ src, uint32_t stride, uint32_t format, uint32_t n,
+                                 float *__restrict__ out)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if(k >= n) return;
+    const uint8_t *r = src + (size_t)k * stride;
+    float3 v;
+    if(format == VKG_NORMALS_OCT_SNORM16)
+    {
+        const float2 e = unpack_snorm_2x16(*reinterpret_cast<const uint32_t *>(r));
+        v = oct_decode(e.x, e.y);
+    }
+    else
+    {
+        const float *f = reinterpret_cast<const float *>(r);
+        v = normalize(f3(f[0], f[1], f[2]));
+    }
+    out[3 * (size_t)k] = v.x;
+    out[3 * (size_t)k + 1] = v.y;
+    out[3 * (size_t)k + 2] = v.z;
+}
+}// namespace
+}// namespace vkg
+
+extern "C" vkg_status vkg_scene_set_normals(vkg_ctx *ctx, vkg_scene *sc, uint32_t mesh, const void *d_src,
+                                            uint32_t stride, uint32_t format, void *stream)
+{
+    if(!ctx) return VKG_ERR_INVALID_ARGUMENT;
+    if(!sc) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_set_normals: NULL scene");
+    if(vkg_status s = bind_device(ctx); s != VKG_OK) return s;
+    const bool instanced = sc->bvh == nullptr; // an instanced scene has per-mesh BVHs instead
+    if(instanced ? mesh >= sc->mesh_nrm.size() : mesh != 0)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_set_normals: mesh %u out of range", mesh);
+    if(format != VKG_NORMALS_FLOAT3 && format != VKG_NORMALS_OCT_SNORM16)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_set_normals: unknown format %u", format);
+    const uint32_t min_stride = format == VKG_NORMALS_FLOAT3 ? 12u : 4u;
+    if(stride == 0) stride = min_stride;
+    if(stride < min_stride || stride % 4u || (reinterpret_cast<uintptr_t>(d_src) & 3u))
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
+                         "vkg_scene_set_normals: stride must be 0 or a multiple of 4 >= %u, the source 4-byte aligned",
+                         min_stride);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    float *&slot = instanced ? sc->mesh_nrm[mesh] : sc->nrm;
+    const uint32_t nv = instanced ? sc->mesh_vertices[mesh] : sc->num_vertices;
+    // the renders queued before keep reading the old array until they finish
+    VKG_TRY_CUDA(ctx, cudaStreamSynchronize(st));
+    VKG_TRY_CUDA(ctx, cudaDeviceSynchronize());
+    cudaFree(slot);
+    slot = nullptr;
+    if(d_src && nv)
+    {
+        VKG_TRY_CUDA(ctx, cudaMalloc(&slot, (size_t)nv * 3 * sizeof(float)));
+        k_vertex_normals<<<(nv + 255) / 256, 256, 0, st>>>(static_cast<const uint8_t *>(d_src), stride, format, nv,
+                                                           slot);
+        VKG_TRY_CUDA(ctx, cudaGetLastError());
+    }
+    if(instanced)
+    {
+        sc->h_meshes[mesh].nrm = slot;
+        VKG_TRY_CUDA(ctx, cudaMemcpyAsync(sc->d_meshes + mesh, &sc->h_meshes[mesh], sizeof(mesh_ref),
+                                          cudaMemcpyHostToDevice, st));
+    }
+    VKG_TRY_CUDA(ctx, cudaStreamSynchronize(st));
+    return VKG_OK;
+}
+
 vkg_status vkg_scene_destroy(vkg_ctx *ctx, vkg_scene *sc)
 {
     if(!sc) return VKG_OK;
@@ -554,7 +627,9 @@ vkg_status vkg_scene_destroy(vkg_ctx *ctx, vkg_scene *sc)
     for(vkg_bvh *b: sc->blas) vkg_bvh_destroy(ctx, b);
     for(float *p: sc->mesh_xyz) cudaFree(p);
     for(uint32_t *p: sc->mesh_idx) cudaFree(p);
+    for(float *p: sc->mesh_nrm) cudaFree(p);
     cudaFree(sc->d_meshes);
+    cudaFree(sc->nrm);
     cudaFree(sc->xyz);
     cudaFree(sc->idx);
     cudaFree(sc->tri_mat);
@@ -631,9 +706,12 @@ vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_de
         sc->blas.push_back(b);
         if(M.twosided && M.num_tris)
             k_set_tri_flags<<<(M.num_tris + 255) / 256, 256, 0, st>>>(b->d_tris, M.num_tris, TRI_FLAG_TWOSIDED);
-        refs[m] = mesh_ref{xyz, idx};
+        refs[m] = mesh_ref{xyz, idx, nullptr};
+        sc->mesh_nrm.push_back(nullptr);
+        sc->mesh_vertices.push_back(M.num_vertices);
         tris += M.num_tris;
     }
+    sc->h_meshes = refs;
     if(e == cudaSuccess && d->num_meshes)
     {
         chk(cudaMalloc(&sc->d_meshes, d->num_meshes * sizeof(mesh_ref)));

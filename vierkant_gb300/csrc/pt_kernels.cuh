@@ -24,6 +24,7 @@ struct mesh_ref
 {
     const float *xyz;
     const uint32_t *idx;
+    const float *nrm; // unit vertex normals (3 floats per vertex) or nullptr: shade with the face normal
 };
 }// namespace vkg
 
@@ -42,6 +43,10 @@ struct vkg_scene
     std::vector<vkg_bvh *> blas;
     std::vector<float *> mesh_xyz;
     std::vector<uint32_t *> mesh_idx;
+    std::vector<float *> mesh_nrm;       // per mesh: unit vertex normals or nullptr
+    std::vector<uint32_t> mesh_vertices; // per mesh: vertex count
+    std::vector<vkg::mesh_ref> h_meshes; // host copy of d_meshes
+    float *nrm = nullptr;                // single-level scenes: unit vertex normals or nullptr
     vkg::mesh_ref *d_meshes = nullptr;
     uint32_t num_instances = 0;
     bool any_transmissive = false;  // a material with transmission > 0 or a null surface (light shadow rays pass)
@@ -74,6 +79,7 @@ struct pt_params
     uint32_t two_level;
     const float *xyz;
     const uint32_t *idx;
+    const float *nrm; // unit vertex normals of a single-level scene, or nullptr (face normals)
     const uint32_t *tri_mat;
     const vkg_material *mats;
     env_view env;
@@ -302,12 +308,16 @@ __global__ void __launch_bounds__(PT_THREADS, STACK <= 64 ? 8 : 6) // 64 / 85 re
 
 // surface point, unit geometric normal (world space) and material of a hit: the triangle's vertices,
 // the barycentric point; for an instanced scene both moved to world space (point by the
-// object -> world transform, normal by the transpose of world -> object)
+// object -> world transform, normal by the transpose of world -> object). ns (when not null): the
+// unit shading normal, the vertex normals interpolated with the barycentric weights (1 - u - v, u, v)
+// and normalised as interpolate_vertex does (raypipeline.slang:336-360), moved like the face normal;
+// the face normal itself when the mesh has no vertex normals
 __device__ __forceinline__ void hit_surface(const pt_params &P, uint32_t prim, uint32_t inst, float bu, float bv,
-                                            float3 &p, float3 &ng, uint32_t &mat)
+                                            float3 &p, float3 &ng, uint32_t &mat, float3 *ns = nullptr)
 {
     const float *xyz = P.xyz;
     const uint32_t *idx = P.idx;
+    const float *nrm = P.nrm;
     const inst_rec *R = nullptr;
     if(P.two_level)
     {
@@ -315,6 +325,7 @@ __device__ __forceinline__ void hit_surface(const pt_params &P, uint32_t prim, u
         const mesh_ref M = P.meshes[__ldg(&R->blas)];
         xyz = M.xyz;
         idx = M.idx;
+        nrm = M.nrm;
     }
     const uint32_t i0 = __ldg(&idx[3 * (size_t)prim]), i1 = __ldg(&idx[3 * (size_t)prim + 1]),
                    i2 = __ldg(&idx[3 * (size_t)prim + 2]);
@@ -324,6 +335,15 @@ __device__ __forceinline__ void hit_surface(const pt_params &P, uint32_t prim, u
     const float3 e1 = v1 - v0, e2 = v2 - v0;
     p = v0 + e1 * bu + e2 * bv;
     float3 n = cross(e1, e2);
+    const bool smooth = ns && nrm;
+    float3 sn = f3(0.f, 0.f, 0.f);
+    if(smooth)
+    {
+        auto vn = [&](uint32_t k) {
+            return f3(__ldg(&nrm[3 * (size_t)k]), __ldg(&nrm[3 * (size_t)k + 1]), __ldg(&nrm[3 * (size_t)k + 2]));
+        };
+        sn = vn(i0) * (1.f - bu - bv) + vn(i1) * bu + vn(i2) * bv;
+    }
     if(R)
     {
         float o[12], w[12];
@@ -336,11 +356,15 @@ __device__ __forceinline__ void hit_surface(const pt_params &P, uint32_t prim, u
                o[8] * p.x + o[9] * p.y + o[10] * p.z + o[11]);
         n = f3(w[0] * n.x + w[4] * n.y + w[8] * n.z, w[1] * n.x + w[5] * n.y + w[9] * n.z,
                w[2] * n.x + w[6] * n.y + w[10] * n.z);
+        if(smooth)
+            sn = f3(w[0] * sn.x + w[4] * sn.y + w[8] * sn.z, w[1] * sn.x + w[5] * sn.y + w[9] * sn.z,
+                    w[2] * sn.x + w[6] * sn.y + w[10] * sn.z);
         mat = __ldg(&R->material);
     }
     else
         mat = __ldg(&P.tri_mat[prim]);
     ng = normalize(n);
+    if(ns) *ns = smooth ? normalize(sn) : ng;
 }
 
 // FULL = false: a scene without lights whose materials are metal-roughness only; the light terms and
@@ -646,12 +670,14 @@ __global__ void __launch_bounds__(PT_THREADS)
             }
             else
             {
-                float3 ng;
+                float3 ng, sn;
                 uint32_t mat;
                 hit_surface(P, h.x, P.two_level ? hit_inst[i] : 0u, __uint_as_float(h.z), __uint_as_float(h.w), P0,
-                            ng, mat);
+                            ng, mat, &sn);
+                // the side comes from the face (HitKind); the shading normal -- the interpolated vertex
+                // normal where the mesh has them -- is turned to that side (raypipeline.slang:359)
                 const bool back_face = !(dot(ng, dir) < 0.f);
-                N = back_face ? -ng : ng; // shading normal faces the incoming ray
+                N = back_face ? -sn : sn;
                 const float3 V = -dir;
                 // media: a boundary pushes its medium on a transmission through a front face and pops
                 // on one through a back face (raypipeline.slang:516-523, :656-664)
@@ -1414,6 +1440,7 @@ inline pt_params make_params(const vkg_scene *sc, const vkg_camera &cam, const v
         P.meshes = sc->d_meshes;
     }
     P.xyz = sc->xyz;
+    P.nrm = sc->nrm;
     P.idx = sc->idx;
     P.tri_mat = sc->tri_mat;
     P.mats = sc->mats;

@@ -61,6 +61,24 @@ def cornell_scene(seed: int = 0x5EED, stream: int = 2, num_spheres: int = 64, n:
     return {"xyz": xyz, "indices": idx, "tri_material": tm, "materials": mats}
 
 
+def cornell_vertex_normals(sc) -> np.ndarray:
+    """Vertex normals for smooth shading of a cornell_scene(): a sphere's vertices point away from its
+    centre (the mean of its vertices), the walls' vertices carry their face normal. float32 [V, 3]."""
+    xyz = np.asarray(sc["xyz"], np.float64)
+    idx = np.asarray(sc["indices"], np.int64)
+    tm = np.asarray(sc["tri_material"])
+    n = np.zeros_like(xyz)
+    fn = np.cross(xyz[idx[:, 1]] - xyz[idx[:, 0]], xyz[idx[:, 2]] - xyz[idx[:, 0]])
+    fn /= np.linalg.norm(fn, axis=1, keepdims=True)
+    wall = tm < 3
+    n[idx[wall].ravel()] = np.repeat(fn[wall], 3, axis=0)
+    for m in np.unique(tm[~wall]):
+        v = np.unique(idx[tm == m].ravel())
+        d = xyz[v] - xyz[v].mean(axis=0)
+        n[v] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    return n.astype(np.float32)
+
+
 SHOWCASE_KINDS = ("metal-rough", "glass", "rough glass", "clearcoat", "sheen", "diffuse transmission", "iridescent")
 
 

@@ -13,8 +13,9 @@ from .raytracing import INSTANCE_DTYPE
 
 def load_gltf(path: str) -> dict:
     """Reads a .gltf / .glb file. Returns dict(meshes=[(xyz [V,3] f32, indices [T,3] u32, twosided)],
-    instances (INSTANCE_DTYPE: object -> world, mesh index in "blas", material), materials
-    (MATERIAL_DTYPE), lights (pathtracer.LIGHT_DTYPE), skipped_primitives)."""
+    normals (per mesh: its NORMAL attribute [V,3] f32 or None), instances (INSTANCE_DTYPE: object ->
+    world, mesh index in "blas", material), materials (MATERIAL_DTYPE), lights
+    (pathtracer.LIGHT_DTYPE), skipped_primitives)."""
     from .pathtracer import LIGHT_DTYPE
     L = lib()
     h = C.c_void_p()
@@ -25,7 +26,7 @@ def load_gltf(path: str) -> dict:
     try:
         n = vkg_gltf_counts()
         check(L.vkg_gltf_counts_get(h, C.byref(n)))
-        meshes = []
+        meshes, normals = [], []
         for i in range(n.num_meshes):
             xp, ip = C.POINTER(C.c_float)(), C.POINTER(C.c_uint32)()
             nv, nt = C.c_uint32(), C.c_uint32()
@@ -33,23 +34,30 @@ def load_gltf(path: str) -> dict:
             xyz = np.ctypeslib.as_array(xp, (nv.value, 3)).copy() if nv.value else np.zeros((0, 3), np.float32)
             idx = np.ctypeslib.as_array(ip, (nt.value, 3)).copy() if nt.value else np.zeros((0, 3), np.uint32)
             meshes.append((xyz, idx, 0))
+            npp = C.POINTER(C.c_float)()
+            check(L.vkg_gltf_mesh_normals(h, i, C.byref(npp)))
+            normals.append(np.ctypeslib.as_array(npp, (nv.value, 3)).copy() if npp and nv.value else None)
         inst = np.zeros(n.num_instances, INSTANCE_DTYPE)
         check(L.vkg_gltf_instances(h, inst.ctypes.data_as(C.c_void_p) if n.num_instances else None))
         mats = np.zeros(n.num_materials, MATERIAL_DTYPE)
         check(L.vkg_gltf_materials(h, mats.ctypes.data_as(C.c_void_p)))
         lights = np.zeros(n.num_lights, LIGHT_DTYPE)
         check(L.vkg_gltf_lights(h, lights.ctypes.data_as(C.c_void_p) if n.num_lights else None))
-        return {"meshes": meshes, "instances": inst, "materials": mats, "lights": lights,
+        return {"meshes": meshes, "normals": normals, "instances": inst, "materials": mats, "lights": lights,
                 "skipped_primitives": n.skipped_primitives}
     finally:
         L.vkg_gltf_destroy(h)
 
 
 def scene_from_gltf(ctx, path: str, env_rgb):
-    """An InstancedScene of a glTF asset with its KHR_lights_punctual lights set."""
+    """An InstancedScene of a glTF asset with its KHR_lights_punctual lights and its meshes' vertex
+    normals (smooth shading) set."""
     from .pathtracer import InstancedScene
     a = load_gltf(path)
     scene = InstancedScene(ctx, a["meshes"], a["instances"], a["materials"], env_rgb)
+    for m, nrm in enumerate(a["normals"]):
+        if nrm is not None:
+            scene.set_normals(nrm, mesh=m)
     if len(a["lights"]):
         scene.set_lights(a["lights"])
     return scene

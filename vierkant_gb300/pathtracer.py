@@ -172,6 +172,25 @@ class _Lights:
               self.ctx.handle, "vkg_scene_set_lights")
 
 
+    def set_normals(self, normals, mesh: int = 0):
+        """Vertex normals for smooth shading (the interpolated vertex normal, turned to the side the
+        ray hit, becomes the shading normal): float [V, 3] (normalised on upload), PACKED_VERTEX_DTYPE
+        records (their octahedral normal words), or None for face normals. mesh: the mesh of an
+        instanced scene."""
+        from ._lib import NORMALS_FLOAT3, NORMALS_OCT_SNORM16
+        dev = f"cuda:{self.ctx.device}"
+        if normals is None:
+            src, stride, fmt = None, 0, NORMALS_FLOAT3
+        elif isinstance(normals, np.ndarray) and normals.dtype == PACKED_VERTEX_DTYPE:
+            buf = torch.from_numpy(np.ascontiguousarray(normals).view(np.uint8).copy()).to(dev)
+            src, stride, fmt = buf.data_ptr() + 12, PACKED_VERTEX_DTYPE.itemsize, NORMALS_OCT_SNORM16
+        else:
+            a = normals if isinstance(normals, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(normals, np.float32))
+            buf = a.to(dev, torch.float32).contiguous()
+            src, stride, fmt = buf.data_ptr(), 12, NORMALS_FLOAT3
+        check(lib().vkg_scene_set_normals(self.ctx.handle, self.handle, mesh, C.c_void_p(src), stride, fmt,
+                                          C.c_void_p(self.ctx.stream())), self.ctx.handle, "vkg_scene_set_normals")
+
 class Scene(_Lights):
     def __init__(self, ctx: Context, xyz, indices, tri_material, materials, env_rgb, leaf_max=2):
         dev = f"cuda:{ctx.device}"
