@@ -129,8 +129,16 @@ vkg_status vkg_geometry_icosphere(float radius, uint32_t tess, float *xyz, uint3
 /* Cornell box (5 quads over [-1,1]^3, open toward +z) + `num_spheres` cube-spheres of
  * 12 * n^2 triangles each with PCG32-drawn radius / centre / GGX material. Counts first, then
  * fill. per-triangle material id -> tri_material; materials: see vkg_material. */
-/* Disney material record (the reference's material_struct_t, RayBuilder.hpp:40-80, without textures). A triangle whose material has transmission > 0 or diffuse_transmission > 0
-   is never culled: rays leave such objects through their back faces. */
+/* Disney material record (the reference's material_struct_t, RayBuilder.hpp:40-116). A triangle whose material has transmission > 0 or diffuse_transmission > 0
+   is never culled: rays leave such objects through their back faces. Texture slots index the scene's
+   textures (vkg_scene_set_textures) or hold VKG_NO_TEXTURE; they take effect on meshes with texture
+   coordinates (vkg_scene_set_texcoords) as the reference's closest-hit shader applies them
+   (raypipeline.slang:526-606): colour multiplies base_color (rgb), emission multiplies a non-zero
+   emission or replaces a zero one (rgb), ao_rough_metal multiplies roughness (g) and metalness (b),
+   transmission multiplies transmission (r), diffuse_transmission multiplies diffuse_transmission (a),
+   diffuse_transmission_color multiplies diffuse_transmission_color (rgb); normal: a tangent-space
+   normal map (rg, needs tangents: vkg_scene_set_tangents). */
+#define VKG_NO_TEXTURE 0xFFFFFFFFu
 typedef struct vkg_material
 {
     float base_color[3];
@@ -164,8 +172,10 @@ typedef struct vkg_material
        wavelength (ior at the d-line); the first transmission locks the wavelength for the rest of the
        path and tints its throughput by the wavelength's colour (raypipeline.slang:481-491, :651-659) */
     float dispersion;
-    float pad;
-} vkg_material; /* 144 B */
+    uint32_t tex_color, tex_normal, tex_emission, tex_ao_rough_metal, tex_transmission;
+    uint32_t tex_diffuse_transmission, tex_diffuse_transmission_color;
+    uint32_t pad[2];
+} vkg_material; /* 176 B */
 /* ---- analytic lights ----------------------------------------------------------------------
  * The reference's LightType (punctual_light.hpp:20-34); AREA is reserved for emissive triangles and
  * rejected here, as the reference leaves it out of the light list (PBRPathTracer.cpp:633-634). */
@@ -455,6 +465,42 @@ enum
 };
 vkg_status vkg_scene_set_normals(vkg_ctx *ctx, vkg_scene *scene, uint32_t mesh, const void *d_src, uint32_t stride,
                                  uint32_t format, void *stream);
+/* Vertex tangents for normal maps (utils::Vertex::tangent): the same formats and rules as the normals;
+ * the bitangent is normalize(cross(normal, tangent)), negated for back faces (raypipeline.slang:545-549). */
+vkg_status vkg_scene_set_tangents(vkg_ctx *ctx, vkg_scene *scene, uint32_t mesh, const void *d_src, uint32_t stride,
+                                  uint32_t format, void *stream);
+/* Texture coordinates (utils::Vertex::tex_coord), interpolated with the barycentric weights:
+ * VKG_TEXCOORD_FLOAT2 (two floats) or VKG_TEXCOORD_HALF2 (two fp16, packed_vertex_t: vertex buffer + 20,
+ * stride 24) at `stride` bytes (0: packed); NULL removes them (textures are then not sampled). */
+enum
+{
+    VKG_TEXCOORD_FLOAT2 = 0u,
+    VKG_TEXCOORD_HALF2 = 1u
+};
+vkg_status vkg_scene_set_texcoords(vkg_ctx *ctx, vkg_scene *scene, uint32_t mesh, const void *d_src, uint32_t stride,
+                                   uint32_t format, void *stream);
+/* The scene's textures (replacing any before): RGBA8 texels read as UNORM (the reference's textures
+ * are R8G8B8A8_UNORM, model_loading.cpp:12-24), row-major from the host, copied. Each gets a full mip
+ * chain (level k + 1 = the rounded mean of 2 x 2 texels of level k, the last row / column repeated for
+ * odd sizes) and is sampled trilinearly at level lambda = lod_constant + log2(cone width) +
+ * 0.5 log2(width * height) - log2(|N.V|) (sample_texture_lod, lod_constant, raypipeline.slang:
+ * 299-320; the ray cone starts at width 0 with the camera's pixel spread angle and grows by spread x t
+ * after each surface, :113-114, :280-286, :608), lambda clamped to the chain; texel centres at
+ * (i + 0.5) / width; wrap per axis. */
+enum
+{
+    VKG_WRAP_REPEAT = 0u,
+    VKG_WRAP_CLAMP_TO_EDGE = 1u,
+    VKG_WRAP_MIRRORED_REPEAT = 2u
+};
+typedef struct vkg_texture_desc
+{
+    const uint8_t *h_rgba8; /* width * height * 4 bytes */
+    uint32_t width, height;
+    uint32_t wrap_s, wrap_t;
+} vkg_texture_desc;
+vkg_status vkg_scene_set_textures(vkg_ctx *ctx, vkg_scene *scene, const vkg_texture_desc *textures, uint32_t n,
+                                  void *stream);
 /* the scene's analytic lights (host array, copied; n = 0 removes them). Directions and tangents are
    normalised; the sun of the tracer settings comes first in the light list of a render. */
 vkg_status vkg_scene_set_lights(vkg_ctx *ctx, vkg_scene *scene, const vkg_light *lights, uint32_t n);
@@ -579,8 +625,11 @@ vkg_status vkg_gltf_destroy(vkg_gltf *g);
 /* material_struct_t -> vkg_material: colour rgb, emission rgb x emission.a (the emissive strength, as
    the closest-hit shader multiplies them), the scalar lobes, sheen colour rgb, iridescence strength /
    ior and the thickness range's maximum (what the shader reads), the media fields and two_sided.
-   Texture indices, blend mode and alpha cutoff have no counterpart and are dropped; *dropped (may
-   be NULL) counts the records that use any of them. Dispersion is read into vkg_material::dispersion. */
+   The texture slots take the index of each texture whose TextureTypeBits flag is set (colour, normal,
+   ao_rough_metal, emission, transmission, diffuse transmission and its colour; types.slang:35-51),
+   VKG_NO_TEXTURE otherwise. Blend mode / alpha cutoff and the textures the tracer does not sample
+   (displacement, thickness, clearcoat, sheen, iridescence) are dropped; *dropped (may be NULL)
+   counts the records that use any of them. Dispersion is read into vkg_material::dispersion. */
 vkg_status vkg_materials_from_wire(const void *records, uint32_t n, vkg_material *out, uint32_t *dropped);
 /* per entry: where its triangles are in the mesh buffers */
 typedef struct vkg_wire_entry_info

@@ -282,12 +282,63 @@ MATERIAL_DTYPE = np.dtype([("base_color", "<f4", 3), ("roughness", "<f4"), ("met
                            ("iridescence_ior", "<f4"), ("iridescence_thickness", "<f4"), ("attenuation_color", "<f4", 3),
                            ("attenuation_distance", "<f4"), ("scatter_color", "<f4", 3), ("scatter_factor", "<f4"),
                            ("phase_g", "<f4"), ("null_surface", "<u4"), ("dispersion", "<f4"),
-                           ("pad", "<f4")])
+                           ("tex_color", "<u4"), ("tex_normal", "<u4"), ("tex_emission", "<u4"),
+                           ("tex_ao_rough_metal", "<u4"), ("tex_transmission", "<u4"),
+                           ("tex_diffuse_transmission", "<u4"), ("tex_diffuse_transmission_color", "<u4"),
+                           ("pad", "<u4", 2)])
 
 
 class orc_pt_scene(C.Structure):
     _fields_ = [("xyz", C.c_void_p), ("idx", C.c_void_p), ("tri_mat", C.c_void_p), ("mats", C.c_void_p),
-                ("ntri", C.c_uint32), ("nmat", C.c_uint32), ("nrm", C.c_void_p)]
+                ("ntri", C.c_uint32), ("nmat", C.c_uint32), ("nrm", C.c_void_p), ("uv", C.c_void_p),
+                ("tng", C.c_void_p), ("tex", C.c_void_p), ("texels", C.c_void_p), ("ntex", C.c_uint32)]
+
+
+TEX_REC_DTYPE = np.dtype([("width", "<u4"), ("height", "<u4"), ("levels", "<u4"), ("wrap", "<u4"),
+                          ("offset", "<u4", 16)])
+
+
+def texture_pool(textures):
+    """Texture records (TEX_REC_DTYPE) and the RGBA8 texel array (uint32) of every level, as
+    vkg_scene_set_textures builds them: level k + 1 is the rounded mean (sum + 2) >> 2 of 2 x 2 texels
+    of level k, the last row / column repeated for odd sizes. textures: uint8 [H, W, 4] arrays or
+    (array, wrap_s, wrap_t) tuples."""
+    recs = np.zeros(len(textures), TEX_REC_DTYPE)
+    pool, total = [], 0
+    for k, t in enumerate(textures):
+        img, ws, wt = t if isinstance(t, tuple) else (t, 0, 0)
+        lvl = np.ascontiguousarray(img, np.uint8).astype(np.uint32)
+        h, w = lvl.shape[:2]
+        recs[k]["width"], recs[k]["height"], recs[k]["wrap"] = w, h, ws | (wt << 8)
+        n = 0
+        while True:
+            recs[k]["offset"][n] = total
+            words = lvl[..., 0] | (lvl[..., 1] << 8) | (lvl[..., 2] << 16) | (lvl[..., 3] << 24)
+            pool.append(words.reshape(-1).astype(np.uint32))
+            total += words.size
+            n += 1
+            if (w == 1 and h == 1) or n == 16:
+                break
+            pw, ph = w, h
+            w, h = max(1, w // 2), max(1, h // 2)
+            xs0 = np.minimum(2 * np.arange(w), pw - 1)
+            xs1 = np.minimum(2 * np.arange(w) + 1, pw - 1)
+            ys0 = np.minimum(2 * np.arange(h), ph - 1)
+            ys1 = np.minimum(2 * np.arange(h) + 1, ph - 1)
+            s = (lvl[ys0][:, xs0] + lvl[ys0][:, xs1] + lvl[ys1][:, xs0] + lvl[ys1][:, xs1] + 2) >> 2
+            lvl = s.astype(np.uint32)
+        recs[k]["levels"] = n
+    texels = np.concatenate(pool) if pool else np.zeros(1, np.uint32)
+    return recs, texels
+
+
+def tex_sample(recs, texels, k, u, v, lam):
+    """texture k sampled at (u, v), level lambda, by the oracle (FP64): RGBA floats"""
+    L = orc()
+    L.orc_tex_sample.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_void_p]
+    out = np.zeros(4, np.float64)
+    L.orc_tex_sample(recs[k:k + 1].ctypes.data, texels.ctypes.data, u, v, lam, out.ctypes.data)
+    return out
 
 
 def _normals(normals):
@@ -419,18 +470,26 @@ def env_tables_fp64(rgb):
 def pt_render(fp64, xyz, idx, tri_mat, mats, bvh: "CpuBVH", env_rgb, cam, spp, *, seed=0x5EED, batch=0, max_depth=6,
               rr_depth=3, mis_mode=0, crop=(0, 0, 0, 0), environment=1.0, draw_skybox=1, max_path_beta=0.0,
               alias_prob=None, alias=None, weight=None, cdf=None, nthreads=0, lights=None, suppress_caustics=False,
-              pixels=None, clip_near=0.1, camera_medium=None, camera_material=None, normals=None):
+              pixels=None, clip_near=0.1, camera_medium=None, camera_material=None, normals=None, uv=None,
+              tangents=None, textures=None):
     """Mean radiance per crop pixel ([h, w, 3] float64), mean squared luminance per pixel, (ext, shadow) rays.
     pixels: optional PIXEL_DTYPE array [h, w] of the crop, filled with the pixel records (radiance left 0)
-    the tracer writes. normals: optional vertex normals [V, 3] (smooth shading)."""
+    the tracer writes. normals / tangents / uv: optional vertex normals [V, 3] (smooth shading),
+    tangents [V, 3] and texture coordinates [V, 2]; textures: as texture_pool takes them."""
     L = orc()
     L.orc_pt_render.argtypes = [C.c_int, C.POINTER(orc_pt_scene), C.POINTER(orc_bvh), C.POINTER(orc_pt_env),
                                 C.POINTER(orc_camera), C.POINTER(orc_pt_settings), C.c_void_p, C.c_void_p, C.c_void_p,
                                 C.c_int]
     keep = [np.ascontiguousarray(a) for a in (xyz, idx, tri_mat, mats)]
     nrm = _normals(normals) if normals is not None else None
+    tng = _normals(tangents) if tangents is not None else None
+    tuv = np.ascontiguousarray(uv, np.float32) if uv is not None else None
+    recs, texels = texture_pool(textures) if textures else (None, None)
+    keep += [a for a in (nrm, tng, tuv, recs, texels) if a is not None]
     scene = orc_pt_scene(ptr(keep[0]), ptr(keep[1]), ptr(keep[2]), ptr(keep[3]), keep[1].shape[0], len(mats),
-                         ptr(nrm) if nrm is not None else None)
+                         ptr(nrm) if nrm is not None else None, ptr(tuv) if tuv is not None else None,
+                         ptr(tng) if tng is not None else None, ptr(recs) if recs is not None else None,
+                         ptr(texels) if texels is not None else None, len(recs) if recs is not None else 0)
     rgb = np.ascontiguousarray(env_rgb, np.float32)
     h, w = rgb.shape[:2]
     if fp64 and (weight is None or cdf is None):
@@ -481,7 +540,8 @@ class orc_pt_instances(C.Structure):
     _fields_ = [("mesh_bvh", C.c_void_p), ("mesh_xyz", C.c_void_p), ("mesh_idx", C.c_void_p),
                 ("mesh_nvert", C.c_void_p), ("mesh_twosided", C.c_void_p), ("num_meshes", C.c_uint32),
                 ("o2w", C.c_void_p), ("inst_mesh", C.c_void_p), ("inst_mat", C.c_void_p),
-                ("num_instances", C.c_uint32), ("mesh_nrm", C.c_void_p)]
+                ("num_instances", C.c_uint32), ("mesh_nrm", C.c_void_p), ("mesh_uv", C.c_void_p),
+                ("mesh_tng", C.c_void_p)]
 
 
 def pt_render_instanced(meshes, o2w, inst_mesh, inst_mat, mats, env_rgb, cam, spp, *, seed=0x5EED, batch=0,

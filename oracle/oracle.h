@@ -133,8 +133,18 @@ typedef struct {
     float attenuation_color[3], attenuation_distance, scatter_color[3], scatter_factor, phase_g;
     uint32_t null_surface;
     float dispersion; /* KHR_materials_dispersion: 20 / Abbe number (with transmission > 0) */
-    float pad;
-} orc_pt_material; /* same 144-byte layout as vkg_material */
+    uint32_t tex_color, tex_normal, tex_emission, tex_ao_rough_metal, tex_transmission;
+    uint32_t tex_diffuse_transmission, tex_diffuse_transmission_color; /* 0xFFFFFFFF: none */
+    uint32_t pad[2];
+} orc_pt_material; /* same 176-byte layout as vkg_material */
+
+/* a texture: size, level count, wrap modes (s: bits 0-7, t: bits 8-15; 0 repeat, 1 clamp to edge,
+   2 mirrored repeat) and the first texel of each level in the scene's RGBA8 texel array; the same
+   80-byte layout as the library's records */
+typedef struct {
+    uint32_t width, height, levels, wrap;
+    uint32_t offset[16];
+} orc_tex_rec;
 
 typedef struct {
     const float *xyz;
@@ -143,7 +153,14 @@ typedef struct {
     const orc_pt_material *mats;
     uint32_t ntri, nmat;
     const float *nrm; /* unit vertex normals (3 per vertex) for smooth shading, or NULL: face normals */
+    const float *uv;  /* texture coordinates (2 per vertex) or NULL */
+    const float *tng; /* unit vertex tangents (3 per vertex) or NULL */
+    const orc_tex_rec *tex; /* ntex textures over the RGBA8 texels (0: textures are not sampled) */
+    const uint32_t *texels;
+    uint32_t ntex;
 } orc_pt_scene;
+/* one trilinear texture sample (FP64), as the tracer samples textures */
+void orc_tex_sample(const orc_tex_rec *rec, const uint32_t *texels, double u, double v, double lambda, double out[4]);
 
 typedef struct {
     const float *rgb;        /* w*h*3 */
@@ -207,6 +224,8 @@ typedef struct {
     const uint32_t *inst_mesh, *inst_mat;
     uint32_t num_instances;
     const float *const *mesh_nrm; /* per mesh: unit vertex normals or NULL (the array itself may be NULL) */
+    const float *const *mesh_uv;  /* per mesh: texture coordinates or NULL (the array may be NULL) */
+    const float *const *mesh_tng; /* per mesh: unit tangents or NULL (the array may be NULL) */
 } orc_pt_instances;
 
 /* mean radiance per crop pixel over spp paths (out: crop_w*crop_h*3 doubles); stats[0] extension

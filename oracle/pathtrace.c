@@ -697,6 +697,9 @@ static void d_transmit_raw(const orc_pt_job *J, double ox, double oy, double oz,
 #define RASIN(x) asinf(x)
 #define REXP(x) expf(x)
 #define RLOG(x) logf(x)
+#define RLOG2(x) log2f(x)
+#define RFLOOR(x) floorf(x)
+#define RATAN(x) atanf(x)
 #include "pt_core.inc"
 #undef REAL
 #undef SFX
@@ -716,6 +719,9 @@ static void d_transmit_raw(const orc_pt_job *J, double ox, double oy, double oz,
 #undef RASIN
 #undef REXP
 #undef RLOG
+#undef RLOG2
+#undef RFLOOR
+#undef RATAN
 
 #define REAL double
 #define SFX(n) d_##n
@@ -735,6 +741,9 @@ static void d_transmit_raw(const orc_pt_job *J, double ox, double oy, double oz,
 #define RASIN(x) asin(x)
 #define REXP(x) exp(x)
 #define RLOG(x) log(x)
+#define RLOG2(x) log2(x)
+#define RFLOOR(x) floor(x)
+#define RATAN(x) atan(x)
 #include "pt_core.inc"
 
 void orc_sun_light(const float color[3], float intensity, const float spherical_coords[2], float angular_size,
@@ -1106,4 +1115,10 @@ void orc_pt_env_procedural(uint32_t w, uint32_t h, const float sun_dir[3], doubl
             size_t t = (size_t)j * w + i;
             rgb[3 * t] = rgb[3 * t + 1] = rgb[3 * t + 2] = (float)(sky + sun);
         }
+}
+
+/* one texture sample (FP64 restatement), for the sampling pins */
+void orc_tex_sample(const orc_tex_rec *rec, const uint32_t *texels, double u, double v, double lambda, double out[4])
+{
+    d_tsample(rec, texels, u, v, lambda, out);
 }

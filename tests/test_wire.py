@@ -54,10 +54,20 @@ def test_materials_from_wire():
     w["dispersion"] = 0.0
     w["null_surface"][1] = 1
     w["two_sided"][2] = 1
-    w["texture_type_flags"][3] = 0x1
+    w["texture_type_flags"][3] = 0x1 | 0x2 | 0x4 | 0x8 | 0x40 | 0x8000 | 0x10000
+    w["albedo_index"][3], w["normalmap_index"][3], w["emission_index"][3] = 7, 8, 9
+    w["ao_rough_metal_index"][3], w["transmission_index"][3] = 10, 11
+    w["diffuse_transmission_index"][3], w["diffuse_transmission_color_index"][3] = 12, 13
+    w["albedo_index"][2] = 5  # an index without its flag: no texture
+    w["texture_type_flags"][1] = 0x80  # a clearcoat texture: not sampled, counted as dropped
     w["dispersion"][4] = 0.2
     m, dropped = materials_from_wire(w.tobytes())
-    assert dropped == 1  # the texture flags; dispersion is read
+    assert dropped == 1  # the clearcoat texture; the sampled textures and dispersion are read
+    NO = 0xFFFFFFFF
+    assert [int(m[f][3]) for f in ("tex_color", "tex_normal", "tex_emission", "tex_ao_rough_metal",
+                                   "tex_transmission", "tex_diffuse_transmission",
+                                   "tex_diffuse_transmission_color")] == [7, 8, 9, 10, 11, 12, 13]
+    assert int(m["tex_color"][2]) == NO and int(m["tex_normal"][1]) == NO and int(m["tex_color"][0]) == NO
     assert np.array_equal(m["dispersion"], w["dispersion"])
     assert np.array_equal(m["base_color"], w["color"][:, :3])
     assert np.allclose(m["emission"], w["emission"][:, :3] * w["emission"][:, 3:4], rtol=1e-7, atol=0)

@@ -21,6 +21,10 @@ RAY_COUNT_STATS = 2
 RAY_KEEP_ORDER = 4
 NORMALS_FLOAT3 = 0
 NORMALS_OCT_SNORM16 = 1
+TEXCOORD_FLOAT2 = 0
+TEXCOORD_HALF2 = 1
+WRAP_REPEAT, WRAP_CLAMP_TO_EDGE, WRAP_MIRRORED_REPEAT = 0, 1, 2
+NO_TEXTURE = 0xFFFFFFFF
 
 
 RNG_PCG32, RNG_REFERENCE = 0, 1
@@ -57,7 +61,15 @@ class vkg_material(C.Structure):
                 ("iridescence_ior", C.c_float), ("iridescence_thickness", C.c_float),
                 ("attenuation_color", C.c_float * 3), ("attenuation_distance", C.c_float),
                 ("scatter_color", C.c_float * 3), ("scatter_factor", C.c_float), ("phase_g", C.c_float),
-                ("null_surface", C.c_uint32), ("dispersion", C.c_float), ("pad", C.c_float)]
+                ("null_surface", C.c_uint32), ("dispersion", C.c_float), ("tex_color", C.c_uint32),
+                ("tex_normal", C.c_uint32), ("tex_emission", C.c_uint32), ("tex_ao_rough_metal", C.c_uint32),
+                ("tex_transmission", C.c_uint32), ("tex_diffuse_transmission", C.c_uint32),
+                ("tex_diffuse_transmission_color", C.c_uint32), ("pad", C.c_uint32 * 2)]
+
+
+class vkg_texture_desc(C.Structure):
+    _fields_ = [("h_rgba8", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("wrap_s", C.c_uint32),
+                ("wrap_t", C.c_uint32)]
 
 
 class vkg_camera(C.Structure):
@@ -234,6 +246,9 @@ SIGNATURES = {
     "vkg_scene_destroy": (I32, [P, P]),
     "vkg_scene_set_lights": (I32, [P, P, P, U32]),
     "vkg_scene_set_normals": (I32, [P, P, U32, P, U32, U32, P]),
+    "vkg_scene_set_tangents": (I32, [P, P, U32, P, U32, U32, P]),
+    "vkg_scene_set_texcoords": (I32, [P, P, U32, P, U32, U32, P]),
+    "vkg_scene_set_textures": (I32, [P, P, P, U32, P]),
     "vkg_tracer_pixel_data": (I32, [P, P, P]),
     "vkg_denoise": (I32, [P, P, U32, U32, P, P, P]),
     "vkg_post_fx_default": (I32, [C.POINTER(vkg_post_fx_settings)]),

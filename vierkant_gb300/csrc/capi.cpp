@@ -728,6 +728,8 @@ vkg_status vkg_material_defaults(vkg_material *m)
     m->iridescence_thickness = 400.f;
     for(int c = 0; c < 3; ++c) m->attenuation_color[c] = m->scatter_color[c] = 1.f;
     m->attenuation_distance = std::numeric_limits<float>::infinity();
+    m->tex_color = m->tex_normal = m->tex_emission = m->tex_ao_rough_metal = m->tex_transmission = VKG_NO_TEXTURE;
+    m->tex_diffuse_transmission = m->tex_diffuse_transmission_color = VKG_NO_TEXTURE;
     return VKG_OK;
 }
 

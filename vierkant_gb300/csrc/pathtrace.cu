@@ -72,6 +72,8 @@ struct vkg_tracer
     uint32_t *bins = nullptr;       // class counts [0..7] and fill cursors [8..15]
     uint4 *mstack = nullptr;        // per-path medium stacks (scenes with media)
     size_t mstack_cap = 0;
+    float *cone = nullptr;          // per-path ray-cone widths (scenes with textures)
+    size_t cone_cap = 0;
     uint32_t *counters = nullptr;           // [0..1] queue lengths, [2] shadow queue length, [3] cache queries,
                                             // [4] training records, [5] training batch length, [6] work
                                             // counter, [7] light shadow queue length
@@ -549,17 +551,40 @@ namespace vkg
 {
 namespace
 {
-// unit vertex normals from the caller's records: three floats, or the octahedral snorm16 pair of the
-// reference's packed_vertex_t (packed_vertex.slang:17-23, unpacked as utils::unpack does with
-// octahedral_map.slang:28-49)
-__global__ void k_vertex_normals(const uint8_t *__restrict__ src, uint32_t stride, uint32_t format, uint32_t n,
-                                 float *__restrict__ out)
+// per-vertex attributes from the caller's records: unit vectors from three floats or from the
+// octahedral snorm16 pair of the reference's packed_vertex_t (packed_vertex.slang:17-23, unpacked
+// as utils::unpack does with octahedral_map.slang:28-49); texture coordinates from two floats or
+// two fp16
+enum attr_kind : uint32_t
+{
+    ATTR_UNIT_F32X3,
+    ATTR_UNIT_OCT16,
+    ATTR_UV_F32X2,
+    ATTR_UV_F16X2
+};
+
+__global__ void k_vertex_attr(const uint8_t *__restrict__ src, uint32_t stride, uint32_t kind, uint32_t n,
+                              float *__restrict__ out)
 {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if(k >= n) return;
     const uint8_t *r = src + (size_t)k * stride;
+    if(kind == ATTR_UV_F32X2 || kind == ATTR_UV_F16X2)
+    {
+        float2 t;
+        if(kind == ATTR_UV_F16X2)
+        {
+            const __half2 h = *reinterpret_cast<const __half2 *>(r);
+            t = __half22float2(h);
+        }
+        else
+            t = make_float2(reinterpret_cast<const float *>(r)[0], reinterpret_cast<const float *>(r)[1]);
+        out[2 * (size_t)k] = t.x;
+        out[2 * (size_t)k + 1] = t.y;
+        return;
+    }
     float3 v;
-    if(format == VKG_NORMALS_OCT_SNORM16)
+    if(kind == ATTR_UNIT_OCT16)
     {
         const float2 e = unpack_snorm_2x16(*reinterpret_cast<const uint32_t *>(r));
         v = oct_decode(e.x, e.y);
@@ -573,48 +598,173 @@ __global__ void k_vertex_normals(const uint8_t *__restrict__ src, uint32_t strid
     out[3 * (size_t)k + 1] = v.y;
     out[3 * (size_t)k + 2] = v.z;
 }
+
+// which attribute a setter fills: the single-level slot and the per-mesh slots
+enum attr_slot
+{
+    SLOT_NORMAL,
+    SLOT_TANGENT,
+    SLOT_UV
+};
+
+vkg_status set_vertex_attr(vkg_ctx *ctx, vkg_scene *sc, uint32_t mesh, const void *d_src, uint32_t stride,
+                           uint32_t format, attr_slot slot, const char *fn, void *stream)
+{
+    if(!ctx) return VKG_ERR_INVALID_ARGUMENT;
+    if(!sc) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "%s: NULL scene", fn);
+    if(vkg_status s = bind_device(ctx); s != VKG_OK) return s;
+    const bool instanced = sc->bvh == nullptr; // an instanced scene has per-mesh BVHs instead
+    if(instanced ? mesh >= sc->mesh_nrm.size() : mesh != 0)
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "%s: mesh %u out of range", fn, mesh);
+    uint32_t kind, comps, min_stride;
+    if(slot == SLOT_UV)
+    {
+        if(format != VKG_TEXCOORD_FLOAT2 && format != VKG_TEXCOORD_HALF2)
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "%s: unknown format %u", fn, format);
+        kind = format == VKG_TEXCOORD_FLOAT2 ? ATTR_UV_F32X2 : ATTR_UV_F16X2;
+        comps = 2;
+        min_stride = format == VKG_TEXCOORD_FLOAT2 ? 8u : 4u;
+    }
+    else
+    {
+        if(format != VKG_NORMALS_FLOAT3 && format != VKG_NORMALS_OCT_SNORM16)
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "%s: unknown format %u", fn, format);
+        kind = format == VKG_NORMALS_FLOAT3 ? ATTR_UNIT_F32X3 : ATTR_UNIT_OCT16;
+        comps = 3;
+        min_stride = format == VKG_NORMALS_FLOAT3 ? 12u : 4u;
+    }
+    if(stride == 0) stride = min_stride;
+    if(stride < min_stride || stride % 4u || (reinterpret_cast<uintptr_t>(d_src) & 3u))
+        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
+                         "%s: stride must be 0 or a multiple of 4 >= %u, the source 4-byte aligned", fn, min_stride);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    std::vector<float *> &per_mesh = slot == SLOT_NORMAL ? sc->mesh_nrm : slot == SLOT_TANGENT ? sc->mesh_tng : sc->mesh_uv;
+    float *&single = slot == SLOT_NORMAL ? sc->nrm : slot == SLOT_TANGENT ? sc->tng : sc->uv;
+    float *&ptr = instanced ? per_mesh[mesh] : single;
+    const uint32_t nv = instanced ? sc->mesh_vertices[mesh] : sc->num_vertices;
+    // the renders queued before keep reading the old array until they finish
+    VKG_TRY_CUDA(ctx, cudaStreamSynchronize(st));
+    VKG_TRY_CUDA(ctx, cudaDeviceSynchronize());
+    cudaFree(ptr);
+    ptr = nullptr;
+    if(d_src && nv)
+    {
+        VKG_TRY_CUDA(ctx, cudaMalloc(&ptr, (size_t)nv * comps * sizeof(float)));
+        k_vertex_attr<<<(nv + 255) / 256, 256, 0, st>>>(static_cast<const uint8_t *>(d_src), stride, kind, nv, ptr);
+        VKG_TRY_CUDA(ctx, cudaGetLastError());
+    }
+    if(instanced)
+    {
+        mesh_ref &r = sc->h_meshes[mesh];
+        (slot == SLOT_NORMAL ? r.nrm : slot == SLOT_TANGENT ? r.tng : r.uv) = ptr;
+        VKG_TRY_CUDA(ctx, cudaMemcpyAsync(sc->d_meshes + mesh, &r, sizeof(mesh_ref), cudaMemcpyHostToDevice, st));
+    }
+    VKG_TRY_CUDA(ctx, cudaStreamSynchronize(st));
+    return VKG_OK;
+}
 }// namespace
 }// namespace vkg
 
 extern "C" vkg_status vkg_scene_set_normals(vkg_ctx *ctx, vkg_scene *sc, uint32_t mesh, const void *d_src,
                                             uint32_t stride, uint32_t format, void *stream)
 {
+    return set_vertex_attr(ctx, sc, mesh, d_src, stride, format, SLOT_NORMAL, "vkg_scene_set_normals", stream);
+}
+
+extern "C" vkg_status vkg_scene_set_tangents(vkg_ctx *ctx, vkg_scene *sc, uint32_t mesh, const void *d_src,
+                                             uint32_t stride, uint32_t format, void *stream)
+{
+    return set_vertex_attr(ctx, sc, mesh, d_src, stride, format, SLOT_TANGENT, "vkg_scene_set_tangents", stream);
+}
+
+extern "C" vkg_status vkg_scene_set_texcoords(vkg_ctx *ctx, vkg_scene *sc, uint32_t mesh, const void *d_src,
+                                              uint32_t stride, uint32_t format, void *stream)
+{
+    return set_vertex_attr(ctx, sc, mesh, d_src, stride, format, SLOT_UV, "vkg_scene_set_texcoords", stream);
+}
+
+extern "C" vkg_status vkg_scene_set_textures(vkg_ctx *ctx, vkg_scene *sc, const vkg_texture_desc *textures, uint32_t n,
+                                             void *stream)
+{
     if(!ctx) return VKG_ERR_INVALID_ARGUMENT;
-    if(!sc) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_set_normals: NULL scene");
+    if(!sc || (n && !textures)) return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_set_textures: NULL argument");
     if(vkg_status s = bind_device(ctx); s != VKG_OK) return s;
-    const bool instanced = sc->bvh == nullptr; // an instanced scene has per-mesh BVHs instead
-    if(instanced ? mesh >= sc->mesh_nrm.size() : mesh != 0)
-        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_set_normals: mesh %u out of range", mesh);
-    if(format != VKG_NORMALS_FLOAT3 && format != VKG_NORMALS_OCT_SNORM16)
-        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_set_normals: unknown format %u", format);
-    const uint32_t min_stride = format == VKG_NORMALS_FLOAT3 ? 12u : 4u;
-    if(stride == 0) stride = min_stride;
-    if(stride < min_stride || stride % 4u || (reinterpret_cast<uintptr_t>(d_src) & 3u))
-        return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
-                         "vkg_scene_set_normals: stride must be 0 or a multiple of 4 >= %u, the source 4-byte aligned",
-                         min_stride);
+    // records and every level on the host: level k + 1 = rounded mean of 2 x 2 texels of level k
+    // (the last row / column repeated for odd sizes)
+    std::vector<tex_rec> recs(n);
+    std::vector<uint32_t> texels;
+    for(uint32_t i = 0; i < n; ++i)
+    {
+        const vkg_texture_desc &d = textures[i];
+        if(!d.h_rgba8 || d.width == 0 || d.height == 0 || d.width > 32768 || d.height > 32768)
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_set_textures: texture %u: empty or larger than 32768", i);
+        if(d.wrap_s > VKG_WRAP_MIRRORED_REPEAT || d.wrap_t > VKG_WRAP_MIRRORED_REPEAT)
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT, "vkg_scene_set_textures: texture %u: unknown wrap mode", i);
+        tex_rec &r = recs[i];
+        r = tex_rec{};
+        r.width = d.width;
+        r.height = d.height;
+        r.wrap = d.wrap_s | (d.wrap_t << 8);
+        uint32_t w = d.width, h = d.height, levels = 1;
+        while((w > 1 || h > 1) && levels < TEX_MAX_LEVELS)
+        {
+            w = std::max(1u, w / 2);
+            h = std::max(1u, h / 2);
+            ++levels;
+        }
+        r.levels = levels;
+        if(texels.size() + (size_t)d.width * d.height * 2 > 0xFFFFFFFFull)
+            return set_error(ctx, VKG_ERR_CAPACITY, "vkg_scene_set_textures: more than 2^32 texels");
+        r.offset[0] = (uint32_t)texels.size();
+        const uint8_t *src = d.h_rgba8;
+        for(size_t k = 0; k < (size_t)d.width * d.height; ++k)
+            texels.push_back((uint32_t)src[4 * k] | ((uint32_t)src[4 * k + 1] << 8) | ((uint32_t)src[4 * k + 2] << 16) |
+                             ((uint32_t)src[4 * k + 3] << 24));
+        w = d.width;
+        h = d.height;
+        for(uint32_t l = 1; l < levels; ++l)
+        {
+            const uint32_t pw = w, ph = h, pbase = r.offset[l - 1];
+            w = std::max(1u, w / 2);
+            h = std::max(1u, h / 2);
+            r.offset[l] = (uint32_t)texels.size();
+            for(uint32_t y = 0; y < h; ++y)
+                for(uint32_t x = 0; x < w; ++x)
+                {
+                    const uint32_t x0 = std::min(2 * x, pw - 1), x1 = std::min(2 * x + 1, pw - 1);
+                    const uint32_t y0 = std::min(2 * y, ph - 1), y1 = std::min(2 * y + 1, ph - 1);
+                    const uint32_t a = texels[pbase + y0 * pw + x0], b = texels[pbase + y0 * pw + x1];
+                    const uint32_t c = texels[pbase + y1 * pw + x0], e = texels[pbase + y1 * pw + x1];
+                    uint32_t out = 0;
+                    for(int ch = 0; ch < 4; ++ch)
+                    {
+                        const uint32_t sh = 8u * (uint32_t)ch;
+                        const uint32_t sum = ((a >> sh) & 0xFFu) + ((b >> sh) & 0xFFu) + ((c >> sh) & 0xFFu) +
+                                             ((e >> sh) & 0xFFu);
+                        out |= ((sum + 2u) >> 2) << sh;
+                    }
+                    texels.push_back(out);
+                }
+        }
+    }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    float *&slot = instanced ? sc->mesh_nrm[mesh] : sc->nrm;
-    const uint32_t nv = instanced ? sc->mesh_vertices[mesh] : sc->num_vertices;
-    // the renders queued before keep reading the old array until they finish
     VKG_TRY_CUDA(ctx, cudaStreamSynchronize(st));
     VKG_TRY_CUDA(ctx, cudaDeviceSynchronize());
-    cudaFree(slot);
-    slot = nullptr;
-    if(d_src && nv)
+    cudaFree(sc->d_tex);
+    cudaFree(sc->d_texels);
+    sc->d_tex = nullptr;
+    sc->d_texels = nullptr;
+    sc->num_textures = 0;
+    if(n)
     {
-        VKG_TRY_CUDA(ctx, cudaMalloc(&slot, (size_t)nv * 3 * sizeof(float)));
-        k_vertex_normals<<<(nv + 255) / 256, 256, 0, st>>>(static_cast<const uint8_t *>(d_src), stride, format, nv,
-                                                           slot);
-        VKG_TRY_CUDA(ctx, cudaGetLastError());
-    }
-    if(instanced)
-    {
-        sc->h_meshes[mesh].nrm = slot;
-        VKG_TRY_CUDA(ctx, cudaMemcpyAsync(sc->d_meshes + mesh, &sc->h_meshes[mesh], sizeof(mesh_ref),
+        VKG_TRY_CUDA(ctx, cudaMalloc(&sc->d_tex, n * sizeof(tex_rec)));
+        VKG_TRY_CUDA(ctx, cudaMalloc(&sc->d_texels, texels.size() * sizeof(uint32_t)));
+        VKG_TRY_CUDA(ctx, cudaMemcpyAsync(sc->d_tex, recs.data(), n * sizeof(tex_rec), cudaMemcpyHostToDevice, st));
+        VKG_TRY_CUDA(ctx, cudaMemcpyAsync(sc->d_texels, texels.data(), texels.size() * sizeof(uint32_t),
                                           cudaMemcpyHostToDevice, st));
+        VKG_TRY_CUDA(ctx, cudaStreamSynchronize(st));
+        sc->num_textures = n;
     }
-    VKG_TRY_CUDA(ctx, cudaStreamSynchronize(st));
     return VKG_OK;
 }
 
@@ -628,8 +778,14 @@ vkg_status vkg_scene_destroy(vkg_ctx *ctx, vkg_scene *sc)
     for(float *p: sc->mesh_xyz) cudaFree(p);
     for(uint32_t *p: sc->mesh_idx) cudaFree(p);
     for(float *p: sc->mesh_nrm) cudaFree(p);
+    for(float *p: sc->mesh_uv) cudaFree(p);
+    for(float *p: sc->mesh_tng) cudaFree(p);
     cudaFree(sc->d_meshes);
     cudaFree(sc->nrm);
+    cudaFree(sc->uv);
+    cudaFree(sc->tng);
+    cudaFree(sc->d_tex);
+    cudaFree(sc->d_texels);
     cudaFree(sc->xyz);
     cudaFree(sc->idx);
     cudaFree(sc->tri_mat);
@@ -706,8 +862,10 @@ vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_de
         sc->blas.push_back(b);
         if(M.twosided && M.num_tris)
             k_set_tri_flags<<<(M.num_tris + 255) / 256, 256, 0, st>>>(b->d_tris, M.num_tris, TRI_FLAG_TWOSIDED);
-        refs[m] = mesh_ref{xyz, idx, nullptr};
+        refs[m] = mesh_ref{xyz, idx, nullptr, nullptr, nullptr};
         sc->mesh_nrm.push_back(nullptr);
+        sc->mesh_uv.push_back(nullptr);
+        sc->mesh_tng.push_back(nullptr);
         sc->mesh_vertices.push_back(M.num_vertices);
         tris += M.num_tris;
     }
@@ -1016,6 +1174,18 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
         }
         P.mstack = t->mstack;
     }
+    if(sc->num_textures)
+    {
+        if(t->cone_cap < paths + train_paths)
+        {
+            cudaFree(t->cone);
+            t->cone = nullptr;
+            t->cone_cap = 0;
+            VKG_TRY_CUDA(ctx, cudaMalloc(&t->cone, (paths + train_paths) * sizeof(float)));
+            t->cone_cap = paths + train_paths;
+        }
+        P.cone = t->cone;
+    }
     P.term_depth = cache_render ? ccfg->terminate_depth : 0xFFFFFFFFu;
     P.rec_depth = rec_depth;
     P.train_paths = train_paths;
@@ -1256,7 +1426,7 @@ vkg_status vkg_tracer_destroy(vkg_tracer *t)
     tracer_free_cache_buffers(t);
     cudaFree(t->counters);
     for(void *p: {(void *)t->d_lights, (void *)t->l_ray, (void *)t->l_pid, (void *)t->l_contrib, (void *)t->mstack,
-                  (void *)t->d_media_cam, (void *)t->ref_chain, (void *)t->ref_offset})
+                  (void *)t->d_media_cam, (void *)t->ref_chain, (void *)t->ref_offset, (void *)t->cone})
         cudaFree(p);
     cudaFree(t->totals);
     if(t->ev0) cudaEventDestroy(t->ev0);

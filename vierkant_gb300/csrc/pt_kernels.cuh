@@ -10,6 +10,7 @@
 #include "medium.cuh"
 #include "pathtrace.cuh"
 #include "pixel.cuh"
+#include "texture.cuh"
 #include "tlas.cuh"
 #include "traverse.cuh"
 
@@ -25,6 +26,8 @@ struct mesh_ref
     const float *xyz;
     const uint32_t *idx;
     const float *nrm; // unit vertex normals (3 floats per vertex) or nullptr: shade with the face normal
+    const float *uv;  // texture coordinates (2 floats per vertex) or nullptr: no textures
+    const float *tng; // unit vertex tangents (3 floats per vertex) or nullptr: no normal maps
 };
 }// namespace vkg
 
@@ -46,7 +49,12 @@ struct vkg_scene
     std::vector<float *> mesh_nrm;       // per mesh: unit vertex normals or nullptr
     std::vector<uint32_t> mesh_vertices; // per mesh: vertex count
     std::vector<vkg::mesh_ref> h_meshes; // host copy of d_meshes
+    std::vector<float *> mesh_uv, mesh_tng;
     float *nrm = nullptr;                // single-level scenes: unit vertex normals or nullptr
+    float *uv = nullptr, *tng = nullptr; // single-level scenes: texture coordinates, tangents
+    vkg::tex_rec *d_tex = nullptr;       // textures: records and all their levels' RGBA8 texels
+    uint32_t *d_texels = nullptr;
+    uint32_t num_textures = 0;
     vkg::mesh_ref *d_meshes = nullptr;
     uint32_t num_instances = 0;
     bool any_transmissive = false;  // a material with transmission > 0 or a null surface (light shadow rays pass)
@@ -80,6 +88,14 @@ struct pt_params
     const float *xyz;
     const uint32_t *idx;
     const float *nrm; // unit vertex normals of a single-level scene, or nullptr (face normals)
+    const float *uv, *tng; // texture coordinates / tangents of a single-level scene, or nullptr
+    // textures (num_textures 0: none) and the per-path ray-cone widths (nullptr: textures are not
+    // sampled); cone_spread: the camera's pixel spread angle (raypipeline.slang:102)
+    const tex_rec *tex;
+    const uint32_t *texels;
+    uint32_t num_textures;
+    float cone_spread;
+    float *cone;
     const uint32_t *tri_mat;
     const vkg_material *mats;
     env_view env;
@@ -266,6 +282,7 @@ __global__ void __launch_bounds__(PT_THREADS)
         rng[p] = g.state;
         beta_pdf[p] = make_float4(1.f, 1.f, 1.f, 0.f);
         radiance[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if(P.cone) P.cone[p] = 0.f; // the ray cone starts at width 0 (raypipeline.slang:112-114)
         // the camera's medium seeds the stack (raypipeline.slang:128-135)
         if(P.mstack)
             P.mstack[p] = P.cam_medium != 0xFFFFFFFFu ? make_uint4(1u, P.cam_medium, 0u, 0u) : make_uint4(0u, 0u, 0u, 0u);
@@ -369,6 +386,119 @@ __device__ __forceinline__ void hit_surface(const pt_params &P, uint32_t prim, u
 
 // FULL = false: a scene without lights whose materials are metal-roughness only; the light terms and
 // the other lobes compile away. MEDIA = true (with FULL): the homogeneous-media terms
+// texture coordinates of a hit (the vertices' interpolated with the barycentric weights), the
+// triangle's texture-LOD constant 0.5 log2(uv area / world area) (lod_constant,
+// raypipeline.slang:299-310; the world area after the instance's object -> world transform) and,
+// when asked for and present, the unit tangent (interpolated, moved by the object -> world
+// transform). false: the mesh has no texture coordinates.
+__device__ __forceinline__ bool hit_texcoords(const pt_params &P, uint32_t prim, uint32_t inst, float bu, float bv,
+                                              bool want_tangent, float2 &uv, float &lod, float3 &tangent, bool &has_tangent)
+{
+    const float *xyz = P.xyz, *tuv = P.uv, *tng = P.tng;
+    const uint32_t *idx = P.idx;
+    const inst_rec *R = nullptr;
+    if(P.two_level)
+    {
+        R = P.tl_by_id + inst;
+        const mesh_ref M = P.meshes[__ldg(&R->blas)];
+        xyz = M.xyz;
+        idx = M.idx;
+        tuv = M.uv;
+        tng = M.tng;
+    }
+    if(!tuv) return false;
+    const uint32_t i0 = __ldg(&idx[3 * (size_t)prim]), i1 = __ldg(&idx[3 * (size_t)prim + 1]),
+                   i2 = __ldg(&idx[3 * (size_t)prim + 2]);
+    auto vtx = [&](uint32_t k) {
+        return f3(__ldg(&xyz[3 * (size_t)k]), __ldg(&xyz[3 * (size_t)k + 1]), __ldg(&xyz[3 * (size_t)k + 2]));
+    };
+    const float2 t0 = make_float2(__ldg(&tuv[2 * (size_t)i0]), __ldg(&tuv[2 * (size_t)i0 + 1]));
+    const float2 t1 = make_float2(__ldg(&tuv[2 * (size_t)i1]), __ldg(&tuv[2 * (size_t)i1 + 1]));
+    const float2 t2 = make_float2(__ldg(&tuv[2 * (size_t)i2]), __ldg(&tuv[2 * (size_t)i2 + 1]));
+    const float w0 = 1.f - bu - bv;
+    uv = make_float2(t0.x * w0 + t1.x * bu + t2.x * bv, t0.y * w0 + t1.y * bu + t2.y * bv);
+    const float3 v0 = vtx(i0);
+    float3 e1 = vtx(i1) - v0, e2 = vtx(i2) - v0;
+    float3 T = f3(0.f, 0.f, 0.f);
+    has_tangent = want_tangent && tng != nullptr;
+    if(has_tangent)
+    {
+        auto tv = [&](uint32_t k) {
+            return f3(__ldg(&tng[3 * (size_t)k]), __ldg(&tng[3 * (size_t)k + 1]), __ldg(&tng[3 * (size_t)k + 2]));
+        };
+        T = tv(i0) * w0 + tv(i1) * bu + tv(i2) * bv;
+    }
+    if(R)
+    {
+        float o[9];
+        for(int r = 0; r < 3; ++r)
+            for(int c = 0; c < 3; ++c) o[3 * r + c] = __ldg(&R->o2w[4 * r + c]);
+        auto lin = [&](float3 a) {
+            return f3(o[0] * a.x + o[1] * a.y + o[2] * a.z, o[3] * a.x + o[4] * a.y + o[5] * a.z,
+                      o[6] * a.x + o[7] * a.y + o[8] * a.z);
+        };
+        e1 = lin(e1);
+        e2 = lin(e2);
+        if(has_tangent) T = lin(T);
+    }
+    const float3 c = cross(e1, e2);
+    const float p_a = sqrtf(dot(c, c));
+    const float t_a = fabsf((t1.x - t0.x) * (t2.y - t0.y) - (t2.x - t0.x) * (t1.y - t0.y));
+    lod = 0.5f * log2f(t_a / p_a);
+    if(has_tangent) tangent = normalize(T);
+    return true;
+}
+
+// the material's textures at a surface hit (raypipeline.slang:526-606): every sample at level
+// lod + log2|cone width| + 0.5 log2(w h) - log2|N.V| (sample_texture_lod, :312-320) with N the
+// shading normal before the normal map; base colour, normal map (tangent frame (T, +-B, N),
+// B = normalize(N x T) negated for back faces, hemisphere clamp), emission, roughness / metalness,
+// transmission and the diffuse-transmission terms
+__device__ __forceinline__ void apply_textures(const pt_params &P, const vkg_material &q, float2 uv, float lod,
+                                               float cone_w, float3 V, bool back_face, bool has_tangent,
+                                               float3 tangent, material_view &m, float3 &emit, float3 &N)
+{
+    const float base_lambda = lod + log2f(fabsf(cone_w)) - log2f(fabsf(dot(V, N)));
+    auto ok = [&](uint32_t t) { return t < P.num_textures; };
+    auto S = [&](uint32_t t) {
+        const tex_rec &T = P.tex[t];
+        return tex_sample(T, P.texels, uv.x, uv.y, base_lambda + 0.5f * log2f((float)T.width * (float)T.height));
+    };
+    if(ok(q.tex_color) && !P.disable_material)
+    {
+        const float4 c = S(q.tex_color);
+        m.base = m.base * f3(c.x, c.y, c.z);
+    }
+    if(ok(q.tex_normal) && has_tangent)
+    {
+        const float4 t = S(q.tex_normal);
+        const float nx = 2.f * (t.x - 0.5f), ny = 2.f * (t.y - 0.5f);
+        const float nz = sqrtf(fmaxf(0.f, 1.f - nx * nx - ny * ny));
+        const float3 b = normalize(cross(N, tangent));
+        const float3 n = normalize(tangent * nx + (back_face ? -b : b) * ny + N * nz);
+        N = normalize(n + N * fmaxf(0.f, -dot(n, N) + 1e-3f));
+    }
+    if(ok(q.tex_emission))
+    {
+        const float4 e = S(q.tex_emission);
+        const float3 te = f3(e.x, e.y, e.z);
+        emit = (emit.x > 0.f || emit.y > 0.f || emit.z > 0.f) ? emit * te : te;
+    }
+    if(ok(q.tex_ao_rough_metal))
+    {
+        const float4 a = S(q.tex_ao_rough_metal);
+        m.roughness *= a.y;
+        m.metalness *= a.z;
+    }
+    if(ok(q.tex_transmission)) m.transmission *= S(q.tex_transmission).x;
+    if(ok(q.tex_diffuse_transmission)) m.diffuse_transmission *= S(q.tex_diffuse_transmission).w;
+    if(ok(q.tex_diffuse_transmission_color))
+    {
+        const float4 c = S(q.tex_diffuse_transmission_color);
+        m.dt_color = m.dt_color * f3(c.x, c.y, c.z);
+    }
+}
+
 // material classes of a queue entry for shading coherence: 0 miss, then by the costliest lobe the
 // material takes (thin film, dielectric, medium boundary / null surface, clearcoat, sheen, diffuse
 // transmission, metal-roughness only)
@@ -713,6 +843,26 @@ __global__ void __launch_bounds__(PT_THREADS)
                 }
                 {
                 material_view m = load_material<FULL>(P.mats, mat, P.disable_material);
+                const float *em = P.mats[mat].emission;
+                float3 emit = f3(em[0], em[1], em[2]);
+                if(P.cone)
+                {
+                    // textures sampled with the ray cone as it reached this surface, which then grows
+                    // by the segment (propagate with no surface spread, raypipeline.slang:608)
+                    const float cone_w = P.cone[pid];
+                    const vkg_material &q = P.mats[mat];
+                    const bool want_t = q.tex_normal < P.num_textures;
+                    float2 tuv;
+                    float lod;
+                    float3 tangent;
+                    bool has_t = false;
+                    if((q.tex_color & q.tex_normal & q.tex_emission & q.tex_ao_rough_metal & q.tex_transmission &
+                        q.tex_diffuse_transmission & q.tex_diffuse_transmission_color) != VKG_NO_TEXTURE &&
+                       hit_texcoords(P, h.x, P.two_level ? hit_inst[i] : 0u, __uint_as_float(h.z),
+                                     __uint_as_float(h.w), want_t, tuv, lod, tangent, has_t))
+                        apply_textures(P, q, tuv, lod, cone_w, V, back_face, has_t, tangent, m, emit, N);
+                    P.cone[pid] = cone_w + P.cone_spread * __uint_as_float(h.y);
+                }
                 // path regularisation (raypipeline.slang:611): after a non-peaked bounce, later vertices
                 // shade (sample and NEE) with roughness >= 0.25
                 if(flags & PATH_REGULARIZE) m.roughness = fmaxf(m.roughness, PT_REGULARIZE_MIN_ROUGHNESS);
@@ -737,8 +887,7 @@ __global__ void __launch_bounds__(PT_THREADS)
                     eta = (back_face ? ior / stack_ior(P.media, mst, mst.x ? mst.x - 1 : 0)
                                      : stack_ior(P.media, mst, mst.x) / ior) + PT_EPS;
                 }
-                const float *em = P.mats[mat].emission;
-                L = L + beta * f3(em[0], em[1], em[2]);
+                L = L + beta * emit;
                 if(depth == 0 && P.gbuf && pid < P.train_base)
                 {
                     vkg_pixel_data &px = P.gbuf[pid % P.npix];
@@ -1441,6 +1590,13 @@ inline pt_params make_params(const vkg_scene *sc, const vkg_camera &cam, const v
     }
     P.xyz = sc->xyz;
     P.nrm = sc->nrm;
+    P.uv = sc->uv;
+    P.tng = sc->tng;
+    P.tex = sc->d_tex;
+    P.texels = sc->d_texels;
+    P.num_textures = sc->num_textures;
+    P.cone_spread = atanf(2.f * cam.tan_half_fovy / (float)cam.height);
+    P.cone = nullptr;
     P.idx = sc->idx;
     P.tri_mat = sc->tri_mat;
     P.mats = sc->mats;

@@ -18,10 +18,21 @@ constexpr size_t color = 0, emission = 16, metalness = 32, roughness = 36, trans
 constexpr size_t attenuation_color = 48, attenuation_distance = 60, ior = 64, clearcoat = 68,
                  clearcoat_roughness = 72, sheen_roughness = 76, sheen_color = 80;
 constexpr size_t iridescence_strength = 96, iridescence_ior = 100, iridescence_thickness_range = 104;
-constexpr size_t albedo_index = 112, texture_type_flags = 132, blend_mode = 136, two_sided = 144,
+constexpr size_t albedo_index = 112, normalmap_index = 116, emission_index = 120, ao_rough_metal_index = 124,
+                 transmission_index = 128, texture_type_flags = 132, blend_mode = 136, two_sided = 144,
                  phase_g = 148, scatter_factor = 152, dispersion = 156, scatter_color = 160,
-                 diffuse_transmission = 172, diffuse_transmission_color = 176;
+                 diffuse_transmission = 172, diffuse_transmission_color = 176, diffuse_transmission_index = 188,
+                 diffuse_transmission_color_index = 192;
 }// namespace mat_off
+
+// TextureTypeBits (shaders/slang/ray/types.slang:35-51) of the textures the tracer samples
+namespace tex_bit
+{
+constexpr uint32_t color = 0x001, normal = 0x002, ao_rough_metal = 0x004, emission = 0x008, transmission = 0x040,
+                   diffuse_transmission = 0x8000, diffuse_transmission_color = 0x10000;
+constexpr uint32_t sampled = color | normal | ao_rough_metal | emission | transmission | diffuse_transmission |
+                             diffuse_transmission_color;
+}// namespace tex_bit
 
 // byte offsets in RayBuilder::entry_t
 namespace entry_off
@@ -82,7 +93,21 @@ vkg_status vkg_materials_from_wire(const void *records, uint32_t n, vkg_material
         m.diffuse_transmission = rd<float>(r, mat_off::diffuse_transmission);
         rd3(r, mat_off::diffuse_transmission_color, m.diffuse_transmission_color);
         m.dispersion = rd<float>(r, mat_off::dispersion);
-        bool unused = rd<uint32_t>(r, mat_off::texture_type_flags) != 0 || rd<uint32_t>(r, mat_off::blend_mode) != 0;
+        // texture slots: the index where its TextureTypeBits flag is set (an index into the scene's
+        // textures, vkg_scene_set_textures, as into the reference's u_textures)
+        const uint32_t flags = rd<uint32_t>(r, mat_off::texture_type_flags);
+        auto slot = [&](uint32_t bit, size_t off) { return (flags & bit) ? rd<uint32_t>(r, off) : VKG_NO_TEXTURE; };
+        m.tex_color = slot(tex_bit::color, mat_off::albedo_index);
+        m.tex_normal = slot(tex_bit::normal, mat_off::normalmap_index);
+        m.tex_emission = slot(tex_bit::emission, mat_off::emission_index);
+        m.tex_ao_rough_metal = slot(tex_bit::ao_rough_metal, mat_off::ao_rough_metal_index);
+        m.tex_transmission = slot(tex_bit::transmission, mat_off::transmission_index);
+        m.tex_diffuse_transmission = slot(tex_bit::diffuse_transmission, mat_off::diffuse_transmission_index);
+        m.tex_diffuse_transmission_color =
+                slot(tex_bit::diffuse_transmission_color, mat_off::diffuse_transmission_color_index);
+        // left out: textures the tracer does not sample (displacement, thickness, clearcoat, sheen,
+        // iridescence) and alpha blending / masking
+        bool unused = (flags & ~tex_bit::sampled) != 0 || rd<uint32_t>(r, mat_off::blend_mode) != 0;
         nd += unused ? 1u : 0u;
         out[i] = m;
     }

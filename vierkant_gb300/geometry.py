@@ -21,7 +21,10 @@ MATERIAL_DTYPE = np.dtype([("base_color", "<f4", 3), ("roughness", "<f4"), ("met
                            ("iridescence_ior", "<f4"), ("iridescence_thickness", "<f4"), ("attenuation_color", "<f4", 3),
                            ("attenuation_distance", "<f4"), ("scatter_color", "<f4", 3), ("scatter_factor", "<f4"),
                            ("phase_g", "<f4"), ("null_surface", "<u4"), ("dispersion", "<f4"),
-                           ("pad", "<f4")])
+                           ("tex_color", "<u4"), ("tex_normal", "<u4"), ("tex_emission", "<u4"),
+                           ("tex_ao_rough_metal", "<u4"), ("tex_transmission", "<u4"),
+                           ("tex_diffuse_transmission", "<u4"), ("tex_diffuse_transmission_color", "<u4"),
+                           ("pad", "<u4", 2)])
 assert MATERIAL_DTYPE.itemsize == C.sizeof(vkg_material)
 
 
@@ -77,6 +80,85 @@ def cornell_vertex_normals(sc) -> np.ndarray:
         d = xyz[v] - xyz[v].mean(axis=0)
         n[v] = d / np.linalg.norm(d, axis=1, keepdims=True)
     return n.astype(np.float32)
+
+
+def cornell_texcoords(sc, repeat: float = 2.0):
+    """Texture coordinates and tangents for a cornell_scene(): each wall quad maps its four corners to
+    (0, 0), (r, 0), (r, r), (0, r) (r = repeat), its tangent along the first edge; a sphere's vertices
+    get longitude / latitude about its centre (u = 0.5 + atan2(z, x) / 2 pi, v = acos(y) / pi) and
+    the tangent of growing longitude. Returns (uv float32 [V, 2], tangents float32 [V, 3])."""
+    xyz = np.asarray(sc["xyz"], np.float64)
+    idx = np.asarray(sc["indices"], np.int64)
+    tm = np.asarray(sc["tri_material"])
+    uv = np.zeros((len(xyz), 2))
+    tg = np.zeros((len(xyz), 3))
+    corners = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float64) * repeat
+    for q in range(5):
+        v = np.arange(4 * q, 4 * q + 4)
+        uv[v] = corners
+        e = xyz[v[1]] - xyz[v[0]]
+        tg[v] = e / np.linalg.norm(e)
+    for m in np.unique(tm[tm >= 3]):
+        v = np.unique(idx[tm == m].ravel())
+        d = xyz[v] - xyz[v].mean(axis=0)
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        uv[v, 0] = 0.5 + np.arctan2(d[:, 2], d[:, 0]) / (2 * np.pi)
+        uv[v, 1] = np.arccos(np.clip(d[:, 1], -1, 1)) / np.pi
+        t = np.stack([-d[:, 2], np.zeros(len(v)), d[:, 0]], axis=1)
+        n = np.linalg.norm(t, axis=1, keepdims=True)
+        tg[v] = np.where(n > 1e-6, t / np.maximum(n, 1e-12), np.array([1.0, 0.0, 0.0]))
+    return uv.astype(np.float32), tg.astype(np.float32)
+
+
+def test_textures(size: int = 64):
+    """Procedural RGBA8 textures for the textured test scenes: [0] a two-colour checker, [1] an
+    ao-rough-metal map (g: roughness stripes, b: metal checker), [2] a tangent-space normal map of
+    bumps, [3] an emission pattern. uint8 [size, size, 4] each."""
+    y, x = np.mgrid[0:size, 0:size].astype(np.float64)
+    u, v = (x + 0.5) / size, (y + 0.5) / size
+    chk = ((x // 8 + y // 8) % 2).astype(bool)
+    color = np.zeros((size, size, 4), np.uint8)
+    color[chk] = (230, 200, 60, 255)
+    color[~chk] = (40, 90, 200, 255)
+    arm = np.zeros((size, size, 4), np.uint8)
+    arm[..., 0] = 255
+    arm[..., 1] = (64 + 191 * (0.5 + 0.5 * np.sin(2 * np.pi * 4 * u))).astype(np.uint8)
+    arm[..., 2] = np.where(((x // 16 + y // 16) % 2) == 0, 255, 0).astype(np.uint8)
+    arm[..., 3] = 255
+    bx, by = np.sin(2 * np.pi * 4 * u), np.sin(2 * np.pi * 4 * v)
+    nx, ny = 0.4 * bx, 0.4 * by
+    nz = np.sqrt(np.maximum(0.0, 1 - nx * nx - ny * ny))
+    nrm = np.stack([(nx * 0.5 + 0.5) * 255, (ny * 0.5 + 0.5) * 255, nz * 255, np.full_like(nx, 255)], axis=-1)
+    nrm = np.rint(nrm).astype(np.uint8)
+    em = np.zeros((size, size, 4), np.uint8)
+    ring = np.abs(np.hypot(u - 0.5, v - 0.5) - 0.3) < 0.08
+    em[ring] = (255, 160, 40, 255)
+    em[~ring] = (0, 0, 0, 255)
+    return [color, arm, nrm, em]
+
+
+def textured_materials(materials: np.ndarray) -> np.ndarray:
+    """The Cornell materials with textures (indices into test_textures()): the back and floor walls
+    checkered, spheres in turn checkered, ao-rough-metal mapped, normal mapped, with an emission
+    pattern, or untextured."""
+    m = np.array(materials, MATERIAL_DTYPE, copy=True)
+    NO = 0xFFFFFFFF
+    for f in ("tex_color", "tex_normal", "tex_emission", "tex_ao_rough_metal", "tex_transmission",
+              "tex_diffuse_transmission", "tex_diffuse_transmission_color"):
+        m[f] = NO
+    m["tex_color"][0] = 0
+    for s in range(len(m) - 3):
+        i, kind = 3 + s, s % 5
+        if kind == 0:
+            m["tex_color"][i] = 0
+        elif kind == 1:
+            m["tex_ao_rough_metal"][i] = 1
+        elif kind == 2:
+            m["tex_normal"][i] = 2
+        elif kind == 3:
+            m["tex_emission"][i] = 3
+            m["emission"][i] = (2.0, 2.0, 2.0)
+    return m
 
 
 SHOWCASE_KINDS = ("metal-rough", "glass", "rough glass", "clearcoat", "sheen", "diffuse transmission", "iridescent")

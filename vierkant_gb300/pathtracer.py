@@ -191,6 +191,48 @@ class _Lights:
         check(lib().vkg_scene_set_normals(self.ctx.handle, self.handle, mesh, C.c_void_p(src), stride, fmt,
                                           C.c_void_p(self.ctx.stream())), self.ctx.handle, "vkg_scene_set_normals")
 
+    def set_tangents(self, tangents, mesh: int = 0):
+        """Vertex tangents for normal maps: float [V, 3] (normalised on upload), PACKED_VERTEX_DTYPE
+        records (their octahedral tangent words), or None."""
+        from ._lib import NORMALS_FLOAT3, NORMALS_OCT_SNORM16
+        src, stride, fmt, _keep = self._attr(tangents, 3, "tangent", 16, NORMALS_FLOAT3, NORMALS_OCT_SNORM16)
+        check(lib().vkg_scene_set_tangents(self.ctx.handle, self.handle, mesh, C.c_void_p(src), stride, fmt,
+                                           C.c_void_p(self.ctx.stream())), self.ctx.handle, "vkg_scene_set_tangents")
+
+    def set_texcoords(self, uv, mesh: int = 0):
+        """Texture coordinates: float [V, 2], PACKED_VERTEX_DTYPE records (their fp16 texcoords), or None."""
+        from ._lib import TEXCOORD_FLOAT2, TEXCOORD_HALF2
+        src, stride, fmt, _keep = self._attr(uv, 2, "texcoord", 20, TEXCOORD_FLOAT2, TEXCOORD_HALF2)
+        check(lib().vkg_scene_set_texcoords(self.ctx.handle, self.handle, mesh, C.c_void_p(src), stride, fmt,
+                                            C.c_void_p(self.ctx.stream())), self.ctx.handle, "vkg_scene_set_texcoords")
+
+    def _attr(self, a, comps, packed_field, packed_offset, fmt_float, fmt_packed):
+        dev = f"cuda:{self.ctx.device}"
+        if a is None:
+            return None, 0, fmt_float, None
+        if isinstance(a, np.ndarray) and a.dtype == PACKED_VERTEX_DTYPE:
+            buf = torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).copy()).to(dev)
+            return buf.data_ptr() + packed_offset, PACKED_VERTEX_DTYPE.itemsize, fmt_packed, buf
+        t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(a, np.float32))
+        buf = t.to(dev, torch.float32).contiguous()
+        assert buf.numel() % comps == 0
+        return buf.data_ptr(), 4 * comps, fmt_float, buf
+
+    def set_textures(self, textures):
+        """The scene's textures: a list of uint8 [H, W, 4] RGBA arrays (UNORM) or (array, wrap_s, wrap_t)
+        tuples (pathtracer.WRAP_*; REPEAT by default); an empty list removes them."""
+        from ._lib import vkg_texture_desc
+        descs = (vkg_texture_desc * max(1, len(textures)))()
+        keep = []
+        for k, t in enumerate(textures):
+            img, ws, wt = (t if isinstance(t, tuple) else (t, 0, 0))
+            img = np.ascontiguousarray(img, np.uint8)
+            assert img.ndim == 3 and img.shape[2] == 4, "RGBA8 [H, W, 4]"
+            keep.append(img)
+            descs[k] = vkg_texture_desc(img.ctypes.data, img.shape[1], img.shape[0], ws, wt)
+        check(lib().vkg_scene_set_textures(self.ctx.handle, self.handle, descs, len(textures),
+                                           C.c_void_p(self.ctx.stream())), self.ctx.handle, "vkg_scene_set_textures")
+
 class Scene(_Lights):
     def __init__(self, ctx: Context, xyz, indices, tri_material, materials, env_rgb, leaf_max=2):
         dev = f"cuda:{ctx.device}"
