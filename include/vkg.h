@@ -593,15 +593,19 @@ vkg_status vkg_scene_camera_medium(const vkg_scene *scene, const float eye[3], u
 
 /* ---- glTF 2.0 ingestion (host only; the reference's model/gltf.cpp path) --------------------
  * vkg_gltf_load reads a .gltf (base64 or file buffers) or .glb file into meshes (one per triangle
- * primitive; float positions, uint32 indices), instances (node placements, object -> world 3x4,
- * mesh index in `blas`, material), materials (vkg_material) and KHR_lights_punctual lights
- * (vkg_light); those feed vkg_scene_create_instanced and vkg_scene_set_lights. Errors: a status and
+ * primitive; float positions, uint32 indices, optional normals / texture coordinates / tangents),
+ * instances (node placements, object -> world 3x4, mesh index in `blas`, material), materials
+ * (vkg_material, texture slots indexing the asset's textures), textures (PNG images decoded to RGBA8)
+ * and KHR_lights_punctual lights (vkg_light); those feed vkg_scene_create_instanced,
+ * vkg_scene_set_normals / _texcoords / _tangents / _textures and vkg_scene_set_lights. Errors: a status and
  * the message in err (may be NULL). The mesh pointers stay valid until vkg_gltf_destroy. */
 typedef struct vkg_gltf vkg_gltf;
 typedef struct vkg_gltf_counts
 {
     uint32_t num_meshes, num_instances, num_materials, num_lights;
     uint32_t skipped_primitives; /* non-triangle primitives left out */
+    uint32_t num_textures;       /* glTF textures (vkg_gltf_textures) */
+    uint32_t skipped_textures;   /* textures whose image is not a PNG (their material slots are empty) */
 } vkg_gltf_counts;
 vkg_status vkg_gltf_load(const char *path, vkg_gltf **out, char *err, size_t err_len);
 vkg_status vkg_gltf_counts_get(const vkg_gltf *g, vkg_gltf_counts *out);
@@ -610,6 +614,14 @@ vkg_status vkg_gltf_mesh(const vkg_gltf *g, uint32_t index, const float **xyz, u
 /* the mesh's vertex normals (3 floats per vertex, the primitive's NORMAL attribute) or NULL when the
    primitive has none; for vkg_scene_set_normals */
 vkg_status vkg_gltf_mesh_normals(const vkg_gltf *g, uint32_t index, const float **normals);
+/* the mesh's TEXCOORD_0 (2 floats per vertex) / tangents (3 floats per vertex: TANGENT xyz, or computed
+   from NORMAL and TEXCOORD_0 as Geometry::compute_tangents does) or NULL; for vkg_scene_set_texcoords /
+   vkg_scene_set_tangents */
+vkg_status vkg_gltf_mesh_texcoords(const vkg_gltf *g, uint32_t index, const float **uv);
+vkg_status vkg_gltf_mesh_tangents(const vkg_gltf *g, uint32_t index, const float **tangents);
+/* the asset's textures (num_textures records; texel pointers valid until vkg_gltf_destroy), in glTF
+   texture order, which the materials' texture slots index: for vkg_scene_set_textures */
+vkg_status vkg_gltf_textures(const vkg_gltf *g, vkg_texture_desc *out);
 vkg_status vkg_gltf_instances(const vkg_gltf *g, vkg_instance *out);
 vkg_status vkg_gltf_materials(const vkg_gltf *g, vkg_material *out);
 vkg_status vkg_gltf_lights(const vkg_gltf *g, vkg_light *out);

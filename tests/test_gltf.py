@@ -201,3 +201,115 @@ def test_vertex_normals(tmp_path):
     with pytest.raises(ValueError, match="NORMAL"):
         load_gltf(str(bad))
 
+
+
+def _expected_rgba(img, color_type, depth, palette=None, trns=None):
+    img = np.asarray(img)
+    if color_type == 3:
+        pal = np.asarray(palette, np.uint8).reshape(-1, 3)
+        out = np.full(img.shape + (4,), 255, np.uint8)
+        out[..., :3] = pal[img]
+        if trns is not None:
+            t = np.full(len(pal), 255, np.uint8)
+            t[:len(trns)] = trns
+            out[..., 3] = t[img]
+        return out
+    hi = (img >> 8).astype(np.uint8) if depth == 16 else img.astype(np.uint8)
+    if depth < 8:
+        hi = (img.astype(np.uint32) * (255 // ((1 << depth) - 1))).astype(np.uint8)
+    out = np.full(img.shape[:2] + (4,), 255, np.uint8)
+    if color_type in (0, 4):
+        g = hi if hi.ndim == 2 else hi[..., 0]
+        out[..., 0] = out[..., 1] = out[..., 2] = g
+        if color_type == 4:
+            out[..., 3] = hi[..., 1]
+    else:
+        out[..., :3] = hi[..., :3]
+        if color_type == 6:
+            out[..., 3] = hi[..., 3]
+    return out
+
+
+def test_png_images_of_every_kind(tmp_path):
+    """PNG images decoded by the loader's own inflate / unfilter: the five colour types, bit depths 1,
+    4, 8, 16, palettes with transparency, all five row filters, stored / fixed / dynamic DEFLATE
+    blocks; a truncated PNG and a JPEG are counted as skipped and leave their material slots empty"""
+    import zlib
+    from gltf_writer import png
+    rng = np.random.default_rng(7)
+    H, W = 13, 19
+    cases = []
+    for ct, ch in ((6, 4), (2, 3), (4, 2)):
+        img = rng.integers(0, 256, (H, W, ch), dtype=np.uint8)
+        cases.append((png(img, ct, 8), _expected_rgba(img, ct, 8)))
+    gray = rng.integers(0, 256, (H, W), dtype=np.uint8)
+    cases.append((png(gray, 0, 8, level=0), _expected_rgba(gray, 0, 8)))
+    img16 = rng.integers(0, 65536, (H, W, 4), dtype=np.uint16)
+    cases.append((png(img16, 6, 16, strategy=zlib.Z_FIXED), _expected_rgba(img16, 6, 16)))
+    g4 = rng.integers(0, 16, (H, W), dtype=np.uint8)
+    cases.append((png(g4, 0, 4), _expected_rgba(g4, 0, 4)))
+    g1 = rng.integers(0, 2, (H, W), dtype=np.uint8)
+    cases.append((png(g1, 0, 1), _expected_rgba(g1, 0, 1)))
+    pal = rng.integers(0, 256, (16, 3), dtype=np.uint8)
+    idx8 = rng.integers(0, 16, (H, W), dtype=np.uint8)
+    trns = rng.integers(0, 256, 10, dtype=np.uint8)
+    cases.append((png(idx8, 3, 8, palette=pal, trns=trns), _expected_rgba(idx8, 3, 8, pal, trns)))
+    cases.append((png(idx8, 3, 4, palette=pal), _expected_rgba(idx8, 3, 4, pal)))
+    bad = [png(gray, 0, 8)[:60], b"\xff\xd8\xff\xe0" + bytes(64)]
+    images = [(data, 10497, 10497) for data, _ in cases] + [(b, 10497, 10497) for b in bad]
+    mats = [{"pbrMetallicRoughness": {"baseColorTexture": {"index": k}}} for k in range(len(images))]
+    path = tmp_path / "png.gltf"
+    write(path, [[(*TRI, k, None)] for k in range(len(images))], [dict(mesh=k) for k in range(len(images))],
+          list(range(len(images))), materials=mats, images=images)
+    a = load_gltf(str(path))
+    assert a["skipped_textures"] == 2 and len(a["textures"]) == len(images)
+    for k, (_, expect) in enumerate(cases):
+        got, ws, wt = a["textures"][k]
+        assert np.array_equal(got, expect), k
+        assert a["materials"][k]["tex_color"] == k
+    for k in range(len(cases), len(images)):
+        assert a["materials"][k]["tex_color"] == 0xFFFFFFFF
+
+
+def test_texcoords_tangents_and_samplers(tmp_path):
+    """TEXCOORD_0 as floats and as normalised bytes, TANGENT xyz, tangents computed from NORMAL and
+    TEXCOORD_0 as Geometry::compute_tangents does, the samplers' wrap modes, the material texture
+    slots (an emissive texture zeroes the emissive factor)"""
+    from gltf_writer import png
+    quad_uv = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+    n = np.tile([0, 0, 1], (4, 1)).astype(np.float32)
+    tg = np.array([[1, 0, 0, 1]] * 4, np.float32)
+    uv8 = np.array([[0, 0], [255, 0], [255, 255], [0, 255]], np.uint8)
+    img = png(np.full((4, 4, 4), 200, np.uint8), 6, 8)
+    meshes = [[(*QUAD, 0, None, n, {"TEXCOORD_0": quad_uv, "TANGENT": tg})],
+              [(*QUAD, 0, None, n, {"TEXCOORD_0": (uv8, 5121)})],
+              [(*QUAD, 0, None, None, {"TEXCOORD_0": quad_uv})]]
+    mats = [{"pbrMetallicRoughness": {"baseColorTexture": {"index": 0}, "metallicRoughnessTexture": {"index": 1}},
+             "normalTexture": {"index": 1}, "emissiveTexture": {"index": 0}, "emissiveFactor": [1, 1, 1],
+             "extensions": {"KHR_materials_transmission": {"transmissionTexture": {"index": 1}}}}]
+    path = tmp_path / "uv.glb"
+    write(path, meshes, [dict(mesh=k) for k in range(3)], [0, 1, 2], materials=mats, mode="glb",
+          images=[(img, 33071, 33648), (img, 10497, 33071)])
+    a = load_gltf(str(path))
+    assert np.array_equal(a["texcoords"][0], quad_uv) and np.allclose(a["tangents"][0], tg[:, :3])
+    assert np.allclose(a["texcoords"][1], quad_uv)
+    # computed: QUAD's u runs along +x, v along +y, normal +z -> tangent +-x, sign as compute_tangents
+    xyz, ix = QUAD
+    assert a["tangents"][1] is not None and np.allclose(np.abs(a["tangents"][1]), [[1, 0, 0]] * 4, atol=1e-6)
+    t = np.zeros((4, 3)); b = np.zeros((4, 3))
+    for tri in ix:
+        v0, v1, v2 = xyz[tri]
+        u0, u1, u2 = quad_uv[tri]
+        x1, x2 = v1 - v0, v2 - v0
+        s1, s2, t1, t2 = u1[0] - u0[0], u2[0] - u0[0], u1[1] - u0[1], u2[1] - u0[1]
+        r = 1 / (s1 * t2 - s2 * t1)
+        t[tri] += (t2 * x1 - t1 * x2) * r
+        b[tri] += (s1 * x2 - s2 * x1) * r
+    sign = np.where(np.einsum("ij,ij->i", np.cross(n, t), b) < 0, 1.0, -1.0)
+    assert np.allclose(a["tangents"][1], t / np.linalg.norm(t, axis=1, keepdims=True) * sign[:, None], atol=1e-6)
+    assert a["tangents"][2] is None and a["normals"][2] is None  # no normals: no tangents either
+    assert [(ws, wt) for _, ws, wt in a["textures"]] == [(1, 2), (0, 1)]
+    m = a["materials"][0]
+    assert (m["tex_color"], m["tex_ao_rough_metal"], m["tex_normal"], m["tex_emission"], m["tex_transmission"]) == \
+        (0, 1, 1, 0, 1)
+    assert np.array_equal(m["emission"], [0, 0, 0])

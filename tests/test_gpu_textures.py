@@ -147,3 +147,63 @@ def test_instanced_textures_match_single_level(ctx, world):
     assert np.mean(np.abs(a - b)) < 0.1 * np.mean(np.abs(b))
     inst_scene.close()
     single.close()
+
+
+def test_gltf_textured_scene_renders_like_the_direct_one(ctx, world, tmp_path):
+    """the textured Cornell scene written as a glTF asset (PNG images, TEXCOORD_0, TANGENT, NORMAL,
+    texture slots) renders bit for bit like the same scene built directly"""
+    from gltf_writer import png, write
+    from vierkant_gb300.gltf import scene_from_gltf
+    sc = geometry.cornell_scene(0x5EED, 2, 8, 8)
+    nrm = geometry.cornell_vertex_normals(sc)
+    uv, tg = geometry.cornell_texcoords(sc)
+    mats = geometry.textured_materials(sc["materials"])
+    meshes, inst = split_cornell(sc, tess=8)
+    idx = sc["indices"]
+    groups = [(2 * q, 2 * q + 2) for q in range(5)] + [(10 + k * 768, 10 + (k + 1) * 768) for k in range(8)]
+    used = [np.unique(idx[a:b].reshape(-1)) for a, b in groups]
+    tex = world["tex"]
+
+    def tref(k):
+        return {"index": int(k)} if k != 0xFFFFFFFF else None
+
+    gmats = []
+    for m in mats:
+        g = {"pbrMetallicRoughness": {"baseColorFactor": [float(c) for c in m["base_color"]] + [1.0],
+                                      "metallicFactor": float(m["metalness"]),
+                                      "roughnessFactor": float(m["roughness"])},
+             "doubleSided": bool(m["twosided"]), "emissiveFactor": [float(c) for c in m["emission"]]}
+        for slot, key, where in (("tex_color", "baseColorTexture", "pbr"),
+                                 ("tex_ao_rough_metal", "metallicRoughnessTexture", "pbr"),
+                                 ("tex_normal", "normalTexture", "top"), ("tex_emission", "emissiveTexture", "top")):
+            r = tref(m[slot])
+            if r is not None:
+                (g["pbrMetallicRoughness"] if where == "pbr" else g)[key] = r
+        gmats.append(g)
+    gm = [[(x, i, int(inst[k]["material"]), None, nrm[u], {"TEXCOORD_0": uv[u],
+                                                             "TANGENT": np.c_[tg[u], np.ones(len(u), np.float32)]})]
+          for k, ((x, i, _), u) in enumerate(zip(meshes, used))]
+    path = tmp_path / "textured.glb"
+    write(path, gm, [dict(mesh=k) for k in range(len(meshes))], list(range(len(meshes))), materials=gmats,
+          mode="glb", images=[(png(t, 6, 8), 10497, 10497) for t in tex])
+    env = procedural_sky(ctx, 256, 128, sun_direction(), 50.0, 0.02)
+    loaded = scene_from_gltf(ctx, str(path), env)
+    direct_mats = mats.copy()
+    direct_mats["emission"] = np.where(mats["tex_emission"][:, None] != 0xFFFFFFFF, 0.0, mats["emission"])
+    direct = InstancedScene(ctx, meshes, inst, direct_mats, env)
+    for m, u in enumerate(used):
+        direct.set_normals(nrm[u], mesh=m)
+        direct.set_texcoords(uv[u], mesh=m)
+        direct.set_tangents(tg[u], mesh=m)
+    direct.set_textures(tex)
+    cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, 1280, 720)
+    for crop in ((560, 300, 64, 64), (600, 100, 64, 64)):
+        p = PBRPathTracer(ctx, seed=4, settings=settings(4, crop))
+        q_ = PBRPathTracer(ctx, seed=4, settings=settings(4, crop))
+        ia = p.render_scene(loaded, cam).clone()
+        ib = q_.render_scene(direct, cam).clone()
+        assert torch.equal(ia, ib), (ia - ib).abs().max().item()
+        p.close()
+        q_.close()
+    loaded.close()
+    direct.close()

@@ -101,7 +101,8 @@ class vkg_post_fx_settings(C.Structure):
 
 class vkg_gltf_counts(C.Structure):
     _fields_ = [("num_meshes", C.c_uint32), ("num_instances", C.c_uint32), ("num_materials", C.c_uint32),
-                ("num_lights", C.c_uint32), ("skipped_primitives", C.c_uint32)]
+                ("num_lights", C.c_uint32), ("skipped_primitives", C.c_uint32), ("num_textures", C.c_uint32),
+                ("skipped_textures", C.c_uint32)]
 
 
 class vkg_wire_entry_info(C.Structure):
@@ -257,6 +258,9 @@ SIGNATURES = {
     "vkg_gltf_mesh": (I32, [P, U32, C.POINTER(C.POINTER(C.c_float)), C.POINTER(U32), C.POINTER(C.POINTER(U32)),
                             C.POINTER(U32)]),
     "vkg_gltf_mesh_normals": (I32, [P, U32, C.POINTER(C.POINTER(C.c_float))]),
+    "vkg_gltf_mesh_texcoords": (I32, [P, U32, C.POINTER(C.POINTER(C.c_float))]),
+    "vkg_gltf_mesh_tangents": (I32, [P, U32, C.POINTER(C.POINTER(C.c_float))]),
+    "vkg_gltf_textures": (I32, [P, P]),
     "vkg_gltf_instances": (I32, [P, P]),
     "vkg_gltf_materials": (I32, [P, P]),
     "vkg_gltf_lights": (I32, [P, P]),

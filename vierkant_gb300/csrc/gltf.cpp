@@ -20,11 +20,19 @@
 //   * KHR_lights_punctual lights placed by their nodes (gltf.cpp:1043-1061, :1182-1190), converted as
 //     convert_light does (punctual_light.hpp:92-111): position = translation, direction = R (0,0,-1),
 //     tangent = R (1,0,0), R the node's rotation (its world matrix's columns normalised).
-// Not read: textures and texture transforms, skins, morph targets, animations, cameras, volume
+//   * per primitive NORMAL, TEXCOORD_0 (float, or normalised unsigned integers) and TANGENT (xyz; when
+//     absent but NORMAL and TEXCOORD_0 are there, computed as Geometry::compute_tangents does,
+//     Geometry.cpp:196-252); the textures the materials use (baseColor, metallicRoughness, normal,
+//     emissive -- which zeroes the emissive factor, as gltf.cpp:377 does -- transmission, diffuse
+//     transmission factor / colour), one per glTF texture: its image decoded from PNG (data URI,
+//     file or buffer view) with its sampler's wrap modes (REPEAT by default); a texture whose image
+//     is not a PNG is counted in skipped_textures and its material slots left empty.
+// Not read: texture transforms, occlusion, skins, morph targets, animations, cameras, volume
 // thickness, specular, sparse accessors, quantised positions. The reference composes transforms as
 // translation / quaternion / scale triples and projects shear away (transform.hpp:106-128); the
 // matrix composition here is the same for every chain without shear.
 #include "internal.hpp"
+#include "png.hpp"
 
 #include <algorithm>
 #include <cmath>
@@ -278,6 +286,14 @@ struct mesh_t
     std::vector<float> xyz;
     std::vector<uint32_t> idx;
     std::vector<float> nrm; // the primitive's NORMAL attribute (3 per vertex), empty when it has none
+    std::vector<float> uv;  // TEXCOORD_0 (2 per vertex), empty when it has none
+    std::vector<float> tng; // TANGENT xyz or computed tangents (3 per vertex), empty when neither
+};
+
+struct texture_t
+{
+    std::vector<uint8_t> rgba; // empty: the image could not be decoded
+    uint32_t width = 0, height = 0, wrap_s = VKG_WRAP_REPEAT, wrap_t = VKG_WRAP_REPEAT;
 };
 
 }// namespace
@@ -288,7 +304,8 @@ struct vkg_gltf
     std::vector<vkg_instance> instances;
     std::vector<vkg_material> materials;
     std::vector<vkg_light> lights;
-    uint32_t skipped_primitives = 0;
+    std::vector<texture_t> textures;
+    uint32_t skipped_primitives = 0, skipped_textures = 0;
 };
 
 namespace
@@ -434,7 +451,9 @@ struct loader
     }
 
     // the elements of an accessor as doubles (components per element in `comps`)
-    bool accessor(long ai, const char *what, std::vector<double> &out, int &comps, bool want_float)
+    // want_float: float components only (or, with unorm_ok, also normalised unsigned bytes / shorts,
+    // mapped to [0, 1]); else integer components only
+    bool accessor(long ai, const char *what, std::vector<double> &out, int &comps, bool want_float, bool unorm_ok = false)
     {
         const auto *accs = doc.arr("accessors");
         if(!accs || ai < 0 || (size_t)ai >= accs->size()) return fail("%s: accessor %ld missing", what, ai);
@@ -445,7 +464,9 @@ struct loader
         if(!comps) return fail("%s: unsupported accessor type", what);
         const long ct = (long)a.num("componentType", 0);
         const size_t csize = ct == 5120 || ct == 5121 ? 1 : ct == 5122 || ct == 5123 ? 2 : ct == 5125 || ct == 5126 ? 4 : 0;
-        if(!csize || (want_float && ct != 5126) || (!want_float && ct == 5126))
+        const jv *nz = a.get("normalized");
+        const bool unorm = unorm_ok && nz && nz->kind == jv::BOOL && nz->b && (ct == 5121 || ct == 5123);
+        if(!csize || (want_float && ct != 5126 && !unorm) || (!want_float && ct == 5126))
             return fail("%s: unsupported component type %ld", what, ct);
         const double count = a.num("count", -1);
         if(count < 0 || count > 1e9) return fail("%s: bad count", what);
@@ -481,8 +502,111 @@ struct loader
                     case 5125: { uint32_t t; std::memcpy(&t, q, 4); v = t; break; }
                     default: { float t; std::memcpy(&t, q, 4); v = t; break; }
                 }
-                out[i * (size_t)comps + (size_t)c] = v;
+                out[i * (size_t)comps + (size_t)c] = unorm ? v / (ct == 5121 ? 255.0 : 65535.0) : v;
             }
+        return true;
+    }
+
+    // Geometry::compute_tangents (Geometry.cpp:196-252): per-triangle UV-derivative tangents summed at
+    // the vertices, Gram-Schmidt against the normal, negated unless dot(cross(n, t), b) < 0
+    static void compute_tangents(mesh_t &M)
+    {
+        const size_t nv = M.xyz.size() / 3;
+        std::vector<float> t(nv * 3, 0.f), b(nv * 3, 0.f);
+        for(size_t i = 0; i + 2 < M.idx.size(); i += 3)
+        {
+            const uint32_t a = M.idx[i], bb = M.idx[i + 1], c = M.idx[i + 2];
+            const float *v0 = &M.xyz[3 * (size_t)a], *v1 = &M.xyz[3 * (size_t)bb], *v2 = &M.xyz[3 * (size_t)c];
+            const float *u0 = &M.uv[2 * (size_t)a], *u1 = &M.uv[2 * (size_t)bb], *u2 = &M.uv[2 * (size_t)c];
+            const float x1 = v1[0] - v0[0], x2 = v2[0] - v0[0], y1 = v1[1] - v0[1], y2 = v2[1] - v0[1];
+            const float z1 = v1[2] - v0[2], z2 = v2[2] - v0[2];
+            const float s1 = u1[0] - u0[0], s2 = u2[0] - u0[0], t1 = u1[1] - u0[1], t2 = u2[1] - u0[1];
+            const float r = 1.f / (s1 * t2 - s2 * t1);
+            const float sd[3] = {(t2 * x1 - t1 * x2) * r, (t2 * y1 - t1 * y2) * r, (t2 * z1 - t1 * z2) * r};
+            const float td[3] = {(s1 * x2 - s2 * x1) * r, (s1 * y2 - s2 * y1) * r, (s1 * z2 - s2 * z1) * r};
+            for(uint32_t v: {a, bb, c})
+                for(int k = 0; k < 3; ++k)
+                {
+                    t[3 * (size_t)v + k] += sd[k];
+                    b[3 * (size_t)v + k] += td[k];
+                }
+        }
+        M.tng.assign(nv * 3, 0.f);
+        for(size_t v = 0; v < nv; ++v)
+        {
+            const float *n = &M.nrm[3 * v], *tv = &t[3 * v], *bv = &b[3 * v];
+            const float d = n[0] * tv[0] + n[1] * tv[1] + n[2] * tv[2];
+            float o[3] = {tv[0] - n[0] * d, tv[1] - n[1] * d, tv[2] - n[2] * d};
+            const float len = std::sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2]);
+            for(float &x: o) x = len > 0.f ? x / len : 0.f;
+            const float cr[3] = {n[1] * tv[2] - n[2] * tv[1], n[2] * tv[0] - n[0] * tv[2], n[0] * tv[1] - n[1] * tv[0]};
+            const float sign = (cr[0] * bv[0] + cr[1] * bv[1] + cr[2] * bv[2]) < 0.f ? 1.f : -1.f;
+            for(int k = 0; k < 3; ++k) M.tng[3 * v + k] = o[k] * sign;
+        }
+    }
+
+    // the bytes of image ii: a data URI, a file next to the asset, or a buffer view
+    bool image_bytes(long ii, std::vector<uint8_t> &out)
+    {
+        const auto *imgs = doc.arr("images");
+        if(!imgs || ii < 0 || (size_t)ii >= imgs->size()) return fail("image %ld missing", ii);
+        const jv &im = (*imgs)[(size_t)ii];
+        if(const std::string *uri = im.str("uri"))
+        {
+            if(uri->rfind("data:", 0) == 0)
+            {
+                const size_t comma = uri->find(',');
+                if(comma == std::string::npos || uri->find(";base64") == std::string::npos || !base64(*uri, comma + 1, out))
+                    return fail("image %ld: unreadable data uri", ii);
+                return true;
+            }
+            if(!read_file(dir + *uri, out)) return fail("image %ld: cannot read '%s'", ii, uri->c_str());
+            return true;
+        }
+        const long bvi = im.idx("bufferView");
+        const auto *bvs = doc.arr("bufferViews");
+        if(bvi < 0 || !bvs || (size_t)bvi >= bvs->size()) return fail("image %ld has no uri and no bufferView", ii);
+        const jv &bv = (*bvs)[(size_t)bvi];
+        const long bi = bv.idx("buffer");
+        if(bi < 0 || (size_t)bi >= buffers.size()) return fail("image %ld: buffer %ld missing", ii, bi);
+        const size_t off = (size_t)bv.num("byteOffset", 0), len = (size_t)bv.num("byteLength", 0);
+        if(off + len > buffers[(size_t)bi].size()) return fail("image %ld: buffer view past its buffer", ii);
+        out.assign(buffers[(size_t)bi].begin() + (long)off, buffers[(size_t)bi].begin() + (long)(off + len));
+        return true;
+    }
+
+    // the asset's textures: PNG images decoded with their samplers' wrap modes; false only on a
+    // malformed reference (a texture whose image is not a PNG is kept empty and counted)
+    bool textures(vkg_gltf &G)
+    {
+        const auto *texs = doc.arr("textures");
+        if(!texs) return true;
+        const auto *samplers = doc.arr("samplers");
+        auto wrap = [](double w) -> uint32_t {
+            return w == 33071 ? VKG_WRAP_CLAMP_TO_EDGE : w == 33648 ? VKG_WRAP_MIRRORED_REPEAT : VKG_WRAP_REPEAT;
+        };
+        for(size_t ti = 0; ti < texs->size(); ++ti)
+        {
+            const jv &t = (*texs)[ti];
+            texture_t T;
+            const long si = t.idx("sampler");
+            if(samplers && si >= 0 && (size_t)si < samplers->size())
+            {
+                T.wrap_s = wrap((*samplers)[(size_t)si].num("wrapS", 10497));
+                T.wrap_t = wrap((*samplers)[(size_t)si].num("wrapT", 10497));
+            }
+            const long src = t.idx("source");
+            std::vector<uint8_t> bytes;
+            if(src < 0) return fail("texture %zu has no source image", ti);
+            if(!image_bytes(src, bytes)) return false;
+            std::string perr;
+            if(!vkg::png_decode(bytes.data(), bytes.size(), T.rgba, T.width, T.height, perr))
+            {
+                T.rgba.clear();
+                ++G.skipped_textures;
+            }
+            G.textures.push_back(std::move(T));
+        }
         return true;
     }
 
@@ -598,6 +722,25 @@ struct loader
                 r.scatter_factor = (float)sc->num("scatterFactor", unified ? 0.0 : 1.0);
             }
         }
+        // texture slots: glTF texture indices, resolved to NO_TEXTURE later if the image fails
+        auto tex = [](const jv *info) -> uint32_t {
+            const long i = info ? info->idx("index") : -1;
+            return i >= 0 ? (uint32_t)i : VKG_NO_TEXTURE;
+        };
+        r.tex_color = tex(pbr ? pbr->get("baseColorTexture") : nullptr);
+        r.tex_ao_rough_metal = tex(pbr ? pbr->get("metallicRoughnessTexture") : nullptr);
+        r.tex_normal = tex(m.get("normalTexture"));
+        r.tex_emission = tex(m.get("emissiveTexture"));
+        if(r.tex_emission != VKG_NO_TEXTURE) em[0] = em[1] = em[2] = 0.f; // the texture alone (gltf.cpp:377)
+        if(ext && ext->kind == jv::OBJ)
+        {
+            if(const jv *e = ext->get("KHR_materials_transmission")) r.tex_transmission = tex(e->get("transmissionTexture"));
+            if(const jv *e = ext->get("KHR_materials_diffuse_transmission"))
+            {
+                r.tex_diffuse_transmission = tex(e->get("diffuseTransmissionTexture"));
+                r.tex_diffuse_transmission_color = tex(e->get("diffuseTransmissionColorTexture"));
+            }
+        }
         for(int c = 0; c < 3; ++c) r.emission[c] = em[c] * strength;
         const jv *ds = m.get("doubleSided");
         r.twosided = ds && ds->kind == jv::BOOL && ds->b ? 1u : 0u;
@@ -616,6 +759,13 @@ struct loader
             vkg_material_defaults(&d);
             G.materials.push_back(d);
         }
+        if(!textures(G)) return false;
+        // material slots of missing or undecoded textures stay empty
+        for(vkg_material &m: G.materials)
+            for(uint32_t *slot: {&m.tex_color, &m.tex_normal, &m.tex_emission, &m.tex_ao_rough_metal, &m.tex_transmission,
+                                 &m.tex_diffuse_transmission, &m.tex_diffuse_transmission_color})
+                if(*slot != VKG_NO_TEXTURE && (*slot >= G.textures.size() || G.textures[*slot].rgba.empty()))
+                    *slot = VKG_NO_TEXTURE;
         // meshes: one per triangle primitive
         const auto *meshes = doc.arr("meshes");
         std::vector<std::vector<std::pair<uint32_t, uint32_t>>> prim_of(meshes ? meshes->size() : 0); // (mesh, material)
@@ -651,6 +801,26 @@ struct loader
                         return fail("mesh %zu primitive %zu: NORMAL is not VEC3 per vertex", mi, pi);
                     M.nrm.assign(nn.begin(), nn.end());
                 }
+                if(const long ta = attr->idx("TEXCOORD_0"); ta >= 0)
+                {
+                    std::vector<double> tt;
+                    int tc = 0;
+                    if(!accessor(ta, "TEXCOORD_0", tt, tc, true, true)) return false;
+                    if(tc != 2 || tt.size() != nv * 2)
+                        return fail("mesh %zu primitive %zu: TEXCOORD_0 is not VEC2 per vertex", mi, pi);
+                    M.uv.assign(tt.begin(), tt.end());
+                }
+                if(const long ga = attr->idx("TANGENT"); ga >= 0)
+                {
+                    std::vector<double> gg;
+                    int gc = 0;
+                    if(!accessor(ga, "TANGENT", gg, gc, true)) return false;
+                    if(gc != 4 || gg.size() != nv * 4)
+                        return fail("mesh %zu primitive %zu: TANGENT is not VEC4 per vertex", mi, pi);
+                    M.tng.resize(nv * 3);
+                    for(size_t k = 0; k < nv; ++k)
+                        for(int c = 0; c < 3; ++c) M.tng[3 * k + c] = (float)gg[4 * k + c];
+                }
                 const long ia = pr.idx("indices");
                 if(ia >= 0)
                 {
@@ -667,6 +837,7 @@ struct loader
                 for(double v: ix)
                     if(v >= (double)nv) return fail("mesh %zu primitive %zu: index %g out of range", mi, pi, v);
                 M.idx.assign(ix.begin(), ix.end());
+                if(M.tng.empty() && !M.uv.empty() && !M.nrm.empty()) compute_tangents(M);
                 long mat = pr.idx("material");
                 if(mat < 0 || (size_t)mat >= G.materials.size()) mat = 0;
                 prim_of[mi].push_back({(uint32_t)G.meshes.size(), (uint32_t)mat});
@@ -823,6 +994,8 @@ vkg_status vkg_gltf_counts_get(const vkg_gltf *g, vkg_gltf_counts *out)
     out->num_materials = (uint32_t)g->materials.size();
     out->num_lights = (uint32_t)g->lights.size();
     out->skipped_primitives = g->skipped_primitives;
+    out->num_textures = (uint32_t)g->textures.size();
+    out->skipped_textures = g->skipped_textures;
     return VKG_OK;
 }
 
@@ -835,6 +1008,34 @@ vkg_status vkg_gltf_mesh(const vkg_gltf *g, uint32_t i, const float **xyz, uint3
     *num_vertices = (uint32_t)(M.xyz.size() / 3);
     *indices = M.idx.data();
     *num_tris = (uint32_t)(M.idx.size() / 3);
+    return VKG_OK;
+}
+
+vkg_status vkg_gltf_mesh_texcoords(const vkg_gltf *g, uint32_t i, const float **uv)
+{
+    if(!g || i >= g->meshes.size() || !uv) return VKG_ERR_INVALID_ARGUMENT;
+    *uv = g->meshes[i].uv.empty() ? nullptr : g->meshes[i].uv.data();
+    return VKG_OK;
+}
+
+vkg_status vkg_gltf_mesh_tangents(const vkg_gltf *g, uint32_t i, const float **tangents)
+{
+    if(!g || i >= g->meshes.size() || !tangents) return VKG_ERR_INVALID_ARGUMENT;
+    *tangents = g->meshes[i].tng.empty() ? nullptr : g->meshes[i].tng.data();
+    return VKG_OK;
+}
+
+vkg_status vkg_gltf_textures(const vkg_gltf *g, vkg_texture_desc *out)
+{
+    if(!g || (!out && !g->textures.empty())) return VKG_ERR_INVALID_ARGUMENT;
+    for(size_t i = 0; i < g->textures.size(); ++i)
+    {
+        const texture_t &T = g->textures[i];
+        // an undecoded image: a 1 x 1 white texture keeps the indices aligned (no material uses it)
+        static const uint8_t white[4] = {255, 255, 255, 255};
+        out[i] = vkg_texture_desc{T.rgba.empty() ? white : T.rgba.data(), T.rgba.empty() ? 1u : T.width,
+                                  T.rgba.empty() ? 1u : T.height, T.wrap_s, T.wrap_t};
+    }
     return VKG_OK;
 }
 
