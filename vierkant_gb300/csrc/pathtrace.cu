@@ -1271,16 +1271,23 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
                                                               t->order);
                 order = t->order;
             }
-#define VKG_SHADE(M, F, MD)                                                                                            \
-    k_pt_shade<M, single_scene, F, MD><<<grid, PT_THREADS, 0, st>>>(SS, depth, t->q_ray[a], t->q_pid[a], t->hits, t->hit_inst, cnt_in,        \
+#define VKG_SHADE(M, F, MD, TX)                                                                                        \
+    k_pt_shade<M, single_scene, F, MD, TX><<<grid, PT_THREADS, 0, st>>>(SS, depth, t->q_ray[a], t->q_pid[a], t->hits, t->hit_inst, cnt_in,    \
                                                t->q_ray[1 - a],                                                          \
                                                t->q_pid[1 - a], cnt_out, t->s_ray, t->s_pid, t->s_contrib, cnt_s,         \
                                                t->rng, t->beta_pdf, t->radiance, io, lq, order)
-            if(mode == MODE_PLAIN && has_media) VKG_SHADE(MODE_PLAIN, true, true);
-            else if(mode == MODE_PLAIN && full) VKG_SHADE(MODE_PLAIN, true, false);
-            else if(mode == MODE_PLAIN) VKG_SHADE(MODE_PLAIN, false, false);
-            else if(full) VKG_SHADE(MODE_CACHE, true, false);
-            else VKG_SHADE(MODE_CACHE, false, false);
+#define VKG_SHADE_T(M, F, MD)                                                                                          \
+    do                                                                                                                 \
+    {                                                                                                                  \
+        if(P.cone) VKG_SHADE(M, F, MD, true);                                                                          \
+        else VKG_SHADE(M, F, MD, false);                                                                               \
+    } while(0)
+            if(mode == MODE_PLAIN && has_media) VKG_SHADE_T(MODE_PLAIN, true, true);
+            else if(mode == MODE_PLAIN && full) VKG_SHADE_T(MODE_PLAIN, true, false);
+            else if(mode == MODE_PLAIN) VKG_SHADE_T(MODE_PLAIN, false, false);
+            else if(full) VKG_SHADE_T(MODE_CACHE, true, false);
+            else VKG_SHADE_T(MODE_CACHE, false, false);
+#undef VKG_SHADE_T
 #undef VKG_SHADE
             if(!empty && tl_persistent)
             {

@@ -577,7 +577,9 @@ __global__ void __launch_bounds__(PT_THREADS)
     }
 }
 
-template<int MODE, class J, bool FULL = true, bool MEDIA = false>
+// TEX: the scene has textures (P.cone set); the untextured variant carries no texture code, which
+// keeps its register budget
+template<int MODE, class J, bool FULL = true, bool MEDIA = false, bool TEX = false>
 __global__ void __launch_bounds__(PT_THREADS)
         k_pt_shade(J S, uint32_t depth, const vkg_ray *__restrict__ in_ray,
                    const uint32_t *__restrict__ in_pid, const vkg_hit *__restrict__ hits,
@@ -845,7 +847,7 @@ __global__ void __launch_bounds__(PT_THREADS)
                 material_view m = load_material<FULL>(P.mats, mat, P.disable_material);
                 const float *em = P.mats[mat].emission;
                 float3 emit = f3(em[0], em[1], em[2]);
-                if(P.cone)
+                if(TEX && P.cone)
                 {
                     // textures sampled with the ray cone as it reached this surface, which then grows
                     // by the segment (propagate with no surface spread, raypipeline.slang:608)
