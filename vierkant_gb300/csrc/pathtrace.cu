@@ -1246,9 +1246,11 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
                 // queues, shortened by Russian roulette and escapes, gain less than binning costs
                 // (720p 64 spp: 69.1 ms binning depth 1, 69.3 ms binning every depth >= 1, 71.0 ms none)
                 const uint32_t *reordered = nullptr;
-                const uint32_t *perm = (depth == 1 && !P.two_level)
-                                               ? bin_rays(ctx, sc->bvh, t->q_ray[a], n, cnt_in, 0u, st, &reordered)
-                                               : nullptr;
+                // (an instanced scene bins by the top level's box: the stress frame 1,334 -> 1,268 ms with
+                // the shadow queues below)
+                const vkg_bvh *bounds = sc->bvh ? sc->bvh : (sc->tlas ? &sc->tlas->top : nullptr);
+                const uint32_t *perm = depth == 1 ? bin_rays(ctx, bounds, t->q_ray[a], n, cnt_in, 0u, st, &reordered)
+                                                  : nullptr;
                 if(small_stack)
                     k_pt_extend<single_scene, 64><<<grid, PT_THREADS, 0, st>>>(SS, t->q_ray[a], t->q_pid[a], cnt_in,
                                                                                 t->hits, t->hit_inst, perm, reordered);
@@ -1300,8 +1302,9 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
                 // the first two environment-shadow queues of a plain render are traced in bins too
                 // (720p 64 spp: 68.5 -> 67.5 ms; the radiance-cache frames gain nothing from it)
                 const uint32_t *s_reordered = nullptr;
-                const uint32_t *s_perm = (mode == MODE_PLAIN && depth <= 1 && !P.two_level)
-                                                 ? bin_rays(ctx, sc->bvh, t->s_ray, n, cnt_s, 0u, st, &s_reordered)
+                const vkg_bvh *s_bounds = sc->bvh ? sc->bvh : (sc->tlas ? &sc->tlas->top : nullptr);
+                const uint32_t *s_perm = (mode == MODE_PLAIN && depth <= 1)
+                                                 ? bin_rays(ctx, s_bounds, t->s_ray, n, cnt_s, 0u, st, &s_reordered)
                                                  : nullptr;
                 if(small_stack)
                     k_pt_shadow<single_scene, 64><<<grid, PT_THREADS, 0, st>>>(SS, t->s_ray, t->s_pid, t->s_contrib,
