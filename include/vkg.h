@@ -174,8 +174,26 @@ typedef struct vkg_material
     float dispersion;
     uint32_t tex_color, tex_normal, tex_emission, tex_ao_rough_metal, tex_transmission;
     uint32_t tex_diffuse_transmission, tex_diffuse_transmission_color;
-    uint32_t pad[2];
-} vkg_material; /* 176 B */
+    /* alpha masking / blending (material_struct_t color.a, blend_mode, alpha_cutoff,
+       RayBuilder.hpp:42, :87-89; the any-hit stages, raypipeline.slang:686-720 and
+       visibility_test.slang:45-87). A material with blend_mode VKG_BLEND_MASK or VKG_BLEND_BLEND that
+       is not a null surface is tested at every candidate hit: alpha times the colour texture's alpha
+       (level 0, at the hit's texture coordinates) is the coverage a. MASK: a < alpha_cutoff is no hit.
+       BLEND: a < xi is no hit, xi uniform in [0, 1): for a path's extension ray the first uniform of
+       the segment that shades the hit, the same for every candidate of the ray (the reference's
+       any_hit draws from a copy of the payload's stream); for shadow rays an independent uniform per
+       (ray, instance, triangle). Opaque materials ignore alpha. */
+    float alpha;        /* base colour alpha, [0, 1] (1) */
+    uint32_t blend_mode; /* VKG_BLEND_OPAQUE (0), VKG_BLEND_BLEND (1), VKG_BLEND_MASK (2): Material.hpp:32-37 */
+    float alpha_cutoff; /* MASK threshold (0.5) */
+    uint32_t pad[3];
+} vkg_material; /* 192 B */
+enum
+{
+    VKG_BLEND_OPAQUE = 0,
+    VKG_BLEND_BLEND = 1,
+    VKG_BLEND_MASK = 2
+};
 /* ---- analytic lights ----------------------------------------------------------------------
  * The reference's LightType (punctual_light.hpp:20-34); AREA is reserved for emissive triangles and
  * rejected here, as the reference leaves it out of the light list (PBRPathTracer.cpp:633-634). */
@@ -224,7 +242,7 @@ vkg_status vkg_light_convert(const vkg_light_source *src, const float rotation[9
 
 /* fills *m with the reference's defaults: base colour 1, roughness 1, ior 1.5, diffuse-transmission colour 1,
    iridescence ior 1.3 and thickness 400 nm, attenuation colour 1 at +inf distance, scatter colour 1,
-   everything else 0 */
+   alpha 1, alpha cutoff 0.5, no textures, everything else 0 */
 vkg_status vkg_material_defaults(vkg_material *m);
 vkg_status vkg_scene_cornell_counts(uint32_t num_spheres, uint32_t n, uint32_t *num_vertices, uint32_t *num_tris,
                                     uint32_t *num_materials);
@@ -595,7 +613,8 @@ vkg_status vkg_scene_camera_medium(const vkg_scene *scene, const float eye[3], u
  * vkg_gltf_load reads a .gltf (base64 or file buffers) or .glb file into meshes (one per triangle
  * primitive; float positions, uint32 indices, optional normals / texture coordinates / tangents),
  * instances (node placements, object -> world 3x4, mesh index in `blas`, material), materials
- * (vkg_material, texture slots indexing the asset's textures), textures (PNG images decoded to RGBA8)
+ * (vkg_material, texture slots indexing the asset's textures; alphaMode / alphaCutoff / the base
+ * colour's alpha into blend_mode / alpha_cutoff / alpha), textures (PNG images decoded to RGBA8)
  * and KHR_lights_punctual lights (vkg_light); those feed vkg_scene_create_instanced,
  * vkg_scene_set_normals / _texcoords / _tangents / _textures and vkg_scene_set_lights. Errors: a status and
  * the message in err (may be NULL). The mesh pointers stay valid until vkg_gltf_destroy. */
@@ -639,9 +658,11 @@ vkg_status vkg_gltf_destroy(vkg_gltf *g);
    ior and the thickness range's maximum (what the shader reads), the media fields and two_sided.
    The texture slots take the index of each texture whose TextureTypeBits flag is set (colour, normal,
    ao_rough_metal, emission, transmission, diffuse transmission and its colour; types.slang:35-51),
-   VKG_NO_TEXTURE otherwise. Blend mode / alpha cutoff and the textures the tracer does not sample
-   (displacement, thickness, clearcoat, sheen, iridescence) are dropped; *dropped (may be NULL)
-   counts the records that use any of them. Dispersion is read into vkg_material::dispersion. */
+   VKG_NO_TEXTURE otherwise. Colour alpha, blend mode and alpha cutoff are read into alpha,
+   blend_mode and alpha_cutoff (a blend mode other than 0-2 reads as opaque). The textures the tracer
+   does not sample (displacement, thickness, clearcoat, sheen, iridescence) are dropped; *dropped (may
+   be NULL) counts the records that use any of them or an unknown blend mode. Dispersion is read into
+   vkg_material::dispersion. */
 vkg_status vkg_materials_from_wire(const void *records, uint32_t n, vkg_material *out, uint32_t *dropped);
 /* per entry: where its triangles are in the mesh buffers */
 typedef struct vkg_wire_entry_info

@@ -439,17 +439,19 @@ static inline int tri_test(const float *r, const float o[3], const float d[3], i
     return 1;
 }
 
-/* cull: 0 none, 1 every back face, 2 back faces of triangles not flagged in twosided[prim] */
+/* cull: 0 none, 1 every back face, 2 back faces of triangles not flagged in twosided[prim]; accept:
+   candidate filter or NULL */
 static void trace_one_ex(const orc_bvh *b, const orc_ray *ray, int cull, const uint8_t *twosided, int any,
-                         orc_hit *hit, uint32_t *occ, uint64_t *nv, uint64_t *nt, orc_tri_fn fn, void *fn_ctx);
+                         orc_hit *hit, uint32_t *occ, uint64_t *nv, uint64_t *nt, orc_tri_fn fn, void *fn_ctx,
+                         orc_accept_fn accept, const void *acc_ctx);
 static void trace_one(const orc_bvh *b, const orc_ray *ray, int cull, int any, orc_hit *hit, uint32_t *occ,
                       uint64_t *nv, uint64_t *nt, orc_tri_fn fn, void *fn_ctx)
 {
-    trace_one_ex(b, ray, cull ? 1 : 0, NULL, any, hit, occ, nv, nt, fn, fn_ctx);
+    trace_one_ex(b, ray, cull ? 1 : 0, NULL, any, hit, occ, nv, nt, fn, fn_ctx, NULL, NULL);
 }
 
-void orc_bvh_trace1(const orc_bvh *b, const orc_ray *ray, int cull_mode, const uint8_t *twosided, int any,
-                    orc_hit *hit, uint32_t *occ)
+void orc_bvh_trace1_filter(const orc_bvh *b, const orc_ray *ray, int cull_mode, const uint8_t *twosided, int any,
+                           orc_accept_fn accept, const void *ctx, orc_hit *hit, uint32_t *occ)
 {
     uint64_t nv = 0, nt = 0;
     if(b->num_tris == 0)
@@ -458,11 +460,18 @@ void orc_bvh_trace1(const orc_bvh *b, const orc_ray *ray, int cull_mode, const u
         if(occ) *occ = 0;
         return;
     }
-    trace_one_ex(b, ray, cull_mode, twosided, any, hit, occ, &nv, &nt, NULL, NULL);
+    trace_one_ex(b, ray, cull_mode, twosided, any, hit, occ, &nv, &nt, NULL, NULL, accept, ctx);
+}
+
+void orc_bvh_trace1(const orc_bvh *b, const orc_ray *ray, int cull_mode, const uint8_t *twosided, int any,
+                    orc_hit *hit, uint32_t *occ)
+{
+    orc_bvh_trace1_filter(b, ray, cull_mode, twosided, any, NULL, NULL, hit, occ);
 }
 
 static void trace_one_ex(const orc_bvh *b, const orc_ray *ray, int cull_mode, const uint8_t *twosided, int any,
-                         orc_hit *hit, uint32_t *occ, uint64_t *nv, uint64_t *nt, orc_tri_fn fn, void *fn_ctx)
+                         orc_hit *hit, uint32_t *occ, uint64_t *nv, uint64_t *nt, orc_tri_fn fn, void *fn_ctx,
+                         orc_accept_fn accept, const void *acc_ctx)
 {
     float inv_d[3];
     int neg[3];
@@ -559,11 +568,13 @@ static void trace_one_ex(const orc_bvh *b, const orc_ray *ray, int cull_mode, co
                 if(!(t > ray->tmin && t < ray->tmax)) continue;
                 if(any)
                 {
+                    if(accept && !accept(acc_ctx, prim, u, v)) continue;
                     done = 1;
                     break;
                 }
                 if(t < best_t || (t == best_t && prim < best))
                 {
+                    if(accept && !accept(acc_ctx, prim, u, v)) continue;
                     best_t = t;
                     best = prim;
                     bu = u;

@@ -114,6 +114,11 @@ int orc_bvh_closest_hit_fn(const orc_bvh *b, const orc_ray *rays, uint32_t nray,
 /* single ray; cull_mode 0 none, 1 all back faces, 2 back faces of triangles with twosided[prim] == 0 */
 void orc_bvh_trace1(const orc_bvh *b, const orc_ray *ray, int cull_mode, const uint8_t *twosided, int any,
                     orc_hit *hit, uint32_t *occ);
+/* the same with a candidate filter (the any-hit stage): a candidate that would count (the nearest so
+   far, or any for any = 1) counts only if accept(ctx, prim, u, v) returns nonzero */
+typedef int (*orc_accept_fn)(const void *ctx, uint32_t prim, float u, float v);
+void orc_bvh_trace1_filter(const orc_bvh *b, const orc_ray *ray, int cull_mode, const uint8_t *twosided, int any,
+                           orc_accept_fn accept, const void *ctx, orc_hit *hit, uint32_t *occ);
 /* two-level queries: instances in input order, w2o [ninst][12], hits are 32-byte {prim, inst, t, u, v, pad} */
 int orc_tlas_closest_hit(const orc_bvh *const *blas, const float *w2o, const uint32_t *inst_blas, uint32_t ninst,
                          const orc_ray *rays, uint32_t nray, int cull, void *hits, int nthreads);
@@ -135,8 +140,13 @@ typedef struct {
     float dispersion; /* KHR_materials_dispersion: 20 / Abbe number (with transmission > 0) */
     uint32_t tex_color, tex_normal, tex_emission, tex_ao_rough_metal, tex_transmission;
     uint32_t tex_diffuse_transmission, tex_diffuse_transmission_color; /* 0xFFFFFFFF: none */
-    uint32_t pad[2];
-} orc_pt_material; /* same 176-byte layout as vkg_material */
+    /* coverage (material_struct_t color.a, blend_mode, alpha_cutoff, RayBuilder.hpp:42, :87-89):
+       blend_mode 0 opaque, 1 blend, 2 mask (Material.hpp:32-37) */
+    float alpha;
+    uint32_t blend_mode;
+    float alpha_cutoff;
+    uint32_t pad[3];
+} orc_pt_material; /* same 192-byte layout as vkg_material */
 
 /* a texture: size, level count, wrap modes (s: bits 0-7, t: bits 8-15; 0 repeat, 1 clamp to edge,
    2 mirrored repeat) and the first texel of each level in the scene's RGBA8 texel array; the same

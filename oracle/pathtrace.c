@@ -102,6 +102,20 @@ static uint32_t orc__any_dispersive(const orc_pt_scene *scene)
     return 0u;
 }
 
+/* a material whose candidate hits are tested for coverage: alpha mask (2) or blend (1), not a null
+   surface (raypipeline.slang:694-695) */
+static int orc__alpha_tested(const orc_pt_material *m)
+{
+    return (m->blend_mode == 1u || m->blend_mode == 2u) && !m->null_surface;
+}
+
+static uint32_t orc__any_alpha(const orc_pt_scene *scene)
+{
+    for(uint32_t i = 0; i < scene->nmat; ++i)
+        if(orc__alpha_tested(&scene->mats[i])) return 1u;
+    return 0u;
+}
+
 typedef struct {
     const orc_pt_scene *scene;
     const orc_bvh *bvh;
@@ -124,20 +138,50 @@ typedef struct {
     atomic_ullong ext, shadow;
     int fp64;
     uint32_t dispersion; /* a transmissive material disperses: one more uniform per segment */
+    uint32_t alpha;      /* a material is alpha-tested: candidate hits go through the coverage filter */
     uint32_t fork_depth; /* the variance split's fork segment (orc_pt_variance_split) */
     double *split;       /* [pixels][4] of orc_pt_variance_split */
 } orc_pt_job;
+
+/* ---- coverage of alpha-tested materials (any_hit, raypipeline.slang:686-720; visibility_test.slang:
+   45-87, :131-152): alpha x the colour texture's alpha at level 0; MASK rejects alpha < cutoff, BLEND
+   rejects alpha < xi. xi: for an extension ray the first uniform of the segment that shades the hit
+   (the path's generator is not advanced); for shadow rays one uniform per candidate hashed from the
+   path's generator state, the ray kind, the instance and the triangle (the GPU kernels' rule) */
+typedef struct {
+    const orc_pt_job *J;
+    uint32_t inst;         /* instanced scenes: the instance being traced */
+    double xi;             /* extension rays */
+    uint64_t key;          /* shadow rays: the path's generator state */
+    uint32_t salt;         /* 0: an extension ray; else the shadow ray's kind */
+    int pass_transmissive; /* light-NEE rays: transmissive surfaces are tinted, not tested */
+} orc_alpha_ctx;
+#define ORC_SALT_SHADOW 0x9E3779B9u
+#define ORC_SALT_LIGHT_SHADOW 0x7F4A7C15u
+
+static float orc_alpha_uniform(uint64_t key, uint32_t salt, uint32_t inst, uint32_t prim)
+{
+    uint32_t h = orc_xxhash32((uint32_t)key ^ salt, (uint32_t)(key >> 32));
+    h = orc_xxhash32(h, inst);
+    h = orc_xxhash32(h, prim);
+    return orc_u01(h);
+}
+
+/* defined after the estimator core (they sample textures) */
+static int f_alpha_accept(const void *ctx, uint32_t prim, float u, float v);
+static int d_alpha_accept(const orc_alpha_ctx *c, uint32_t prim, double u, double v);
 
 /* ---- FP32 twin hooks ------------------------------------------------------------------------ */
 static inline float f_draw_raw(orc_pcg32 *g) { return orc_u01(orc_pcg32_next(g)); }
 
 static void f_hit_raw(const orc_pt_job *J, float ox, float oy, float oz, float tmin, float dx, float dy, float dz,
-                      uint32_t *prim, uint32_t *inst, float *u, float *v, float *t)
+                      float xi, uint32_t *prim, uint32_t *inst, float *u, float *v, float *t)
 {
     *inst = 0;
     orc_ray r = {{ox, oy, oz}, tmin, {dx, dy, dz}, 1e4f};
     orc_hit h;
-    orc_bvh_trace1(J->bvh, &r, 2, J->twosided, 0, &h, NULL);
+    const orc_alpha_ctx ac = {J, 0u, (double)xi, 0u, 0u, 0};
+    orc_bvh_trace1_filter(J->bvh, &r, 2, J->twosided, 0, J->alpha ? f_alpha_accept : NULL, &ac, &h, NULL);
     *prim = h.prim;
     *u = h.u;
     *v = h.v;
@@ -148,15 +192,16 @@ static void f_hit_raw(const orc_pt_job *J, float ox, float oy, float oz, float t
    else transmission x base colour of every transmissive surface crossed, nearest first; null surfaces
    pass unattenuated */
 static void f_transmit_raw(const orc_pt_job *J, float ox, float oy, float oz, float tmin, float dx, float dy, float dz,
-                           float tmax, int cull, float T[3])
+                           float tmax, int cull, float T[3], uint64_t key)
 {
     T[0] = T[1] = T[2] = 1.f;
     float od[3] = {0.f, 0.f, 0.f};
+    const orc_alpha_ctx ac = {J, 0u, 0.0, key, ORC_SALT_LIGHT_SHADOW, 1};
     for(int k = 0;; ++k)
     {
         orc_ray r = {{ox, oy, oz}, tmin, {dx, dy, dz}, tmax};
         orc_hit h;
-        orc_bvh_trace1(J->bvh, &r, cull ? 1 : 0, NULL, 0, &h, NULL);
+        orc_bvh_trace1_filter(J->bvh, &r, cull ? 1 : 0, NULL, 0, J->alpha ? f_alpha_accept : NULL, &ac, &h, NULL);
         if(h.prim == ORC_MISS) break;
         const uint32_t mi = J->scene->tri_mat[h.prim];
         const orc_pt_material *m = &J->scene->mats[mi];
@@ -193,11 +238,12 @@ static void f_transmit_raw(const orc_pt_job *J, float ox, float oy, float oz, fl
 }
 
 static int f_occluded_raw(const orc_pt_job *J, float ox, float oy, float oz, float tmin, float dx, float dy, float dz,
-                          int cull)
+                          int cull, uint64_t key)
 {
     orc_ray r = {{ox, oy, oz}, tmin, {dx, dy, dz}, 1e4f};
     uint32_t occ = 0;
-    orc_bvh_trace1(J->bvh, &r, cull ? 1 : 0, NULL, 1, NULL, &occ);
+    const orc_alpha_ctx ac = {J, 0u, 0.0, key, ORC_SALT_SHADOW, 0};
+    orc_bvh_trace1_filter(J->bvh, &r, cull ? 1 : 0, NULL, 1, J->alpha ? f_alpha_accept : NULL, &ac, NULL, &occ);
     return (int)occ;
 }
 
@@ -236,7 +282,7 @@ static inline float exp_scale_f(uint8_t e)
    (tmin, tmax); two-sidedness per triangle (twosided[prim]) or for the whole mesh (all_twosided) */
 static int d_trace_bvh(const orc_bvh *b, const uint8_t *twosided, int all_twosided, const double o[3], double tmin,
                        const double d[3], double tmax, int cull_mode, int any, uint32_t *prim_out, double *t_out,
-                       double *u_out, double *v_out)
+                       double *u_out, double *v_out, const orc_alpha_ctx *ac)
 {
     *prim_out = ORC_MISS;
     if(b->num_tris == 0) return 0;
@@ -297,9 +343,14 @@ static int d_trace_bvh(const orc_bvh *b, const uint8_t *twosided, int all_twosid
                 if(vv < 0.0 || uu + vv > 1.0) continue;
                 double t = (e2[0] * q[0] + e2[1] * q[1] + e2[2] * q[2]) * id;
                 if(!(t > tmin && t < tmax)) continue;
-                if(any) return 1;
+                if(any)
+                {
+                    if(ac && !d_alpha_accept(ac, prim, uu, vv)) continue;
+                    return 1;
+                }
                 if(t < best_t)
                 {
+                    if(ac && !d_alpha_accept(ac, prim, uu, vv)) continue;
                     best_t = t;
                     best = prim;
                     bu = uu;
@@ -316,9 +367,10 @@ static int d_trace_bvh(const orc_bvh *b, const uint8_t *twosided, int all_twosid
 }
 
 static int d_trace(const orc_pt_job *J, const double o[3], double tmin, const double d[3], double tmax, int cull_mode,
-                   int any, uint32_t *prim_out, double *t_out, double *u_out, double *v_out)
+                   int any, uint32_t *prim_out, double *t_out, double *u_out, double *v_out, const orc_alpha_ctx *ac)
 {
-    return d_trace_bvh(J->bvh, J->twosided, 0, o, tmin, d, tmax, cull_mode, any, prim_out, t_out, u_out, v_out);
+    return d_trace_bvh(J->bvh, J->twosided, 0, o, tmin, d, tmax, cull_mode, any, prim_out, t_out, u_out, v_out,
+                       J->alpha ? ac : NULL);
 }
 
 /* ---- instanced scenes (FP64) ----------------------------------------------------------------
@@ -515,7 +567,7 @@ static int slab(const double lo[3], const double hi[3], const double o[3], const
 
 static int d_trace_inst(const orc_pt_job *J, const double o[3], double tmin, const double d[3], double tmax,
                         int cull_mode, int any, uint32_t *prim_out, uint32_t *inst_out, double *t_out, double *u_out,
-                        double *v_out)
+                        double *v_out, const orc_alpha_ctx *ac)
 {
     const orc_pt_instances *I = J->inst;
     const inst_bvh *B = (const inst_bvh *)J->ibvh;
@@ -553,8 +605,17 @@ static int d_trace_inst(const orc_pt_job *J, const double o[3], double tmin, con
             const uint32_t m = I->inst_mesh[k];
             uint32_t prim;
             double t, u, v;
+            /* the coverage filter for an instance of an alpha-tested material */
+            orc_alpha_ctx ik;
+            const orc_alpha_ctx *iac = NULL;
+            if(ac && J->alpha && orc__alpha_tested(&J->scene->mats[I->inst_mat[k]]))
+            {
+                ik = *ac;
+                ik.inst = k;
+                iac = &ik;
+            }
             if(!d_trace_bvh(I->mesh_bvh[m], NULL, B->mesh_unculled[m], oo, tmin, dd, best_t, cull_mode, any, &prim, &t,
-                            &u, &v))
+                            &u, &v, iac))
                 continue;
             if(any) return 1;
             best_t = t;
@@ -597,36 +658,39 @@ static void d_env_sample_raw(const orc_pt_env *e, double u0, double u1, double u
 }
 
 static void d_hit_raw(const orc_pt_job *J, double ox, double oy, double oz, double tmin, double dx, double dy,
-                      double dz, uint32_t *prim, uint32_t *inst, double *u, double *v, double *t)
+                      double dz, double xi, uint32_t *prim, uint32_t *inst, double *u, double *v, double *t)
 {
     double o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz};
     *u = *v = 0;
     *t = 1e4;
     *inst = 0;
-    if(J->inst) d_trace_inst(J, o, tmin, d, 1e4, 2, 0, prim, inst, t, u, v);
-    else d_trace(J, o, tmin, d, 1e4, 2, 0, prim, t, u, v);
+    const orc_alpha_ctx ac = {J, 0u, xi, 0u, 0u, 0};
+    if(J->inst) d_trace_inst(J, o, tmin, d, 1e4, 2, 0, prim, inst, t, u, v, &ac);
+    else d_trace(J, o, tmin, d, 1e4, 2, 0, prim, t, u, v, &ac);
 }
 
 static int d_occluded_raw(const orc_pt_job *J, double ox, double oy, double oz, double tmin, double dx, double dy,
-                          double dz, int cull)
+                          double dz, int cull, uint64_t key)
 {
     double o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz}, u, v, t;
     uint32_t prim, inst;
-    if(J->inst) return d_trace_inst(J, o, tmin, d, 1e4, cull ? 1 : 0, 1, &prim, &inst, &t, &u, &v);
-    return d_trace(J, o, tmin, d, 1e4, cull ? 1 : 0, 1, &prim, &t, &u, &v);
+    const orc_alpha_ctx ac = {J, 0u, 0.0, key, ORC_SALT_SHADOW, 0};
+    if(J->inst) return d_trace_inst(J, o, tmin, d, 1e4, cull ? 1 : 0, 1, &prim, &inst, &t, &u, &v, &ac);
+    return d_trace(J, o, tmin, d, 1e4, cull ? 1 : 0, 1, &prim, &t, &u, &v, &ac);
 }
 
 static void d_transmit_raw(const orc_pt_job *J, double ox, double oy, double oz, double tmin, double dx, double dy,
-                           double dz, double tmax, int cull, double T[3])
+                           double dz, double tmax, int cull, double T[3], uint64_t key)
 {
     double o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz}, od[3] = {0, 0, 0};
     T[0] = T[1] = T[2] = 1.0;
+    const orc_alpha_ctx ac = {J, 0u, 0.0, key, ORC_SALT_LIGHT_SHADOW, 1};
     for(int k = 0;; ++k)
     {
         uint32_t prim, inst = 0;
         double t, u, v;
-        int hit = J->inst ? d_trace_inst(J, o, tmin, d, tmax, cull ? 1 : 0, 0, &prim, &inst, &t, &u, &v)
-                          : d_trace(J, o, tmin, d, tmax, cull ? 1 : 0, 0, &prim, &t, &u, &v);
+        int hit = J->inst ? d_trace_inst(J, o, tmin, d, tmax, cull ? 1 : 0, 0, &prim, &inst, &t, &u, &v, &ac)
+                          : d_trace(J, o, tmin, d, tmax, cull ? 1 : 0, 0, &prim, &t, &u, &v, &ac);
         if(!hit) break;
         const uint32_t mat = J->inst ? J->inst->inst_mat[inst] : J->scene->tri_mat[prim];
         const orc_pt_material *m = &J->scene->mats[mat];
@@ -701,6 +765,10 @@ static void d_transmit_raw(const orc_pt_job *J, double ox, double oy, double oz,
 #define RFLOOR(x) floorf(x)
 #define RATAN(x) atanf(x)
 #include "pt_core.inc"
+static int f_alpha_accept(const void *ctx, uint32_t prim, float u, float v)
+{
+    return f_alpha_core((const orc_alpha_ctx *)ctx, prim, u, v);
+}
 #undef REAL
 #undef SFX
 #undef RSQRT
@@ -745,6 +813,7 @@ static void d_transmit_raw(const orc_pt_job *J, double ox, double oy, double oz,
 #define RFLOOR(x) floor(x)
 #define RATAN(x) atan(x)
 #include "pt_core.inc"
+static int d_alpha_accept(const orc_alpha_ctx *c, uint32_t prim, double u, double v) { return d_alpha_core(c, prim, u, v); }
 
 void orc_sun_light(const float color[3], float intensity, const float spherical_coords[2], float angular_size,
                    orc_pt_light *out)
@@ -874,6 +943,7 @@ int orc_pt_render(int fp64, const orc_pt_scene *scene, const orc_bvh *bvh, const
     memset(&J, 0, sizeof(J));
     J.scene = scene;
     J.dispersion = orc__any_dispersive(scene);
+    J.alpha = orc__any_alpha(scene);
     J.bvh = bvh;
     J.env = env;
     J.cam = cam;
@@ -975,6 +1045,7 @@ int orc_pt_variance_split(const orc_pt_scene *scene, const orc_bvh *bvh, const o
     memset(&J, 0, sizeof(J));
     J.scene = scene;
     J.dispersion = orc__any_dispersive(scene);
+    J.alpha = orc__any_alpha(scene);
     J.bvh = bvh;
     J.env = env;
     J.cam = cam;
@@ -1028,6 +1099,7 @@ int orc_pt_render_instanced(const orc_pt_scene *scene, const orc_pt_instances *i
     memset(&J, 0, sizeof(J));
     J.scene = scene;
     J.dispersion = orc__any_dispersive(scene);
+    J.alpha = orc__any_alpha(scene);
     J.inst = inst;
     J.ibvh = B;
     J.env = env;

@@ -87,6 +87,8 @@ def test_materials(tmp_path):
                         "KHR_materials_iridescence": {"iridescenceFactor": 0.8, "iridescenceIOR": 1.4,
                                                       "iridescenceThicknessMinimum": 150,
                                                       "iridescenceThicknessMaximum": 520}}},
+        {"pbrMetallicRoughness": {"baseColorFactor": [1, 1, 1, 0.3]}, "alphaMode": "MASK", "alphaCutoff": 0.25},
+        {"alphaMode": "BLEND"},
         {},
     ]
     path = tmp_path / "m.gltf"
@@ -104,8 +106,12 @@ def test_materials(tmp_path):
     assert m[1]["iridescence"] == np.float32(0.8) and m[1]["iridescence_ior"] == np.float32(1.4)
     assert m[1]["iridescence_thickness"] == 520  # the range's maximum, as the shader reads it
     assert m[0]["iridescence"] == 0 and m[0]["iridescence_ior"] == np.float32(1.3)
-    # glTF defaults: metallic 1, roughness 1, white
-    assert m[2]["metalness"] == 1 and m[2]["roughness"] == 1 and np.all(m[2]["base_color"] == 1)
+    # alphaMode / alphaCutoff / the base colour's alpha (the reference's gltf.cpp:323-326)
+    assert (m[2]["blend_mode"], m[2]["alpha"], m[2]["alpha_cutoff"]) == (2, np.float32(0.3), np.float32(0.25))
+    assert (m[3]["blend_mode"], m[3]["alpha"], m[3]["alpha_cutoff"]) == (1, 1.0, 0.5)
+    # glTF defaults: metallic 1, roughness 1, white, opaque
+    assert m[4]["metalness"] == 1 and m[4]["roughness"] == 1 and np.all(m[4]["base_color"] == 1)
+    assert (m[4]["blend_mode"], m[4]["alpha"], m[4]["alpha_cutoff"]) == (0, 1.0, 0.5)
     assert list(a["instances"]["material"]) == [0, 1, 0]  # no material -> index 0, as the reference
 
 

@@ -20,7 +20,9 @@ pytestmark = pytest.mark.gpu
 def wire_materials(mats):
     w = np.zeros(len(mats), MATERIAL_STRUCT_T)
     w["color"][:, :3] = mats["base_color"]
-    w["color"][:, 3] = 1.0
+    w["color"][:, 3] = mats["alpha"]
+    w["blend_mode"] = mats["blend_mode"]
+    w["alpha_cutoff"] = mats["alpha_cutoff"]
     w["emission"][:, :3] = mats["emission"]
     w["emission"][:, 3] = 1.0
     for theirs, ours in (("metalness", "metalness"), ("roughness", "roughness"), ("transmission", "transmission"),

@@ -61,8 +61,11 @@ def test_materials_from_wire():
     w["albedo_index"][2] = 5  # an index without its flag: no texture
     w["texture_type_flags"][1] = 0x80  # a clearcoat texture: not sampled, counted as dropped
     w["dispersion"][4] = 0.2
+    w["blend_mode"] = (0, 2, 1, 0, 7)  # opaque, mask, blend; 7 is no BlendMode: opaque, counted as dropped
     m, dropped = materials_from_wire(w.tobytes())
-    assert dropped == 1  # the clearcoat texture; the sampled textures and dispersion are read
+    assert dropped == 2  # the clearcoat texture and the unknown blend mode; the rest is read
+    assert list(m["blend_mode"]) == [0, 2, 1, 0, 0]
+    assert np.array_equal(m["alpha"], w["color"][:, 3]) and np.array_equal(m["alpha_cutoff"], w["alpha_cutoff"])
     NO = 0xFFFFFFFF
     assert [int(m[f][3]) for f in ("tex_color", "tex_normal", "tex_emission", "tex_ao_rough_metal",
                                    "tex_transmission", "tex_diffuse_transmission",

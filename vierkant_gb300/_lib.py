@@ -25,6 +25,7 @@ TEXCOORD_FLOAT2 = 0
 TEXCOORD_HALF2 = 1
 WRAP_REPEAT, WRAP_CLAMP_TO_EDGE, WRAP_MIRRORED_REPEAT = 0, 1, 2
 NO_TEXTURE = 0xFFFFFFFF
+BLEND_OPAQUE, BLEND_BLEND, BLEND_MASK = 0, 1, 2
 
 
 RNG_PCG32, RNG_REFERENCE = 0, 1
@@ -64,7 +65,8 @@ class vkg_material(C.Structure):
                 ("null_surface", C.c_uint32), ("dispersion", C.c_float), ("tex_color", C.c_uint32),
                 ("tex_normal", C.c_uint32), ("tex_emission", C.c_uint32), ("tex_ao_rough_metal", C.c_uint32),
                 ("tex_transmission", C.c_uint32), ("tex_diffuse_transmission", C.c_uint32),
-                ("tex_diffuse_transmission_color", C.c_uint32), ("pad", C.c_uint32 * 2)]
+                ("tex_diffuse_transmission_color", C.c_uint32), ("alpha", C.c_float),
+                ("blend_mode", C.c_uint32), ("alpha_cutoff", C.c_float), ("pad", C.c_uint32 * 3)]
 
 
 class vkg_texture_desc(C.Structure):

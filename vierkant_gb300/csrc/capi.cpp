@@ -730,6 +730,9 @@ vkg_status vkg_material_defaults(vkg_material *m)
     m->attenuation_distance = std::numeric_limits<float>::infinity();
     m->tex_color = m->tex_normal = m->tex_emission = m->tex_ao_rough_metal = m->tex_transmission = VKG_NO_TEXTURE;
     m->tex_diffuse_transmission = m->tex_diffuse_transmission_color = VKG_NO_TEXTURE;
+    m->alpha = 1.f;
+    m->blend_mode = VKG_BLEND_OPAQUE;
+    m->alpha_cutoff = 0.5f;
     return VKG_OK;
 }
 

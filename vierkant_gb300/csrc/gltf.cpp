@@ -667,6 +667,13 @@ struct loader
         };
         const jv *pbr = m.get("pbrMetallicRoughness");
         rd(pbr, "baseColorFactor", r.base_color, 3);
+        float bc[4] = {r.base_color[0], r.base_color[1], r.base_color[2], 1.f};
+        rd(pbr, "baseColorFactor", bc, 4);
+        r.alpha = bc[3];
+        // alphaMode (gltf.cpp:323-326 of the reference): OPAQUE (default), BLEND, MASK; alphaCutoff 0.5
+        if(const std::string *am = m.str("alphaMode"))
+            r.blend_mode = *am == "BLEND" ? VKG_BLEND_BLEND : (*am == "MASK" ? VKG_BLEND_MASK : VKG_BLEND_OPAQUE);
+        r.alpha_cutoff = (float)m.num("alphaCutoff", 0.5);
         r.metalness = pbr ? clampf(pbr->num("metallicFactor", 1.0), 0, 1) : 1.f;
         r.roughness = pbr ? (float)pbr->num("roughnessFactor", 1.0) : 1.f;
         float em[3] = {0, 0, 0};

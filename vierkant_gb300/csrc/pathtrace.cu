@@ -242,6 +242,11 @@ vkg_status check_material_values(vkg_ctx *ctx, const vkg_material *d_mats, uint3
             return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
                              "%s: material %u: attenuation colour in (0, 1], scatter factor / colour in [0, 1], "
                              "phase g in (-1, 1)", fn, i);
+        if(m.blend_mode > VKG_BLEND_MASK ||
+           (material_alpha_tested(m) && !(std::isfinite(m.alpha) && std::isfinite(m.alpha_cutoff))))
+            return set_error(ctx, VKG_ERR_INVALID_ARGUMENT,
+                             "%s: material %u: blend_mode must be VKG_BLEND_OPAQUE / _BLEND / _MASK, alpha and "
+                             "alpha_cutoff finite", fn, i);
         *any_transmissive = *any_transmissive || m.transmission > 0.f || m.null_surface;
         *any_full = *any_full || material_full(m);
         media[i] = medium_from_material(m);
@@ -471,7 +476,11 @@ vkg_status vkg_scene_create(vkg_ctx *ctx, const vkg_scene_desc *d, vkg_scene **o
         vkg_scene_destroy(ctx, sc);
         return s;
     }
-    for(const vkg_material &m: sc->h_mats) sc->any_dispersion = sc->any_dispersion || material_dispersive(m);
+    for(const vkg_material &m: sc->h_mats)
+    {
+        sc->any_dispersion = sc->any_dispersion || material_dispersive(m);
+        sc->any_alpha = sc->any_alpha || material_alpha_tested(m);
+    }
     vkg_bvh_build_options opt{d->leaf_max};
     vkg_status s = vkg_bvh_build(ctx, sc->xyz, d->num_vertices, sc->idx, d->num_tris, &opt, &sc->bvh, stream);
     if(s != VKG_OK)
@@ -828,7 +837,11 @@ vkg_status vkg_scene_create_instanced(vkg_ctx *ctx, const vkg_instanced_scene_de
                                                  &sc->h_media, &sc->h_mats);
        s != VKG_OK)
         return fail(s);
-    for(const vkg_material &m: sc->h_mats) sc->any_dispersion = sc->any_dispersion || material_dispersive(m);
+    for(const vkg_material &m: sc->h_mats)
+    {
+        sc->any_dispersion = sc->any_dispersion || material_dispersive(m);
+        sc->any_alpha = sc->any_alpha || material_alpha_tested(m);
+    }
     std::vector<mesh_ref> refs(d->num_meshes);
     uint64_t tris = 0;
     for(uint32_t m = 0; m < d->num_meshes && e == cudaSuccess; ++m)
@@ -1194,7 +1207,9 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
     uint32_t *cnt_q = t->counters + 3, *cnt_rec = t->counters + 4, *cnt_b = t->counters + 5, *cnt_work = t->counters + 6;
     // instanced scenes: grid-stride two-level tracers (faster on the stress scene: 274 vs 252 Mrays/s);
     // VKG_TL_KERNEL=persistent selects the refilling persistent ones
-    const bool tl_persistent = sc->tlas && tl_persistent_selected() && !has_media;
+    const bool tl_persistent = sc->tlas && tl_persistent_selected() && !has_media && !sc->any_alpha;
+    // alpha-tested materials: the queue tracers with the coverage filter (alpha_filter)
+    const bool alpha = sc->any_alpha;
     const bool bin_materials = pt_binning_selected();
     // a 64-entry traversal stack serves BVHs up to 10 levels deep (7 (depth - 1) + 1 entries)
     const bool small_stack = sc->bvh && sc->bvh->depth <= 10;
@@ -1251,7 +1266,13 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
                 const vkg_bvh *bounds = sc->bvh ? sc->bvh : (sc->tlas ? &sc->tlas->top : nullptr);
                 const uint32_t *perm = depth == 1 ? bin_rays(ctx, bounds, t->q_ray[a], n, cnt_in, 0u, st, &reordered)
                                                   : nullptr;
-                if(small_stack)
+                if(alpha && small_stack)
+                    k_pt_extend<single_scene, 64, true><<<grid, PT_THREADS, 0, st>>>(
+                            SS, t->q_ray[a], t->q_pid[a], cnt_in, t->hits, t->hit_inst, perm, reordered, t->rng, depth);
+                else if(alpha)
+                    k_pt_extend<single_scene, (int)TRAVERSAL_STACK, true><<<grid, PT_THREADS, 0, st>>>(
+                            SS, t->q_ray[a], t->q_pid[a], cnt_in, t->hits, t->hit_inst, perm, reordered, t->rng, depth);
+                else if(small_stack)
                     k_pt_extend<single_scene, 64><<<grid, PT_THREADS, 0, st>>>(SS, t->q_ray[a], t->q_pid[a], cnt_in,
                                                                                 t->hits, t->hit_inst, perm, reordered);
                 else
@@ -1306,7 +1327,13 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
                 const uint32_t *s_perm = (mode == MODE_PLAIN && depth <= 1)
                                                  ? bin_rays(ctx, s_bounds, t->s_ray, n, cnt_s, 0u, st, &s_reordered)
                                                  : nullptr;
-                if(small_stack)
+                if(alpha && small_stack)
+                    k_pt_shadow<single_scene, 64, true><<<grid, PT_THREADS, 0, st>>>(
+                            SS, t->s_ray, t->s_pid, t->s_contrib, cnt_s, t->radiance, s_perm, s_reordered, t->rng);
+                else if(alpha)
+                    k_pt_shadow<single_scene, (int)TRAVERSAL_STACK, true><<<grid, PT_THREADS, 0, st>>>(
+                            SS, t->s_ray, t->s_pid, t->s_contrib, cnt_s, t->radiance, s_perm, s_reordered, t->rng);
+                else if(small_stack)
                     k_pt_shadow<single_scene, 64><<<grid, PT_THREADS, 0, st>>>(SS, t->s_ray, t->s_pid, t->s_contrib,
                                                                                 cnt_s, t->radiance, s_perm, s_reordered);
                 else
@@ -1316,7 +1343,12 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
             }
             if(cnt_l && !empty)
             {
-                if(small_stack)
+                if(alpha && small_stack)
+                    k_pt_light_shadow<single_scene, 64, true><<<grid, PT_THREADS, 0, st>>>(SS, lq, t->radiance, t->rng);
+                else if(alpha)
+                    k_pt_light_shadow<single_scene, (int)TRAVERSAL_STACK, true>
+                            <<<grid, PT_THREADS, 0, st>>>(SS, lq, t->radiance, t->rng);
+                else if(small_stack)
                     k_pt_light_shadow<single_scene, 64><<<grid, PT_THREADS, 0, st>>>(SS, lq, t->radiance);
                 else
                     k_pt_light_shadow<<<grid, PT_THREADS, 0, st>>>(SS, lq, t->radiance);

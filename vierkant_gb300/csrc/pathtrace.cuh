@@ -59,6 +59,13 @@ __host__ __device__ inline bool material_unculled(const vkg_material &m)
            (m.attenuation_distance > 0.f && m.attenuation_distance < 3.0e38f);
 }
 
+// a material whose candidate hits are tested for coverage (alpha mask or blend; null surfaces are
+// not, raypipeline.slang:694-695)
+__host__ __device__ inline bool material_alpha_tested(const vkg_material &m)
+{
+    return (m.blend_mode == VKG_BLEND_MASK || m.blend_mode == VKG_BLEND_BLEND) && m.null_surface == 0u;
+}
+
 // a material that uses a lobe beyond metal-roughness (the shade kernels' FULL variant)
 __host__ __device__ inline bool material_full(const vkg_material &m)
 {

@@ -16,6 +16,7 @@
 
 #include <cmath>
 #include <limits>
+#include <type_traits>
 #include <vector>
 
 namespace vkg
@@ -60,6 +61,7 @@ struct vkg_scene
     bool any_transmissive = false;  // a material with transmission > 0 or a null surface (light shadow rays pass)
     bool any_full = false;          // a material with a lobe beyond metal-roughness
     bool any_dispersion = false;    // a transmissive material with dispersion > 0
+    bool any_alpha = false;         // an alpha-masked or blended material (material_alpha_tested)
     vkg::medium_rec *d_media = nullptr; // per-material medium records, when a material bounds a medium
     std::vector<vkg::medium_rec> h_media; // the same records for every material (host)
     std::vector<vkg_material> h_mats;     // host copy of the materials
@@ -202,6 +204,92 @@ struct job_table
     __device__ __forceinline__ uint64_t inc(uint32_t pid) const { return pinc[pid]; }
 };
 
+// Coverage of alpha-masked / blended materials at a candidate hit: the traversal's candidate filter
+// (no_filter, traverse.cuh) for the path tracer's queries. The reference tests coverage in its any-hit
+// stages (raypipeline.slang:686-720 for the closest-hit trace, visibility_test.slang:45-87 and
+// :131-152 for shadow rays): alpha = the material's alpha times the colour texture's alpha sampled at
+// level 0 at the candidate's texture coordinates; MASK rejects alpha < alpha_cutoff, BLEND rejects
+// alpha < xi. xi: for an extension ray the first uniform of the segment that will shade the hit,
+// drawn from a copy of the path's generator (any_hit reads a copy of the payload's stream, so every
+// candidate of the ray sees the same value and the path's stream does not move); for shadow rays,
+// whose reference stream advances once per tested candidate in the hardware's traversal order, an
+// independent uniform per candidate hashed from the path's generator state, the ray kind, the
+// instance and the triangle, so that the answer does not depend on the order of the traversal.
+constexpr uint32_t ALPHA_SALT_SHADOW = 0x9E3779B9u;      // the environment-NEE shadow queue
+constexpr uint32_t ALPHA_SALT_LIGHT_SHADOW = 0x7F4A7C15u; // the light-NEE shadow queue
+
+__device__ __forceinline__ float alpha_uniform(uint64_t key, uint32_t salt, uint32_t inst, uint32_t prim)
+{
+    uint32_t h = xxhash32((uint32_t)key ^ salt, (uint32_t)(key >> 32));
+    h = xxhash32(h, inst);
+    h = xxhash32(h, prim);
+    return u01(h);
+}
+
+// the first uniform the shade kernel will draw for segment `depth` of a path whose generator state is
+// `state` (PCG32, or the reference's chained streams), without advancing it
+__device__ __forceinline__ float peek_uniform(const pt_params &P, uint64_t state, uint64_t inc, uint32_t depth)
+{
+    if(P.ref_rng)
+    {
+        uint32_t l = xxhash32((uint32_t)state, depth);
+        return rnd(l);
+    }
+    pcg32 g{state, inc};
+    return u01(pcg32_next(g));
+}
+
+struct alpha_filter
+{
+    static constexpr bool active = true;
+    const pt_params *P;
+    uint64_t key;     // shadow rays: the path's generator state
+    float xi;         // extension rays: the segment's first uniform
+    uint32_t salt;    // 0: an extension ray (xi, and disable_material applies); else the shadow ray's kind
+    bool pass_transmissive; // light-NEE rays: transmissive surfaces are tinted, never tested
+
+    __device__ __forceinline__ bool tests_material(uint32_t mat) const { return material_alpha_tested(P->mats[mat]); }
+
+    __device__ bool accept(uint32_t inst, uint32_t prim, float bu, float bv) const
+    {
+        const pt_params &Q = *P;
+        uint32_t mat;
+        const float *tuv = Q.uv;
+        const uint32_t *idx = Q.idx;
+        if(Q.two_level)
+        {
+            const inst_rec *R = Q.tl_by_id + inst;
+            mat = __ldg(&R->material);
+            const mesh_ref &M = Q.meshes[__ldg(&R->blas)];
+            tuv = M.uv;
+            idx = M.idx;
+        }
+        else
+            mat = __ldg(&Q.tri_mat[prim]);
+        const vkg_material &m = Q.mats[mat];
+        if(!material_alpha_tested(m) || (pass_transmissive && m.transmission > 0.f)) return true;
+        float a;
+        if(salt == 0u && Q.disable_material) a = 1.f; // the closest-hit stage's grey override
+        else
+        {
+            a = m.alpha;
+            if(m.tex_color < Q.num_textures && tuv)
+            {
+                const uint32_t i0 = __ldg(&idx[3 * (size_t)prim]), i1 = __ldg(&idx[3 * (size_t)prim + 1]),
+                               i2 = __ldg(&idx[3 * (size_t)prim + 2]);
+                const float w0 = 1.f - bu - bv;
+                const float u = __ldg(&tuv[2 * (size_t)i0]) * w0 + __ldg(&tuv[2 * (size_t)i1]) * bu +
+                                __ldg(&tuv[2 * (size_t)i2]) * bv;
+                const float v = __ldg(&tuv[2 * (size_t)i0 + 1]) * w0 + __ldg(&tuv[2 * (size_t)i1 + 1]) * bu +
+                                __ldg(&tuv[2 * (size_t)i2 + 1]) * bv;
+                a *= tex_bilinear(Q.tex[m.tex_color], Q.texels, 0u, u, v).w;
+            }
+        }
+        if(m.blend_mode == VKG_BLEND_MASK) return !(a < m.alpha_cutoff);
+        return !(a < (salt ? alpha_uniform(key, salt, Q.two_level ? inst : 0u, prim) : xi));
+    }
+};
+
 // camera ray through pixel (x, y) jittered by (jx, jy): PBRPathTracer's pinhole (raypipeline.slang:58-89)
 __device__ __forceinline__ void camera_ray(const vkg_camera &c, uint32_t x, uint32_t y, float jx, float jy,
                                            float4 *o)
@@ -290,11 +378,14 @@ __global__ void __launch_bounds__(PT_THREADS)
     if(blockIdx.x == 0 && threadIdx.x == 0) counters[0] = n;
 }
 
-template<class J, int STACK = (int)TRAVERSAL_STACK>
+// ALPHA: the scene has alpha-tested materials (alpha_filter); rng and depth then give each ray its
+// segment's first uniform
+template<class J, int STACK = (int)TRAVERSAL_STACK, bool ALPHA = false>
 __global__ void __launch_bounds__(PT_THREADS, STACK <= 64 ? 8 : 6) // 64 / 85 registers
         k_pt_extend(J S, const vkg_ray *__restrict__ q_ray, const uint32_t *__restrict__ q_pid,
                     const uint32_t *__restrict__ count, vkg_hit *__restrict__ hits, uint32_t *__restrict__ hit_inst,
-                    const uint32_t *__restrict__ perm = nullptr, const uint32_t *__restrict__ reordered = nullptr)
+                    const uint32_t *__restrict__ perm = nullptr, const uint32_t *__restrict__ reordered = nullptr,
+                    const uint64_t *__restrict__ rng = nullptr, uint32_t depth = 0)
 {
     const uint32_t n = *count;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -303,21 +394,25 @@ __global__ void __launch_bounds__(PT_THREADS, STACK <= 64 ? 8 : 6) // 64 / 85 re
     for(uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride)
     {
         const uint32_t i = perm ? __ldg(perm + j) : j;
-        const pt_params &P = S.params(J::per_path ? q_pid[i] : 0u);
+        const uint32_t pid = (J::per_path || ALPHA) ? q_pid[i] : 0u;
+        const pt_params &P = S.params(J::per_path ? pid : 0u);
         const float4 *rp = reinterpret_cast<const float4 *>(q_ray + i);
         const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
+        using F = std::conditional_t<ALPHA, alpha_filter, no_filter>;
+        F f{};
+        if constexpr(ALPHA) f = alpha_filter{&P, 0ull, peek_uniform(P, rng[pid], S.inc(pid), depth), 0u, false};
         if(P.two_level)
         {
-            const tlas_result r = trace_tlas<false>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y,
-                                                    r1.z, r1.w, CULL_BACK_UNLESS_TWOSIDED);
+            const tlas_result r = trace_tlas<false, F>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z, r0.w, r1.x,
+                                                       r1.y, r1.z, r1.w, CULL_BACK_UNLESS_TWOSIDED, f);
             reinterpret_cast<uint4 *>(hits)[i] =
                     make_uint4(r.prim, __float_as_uint(r.t), __float_as_uint(r.u), __float_as_uint(r.v));
             hit_inst[i] = r.inst;
             continue;
         }
         unsigned long long v = 0, t = 0;
-        trace_result r = trace_ray<false, false, STACK>(P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z,
-                                                        r1.w, CULL_BACK_UNLESS_TWOSIDED, v, t, nullptr);
+        trace_result r = trace_ray<false, false, STACK, F>(P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z,
+                                                           r1.w, CULL_BACK_UNLESS_TWOSIDED, v, t, nullptr, f);
         reinterpret_cast<uint4 *>(hits)[i] =
                 make_uint4(r.prim, __float_as_uint(r.t), __float_as_uint(r.u), __float_as_uint(r.v));
     }
@@ -1101,12 +1196,13 @@ __global__ void __launch_bounds__(PT_THREADS)
     }
 }
 
-template<class J, int STACK = (int)TRAVERSAL_STACK>
+// ALPHA: alpha-tested materials (alpha_filter), each candidate's uniform hashed from rng[path]
+template<class J, int STACK = (int)TRAVERSAL_STACK, bool ALPHA = false>
 __global__ void __launch_bounds__(PT_THREADS, STACK <= 64 ? 8 : 6) // 64 / 85 registers
         k_pt_shadow(J S, const vkg_ray *__restrict__ s_ray, const uint32_t *__restrict__ s_pid,
                     const float4 *__restrict__ s_contrib, const uint32_t *__restrict__ count,
                     float4 *__restrict__ radiance, const uint32_t *__restrict__ perm = nullptr,
-                    const uint32_t *__restrict__ reordered = nullptr)
+                    const uint32_t *__restrict__ reordered = nullptr, const uint64_t *__restrict__ rng = nullptr)
 {
     const uint32_t n = *count;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -1120,16 +1216,19 @@ __global__ void __launch_bounds__(PT_THREADS, STACK <= 64 ? 8 : 6) // 64 / 85 re
         const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
         const float4 c = s_contrib[i];
         const int cull = c.w != 0.f ? CULL_BACK : CULL_NONE; // from inside a medium: back faces culled
+        using F = std::conditional_t<ALPHA, alpha_filter, no_filter>;
+        F f{};
+        if constexpr(ALPHA) f = alpha_filter{&P, rng[s_pid[i]], 0.f, ALPHA_SALT_SHADOW, false};
         bool occluded;
         if(P.two_level)
-            occluded = trace_tlas<true>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w,
-                                        cull)
+            occluded = trace_tlas<true, F>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z,
+                                           r1.w, cull, f)
                                .occluded;
         else
         {
             unsigned long long v = 0, t = 0;
-            occluded = trace_ray<true, false, STACK>(P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w,
-                                                     cull, v, t, nullptr)
+            occluded = trace_ray<true, false, STACK, F>(P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w,
+                                                        cull, v, t, nullptr, f)
                                .occluded;
         }
         if(!occluded)
@@ -1152,9 +1251,9 @@ __global__ void __launch_bounds__(PT_THREADS, STACK <= 64 ? 8 : 6) // 64 / 85 re
 // environment shadow kernel, so each path's radiance has one writer at a time.
 constexpr int PT_MAX_CROSSINGS = 32;
 
-template<class J, int STACK = (int)TRAVERSAL_STACK>
+template<class J, int STACK = (int)TRAVERSAL_STACK, bool ALPHA = false>
 __global__ void __launch_bounds__(PT_THREADS, STACK <= 64 ? 8 : 6) // 64 / 85 registers
-        k_pt_light_shadow(J S, light_queue lq, float4 *__restrict__ radiance)
+        k_pt_light_shadow(J S, light_queue lq, float4 *__restrict__ radiance, const uint64_t *__restrict__ rng = nullptr)
 {
     const uint32_t n = *lq.count;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -1169,13 +1268,17 @@ __global__ void __launch_bounds__(PT_THREADS, STACK <= 64 ? 8 : 6) // 64 / 85 re
         const int cull = cc.w != 0.f ? CULL_BACK : CULL_NONE;
         float3 T = f3(1.f, 1.f, 1.f);
         unsigned long long v = 0, c = 0;
+        using F = std::conditional_t<ALPHA, alpha_filter, no_filter>;
+        F f{};
+        if constexpr(ALPHA) f = alpha_filter{&P, rng[pid], 0.f, ALPHA_SALT_LIGHT_SHADOW, true};
         if(!P.transmissive)
         {
-            const bool occ = P.two_level ? trace_tlas<true>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z, r0.w,
-                                                            r1.x, r1.y, r1.z, r1.w, cull)
+            const bool occ = P.two_level ? trace_tlas<true, F>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z, r0.w,
+                                                               r1.x, r1.y, r1.z, r1.w, cull, f)
                                                    .occluded
-                                         : trace_ray<true, false, STACK>(P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w, r1.x,
-                                                                         r1.y, r1.z, r1.w, cull, v, c, nullptr)
+                                         : trace_ray<true, false, STACK, F>(P.nodes, P.tris, r0.x, r0.y, r0.z, r0.w,
+                                                                            r1.x, r1.y, r1.z, r1.w, cull, v, c, nullptr,
+                                                                            f)
                                                    .occluded;
             if(occ) T = f3(0.f, 0.f, 0.f);
         }
@@ -1198,7 +1301,8 @@ __global__ void __launch_bounds__(PT_THREADS, STACK <= 64 ? 8 : 6) // 64 / 85 re
                             od = od + st * (front ? -t : t);
                         }
                         return f3(q.base_color[0], q.base_color[1], q.base_color[2]) * q.transmission;
-                    });
+                    },
+                    f);
             if(!open) T = f3(0.f, 0.f, 0.f);
             else if(P.media)
                 T = T * f3(expf(-fmaxf(od.x, 0.f)), expf(-fmaxf(od.y, 0.f)), expf(-fmaxf(od.z, 0.f)));
@@ -1216,8 +1320,8 @@ __global__ void __launch_bounds__(PT_THREADS, STACK <= 64 ? 8 : 6) // 64 / 85 re
                 float t, hu = 0.f, hv = 0.f;
                 if(P.two_level)
                 {
-                    const tlas_result r = trace_tlas<false>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z, tmin,
-                                                            r1.x, r1.y, r1.z, r1.w, cull);
+                    const tlas_result r = trace_tlas<false, F>(P.tl_nodes, P.tl_inst, P.tl_blas, r0.x, r0.y, r0.z,
+                                                               tmin, r1.x, r1.y, r1.z, r1.w, cull, f);
                     prim = r.prim;
                     t = r.t;
                     inst = r.inst;
@@ -1227,8 +1331,9 @@ __global__ void __launch_bounds__(PT_THREADS, STACK <= 64 ? 8 : 6) // 64 / 85 re
                 }
                 else
                 {
-                    const trace_result r = trace_ray<false, false, STACK>(P.nodes, P.tris, r0.x, r0.y, r0.z, tmin, r1.x,
-                                                                          r1.y, r1.z, r1.w, cull, v, c, nullptr);
+                    const trace_result r = trace_ray<false, false, STACK, F>(P.nodes, P.tris, r0.x, r0.y, r0.z, tmin,
+                                                                             r1.x, r1.y, r1.z, r1.w, cull, v, c,
+                                                                             nullptr, f);
                     prim = r.prim;
                     t = r.t;
                     hu = r.u;
@@ -1549,7 +1654,8 @@ __global__ void k_tri_flags(tri_rec *__restrict__ tris, uint32_t n, const uint32
     if(i >= n) return;
     const uint32_t m = tri_mat[tris[i].prim];
     tris[i].pad[0] = (m < num_mats && material_unculled(mats[m]) ? TRI_FLAG_TWOSIDED : 0u) |
-                     (m < num_mats && (mats[m].transmission > 0.f || mats[m].null_surface) ? TRI_FLAG_TRANSMISSIVE : 0u);
+                     (m < num_mats && (mats[m].transmission > 0.f || mats[m].null_surface) ? TRI_FLAG_TRANSMISSIVE : 0u) |
+                     (m < num_mats && material_alpha_tested(mats[m]) ? TRI_FLAG_ALPHA : 0u);
 }
 
 __global__ void k_check_materials(const uint32_t *__restrict__ tri_mat, uint32_t n, uint32_t num_mats,

@@ -48,6 +48,7 @@ struct tl_state
     const tri_rec *tris;
     int sp;
     bool in_blas, done;
+    bool cur_alpha; // the current instance's material is tested by the candidate filter
     uint2 *st; // uint2[TL_STACK] {entry, entry distance (float bits)}, a separate local array so that
                // the fields stay in registers (see ray_state_t)
 };
@@ -74,14 +75,16 @@ __device__ __forceinline__ void tl_init(tl_state &s, const node8 *tnodes, float 
     s.tris = nullptr;
     s.in_blas = false;
     s.done = false;
+    s.cur_alpha = false;
     s.sp = 1;
     s.st[0] = make_uint2(0u, __float_as_uint(tmin));
 }
 
-// one node of the two-level traversal; false once the ray is finished
-template<bool ANY>
+// one node of the two-level traversal; false once the ray is finished. f: the candidate filter
+// (no_filter, traverse.cuh), asked per instance whether its material is tested
+template<bool ANY, class F = no_filter>
 __device__ __forceinline__ bool tl_step(tl_state &s, const node8 *__restrict__ tnodes, const inst_rec *__restrict__ inst,
-                                        const blas_ref *__restrict__ blas, int cull)
+                                        const blas_ref *__restrict__ blas, int cull, const F &f = F())
 {
     while(s.sp > 0 && !s.done)
     {
@@ -114,6 +117,7 @@ __device__ __forceinline__ bool tl_step(tl_state &s, const node8 *__restrict__ t
             s.nodes = B.nodes;
             s.tris = B.tris;
             s.cur_inst = meta.y;
+            if(F::active) s.cur_alpha = f.tests_material(meta.z);
             s.in_blas = true;
             s.st[s.sp] = make_uint2(TL_RETURN, __float_as_uint(s.tmin));
             s.st[s.sp + 1] = make_uint2(0u, __float_as_uint(s.tmin));
@@ -147,15 +151,18 @@ __device__ __forceinline__ bool tl_step(tl_state &s, const node8 *__restrict__ t
                                  s.d[2], tcull, t, u, v))
                         continue;
                     if(!(t > s.tmin && t < s.tmax)) continue;
+                    const uint32_t prim = __float_as_uint(cc.y);
+                    const bool tested = F::active && s.cur_alpha;
                     if(ANY)
                     {
+                        if(tested && !f.accept(s.cur_inst, prim, u, v)) continue;
                         s.done = true;
                         break;
                     }
-                    const uint32_t prim = __float_as_uint(cc.y);
                     if(s.best_prim == VKG_MISS || t < s.best_t ||
                        (t == s.best_t && (s.cur_inst < s.best_inst || (s.cur_inst == s.best_inst && prim < s.best_prim))))
                     {
+                        if(tested && !f.accept(s.cur_inst, prim, u, v)) continue;
                         s.best_t = t;
                         s.best_prim = prim;
                         s.best_inst = s.cur_inst;
@@ -197,16 +204,17 @@ __device__ __forceinline__ bool tl_step(tl_state &s, const node8 *__restrict__ t
     return false;
 }
 
-template<bool ANY>
+template<bool ANY, class F = no_filter>
 __device__ __forceinline__ tlas_result trace_tlas(const node8 *__restrict__ tnodes, const inst_rec *__restrict__ inst,
                                                   const blas_ref *__restrict__ blas, float ox, float oy, float oz,
-                                                  float tmin, float dx, float dy, float dz, float tmax, int cull)
+                                                  float tmin, float dx, float dy, float dz, float tmax, int cull,
+                                                  const F &f = F())
 {
     tl_state s;
     uint2 stack[TL_STACK];
     s.st = stack;
     tl_init(s, tnodes, ox, oy, oz, tmin, dx, dy, dz, tmax);
-    while(tl_step<ANY>(s, tnodes, inst, blas, cull)) {}
+    while(tl_step<ANY, F>(s, tnodes, inst, blas, cull, f)) {}
     tlas_result R;
     R.occluded = s.done;
     R.prim = s.best_prim;

@@ -25,6 +25,19 @@ enum cull_mode : int
 };
 constexpr uint32_t TRI_FLAG_TWOSIDED = 1u;
 constexpr uint32_t TRI_FLAG_TRANSMISSIVE = 2u; // light shadow rays pass: transmission > 0 or a null surface
+constexpr uint32_t TRI_FLAG_ALPHA = 4u;        // candidate hits are tested for coverage (alpha mask / blend)
+
+// Candidate filter of the traversal (the any-hit stage): with `active` false the test compiles away.
+// Otherwise a candidate hit that would count (the nearest so far, or any for an any-hit query) on a
+// triangle flagged TRI_FLAG_ALPHA (single level), or inside an instance whose material
+// tests_material() (two levels), counts only if accept(instance, triangle, u, v) says so. The
+// filter's answer depends on the candidate alone, never on the order candidates are met in.
+struct no_filter
+{
+    static constexpr bool active = false;
+    __device__ __forceinline__ bool accept(uint32_t, uint32_t, float, float) const { return true; }
+    __device__ __forceinline__ bool tests_material(uint32_t) const { return false; }
+};
 
 struct trace_result
 {
@@ -195,11 +208,11 @@ __device__ __forceinline__ void node_keys(const node8 *__restrict__ nodes, uint3
 }
 
 // one node of the traversal; returns false once the ray is finished. POS: the ray's tmin is >= +0
-// (key_pos)
-template<bool ANY, bool STATS, int STACK, bool POS = false>
+// (key_pos); f: the candidate filter
+template<bool ANY, bool STATS, int STACK, bool POS = false, class F = no_filter>
 __device__ __forceinline__ bool ray_step(ray_state_t<STACK> &s, const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
                                          int cull, unsigned long long &visits, unsigned long long &tests,
-                                         unsigned long long *__restrict__ counters)
+                                         unsigned long long *__restrict__ counters, const F &f = F())
 {
     while(s.sp > 0 && !s.done)
     {
@@ -249,14 +262,17 @@ __device__ __forceinline__ bool ray_step(ray_state_t<STACK> &s, const node8 *__r
                              u, v))
                     continue;
                 if(!(t > s.tmin && t < s.tmax)) continue;
+                const uint32_t prim = __float_as_uint(cc.y);
+                const bool tested = F::active && (__float_as_uint(cc.z) & TRI_FLAG_ALPHA);
                 if(ANY)
                 {
+                    if(tested && !f.accept(0u, prim, u, v)) continue;
                     s.done = true;
                     break;
                 }
-                const uint32_t prim = __float_as_uint(cc.y);
                 if(t < s.best_t || (t == s.best_t && prim < s.best))
                 {
+                    if(tested && !f.accept(0u, prim, u, v)) continue;
                     s.best_t = t;
                     s.best = prim;
                     s.bu = u;
@@ -286,13 +302,15 @@ __device__ __forceinline__ trace_result ray_result(const ray_state_t<STACK> &s)
 // transmittance of a segment (light-NEE visibility): one pass over every triangle the ray crosses in
 // (tmin, tmax) (back faces culled when cull == CULL_BACK), in traversal order; false at the first
 // triangle without TRI_FLAG_TRANSMISSIVE, else T is multiplied by tint(prim, t, front face) of each
-// crossed transmissive triangle.
+// crossed transmissive triangle. A triangle that is not transmissive but flagged TRI_FLAG_ALPHA
+// blocks only if the filter accepts it (transmittance_test tints transmissive candidates before it
+// tests coverage, visibility_test.slang:116-152).
 // Every triangle sits in one leaf and every node is visited at most once, so each crossing counts
 // once; the children need no ordering.
-template<int STACK, class Tint>
+template<int STACK, class Tint, class F = no_filter>
 __device__ __forceinline__ bool trace_transmit(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
                                                float ox, float oy, float oz, float tmin, float dx, float dy, float dz,
-                                               float tmax, int cull, float3 &T, Tint tint)
+                                               float tmax, int cull, float3 &T, Tint tint, const F &f = F())
 {
     const float ix = safe_rcp(dx), iy = safe_rcp(dy), iz = safe_rcp(dz);
     uint32_t st[STACK];
@@ -324,7 +342,12 @@ __device__ __forceinline__ bool trace_transmit(const node8 *__restrict__ nodes, 
                              cull == CULL_BACK ? 1 : 0, t, u, v))
                     continue;
                 if(!(t > tmin && t < tmax)) continue;
-                if(!(__float_as_uint(cc.z) & TRI_FLAG_TRANSMISSIVE)) return false;
+                const uint32_t fl = __float_as_uint(cc.z);
+                if(!(fl & TRI_FLAG_TRANSMISSIVE))
+                {
+                    if(F::active && (fl & TRI_FLAG_ALPHA) && !f.accept(0u, __float_as_uint(cc.y), u, v)) continue;
+                    return false;
+                }
                 // front face: the ray runs against the normal e1 x e2
                 const float nx = b.x * cc.x - b.y * b.w, ny = b.y * b.z - a.w * cc.x, nz = a.w * b.w - b.x * b.z;
                 const float3 m = tint(__float_as_uint(cc.y), t, nx * dx + ny * dy + nz * dz < 0.f);
@@ -337,34 +360,34 @@ __device__ __forceinline__ bool trace_transmit(const node8 *__restrict__ nodes, 
     return true;
 }
 
-template<bool ANY, bool STATS, int STACK, bool POS>
+template<bool ANY, bool STATS, int STACK, bool POS, class F = no_filter>
 __device__ __forceinline__ trace_result trace_ray_mode(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
                                                        float ox, float oy, float oz, float tmin, float dx, float dy,
                                                        float dz, float tmax, int cull, unsigned long long &visits,
                                                        unsigned long long &tests,
-                                                       unsigned long long *__restrict__ counters)
+                                                       unsigned long long *__restrict__ counters, const F &f = F())
 {
     ray_state_t<STACK> s;
     uint2 stack[STACK];
     s.st = stack;
     ray_init(s, ox, oy, oz, tmin, dx, dy, dz, tmax);
-    while(ray_step<ANY, STATS, STACK, POS>(s, nodes, tris, cull, visits, tests, counters)) {}
+    while(ray_step<ANY, STATS, STACK, POS, F>(s, nodes, tris, cull, visits, tests, counters, f)) {}
     return ray_result(s);
 }
 
 // one ray, in the key mode its tmin allows
-template<bool ANY, bool STATS, int STACK = (int)TRAVERSAL_STACK>
+template<bool ANY, bool STATS, int STACK = (int)TRAVERSAL_STACK, class F = no_filter>
 __device__ __forceinline__ trace_result trace_ray(const node8 *__restrict__ nodes, const tri_rec *__restrict__ tris,
                                                   float ox, float oy, float oz, float tmin, float dx, float dy,
                                                   float dz, float tmax, int cull,
                                                   unsigned long long &visits, unsigned long long &tests,
-                                                  unsigned long long *__restrict__ counters)
+                                                  unsigned long long *__restrict__ counters, const F &f = F())
 {
     if(key_pos(tmin))
-        return trace_ray_mode<ANY, STATS, STACK, true>(nodes, tris, ox, oy, oz, tmin, dx, dy, dz, tmax, cull, visits,
-                                                        tests, counters);
-    return trace_ray_mode<ANY, STATS, STACK, false>(nodes, tris, ox, oy, oz, tmin, dx, dy, dz, tmax, cull, visits,
-                                                     tests, counters);
+        return trace_ray_mode<ANY, STATS, STACK, true, F>(nodes, tris, ox, oy, oz, tmin, dx, dy, dz, tmax, cull, visits,
+                                                           tests, counters, f);
+    return trace_ray_mode<ANY, STATS, STACK, false, F>(nodes, tris, ox, oy, oz, tmin, dx, dy, dz, tmax, cull, visits,
+                                                        tests, counters, f);
 }
 
 // one node of a ray's traversal (ray_step) in the key mode its tmin allows

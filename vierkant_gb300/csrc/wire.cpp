@@ -19,7 +19,8 @@ constexpr size_t attenuation_color = 48, attenuation_distance = 60, ior = 64, cl
                  clearcoat_roughness = 72, sheen_roughness = 76, sheen_color = 80;
 constexpr size_t iridescence_strength = 96, iridescence_ior = 100, iridescence_thickness_range = 104;
 constexpr size_t albedo_index = 112, normalmap_index = 116, emission_index = 120, ao_rough_metal_index = 124,
-                 transmission_index = 128, texture_type_flags = 132, blend_mode = 136, two_sided = 144,
+                 transmission_index = 128, texture_type_flags = 132, blend_mode = 136, alpha_cutoff = 140,
+                 two_sided = 144,
                  phase_g = 148, scatter_factor = 152, dispersion = 156, scatter_color = 160,
                  diffuse_transmission = 172, diffuse_transmission_color = 176, diffuse_transmission_index = 188,
                  diffuse_transmission_color_index = 192;
@@ -69,6 +70,8 @@ vkg_status vkg_materials_from_wire(const void *records, uint32_t n, vkg_material
         vkg_material m;
         vkg_material_defaults(&m);
         rd3(r, mat_off::color, m.base_color);
+        m.alpha = rd<float>(r, mat_off::color + 12);
+        m.alpha_cutoff = rd<float>(r, mat_off::alpha_cutoff);
         float em[4];
         std::memcpy(em, r + mat_off::emission, sizeof(em));
         for(int c = 0; c < 3; ++c) m.emission[c] = em[c] * em[3];
@@ -105,9 +108,13 @@ vkg_status vkg_materials_from_wire(const void *records, uint32_t n, vkg_material
         m.tex_diffuse_transmission = slot(tex_bit::diffuse_transmission, mat_off::diffuse_transmission_index);
         m.tex_diffuse_transmission_color =
                 slot(tex_bit::diffuse_transmission_color, mat_off::diffuse_transmission_color_index);
+        // BlendMode (Material.hpp:32-37): Opaque 0, Blend 1, Mask 2; another value reads as opaque and
+        // counts as dropped
+        const uint32_t blend = rd<uint32_t>(r, mat_off::blend_mode);
+        m.blend_mode = blend <= VKG_BLEND_MASK ? blend : VKG_BLEND_OPAQUE;
         // left out: textures the tracer does not sample (displacement, thickness, clearcoat, sheen,
-        // iridescence) and alpha blending / masking
-        bool unused = (flags & ~tex_bit::sampled) != 0 || rd<uint32_t>(r, mat_off::blend_mode) != 0;
+        // iridescence)
+        bool unused = (flags & ~tex_bit::sampled) != 0 || blend > VKG_BLEND_MASK;
         nd += unused ? 1u : 0u;
         out[i] = m;
     }

@@ -24,13 +24,15 @@ MATERIAL_DTYPE = np.dtype([("base_color", "<f4", 3), ("roughness", "<f4"), ("met
                            ("tex_color", "<u4"), ("tex_normal", "<u4"), ("tex_emission", "<u4"),
                            ("tex_ao_rough_metal", "<u4"), ("tex_transmission", "<u4"),
                            ("tex_diffuse_transmission", "<u4"), ("tex_diffuse_transmission_color", "<u4"),
-                           ("pad", "<u4", 2)])
+                           ("alpha", "<f4"), ("blend_mode", "<u4"), ("alpha_cutoff", "<f4"),
+                           ("pad", "<u4", 3)])
 assert MATERIAL_DTYPE.itemsize == C.sizeof(vkg_material)
 
 
 def default_materials(n: int) -> np.ndarray:
     """n material records with the reference's defaults (base colour 1, roughness 1, ior 1.5,
-    diffuse-transmission colour 1, everything else 0), filled by the library."""
+    diffuse-transmission colour 1, alpha 1, alpha cutoff 0.5, no textures, everything else 0), filled
+    by the library."""
     m = vkg_material()
     check(lib().vkg_material_defaults(C.byref(m)))
     one = np.frombuffer(bytes(m), MATERIAL_DTYPE, count=1)
@@ -158,6 +160,52 @@ def textured_materials(materials: np.ndarray) -> np.ndarray:
         elif kind == 3:
             m["tex_emission"][i] = 3
             m["emission"][i] = (2.0, 2.0, 2.0)
+    return m
+
+
+def alpha_textures(size: int = 64):
+    """test_textures() plus two colour textures with coverage in alpha: [4] a cut-out (an orange
+    checker whose other squares have alpha 0), [5] a teal colour whose alpha ramps from 0 to 1 along u.
+    uint8 [size, size, 4] each."""
+    y, x = np.mgrid[0:size, 0:size].astype(np.float64)
+    chk = ((x // 8 + y // 8) % 2).astype(bool)
+    cut = np.zeros((size, size, 4), np.uint8)
+    cut[..., :3] = (240, 140, 40)
+    cut[..., 3] = np.where(chk, 255, 0).astype(np.uint8)
+    ramp = np.zeros((size, size, 4), np.uint8)
+    ramp[..., :3] = (40, 200, 190)
+    ramp[..., 3] = np.rint(255 * (x + 0.5) / size).astype(np.uint8)
+    return test_textures(size) + [cut, ramp]
+
+
+ALPHA_KINDS = ("mask, cut-out texture", "blend, ramp texture", "blend, alpha 0.4", "opaque")
+
+
+def alpha_materials(materials: np.ndarray) -> np.ndarray:
+    """The Cornell materials with coverage (textures from alpha_textures()): the left wall
+    (material 1) masked by the cut-out texture, so that light comes in through its holes; sphere s
+    (material 3 + s) becomes ALPHA_KINDS[s % 4]. Alpha 1 and cut-off 0.5 unless stated."""
+    from ._lib import BLEND_BLEND, BLEND_MASK
+    m = np.array(materials, MATERIAL_DTYPE, copy=True)
+    NO = 0xFFFFFFFF
+    for f in ("tex_color", "tex_normal", "tex_emission", "tex_ao_rough_metal", "tex_transmission",
+              "tex_diffuse_transmission", "tex_diffuse_transmission_color"):
+        m[f] = NO
+    m["alpha"] = 1.0
+    m["alpha_cutoff"] = 0.5
+    m["blend_mode"][1] = BLEND_MASK
+    m["tex_color"][1] = 4
+    for s in range(len(m) - 3):
+        i, kind = 3 + s, s % 4
+        if kind == 0:
+            m["blend_mode"][i] = BLEND_MASK
+            m["tex_color"][i] = 4
+        elif kind == 1:
+            m["blend_mode"][i] = BLEND_BLEND
+            m["tex_color"][i] = 5
+        elif kind == 2:
+            m["blend_mode"][i] = BLEND_BLEND
+            m["alpha"][i] = 0.4
     return m
 
 
