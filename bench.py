@@ -657,8 +657,9 @@ def features_block(ctx):
     glass, clearcoat, sheen, diffuse transmission, iridescence, metal-rough), one light of every
     analytic type and a sun disc, and the same box with its spheres cycled through homogeneous media
     (fog, absorbing glass, emissive gas, scattering glass) and the same lights, against the box with
-    metal-rough materials and no lights, all at 1280x720 x 64 spp, 8 segments (samples/s, Mrays/s).
-    Parity: the 16-sphere lit scene and the 16-sphere media scene at 256x144 x 1024 spp against their
+    metal-rough materials and no lights, all at 1280x720 x 64 spp, 8 segments (samples/s, Mrays/s);
+    also the textured box (smooth normals; checker, ao-rough-metal, normal and emission maps) and the
+    alpha box (a cut-out wall, masked and blended spheres), unlit. Parity: the 16-sphere lit scene and the 16-sphere media scene at 256x144 x 1024 spp against their
     FP64 oracles (4096 spp full frame)."""
     import math
     import numpy as np
@@ -684,12 +685,27 @@ def features_block(ctx):
     out = {}
     sc = geometry.cornell_scene(SEED, 2, 64, 16)
     cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, 1280, 720)
-    for name, mats, lit in (("plain_720p_64spp_8seg", sc["materials"], False),
-                            ("materials_lights_720p_64spp_8seg", geometry.showcase_materials(sc["materials"]), True),
-                            ("media_lights_720p_64spp_8seg", geometry.media_materials(sc["materials"]), True)):
+    nrm = geometry.cornell_vertex_normals(sc)
+    uv, tg = geometry.cornell_texcoords(sc)
+    for name, mats, lit, tex in (("plain_720p_64spp_8seg", sc["materials"], False, None),
+                                 ("materials_lights_720p_64spp_8seg", geometry.showcase_materials(sc["materials"]),
+                                  True, None),
+                                 ("media_lights_720p_64spp_8seg", geometry.media_materials(sc["materials"]), True,
+                                  None),
+                                 ("textured_720p_64spp_8seg", geometry.textured_materials(sc["materials"]), False,
+                                  geometry.test_textures()),
+                                 ("alpha_720p_64spp_8seg", geometry.alpha_materials(sc["materials"]), False,
+                                  geometry.alpha_textures())):
         scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], mats, env)
         if lit:
             scene.set_lights(cornell_lights())
+        if tex is not None:
+            # smooth normals, texture coordinates, tangents and the textures (the textured and the
+            # alpha-masked / blended Cornell scenes of the parity tests)
+            scene.set_normals(nrm)
+            scene.set_texcoords(uv)
+            scene.set_tangents(tg)
+            scene.set_textures(tex)
         pt = PBRPathTracer(ctx, seed=SEED, settings=settings(64, 1280, 720, lit))
         pt.render_scene(scene, cam)
         pt.reset_accumulator()
@@ -704,6 +720,10 @@ def features_block(ctx):
                                                   out["plain_720p_64spp_8seg"]["ms"], 3)
     out["media_lights_time_vs_plain"] = round(out["media_lights_720p_64spp_8seg"]["ms"] /
                                               out["plain_720p_64spp_8seg"]["ms"], 3)
+    out["textured_time_vs_plain"] = round(out["textured_720p_64spp_8seg"]["ms"] / out["plain_720p_64spp_8seg"]["ms"],
+                                          3)
+    out["alpha_time_vs_textured"] = round(out["alpha_720p_64spp_8seg"]["ms"] / out["textured_720p_64spp_8seg"]["ms"],
+                                          3)
     g = np.load(ROOT / "tests" / "golden" / "pt_oracle_lights.npz")
     sc = geometry.cornell_scene(SEED, 2, int(g["num_spheres"]), 16)
     scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], geometry.showcase_materials(sc["materials"]),

@@ -760,7 +760,8 @@ vkg_status vkg_tracer_destroy(vkg_tracer *tracer);
  * one set of wavefront queues (every path carries its job index), waves are packed from whole
  * samples of the jobs, and a render is one CUDA-graph launch. Each job's image equals what
  * vkg_tracer_render would produce for it alone with the same seed and settings (same PCG32 streams,
- * same per-pixel summation order). No radiance cache in batch mode. */
+ * same per-pixel summation order; textures and alpha-tested materials included). No radiance cache
+ * and no media in batch mode. */
 typedef struct vkg_batch vkg_batch;
 typedef struct vkg_batch_job
 {

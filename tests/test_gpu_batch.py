@@ -83,3 +83,47 @@ def test_autotune_keeps_images(ctx, jobs):
     again = [i.clone() for i in br.render()]
     assert all(torch.equal(a, b) for a, b in zip(imgs, again))
     br.close()
+
+
+@pytest.mark.parametrize("extend", [1, 2])
+def test_batch_textures_and_alpha_equal_single_scene_tracer(ctx, extend):
+    """jobs with textures (the textured Cornell scene) and with alpha-tested materials (the alpha
+    scene) render in a batch bit for bit like the tracer renders them; an untextured job of the same
+    batch shades with the textured variant and equals its tracer render up to that variant's rounding"""
+    env = procedural_sky(ctx, 256, 128, sun_direction(), 50.0, 0.02)
+    scenes, jobs = [], []
+    for k, (mats_of, tex) in enumerate(((geometry.alpha_materials, geometry.alpha_textures()),
+                                        (geometry.textured_materials, geometry.test_textures()),
+                                        (None, None))):
+        sc = geometry.cornell_scene(0x5EED, 2, 8, 8)
+        mats = mats_of(sc["materials"]) if mats_of else sc["materials"]
+        scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], mats, env)
+        if tex is not None:
+            uv, tg = geometry.cornell_texcoords(sc)
+            scene.set_normals(geometry.cornell_vertex_normals(sc))
+            scene.set_texcoords(uv)
+            scene.set_tangents(tg)
+            scene.set_textures(tex)
+        scenes.append(scene)
+        w, h = (160, 96) if k < 2 else (64, 48)
+        cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, w, h)
+        s = PBRPathTracer.default_settings()
+        s.resolution[0], s.resolution[1] = w, h
+        s.num_samples, s.max_trace_depth, s.rr_start_depth = 4, 6, 3
+        jobs.append(BatchJob(scene, cam, s, 21 + k))
+    t = BatchRenderer.default_tuning()
+    t.extend_kernel = extend
+    br = BatchRenderer(ctx, jobs, t)
+    imgs = [i.clone() for i in br.render()]
+    torch.cuda.synchronize()
+    for k, job in enumerate(jobs):
+        ref = single(ctx, job, 1)
+        if k < 2:
+            assert torch.equal(imgs[k], ref), (k, (imgs[k] - ref).abs().max().item())
+        else:
+            a, b = imgs[k].cpu().numpy().astype(np.float64), ref.cpu().numpy().astype(np.float64)
+            close = np.mean(np.all(np.abs(a - b) <= 1e-3 * np.maximum(np.abs(b), 1e-2), axis=-1))
+            assert close > 0.97, close
+    br.close()
+    for s in scenes:
+        s.close()

@@ -25,6 +25,11 @@
 // tracer does. One shade variant serves all jobs of a batch: the full one when any job needs it
 // (materials beyond metal-roughness or lights), so a metal-rough job in such a batch equals its
 // tracer render up to the rounding of the out-of-line BSDF evaluation. Media are refused.
+//
+// Textures and alpha coverage: when a job's scene has textures the batch keeps one ray-cone width
+// per wave path (the jobs with textures point at it, the others leave their cone null) and shades
+// with the textured variant; when a job's scene has alpha-tested materials the grid-stride queue
+// kernels run with the coverage filter (the persistent tracers are then not used).
 #include "pt_kernels.cuh"
 
 #include <algorithm>
@@ -72,6 +77,7 @@ __global__ void __launch_bounds__(PT_THREADS)
         const uint32_t x = P.cx0 + pix % P.cw, y = P.cy0 + pix / P.cw;
         const float jx = u01(pcg32_next(g)), jy = u01(pcg32_next(g));
         camera_ray(P.cam, x, y, jx, jy, reinterpret_cast<float4 *>(q_ray + p));
+        if(P.cone) P.cone[p] = 0.f; // the ray cone starts at width 0 (raypipeline.slang:112-114)
         q_pid[p] = p;
         rng[p] = g.state;
         pinc[p] = (seq << 1u) | 1u;
@@ -151,6 +157,9 @@ struct vkg_batch
     uint32_t njobs = 0, total_pix = 0, max_depth = 0;
     bool any_instanced = false;
     bool any_full = false; // a job scene with materials beyond metal-roughness
+    bool any_textures = false; // a job scene with textures: the textured shade variant, per-path cone widths
+    bool any_alpha = false;    // a job scene with alpha-tested materials: the coverage-testing queue kernels
+    float *cone = nullptr;     // ray-cone width per path of a wave (jobs with textures)
     uint32_t max_bvh_depth = 0;
     uint64_t total_paths = 0;
     vkg_batch_tuning tuning{};
@@ -202,8 +211,9 @@ void free_waves(vkg_batch *b)
                   (void *)b->hit_inst,
                   (void *)b->s_ray, (void *)b->s_pid, (void *)b->s_contrib, (void *)b->rng, (void *)b->pinc,
                   (void *)b->pjob, (void *)b->beta_pdf, (void *)b->radiance, (void *)b->d_chunks, (void *)b->l_ray,
-                  (void *)b->l_pid, (void *)b->l_contrib})
+                  (void *)b->l_pid, (void *)b->l_contrib, (void *)b->cone})
         cudaFree(p);
+    b->cone = nullptr;
     b->l_ray = nullptr;
     b->l_pid = nullptr;
     b->l_contrib = nullptr;
@@ -300,6 +310,13 @@ vkg_status ensure_waves(vkg_batch *b, const std::vector<vkg_batch::wave> &waves,
             al((void **)&b->l_pid, need * sizeof(uint32_t));
             al((void **)&b->l_contrib, need * sizeof(float4));
         }
+        if(b->any_textures) al((void **)&b->cone, need * sizeof(float));
+        // the jobs with textures sample them through the wave's cone widths
+        if(b->any_textures && e == cudaSuccess)
+        {
+            for(uint32_t j = 0; j < b->njobs; ++j) b->params[j].cone = b->jobs[j].scene->num_textures ? b->cone : nullptr;
+            e = cudaMemcpy(b->d_params, b->params.data(), b->njobs * sizeof(pt_params), cudaMemcpyHostToDevice);
+        }
         if(e != cudaSuccess)
         {
             free_waves(b);
@@ -319,7 +336,8 @@ vkg_status enqueue(vkg_batch *b, const std::vector<vkg_batch::wave> &waves, cuda
 {
     vkg_ctx *ctx = b->ctx;
     vkg_batch_tuning T = b->tuning;
-    if(b->any_instanced) T.extend_kernel = 1; // the persistent tracers handle single-level scenes only
+    // the persistent tracers handle single-level scenes without alpha-tested materials only
+    if(b->any_instanced || b->any_alpha) T.extend_kernel = 1;
     // a 64-entry stack serves BVHs of depth <= 10 (7 (depth - 1) + 1 entries at most)
     if(b->max_bvh_depth > 10) T.stack_depth = 128;
     const job_table J{b->d_params, b->pjob, b->pinc};
@@ -350,6 +368,12 @@ vkg_status enqueue(vkg_batch *b, const std::vector<vkg_batch::wave> &waves, cuda
                     k_pt_trace_persistent<false, job_table><<<grid, bs, 0, st>>>(
                             J, b->q_ray[a], b->q_pid[a], cnt_in, b->hits, b->hit_inst, nullptr, nullptr, b->counters + 3);
             }
+            else if(b->any_alpha && T.stack_depth == 64)
+                k_pt_extend<job_table, 64, true><<<grid, bs, 0, st>>>(J, b->q_ray[a], b->q_pid[a], cnt_in, b->hits,
+                                                                       b->hit_inst, nullptr, nullptr, b->rng, depth);
+            else if(b->any_alpha)
+                k_pt_extend<job_table, (int)TRAVERSAL_STACK, true><<<grid, bs, 0, st>>>(
+                        J, b->q_ray[a], b->q_pid[a], cnt_in, b->hits, b->hit_inst, nullptr, nullptr, b->rng, depth);
             else if(T.stack_depth == 64)
                 k_pt_extend<job_table, 64><<<grid, bs, 0, st>>>(J, b->q_ray[a], b->q_pid[a], cnt_in, b->hits, b->hit_inst);
             else
@@ -357,17 +381,18 @@ vkg_status enqueue(vkg_batch *b, const std::vector<vkg_batch::wave> &waves, cuda
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_out, 0, sizeof(uint32_t), st));
             VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_s, 0, sizeof(uint32_t), st));
             if(cnt_l) VKG_TRY_CUDA(ctx, cudaMemsetAsync(cnt_l, 0, sizeof(uint32_t), st));
-            if(b->any_full || b->any_lights)
-                k_pt_shade<MODE_PLAIN, job_table, true><<<grid, bs, 0, st>>>(J, depth, b->q_ray[a], b->q_pid[a], b->hits,
-                                                                             b->hit_inst, cnt_in, b->q_ray[1 - a],
-                                                                             b->q_pid[1 - a], cnt_out, b->s_ray,
-                                                                             b->s_pid, b->s_contrib, cnt_s, b->rng,
-                                                                             b->beta_pdf, b->radiance, io, lq, nullptr);
-            else
-            k_pt_shade<MODE_PLAIN, job_table, false><<<grid, bs, 0, st>>>(J, depth, b->q_ray[a], b->q_pid[a], b->hits, b->hit_inst, cnt_in,
-                                                       b->q_ray[1 - a], b->q_pid[1 - a], cnt_out, b->s_ray, b->s_pid,
-                                                       b->s_contrib, cnt_s, b->rng, b->beta_pdf, b->radiance, io,
-                                                       light_queue{}, nullptr);
+            // the shade variant: the full material set and the lights or metal-roughness only, each
+            // with the texture terms when a job has textures
+#define VKG_BATCH_SHADE(F, TX, LQ)                                                                                     \
+    k_pt_shade<MODE_PLAIN, job_table, F, false, TX><<<grid, bs, 0, st>>>(                                              \
+            J, depth, b->q_ray[a], b->q_pid[a], b->hits, b->hit_inst, cnt_in, b->q_ray[1 - a], b->q_pid[1 - a],       \
+            cnt_out, b->s_ray, b->s_pid, b->s_contrib, cnt_s, b->rng, b->beta_pdf, b->radiance, io, LQ, nullptr)
+            const bool full = b->any_full || b->any_lights;
+            if(full && b->any_textures) VKG_BATCH_SHADE(true, true, lq);
+            else if(full) VKG_BATCH_SHADE(true, false, lq);
+            else if(b->any_textures) VKG_BATCH_SHADE(false, true, light_queue{});
+            else VKG_BATCH_SHADE(false, false, light_queue{});
+#undef VKG_BATCH_SHADE
             if(T.extend_kernel == 2)
             {
                 VKG_TRY_CUDA(ctx, cudaMemsetAsync(b->counters + 3, 0, sizeof(uint32_t), st));
@@ -378,12 +403,22 @@ vkg_status enqueue(vkg_batch *b, const std::vector<vkg_batch::wave> &waves, cuda
                     k_pt_trace_persistent<true, job_table><<<grid, bs, 0, st>>>(
                             J, b->s_ray, b->s_pid, cnt_s, nullptr, nullptr, b->s_contrib, b->radiance, b->counters + 3);
             }
+            else if(b->any_alpha && T.stack_depth == 64)
+                k_pt_shadow<job_table, 64, true><<<grid, bs, 0, st>>>(J, b->s_ray, b->s_pid, b->s_contrib, cnt_s,
+                                                                       b->radiance, nullptr, nullptr, b->rng);
+            else if(b->any_alpha)
+                k_pt_shadow<job_table, (int)TRAVERSAL_STACK, true><<<grid, bs, 0, st>>>(
+                        J, b->s_ray, b->s_pid, b->s_contrib, cnt_s, b->radiance, nullptr, nullptr, b->rng);
             else if(T.stack_depth == 64)
                 k_pt_shadow<job_table, 64><<<grid, bs, 0, st>>>(J, b->s_ray, b->s_pid, b->s_contrib, cnt_s, b->radiance);
             else
                 k_pt_shadow<<<grid, bs, 0, st>>>(J, b->s_ray, b->s_pid, b->s_contrib, cnt_s, b->radiance);
             // light NEE after the environment shadow launch: one writer per path at a time
-            if(cnt_l && T.stack_depth == 64)
+            if(cnt_l && b->any_alpha && T.stack_depth == 64)
+                k_pt_light_shadow<job_table, 64, true><<<grid, bs, 0, st>>>(J, lq, b->radiance, b->rng);
+            else if(cnt_l && b->any_alpha)
+                k_pt_light_shadow<job_table, (int)TRAVERSAL_STACK, true><<<grid, bs, 0, st>>>(J, lq, b->radiance, b->rng);
+            else if(cnt_l && T.stack_depth == 64)
                 k_pt_light_shadow<job_table, 64><<<grid, bs, 0, st>>>(J, lq, b->radiance);
             else if(cnt_l)
                 k_pt_light_shadow<job_table><<<grid, bs, 0, st>>>(J, lq, b->radiance);
@@ -521,6 +556,8 @@ vkg_status vkg_batch_create(vkg_ctx *ctx, const vkg_batch_job *jobs, uint32_t nj
         all_lights.insert(all_lights.end(), jl.begin(), jl.end());
         b->any_instanced = b->any_instanced || jb.scene->tlas != nullptr;
         b->any_full = b->any_full || jb.scene->any_full;
+        b->any_textures = b->any_textures || jb.scene->num_textures > 0;
+        b->any_alpha = b->any_alpha || jb.scene->any_alpha;
         if(jb.scene->bvh) b->max_bvh_depth = std::max(b->max_bvh_depth, jb.scene->bvh->depth);
         const uint32_t npix = b->params.back().npix;
         b->jdev.push_back(batch_job_dev{npix, jb.settings.num_samples, off, jb.d_rgb_out});
