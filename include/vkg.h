@@ -186,8 +186,14 @@ typedef struct vkg_material
     float alpha;        /* base colour alpha, [0, 1] (1) */
     uint32_t blend_mode; /* VKG_BLEND_OPAQUE (0), VKG_BLEND_BLEND (1), VKG_BLEND_MASK (2): Material.hpp:32-37 */
     float alpha_cutoff; /* MASK threshold (0.5) */
-    uint32_t pad[3];
-} vkg_material; /* 192 B */
+    /* texture-coordinate transform: the entry's texture_matrix (raypipeline.slang:350), which the
+       reference fills from the colour texture's KHR_texture_transform (gltf.cpp:162-194,
+       RayBuilder.cpp:596-597, :633). With has_uv_transform != 0 every texture the closest-hit stage
+       samples is read at (u', v') = (t0 u + t1 v + t2, t3 u + t4 v + t5); the coverage test and the
+       texture LOD use the untransformed coordinates, as the reference's any_hit and lod_constant do. */
+    uint32_t has_uv_transform; /* 0: identity (default) */
+    float uv_transform[6];     /* row-major 2 x 3 */
+} vkg_material; /* 208 B */
 enum
 {
     VKG_BLEND_OPAQUE = 0,
@@ -614,7 +620,8 @@ vkg_status vkg_scene_camera_medium(const vkg_scene *scene, const float eye[3], u
  * primitive; float positions, uint32 indices, optional normals / texture coordinates / tangents),
  * instances (node placements, object -> world 3x4, mesh index in `blas`, material), materials
  * (vkg_material, texture slots indexing the asset's textures; alphaMode / alphaCutoff / the base
- * colour's alpha into blend_mode / alpha_cutoff / alpha), textures (PNG images decoded to RGBA8)
+ * colour's alpha into blend_mode / alpha_cutoff / alpha; the colour texture's KHR_texture_transform
+ * into uv_transform), textures (PNG images decoded to RGBA8)
  * and KHR_lights_punctual lights (vkg_light); those feed vkg_scene_create_instanced,
  * vkg_scene_set_normals / _texcoords / _tangents / _textures and vkg_scene_set_lights. Errors: a status and
  * the message in err (may be NULL). The mesh pointers stay valid until vkg_gltf_destroy. */
@@ -671,6 +678,10 @@ typedef struct vkg_wire_entry_info
     uint32_t base_index;    /* first index of the entry in the index buffer */
     int32_t vertex_offset;  /* added to every index */
     float aabb_min[3], aabb_max[3]; /* object-space box */
+    /* the entry's texture_matrix (RayBuilder.hpp:26, applied to (u, v, 0, 1)) as vkg_material's
+       uv_transform: a caller copies it into the entry's material (has_uv_transform = 0 when identity) */
+    uint32_t has_uv_transform;
+    float uv_transform[6];
 } vkg_wire_entry_info;
 /* entry_t -> vkg_instance: object -> world = T R S of the entry's transform_t (translation, rotation
    quaternion stored x y z w, scale; the shader's apply_transform, utils/transform.slang:19-24) as a

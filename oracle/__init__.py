@@ -286,7 +286,7 @@ MATERIAL_DTYPE = np.dtype([("base_color", "<f4", 3), ("roughness", "<f4"), ("met
                            ("tex_ao_rough_metal", "<u4"), ("tex_transmission", "<u4"),
                            ("tex_diffuse_transmission", "<u4"), ("tex_diffuse_transmission_color", "<u4"),
                            ("alpha", "<f4"), ("blend_mode", "<u4"), ("alpha_cutoff", "<f4"),
-                           ("pad", "<u4", 3)])
+                           ("has_uv_transform", "<u4"), ("uv_transform", "<f4", 6)])
 
 
 class orc_pt_scene(C.Structure):
@@ -482,7 +482,7 @@ def pt_render(fp64, xyz, idx, tri_mat, mats, bvh: "CpuBVH", env_rgb, cam, spp, *
                                 C.POINTER(orc_camera), C.POINTER(orc_pt_settings), C.c_void_p, C.c_void_p, C.c_void_p,
                                 C.c_int]
     if np.asarray(mats).dtype.itemsize != MATERIAL_DTYPE.itemsize:
-        raise ValueError("materials must be 192-byte material records")
+        raise ValueError("materials must be 208-byte material records")
     keep = [np.ascontiguousarray(a) for a in (xyz, idx, tri_mat, mats)]
     nrm = _normals(normals) if normals is not None else None
     tng = _normals(tangents) if tangents is not None else None
@@ -574,7 +574,7 @@ def pt_render_instanced(meshes, o2w, inst_mesh, inst_mat, mats, env_rgb, cam, sp
     imat = np.ascontiguousarray(inst_mat, np.uint32)
     mats = np.ascontiguousarray(mats)
     if mats.dtype.itemsize != MATERIAL_DTYPE.itemsize:
-        raise ValueError("materials must be 192-byte material records")
+        raise ValueError("materials must be 208-byte material records")
     keep += [nvert, twos, o2w, im, imat, mats]
     nrm_arr = None
     if mesh_normals is not None:

@@ -145,8 +145,11 @@ typedef struct {
     float alpha;
     uint32_t blend_mode;
     float alpha_cutoff;
-    uint32_t pad[3];
-} orc_pt_material; /* same 192-byte layout as vkg_material */
+    /* texture-coordinate transform of the closest-hit stage (raypipeline.slang:350): with
+       has_uv_transform, (u, v) -> (t0 u + t1 v + t2, t3 u + t4 v + t5) */
+    uint32_t has_uv_transform;
+    float uv_transform[6];
+} orc_pt_material; /* same 208-byte layout as vkg_material */
 
 /* a texture: size, level count, wrap modes (s: bits 0-7, t: bits 8-15; 0 repeat, 1 clamp to edge,
    2 mirrored repeat) and the first texel of each level in the scene's RGBA8 texel array; the same

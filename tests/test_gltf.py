@@ -290,7 +290,8 @@ def test_texcoords_tangents_and_samplers(tmp_path):
     meshes = [[(*QUAD, 0, None, n, {"TEXCOORD_0": quad_uv, "TANGENT": tg})],
               [(*QUAD, 0, None, n, {"TEXCOORD_0": (uv8, 5121)})],
               [(*QUAD, 0, None, None, {"TEXCOORD_0": quad_uv})]]
-    mats = [{"pbrMetallicRoughness": {"baseColorTexture": {"index": 0}, "metallicRoughnessTexture": {"index": 1}},
+    mats = [{"pbrMetallicRoughness": {"baseColorTexture": {"index": 0, "extensions": {"KHR_texture_transform": {
+                 "offset": [0.25, -0.5], "rotation": 0.3, "scale": [2.0, 3.0]}}}, "metallicRoughnessTexture": {"index": 1}},
              "normalTexture": {"index": 1}, "emissiveTexture": {"index": 0}, "emissiveFactor": [1, 1, 1],
              "extensions": {"KHR_materials_transmission": {"transmissionTexture": {"index": 1}}}}]
     path = tmp_path / "uv.glb"
@@ -319,3 +320,7 @@ def test_texcoords_tangents_and_samplers(tmp_path):
     assert (m["tex_color"], m["tex_ao_rough_metal"], m["tex_normal"], m["tex_emission"], m["tex_transmission"]) == \
         (0, 1, 1, 0, 1)
     assert np.array_equal(m["emission"], [0, 0, 0])
+    # the colour texture's KHR_texture_transform: T(offset) R(rotation about -z) S(scale) on (u, v, 0, 1)
+    c, s_ = math.cos(0.3), math.sin(0.3)
+    assert m["has_uv_transform"] == 1
+    assert np.allclose(m["uv_transform"], [2 * c, 3 * s_, 0.25, -2 * s_, 3 * c, -0.5], rtol=0, atol=1e-6)

@@ -209,3 +209,62 @@ def test_gltf_textured_scene_renders_like_the_direct_one(ctx, world, tmp_path):
         q_.close()
     loaded.close()
     direct.close()
+
+
+def test_uv_transform(ctx, world):
+    """the texture-coordinate transform (raypipeline.slang:350): the identity renders bit for bit like
+    none, scaling by 2 like texture coordinates scaled by 2 on primary hits (both read level 0), and a
+    rotated transform matches the FP32 twin path for path"""
+    sc = world["sc"]
+    crop = (600, 560, 48, 48)
+
+    def scene(mats, uv):
+        s = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], mats, world["env"])
+        s.set_normals(world["nrm"])
+        s.set_texcoords(uv)
+        s.set_tangents(world["tg"])
+        s.set_textures(world["tex"])
+        return s
+
+    def render(mats, uv, depth=6, spp=4):
+        s = scene(mats, uv)
+        p = PBRPathTracer(ctx, seed=0x5EED, settings=settings(spp, crop, max_depth=depth))
+        img = p.render_scene(s, world["cam"]).clone()
+        p.close()
+        s.close()
+        return img
+
+    base = world["mats"]
+    plain = render(base, world["uv"])
+    ident = base.copy()
+    ident["has_uv_transform"] = 1
+    ident["uv_transform"] = (1, 0, 0, 0, 1, 0)
+    assert torch.equal(plain, render(ident, world["uv"]))
+    twice = base.copy()
+    twice["has_uv_transform"] = 1
+    twice["uv_transform"] = (2, 0, 0, 0, 2, 0)
+    a = render(twice, world["uv"], depth=1)
+    assert torch.equal(a, render(base, world["uv"] * 2, depth=1))
+    assert not torch.equal(a, render(base, world["uv"], depth=1))
+    rot = base.copy()
+    rot["has_uv_transform"] = 1
+    c, s_ = math.cos(0.7), math.sin(0.7)
+    rot["uv_transform"] = (c, s_, 0.1, -s_, c, 0.2)
+    spp = 8
+    img = render(rot, world["uv"], spp=spp).cpu().numpy().astype(np.float64)
+    ref = plain.cpu().numpy().astype(np.float64)
+    assert np.abs(img - ref).mean() > 1e-3 * np.abs(ref).mean()
+    s = scene(rot, world["uv"])
+    wptr, aptr, W, H = s.env_tables()
+    n = W * H
+    w = d2h(wptr, 4 * n, np.float32)
+    tab = d2h(aptr, 8 * n, np.uint32).reshape(n, 2)
+    s.close()
+    bvh = oracle.CpuBVH(sc["xyz"], sc["indices"], 4)
+    twin, _, _ = oracle.pt_render(False, sc["xyz"], sc["indices"], sc["tri_material"], rot, bvh,
+                                  world["env"].cpu().numpy(), world["ocam"], spp, seed=0x5EED, batch=0, rr_depth=3,
+                                  crop=crop, alias_prob=np.ascontiguousarray(tab[:, 0].view(np.float32)),
+                                  alias=np.ascontiguousarray(tab[:, 1]), weight=w, normals=world["nrm"],
+                                  uv=world["uv"], tangents=world["tg"], textures=world["tex"])
+    rel = np.abs(img - twin) / np.maximum(np.abs(twin), 1e-2)
+    assert np.mean(np.all(rel < 1e-3, axis=-1)) > 0.97

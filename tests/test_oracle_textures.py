@@ -98,3 +98,43 @@ def test_textured_render_differs():
     c, _, _ = oracle.pt_render(True, sc["xyz"], sc["indices"], sc["tri_material"], tmats, bvh, env, cam, 8,
                                crop=crop, normals=nrm, textures=geometry.test_textures())
     assert np.array_equal(a, c)
+
+
+def test_uv_transform():
+    """the texture-coordinate transform of the closest-hit stage (raypipeline.slang:350): the identity
+    changes nothing; scaling by 2 equals texture coordinates scaled by 2 on primary hits (where both
+    read level 0: the LOD keeps the untransformed coordinates' constant); a rotation changes the image"""
+    sc = oracle.cornell_scene(0x5EED, 2, 8, 8)
+    mats = oracle.cornell_materials(0x5EED, 2, 8)
+    th = float(np.float32(math.tan(math.radians(45.0) / 2.0)))
+    cam = oracle.camera((0, 0, 3.4), (0, 0, 0), (0, 1, 0), th, 320, 180)
+    env = oracle.env_procedural(256, 128, np.array([0.2962, 0.5, 0.8138], np.float32))
+    bvh = oracle.CpuBVH(sc["xyz"], sc["indices"], 4)
+    uv, tg = geometry.cornell_texcoords(sc)
+    nrm = geometry.cornell_vertex_normals(sc)
+    tmats = geometry.textured_materials(mats)
+    crop = (100, 60, 64, 64)
+
+    def render(m, tuv, depth=6):
+        img, _, _ = oracle.pt_render(True, sc["xyz"], sc["indices"], sc["tri_material"], m, bvh, env, cam, 4,
+                                     crop=crop, normals=nrm, uv=tuv, tangents=tg, textures=geometry.test_textures(),
+                                     max_depth=depth)
+        return img
+
+    plain = render(tmats, uv)
+    ident = tmats.copy()
+    ident["has_uv_transform"] = 1
+    ident["uv_transform"] = (1, 0, 0, 0, 1, 0)
+    assert np.array_equal(plain, render(ident, uv))
+    twice = tmats.copy()
+    twice["has_uv_transform"] = 1
+    twice["uv_transform"] = (2, 0, 0, 0, 2, 0)
+    a = render(twice, uv, depth=1)
+    b = render(tmats, uv * 2, depth=1)
+    assert np.array_equal(a, b)
+    assert not np.array_equal(a, render(tmats, uv, depth=1))
+    rot = tmats.copy()
+    rot["has_uv_transform"] = 1
+    c, s = math.cos(0.7), math.sin(0.7)
+    rot["uv_transform"] = (c, s, 0.1, -s, c, 0.2)
+    assert np.abs(render(rot, uv) - plain).mean() > 1e-3 * np.abs(plain).mean()

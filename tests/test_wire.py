@@ -114,7 +114,15 @@ def test_instances_from_wire():
     e["vertex_offset"] = [0, -4, 7, 100, 0, 3]
     e["base_index"] = np.arange(6) * 12
     e["buffer_index"] = [0, 1, 1, 2, 0, 5]
+    e["texture_matrix"] = np.eye(4, dtype=np.float32).reshape(-1)
+    # entry 2: a glm::mat4 (column-major) scaling u by 2, v by 3 and offsetting by (0.5, -1)
+    tm = np.eye(4, dtype=np.float32)
+    tm[0, 0], tm[1, 1], tm[0, 3], tm[1, 3] = 2.0, 3.0, 0.5, -1.0
+    e["texture_matrix"][2] = tm.T.reshape(-1)  # column-major storage
     inst, info = instances_from_wire(e)
+    assert list(info["has_uv_transform"]) == [0, 0, 1, 0, 0, 0]
+    assert np.array_equal(info["uv_transform"][2], [2.0, 0.0, 0.5, 0.0, 3.0, -1.0])
+    assert np.array_equal(info["uv_transform"][0], [1, 0, 0, 0, 1, 0])
     assert list(inst["blas"]) == list(e["buffer_index"]) and list(inst["material"]) == list(e["material_index"])
     assert list(info["vertex_offset"]) == list(e["vertex_offset"]) and list(info["base_index"]) == list(e["base_index"])
     assert np.array_equal(info["aabb_min"], e["aabb_min"]) and np.array_equal(info["aabb_max"], e["aabb_max"])

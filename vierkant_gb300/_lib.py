@@ -66,7 +66,8 @@ class vkg_material(C.Structure):
                 ("tex_normal", C.c_uint32), ("tex_emission", C.c_uint32), ("tex_ao_rough_metal", C.c_uint32),
                 ("tex_transmission", C.c_uint32), ("tex_diffuse_transmission", C.c_uint32),
                 ("tex_diffuse_transmission_color", C.c_uint32), ("alpha", C.c_float),
-                ("blend_mode", C.c_uint32), ("alpha_cutoff", C.c_float), ("pad", C.c_uint32 * 3)]
+                ("blend_mode", C.c_uint32), ("alpha_cutoff", C.c_float), ("has_uv_transform", C.c_uint32),
+                ("uv_transform", C.c_float * 6)]
 
 
 class vkg_texture_desc(C.Structure):
@@ -109,7 +110,8 @@ class vkg_gltf_counts(C.Structure):
 
 class vkg_wire_entry_info(C.Structure):
     _fields_ = [("buffer_index", C.c_uint32), ("base_index", C.c_uint32), ("vertex_offset", C.c_int32),
-                ("aabb_min", C.c_float * 3), ("aabb_max", C.c_float * 3)]
+                ("aabb_min", C.c_float * 3), ("aabb_max", C.c_float * 3), ("has_uv_transform", C.c_uint32),
+                ("uv_transform", C.c_float * 6)]
 
 
 class vkg_pixel_data(C.Structure):

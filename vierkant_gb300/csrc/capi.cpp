@@ -733,6 +733,8 @@ vkg_status vkg_material_defaults(vkg_material *m)
     m->alpha = 1.f;
     m->blend_mode = VKG_BLEND_OPAQUE;
     m->alpha_cutoff = 0.5f;
+    m->has_uv_transform = 0u;
+    m->uv_transform[0] = m->uv_transform[4] = 1.f;
     return VKG_OK;
 }
 

@@ -735,6 +735,22 @@ struct loader
             return i >= 0 ? (uint32_t)i : VKG_NO_TEXTURE;
         };
         r.tex_color = tex(pbr ? pbr->get("baseColorTexture") : nullptr);
+        // KHR_texture_transform of the colour texture, the one the reference keeps per entry
+        // (texture_transform, gltf.cpp:162-194; RayBuilder.cpp:596-597): T(offset) R(rotation about -z)
+        // S(scale) applied to (u, v, 0, 1)
+        if(const jv *bct = pbr ? pbr->get("baseColorTexture") : nullptr)
+            if(const jv *bx = bct->get("extensions"))
+                if(const jv *tt = bx->get("KHR_texture_transform"))
+                {
+                    float off[2] = {0.f, 0.f}, sc[2] = {1.f, 1.f};
+                    rd(tt, "offset", off, 2);
+                    rd(tt, "scale", sc, 2);
+                    const double rot = tt->num("rotation", 0.0), c = std::cos(rot), sn = std::sin(rot);
+                    const float t6[6] = {(float)(c * sc[0]), (float)(sn * sc[1]), off[0],
+                                         (float)(-sn * sc[0]), (float)(c * sc[1]), off[1]};
+                    std::memcpy(r.uv_transform, t6, sizeof(t6));
+                    r.has_uv_transform = 1u;
+                }
         r.tex_ao_rough_metal = tex(pbr ? pbr->get("metallicRoughnessTexture") : nullptr);
         r.tex_normal = tex(m.get("normalTexture"));
         r.tex_emission = tex(m.get("emissiveTexture"));

@@ -957,7 +957,16 @@ __global__ void __launch_bounds__(PT_THREADS)
                         q.tex_diffuse_transmission & q.tex_diffuse_transmission_color) != VKG_NO_TEXTURE &&
                        hit_texcoords(P, h.x, P.two_level ? hit_inst[i] : 0u, __uint_as_float(h.z),
                                      __uint_as_float(h.w), want_t, tuv, lod, tangent, has_t))
+                    {
+                        // the texture-coordinate transform (raypipeline.slang:350); the LOD keeps the
+                        // untransformed coordinates' constant
+                        if(q.has_uv_transform)
+                        {
+                            const float *t6 = q.uv_transform;
+                            tuv = make_float2(t6[0] * tuv.x + t6[1] * tuv.y + t6[2], t6[3] * tuv.x + t6[4] * tuv.y + t6[5]);
+                        }
                         apply_textures(P, q, tuv, lod, cone_w, V, back_face, has_t, tangent, m, emit, N);
+                    }
                     P.cone[pid] = cone_w + P.cone_spread * __uint_as_float(h.y);
                 }
                 // path regularisation (raypipeline.slang:611): after a non-peaked bounce, later vertices

@@ -155,6 +155,14 @@ vkg_status vkg_instances_from_wire(const void *records, uint32_t n, vkg_instance
             e.vertex_offset = rd<int32_t>(r, entry_off::vertex_offset);
             rd3(r, entry_off::aabb, e.aabb_min);
             rd3(r, entry_off::aabb + 12, e.aabb_max);
+            // texture_matrix: a glm::mat4 (column-major, element (row, column) at 4 column + row)
+            // applied to (u, v, 0, 1): u' = M00 u + M01 v + M03, v' = M10 u + M11 v + M13
+            float m[16];
+            std::memcpy(m, r + entry_off::texture_matrix, sizeof(m));
+            const float t6[6] = {m[0], m[4], m[12], m[1], m[5], m[13]};
+            const float id6[6] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f};
+            e.has_uv_transform = std::memcmp(t6, id6, sizeof(t6)) != 0 ? 1u : 0u;
+            std::memcpy(e.uv_transform, t6, sizeof(t6));
         }
     }
     return VKG_OK;

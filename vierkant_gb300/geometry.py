@@ -25,7 +25,7 @@ MATERIAL_DTYPE = np.dtype([("base_color", "<f4", 3), ("roughness", "<f4"), ("met
                            ("tex_ao_rough_metal", "<u4"), ("tex_transmission", "<u4"),
                            ("tex_diffuse_transmission", "<u4"), ("tex_diffuse_transmission_color", "<u4"),
                            ("alpha", "<f4"), ("blend_mode", "<u4"), ("alpha_cutoff", "<f4"),
-                           ("pad", "<u4", 3)])
+                           ("has_uv_transform", "<u4"), ("uv_transform", "<f4", 6)])
 assert MATERIAL_DTYPE.itemsize == C.sizeof(vkg_material)
 
 

@@ -14,7 +14,8 @@ from .raytracing import INSTANCE_DTYPE
 WIRE_MATERIAL_BYTES = 208
 WIRE_ENTRY_BYTES = 192
 ENTRY_INFO_DTYPE = np.dtype([("buffer_index", "<u4"), ("base_index", "<u4"), ("vertex_offset", "<i4"),
-                             ("aabb_min", "<f4", 3), ("aabb_max", "<f4", 3)])
+                             ("aabb_min", "<f4", 3), ("aabb_max", "<f4", 3), ("has_uv_transform", "<u4"),
+                             ("uv_transform", "<f4", 6)])
 assert ENTRY_INFO_DTYPE.itemsize == C.sizeof(vkg_wire_entry_info)
 
 
