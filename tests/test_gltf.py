@@ -239,7 +239,8 @@ def _expected_rgba(img, color_type, depth, palette=None, trns=None):
 def test_png_images_of_every_kind(tmp_path):
     """PNG images decoded by the loader's own inflate / unfilter: the five colour types, bit depths 1,
     4, 8, 16, palettes with transparency, all five row filters, stored / fixed / dynamic DEFLATE
-    blocks; a truncated PNG and a JPEG are counted as skipped and leave their material slots empty"""
+    blocks; a truncated PNG and a malformed JPEG are counted as skipped and leave their material slots
+    empty"""
     import zlib
     from gltf_writer import png
     rng = np.random.default_rng(7)
@@ -324,3 +325,34 @@ def test_texcoords_tangents_and_samplers(tmp_path):
     c, s_ = math.cos(0.3), math.sin(0.3)
     assert m["has_uv_transform"] == 1
     assert np.allclose(m["uv_transform"], [2 * c, 3 * s_, 0.25, -2 * s_, 3 * c, -0.5], rtol=0, atol=1e-6)
+
+
+def test_jpeg_images(tmp_path):
+    """sequential JPEG images decoded by the loader's own decoder (jpeg.cpp): YCbCr at 4:2:0, 4:2:2 and
+    4:4:4, with and without restart intervals, and grey, against the image the encoder's quantised
+    coefficients define (tests/jpeg_writer.py; one level of rounding allowed); a progressive JPEG is
+    counted as skipped"""
+    from jpeg_writer import jpeg
+    rng = np.random.default_rng(12)
+    yy, xx = np.mgrid[0:21, 0:29]
+    smooth = np.stack([(120 + 80 * np.sin(xx / 4.0 + c) * np.cos(yy / 5.0)) for c in range(3)], -1)
+    rgb = np.clip(smooth + rng.normal(0, 12, smooth.shape), 0, 255).astype(np.uint8)
+    grey = np.clip(100 + 60 * np.sin(xx[:17, :23] / 3.0) + rng.normal(0, 20, (17, 23)), 0, 255).astype(np.uint8)
+    cases = [jpeg(rgb, (2, 2)), jpeg(rgb, (1, 1), restart=3), jpeg(rgb, (2, 1), restart=1), jpeg(grey),
+             jpeg(np.full((9, 10, 3), (200, 40, 90), np.uint8), (2, 2))]
+    # a progressive frame header (SOF2) after SOI
+    prog = b"\xff\xd8" + bytes([0xFF, 0xC2, 0, 11, 8, 0, 8, 0, 8, 1, 1, 0x11, 0]) + b"\xff\xd9"
+    images = [(data, 10497, 10497) for data, _ in cases] + [(prog, 10497, 10497)]
+    mats = [{"pbrMetallicRoughness": {"baseColorTexture": {"index": k}}} for k in range(len(images))]
+    path = tmp_path / "jpeg.gltf"
+    write(path, [[(*TRI, k, None)] for k in range(len(images))], [dict(mesh=k) for k in range(len(images))],
+          list(range(len(images))), materials=mats, images=images)
+    a = load_gltf(str(path))
+    assert a["skipped_textures"] == 1 and len(a["textures"]) == len(images)
+    for k, (_, expect) in enumerate(cases):
+        got, _, _ = a["textures"][k]
+        assert got.shape == expect.shape, k
+        d = np.abs(got.astype(np.int64) - expect.astype(np.int64))
+        assert d.max() <= 1 and d.mean() < 0.02, (k, d.max(), d.mean())
+        assert a["materials"][k]["tex_color"] == k
+    assert a["materials"][len(cases)]["tex_color"] == 0xFFFFFFFF

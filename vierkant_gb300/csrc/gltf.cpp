@@ -24,14 +24,17 @@
 //     absent but NORMAL and TEXCOORD_0 are there, computed as Geometry::compute_tangents does,
 //     Geometry.cpp:196-252); the textures the materials use (baseColor, metallicRoughness, normal,
 //     emissive -- which zeroes the emissive factor, as gltf.cpp:377 does -- transmission, diffuse
-//     transmission factor / colour), one per glTF texture: its image decoded from PNG (data URI,
-//     file or buffer view) with its sampler's wrap modes (REPEAT by default); a texture whose image
-//     is not a PNG is counted in skipped_textures and its material slots left empty.
-// Not read: texture transforms, occlusion, skins, morph targets, animations, cameras, volume
+//     transmission factor / colour), one per glTF texture: its image decoded from PNG or sequential
+//     JPEG (data URI, file or buffer view) with its sampler's wrap modes (REPEAT by default); a
+//     texture whose image cannot be decoded (another format, a progressive JPEG) is counted in
+//     skipped_textures and its material slots left empty. The colour texture's KHR_texture_transform
+//     becomes the material's uv_transform.
+// Not read: occlusion, skins, morph targets, animations, cameras, volume
 // thickness, specular, sparse accessors, quantised positions. The reference composes transforms as
 // translation / quaternion / scale triples and projects shear away (transform.hpp:106-128); the
 // matrix composition here is the same for every chain without shear.
 #include "internal.hpp"
+#include "jpeg.hpp"
 #include "png.hpp"
 
 #include <algorithm>
@@ -599,8 +602,12 @@ struct loader
             std::vector<uint8_t> bytes;
             if(src < 0) return fail("texture %zu has no source image", ti);
             if(!image_bytes(src, bytes)) return false;
+            // PNG or JPEG by their signatures (the MIME type is advisory); anything else is skipped
             std::string perr;
-            if(!vkg::png_decode(bytes.data(), bytes.size(), T.rgba, T.width, T.height, perr))
+            const bool is_jpeg = bytes.size() >= 2 && bytes[0] == 0xFF && bytes[1] == 0xD8;
+            const bool ok = is_jpeg ? vkg::jpeg_decode(bytes.data(), bytes.size(), T.rgba, T.width, T.height, perr)
+                                    : vkg::png_decode(bytes.data(), bytes.size(), T.rgba, T.width, T.height, perr);
+            if(!ok)
             {
                 T.rgba.clear();
                 ++G.skipped_textures;
