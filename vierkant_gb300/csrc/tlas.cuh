@@ -81,8 +81,9 @@ __device__ __forceinline__ void tl_init(tl_state &s, const node8 *tnodes, float 
 }
 
 // one node of the two-level traversal; false once the ray is finished. f: the candidate filter
-// (no_filter, traverse.cuh), asked per instance whether its material is tested
-template<bool ANY, class F = no_filter>
+// (no_filter, traverse.cuh), asked per instance whether its material is tested. POS: the ray's tmin
+// is >= +0 (key_pos): the child keys are the entry distances' float bits
+template<bool ANY, class F = no_filter, bool POS = false>
 __device__ __forceinline__ bool tl_step(tl_state &s, const node8 *__restrict__ tnodes, const inst_rec *__restrict__ inst,
                                         const blas_ref *__restrict__ blas, int cull, const F &f = F())
 {
@@ -126,7 +127,8 @@ __device__ __forceinline__ bool tl_step(tl_state &s, const node8 *__restrict__ t
         }
         uint32_t key[8];
         uint4 w4, w5;
-        node_keys(s.nodes, e, s.o[0], s.o[1], s.o[2], s.inv[0], s.inv[1], s.inv[2], s.tmin, s.best_t, key, w4, w5);
+        node_keys<false, POS>(s.nodes, e, s.o[0], s.o[1], s.o[2], s.inv[0], s.inv[1], s.inv[2], s.tmin, s.best_t, key,
+                              w4, w5);
         sort8(key);
         if(s.in_blas)
         {
@@ -138,7 +140,7 @@ __device__ __forceinline__ bool tl_step(tl_state &s, const node8 *__restrict__ t
                 const uint32_t k = key[h] & 7u;
                 const uint32_t c = (k & 4u) ? sel4(w5, k & 3u) : sel4(w4, k & 3u);
                 if(!(c & LEAF_BIT)) continue;
-                if(tdec(key[h] & ~7u) > s.best_t) continue;
+                if(key_dist<POS>(key[h]) > s.best_t) continue;
                 const uint32_t start = c & 0x07FFFFFFu, cnt = ((c >> 27) & 0xFu) + 1u;
                 for(uint32_t ti = start; ti < start + cnt; ++ti)
                 {
@@ -180,7 +182,7 @@ __device__ __forceinline__ bool tl_step(tl_state &s, const node8 *__restrict__ t
             if(key[h] == 0xFFFFFFFFu) continue;
             const uint32_t k = key[h] & 7u;
             const uint32_t c = (k & 4u) ? sel4(w5, k & 3u) : sel4(w4, k & 3u);
-            const float te = tdec(key[h] & ~7u);
+            const float te = key_dist<POS>(key[h]);
             if(c & LEAF_BIT)
             {
                 if(s.in_blas) continue;
@@ -214,7 +216,10 @@ __device__ __forceinline__ tlas_result trace_tlas(const node8 *__restrict__ tnod
     uint2 stack[TL_STACK];
     s.st = stack;
     tl_init(s, tnodes, ox, oy, oz, tmin, dx, dy, dz, tmax);
-    while(tl_step<ANY, F>(s, tnodes, inst, blas, cull, f)) {}
+    if(key_pos(tmin))
+        while(tl_step<ANY, F, true>(s, tnodes, inst, blas, cull, f)) {}
+    else
+        while(tl_step<ANY, F, false>(s, tnodes, inst, blas, cull, f)) {}
     tlas_result R;
     R.occluded = s.done;
     R.prim = s.best_prim;
