@@ -85,11 +85,14 @@ def test_autotune_keeps_images(ctx, jobs):
     br.close()
 
 
-@pytest.mark.parametrize("extend", [1, 2])
-def test_batch_textures_and_alpha_equal_single_scene_tracer(ctx, extend):
+@pytest.mark.parametrize("extend,lit", [(1, False), (2, False), (1, True)])
+def test_batch_textures_and_alpha_equal_single_scene_tracer(ctx, extend, lit):
     """jobs with textures (the textured Cornell scene) and with alpha-tested materials (the alpha
     scene) render in a batch bit for bit like the tracer renders them; an untextured job of the same
-    batch shades with the textured variant and equals its tracer render up to that variant's rounding"""
+    batch shades with the textured variant and equals its tracer render up to that variant's rounding.
+    lit: the alpha scene also has the analytic lights (light shadow rays through the coverage test);
+    the other jobs then shade with the batch's full variant, equal up to its rounding"""
+    from vierkant_gb300.pathtracer import cornell_lights
     env = procedural_sky(ctx, 256, 128, sun_direction(), 50.0, 0.02)
     scenes, jobs = [], []
     for k, (mats_of, tex) in enumerate(((geometry.alpha_materials, geometry.alpha_textures()),
@@ -104,6 +107,8 @@ def test_batch_textures_and_alpha_equal_single_scene_tracer(ctx, extend):
             scene.set_texcoords(uv)
             scene.set_tangents(tg)
             scene.set_textures(tex)
+        if lit and k == 0:
+            scene.set_lights(cornell_lights())
         scenes.append(scene)
         w, h = (160, 96) if k < 2 else (64, 48)
         cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, w, h)
@@ -118,7 +123,7 @@ def test_batch_textures_and_alpha_equal_single_scene_tracer(ctx, extend):
     torch.cuda.synchronize()
     for k, job in enumerate(jobs):
         ref = single(ctx, job, 1)
-        if k < 2:
+        if k == 0 or (k == 1 and not lit):
             assert torch.equal(imgs[k], ref), (k, (imgs[k] - ref).abs().max().item())
         else:
             a, b = imgs[k].cpu().numpy().astype(np.float64), ref.cpu().numpy().astype(np.float64)
