@@ -123,6 +123,17 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def traversal_sources_digest():
+    """sha256 prefix of the closest-hit kernel's sources (traverse.cu, traverse.cuh, vkg_common.cuh):
+    the committed capture summary records the digest of the sources it was taken on, so a bench line
+    says whether its traffic figure still describes the kernel it timed"""
+    import hashlib
+    h = hashlib.sha256()
+    for f in ("traverse.cu", "traverse.cuh", "vkg_common.cuh"):
+        h.update((ROOT / "vierkant_gb300" / "csrc" / f).read_bytes())
+    return h.hexdigest()[:16]
+
+
 def profiled_counters():
     """Per-ray DRAM bytes and issue statistics of the traversal kernel from the committed ncu capture
     summary (one launch on this batch), or None. These are profile figures: the bench cannot read
@@ -323,6 +334,8 @@ def run_ours(args):
         dram = prof["dram_bytes_per_ray"] * n
         roofline.update({
             "traffic": round(dram), "traffic_source": "profile: " + prof["source"],
+            # the capture was taken on the sources the bench runs (else the figure is stale)
+            "traffic_current": prof.get("sources_sha256_16") == traversal_sources_digest(),
             "dram_frac": round(dram / (ms_step * 1e-3) / 1e9 / peak, 4),
             "threads_per_instruction": prof.get("threads_per_instruction"),
             "warp_instructions_per_ray": prof.get("warp_instructions_per_ray"),
