@@ -938,7 +938,9 @@ def profile_case(name: str):
     batch      batched renderer, 4 scenes of the batched workload at 1 spp
     stress     instanced scene: 512^2 terrain + 10,000 instances, 960x540 x 2 spp, 8 segments
     features   Cornell scene with the showcase materials, the six analytic lights and a sun disc,
-               1280x720 x 4 spp, 8 segments"""
+               1280x720 x 4 spp, 8 segments
+    alpha      Cornell scene with the alpha materials and textures (a cut-out wall, masked and blended
+               spheres), 1280x720 x 4 spp, 8 segments"""
     import numpy as np
     import torch
     from vierkant_gb300 import geometry
@@ -1012,6 +1014,20 @@ def profile_case(name: str):
         s.sun_color[0] = s.sun_color[1] = s.sun_color[2] = 1.0
         s.sun_intensity, s.sun_angular_size = 3.0, 0.05
         s.sun_spherical_coords[0], s.sun_spherical_coords[1] = math.radians(30), math.radians(200)
+        PBRPathTracer(ctx, seed=SEED, settings=s).render_scene(scene, cam)
+    elif name == "alpha":
+        sc = geometry.cornell_scene(SEED, 2, 64, 16)
+        envc = torch.full((64, 128, 3), 0.1, dtype=torch.float32, device="cuda")
+        scene = Scene(ctx, sc["xyz"], sc["indices"], sc["tri_material"], geometry.alpha_materials(sc["materials"]),
+                      envc)
+        uv, tg = geometry.cornell_texcoords(sc)
+        scene.set_normals(geometry.cornell_vertex_normals(sc))
+        scene.set_texcoords(uv)
+        scene.set_tangents(tg)
+        scene.set_textures(geometry.alpha_textures())
+        cam = geometry.camera_lookat((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 45.0, 1280, 720)
+        s = PBRPathTracer.default_settings()
+        s.num_samples, s.max_trace_depth, s.rr_start_depth = 4, 8, 3
         PBRPathTracer(ctx, seed=SEED, settings=s).render_scene(scene, cam)
     elif name == "media":
         from vierkant_gb300.pathtracer import cornell_lights
@@ -1235,7 +1251,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-pt", action="store_true", help="skip the path-tracer / radiance-cache block")
     ap.add_argument("--nrc-frames", type=int, default=256)
-    ap.add_argument("--profile-case", choices=["pt-frame", "nrc", "batch", "stress", "features", "media"], default=None,
+    ap.add_argument("--profile-case", choices=["pt-frame", "nrc", "batch", "stress", "features", "media", "alpha"], default=None,
                     help="run one small workload for a profiler capture and exit (no JSON line)")
     ap.add_argument("--nrc-cut-sweep", action="store_true",
                     help="measure the radiance cache's equal-RMSE time for terminate_depth 0, 1, 2 and exit")
