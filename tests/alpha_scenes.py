@@ -42,6 +42,25 @@ def blend_quads(alpha: float):
     return xyz, idx, tm, m
 
 
+def blend_stack(alpha: float):
+    """two blended emitters of the same alpha (red in front, green behind it) before an opaque blue one:
+    the reference's any_hit compares every candidate of a ray with the same uniform, so a ray that
+    passes the red one passes the green one too: radiance (a, 0, 1 - a), where independent uniforms per
+    candidate would give (a, a (1 - a), (1 - a)^2)"""
+    xyz = np.concatenate([_quad(-1, 1, -1, 1, 0.5), _quad(-1.5, 1.5, -1.5, 1.5, 0.0), _quad(-2, 2, -2, 2, -0.5)])
+    idx = np.array([[0, 1, 2], [0, 2, 3], [4, 5, 6], [4, 6, 7], [8, 9, 10], [8, 10, 11]], np.uint32)
+    tm = np.array([0, 0, 1, 1, 2, 2], np.uint32)
+    m = geometry.default_materials(3)
+    m["base_color"] = 0.0
+    m["twosided"] = 1
+    m["emission"][0] = (1.0, 0.0, 0.0)
+    m["emission"][1] = (0.0, 1.0, 0.0)
+    m["emission"][2] = (0.0, 0.0, 1.0)
+    m["blend_mode"][:2] = BLEND_BLEND
+    m["alpha"][:2] = alpha
+    return xyz, idx, tm, m
+
+
 def blend_shadow(alpha: float, with_occluder: bool = True):
     floor = _quad(-1, 1, -1, 1, -0.5)
     # the occluder: the plane x = 1.5, y in [-2, 2], z in [-1.5, 3]

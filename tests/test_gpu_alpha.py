@@ -17,7 +17,7 @@ import torch
 
 import oracle
 from alpha_scenes import CROP as QCROP
-from alpha_scenes import EYE, FOVY, HEIGHT, TARGET, UP, WIDTH, blend_quads, blend_shadow, sun
+from alpha_scenes import EYE, FOVY, HEIGHT, TARGET, UP, WIDTH, blend_quads, blend_shadow, blend_stack, sun
 from radiance_stats import check, compare, render_batches, report
 from scene_helpers import split_cornell
 from test_gpu_pathtracer import CROP, d2h, settings
@@ -157,6 +157,20 @@ def test_blended_emitter_is_seen_by_alpha_of_the_paths(ctx, alpha):
     tol = 5.0 * math.sqrt(alpha * (1 - alpha) / n) + 1e-3
     assert abs(mean[0] - alpha) < tol, mean
     assert abs(mean[2] - (1 - alpha)) < tol, mean
+
+
+def test_blended_candidates_of_a_ray_share_one_uniform(ctx):
+    alpha = 0.4
+    s = _quad_scene(ctx, *blend_stack(alpha))
+    cam = geometry.camera_lookat(EYE, TARGET, UP, FOVY, WIDTH, HEIGHT)
+    spp = 256
+    img = _render(ctx, s, cam, QCROP, spp=spp, max_depth=1, resolution=(WIDTH, HEIGHT)).cpu().numpy().astype(np.float64)
+    s.close()
+    mean = img[..., :3].mean(axis=(0, 1))
+    n = QCROP[2] * QCROP[3] * spp
+    tol = 5.0 * math.sqrt(alpha * (1 - alpha) / n) + 1e-3
+    assert abs(mean[0] - alpha) < tol and abs(mean[2] - (1 - alpha)) < tol, mean
+    assert mean[1] < 1e-3, mean  # independent uniforms would show green at a (1 - a) = 0.24
 
 
 def test_blended_occluder_passes_one_minus_alpha_of_the_light(ctx):

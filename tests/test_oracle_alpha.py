@@ -11,7 +11,8 @@ import numpy as np
 import pytest
 
 import oracle
-from alpha_scenes import CROP, EYE, FOVY, HEIGHT, TARGET, UP, WIDTH, blend_quads, blend_shadow, env_rgb, sun
+from alpha_scenes import (CROP, EYE, FOVY, HEIGHT, TARGET, UP, WIDTH, blend_quads, blend_shadow, blend_stack,
+                          env_rgb, sun)
 from vierkant_gb300._lib import BLEND_MASK
 
 SUN_DIR = np.array([0.25, 0.6, 0.76])
@@ -113,3 +114,16 @@ def test_blended_occluder_passes_one_minus_alpha_of_the_light():
     assert open_ > 0.05
     n = CROP[2] * CROP[3] * 128
     assert abs(shaded / open_ - (1 - alpha)) < 5.0 * math.sqrt(alpha * (1 - alpha) / n) + 2e-3, (open_, shaded)
+
+
+def test_blended_candidates_of_a_ray_share_one_uniform():
+    alpha = 0.4
+    xyz, idx, tm, m = blend_stack(alpha)
+    bvh = oracle.CpuBVH(xyz, idx, 4)
+    img, _, _ = oracle.pt_render(True, xyz, idx, tm, m, bvh, env_rgb(), _camera(), 256, seed=3, max_depth=1,
+                                 crop=CROP)
+    mean = img.mean(axis=(0, 1))
+    n = CROP[2] * CROP[3] * 256
+    tol = 5.0 * math.sqrt(alpha * (1 - alpha) / n) + 1e-3
+    assert abs(mean[0] - alpha) < tol and abs(mean[2] - (1 - alpha)) < tol, mean
+    assert mean[1] < 1e-3, mean  # independent uniforms would show green at a (1 - a) = 0.24
