@@ -621,7 +621,7 @@ vkg_status vkg_scene_camera_medium(const vkg_scene *scene, const float eye[3], u
  * instances (node placements, object -> world 3x4, mesh index in `blas`, material), materials
  * (vkg_material, texture slots indexing the asset's textures; alphaMode / alphaCutoff / the base
  * colour's alpha into blend_mode / alpha_cutoff / alpha; the colour texture's KHR_texture_transform
- * into uv_transform), textures (PNG and sequential JPEG images decoded to RGBA8)
+ * into uv_transform), textures (PNG and JPEG images decoded to RGBA8)
  * and KHR_lights_punctual lights (vkg_light); those feed vkg_scene_create_instanced,
  * vkg_scene_set_normals / _texcoords / _tangents / _textures and vkg_scene_set_lights. Errors: a status and
  * the message in err (may be NULL). The mesh pointers stay valid until vkg_gltf_destroy. */
@@ -631,8 +631,8 @@ typedef struct vkg_gltf_counts
     uint32_t num_meshes, num_instances, num_materials, num_lights;
     uint32_t skipped_primitives; /* non-triangle primitives left out */
     uint32_t num_textures;       /* glTF textures (vkg_gltf_textures) */
-    uint32_t skipped_textures;   /* textures whose image is neither a PNG nor a sequential JPEG (their
-                                    material slots are empty) */
+    uint32_t skipped_textures;   /* textures whose image is neither a PNG nor a JPEG this loader decodes
+                                    (their material slots are empty) */
 } vkg_gltf_counts;
 vkg_status vkg_gltf_load(const char *path, vkg_gltf **out, char *err, size_t err_len);
 vkg_status vkg_gltf_counts_get(const vkg_gltf *g, vkg_gltf_counts *out);

@@ -1,9 +1,10 @@
-"""A small sequential-DCT JPEG encoder for the loader tests (ITU-T T.81 baseline: 8-bit samples,
+"""A small DCT JPEG encoder for the loader tests (ITU-T T.81 baseline and progressive: 8-bit samples,
 Huffman coding), and the image a decoder following the loader's rules must produce from it.
 
-jpeg(img, sampling=(2, 2), restart=0) -> (file bytes, expected RGBA8): img is uint8 [h, w, 3] (JFIF
-YCbCr, the luma component sampled (h, v) times the chroma's) or [h, w] (grey). The expected image is
-computed from the quantised coefficients the file holds: dequantised, inverse DCT in float64, level
+jpeg(img, sampling=(2, 2), restart=0, progressive=False) -> (file bytes, expected RGBA8): img is uint8
+[h, w, 3] (JFIF YCbCr, the luma component sampled (h, v) times the chroma's) or [h, w] (grey);
+progressive files carry the same quantised coefficients in the scans of PROGRESSIVE_SCANS, so they
+decode to the same image. The expected image is computed from the quantised coefficients the file holds: dequantised, inverse DCT in float64, level
 shift, rounding and clamping, chroma replicated, YCbCr -> RGB with the JFIF constants; a float32
 decoder may differ from it by one level. Huffman tables are canonical codes over the symbols that
 occur (lengths 2, 2, 3, 3, 4, 4, 5, 5, then 12), so codes of several lengths are exercised.
@@ -79,7 +80,132 @@ def _seg(marker, payload):
     return bytes([0xFF, marker]) + (len(payload) + 2).to_bytes(2, "big") + bytes(payload)
 
 
-def jpeg(img, sampling=(2, 2), restart=0):
+# the progressive scan script (spectral selection, successive approximation) of a three-component
+# image: (components, Ss, Se, Ah, Al); a grey image keeps the scans of component 0
+PROGRESSIVE_SCANS = [((0, 1, 2), 0, 0, 0, 1), ((0,), 1, 5, 0, 2), ((2,), 1, 63, 0, 1), ((1,), 1, 63, 0, 1),
+                     ((0,), 6, 63, 0, 2), ((0,), 1, 63, 2, 1), ((0, 1, 2), 0, 0, 1, 0), ((2,), 1, 63, 1, 0),
+                     ((1,), 1, 63, 1, 0), ((0,), 1, 63, 1, 0)]
+
+
+def _progressive_scans(coefs, factors, hmax, vmax, mcux, mcuy, w, h):
+    """the entropy-coded scans of a progressive file: per scan its component list, band, table
+    definitions and data (T.81 G.1.2: DC first / refinement, AC first with end-of-band runs, AC
+    refinement with correction bits buffered over the runs)"""
+    ncomp = len(coefs)
+    out = []
+    for comps, ss, se, ah, al in PROGRESSIVE_SCANS:
+        comps = tuple(c for c in comps if c < ncomp)
+        if not comps:
+            continue
+        if len(comps) > 1:
+            order = [(k, my * factors[k][1] + v, mx * factors[k][0] + u) for my in range(mcuy) for mx in range(mcux)
+                     for k in comps for v in range(factors[k][1]) for u in range(factors[k][0])]
+        else:
+            k = comps[0]
+            cw, ch = -(-w * factors[k][0] // hmax), -(-h * factors[k][1] // vmax)
+            order = [(k, by, bx) for by in range(-(-ch // 8)) for bx in range(-(-cw // 8))]
+        ev = []  # ("sym", class, symbol) or ("bits", value, n)
+        if ss == 0:
+            pred = [0] * ncomp
+            for k, by, bx in order:
+                c = int(coefs[k][by, bx, 0, 0])
+                if ah == 0:
+                    v = c >> al
+                    d = v - pred[k]
+                    pred[k] = v
+                    cat = _category(d)
+                    ev.append(("sym", "dc", cat))
+                    if cat:
+                        ev.append(("bits", _amp_bits(d, cat), cat))
+                else:
+                    ev.append(("bits", (c >> al) & 1, 1))
+        else:
+            st = {"run": 0, "be": []}
+
+            def flush():
+                if st["run"]:
+                    nb = st["run"].bit_length() - 1
+                    ev.append(("sym", "ac", nb << 4))
+                    if nb:
+                        ev.append(("bits", st["run"] - (1 << nb), nb))
+                    ev.extend(("bits", b, 1) for b in st["be"])
+                    st["run"], st["be"] = 0, []
+
+            for k, by, bx in order:
+                zz = coefs[k][by, bx].reshape(-1)[ZIGZAG]
+                if ah == 0:
+                    r = 0
+                    for i in range(ss, se + 1):
+                        c = int(zz[i])
+                        t = (abs(c) >> al) * (1 if c > 0 else -1)
+                        if t == 0:
+                            r += 1
+                            continue
+                        flush()
+                        while r > 15:
+                            ev.append(("sym", "ac", 0xF0))
+                            r -= 16
+                        cat = _category(t)
+                        ev.append(("sym", "ac", (r << 4) | cat))
+                        ev.append(("bits", _amp_bits(t, cat), cat))
+                        r = 0
+                    if r:
+                        st["run"] += 1
+                        if st["run"] == 0x7FFF:
+                            flush()
+                else:
+                    absv = [abs(int(zz[i])) >> al for i in range(64)]
+                    eob = max([i for i in range(ss, se + 1) if absv[i] == 1], default=-1)
+                    r, br = 0, []
+                    for i in range(ss, se + 1):
+                        t = absv[i]
+                        if t == 0:
+                            r += 1
+                            continue
+                        while r > 15 and i <= eob:
+                            flush()
+                            ev.append(("sym", "ac", 0xF0))
+                            r -= 16
+                            ev.extend(("bits", b, 1) for b in br)
+                            br = []
+                        if t > 1:
+                            br.append(t & 1)
+                            continue
+                        flush()
+                        ev.append(("sym", "ac", (r << 4) | 1))
+                        ev.append(("bits", 1 if zz[i] > 0 else 0, 1))
+                        ev.extend(("bits", b, 1) for b in br)
+                        br, r = [], 0
+                    if r or br:
+                        st["run"] += 1
+                        st["be"].extend(br)
+                        if st["run"] == 0x7FFF or len(st["be"]) > 900:
+                            flush()
+            flush()
+        syms = {}
+        for e in ev:
+            if e[0] == "sym":
+                syms.setdefault(e[1], []).append(e[2])
+        tables = {cls: _table(v) for cls, v in syms.items()}
+        bits = _Bits()
+        for e in ev:
+            if e[0] == "sym":
+                code, L = tables[e[1]][2][e[2]]
+                bits.put(code, L)
+            else:
+                bits.put(e[1], e[2])
+        bits.align()
+        dht = b"".join(_seg(0xC4, bytes([(0 if cls == "dc" else 1) << 4]) + bytes(t[0]) + bytes(t[1]))
+                       for cls, t in sorted(tables.items()))
+        sos = bytearray([len(comps)])
+        for k in comps:
+            sos += bytes([k + 1, 0x00])  # DC and AC tables 0, redefined before every scan
+        sos += bytes([ss, se, (ah << 4) | al])
+        out.append(dht + _seg(0xDA, sos) + bytes(bits.out))
+    return out
+
+
+def jpeg(img, sampling=(2, 2), restart=0, progressive=False):
     img = np.asarray(img, np.uint8)
     grey = img.ndim == 2
     h, w = img.shape[:2]
@@ -127,6 +253,20 @@ def jpeg(img, sampling=(2, 2), restart=0):
         rgb = [Y + 1.402 * Cr, Y - 0.344136 * Cb - 0.714136 * Cr, Y + 1.772 * Cb]
         for i in range(3):
             exp[..., i] = np.clip(np.floor(rgb[i] + 0.5), 0, 255).astype(np.uint8)
+
+    if progressive:
+        data = bytearray(b"\xFF\xD8")
+        data += _seg(0xE0, b"JFIF\x00\x01\x01\x00\x00\x01\x00\x01\x00\x00")
+        for t, q in enumerate(quant[:1] if grey else quant[:2]):
+            data += _seg(0xDB, bytes([t]) + bytes(int(v) for v in q.reshape(-1)[ZIGZAG]))
+        comps = bytearray([8]) + h.to_bytes(2, "big") + w.to_bytes(2, "big") + bytes([len(coefs)])
+        for k in range(len(coefs)):
+            comps += bytes([k + 1, (factors[k][0] << 4) | factors[k][1], 0 if k == 0 else 1])
+        data += _seg(0xC2, comps)
+        for scan in _progressive_scans(coefs, factors, hmax, vmax, mcux, mcuy, w, h):
+            data += scan
+        data += b"\xFF\xD9"
+        return bytes(data), exp
 
     # the MCU sequence: (component, block row, block column) per block, MCUs in raster order
     def blocks():

@@ -328,18 +328,27 @@ def test_texcoords_tangents_and_samplers(tmp_path):
 
 
 def test_jpeg_images(tmp_path):
-    """sequential JPEG images decoded by the loader's own decoder (jpeg.cpp): YCbCr at 4:2:0, 4:2:2 and
-    4:4:4, with and without restart intervals, and grey, against the image the encoder's quantised
-    coefficients define (tests/jpeg_writer.py; one level of rounding allowed); a progressive JPEG is
-    counted as skipped"""
+    """JPEG images decoded by the loader's own decoder (jpeg.cpp): sequential YCbCr at 4:2:0, 4:2:2 and
+    4:4:4, with and without restart intervals, and grey; progressive files of the same images
+    (spectral selection, successive approximation, end-of-band runs over flat regions); each against
+    the image the encoder's quantised coefficients define (tests/jpeg_writer.py; one level of rounding
+    allowed); a progressive frame header without scans is counted as skipped"""
     from jpeg_writer import jpeg
     rng = np.random.default_rng(12)
     yy, xx = np.mgrid[0:21, 0:29]
     smooth = np.stack([(120 + 80 * np.sin(xx / 4.0 + c) * np.cos(yy / 5.0)) for c in range(3)], -1)
     rgb = np.clip(smooth + rng.normal(0, 12, smooth.shape), 0, 255).astype(np.uint8)
     grey = np.clip(100 + 60 * np.sin(xx[:17, :23] / 3.0) + rng.normal(0, 20, (17, 23)), 0, 255).astype(np.uint8)
+    # mostly flat with a few busy blocks: long end-of-band runs, zero runs past 16 in the refinements
+    patchy = np.full((48, 56, 3), 128, np.uint8)
+    patchy[8:16, 16:24] = rng.integers(0, 256, (8, 8, 3), dtype=np.uint8)
+    patchy[30:38, 40:48, 0] = 255
     cases = [jpeg(rgb, (2, 2)), jpeg(rgb, (1, 1), restart=3), jpeg(rgb, (2, 1), restart=1), jpeg(grey),
-             jpeg(np.full((9, 10, 3), (200, 40, 90), np.uint8), (2, 2))]
+             jpeg(np.full((9, 10, 3), (200, 40, 90), np.uint8), (2, 2)),
+             jpeg(rgb, (2, 2), progressive=True), jpeg(rgb, (1, 1), progressive=True), jpeg(grey, progressive=True),
+             jpeg(patchy, (2, 1), progressive=True), jpeg(patchy, (1, 1), progressive=True)]
+    # the progressive and the sequential file of an image decode alike
+    assert np.array_equal(cases[5][1], cases[0][1]) and np.array_equal(cases[7][1], cases[3][1])
     # a progressive frame header (SOF2) after SOI
     prog = b"\xff\xd8" + bytes([0xFF, 0xC2, 0, 11, 8, 0, 8, 0, 8, 1, 1, 0x11, 0]) + b"\xff\xd9"
     images = [(data, 10497, 10497) for data, _ in cases] + [(prog, 10497, 10497)]

@@ -24,10 +24,10 @@
 //     absent but NORMAL and TEXCOORD_0 are there, computed as Geometry::compute_tangents does,
 //     Geometry.cpp:196-252); the textures the materials use (baseColor, metallicRoughness, normal,
 //     emissive -- which zeroes the emissive factor, as gltf.cpp:377 does -- transmission, diffuse
-//     transmission factor / colour), one per glTF texture: its image decoded from PNG or sequential
-//     JPEG (data URI, file or buffer view) with its sampler's wrap modes (REPEAT by default); a
-//     texture whose image cannot be decoded (another format, a progressive JPEG) is counted in
-//     skipped_textures and its material slots left empty. The colour texture's KHR_texture_transform
+//     transmission factor / colour), one per glTF texture: its image decoded from PNG or JPEG
+//     (sequential or progressive; data URI, file or buffer view) with its sampler's wrap modes (REPEAT
+//     by default); a texture whose image cannot be decoded (another format, a lossless or arithmetic-
+//     coded JPEG) is counted in skipped_textures and its material slots left empty. The colour texture's KHR_texture_transform
 //     becomes the material's uv_transform.
 // Not read: occlusion, skins, morph targets, animations, cameras, volume
 // thickness, specular, sparse accessors, quantised positions. The reference composes transforms as

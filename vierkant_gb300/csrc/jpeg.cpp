@@ -1,7 +1,9 @@
-// Sequential-DCT JPEG decoder (ITU-T T.81, Annex F): marker segments, canonical Huffman tables
-// (F.2.2.3's code-length decoding), DC prediction per component, run-length AC coefficients in zig-zag
-// order, dequantisation, a separable floating-point inverse DCT, level shift, chroma replication and
-// the JFIF YCbCr -> RGB conversion.
+// DCT JPEG decoder with Huffman coding (ITU-T T.81): sequential (Annex F) and progressive (Annex G:
+// spectral selection and successive approximation, end-of-band runs) frames. Marker segments,
+// canonical Huffman tables (F.2.2.3's code-length decoding), DC prediction per component, run-length
+// AC coefficients in zig-zag order collected per block over all scans, then dequantisation, a
+// separable floating-point inverse DCT, level shift, chroma replication and the JFIF YCbCr -> RGB
+// conversion.
 #include "jpeg.hpp"
 
 #include <algorithm>
@@ -32,6 +34,7 @@ struct component
     uint32_t id, h, v, tq;
     uint32_t td = 0, ta = 0;
     uint32_t bw = 0, bh = 0; // blocks per row / column in the plane (whole MCUs)
+    std::vector<int16_t> coef; // per block 64 coefficients in zig-zag order, over all scans
     std::vector<uint8_t> plane;
     int32_t pred = 0;
 };
@@ -45,7 +48,9 @@ struct decoder
     huffman dc[4], ac[4];
     std::vector<component> comps;
     uint32_t width = 0, height = 0, hmax = 1, vmax = 1, mcux = 0, mcuy = 0, restart = 0;
-    bool frame = false, adobe = false;
+    bool frame = false, adobe = false, progressive = false;
+    uint32_t ss = 0, se = 63, ah = 0, al = 0; // the current scan's band and successive approximation
+    uint32_t eobrun = 0;                     // blocks left in the current end-of-band run
     uint8_t adobe_transform = 1;
     // entropy-coded bit reader
     const uint8_t *s = nullptr;
@@ -141,36 +146,139 @@ struct decoder
     }
     static int32_t extend(uint32_t v, int t) { return t && v < (1u << (t - 1)) ? (int32_t)v - (1 << t) + 1 : (int32_t)v; }
 
-    // ---- one block: entropy decoding, dequantisation, inverse DCT into the plane at (bx, by)
+    // ---- one block of a scan into the component's coefficients at block (bx, by)
     bool block(component &c, uint32_t bx, uint32_t by)
     {
-        const huffman &hd = dc[c.td], &ha = ac[c.ta];
-        if(!hd.defined || !ha.defined) return fail("JPEG: scan uses an undefined Huffman table");
-        const uint16_t *qt = q[c.tq];
-        float coef[64] = {};
+        int16_t *z = c.coef.data() + ((size_t)by * c.bw + bx) * 64;
         bool ok = true;
-        const int t = decode(hd, ok);
-        if(!ok || t > 11) return fail("JPEG: bad DC code");
-        c.pred += extend(bits(t), t);
-        coef[0] = (float)c.pred * (float)qt[0];
-        for(int k = 1; k < 64;)
+        if(ss == 0)
+        {
+            // DC: the whole coefficient (sequential), its high bits (first scan) or one more bit
+            if(ah == 0)
+            {
+                if(!dc[c.td].defined) return fail("JPEG: scan uses an undefined Huffman table");
+                const int t = decode(dc[c.td], ok);
+                if(!ok || t > 11) return fail("JPEG: bad DC code");
+                c.pred += extend(bits(t), t);
+                z[0] = (int16_t)(c.pred * (1 << al));
+            }
+            else if(bits(1))
+                z[0] = (int16_t)(z[0] | (1 << al));
+            if(!progressive) return ac_first(c, z, 1);
+            return true;
+        }
+        return ah == 0 ? ac_first(c, z, ss) : ac_refine(c, z);
+    }
+
+    // AC coefficients k0..se of a sequential block or a progressive first scan (values << al); an
+    // end-of-band symbol ends this block and, in progressive scans, starts a run over the next ones
+    bool ac_first(component &c, int16_t *z, uint32_t k0)
+    {
+        if(eobrun > 0)
+        {
+            --eobrun;
+            return true;
+        }
+        const huffman &ha = ac[c.ta];
+        if(!ha.defined) return fail("JPEG: scan uses an undefined Huffman table");
+        bool ok = true;
+        for(uint32_t k = k0; k <= se;)
         {
             const int rs = decode(ha, ok);
             if(!ok) return fail("JPEG: bad AC code");
             const int r = rs >> 4, sz = rs & 15;
             if(sz == 0)
             {
-                if(r != 15) break; // end of block
-                k += 16;
-                continue;
+                if(r == 15)
+                {
+                    k += 16;
+                    continue;
+                }
+                if(progressive) eobrun = (1u << r) - 1u + (r ? bits(r) : 0u);
+                break;
             }
-            k += r;
-            if(k > 63) return fail("JPEG: AC run past the block");
-            coef[ZIGZAG[k]] = (float)extend(bits(sz), sz) * (float)qt[k];
+            k += (uint32_t)r;
+            if(k > se) return fail("JPEG: AC run past the band");
+            z[k] = (int16_t)(extend(bits(sz), sz) * (1 << al));
             ++k;
         }
-        idct(coef, c.plane.data() + (size_t)by * 8 * c.bw * 8 + (size_t)bx * 8, c.bw * 8);
         return true;
+    }
+
+    // the refinement bit of an already non-zero coefficient
+    void refine(int16_t &v)
+    {
+        if(bits(1) && (v & (1 << al)) == 0) v = (int16_t)(v + (v >= 0 ? (1 << al) : -(1 << al)));
+    }
+
+    // a progressive AC refinement scan (G.1.2.3): newly non-zero coefficients (+-1 << al) placed after
+    // r zero-history coefficients, a correction bit for every non-zero one passed on the way, and for
+    // every non-zero coefficient after the end of band
+    bool ac_refine(component &c, int16_t *z)
+    {
+        const huffman &ha = ac[c.ta];
+        if(!ha.defined) return fail("JPEG: scan uses an undefined Huffman table");
+        bool ok = true;
+        uint32_t k = ss;
+        if(eobrun == 0)
+        {
+            for(; k <= se; ++k)
+            {
+                const int rs = decode(ha, ok);
+                if(!ok) return fail("JPEG: bad AC code");
+                int r = rs >> 4;
+                const int sz = rs & 15;
+                int v = 0;
+                if(sz)
+                {
+                    if(sz != 1) return fail("JPEG: bad refinement code");
+                    v = bits(1) ? (1 << al) : -(1 << al);
+                }
+                else if(r != 15)
+                {
+                    eobrun = (1u << r) + (r ? bits(r) : 0u);
+                    break;
+                }
+                while(k <= se)
+                {
+                    int16_t &w = z[k];
+                    if(w != 0)
+                        refine(w);
+                    else if(--r < 0)
+                        break;
+                    ++k;
+                }
+                if(v)
+                {
+                    if(k > se) return fail("JPEG: refinement past the band");
+                    z[k] = (int16_t)v;
+                }
+            }
+        }
+        if(eobrun > 0)
+        {
+            for(; k <= se; ++k)
+                if(z[k] != 0) refine(z[k]);
+            --eobrun;
+        }
+        return true;
+    }
+
+    // dequantise every block and transform it into the component's plane
+    void reconstruct()
+    {
+        for(component &c: comps)
+        {
+            const uint16_t *qt = q[c.tq];
+            for(uint32_t by = 0; by < c.bh; ++by)
+                for(uint32_t bx = 0; bx < c.bw; ++bx)
+                {
+                    const int16_t *z = c.coef.data() + ((size_t)by * c.bw + bx) * 64;
+                    float F[64];
+                    for(int k = 0; k < 64; ++k) F[ZIGZAG[k]] = (float)z[k] * (float)qt[k];
+                    idct(F, c.plane.data() + (size_t)by * 8 * c.bw * 8 + (size_t)bx * 8, c.bw * 8);
+                }
+        }
     }
 
     // f(x, y) = 1/4 sum_u sum_v C(u) C(v) F(v, u) cos((2x + 1) u pi / 16) cos((2y + 1) v pi / 16),
@@ -214,6 +322,7 @@ struct decoder
         s += 2;
         hit_marker = false;
         for(component &c: comps) c.pred = 0;
+        eobrun = 0;
         return true;
     }
 
@@ -235,10 +344,19 @@ struct decoder
             sc.push_back(c);
         }
         const uint8_t *tail = seg + 1 + 2 * ns;
-        if(tail[0] != 0 || tail[1] != 63 || tail[2] != 0) return fail("JPEG: not a sequential scan");
+        ss = tail[0];
+        se = tail[1];
+        ah = tail[2] >> 4;
+        al = tail[2] & 15;
+        if(!progressive && (ss != 0 || se != 63 || tail[2] != 0)) return fail("JPEG: bad sequential scan");
+        // progressive: a DC band alone, AC bands of one component; each refinement adds one bit
+        if(progressive && (se > 63 || ss > se || (ss == 0 && se != 0) || (ss > 0 && ns != 1) || al > 13 ||
+                           (ah != 0 && ah != al + 1)))
+            return fail("JPEG: bad progressive scan");
         for(component *c: sc)
             if(!q_defined[c->tq]) return fail("JPEG: undefined quantisation table");
         for(component &c: comps) c.pred = 0;
+        eobrun = 0;
         s = seg + len;
         acc = 0;
         nbits = 0;
@@ -297,8 +415,9 @@ struct decoder
             const uint8_t *seg = p + 2;
             const uint32_t n = len - 2;
             p += len;
-            if(mk == 0xC0 || mk == 0xC1)
+            if(mk == 0xC0 || mk == 0xC1 || mk == 0xC2)
             {
+                progressive = mk == 0xC2;
                 if(frame) return fail("JPEG: second frame header");
                 if(n < 6 || seg[0] != 8) return fail("JPEG: only 8-bit samples are supported");
                 height = u16(seg + 1);
@@ -325,12 +444,13 @@ struct decoder
                 {
                     c.bw = mcux * c.h;
                     c.bh = mcuy * c.v;
+                    c.coef.assign((size_t)c.bw * c.bh * 64, 0);
                     c.plane.assign((size_t)c.bw * 8 * c.bh * 8, 0);
                 }
                 frame = true;
             }
-            else if((mk >= 0xC2 && mk <= 0xC3) || (mk >= 0xC5 && mk <= 0xCF && mk != 0xC8 && mk != 0xCC))
-                return fail("JPEG: progressive, lossless or arithmetic-coded images are not supported");
+            else if(mk == 0xC3 || (mk >= 0xC5 && mk <= 0xCF && mk != 0xC8 && mk != 0xCC))
+                return fail("JPEG: lossless, hierarchical or arithmetic-coded images are not supported");
             else if(mk == 0xDB)
             {
                 for(uint32_t k = 0; k < n;)
@@ -377,6 +497,7 @@ struct decoder
             }
         }
         if(!frame || !scanned) return fail("JPEG: no image data");
+        reconstruct();
         // colour: planes upsampled by replication, then YCbCr -> RGB (JFIF) unless Adobe says RGB
         rgba.assign((size_t)width * height * 4, 255);
         const bool ycc = comps.size() == 3 && !(adobe && adobe_transform == 0);
