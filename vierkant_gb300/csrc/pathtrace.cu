@@ -1261,11 +1261,13 @@ vkg_status vkg_tracer_render(vkg_tracer *t, const vkg_scene *sc, const vkg_camer
                 // queues, shortened by Russian roulette and escapes, gain less than binning costs
                 // (720p 64 spp: 69.1 ms binning depth 1, 69.3 ms binning every depth >= 1, 71.0 ms none)
                 const uint32_t *reordered = nullptr;
-                // (an instanced scene bins by the top level's box: the stress frame 1,334 -> 1,268 ms with
-                // the shadow queues below)
+                // (an instanced scene bins by the top level's box, its second bounce too, where the
+                // costlier two-level traversal still gains: the stress frame 1,334 -> 1,268 ms with the
+                // shadow queues below, 1,233 -> 1,215 ms with the second bounce)
                 const vkg_bvh *bounds = sc->bvh ? sc->bvh : (sc->tlas ? &sc->tlas->top : nullptr);
-                const uint32_t *perm = depth == 1 ? bin_rays(ctx, bounds, t->q_ray[a], n, cnt_in, 0u, st, &reordered)
-                                                  : nullptr;
+                const bool bin_queue = depth == 1 || (sc->tlas && depth == 2);
+                const uint32_t *perm =
+                        bin_queue ? bin_rays(ctx, bounds, t->q_ray[a], n, cnt_in, 0u, st, &reordered) : nullptr;
                 if(alpha && small_stack)
                     k_pt_extend<single_scene, 64, true><<<grid, PT_THREADS, 0, st>>>(
                             SS, t->q_ray[a], t->q_pid[a], cnt_in, t->hits, t->hit_inst, perm, reordered, t->rng, depth);
