@@ -87,10 +87,11 @@ PROGRESSIVE_SCANS = [((0, 1, 2), 0, 0, 0, 1), ((0,), 1, 5, 0, 2), ((2,), 1, 63, 
                      ((1,), 1, 63, 1, 0), ((0,), 1, 63, 1, 0)]
 
 
-def _progressive_scans(coefs, factors, hmax, vmax, mcux, mcuy, w, h):
+def _progressive_scans(coefs, factors, hmax, vmax, mcux, mcuy, w, h, restart=0):
     """the entropy-coded scans of a progressive file: per scan its component list, band, table
     definitions and data (T.81 G.1.2: DC first / refinement, AC first with end-of-band runs, AC
-    refinement with correction bits buffered over the runs)"""
+    refinement with correction bits buffered over the runs); restart: a marker every `restart` MCUs
+    (a block in a one-component scan), the end-of-band run and the DC predictions ended there"""
     ncomp = len(coefs)
     out = []
     for comps, ss, se, ah, al in PROGRESSIVE_SCANS:
@@ -98,16 +99,36 @@ def _progressive_scans(coefs, factors, hmax, vmax, mcux, mcuy, w, h):
         if not comps:
             continue
         if len(comps) > 1:
-            order = [(k, my * factors[k][1] + v, mx * factors[k][0] + u) for my in range(mcuy) for mx in range(mcux)
-                     for k in comps for v in range(factors[k][1]) for u in range(factors[k][0])]
+            mcus = [[(k, my * factors[k][1] + v, mx * factors[k][0] + u) for k in comps for v in range(factors[k][1])
+                     for u in range(factors[k][0])] for my in range(mcuy) for mx in range(mcux)]
         else:
             k = comps[0]
             cw, ch = -(-w * factors[k][0] // hmax), -(-h * factors[k][1] // vmax)
-            order = [(k, by, bx) for by in range(-(-ch // 8)) for bx in range(-(-cw // 8))]
-        ev = []  # ("sym", class, symbol) or ("bits", value, n)
+            mcus = [[(k, by, bx)] for by in range(-(-ch // 8)) for bx in range(-(-cw // 8))]
+        ev = []  # ("sym", class, symbol), ("bits", value, n) or ("rst", n)
+        st = {"run": 0, "be": []}
+
+        def flush():
+            if st["run"]:
+                nb = st["run"].bit_length() - 1
+                ev.append(("sym", "ac", nb << 4))
+                if nb:
+                    ev.append(("bits", st["run"] - (1 << nb), nb))
+                ev.extend(("bits", b, 1) for b in st["be"])
+                st["run"], st["be"] = 0, []
+
+        pred = [0] * ncomp
+
+        def order():
+            for m, mcu in enumerate(mcus):
+                if restart and m and m % restart == 0:
+                    flush()
+                    pred[:] = [0] * ncomp
+                    ev.append(("rst", (m // restart - 1) % 8))
+                yield from mcu
+
         if ss == 0:
-            pred = [0] * ncomp
-            for k, by, bx in order:
+            for k, by, bx in order():
                 c = int(coefs[k][by, bx, 0, 0])
                 if ah == 0:
                     v = c >> al
@@ -120,18 +141,7 @@ def _progressive_scans(coefs, factors, hmax, vmax, mcux, mcuy, w, h):
                 else:
                     ev.append(("bits", (c >> al) & 1, 1))
         else:
-            st = {"run": 0, "be": []}
-
-            def flush():
-                if st["run"]:
-                    nb = st["run"].bit_length() - 1
-                    ev.append(("sym", "ac", nb << 4))
-                    if nb:
-                        ev.append(("bits", st["run"] - (1 << nb), nb))
-                    ev.extend(("bits", b, 1) for b in st["be"])
-                    st["run"], st["be"] = 0, []
-
-            for k, by, bx in order:
+            for k, by, bx in order():
                 zz = coefs[k][by, bx].reshape(-1)[ZIGZAG]
                 if ah == 0:
                     r = 0
@@ -192,6 +202,9 @@ def _progressive_scans(coefs, factors, hmax, vmax, mcux, mcuy, w, h):
             if e[0] == "sym":
                 code, L = tables[e[1]][2][e[2]]
                 bits.put(code, L)
+            elif e[0] == "rst":
+                bits.align()
+                bits.out += bytes([0xFF, 0xD0 + e[1]])
             else:
                 bits.put(e[1], e[2])
         bits.align()
@@ -205,13 +218,17 @@ def _progressive_scans(coefs, factors, hmax, vmax, mcux, mcuy, w, h):
     return out
 
 
-def jpeg(img, sampling=(2, 2), restart=0, progressive=False):
+def jpeg(img, sampling=(2, 2), restart=0, progressive=False, adobe_rgb=False):
     img = np.asarray(img, np.uint8)
     grey = img.ndim == 2
     h, w = img.shape[:2]
     if grey:
         planes_full = [img.astype(np.float64)]
         factors = [(1, 1)]
+    elif adobe_rgb:
+        # an Adobe APP14 marker with transform 0: the components are R, G, B, not subsampled
+        planes_full = [img[..., i].astype(np.float64) for i in range(3)]
+        factors = [(1, 1)] * 3
     else:
         r, g, b = (img[..., i].astype(np.float64) for i in range(3))
         y = 0.299 * r + 0.587 * g + 0.114 * b
@@ -248,22 +265,28 @@ def jpeg(img, sampling=(2, 2), restart=0, progressive=False):
     exp = np.full((h, w, 4), 255, np.uint8)
     if grey:
         exp[..., 0] = exp[..., 1] = exp[..., 2] = samp[0].astype(np.uint8)
+    elif adobe_rgb:
+        for i in range(3):
+            exp[..., i] = samp[i].astype(np.uint8)
     else:
         Y, Cb, Cr = samp[0], samp[1] - 128.0, samp[2] - 128.0
         rgb = [Y + 1.402 * Cr, Y - 0.344136 * Cb - 0.714136 * Cr, Y + 1.772 * Cb]
         for i in range(3):
             exp[..., i] = np.clip(np.floor(rgb[i] + 0.5), 0, 255).astype(np.uint8)
 
+    app = _seg(0xEE, b"Adobe\x00\x64\x00\x00\x00\x00\x00") if adobe_rgb else \
+        _seg(0xE0, b"JFIF\x00\x01\x01\x00\x00\x01\x00\x01\x00\x00")
     if progressive:
-        data = bytearray(b"\xFF\xD8")
-        data += _seg(0xE0, b"JFIF\x00\x01\x01\x00\x00\x01\x00\x01\x00\x00")
+        data = bytearray(b"\xFF\xD8") + app
         for t, q in enumerate(quant[:1] if grey else quant[:2]):
             data += _seg(0xDB, bytes([t]) + bytes(int(v) for v in q.reshape(-1)[ZIGZAG]))
         comps = bytearray([8]) + h.to_bytes(2, "big") + w.to_bytes(2, "big") + bytes([len(coefs)])
         for k in range(len(coefs)):
             comps += bytes([k + 1, (factors[k][0] << 4) | factors[k][1], 0 if k == 0 else 1])
         data += _seg(0xC2, comps)
-        for scan in _progressive_scans(coefs, factors, hmax, vmax, mcux, mcuy, w, h):
+        if restart:
+            data += _seg(0xDD, restart.to_bytes(2, "big"))
+        for scan in _progressive_scans(coefs, factors, hmax, vmax, mcux, mcuy, w, h, restart):
             data += scan
         data += b"\xFF\xD9"
         return bytes(data), exp
@@ -322,8 +345,7 @@ def jpeg(img, sampling=(2, 2), restart=0, progressive=False):
                 bits.put(_amp_bits(v, cat), cat)
     bits.align()
 
-    data = bytearray(b"\xFF\xD8")
-    data += _seg(0xE0, b"JFIF\x00\x01\x01\x00\x00\x01\x00\x01\x00\x00")
+    data = bytearray(b"\xFF\xD8") + app
     for t, q in enumerate(quant[:1] if grey else quant[:2]):
         data += _seg(0xDB, bytes([t]) + bytes(int(v) for v in q.reshape(-1)[ZIGZAG]))
     comps = bytearray([8]) + h.to_bytes(2, "big") + w.to_bytes(2, "big") + bytes([len(coefs)])

@@ -330,7 +330,8 @@ def test_texcoords_tangents_and_samplers(tmp_path):
 def test_jpeg_images(tmp_path):
     """JPEG images decoded by the loader's own decoder (jpeg.cpp): sequential YCbCr at 4:2:0, 4:2:2 and
     4:4:4, with and without restart intervals, and grey; progressive files of the same images
-    (spectral selection, successive approximation, end-of-band runs over flat regions); each against
+    (spectral selection, successive approximation, end-of-band runs over flat regions, restart
+    intervals); RGB components under an Adobe marker; each against
     the image the encoder's quantised coefficients define (tests/jpeg_writer.py; one level of rounding
     allowed); a progressive frame header without scans is counted as skipped"""
     from jpeg_writer import jpeg
@@ -346,9 +347,12 @@ def test_jpeg_images(tmp_path):
     cases = [jpeg(rgb, (2, 2)), jpeg(rgb, (1, 1), restart=3), jpeg(rgb, (2, 1), restart=1), jpeg(grey),
              jpeg(np.full((9, 10, 3), (200, 40, 90), np.uint8), (2, 2)),
              jpeg(rgb, (2, 2), progressive=True), jpeg(rgb, (1, 1), progressive=True), jpeg(grey, progressive=True),
-             jpeg(patchy, (2, 1), progressive=True), jpeg(patchy, (1, 1), progressive=True)]
-    # the progressive and the sequential file of an image decode alike
+             jpeg(patchy, (2, 1), progressive=True), jpeg(patchy, (1, 1), progressive=True),
+             jpeg(rgb, (2, 2), restart=2, progressive=True), jpeg(patchy, (2, 2), restart=5, progressive=True),
+             jpeg(rgb, adobe_rgb=True), jpeg(patchy, adobe_rgb=True, progressive=True)]
+    # the progressive and the sequential file of an image decode alike, restart intervals or not
     assert np.array_equal(cases[5][1], cases[0][1]) and np.array_equal(cases[7][1], cases[3][1])
+    assert np.array_equal(cases[10][1], cases[0][1])
     # a progressive frame header (SOF2) after SOI
     prog = b"\xff\xd8" + bytes([0xFF, 0xC2, 0, 11, 8, 0, 8, 0, 8, 1, 1, 0x11, 0]) + b"\xff\xd9"
     images = [(data, 10497, 10497) for data, _ in cases] + [(prog, 10497, 10497)]
