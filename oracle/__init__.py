@@ -90,6 +90,9 @@ def orc() -> C.CDLL:
             f = getattr(L, name)
             f.restype = res
             f.argtypes = args
+        L.orc_pt_material_size.restype = u32
+        if L.orc_pt_material_size() != MATERIAL_DTYPE.itemsize:
+            raise RuntimeError("liboracle.so's material record does not match MATERIAL_DTYPE: rebuild the oracle")
         _orc = L
     return _orc
 

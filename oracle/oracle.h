@@ -150,6 +150,7 @@ typedef struct {
     uint32_t has_uv_transform;
     float uv_transform[6];
 } orc_pt_material; /* same 208-byte layout as vkg_material */
+uint32_t orc_pt_material_size(void);
 
 /* a texture: size, level count, wrap modes (s: bits 0-7, t: bits 8-15; 0 repeat, 1 clamp to edge,
    2 mirrored repeat) and the first texel of each level in the scene's RGBA8 texel array; the same

@@ -1142,6 +1142,9 @@ int orc_pt_render_instanced(const orc_pt_scene *scene, const orc_pt_instances *i
     return n;
 }
 
+/* the material record's size, checked by the Python binding against its own record */
+uint32_t orc_pt_material_size(void) { return (uint32_t)sizeof(orc_pt_material); }
+
 void orc_pt_env_tables(const float *rgb, uint32_t w, uint32_t h, float *weight, double *cdf)
 {
     const size_t n = (size_t)w * h;
